@@ -1,0 +1,401 @@
+"""Time-to-solve benchmark of the dense mollified-BEM hot path on one GB300.
+
+One step = one complete solve of the workload: assemble the FP64 collocation
+matrix of the calibrated dense backend (CUDA pair kernels, straight into
+HBM), the calibration row sums and free-term diagonal, the fault right-hand
+side, then deflated FGMRES(50) on the device to a true relative residual of
+1e-8. ``value`` is seconds per solve with the mesh arrays already resident
+in HBM; ``e2e`` is the same through the public API from host numpy arrays
+(model -> assemble -> solve -> numpy solution), host<->device copies inside.
+
+Workloads (mesh: traction-free cube of side 4, n x n squares per face, two
+triangles each; vertical fault 1 x 1 at the centre, uniform slip (1,0,0);
+mu = 1, lam = 1; eps = half the cube grid spacing):
+  cube48: n = 48, fault 32 x 32 -> 27,648 + 2,048 elements, 82,944 unknowns
+          (A = 55 GB FP64, larger than L2: no flush needed)
+  cube12: n = 12, fault 8 x 8 -> 5,184 unknowns (quick check)
+
+``--impl reference`` times the CPU restatement of the reference's kernels
+(oracle/, C + OpenMP on all host cores) on bounded samples of the same
+workload and extrapolates to one solve.
+
+Multi-GPU: the path does not shard across GPUs here (replicas only): under
+torchrun every rank solves its own replica; value is the max over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "cube48": dict(n_face=48, n_fault=32),
+    "cube24": dict(n_face=24, n_fault=16),
+    "cube12": dict(n_face=12, n_fault=8),
+}
+RTOL = 1e-8
+RESTART = 50
+METRIC = "time-to-solve at 1e-8 rel. residual (FP64 true residual, assembly included)"
+
+
+def _dist():
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1 and not torch.distributed.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        torch.distributed.init_process_group(backend)
+    return rank, ws
+
+
+def _barrier(ws):
+    import torch
+    if ws > 1:
+        torch.distributed.barrier()
+
+
+def _max_over_ranks(v, ws):
+    import torch
+    if ws == 1:
+        return v
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def fp64_peak_tflops():
+    """DFMA throughput of this GPU (own probe kernel, CUDA events)."""
+    import torch
+    from mbem_gb300 import _native as nat
+    from mbem_gb300._device import ptr, stream_handle
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 4096
+    for _ in range(2):
+        nat.call("mbem_fp64_fma_probe", ptr(out), iters, blocks, threads, stream_handle())
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    nat.call("mbem_fp64_fma_probe", ptr(out), iters, blocks, threads, stream_handle())
+    e.record()
+    e.synchronize()
+    sec = s.elapsed_time(e) / 1e3
+    return 16.0 * iters * blocks * threads / sec / 1e12
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args, rank, ws):
+    import torch
+    from mbem_gb300 import _native as nat
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.model import generate_system
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    cfg = WORKLOADS[args.workload]
+    model, eps = cube_fault_model(cfg["n_face"], cfg["n_fault"])
+    system = generate_system(model)
+    n = system.layout.n_unknowns
+    backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART)
+    arrays = {}     # device-resident mesh arrays, filled by the first assembly
+
+    def step(timer=None):
+        asm = backend.assemble(system, eps, arrays=arrays, timer=timer)
+        x = asm.solve_device()
+        rep = asm.report
+        asm.A = None
+        return x, rep
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    _barrier(ws)
+
+    timer = []
+    reps = []
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = nat.lib().mbem_launch_count()
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        start.record()
+        for _ in range(args.steps):
+            _, rep = step(timer)
+            reps.append(rep)
+        end.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = nat.lib().mbem_launch_count() - launches0
+    dev_s = start.elapsed_time(end) / 1e3 / args.steps
+    dev_s = _max_over_ranks(dev_s, ws)
+
+    # the dominant kernel: the FP64 T-kernel assembly (one launch per block)
+    asm_ms = [s.elapsed_time(e) for (k, nf, ns, s, e) in timer]
+    pairs = [nf * ns for (k, nf, ns, s, e) in timer]
+    asm_launch_ms = float(np.mean(asm_ms))
+    pairs_per_launch = float(np.mean(pairs))
+
+    # end to end through the public API from host arrays
+    e2e = None
+    if not args.skip_e2e:
+        from mbem_gb300 import mesh as M
+        from mbem_gb300.model import BCType, Patch, Region, RegionModel
+        host_cube = M.cube(cfg["n_face"])
+        host_fault = M.centre_fault(cfg["n_fault"])
+
+        def e2e_step():
+            cube_p = Patch("cube", host_cube, BCType.FREE_TRACTION)
+            fault_p = Patch("fault", host_fault, BCType.FAULT, value=np.array([1.0, 0.0, 0.0]))
+            m = RegionModel([Region("body", M.ElasticMaterial(1.0, 1.0), [cube_p], np.zeros(3),
+                                    faults=[fault_p])])
+            asm = backend.assemble(generate_system(m), eps)
+            sol = asm.solve()
+            asm.A = None
+            return sol
+
+        e2e_step()
+        torch.cuda.synchronize()
+        _barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_s = _max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, ws)
+        n_c, n_f = host_cube.n_triangles, host_fault.n_triangles
+        h2d = 8 * (n_c * (9 + 3 + 1 + 3 + 3) + n_f * (9 + 3 + 1) + 3 * n_f + 9 * n_c)
+        e2e = {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 8 * n}
+
+    peaks = measured_peaks()
+    fp64 = fp64_peak_tflops()
+    flop_pair = FLOP_PER_T_PAIR
+    achieved = flop_pair * pairs_per_launch / (asm_launch_ms / 1e3) / 1e12
+    line = {
+        "metric": METRIC,
+        "value": dev_s,
+        "unit": "s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_s * 1e3,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded mesh generators; no dataset)",
+        "config": {"workload": args.workload, "n_face": cfg["n_face"], "n_fault": cfg["n_fault"],
+                   "unknowns": n, "precision": "fp64", "solver": f"deflated FGMRES({RESTART})",
+                   "rtol": RTOL, "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "inputs larger than L2 (A = %.1f GB FP64)" % (8.0 * n * n / 1e9)},
+        "iterations": reps[-1].iterations,
+        "true_relres": reps[-1].true_relres,
+        "wall_s_per_step": wall / args.steps,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": "p0_matrix_kernel<T_DIRECT>", "bound": "fp64",
+                     "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
+                     "frac": achieved / fp64, "traffic": None,
+                     "flop_per_pair": flop_pair, "pairs_per_launch": pairs_per_launch,
+                     "launch_ms": asm_launch_ms,
+                     "peak_source": "own DFMA probe (mbem_fp64_fma_probe), measured in this run"},
+        "assembly_share": float(np.sum(asm_ms)) / 1e3 / args.steps / dev_s,
+        "measured_peaks": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops")},
+    }
+    clocks = clk.summary()
+    if clocks:
+        line["clocks"] = clocks
+    if rank == 0 and not args.skip_cpu:
+        line["cpu_baseline"] = cpu_baseline(args, reps[-1].iterations)
+    return line
+
+
+# FP64 operations per T-kernel pair of the CUDA formulation, counted from
+# the source of p0_pair.cuh (t_moments + t_block; FMA = 2, add/mul = 1,
+# each sqrt/div/log/atan2 = 1).
+FLOP_PER_T_PAIR = 480.0
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle restatement of the reference's kernels)
+# ---------------------------------------------------------------------------
+
+def cpu_baseline(args, iterations):
+    """Times the C restatement on all host cores on a bounded sample of the
+    workload and extrapolates one solve: assembly of a source-column sample
+    (all field points) and the dense FP64 matvec on a row sample, times the
+    FGMRES iteration count."""
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.kernels import basis as kb
+    from oracle import oracle as orc
+
+    threads = orc.set_threads(os.cpu_count() or 1)
+    cfg = WORKLOADS[args.workload]
+    model, eps = cube_fault_model(cfg["n_face"], cfg["n_fault"])
+    cube = model.regions[0].patches[0]
+    x = cube.collocation_points()
+    tv = cube.tri_verts()
+    nrm, _ = cube.mesh.normals_and_areas()
+    e = np.full(tv.shape[0], eps)
+    c = kb.t_coeffs(1.0, 1.0)
+    Ns = tv.shape[0]
+    # grow the source sample until it takes >= 2 s
+    s1 = 16
+    while True:
+        t0 = time.perf_counter()
+        orc.matrix("t", x, tv[:s1], nrm[:s1], e[:s1], c)
+        dt = time.perf_counter() - t0
+        if dt >= 2.0 or s1 >= Ns:
+            break
+        s1 = min(Ns, s1 * 4)
+    asm_s = dt * Ns / s1
+    n = 3 * Ns
+    rows = 1024
+    A = np.random.default_rng(0).normal(size=(rows, n))
+    xv = np.ones(n)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        orc.dgemv(A, xv)
+    mv_s = (time.perf_counter() - t0) / 5 * n / rows
+    total = asm_s + (iterations + 2) * mv_s
+    return {"value": total, "unit": "s", "cores": threads, "kind": "port",
+            "sample": f"T-kernel assembly of {s1} of {Ns} source columns x {x.shape[0]} field points "
+                      f"({dt:.2f} s, extrapolated x{Ns / s1:.1f}) + FP64 matvec on {rows} of {n} rows "
+                      f"x {iterations + 2} matvecs; host {os.uname().machine}"}
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return None
+    from oracle import oracle as orc
+    orc.lib()
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(args, ITER_GUESS)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(args, ITER_GUESS))
+    v = float(np.mean([b["value"] for b in vals]))
+    base = vals[-1]
+    cfg = WORKLOADS[args.workload]
+    return {"metric": METRIC, "value": v, "unit": "s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded mesh generators; no dataset)",
+            "config": {"workload": args.workload, "n_face": cfg["n_face"], "n_fault": cfg["n_fault"],
+                       "precision": "fp64", "solver": f"deflated FGMRES({RESTART})", "rtol": RTOL},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "s", "cores": base["cores"], "kind": "port",
+                             "sample": base["sample"]},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# FGMRES(50) iterations of the reference on the calibrated cube (the
+# reference took 20 to 1e-8 at n = 12); the CPU arm has no solve of its own
+# to count, so it uses this figure for the matvec count.
+ITER_GUESS = 20
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cube48", choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    rank, ws = _dist()
+    if args.impl == "reference":
+        line = run_reference(args, rank, ws)
+    else:
+        line = run_ours(args, rank, ws)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

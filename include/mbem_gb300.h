@@ -1,0 +1,181 @@
+/*
+ * mbem_gb300 C ABI: the GB300 (sm_103a) hot path of the mollified boundary
+ * element method behind plain pointers and sizes.
+ *
+ * Conventions for every entry point:
+ *  - array arguments are DEVICE pointers to C-contiguous float64 arrays in
+ *    the reference's layouts (x_field (Nf,3); tri_verts (Ns,3,3) vertex
+ *    major; normals (Ns,3); eps (Ns,); density (K*Ns,3); matrices row-major
+ *    (3Nf, 3KNs) with block (3f+i, 3(K s+k)+j); stress (Nf,3,3));
+ *  - small coefficient vectors (`coeffs`, `shape`, slot ranges) are HOST
+ *    pointers;
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream); every call
+ *    is asynchronous on it unless stated otherwise;
+ *  - the return value is an mbem_status; mbem_last_error() describes the
+ *    last failure of the calling thread;
+ *  - nothing allocates device memory: scratch comes from a caller-provided
+ *    workspace whose size the matching *_workspace_size query returns.
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the reference project's root).
+ */
+#ifndef MBEM_GB300_H
+#define MBEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MBEM_OK = 0,
+    MBEM_ERR_ARG = 1,          /* invalid argument: NULL pointer, bad size, order or kind */
+    MBEM_ERR_UNSUPPORTED = 2,  /* a combination the library does not implement */
+    MBEM_ERR_CUDA = 3,         /* a CUDA runtime or launch failure */
+    MBEM_ERR_WAIT = 4,         /* a bounded device-side wait expired */
+    MBEM_ERR_SIZE = 5,         /* a size beyond a stated maximum, or a workspace too small */
+    MBEM_ERR_NUMERIC = 6       /* breakdown detected (zero pivot, non-finite value) */
+} mbem_status;
+
+/* Kinds of mbem_stress_contract. */
+enum {
+    MBEM_STRESS_DD = 0,        /* slip -> total stress (tri_nodal.py:1344 dd_stress_contract) */
+    MBEM_STRESS_KELVIN = 1,    /* force -> stress (tri_nodal.py:1334 kelvin_stress_contract) */
+    MBEM_STRESS_EIGEN = 2,     /* exact eigenstress +C:eps* (tri_nodal.py:1355 eigenstress_contract) */
+    MBEM_STRESS_ELASTIC = 3    /* dd minus eigen in one pass (evaluate.py:383-407 _double_layer_stress) */
+};
+
+/* Library identity and the last error message of the calling thread. */
+int mbem_version(void);
+const char* mbem_last_error(void);
+/* Kernels this library has launched since it was loaded (all threads). */
+unsigned long long mbem_launch_count(void);
+/* FP64 pipe throughput probe: blocks*threads threads each run 8 independent
+ * DFMA chains of `iters` steps (16*iters FLOP per thread); time it with
+ * events for the FP64 roofline denominator. No reference counterpart. */
+int mbem_fp64_fma_probe(double* out, int64_t iters, int blocks, int threads, void* stream);
+
+/* ---- kernel matrices: src/mbem/kernels/tri_nodal.py:1289-1306 (public
+ * drivers) and src/mbem/kernels/tri_kernels.py:547-591 (P0 direct).
+ * out(3Nf, 3KNs) at leading dimension ld_out: out = alpha*M (accumulate=0)
+ * or out += alpha*M (accumulate=1), so a block lands directly inside a
+ * larger system matrix. coeffs: 6 T coefficients (basis.py:58-72 t_coeffs)
+ * or 3 U coefficients (basis.py:46-55 u_coeffs). ---------------------- */
+int mbem_t_matrix_direct(const double* x_field, int64_t n_field, const double* tri_verts,
+                         const double* normals, const double* eps, int64_t n_src,
+                         const double* coeffs, int order, double alpha, int accumulate,
+                         double* out, int64_t ld_out, void* stream);
+int mbem_u_matrix_direct(const double* x_field, int64_t n_field, const double* tri_verts,
+                         const double* eps, int64_t n_src, const double* coeffs, int order,
+                         double alpha, int accumulate, double* out, int64_t ld_out, void* stream);
+
+/* Geometry-only basis stacks (6 or 3, 3Nf, 3KNs), contiguous:
+ * tri_nodal.py t_basis_matrices / u_basis_matrices (tri_kernels.py:451-492). */
+int mbem_t_basis_matrices(const double* x_field, int64_t n_field, const double* tri_verts,
+                          const double* normals, const double* eps, int64_t n_src, int order,
+                          double* out, void* stream);
+int mbem_u_basis_matrices(const double* x_field, int64_t n_field, const double* tri_verts,
+                          const double* eps, int64_t n_src, int order, double* out, void* stream);
+
+/* ---- matrix-free contractions (tri_kernels.py:976-1260; tri_nodal.py
+ * :1310-1366). Displacement out (Nf,3); stress out (Nf,3,3). out = alpha*r
+ * or out += alpha*r. Sources with an all-zero density are skipped, as the
+ * reference does. ------------------------------------------------------ */
+int mbem_t_disp_contract(const double* x_field, int64_t n_field, const double* tri_verts,
+                         const double* normals, const double* eps, int64_t n_src,
+                         const double* density, const double* coeffs, int order, double alpha,
+                         int accumulate, double* out, void* stream);
+int mbem_u_disp_contract(const double* x_field, int64_t n_field, const double* tri_verts,
+                         const double* eps, int64_t n_src, const double* density,
+                         const double* coeffs, int order, double alpha, int accumulate,
+                         double* out, void* stream);
+int mbem_stress_contract(int kind, const double* x_field, int64_t n_field,
+                         const double* tri_verts, const double* normals, const double* eps,
+                         int64_t n_src, const double* density, double mu, double lam, int order,
+                         double alpha, int accumulate, double* out, void* stream);
+
+/* ---- traction rows: tri_nodal.py:1370-1404 traction_matrix /
+ * basis.py:406-427 assemble_traction_matrix. which: 0 "slip" (total minus
+ * eigen), 1 "force", 2 "eigen", 3 "total". ids (Ns,K) int64 DEVICE array
+ * scattering element-node columns onto n_cols shared columns; out
+ * (3Nf, 3 n_cols) at ld_out, accumulated (out += alpha * rows). -------- */
+int mbem_traction_matrix(const double* x_field, const double* n_field, int64_t n_pts,
+                         const double* tri_verts, const double* normals, const double* eps,
+                         int64_t n_src, const int64_t* ids, int64_t n_cols, double mu, double lam,
+                         int order, int which, double alpha, double* out, int64_t ld_out,
+                         void* stream);
+
+/* ---- dense-system helpers of the calibrated dense backend
+ * (src/mbem/backends/dense.py:480-528). ------------------------------- */
+
+/* out[r, j] (+)= alpha * sum_c A[r, 3c + j] for c < n_col_nodes: the
+ * calibration row sums (dense.py:497-500 rowsum, equations.py:512-537). */
+int mbem_block_rowsum3(const double* A, int64_t ld, int64_t n_rows, int64_t n_col_nodes,
+                       double alpha, int accumulate, double* out, void* stream);
+
+/* A[r0 + 3c + a, c0 + 3(K s + k) + b] += shape[kc*K + k] * D[c, a, b] for
+ * c = K s + kc (equations.py:566-582 add_block_diagonal). A points at the
+ * block's top-left corner; shape is a HOST (K,K) array. */
+int mbem_add_block_diagonal(double* A, int64_t ld, const double* D, int64_t n_c, int K,
+                            const double* shape, void* stream);
+
+/* y = alpha * A x + beta * y, FP64 row-major (the dense matvec of
+ * la/solver.py:513-520 _as_matvec on an AssembledDense.A). */
+int mbem_dgemv(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols, const double* x,
+               double alpha, double beta, double* y, void* stream);
+
+/* Y = A X for k right-hand sides (X, Y row-major (n, k)): the multi-RHS
+ * refinement product of la/lu.py:210. */
+int mbem_dgemm_multi(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols, const double* X,
+                     int64_t k, double* Y, void* stream);
+
+/* ---- deflated FGMRES on a dense operator (la/solver.py:115-245 fgmres,
+ * wired as backends/hmat.py:678-690: P A P y = P b, P = I - Z Z^T with Z
+ * the rigid-translation basis of backends/dense.py:190-208). ---------- */
+typedef struct {
+    int restart;            /* Krylov dimension per cycle (la/solver.py restart) */
+    int maxiter;            /* total iteration cap */
+    double rtol;            /* relative residual target on the true residual */
+    int stagnation_window;  /* iterations without a stagnation_factor gain before stopping */
+    double stagnation_factor;
+    int n_u_ranges;         /* deflation: number of (offset, size) u-slot ranges, 0 = none */
+    const int64_t* u_ranges;/* HOST array of 2*n_u_ranges int64 */
+    int precond;            /* 0 none, 1 block-Jacobi (mbem_bj_*), 2 learned (mbem_nn_*) */
+    const void* precond_state; /* the preconditioner object for precond != 0 */
+} mbem_fgmres_params;
+
+typedef struct {
+    int converged;
+    int iterations;
+    int restarts;
+    int stagnated;
+    double true_relres;
+    double arnoldi_relres;
+    double* history;        /* optional HOST array of maxiter doubles, filled if non-NULL */
+} mbem_fgmres_report;
+
+/* Bytes of device workspace mbem_fgmres_dense needs for n unknowns. */
+size_t mbem_fgmres_workspace_size(int64_t n, int restart);
+
+/* Solve A x = b (A FP64 (n,n) at leading dimension ld; b, x device (n,)).
+ * x holds the initial guess on entry (zeros for none) and the solution on
+ * exit (the zero-mean-translation representative P y when deflating).
+ * Synchronises `stream` once per iteration (the Givens step runs on the
+ * host on (restart+1) scalars). */
+int mbem_fgmres_dense(const double* A, int64_t ld, int64_t n, const double* b, double* x,
+                      const mbem_fgmres_params* params, void* work, size_t work_bytes,
+                      mbem_fgmres_report* report, void* stream);
+
+/* The deflation projection v_out = P v_in (hmat.py:684-685 proj). work:
+ * 3 doubles of device memory. */
+int mbem_project_translation(const double* v_in, double* v_out, int64_t n,
+                             const int64_t* u_ranges, int n_u_ranges, double* work,
+                             void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MBEM_GB300_H */

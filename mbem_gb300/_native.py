@@ -1,0 +1,118 @@
+"""ctypes binding of the C ABI in ``include/mbem_gb300.h``.
+
+The library is the product path: there is no CPU fallback. If
+``_lib/libmbem_gb300.so`` is missing, importing a GPU entry point raises
+with the instruction to build it (``python -m mbem_gb300.build`` or
+``__graft_entry__.build()``).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, Structure, c_double, c_int, c_int64, c_size_t, c_void_p
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libmbem_gb300.so")
+
+# status codes (mbem_status)
+OK = 0
+ERR_ARG = 1
+ERR_UNSUPPORTED = 2
+ERR_CUDA = 3
+ERR_WAIT = 4
+ERR_SIZE = 5
+ERR_NUMERIC = 6
+
+STRESS_DD, STRESS_KELVIN, STRESS_EIGEN, STRESS_ELASTIC = 0, 1, 2, 3
+
+
+class MbemError(RuntimeError):
+    """A non-zero mbem_status from the CUDA library."""
+
+    def __init__(self, code: int, what: str, message: str):
+        super().__init__(f"{what}: status {code}: {message}")
+        self.code = code
+
+
+class FgmresParams(Structure):
+    _fields_ = [("restart", c_int), ("maxiter", c_int), ("rtol", c_double),
+                ("stagnation_window", c_int), ("stagnation_factor", c_double),
+                ("n_u_ranges", c_int), ("u_ranges", POINTER(c_int64)),
+                ("precond", c_int), ("precond_state", c_void_p)]
+
+
+class FgmresReport(Structure):
+    _fields_ = [("converged", c_int), ("iterations", c_int), ("restarts", c_int),
+                ("stagnated", c_int), ("true_relres", c_double), ("arnoldi_relres", c_double),
+                ("history", POINTER(c_double))]
+
+
+_P = c_void_p
+_I = c_int64
+_D = c_double
+
+# name -> (restype, argtypes)
+_SIGNATURES = {
+    "mbem_version": (c_int, []),
+    "mbem_last_error": (ctypes.c_char_p, []),
+    "mbem_launch_count": (ctypes.c_ulonglong, []),
+    "mbem_fp64_fma_probe": (c_int, [_P, _I, c_int, c_int, _P]),
+    "mbem_t_matrix_direct": (c_int, [_P, _I, _P, _P, _P, _I, _P, c_int, _D, c_int, _P, _I, _P]),
+    "mbem_u_matrix_direct": (c_int, [_P, _I, _P, _P, _I, _P, c_int, _D, c_int, _P, _I, _P]),
+    "mbem_t_basis_matrices": (c_int, [_P, _I, _P, _P, _P, _I, c_int, _P, _P]),
+    "mbem_u_basis_matrices": (c_int, [_P, _I, _P, _P, _I, c_int, _P, _P]),
+    "mbem_t_disp_contract": (c_int, [_P, _I, _P, _P, _P, _I, _P, _P, c_int, _D, c_int, _P, _P]),
+    "mbem_u_disp_contract": (c_int, [_P, _I, _P, _P, _I, _P, _P, c_int, _D, c_int, _P, _P]),
+    "mbem_stress_contract": (c_int, [c_int, _P, _I, _P, _P, _P, _I, _P, _D, _D, c_int, _D, c_int,
+                                     _P, _P]),
+    "mbem_traction_matrix": (c_int, [_P, _P, _I, _P, _P, _P, _I, _P, _I, _D, _D, c_int, c_int, _D,
+                                     _P, _I, _P]),
+    "mbem_block_rowsum3": (c_int, [_P, _I, _I, _I, _D, c_int, _P, _P]),
+    "mbem_add_block_diagonal": (c_int, [_P, _I, _P, _I, c_int, _P, _P]),
+    "mbem_dgemv": (c_int, [_P, _I, _I, _I, _P, _D, _D, _P, _P]),
+    "mbem_dgemm_multi": (c_int, [_P, _I, _I, _I, _P, _I, _P, _P]),
+    "mbem_project_translation": (c_int, [_P, _P, _I, _P, c_int, _P, _P]),
+    "mbem_fgmres_workspace_size": (c_size_t, [_I, c_int]),
+    "mbem_fgmres_dense": (c_int, [_P, _I, _I, _P, _P, POINTER(FgmresParams), _P, c_size_t,
+                                  POINTER(FgmresReport), _P]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded library (loaded once; raises if it was never built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"mbem_gb300 CUDA library not found at {LIB_PATH}: build it with "
+                f"`python -m mbem_gb300.build` (nvcc, sm_103a). There is no CPU fallback.")
+        h = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = h
+    return _lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGNATURES)
+
+
+def call(name: str, *args) -> None:
+    """Call an entry point and raise MbemError on a non-zero status."""
+    st = getattr(lib(), name)(*args)
+    if st != OK:
+        msg = lib().mbem_last_error()
+        msg = msg.decode(errors="replace") if msg else ""
+        if st == ERR_ARG:
+            raise ValueError(f"{name}: {msg}")
+        raise MbemError(st, name, msg)
+
+
+def dbl_array(values) -> ctypes.Array:
+    vals = [float(v) for v in values]
+    return (c_double * len(vals))(*vals)

@@ -1,0 +1,69 @@
+// Library identity, error reporting, and the not-yet-specialised paths.
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <atomic>
+
+#include "common.cuh"
+
+namespace mbem {
+
+static thread_local char g_last_error[512] = "";
+
+int set_error(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+static std::atomic<unsigned long long> g_launches{0};
+
+void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+
+int launch_status(const char* what, int n_launched) {
+    count_launches(n_launched);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return MBEM_OK;
+}
+
+}  // namespace mbem
+
+namespace mbem {
+
+// Independent DFMA chains (8 per thread) for the FP64 pipe's throughput.
+__global__ void fp64_fma_probe_kernel(double* out, int64_t iters) {
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) a[k] = 1.0 + 1e-9 * (threadIdx.x + k);
+    const double m = 0.999999999, c = 1e-12;
+    for (int64_t i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = fma(a[k], m, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += a[k];
+    if (s == 12345.678) out[0] = s;   // keeps the chains live; never true
+}
+
+}  // namespace mbem
+
+extern "C" {
+
+unsigned long long mbem_launch_count(void) { return mbem::g_launches.load(); }
+
+int mbem_fp64_fma_probe(double* out, int64_t iters, int blocks, int threads, void* stream) {
+    MBEM_REQUIRE(out && iters > 0 && blocks > 0 && threads > 0 && threads <= 1024, MBEM_ERR_ARG,
+                 "bad probe launch");
+    mbem::fp64_fma_probe_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(out, iters);
+    return mbem::launch_status("fp64_fma_probe_kernel");
+}
+
+int mbem_version(void) { return 1; }
+
+const char* mbem_last_error(void) { return mbem::g_last_error; }
+
+}  // extern "C"

@@ -1,0 +1,42 @@
+// Shared definitions for the mbem_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mbem_gb300.h"
+
+#define MBEM_PI 3.14159265358979323846
+
+namespace mbem {
+
+// Records the last error message for mbem_last_error(); returns `code`.
+int set_error(int code, const char* fmt, ...);
+
+// Counts `n_launched` kernel launches and maps the launch status of the last
+// kernel to an mbem status.
+int launch_status(const char* what, int n_launched = 1);
+
+// Counts kernel launches whose status is checked later.
+void count_launches(int n);
+
+// Nodal (P1/P2) drivers behind the public entry points when order > 0.
+// kind for nodal_matrix: 0 T direct, 1 U direct, 2 T basis, 3 U basis;
+// for nodal_contract: 0 T disp, 1 U disp, 2 + MBEM_STRESS_* for stress.
+int nodal_matrix(int kind, const double* x, int64_t nf, const double* tv, const double* normals,
+                 const double* eps, int64_t ns, const double* coeffs, int order, double alpha,
+                 int accumulate, double* out, int64_t ld, void* stream);
+int nodal_contract(int kind, const double* x, int64_t nf, const double* tv, const double* normals,
+                   const double* eps, int64_t ns, const double* density, const double* coeffs,
+                   double mu, double lam, int order, double alpha, int accumulate, double* out,
+                   void* stream);
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+__host__ __device__ inline int64_t lmin(int64_t a, int64_t b) { return a < b ? a : b; }
+
+}  // namespace mbem
+
+#define MBEM_REQUIRE(cond, code, ...)                      \
+    do {                                                   \
+        if (!(cond)) return mbem::set_error((code), __VA_ARGS__); \
+    } while (0)

@@ -1,0 +1,598 @@
+// Dense-system kernels of the calibrated dense backend and the deflated
+// FGMRES that solves it, FP64 (sm_103a).
+//
+// The matvec streams A once from HBM with 128-bit loads (4 rows per warp so
+// each x load from L2 serves four rows); every reduction runs in a fixed
+// order (per-block partials, then one ordered pass), so results are
+// bit-reproducible run to run. The Arnoldi basis of an 83k-unknown system
+// at restart 50 is ~34 MB and stays L2-resident.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace mbem {
+
+// ---------------------------------------------------------------------------
+// calibration row sums: out[r, j] (+)= alpha * sum_c A[r, 3c + j]
+// ---------------------------------------------------------------------------
+__global__ void rowsum3_kernel(const double* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_cols,
+                               double alpha, int accumulate, double* __restrict__ out) {
+    const int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (r >= n_rows) return;
+    const double* row = A + r * ld;
+    double acc[3] = {0.0, 0.0, 0.0};
+    // lane l visits columns l, l+32, ...; column c belongs to component c % 3
+    int j = lane % 3;
+    for (int64_t c = lane; c < n_cols; c += 32) {
+        acc[j] += row[c];
+        j += 2;                 // (c + 32) % 3 == (c % 3 + 2) % 3
+        if (j >= 3) j -= 3;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const double v = alpha * acc[k];
+            out[3 * r + k] = accumulate ? out[3 * r + k] + v : v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// free-term diagonal spread over the element's nodes by the collocation shape
+// ---------------------------------------------------------------------------
+struct ShapeK {
+    double w[36];
+};
+
+__global__ void add_block_diag_kernel(double* __restrict__ A, int64_t ld, const double* __restrict__ D,
+                                      int64_t n_c, int K, ShapeK shape) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_c) return;
+    const int64_t s = c / K;
+    const int kc = (int)(c % K);
+    for (int k = 0; k < K; k++) {
+        const double w = shape.w[kc * K + k];
+        if (w == 0.0) continue;
+        const int64_t col = 3 * (K * s + k);
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) A[(3 * c + a) * ld + col + b] += w * D[9 * c + 3 * a + b];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// y = alpha A x + beta y: 4 rows per warp, 128-bit streaming loads of A
+// ---------------------------------------------------------------------------
+constexpr int GEMV_ROWS = 4;
+constexpr int GEMV_THREADS = 256;
+
+__global__ void __launch_bounds__(GEMV_THREADS)
+dgemv_vec_kernel(const double* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_cols,
+                 const double* __restrict__ x, double alpha, double beta, double* __restrict__ y) {
+    const int64_t warp = (int64_t)blockIdx.x * (GEMV_THREADS / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    const int64_t r0 = warp * GEMV_ROWS;
+    if (r0 >= n_rows) return;
+    const int nr = (int)lmin(GEMV_ROWS, n_rows - r0);
+    double acc[GEMV_ROWS] = {0.0, 0.0, 0.0, 0.0};
+    const int64_t n2 = n_cols / 2;
+    const double2* x2 = reinterpret_cast<const double2*>(x);
+    const double2* rows[GEMV_ROWS];
+#pragma unroll
+    for (int i = 0; i < GEMV_ROWS; i++)
+        rows[i] = reinterpret_cast<const double2*>(A + (r0 + min(i, nr - 1)) * ld);
+    for (int64_t c = lane; c < n2; c += 32) {
+        const double2 xv = __ldg(x2 + c);
+#pragma unroll
+        for (int i = 0; i < GEMV_ROWS; i++) {
+            const double2 av = __ldcs(rows[i] + c);
+            acc[i] = fma(av.x, xv.x, acc[i]);
+            acc[i] = fma(av.y, xv.y, acc[i]);
+        }
+    }
+    if ((n_cols & 1) && lane == 0) {
+        const double xv = x[n_cols - 1];
+#pragma unroll
+        for (int i = 0; i < GEMV_ROWS; i++)
+            acc[i] = fma(A[(r0 + min(i, nr - 1)) * ld + n_cols - 1], xv, acc[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < GEMV_ROWS; i++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+    if (lane < nr) {
+        double v = acc[0];
+#pragma unroll
+        for (int i = 1; i < GEMV_ROWS; i++)
+            if (lane == i) v = acc[i];
+        const int64_t r = r0 + lane;
+        y[r] = (beta == 0.0) ? alpha * v : alpha * v + beta * y[r];
+    }
+}
+
+__global__ void __launch_bounds__(GEMV_THREADS)
+dgemv_scalar_kernel(const double* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_cols,
+                    const double* __restrict__ x, double alpha, double beta, double* __restrict__ y) {
+    const int64_t r = (int64_t)blockIdx.x * (GEMV_THREADS / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (r >= n_rows) return;
+    double acc = 0.0;
+    for (int64_t c = lane; c < n_cols; c += 32) acc = fma(A[r * ld + c], x[c], acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[r] = (beta == 0.0) ? alpha * acc : alpha * acc + beta * y[r];
+}
+
+int dgemv(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols, const double* x, double alpha,
+          double beta, double* y, cudaStream_t st) {
+    if (n_rows == 0) return MBEM_OK;
+    const bool vec = ((uintptr_t)A % 16 == 0) && ((uintptr_t)x % 16 == 0) && (ld % 2 == 0);
+    if (vec) {
+        const int64_t warps = ceil_div(n_rows, GEMV_ROWS);
+        dgemv_vec_kernel<<<(unsigned)ceil_div(warps, GEMV_THREADS / 32), GEMV_THREADS, 0, st>>>(
+            A, ld, n_rows, n_cols, x, alpha, beta, y);
+    } else {
+        dgemv_scalar_kernel<<<(unsigned)ceil_div(n_rows, GEMV_THREADS / 32), GEMV_THREADS, 0, st>>>(
+            A, ld, n_rows, n_cols, x, alpha, beta, y);
+    }
+    return launch_status("dgemv");
+}
+
+// ---------------------------------------------------------------------------
+// Y = A X, X and Y row-major (n, k): one warp per row, k <= 64 per pass
+// ---------------------------------------------------------------------------
+__global__ void dgemm_multi_kernel(const double* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_cols,
+                                   const double* __restrict__ X, int64_t k, int64_t k0, int kc,
+                                   double* __restrict__ Y) {
+    const int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (r >= n_rows) return;
+    double acc[64];
+    for (int q = 0; q < kc; q++) acc[q] = 0.0;
+    for (int64_t c = lane; c < n_cols; c += 32) {
+        const double a = A[r * ld + c];
+        const double* xr = X + c * k + k0;
+        for (int q = 0; q < kc; q++) acc[q] = fma(a, xr[q], acc[q]);
+    }
+    for (int q = 0; q < kc; q++) {
+        double v = acc[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) Y[r * k + k0 + q] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Krylov vector kernels (fixed-order reductions)
+// ---------------------------------------------------------------------------
+constexpr int KV_THREADS = 256;
+constexpr int KV_COLS = 2 * KV_THREADS;      // columns per block
+constexpr int KV_MAXV = 64;                  // vectors per multi-dot pass
+
+// partial[b * k + i] = sum over block b's columns of V[i, c] * w[c]
+__global__ void __launch_bounds__(KV_THREADS)
+multidot_partial_kernel(const double* __restrict__ V, int64_t ldv, int k, int64_t n,
+                        const double* __restrict__ w, double* __restrict__ partial) {
+    __shared__ double red[KV_THREADS / 32][KV_MAXV];
+    const int64_t c0 = (int64_t)blockIdx.x * KV_COLS + 2 * threadIdx.x;
+    double w0 = 0.0, w1 = 0.0;
+    if (c0 < n) w0 = w[c0];
+    if (c0 + 1 < n) w1 = w[c0 + 1];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = 0; i < k; i++) {
+        const double* v = V + (int64_t)i * ldv;
+        double p = 0.0;
+        if (c0 < n) p = v[c0] * w0;
+        if (c0 + 1 < n) p = fma(v[c0 + 1], w1, p);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+        if (lane == 0) red[wid][i] = p;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < k; i += KV_THREADS) {
+        double s = 0.0;
+        for (int q = 0; q < KV_THREADS / 32; q++) s += red[q][i];
+        partial[(int64_t)blockIdx.x * k + i] = s;
+    }
+}
+
+// h[i] (+)= sum_b partial[b * k + i], in block order
+__global__ void multidot_final_kernel(const double* __restrict__ partial, int nblocks, int k, int accumulate,
+                                      double* __restrict__ h) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    double s = 0.0;
+    for (int b = 0; b < nblocks; b++) s += partial[(int64_t)b * k + i];
+    h[i] = accumulate ? h[i] + s : s;
+}
+
+// w[c] += sign * sum_i V[i, c] h[i]
+__global__ void multiaxpy_kernel(double* __restrict__ w, const double* __restrict__ V, int64_t ldv, int k,
+                                 int64_t n, const double* __restrict__ h, double sign) {
+    __shared__ double hs[KV_MAXV];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) hs[i] = sign * h[i];
+    __syncthreads();
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    double acc = w[c];
+    for (int i = 0; i < k; i++) acc = fma(V[(int64_t)i * ldv + c], hs[i], acc);
+    w[c] = acc;
+}
+
+// v_out = v_in * (1 / sqrt(*nrm2)), nrm2 on the device
+__global__ void scale_by_rnorm_kernel(const double* __restrict__ v_in, double* __restrict__ v_out, int64_t n,
+                                      const double* __restrict__ nrm2) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const double s = *nrm2;
+    const double inv = (s > 0.0 ? 1.0 / sqrt(s) : 0.0);
+    v_out[c] = v_in[c] * inv;
+}
+
+__global__ void axpby_kernel(double* __restrict__ y, const double* __restrict__ x, int64_t n, double a,
+                             double b) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < n) y[c] = a * x[c] + b * y[c];
+}
+
+// ---------------------------------------------------------------------------
+// deflation projection: subtract, per component, the mean over the u-slots
+// ---------------------------------------------------------------------------
+struct URanges {
+    int64_t off[8];
+    int64_t len[8];
+    int n;
+};
+
+constexpr int PROJ_THREADS = 1024;
+
+__global__ void __launch_bounds__(PROJ_THREADS)
+project_kernel(const double* __restrict__ vin, double* __restrict__ vout, int64_t n, URanges ur) {
+    __shared__ double red[PROJ_THREADS / 32][3];
+    __shared__ double mean[3];
+    double acc[3] = {0.0, 0.0, 0.0};
+    int64_t total = 0;
+    for (int q = 0; q < ur.n; q++) {
+        const int64_t off = ur.off[q], len = ur.len[q];
+        total += len;
+        for (int64_t t = threadIdx.x; t < len; t += PROJ_THREADS) acc[t % 3] += vin[off + t];
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+        if (lane == 0) red[wid][k] = acc[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double s = 0.0;
+        for (int q = 0; q < PROJ_THREADS / 32; q++) s += red[q][threadIdx.x];
+        // Z_k = 1/sqrt(M) on component-k u entries: Z (Z^T v) = sum / M
+        mean[threadIdx.x] = (total > 0) ? s / (double)(total / 3) : 0.0;
+    }
+    __syncthreads();
+    if (vout != vin)
+        for (int64_t c = threadIdx.x; c < n; c += PROJ_THREADS) vout[c] = vin[c];
+    __syncthreads();
+    for (int q = 0; q < ur.n; q++) {
+        const int64_t off = ur.off[q], len = ur.len[q];
+        for (int64_t t = threadIdx.x; t < len; t += PROJ_THREADS) vout[off + t] = vin[off + t] - mean[t % 3];
+    }
+}
+
+static int make_ranges(const int64_t* r, int nr, URanges& ur) {
+    MBEM_REQUIRE(nr >= 0 && nr <= 8, MBEM_ERR_ARG, "at most 8 u-slot ranges (got %d)", nr);
+    ur.n = nr;
+    for (int q = 0; q < nr; q++) {
+        ur.off[q] = r[2 * q];
+        ur.len[q] = r[2 * q + 1];
+        MBEM_REQUIRE(ur.off[q] >= 0 && ur.len[q] >= 0 && ur.len[q] % 3 == 0, MBEM_ERR_ARG,
+                     "bad u-slot range (%lld, %lld)", (long long)ur.off[q], (long long)ur.len[q]);
+    }
+    return MBEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FGMRES (la/solver.py:115-245) with classical Gram-Schmidt applied twice
+// (CGS2) in place of the reference's modified Gram-Schmidt: the same Arnoldi
+// relation to rounding, two fused passes instead of j+1 dependent ones.
+// ---------------------------------------------------------------------------
+struct FgmresWork {
+    double* V;        // (m+1, n)
+    double* w;        // n
+    double* t;        // n
+    double* r;        // n
+    double* partial;  // nblocks * (m+1)
+    double* h;        // m+2
+    double* h2;       // m+2
+    double* y;        // m
+    double* scal;     // 8
+};
+
+static size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static size_t fgmres_layout(int64_t n, int m, char* base, FgmresWork* w) {
+    const int64_t nb = ceil_div(n, KV_COLS);
+    size_t off = 0;
+    auto take = [&](size_t count) {
+        char* p = base ? base + off : nullptr;
+        off += align_up(count * sizeof(double));
+        return reinterpret_cast<double*>(p);
+    };
+    FgmresWork tmp;
+    tmp.V = take((size_t)(m + 1) * n);
+    tmp.w = take(n);
+    tmp.t = take(n);
+    tmp.r = take(n);
+    tmp.partial = take((size_t)nb * (m + 2));
+    tmp.h = take(m + 2);
+    tmp.h2 = take(m + 2);
+    tmp.y = take(m + 1);
+    tmp.scal = take(8);
+    if (w) *w = tmp;
+    return off;
+}
+
+struct Fgmres {
+    const double* A;
+    int64_t ld, n;
+    URanges ur;
+    bool deflate;
+    cudaStream_t st;
+    FgmresWork W;
+    int64_t nb;
+
+    int proj(const double* in, double* out) {
+        if (!deflate) {
+            if (in != out) cudaMemcpyAsync(out, in, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+            return launch_status("copy", 0);
+        }
+        project_kernel<<<1, PROJ_THREADS, 0, st>>>(in, out, n, ur);
+        return launch_status("project_kernel");
+    }
+    // out = P A P in (uses W.t)
+    int op(const double* in, double* out) {
+        int e = proj(in, W.t);
+        if (e) return e;
+        e = dgemv(A, ld, n, n, W.t, 1.0, 0.0, out, st);
+        if (e) return e;
+        return proj(out, out);
+    }
+    // h[0..k) (+)= V[0..k) . w
+    int multidot(const double* V, int k, const double* w, double* h, int accumulate) {
+        for (int i0 = 0; i0 < k; i0 += KV_MAXV) {
+            const int kc = min(KV_MAXV, k - i0);
+            multidot_partial_kernel<<<(unsigned)nb, KV_THREADS, 0, st>>>(V + (int64_t)i0 * n, n, kc, n, w,
+                                                                        W.partial);
+            multidot_final_kernel<<<1, 64, 0, st>>>(W.partial, (int)nb, kc, accumulate, h + i0);
+            count_launches(2);
+        }
+        return launch_status("multidot", 0);
+    }
+    int multiaxpy(double* w, const double* V, int k, const double* h, double sign) {
+        for (int i0 = 0; i0 < k; i0 += KV_MAXV) {
+            const int kc = min(KV_MAXV, k - i0);
+            multiaxpy_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(w, V + (int64_t)i0 * n, n, kc, n,
+                                                                       h + i0, sign);
+            count_launches(1);
+        }
+        return launch_status("multiaxpy", 0);
+    }
+    int norm2(const double* v, double* out_dev) { return multidot(v, 1, v, out_dev, 0); }
+};
+
+}  // namespace mbem
+
+using namespace mbem;
+
+extern "C" {
+
+int mbem_block_rowsum3(const double* A, int64_t ld, int64_t n_rows, int64_t n_col_nodes, double alpha,
+                       int accumulate, double* out, void* stream) {
+    MBEM_REQUIRE(n_rows >= 0 && n_col_nodes >= 0 && ld >= 3 * n_col_nodes, MBEM_ERR_ARG,
+                 "bad rowsum3 shape");
+    if (n_rows == 0) return MBEM_OK;
+    rowsum3_kernel<<<(unsigned)ceil_div(n_rows, 8), 256, 0, (cudaStream_t)stream>>>(
+        A, ld, n_rows, 3 * n_col_nodes, alpha, accumulate, out);
+    return launch_status("rowsum3_kernel");
+}
+
+int mbem_add_block_diagonal(double* A, int64_t ld, const double* D, int64_t n_c, int K, const double* shape,
+                            void* stream) {
+    MBEM_REQUIRE(K == 1 || K == 3 || K == 6, MBEM_ERR_ARG, "K must be 1, 3 or 6 (got %d)", K);
+    MBEM_REQUIRE(n_c >= 0 && n_c % K == 0, MBEM_ERR_ARG, "n_c must be a multiple of K");
+    MBEM_REQUIRE(shape != nullptr, MBEM_ERR_ARG, "shape is NULL");
+    if (n_c == 0) return MBEM_OK;
+    ShapeK sk;
+    memset(&sk, 0, sizeof(sk));
+    for (int i = 0; i < K * K; i++) sk.w[i] = shape[i];
+    add_block_diag_kernel<<<(unsigned)ceil_div(n_c, 128), 128, 0, (cudaStream_t)stream>>>(A, ld, D, n_c, K, sk);
+    return launch_status("add_block_diag_kernel");
+}
+
+int mbem_dgemv(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols, const double* x, double alpha,
+               double beta, double* y, void* stream) {
+    MBEM_REQUIRE(n_rows >= 0 && n_cols >= 0 && ld >= n_cols, MBEM_ERR_ARG, "bad dgemv shape");
+    return dgemv(A, ld, n_rows, n_cols, x, alpha, beta, y, (cudaStream_t)stream);
+}
+
+int mbem_dgemm_multi(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols, const double* X, int64_t k,
+                     double* Y, void* stream) {
+    MBEM_REQUIRE(n_rows >= 0 && n_cols >= 0 && ld >= n_cols && k >= 0, MBEM_ERR_ARG, "bad dgemm shape");
+    for (int64_t k0 = 0; k0 < k; k0 += 64) {
+        const int kc = (int)lmin(64, k - k0);
+        dgemm_multi_kernel<<<(unsigned)ceil_div(n_rows, 8), 256, 0, (cudaStream_t)stream>>>(A, ld, n_rows, n_cols,
+                                                                                           X, k, k0, kc, Y);
+        count_launches(1);
+    }
+    return launch_status("dgemm_multi_kernel", 0);
+}
+
+int mbem_project_translation(const double* v_in, double* v_out, int64_t n, const int64_t* u_ranges,
+                             int n_u_ranges, double* work, void* stream) {
+    (void)work;
+    URanges ur;
+    int e = make_ranges(u_ranges, n_u_ranges, ur);
+    if (e) return e;
+    project_kernel<<<1, PROJ_THREADS, 0, (cudaStream_t)stream>>>(v_in, v_out, n, ur);
+    return launch_status("project_kernel");
+}
+
+size_t mbem_fgmres_workspace_size(int64_t n, int restart) {
+    return fgmres_layout(n, restart, nullptr, nullptr);
+}
+
+int mbem_fgmres_dense(const double* A, int64_t ld, int64_t n, const double* b, double* x,
+                      const mbem_fgmres_params* prm, void* work, size_t work_bytes, mbem_fgmres_report* rep,
+                      void* stream) {
+    MBEM_REQUIRE(prm != nullptr && rep != nullptr, MBEM_ERR_ARG, "params/report is NULL");
+    MBEM_REQUIRE(n > 0 && ld >= n, MBEM_ERR_ARG, "bad system size");
+    const int m = prm->restart;
+    MBEM_REQUIRE(m >= 1 && m <= 1000, MBEM_ERR_ARG, "restart must be in [1, 1000]");
+    MBEM_REQUIRE(prm->precond == 0, MBEM_ERR_UNSUPPORTED, "preconditioner %d not available here", prm->precond);
+    const size_t need = fgmres_layout(n, m, nullptr, nullptr);
+    MBEM_REQUIRE(work != nullptr && work_bytes >= need, MBEM_ERR_SIZE, "workspace %zu < %zu bytes", work_bytes,
+                 need);
+    Fgmres F;
+    F.A = A; F.ld = ld; F.n = n; F.st = (cudaStream_t)stream;
+    F.nb = ceil_div(n, KV_COLS);
+    fgmres_layout(n, m, (char*)work, &F.W);
+    int e = make_ranges(prm->u_ranges, prm->n_u_ranges, F.ur);
+    if (e) return e;
+    F.deflate = prm->n_u_ranges > 0;
+    FgmresWork& W = F.W;
+    cudaStream_t st = F.st;
+
+    memset(rep, 0, sizeof(*rep));
+    std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m, 0.0), sn(m, 0.0), g(m + 1, 0.0), hcol(m + 2);
+    double bnorm2 = 0.0, tmp;
+
+    // b' = P b (kept in W.r until the first residual overwrites it)
+    if ((e = F.proj(b, W.r))) return e;
+    if ((e = F.norm2(W.r, W.scal))) return e;
+    cudaMemcpyAsync(&bnorm2, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
+    const double bnorm = sqrt(bnorm2);
+    double* bproj = W.w;   // hold P b in w across cycles would clash; recompute each cycle instead
+    (void)bproj;
+    if (bnorm == 0.0) {
+        cudaMemsetAsync(x, 0, n * sizeof(double), st);
+        rep->converged = 1;
+        return launch_status("fgmres zero rhs", 0);
+    }
+    const int maxiter = prm->maxiter;
+    int total = 0, restarts = 0;
+    double best = INFINITY;
+    int best_at = 0;
+    bool stagnated = false;
+    double arnoldi = 1.0;
+    while (total < maxiter && !stagnated) {
+        // r = P b - P A P x
+        if ((e = F.op(x, W.w))) return e;
+        if ((e = F.proj(b, W.r))) return e;
+        axpby_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.w, n, -1.0, 1.0);
+        count_launches(1);
+        if ((e = F.norm2(W.r, W.scal))) return e;
+        cudaMemcpyAsync(&tmp, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
+        const double beta = sqrt(tmp);
+        arnoldi = beta / bnorm;
+        if (arnoldi < prm->rtol) break;
+        const int mm = min(m, maxiter - total);
+        std::fill(H.begin(), H.end(), 0.0);
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        scale_by_rnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.V, n, W.scal);
+        count_launches(1);
+        int jdone = 0;
+        for (int j = 0; j < mm; j++) {
+            double* vj = W.V + (int64_t)j * n;
+            double* vn = W.V + (int64_t)(j + 1) * n;
+            if ((e = F.op(vj, W.w))) return e;                  // w = P A P v_j (no preconditioner)
+            if ((e = F.multidot(W.V, j + 1, W.w, W.h, 0))) return e;
+            if ((e = F.multiaxpy(W.w, W.V, j + 1, W.h, -1.0))) return e;
+            if ((e = F.multidot(W.V, j + 1, W.w, W.h2, 0))) return e;
+            if ((e = F.multiaxpy(W.w, W.V, j + 1, W.h2, -1.0))) return e;
+            if ((e = F.norm2(W.w, W.h + (j + 1)))) return e;
+            scale_by_rnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.w, vn, n, W.h + (j + 1));
+            count_launches(1);
+            cudaMemcpyAsync(hcol.data(), W.h, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, st);
+            std::vector<double> h2col(j + 1);
+            cudaMemcpyAsync(h2col.data(), W.h2, (j + 1) * sizeof(double), cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
+            for (int i = 0; i <= j; i++) H[(size_t)i * m + j] = hcol[i] + h2col[i];
+            H[(size_t)(j + 1) * m + j] = sqrt(hcol[j + 1]);
+            // apply accumulated Givens rotations, then form a new one (solver.py:188-205)
+            for (int i = 0; i < j; i++) {
+                const double hi = H[(size_t)i * m + j], hi1 = H[(size_t)(i + 1) * m + j];
+                H[(size_t)i * m + j] = cs[i] * hi + sn[i] * hi1;
+                H[(size_t)(i + 1) * m + j] = -sn[i] * hi + cs[i] * hi1;
+            }
+            const double hjj = H[(size_t)j * m + j], hj1 = H[(size_t)(j + 1) * m + j];
+            const double den = sqrt(hjj * hjj + hj1 * hj1);
+            if (den == 0.0) {
+                // exact breakdown with a zero pivot: drop the column
+                jdone = j;
+                break;
+            }
+            cs[j] = fabs(hjj) > 0 ? fabs(hjj) / den : 0.0;
+            sn[j] = fabs(hjj) > 0 ? (hjj / fabs(hjj)) * hj1 / den : 1.0;
+            H[(size_t)j * m + j] = cs[j] * hjj + sn[j] * hj1;
+            H[(size_t)(j + 1) * m + j] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            total++;
+            jdone = j + 1;
+            arnoldi = fabs(g[j + 1]) / bnorm;
+            if (rep->history && total <= maxiter) rep->history[total - 1] = arnoldi;
+            if (arnoldi < best / prm->stagnation_factor) {
+                best = arnoldi;
+                best_at = total;
+            } else if (total - best_at >= prm->stagnation_window) {
+                stagnated = true;
+                break;
+            }
+            if (arnoldi < prm->rtol || total >= maxiter) break;
+        }
+        if (jdone > 0) {
+            // back substitution (solver.py:503-510), then x += V[:j]^T y
+            std::vector<double> y(jdone, 0.0);
+            for (int i = jdone - 1; i >= 0; i--) {
+                double s = g[i];
+                for (int q = i + 1; q < jdone; q++) s -= H[(size_t)i * m + q] * y[q];
+                y[i] = s / H[(size_t)i * m + i];
+            }
+            cudaMemcpyAsync(W.y, y.data(), jdone * sizeof(double), cudaMemcpyHostToDevice, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
+            if ((e = F.multiaxpy(x, W.V, jdone, W.y, 1.0))) return e;
+        }
+        restarts++;
+        if (stagnated) break;
+    }
+    // true residual (solver.py:234) and the zero-mean representative P x
+    if ((e = F.op(x, W.w))) return e;
+    if ((e = F.proj(b, W.r))) return e;
+    axpby_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.w, n, -1.0, 1.0);
+        count_launches(1);
+    if ((e = F.norm2(W.r, W.scal))) return e;
+    if ((e = F.proj(x, x))) return e;
+    cudaMemcpyAsync(&tmp, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
+    rep->true_relres = sqrt(tmp) / bnorm;
+    rep->arnoldi_relres = arnoldi;
+    rep->iterations = total;
+    rep->restarts = restarts - 1 < 0 ? 0 : restarts - 1;
+    rep->converged = rep->true_relres < prm->rtol;
+    rep->stagnated = stagnated && !rep->converged;
+    return MBEM_OK;
+}
+
+}  // extern "C"

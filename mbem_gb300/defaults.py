@@ -1,0 +1,48 @@
+"""Constants of the dense hot path, one place.
+
+Values that the reference fixes are mirrored from its ``src/mbem/defaults.py``
+(line numbers in the comments) so that a result here is comparable with the
+reference's at the same settings; GPU-only settings follow.
+"""
+
+# ---- solver (defaults.py:10-17) ----
+SOLUTION_RTOL = 1e-6
+GMRES_RTOL = 1e-8
+GMRES_RESTART = 200
+GMRES_MAXITER = 600
+GMRES_STAGNATION_WINDOW = 100
+GMRES_STAGNATION_FACTOR = 10.0
+COND_WARN_THRESHOLD = 1e10            # defaults.py:118
+
+# ---- eps (defaults.py:798-808) ----
+EPS_OVER_H = 0.1
+FAULT_EPS_OVER_H = 0.07
+HALF_JUMP_MAX_EPS_OVER_H = 0.5
+
+# ---- readout (defaults.py:846) ----
+EIGEN_NEAR_RADIUS_EPS = 20.0
+NEAR_BOUNDARY_H_RATIO = 0.5
+
+# ---- nodal kernels (defaults.py:916-932) ----
+NODAL_D_STAR = 10.0
+NODAL_FAR_GAUSS_N = 12
+NODAL_FAR_GAUSS_N_DISTANT = 8
+NODAL_D_STAR_DISTANT = 40.0
+NODAL_SERIES_U_OVER_RHO = 2.0
+NODAL_SERIES_TERMS = 32
+NODAL_SMALL_U_OVER_RHO = 0.5
+NODAL_MIN_HEIGHT_OVER_L = 1e-3
+
+# ---- layout (defaults.py:957-981) ----
+COLLOCATION_SHRINK_BY_ORDER = {0: 0.0, 1: 0.5, 2: 0.5}
+COLLOCATION_FAULT_CLEARANCE_EPS = 1.0
+FRAME_FLAT_TOL = 1e-12
+MIN_TRIANGLE_HEIGHT_OVER_L = 1e-6
+TRACTION_VALUE_NORMAL_TOL = 1e-12
+
+# ---- block-Jacobi preconditioner (defaults.py:712) ----
+PRECOND_BJ_CHUNK_DOF = 9000
+
+# ---- GPU mixed-precision path ----
+MIXED_BLOCK = 64                      # BF16 scale block (rows x columns)
+MIXED_NEAR_RADIUS_FACTOR = 3.0        # near field: centroid distance < 3 max(eps, h)

@@ -1,0 +1,221 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Run in a container that holds the reference sources (read-only) at
+``/root/reference``; the GPU tests never run this script, they only read the
+``.npz`` files it writes. numba is absent here, so a test-only stand-in
+(``_numba_stub``: identity ``njit``, ``prange = range``) is put first on
+``sys.path``; the reference's kernels then run as plain Python with the same
+arithmetic.
+
+    python tests/golden/make_golden.py p0_pairs cube_small c1_rows
+
+Every fixture stores its inputs next to the reference's outputs, so the
+tests feed the identical arrays to the CUDA path and to the C oracle.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SRC = "/root/reference/src"
+sys.dont_write_bytecode = True
+sys.path[:0] = [os.path.join(HERE, "_numba_stub"), REF_SRC]
+
+
+def _ref():
+    import mbem.kernels.tri_kernels as tk
+    import mbem.kernels.basis as kb
+    return tk, kb
+
+
+# ---------------------------------------------------------------------------
+# P0 pair kernels on scattered geometry with edge cases
+# ---------------------------------------------------------------------------
+
+def pair_geometry(seed: int = 1234):
+    """Scattered sources and observers, with the cases the reference guards:
+    a degenerate (collinear) triangle, a needle, a tiny and a large
+    triangle, reversed source normals, observers on a vertex, on an edge, at
+    a centroid, coplanar outside, on an edge's extension, far away and just
+    above a centroid."""
+    rng = np.random.default_rng(seed)
+    tv = rng.normal(size=(16, 3, 3))
+    needle = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.5, 2e-3, 0.0]]) + 0.3
+    tiny = rng.normal(size=(3, 3)) * 1e-3 + np.array([0.2, -0.1, 0.4])
+    large = rng.normal(size=(3, 3)) * 10.0
+    degen = np.array([[0.0, 0.0, 0.0], [1.0, 1.0, 1.0], [2.0, 2.0, 2.0]])
+    tv = np.concatenate([tv, needle[None], tiny[None], large[None], degen[None]])
+    Ns = tv.shape[0]
+    cr = np.cross(tv[:, 1] - tv[:, 0], tv[:, 2] - tv[:, 0])
+    nrm = np.linalg.norm(cr, axis=1)
+    normals = np.where(nrm[:, None] > 0, cr / np.where(nrm > 0, nrm, 1.0)[:, None],
+                       np.array([0.0, 0.0, 1.0]))
+    normals[[2, 7, 11]] *= -1.0                      # reversed normals
+    eps = rng.uniform(0.05, 0.3, Ns)
+    x = rng.normal(size=(24, 3)) * 1.5
+    special = [
+        tv[0, 0],                                    # on a vertex
+        0.5 * (tv[1, 0] + tv[1, 1]),                 # on an edge
+        tv[2].mean(axis=0),                          # at a centroid
+        tv[3, 0] + 2.0 * (tv[3, 1] - tv[3, 0]) + 1.5 * (tv[3, 2] - tv[3, 0]),  # coplanar outside
+        tv[4, 0] + 3.0 * (tv[4, 1] - tv[4, 0]),      # on an edge's line, outside
+        np.array([50.0, -30.0, 20.0]),               # far
+        tv[5].mean(axis=0) + 1e-9 * normals[5],      # just above a centroid
+    ]
+    x = np.concatenate([x, np.array(special)])
+    density = rng.normal(size=(Ns, 3))
+    density[6] = 0.0
+    density[9] = 0.0
+    density[10, 1] = 0.0
+    return (np.ascontiguousarray(x), np.ascontiguousarray(tv),
+            np.ascontiguousarray(normals), np.ascontiguousarray(eps),
+            np.ascontiguousarray(density))
+
+
+MATERIALS = np.array([[1.0, 1.0], [1.3, 1.95]])      # nu = 0.25 and nu = 0.30
+
+
+def make_p0_pairs(path):
+    tk, kb = _ref()
+    x, tv, n, eps, dens = pair_geometry()
+    out = dict(x_field=x, tri_verts=tv, normals=n, eps=eps, density=dens,
+               materials=MATERIALS)
+    t0 = time.time()
+    out["t_basis"] = tk.t_basis_matrices(x, tv, n, eps)
+    out["u_basis"] = tk.u_basis_matrices(x, tv, eps)
+    for m, (mu, lam) in enumerate(MATERIALS):
+        c = kb.t_coeffs(mu, lam)
+        g = kb.u_coeffs(mu, lam)
+        out[f"t_coeffs_{m}"] = c
+        out[f"u_coeffs_{m}"] = g
+        out[f"t_matrix_{m}"] = tk.t_matrix_direct(x, tv, n, eps, *c)
+        out[f"u_matrix_{m}"] = tk.u_matrix_direct(x, tv, eps, *g)
+        out[f"t_disp_{m}"] = tk.t_disp_contract(x, tv, n, eps, dens, *c)
+        out[f"u_disp_{m}"] = tk.u_disp_contract(x, tv, eps, dens, *g)
+        out[f"dd_stress_{m}"] = tk.dd_stress_contract(x, tv, n, eps, dens, mu, lam)
+        out[f"kelvin_stress_{m}"] = tk.kelvin_stress_contract(x, tv, eps, dens, mu, lam)
+        out[f"eigenstress_{m}"] = tk.eigenstress_contract(x, tv, n, eps, dens, mu, lam)
+    print(f"p0_pairs: {time.time() - t0:.1f} s")
+    np.savez_compressed(path, **out)
+
+
+# ---------------------------------------------------------------------------
+# Whole dense systems: cube + fault through the reference's own backend
+# ---------------------------------------------------------------------------
+
+def reference_cube_model(n_face: int, n_fault: int, mu: float, lam: float,
+                         side: float = 4.0):
+    """The traction-free cube with an embedded vertical fault, built with the
+    reference's own mesh generators and model API."""
+    import local_box_mesh as lbm
+    from mollified_bem import ElasticMaterial
+    from mbem.model import BCType, Patch, Region, RegionModel
+
+    a = side / 2.0
+    faces = [
+        lbm.make_rectangular_patch((-a, a), (-a, a), a, n_face, n_face, normal_up=True),
+        lbm.make_rectangular_patch((-a, a), (-a, a), -a, n_face, n_face, normal_up=False),
+        lbm.make_vertical_panel("x", a, (-a, a), (-a, a), n_face, n_face, +1),
+        lbm.make_vertical_panel("x", -a, (-a, a), (-a, a), n_face, n_face, -1),
+        lbm.make_vertical_panel("y", a, (-a, a), (-a, a), n_face, n_face, +1),
+        lbm.make_vertical_panel("y", -a, (-a, a), (-a, a), n_face, n_face, -1),
+    ]
+    cube = lbm._concatenate_meshes(faces)
+    fmesh, _, _ = lbm.make_vertical_fault_xy(1.0, (-1.0, 0.0), n_fault, n_fault,
+                                             strike_azimuth_deg=90.0)
+    fmesh.vertices = fmesh.vertices + np.array([0.0, 0.0, 0.5])
+    mat = ElasticMaterial(mu=mu, lam=lam)
+    cube_p = Patch("cube", cube, BCType.FREE_TRACTION)
+    fault_p = Patch("fault", fmesh, BCType.FAULT, value=np.array([1.0, 0.0, 0.0]))
+    region = Region("body", mat, [cube_p], np.zeros(3), faults=[fault_p])
+    return RegionModel([region]), cube, fmesh
+
+
+def _system_fixture(n_face, n_fault, mu, lam, mode, points, rows=None,
+                    fgmres_rtols=()):
+    from mbem.backends.dense import AssembledDense, translation_basis
+    from mbem.evaluate import evaluate_stress
+    from mbem.model.equations import generate_system
+
+    model, cube, fmesh = reference_cube_model(n_face, n_fault, mu, lam)
+    eps = (4.0 / n_face) / 2.0
+    t0 = time.time()
+    system = generate_system(model)
+    asm = AssembledDense(system, eps, mode, jump="calibrated", deflate=True)
+    t1 = time.time()
+    sol = asm.solve()
+    t2 = time.time()
+    out = dict(cube_vertices=cube.vertices, cube_triangles=cube.triangles,
+               fault_vertices=fmesh.vertices, fault_triangles=fmesh.triangles,
+               mu=mu, lam=lam, eps=eps, n_face=n_face, n_fault=n_fault,
+               b=asm.b, x=sol["u:cube"].ravel(), cond=asm.report.cond_estimate,
+               calib=next(iter(asm.calib.values())), assembly_s=t1 - t0,
+               lu_s=t2 - t1)
+    if rows is None:
+        out["A"] = asm.A
+    else:
+        out["A_rows"] = np.ascontiguousarray(asm.A[rows])
+        out["rows"] = np.asarray(rows, np.int64)
+    # deflated FGMRES, the pairing the GPU backend uses
+    if fgmres_rtols:
+        from mbem.la.solver import fgmres
+        Z = translation_basis(asm.layout)
+
+        def proj(v):
+            return v - Z @ (Z.T @ v)
+
+        its = []
+        for rtol in fgmres_rtols:
+            xg, rep = fgmres(lambda v: proj(asm.A @ proj(v)), proj(asm.b),
+                             rtol=rtol, restart=50, maxiter=600)
+            its.append([rtol, rep.iterations, rep.true_relres,
+                        float(np.linalg.norm(proj(xg) - out["x"]) / np.linalg.norm(out["x"]))])
+        out["fgmres"] = np.array(its)
+    t3 = time.time()
+    sig, eig = evaluate_stress(model, "body", sol, points, eps,
+                               subtract_anelastic=True, parts=True)
+    out.update(points=points, stress=sig, stress_eigen=eig, readout_s=time.time() - t3)
+    print(f"system n={n_face}: assembly {t1 - t0:.1f} s, LU {t2 - t1:.1f} s, "
+          f"readout {time.time() - t3:.1f} s")
+    return out
+
+
+def make_cube_small(path):
+    rng = np.random.default_rng(7)
+    pts = rng.uniform(-1.5, 1.5, size=(10, 3))
+    pts = np.concatenate([pts, [[0.1, 0.05, 0.2], [0.0, 0.0, 0.0], [0.45, -0.02, -0.3]]])
+    out = _system_fixture(3, 2, 1.0, 1.0, "direct", pts)
+    out2 = _system_fixture(2, 2, 1.3, 1.95, "direct", pts[:6])
+    out.update({f"nu30_{k}": v for k, v in out2.items()})
+    np.savez_compressed(path, **out)
+
+
+def make_c1_rows(path):
+    """Config-1 cube (12x12 per face, fault 8x8, eps = h/2): sampled rows of
+    A, the full b, the deflated LU solution, FGMRES(50) iteration counts and a
+    readout subset of the 64x64 grid on y = 0.1."""
+    g = (np.arange(64) + 0.5) / 64.0 * 4.0 - 2.0
+    X, Zc = np.meshgrid(g, g, indexing="xy")
+    grid = np.column_stack([X.ravel(), np.full(X.size, 0.1), Zc.ravel()])
+    pick = np.random.default_rng(11).choice(grid.shape[0], 16, replace=False)
+    rng = np.random.default_rng(3)
+    rows = np.unique(np.concatenate([[0, 1, 2, 2591, 2592, 5181, 5182, 5183],
+                                     rng.choice(5184, 16, replace=False)]))
+    out = _system_fixture(12, 8, 1.0, 1.0, "legacy", grid[pick], rows=rows,
+                          fgmres_rtols=(1e-8, 1e-10))
+    out["grid_index"] = pick
+    np.savez_compressed(path, **out)
+
+
+CASES = {"p0_pairs": make_p0_pairs, "cube_small": make_cube_small,
+         "c1_rows": make_c1_rows}
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        CASES[name](os.path.join(HERE, f"{name}.npz"))
