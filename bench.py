@@ -175,7 +175,8 @@ def run_ours(args, rank, ws):
     model, eps = cube_fault_model(cfg["n_face"], cfg["n_fault"])
     system = generate_system(model)
     n = system.layout.n_unknowns
-    backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART)
+    backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART,
+                           precision=args.precision)
     arrays = {}     # device-resident mesh arrays, filled by the first assembly
 
     def step(timer=None):
@@ -183,6 +184,7 @@ def run_ours(args, rank, ws):
         x = asm.solve_device()
         rep = asm.report
         asm.A = None
+        asm.op = None
         return x, rep
 
     for _ in range(args.warmup):
@@ -262,7 +264,7 @@ def run_ours(args, rank, ws):
         "dtype": "f64",
         "data": "synthetic (seeded mesh generators; no dataset)",
         "config": {"workload": args.workload, "n_face": cfg["n_face"], "n_fault": cfg["n_fault"],
-                   "unknowns": n, "precision": "fp64", "solver": f"deflated FGMRES({RESTART})",
+                   "unknowns": n, "precision": args.precision, "solver": f"deflated FGMRES({RESTART})",
                    "rtol": RTOL, "parallelism": "replicas" if ws > 1 else "single",
                    "l2": "inputs larger than L2 (A = %.1f GB FP64)" % (8.0 * n * n / 1e9)},
         "iterations": reps[-1].iterations,
@@ -382,6 +384,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

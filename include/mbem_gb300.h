@@ -131,6 +131,59 @@ int mbem_dgemv(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols, cons
 int mbem_dgemm_multi(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols, const double* X,
                      int64_t k, double* Y, void* stream);
 
+/* ---- mixed-precision operator: A = A_far (FP32 dense) + A_near (FP64
+ * 3x3 blocks in CSR by field point). It replaces the FP64 AssembledDense.A
+ * of backends/dense.py:480-528 in the mixed mode; no reference counterpart
+ * beyond that role. ------------------------------------------------- */
+typedef struct {
+    int64_t row0, col0;      /* offsets of this block in the system's rows / columns */
+    int64_t n_field;         /* field points (row blocks of 3 rows) */
+    const int64_t* rowptr;   /* (n_field + 1) device */
+    const int64_t* cols;     /* (nnz) source index of each near block, device */
+    const double* vals;      /* (nnz, 3, 3) device */
+} mbem_near_blocks;
+
+typedef struct {
+    int64_t n_rows, n_cols;  /* square (the unknowns) for a solve; any shape for a product */
+    const float* A32;        /* (n_rows, n_cols) FP32 far field at leading dimension ld32, device */
+    int64_t ld32;
+    int n_near;
+    const mbem_near_blocks* near;  /* HOST array of n_near descriptors */
+} mbem_mixed_operator;
+
+/* FP32 far-field block (kernel 0 = T with 6 coeffs, 1 = U with 3) of
+ * alpha * M into out (3Nf, 3Ns) at ld_out; near pairs (centroid distance
+ * below near_factor * max(eps, mean edge), or below 1.5 longest edge) are
+ * written as zeros. */
+int mbem_far_matrix(int kernel, const double* x_field, int64_t n_field, const double* tri_verts,
+                    const double* normals, const double* eps, int64_t n_src, const double* coeffs,
+                    double near_factor, double alpha, float* out, int64_t ld_out, void* stream);
+/* Near list, pass 1: rowptr (n_field+1) device; nnz returned on the host
+ * (the call synchronises `stream`). work >= mbem_near_list_workspace_size. */
+size_t mbem_near_list_workspace_size(int64_t n_field);
+int mbem_near_count(const double* x_field, int64_t n_field, const double* tri_verts, const double* eps,
+                    int64_t n_src, double near_factor, int64_t* rowptr, void* work, size_t work_bytes,
+                    int64_t* nnz_host, void* stream);
+/* Near list, pass 2: source indices in increasing order per field point. */
+int mbem_near_fill(const double* x_field, int64_t n_field, const double* tri_verts, const double* eps,
+                   int64_t n_src, double near_factor, const int64_t* rowptr, int64_t* cols, void* stream);
+/* FP64 closed-form blocks alpha * M for the near list (kernel as above). */
+int mbem_near_eval(int kernel, const double* x_field, int64_t n_field, const double* tri_verts,
+                   const double* normals, const double* eps, const int64_t* rowptr, const int64_t* cols,
+                   int64_t nnz, const double* coeffs, double alpha, double* vals, void* stream);
+/* Calibration row sums of far + near: out (n_rows/3, 3, 3) = sum over
+ * column nodes (far in double-float, near in FP64). */
+int mbem_mixed_rowsum3(const float* A32, int64_t ld, int64_t n_rows, int64_t n_col_nodes,
+                       const int64_t* rowptr, const double* vals, double* out, void* stream);
+/* Adds D (n_field,3,3) to each row's self block; *missing counts rows
+ * without one (device int). */
+int mbem_near_add_diagonal(const int64_t* rowptr, const int64_t* cols, double* vals, int64_t n_field,
+                           const double* D, int* missing, void* stream);
+/* y = A x for the mixed operator (far in double-float, near in FP64);
+ * y (n_rows) is overwritten. work >= 2 n_cols floats + 64 bytes. */
+int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, void* work,
+                      size_t work_bytes, void* stream);
+
 /* ---- deflated FGMRES on a dense operator (la/solver.py:115-245 fgmres,
  * wired as backends/hmat.py:678-690: P A P y = P b, P = I - Z Z^T with Z
  * the rigid-translation basis of backends/dense.py:190-208). ---------- */
@@ -156,8 +209,15 @@ typedef struct {
     double* history;        /* optional HOST array of maxiter doubles, filled if non-NULL */
 } mbem_fgmres_report;
 
-/* Bytes of device workspace mbem_fgmres_dense needs for n unknowns. */
+/* Bytes of device workspace mbem_fgmres_dense / mbem_fgmres_mixed need for
+ * n unknowns. */
 size_t mbem_fgmres_workspace_size(int64_t n, int restart);
+
+/* As mbem_fgmres_dense for the mixed operator: the residuals and the true
+ * residual are those of the mixed operator, evaluated to ~1e-14. */
+int mbem_fgmres_mixed(const mbem_mixed_operator* op, const double* b, double* x,
+                      const mbem_fgmres_params* params, void* work, size_t work_bytes,
+                      mbem_fgmres_report* report, void* stream);
 
 /* Solve A x = b (A FP64 (n,n) at leading dimension ld; b, x device (n,)).
  * x holds the initial guess on entry (zeros for none) and the solution on

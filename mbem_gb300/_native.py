@@ -48,6 +48,16 @@ class FgmresReport(Structure):
                 ("history", POINTER(c_double))]
 
 
+class NearBlocks(Structure):
+    _fields_ = [("row0", c_int64), ("col0", c_int64), ("n_field", c_int64), ("rowptr", c_void_p),
+                ("cols", c_void_p), ("vals", c_void_p)]
+
+
+class MixedOperator(Structure):
+    _fields_ = [("n_rows", c_int64), ("n_cols", c_int64), ("A32", c_void_p), ("ld32", c_int64),
+                ("n_near", c_int), ("near", POINTER(NearBlocks))]
+
+
 _P = c_void_p
 _I = c_int64
 _D = c_double
@@ -76,6 +86,16 @@ _SIGNATURES = {
     "mbem_fgmres_workspace_size": (c_size_t, [_I, c_int]),
     "mbem_fgmres_dense": (c_int, [_P, _I, _I, _P, _P, POINTER(FgmresParams), _P, c_size_t,
                                   POINTER(FgmresReport), _P]),
+    "mbem_fgmres_mixed": (c_int, [POINTER(MixedOperator), _P, _P, POINTER(FgmresParams), _P, c_size_t,
+                                  POINTER(FgmresReport), _P]),
+    "mbem_far_matrix": (c_int, [c_int, _P, _I, _P, _P, _P, _I, _P, _D, _D, _P, _I, _P]),
+    "mbem_near_list_workspace_size": (c_size_t, [_I]),
+    "mbem_near_count": (c_int, [_P, _I, _P, _P, _I, _D, _P, _P, c_size_t, POINTER(c_int64), _P]),
+    "mbem_near_fill": (c_int, [_P, _I, _P, _P, _I, _D, _P, _P, _P]),
+    "mbem_near_eval": (c_int, [c_int, _P, _I, _P, _P, _P, _P, _P, _I, _P, _D, _P, _P]),
+    "mbem_mixed_rowsum3": (c_int, [_P, _I, _I, _I, _P, _P, _P, _P]),
+    "mbem_near_add_diagonal": (c_int, [_P, _P, _P, _I, _P, _P, _P]),
+    "mbem_mixed_matvec": (c_int, [POINTER(MixedOperator), _P, _P, _P, c_size_t, _P]),
 }
 
 _lib = None

@@ -28,7 +28,7 @@ from .._device import as_cuda, ptr, require_cuda, stream_handle
 from ..kernels import KERNEL_GT, KERNEL_HT, KERNEL_T, KERNEL_U
 from ..kernels import basis as kb
 from ..kernels import tri_nodal as tn
-from ..la.solver import SolveReport, fgmres_dense
+from ..la.solver import SolveReport, fgmres_dense, fgmres_mixed
 from ..model.core import BCType
 from ..model.equations import BlockSystem, calibrated_diagonal, term_diagonal
 
@@ -41,19 +41,29 @@ class DenseBackend:
 
     def __init__(self, mode: str = "direct", jump: str = "calibrated", deflate: bool = False,
                  lu: str | None = None, rtol: float = 1e-10, restart: int = 50,
-                 maxiter: int = defaults.GMRES_MAXITER):
+                 maxiter: int = defaults.GMRES_MAXITER, precision: str = "fp64",
+                 near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR):
+        """``precision="fp64"``: every entry by the FP64 closed form, the
+        reference's operator. ``"mixed"``: pairs beyond near_factor *
+        max(eps, h) of the source by FP32 quadrature (stored FP32), the near
+        pairs by the FP64 closed form (stored as 3x3 blocks); the solve's
+        residuals are those of that operator."""
         if mode not in ("direct", "basis", "legacy"):
             raise ValueError(mode)
         if jump not in ("half", "calibrated"):
             raise ValueError(jump)
         if lu is not None:
             raise ValueError("the GPU dense backend solves by FGMRES; lu= is not used")
+        if precision not in ("fp64", "mixed"):
+            raise ValueError(f"precision must be 'fp64' or 'mixed' (got {precision!r})")
         self.mode = "direct"
         self.jump = jump
         self.deflate = deflate
         self.rtol = rtol
         self.restart = restart
         self.maxiter = maxiter
+        self.precision = precision
+        self.near_factor = near_factor
 
     def assemble(self, system: BlockSystem, eps, arrays: dict | None = None,
                  timer: list | None = None) -> "AssembledDense":
@@ -62,7 +72,8 @@ class DenseBackend:
         when it is already filled). ``timer``: an optional list that receives
         (start, end) CUDA events around every kernel-block launch."""
         return AssembledDense(system, eps, jump=self.jump, deflate=self.deflate, rtol=self.rtol,
-                              restart=self.restart, maxiter=self.maxiter, arrays=arrays, timer=timer)
+                              restart=self.restart, maxiter=self.maxiter, arrays=arrays, timer=timer,
+                              precision=self.precision, near_factor=self.near_factor)
 
 
 def require_anchor_or_deflate(system: BlockSystem, jump: str, deflate: bool):
@@ -99,13 +110,17 @@ class AssembledDense:
     def __init__(self, system: BlockSystem, eps, mode: str = "direct", jump: str = "calibrated",
                  deflate: bool = False, rtol: float = 1e-10, restart: int = 50,
                  maxiter: int = defaults.GMRES_MAXITER, arrays: dict | None = None,
-                 timer: list | None = None):
+                 timer: list | None = None, precision: str = "fp64",
+                 near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR):
         if jump not in ("half", "calibrated"):
             raise ValueError(jump)
         require_anchor_or_deflate(system, jump, deflate)
         require_cuda()
         self._arrays_in = arrays
         self._timer = timer
+        self.precision = precision
+        self.near_factor = near_factor
+        self.op = None
         self.system = system
         self.layout = system.layout
         self.eps = eps
@@ -168,7 +183,104 @@ class AssembledDense:
                  stream_handle())
         return res.reshape(rows // 3, 3, 3)
 
+    # -- mixed precision: FP32 far field + FP64 near blocks -------------
+    def _mixed_block(self, far_out, q, p, kernel, material, alpha, row0, col0):
+        from ..la.mixed import far_near_block
+        if p.order != 0 or q.order != 0:
+            raise NotImplementedError("the mixed-precision operator is P0 (order 0) only")
+        if kernel not in (KERNEL_T, KERNEL_U):
+            raise NotImplementedError("traction rows are not in the mixed-precision operator")
+        f = self._patch_arrays(q)
+        s = self._patch_arrays(p)
+        if kernel == KERNEL_T:
+            coeffs = kb.t_coeffs(material.mu, material.lam)
+            return far_near_block("T", f["coll"], s["tv"], s["normals"], s["eps"], coeffs, alpha, far_out,
+                                  row0, col0, self.near_factor, self._timer)
+        coeffs = kb.u_coeffs(material.mu, material.lam)
+        return far_near_block("U", f["coll"], s["tv"], s["normals"], s["eps"], coeffs, alpha, far_out, row0,
+                              col0, self.near_factor, self._timer)
+
+    def _build_mixed(self):
+        from ..la.mixed import MixedOperator
+        dev = require_cuda()
+        n = self.layout.n_unknowns
+        self._arrays = self._arrays_in if self._arrays_in is not None else {}
+        counts = {}
+        for t in self.system.terms:
+            counts[(t.row.offset, t.col.offset)] = counts.get((t.row.offset, t.col.offset), 0) + 1
+        if any(v > 1 for v in counts.values()):
+            raise NotImplementedError("mixed precision: two terms on one block")
+        covered = sum(t.row.size * t.col.size for t in self.system.terms)
+        A32 = (torch.empty if covered == n * n else torch.zeros)((n, n), dtype=torch.float32, device=dev)
+        op = MixedOperator(A32, [])
+        placed = {}
+        for t in self.system.terms:
+            mat = self.materials[t.region.name]
+            view = A32[t.row.offset:t.row.stop, t.col.offset:t.col.stop]
+            nl = self._mixed_block(view, t.field_patch, t.source_patch, t.kernel, mat, t.scale, t.row.offset,
+                                   t.col.offset)
+            op.near.append(nl)
+            placed[(id(t.field_patch), id(t.source_patch), t.kernel, id(mat))] = (t, nl)
+
+        temp = {}
+
+        def block(q, p, kernel, region):
+            mat = self.materials[region.name]
+            key = (id(q), id(p), kernel, id(mat))
+            if key in placed:
+                t, nl = placed[key]
+                return MixedOperator(A32[t.row.offset:t.row.stop, t.col.offset:t.col.stop], [
+                    type(nl)(0, 0, nl.n_field, nl.rowptr, nl.cols, nl.vals)]), t.scale
+            if key not in temp:
+                far = torch.empty((3 * q.n_dofs, 3 * p.n_nodes), dtype=torch.float32, device=dev)
+                nl = self._mixed_block(far, q, p, kernel, mat, 1.0, 0, 0)
+                temp[key] = (MixedOperator(far, [nl]), 1.0)
+            return temp[key]
+
+        self.calib = None
+        if self.jump == "calibrated":
+            def rowsum(region, q, p):
+                bop, scale = block(q, p, KERNEL_T, region)
+                rs = bop.rowsum3(0, bop.A32.shape[0], 0, bop.A32.shape[1], bop.near[0])
+                return rs if scale == 1.0 else rs * (1.0 / scale)
+            self.calib = calibrated_diagonal(self.system, rowsum)
+        missing = torch.zeros(1, dtype=torch.int32, device=dev)
+        for t, nl in zip(self.system.terms, op.near):
+            D = term_diagonal(t, self.calib)
+            if D is None:
+                continue
+            Dd = (as_cuda(np.ascontiguousarray(D)) if not isinstance(D, torch.Tensor) else D.contiguous())
+            nat.call("mbem_near_add_diagonal", ptr(nl.rowptr), ptr(nl.cols), ptr(nl.vals), nl.n_field, ptr(Dd),
+                     ptr(missing), stream_handle())
+        if int(missing.item()) != 0:
+            raise RuntimeError("mixed precision: a collocation row has no self block in its near list")
+        b = torch.zeros(n, dtype=torch.float64, device=dev)
+        for rt in self.system.rhs_terms:
+            bop, _ = block(rt.field_patch, rt.source_patch, rt.kernel, rt.region)
+            dens = as_cuda(np.asarray(rt.vector, float))
+            y = bop.matvec(dens)
+            b[rt.row.offset:rt.row.stop] += rt.scale * y
+        for rv in self.system.rhs_values:
+            b[rv.row.offset:rv.row.stop] += as_cuda(np.asarray(rv.vector, float))
+        for rt in self.system.rhs_terms:
+            if not rt.add_half_of_vector:
+                continue
+            u_c = as_cuda(rt.field_patch.collocation_values(rt.vector)).reshape(-1, 3)
+            bview = b[rt.row.offset:rt.row.stop].view(-1, 3)
+            if self.calib is None:
+                bview += rt.scale_half * u_c
+            else:
+                bview -= torch.einsum("nij,nj->ni", self.calib[(id(rt.region), id(rt.field_patch))], u_c)
+        if self.system.traction_faults():
+            raise NotImplementedError("mixed precision: FAULT_TRACTION rows are not in the mixed operator")
+        self._arrays = None
+        self.op = op
+        self.A = None
+        self.b = b
+
     def _build(self):
+        if self.precision == "mixed":
+            return self._build_mixed()
         dev = require_cuda()
         lay = self.layout
         n = lay.n_unknowns
@@ -274,10 +386,13 @@ class AssembledDense:
                      maxiter: int | None = None, x0=None) -> torch.Tensor:
         """FGMRES on the device; returns the solution vector as a CUDA tensor
         and leaves ``self.report``."""
-        x, rep = fgmres_dense(self.A, self.b, x0=x0, rtol=self.rtol if rtol is None else rtol,
-                              restart=self.restart if restart is None else restart,
-                              maxiter=self.maxiter if maxiter is None else maxiter,
-                              u_ranges=self.u_ranges())
+        kw = dict(x0=x0, rtol=self.rtol if rtol is None else rtol,
+                  restart=self.restart if restart is None else restart,
+                  maxiter=self.maxiter if maxiter is None else maxiter, u_ranges=self.u_ranges())
+        if self.op is not None:
+            x, rep = fgmres_mixed(self.op, self.b, **kw)
+        else:
+            x, rep = fgmres_dense(self.A, self.b, **kw)
         self.report = rep
         if not rep.converged:
             warnings.warn(f"dense GPU solve: {rep}")

@@ -31,6 +31,10 @@ int nodal_contract(int kind, const double* x, int64_t nf, const double* tv, cons
                    double mu, double lam, int order, double alpha, int accumulate, double* out,
                    void* stream);
 
+// y = A x for the mixed operator; xh, xl: n floats each (scratch).
+int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, float* xh, float* xl,
+                 cudaStream_t st);
+
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 __host__ __device__ inline int64_t lmin(int64_t a, int64_t b) { return a < b ? a : b; }
 

@@ -315,6 +315,8 @@ struct FgmresWork {
     double* h2;       // m+2
     double* y;        // m
     double* scal;     // 8
+    float* xh;        // n (mixed operator: split of the matvec input)
+    float* xl;        // n
 };
 
 static size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -337,12 +339,15 @@ static size_t fgmres_layout(int64_t n, int m, char* base, FgmresWork* w) {
     tmp.h2 = take(m + 2);
     tmp.y = take(m + 1);
     tmp.scal = take(8);
+    tmp.xh = reinterpret_cast<float*>(take((n + 1) / 2));
+    tmp.xl = reinterpret_cast<float*>(take((n + 1) / 2));
     if (w) *w = tmp;
     return off;
 }
 
 struct Fgmres {
-    const double* A;
+    const double* A;                      // dense FP64 operator, or
+    const mbem_mixed_operator* mop;       // the mixed operator
     int64_t ld, n;
     URanges ur;
     bool deflate;
@@ -362,7 +367,7 @@ struct Fgmres {
     int op(const double* in, double* out) {
         int e = proj(in, W.t);
         if (e) return e;
-        e = dgemv(A, ld, n, n, W.t, 1.0, 0.0, out, st);
+        e = mop ? mixed_matvec(mop, W.t, out, W.xh, W.xl, st) : dgemv(A, ld, n, n, W.t, 1.0, 0.0, out, st);
         if (e) return e;
         return proj(out, out);
     }
@@ -450,11 +455,32 @@ size_t mbem_fgmres_workspace_size(int64_t n, int restart) {
     return fgmres_layout(n, restart, nullptr, nullptr);
 }
 
+static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mop, int64_t n, const double* b,
+                      double* x, const mbem_fgmres_params* prm, void* work, size_t work_bytes,
+                      mbem_fgmres_report* rep, void* stream);
+
 int mbem_fgmres_dense(const double* A, int64_t ld, int64_t n, const double* b, double* x,
                       const mbem_fgmres_params* prm, void* work, size_t work_bytes, mbem_fgmres_report* rep,
                       void* stream) {
+    MBEM_REQUIRE(A != nullptr && ld >= n, MBEM_ERR_ARG, "bad dense operator");
+    return fgmres_run(A, ld, nullptr, n, b, x, prm, work, work_bytes, rep, stream);
+}
+
+int mbem_fgmres_mixed(const mbem_mixed_operator* op, const double* b, double* x, const mbem_fgmres_params* prm,
+                      void* work, size_t work_bytes, mbem_fgmres_report* rep, void* stream) {
+    MBEM_REQUIRE(op != nullptr && op->A32 != nullptr && op->n_rows == op->n_cols && op->ld32 >= op->n_cols,
+                 MBEM_ERR_ARG, "bad mixed operator (must be square)");
+    MBEM_REQUIRE(op->n_near >= 0 && (op->n_near == 0 || op->near), MBEM_ERR_ARG, "bad near blocks");
+    return fgmres_run(nullptr, 0, op, op->n_rows, b, x, prm, work, work_bytes, rep, stream);
+}
+
+}  // extern "C"
+
+static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mop, int64_t n, const double* b,
+                      double* x, const mbem_fgmres_params* prm, void* work, size_t work_bytes,
+                      mbem_fgmres_report* rep, void* stream) {
     MBEM_REQUIRE(prm != nullptr && rep != nullptr, MBEM_ERR_ARG, "params/report is NULL");
-    MBEM_REQUIRE(n > 0 && ld >= n, MBEM_ERR_ARG, "bad system size");
+    MBEM_REQUIRE(n > 0, MBEM_ERR_ARG, "bad system size");
     const int m = prm->restart;
     MBEM_REQUIRE(m >= 1 && m <= 1000, MBEM_ERR_ARG, "restart must be in [1, 1000]");
     MBEM_REQUIRE(prm->precond == 0, MBEM_ERR_UNSUPPORTED, "preconditioner %d not available here", prm->precond);
@@ -462,7 +488,7 @@ int mbem_fgmres_dense(const double* A, int64_t ld, int64_t n, const double* b, d
     MBEM_REQUIRE(work != nullptr && work_bytes >= need, MBEM_ERR_SIZE, "workspace %zu < %zu bytes", work_bytes,
                  need);
     Fgmres F;
-    F.A = A; F.ld = ld; F.n = n; F.st = (cudaStream_t)stream;
+    F.A = A; F.mop = mop; F.ld = ld; F.n = n; F.st = (cudaStream_t)stream;
     F.nb = ceil_div(n, KV_COLS);
     fgmres_layout(n, m, (char*)work, &F.W);
     int e = make_ranges(prm->u_ranges, prm->n_u_ranges, F.ur);
@@ -471,7 +497,9 @@ int mbem_fgmres_dense(const double* A, int64_t ld, int64_t n, const double* b, d
     FgmresWork& W = F.W;
     cudaStream_t st = F.st;
 
+    double* history = rep->history;
     memset(rep, 0, sizeof(*rep));
+    rep->history = history;
     std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m, 0.0), sn(m, 0.0), g(m + 1, 0.0), hcol(m + 2);
     double bnorm2 = 0.0, tmp;
 
@@ -492,9 +520,13 @@ int mbem_fgmres_dense(const double* A, int64_t ld, int64_t n, const double* b, d
     int total = 0, restarts = 0;
     double best = INFINITY;
     int best_at = 0;
-    bool stagnated = false;
+    bool stagnated = false, breakdown = false;
     double arnoldi = 1.0;
-    while (total < maxiter && !stagnated) {
+    // every cycle either adds an iteration or ends the solve; the cap makes
+    // termination independent of that argument
+    const int max_cycles = maxiter + 2;
+    int cycles = 0;
+    while (total < maxiter && !stagnated && !breakdown && cycles++ < max_cycles) {
         // r = P b - P A P x
         if ((e = F.op(x, W.w))) return e;
         if ((e = F.proj(b, W.r))) return e;
@@ -539,8 +571,11 @@ int mbem_fgmres_dense(const double* A, int64_t ld, int64_t n, const double* b, d
             const double hjj = H[(size_t)j * m + j], hj1 = H[(size_t)(j + 1) * m + j];
             const double den = sqrt(hjj * hjj + hj1 * hj1);
             if (den == 0.0) {
-                // exact breakdown with a zero pivot: drop the column
+                // exact breakdown with a zero pivot: the Krylov space is
+                // invariant and this column adds nothing; finish with the
+                // iterate of the columns before it
                 jdone = j;
+                breakdown = true;
                 break;
             }
             cs[j] = fabs(hjj) > 0 ? fabs(hjj) / den : 0.0;
@@ -591,8 +626,6 @@ int mbem_fgmres_dense(const double* A, int64_t ld, int64_t n, const double* b, d
     rep->iterations = total;
     rep->restarts = restarts - 1 < 0 ? 0 : restarts - 1;
     rep->converged = rep->true_relres < prm->rtol;
-    rep->stagnated = stagnated && !rep->converged;
+    rep->stagnated = (stagnated || breakdown) && !rep->converged;
     return MBEM_OK;
 }
-
-}  // extern "C"

@@ -1,0 +1,725 @@
+// Mixed-precision operator of the calibrated dense backend (sm_103a).
+//
+// A = A_far (FP32, dense) + A_near (FP64, 3x3 blocks in CSR by field point).
+//
+// Near pairs (source centroid within r_s = 3 max(eps_s, h_s) of the field
+// point, or closer than 1.5 L_s) are the closed-form FP64 pair of
+// p0_pair.cuh, exact to the reference. Far pairs are integrated in FP32 by
+// collapsed Gauss-Legendre product rules (n x n points, n = 3..6 chosen by
+// D / L) of the smooth mollified point kernel; at these distances the
+// quadrature matches the FP64 closed form to ~1.5e-7 of the block (and is
+// more accurate than the closed form beyond D/L ~ 40, where the
+// divergence-theorem form cancels). The field-to-centroid offset is formed
+// in double-float (hi/lo FP32 pairs with an error-free difference), so FP32
+// keeps its relative accuracy at every distance; no FP64 instruction runs
+// in the far kernel.
+//
+// The matvec reads the FP32 matrix once from HBM and accumulates each row in
+// double-float (error-free products and sums on the FP32 pipes), so the
+// operator is applied to ~1e-14 relative accuracy at the HBM roofline; the
+// near blocks are applied in FP64.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "p0_pair.cuh"
+
+namespace mbem {
+
+// ---------------------------------------------------------------------------
+// quadrature rules: collapsed Gauss-Legendre n x n on (0,0),(1,0),(0,1)
+// ---------------------------------------------------------------------------
+constexpr int QR_MIN = 3, QR_MAX = 6;
+constexpr int QR_POINTS = 9 + 16 + 25 + 36;
+
+struct QuadRules {
+    float a[QR_POINTS];    // xi1 - 1/3
+    float b[QR_POINTS];    // xi2 - 1/3
+    float w[QR_POINTS];    // weights, sum 1/2 per rule
+    int off[QR_MAX + 1];
+};
+
+// Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on P_n.
+static void gauss_legendre(int n, double* x, double* w) {
+    for (int i = 0; i < n; i++) {
+        double z = cos(MBEM_PI * (i + 0.75) / (n + 0.5));
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; k++) {
+                double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            double dp = n * (z * p1 - p0) / (z * z - 1.0);
+            double dz = p1 / dp;
+            z -= dz;
+            if (fabs(dz) < 1e-16) break;
+        }
+        double p0 = 1.0, p1 = z;
+        for (int k = 2; k <= n; k++) {
+            double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+            p0 = p1;
+            p1 = p2;
+        }
+        double dp = n * (z * p1 - p0) / (z * z - 1.0);
+        x[i] = z;
+        w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+static QuadRules make_rules() {
+    QuadRules r;
+    int k = 0;
+    for (int n = 0; n <= QR_MAX; n++) r.off[n] = 0;
+    for (int n = QR_MIN; n <= QR_MAX; n++) {
+        r.off[n] = k;
+        double g[QR_MAX], gw[QR_MAX];
+        gauss_legendre(n, g, gw);
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                const double gi = 0.5 * (g[i] + 1.0), gj = 0.5 * (g[j] + 1.0);
+                const double wi = 0.5 * gw[i], wj = 0.5 * gw[j];
+                const double x1 = gi, x2 = gj * (1.0 - gi);
+                r.a[k] = (float)(x1 - 1.0 / 3.0);
+                r.b[k] = (float)(x2 - 1.0 / 3.0);
+                r.w[k] = (float)(wi * wj * (1.0 - gi));
+                k++;
+            }
+    }
+    return r;
+}
+
+static const QuadRules& rules() {
+    static const QuadRules r = make_rules();
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// double-float helpers
+// ---------------------------------------------------------------------------
+struct F2 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ F2 split_d(double v) {
+    F2 r;
+    r.hi = (float)v;
+    r.lo = (float)(v - (double)r.hi);
+    return r;
+}
+
+// (a_hi + a_lo) - (b_hi + b_lo) rounded to FP32 with the hi difference exact
+// (Knuth's TwoSum; the _rn intrinsics keep the compiler from contracting or
+// reassociating the error-free steps)
+__device__ __forceinline__ float df_diff(F2 a, F2 b) {
+    const float s = __fsub_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(-b.hi, bb));
+    return __fadd_rn(s, __fadd_rn(err, __fsub_rn(a.lo, b.lo)));
+}
+
+// ---------------------------------------------------------------------------
+// per-source far-field constants
+// ---------------------------------------------------------------------------
+struct SrcFar {
+    F2 c[3];            // centroid
+    float e1[3], e2[3]; // edges from vertex 0
+    float n[3];         // normal as passed (T kernel)
+    float area2, eps2;
+    float L2;           // longest edge squared
+    float rnear2;       // near radius squared
+    bool ok;
+};
+
+__device__ __forceinline__ void far_setup(const double* __restrict__ tv, const double* __restrict__ nrm,
+                                          double eps, double near_factor, SrcFar& s) {
+    const double e1x = tv[3] - tv[0], e1y = tv[4] - tv[1], e1z = tv[5] - tv[2];
+    const double e2x = tv[6] - tv[0], e2y = tv[7] - tv[1], e2z = tv[8] - tv[2];
+    const double e3x = tv[6] - tv[3], e3y = tv[7] - tv[4], e3z = tv[8] - tv[5];
+    const double cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
+    const double a2 = sqrt(cx * cx + cy * cy + cz * cz);
+    s.ok = a2 >= 1e-30;
+    const double l1 = sqrt(e1x * e1x + e1y * e1y + e1z * e1z);
+    const double l2 = sqrt(e2x * e2x + e2y * e2y + e2z * e2z);
+    const double l3 = sqrt(e3x * e3x + e3y * e3y + e3z * e3z);
+    const double Lm = fmax(fmax(l1, l2), l3);
+    const double h = (l1 + l2 + l3) / 3.0;    // mean edge length
+    const double rn = near_factor * fmax(eps, h);
+    for (int k = 0; k < 3; k++) s.c[k] = split_d((tv[k] + tv[3 + k] + tv[6 + k]) / 3.0);
+    s.e1[0] = (float)e1x; s.e1[1] = (float)e1y; s.e1[2] = (float)e1z;
+    s.e2[0] = (float)e2x; s.e2[1] = (float)e2y; s.e2[2] = (float)e2z;
+    if (nrm) {
+        s.n[0] = (float)nrm[0]; s.n[1] = (float)nrm[1]; s.n[2] = (float)nrm[2];
+    } else {
+        s.n[0] = s.n[1] = s.n[2] = 0.0f;
+    }
+    s.area2 = (float)a2;
+    s.eps2 = (float)(eps * eps);
+    s.L2 = (float)(Lm * Lm);
+    const double r2 = fmax(rn * rn, 2.25 * Lm * Lm);
+    s.rnear2 = (float)r2;
+}
+
+// The one near/far decision, shared by every kernel that needs it.
+__device__ __forceinline__ bool is_near(const F2 x[3], const SrcFar& s, float d[3], float& D2) {
+    d[0] = df_diff(x[0], s.c[0]);
+    d[1] = df_diff(x[1], s.c[1]);
+    d[2] = df_diff(x[2], s.c[2]);
+    D2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    return D2 < s.rnear2;
+}
+
+__device__ __forceinline__ int far_rule(float D2, float L2) {
+    // n by D / L_max (measured against the FP64 closed form: <= ~1.5e-7)
+    if (D2 >= 50.0f * L2) return 3;        // D/L >= 7.07
+    if (D2 >= 8.0f * L2) return 4;         // D/L >= 2.83
+    if (D2 >= 3.125f * L2) return 5;       // D/L >= 1.77
+    return 6;
+}
+
+// Far T block (FP32): out_ij = n_j alpha_i + n_i beta_j + d_ij gamma - 6 c5 W_ij
+// from the quadrature sums V3 = int d/R^3, V5 = int d/R^5,
+// t = int d |d|^2/R^5, W = int d d (d.n)/R^5 (d = x - y).
+template <bool TKERNEL>
+__device__ __forceinline__ void far_block(const QuadRules& Q, const SrcFar& s, const float dc[3], float D2,
+                                          const float c[6], float out[3][3]) {
+    const int nq = far_rule(D2, s.L2);
+    const int q0 = Q.off[nq], q1 = q0 + nq * nq;
+    float V3[3] = {0, 0, 0}, V5[3] = {0, 0, 0}, t[3] = {0, 0, 0};
+    float W00 = 0, W01 = 0, W02 = 0, W11 = 0, W12 = 0, W22 = 0;
+    float I1 = 0, I3 = 0;   // U kernel: int 1/R, int 1/R^3
+    for (int q = q0; q < q1; q++) {
+        const float a = Q.a[q], b = Q.b[q];
+        const float dx = dc[0] - (a * s.e1[0] + b * s.e2[0]);
+        const float dy = dc[1] - (a * s.e1[1] + b * s.e2[1]);
+        const float dz = dc[2] - (a * s.e1[2] + b * s.e2[2]);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float iR = rsqrtf(r2 + s.eps2);
+        const float w = Q.w[q];
+        const float iR2 = iR * iR;
+        const float w3 = w * iR2 * iR;
+        if (TKERNEL) {
+            const float w5 = w3 * iR2;
+            V3[0] += w3 * dx; V3[1] += w3 * dy; V3[2] += w3 * dz;
+            V5[0] += w5 * dx; V5[1] += w5 * dy; V5[2] += w5 * dz;
+            const float wt = w5 * r2;
+            t[0] += wt * dx; t[1] += wt * dy; t[2] += wt * dz;
+            const float wn = w5 * (dx * s.n[0] + dy * s.n[1] + dz * s.n[2]);
+            const float ux = wn * dx, uy = wn * dy, uz = wn * dz;
+            W00 += ux * dx; W01 += ux * dy; W02 += ux * dz;
+            W11 += uy * dy; W12 += uy * dz; W22 += uz * dz;
+        } else {
+            I1 += w * iR;
+            I3 += w3;
+            const float ux = w3 * dx, uy = w3 * dy, uz = w3 * dz;   // T2[3] = int d d / R^3
+            W00 += ux * dx; W01 += ux * dy; W02 += ux * dz;
+            W11 += uy * dy; W12 += uy * dz; W22 += uz * dz;
+        }
+    }
+    const float A = s.area2;
+    const float W[3][3] = {{W00, W01, W02}, {W01, W11, W12}, {W02, W12, W22}};
+    if (TKERNEL) {
+        const float* n = s.n;
+        const float nV3 = n[0] * V3[0] + n[1] * V3[1] + n[2] * V3[2];
+        const float nV5 = n[0] * V5[0] + n[1] * V5[1] + n[2] * V5[2];
+        const float ca = c[0] + 4.0f * c[1] + 2.0f * c[4];
+        const float cb = c[3] + c[4];
+        const float ce3 = c[2] * s.eps2, ce6 = c[5] * s.eps2;
+        const float gam = cb * nV3 + ce6 * nV5;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float al = ca * V3[i] - 3.0f * c[1] * t[i] + ce3 * V5[i];
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const float be = cb * V3[j] + ce6 * V5[j];
+                out[i][j] = A * (n[j] * al + n[i] * be - 6.0f * c[4] * W[i][j] + (i == j ? gam : 0.0f));
+            }
+        }
+    } else {
+        const float dg = c[0] * I1 + c[1] * s.eps2 * I3;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) out[i][j] = A * (c[2] * W[i][j] + (i == j ? dg : 0.0f));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// far assembly: one thread per source, FIELD_TILE field points per block
+// ---------------------------------------------------------------------------
+constexpr int FAR_THREADS = 128;
+constexpr int FAR_FIELD_TILE = 32;
+
+struct FarArgs {
+    const double* x_field;
+    int64_t n_field;
+    const double* tri_verts;
+    const double* normals;
+    const double* eps;
+    int64_t n_src;
+    float c[6];
+    float alpha;
+    double near_factor;
+    float* out;
+    int64_t ld;
+};
+
+template <bool TKERNEL>
+__global__ void __launch_bounds__(FAR_THREADS)
+far_assemble_kernel(FarArgs a, QuadRules Q) {
+    __shared__ F2 xs[FAR_FIELD_TILE][3];
+    const int64_t s = (int64_t)blockIdx.x * FAR_THREADS + threadIdx.x;
+    const bool active = s < a.n_src;
+    SrcFar src;
+    if (active) far_setup(a.tri_verts + 9 * s, TKERNEL ? a.normals + 3 * s : nullptr, a.eps[s], a.near_factor, src);
+    for (int64_t f0 = (int64_t)blockIdx.y * FAR_FIELD_TILE; f0 < a.n_field;
+         f0 += (int64_t)gridDim.y * FAR_FIELD_TILE) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < FAR_FIELD_TILE * 3; t += FAR_THREADS) {
+            const int64_t f = f0 + t / 3;
+            xs[t / 3][t % 3] = split_d(f < a.n_field ? a.x_field[3 * f0 + t] : 0.0);
+        }
+        __syncthreads();
+        if (!active) continue;
+        const int nf = (int)lmin(FAR_FIELD_TILE, a.n_field - f0);
+        for (int ff = 0; ff < nf; ff++) {
+            const int64_t f = f0 + ff;
+            float d[3], D2;
+            float blk[3][3];
+            const bool near = is_near(xs[ff], src, d, D2);
+            if (near || !src.ok) {
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++) blk[i][j] = 0.0f;
+            } else {
+                far_block<TKERNEL>(Q, src, d, D2, a.c, blk);
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                float* row = a.out + (3 * f + i) * a.ld + 3 * s;
+#pragma unroll
+                for (int j = 0; j < 3; j++) row[j] = a.alpha * blk[i][j];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// near list: count per field point, scan, fill (deterministic source order)
+// ---------------------------------------------------------------------------
+constexpr int NL_THREADS = 128;
+constexpr int NL_SRC_TILE = 128;
+
+struct NearArgs {
+    const double* x_field;
+    int64_t n_field;
+    const double* tri_verts;
+    const double* eps;
+    int64_t n_src;
+    double near_factor;
+    int64_t* counts;       // (n_field,) or rowptr (n_field + 1)
+    int64_t* cols;         // fill pass only
+};
+
+template <bool FILL>
+__global__ void __launch_bounds__(NL_THREADS)
+near_list_kernel(NearArgs a) {
+    __shared__ SrcFar tile[NL_SRC_TILE];
+    const int64_t f = (int64_t)blockIdx.x * NL_THREADS + threadIdx.x;
+    const bool active = f < a.n_field;
+    F2 x[3];
+    for (int k = 0; k < 3; k++) x[k] = split_d(active ? a.x_field[3 * f + k] : 0.0);
+    int64_t cnt = 0;
+    int64_t pos = (FILL && active) ? a.counts[f] : 0;
+    for (int64_t s0 = 0; s0 < a.n_src; s0 += NL_SRC_TILE) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < NL_SRC_TILE; t += NL_THREADS) {
+            const int64_t s = s0 + t;
+            if (s < a.n_src) far_setup(a.tri_verts + 9 * s, nullptr, a.eps[s], a.near_factor, tile[t]);
+        }
+        __syncthreads();
+        if (!active) continue;
+        const int ns = (int)lmin(NL_SRC_TILE, a.n_src - s0);
+        for (int t = 0; t < ns; t++) {
+            float d[3], D2;
+            if (is_near(x, tile[t], d, D2)) {
+                if (FILL) a.cols[pos++] = s0 + t;
+                else cnt++;
+            }
+        }
+    }
+    if (!FILL && active) a.counts[f] = cnt;
+}
+
+// exclusive scan of n counts into rowptr[0..n] (one block, fixed order)
+__global__ void scan_kernel(const int64_t* __restrict__ counts, int64_t n, int64_t* __restrict__ rowptr) {
+    __shared__ int64_t part[1024];
+    const int t = threadIdx.x;
+    const int64_t chunk = (n + blockDim.x - 1) / blockDim.x;
+    const int64_t b0 = t * chunk, b1 = lmin(n, b0 + chunk);
+    int64_t s = 0;
+    for (int64_t i = b0; i < b1; i++) s += counts[i];
+    part[t] = s;
+    __syncthreads();
+    if (t == 0) {
+        int64_t run = 0;
+        for (int i = 0; i < (int)blockDim.x; i++) {
+            const int64_t v = part[i];
+            part[i] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    int64_t run = part[t];
+    for (int64_t i = b0; i < b1; i++) {
+        rowptr[i] = run;
+        run += counts[i];
+    }
+    if (b1 == n && b0 < b1) rowptr[n] = run;
+    if (n == 0 && t == 0) rowptr[0] = 0;
+}
+
+// near T/U blocks in FP64 (closed form), one thread per near pair
+struct NearEvalArgs {
+    const double* x_field;
+    int64_t n_field;
+    const double* tri_verts;
+    const double* normals;
+    const double* eps;
+    const int64_t* rowptr;
+    const int64_t* cols;
+    int64_t nnz;
+    double c[6];
+    double alpha;
+    double* vals;          // (nnz, 3, 3)
+};
+
+template <bool TKERNEL>
+__global__ void __launch_bounds__(128)
+near_eval_kernel(NearEvalArgs a) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.nnz) return;
+    // field point of pair k: binary search in rowptr
+    int64_t lo = 0, hi = a.n_field;
+    while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (a.rowptr[mid] <= k) lo = mid;
+        else hi = mid;
+    }
+    const int64_t f = lo, s = a.cols[k];
+    SrcP0 src;
+    src_setup(a.tri_verts + 9 * s, a.eps[s], src);
+    double blk[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    if (src.ok) {
+        PairP0 p;
+        pair_setup(src, a.x_field[3 * f], a.x_field[3 * f + 1], a.x_field[3 * f + 2], p);
+        if (TKERNEL) {
+            const double* nrm = a.normals + 3 * s;
+            TMoments m;
+            t_moments(src, nrm, p, m);
+            t_block(m, nrm, a.c, src.eps2, blk);
+        } else {
+            UMoments m;
+            u_moments(src, p, m);
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+                    blk[i][j] = a.c[2] * m.T2[i][j] + (i == j ? a.c[0] * m.I1 + a.c[1] * src.eps2 * m.I3 : 0.0);
+        }
+    }
+    double* v = a.vals + 9 * k;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) v[3 * i + j] = a.alpha * blk[i][j];
+}
+
+// near blocks: calibration row sums out[f, i, j] += sum_k vals[k, i, j]
+__global__ void near_rowsum_kernel(const int64_t* __restrict__ rowptr, const double* __restrict__ vals,
+                                   int64_t n_field, double* __restrict__ out) {
+    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_field) return;
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t k = rowptr[f]; k < rowptr[f + 1]; k++)
+#pragma unroll
+        for (int q = 0; q < 9; q++) acc[q] += vals[9 * k + q];
+#pragma unroll
+    for (int q = 0; q < 9; q++) out[9 * f + q] += acc[q];
+}
+
+// add D[c] to the diagonal (self) block of row c, shape weights at P0 = 1
+__global__ void near_add_diag_kernel(const int64_t* __restrict__ rowptr, const int64_t* __restrict__ cols,
+                                     double* __restrict__ vals, int64_t n_field, const double* __restrict__ D,
+                                     int* __restrict__ missing) {
+    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_field) return;
+    for (int64_t k = rowptr[f]; k < rowptr[f + 1]; k++) {
+        if (cols[k] == f) {
+#pragma unroll
+            for (int q = 0; q < 9; q++) vals[9 * k + q] += D[9 * f + q];
+            return;
+        }
+    }
+    atomicAdd(missing, 1);
+}
+
+// FP32 row sums with double-float accumulation: out[r, j] (+)= sum_c A[r, 3c+j]
+__global__ void rowsum3_f32_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_cols,
+                                   double alpha, int accumulate, double* __restrict__ out) {
+    const int64_t r = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (r >= n_rows) return;
+    const float* row = A + r * ld;
+    float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
+    int j = lane % 3;
+    for (int64_t c = lane; c < n_cols; c += 32) {
+        const float v = row[c];
+        const float s = __fadd_rn(hi[j], v);
+        const float bb = __fsub_rn(s, hi[j]);
+        lo[j] = __fadd_rn(lo[j], __fadd_rn(__fsub_rn(hi[j], __fsub_rn(s, bb)), __fsub_rn(v, bb)));
+        hi[j] = s;
+        j += 2;
+        if (j >= 3) j -= 3;
+    }
+    double acc[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        acc[k] = (double)hi[k] + (double)lo[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    }
+    if (lane == 0)
+        for (int k = 0; k < 3; k++) {
+            const double v = alpha * acc[k];
+            out[3 * r + k] = accumulate ? out[3 * r + k] + v : v;
+        }
+}
+
+// ---------------------------------------------------------------------------
+// mixed matvec: y = alpha * (A32 x + sum of near blocks x) + beta * y
+// ---------------------------------------------------------------------------
+__global__ void split_vec_kernel(const double* __restrict__ x, int64_t n, float* __restrict__ xh,
+                                 float* __restrict__ xl) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const F2 v = split_d(x[i]);
+    xh[i] = v.hi;
+    xl[i] = v.lo;
+}
+
+constexpr int SGEMV_ROWS = 4;
+constexpr int SGEMV_THREADS = 256;
+
+// double-float accumulate of a (FP32, exact) times x = xh + xl
+__device__ __forceinline__ void df_acc(float& sh, float& sl, float a, float xh, float xl) {
+    const float p = __fmul_rn(a, xh);
+    const float e = __fmaf_rn(a, xh, -p);      // exact product error (TwoProd)
+    const float q = __fmaf_rn(a, xl, e);
+    const float s = __fadd_rn(sh, p);          // TwoSum of sh + p
+    const float bb = __fsub_rn(s, sh);
+    sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb)), q));
+    sh = s;
+}
+
+__global__ void __launch_bounds__(SGEMV_THREADS)
+sgemv_df_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_cols,
+                const float* __restrict__ xh, const float* __restrict__ xl, double* __restrict__ y) {
+    const int64_t warp = (int64_t)blockIdx.x * (SGEMV_THREADS / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    const int64_t r0 = warp * SGEMV_ROWS;
+    if (r0 >= n_rows) return;
+    const int nr = (int)lmin(SGEMV_ROWS, n_rows - r0);
+    float sh[SGEMV_ROWS], sl[SGEMV_ROWS];
+#pragma unroll
+    for (int i = 0; i < SGEMV_ROWS; i++) sh[i] = sl[i] = 0.0f;
+    const int64_t n4 = n_cols / 4;
+    const float4* xh4 = reinterpret_cast<const float4*>(xh);
+    const float4* xl4 = reinterpret_cast<const float4*>(xl);
+    const float4* rows[SGEMV_ROWS];
+#pragma unroll
+    for (int i = 0; i < SGEMV_ROWS; i++) rows[i] = reinterpret_cast<const float4*>(A + (r0 + min(i, nr - 1)) * ld);
+    for (int64_t c = lane; c < n4; c += 32) {
+        const float4 h = __ldg(xh4 + c), l = __ldg(xl4 + c);
+#pragma unroll
+        for (int i = 0; i < SGEMV_ROWS; i++) {
+            const float4 v = __ldcs(rows[i] + c);
+            df_acc(sh[i], sl[i], v.x, h.x, l.x);
+            df_acc(sh[i], sl[i], v.y, h.y, l.y);
+            df_acc(sh[i], sl[i], v.z, h.z, l.z);
+            df_acc(sh[i], sl[i], v.w, h.w, l.w);
+        }
+    }
+    for (int64_t c = 4 * n4 + lane; c < n_cols; c += 32) {
+#pragma unroll
+        for (int i = 0; i < SGEMV_ROWS; i++)
+            df_acc(sh[i], sl[i], A[(r0 + min(i, nr - 1)) * ld + c], xh[c], xl[c]);
+    }
+    double acc[SGEMV_ROWS];
+#pragma unroll
+    for (int i = 0; i < SGEMV_ROWS; i++) {
+        acc[i] = (double)sh[i] + (double)sl[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+    }
+    if (lane < nr) {
+        double v = acc[0];
+#pragma unroll
+        for (int i = 1; i < SGEMV_ROWS; i++)
+            if (lane == i) v = acc[i];
+        y[r0 + lane] = v;
+    }
+}
+
+// y[3f + i] += sum_k vals[k, i, j] x[3 cols[k] + j]  (one thread per row block)
+__global__ void near_matvec_kernel(const int64_t* __restrict__ rowptr, const int64_t* __restrict__ cols,
+                                   const double* __restrict__ vals, int64_t n_field, const double* __restrict__ x,
+                                   double* __restrict__ y) {
+    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_field) return;
+    double a0 = 0, a1 = 0, a2 = 0;
+    for (int64_t k = rowptr[f]; k < rowptr[f + 1]; k++) {
+        const int64_t s = cols[k];
+        const double x0 = x[3 * s], x1 = x[3 * s + 1], x2 = x[3 * s + 2];
+        const double* v = vals + 9 * k;
+        a0 += v[0] * x0 + v[1] * x1 + v[2] * x2;
+        a1 += v[3] * x0 + v[4] * x1 + v[5] * x2;
+        a2 += v[6] * x0 + v[7] * x1 + v[8] * x2;
+    }
+    y[3 * f] += a0;
+    y[3 * f + 1] += a1;
+    y[3 * f + 2] += a2;
+}
+
+int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, float* xh, float* xl,
+                 cudaStream_t st) {
+    const int64_t nr = op->n_rows, nc = op->n_cols;
+    if (nr == 0) return MBEM_OK;
+    split_vec_kernel<<<(unsigned)ceil_div(nc > 0 ? nc : 1, 256), 256, 0, st>>>(x, nc, xh, xl);
+    const int64_t warps = ceil_div(nr, SGEMV_ROWS);
+    const bool vec = ((uintptr_t)op->A32 % 16 == 0) && (op->ld32 % 4 == 0);
+    MBEM_REQUIRE(vec, MBEM_ERR_ARG, "the FP32 far matrix must be 16-byte aligned with ld32 %% 4 == 0");
+    sgemv_df_kernel<<<(unsigned)ceil_div(warps, SGEMV_THREADS / 32), SGEMV_THREADS, 0, st>>>(
+        op->A32, op->ld32, nr, nc, xh, xl, y);
+    int launches = 2;
+    for (int q = 0; q < op->n_near; q++) {
+        const mbem_near_blocks& nb = op->near[q];
+        near_matvec_kernel<<<(unsigned)ceil_div(nb.n_field, 128), 128, 0, st>>>(
+            nb.rowptr, nb.cols, nb.vals, nb.n_field, x + nb.col0, y + nb.row0);
+        launches++;
+    }
+    return launch_status("mixed_matvec", launches);
+}
+
+}  // namespace mbem
+
+using namespace mbem;
+
+extern "C" {
+
+int mbem_far_matrix(int kernel, const double* x_field, int64_t n_field, const double* tri_verts,
+                    const double* normals, const double* eps, int64_t n_src, const double* coeffs,
+                    double near_factor, double alpha, float* out, int64_t ld_out, void* stream) {
+    MBEM_REQUIRE(kernel == 0 || kernel == 1, MBEM_ERR_ARG, "kernel must be 0 (T) or 1 (U)");
+    MBEM_REQUIRE(n_field >= 0 && n_src >= 0 && ld_out >= 3 * n_src, MBEM_ERR_ARG, "bad far matrix shape");
+    MBEM_REQUIRE(coeffs != nullptr && near_factor > 0.0, MBEM_ERR_ARG, "coeffs/near_factor");
+    MBEM_REQUIRE(kernel == 1 || n_src == 0 || normals, MBEM_ERR_ARG, "normals is NULL");
+    if (n_field == 0 || n_src == 0) return MBEM_OK;
+    FarArgs a;
+    a.x_field = x_field; a.n_field = n_field; a.tri_verts = tri_verts; a.normals = normals; a.eps = eps;
+    a.n_src = n_src;
+    const int nc = kernel == 0 ? 6 : 3;
+    for (int i = 0; i < 6; i++) a.c[i] = i < nc ? (float)coeffs[i] : 0.0f;
+    a.alpha = (float)alpha; a.near_factor = near_factor; a.out = out; a.ld = ld_out;
+    dim3 grid((unsigned)ceil_div(n_src, FAR_THREADS), (unsigned)lmin(ceil_div(n_field, FAR_FIELD_TILE), 65535));
+    if (kernel == 0)
+        far_assemble_kernel<true><<<grid, FAR_THREADS, 0, (cudaStream_t)stream>>>(a, rules());
+    else
+        far_assemble_kernel<false><<<grid, FAR_THREADS, 0, (cudaStream_t)stream>>>(a, rules());
+    return launch_status("far_assemble_kernel");
+}
+
+size_t mbem_near_list_workspace_size(int64_t n_field) { return (size_t)(n_field + 1) * sizeof(int64_t); }
+
+int mbem_near_count(const double* x_field, int64_t n_field, const double* tri_verts, const double* eps,
+                    int64_t n_src, double near_factor, int64_t* rowptr, void* work, size_t work_bytes,
+                    int64_t* nnz_host, void* stream) {
+    MBEM_REQUIRE(n_field >= 0 && n_src >= 0 && rowptr && nnz_host, MBEM_ERR_ARG, "bad near-count args");
+    MBEM_REQUIRE(work && work_bytes >= mbem_near_list_workspace_size(n_field), MBEM_ERR_SIZE,
+                 "near-count workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    int64_t* counts = (int64_t*)work;
+    NearArgs a;
+    a.x_field = x_field; a.n_field = n_field; a.tri_verts = tri_verts; a.eps = eps; a.n_src = n_src;
+    a.near_factor = near_factor; a.counts = counts; a.cols = nullptr;
+    if (n_field > 0)
+        near_list_kernel<false><<<(unsigned)ceil_div(n_field, NL_THREADS), NL_THREADS, 0, st>>>(a);
+    scan_kernel<<<1, 1024, 0, st>>>(counts, n_field, rowptr);
+    cudaMemcpyAsync(nnz_host, rowptr + n_field, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("near_count sync", 2);
+    return launch_status("near_count", 2);
+}
+
+int mbem_near_fill(const double* x_field, int64_t n_field, const double* tri_verts, const double* eps,
+                   int64_t n_src, double near_factor, const int64_t* rowptr, int64_t* cols, void* stream) {
+    // cols may be NULL when the list is empty: the kernel writes only near pairs
+    MBEM_REQUIRE(n_field >= 0 && rowptr, MBEM_ERR_ARG, "bad near-fill args");
+    if (n_field == 0) return MBEM_OK;
+    NearArgs a;
+    a.x_field = x_field; a.n_field = n_field; a.tri_verts = tri_verts; a.eps = eps; a.n_src = n_src;
+    a.near_factor = near_factor; a.counts = const_cast<int64_t*>(rowptr); a.cols = cols;
+    near_list_kernel<true><<<(unsigned)ceil_div(n_field, NL_THREADS), NL_THREADS, 0, (cudaStream_t)stream>>>(a);
+    return launch_status("near_fill");
+}
+
+int mbem_near_eval(int kernel, const double* x_field, int64_t n_field, const double* tri_verts,
+                   const double* normals, const double* eps, const int64_t* rowptr, const int64_t* cols,
+                   int64_t nnz, const double* coeffs, double alpha, double* vals, void* stream) {
+    MBEM_REQUIRE(kernel == 0 || kernel == 1, MBEM_ERR_ARG, "kernel must be 0 (T) or 1 (U)");
+    MBEM_REQUIRE(coeffs && nnz >= 0, MBEM_ERR_ARG, "bad near-eval args");
+    if (nnz == 0) return MBEM_OK;
+    NearEvalArgs a;
+    a.x_field = x_field; a.n_field = n_field; a.tri_verts = tri_verts; a.normals = normals; a.eps = eps;
+    a.rowptr = rowptr; a.cols = cols; a.nnz = nnz; a.alpha = alpha; a.vals = vals;
+    const int nc = kernel == 0 ? 6 : 3;
+    for (int i = 0; i < 6; i++) a.c[i] = i < nc ? coeffs[i] : 0.0;
+    const unsigned g = (unsigned)ceil_div(nnz, 128);
+    if (kernel == 0) near_eval_kernel<true><<<g, 128, 0, (cudaStream_t)stream>>>(a);
+    else near_eval_kernel<false><<<g, 128, 0, (cudaStream_t)stream>>>(a);
+    return launch_status("near_eval_kernel");
+}
+
+int mbem_mixed_rowsum3(const float* A32, int64_t ld, int64_t n_rows, int64_t n_col_nodes,
+                       const int64_t* rowptr, const double* vals, double* out, void* stream) {
+    MBEM_REQUIRE(n_rows >= 0 && n_rows % 3 == 0 && ld >= 3 * n_col_nodes, MBEM_ERR_ARG, "bad rowsum shape");
+    if (n_rows == 0) return MBEM_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    rowsum3_f32_kernel<<<(unsigned)ceil_div(n_rows, 8), 256, 0, st>>>(A32, ld, n_rows, 3 * n_col_nodes, 1.0, 0,
+                                                                     out);
+    near_rowsum_kernel<<<(unsigned)ceil_div(n_rows / 3, 128), 128, 0, st>>>(rowptr, vals, n_rows / 3, out);
+    return launch_status("mixed_rowsum3", 2);
+}
+
+int mbem_near_add_diagonal(const int64_t* rowptr, const int64_t* cols, double* vals, int64_t n_field,
+                           const double* D, int* missing, void* stream) {
+    MBEM_REQUIRE(rowptr && D && missing, MBEM_ERR_ARG, "bad near-diag args");
+    if (n_field == 0) return MBEM_OK;
+    near_add_diag_kernel<<<(unsigned)ceil_div(n_field, 128), 128, 0, (cudaStream_t)stream>>>(rowptr, cols, vals,
+                                                                                          n_field, D, missing);
+    return launch_status("near_add_diag_kernel");
+}
+
+int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, void* work, size_t work_bytes,
+                      void* stream) {
+    MBEM_REQUIRE(op && x && y && op->n_rows >= 0 && op->n_cols >= 0 && op->ld32 >= op->n_cols, MBEM_ERR_ARG,
+                 "bad mixed matvec args");
+    MBEM_REQUIRE(work && work_bytes >= 2 * (size_t)op->n_cols * sizeof(float) + 64, MBEM_ERR_SIZE,
+                 "mixed matvec workspace too small");
+    float* xh = (float*)work;
+    float* xl = xh + ((op->n_cols + 15) / 16) * 16;
+    return mixed_matvec(op, x, y, xh, xl, (cudaStream_t)stream);
+}
+
+}  // extern "C"

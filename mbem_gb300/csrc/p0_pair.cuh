@@ -89,26 +89,32 @@ __device__ __forceinline__ void src_setup(const double* __restrict__ tv, double 
 // Pair geometry shared by all kernels: height, lift, projected vertices,
 // vertex distances and I3 = -Omega / h (tri_kernels.py:257-273).
 struct PairP0 {
-    double z, h2, h;
+    double z, h2, h, ih2;        // ih2 = 1 / h^2
     double px[3], py[3];
     double R[3], iR[3];
     double I3;
 };
 
+// FP64 work is the cost of every pair (the FP64 pipe is 1/64 of FP32 on
+// this part), so reciprocals come from rsqrt (R and 1/R from one call) and
+// from shared divisions.
 __device__ __forceinline__ void pair_setup(const SrcP0& s, double ox, double oy, double oz, PairP0& p) {
     double dx = ox - s.v0[0], dy = oy - s.v0[1], dz = oz - s.v0[2];
     p.z = dx * s.nh[0] + dy * s.nh[1] + dz * s.nh[2];
     double qx = dx * s.ex[0] + dy * s.ex[1] + dz * s.ex[2];
     double qy = dx * s.ey[0] + dy * s.ey[1] + dz * s.ey[2];
     p.h2 = p.z * p.z + s.eps2;
-    p.h = sqrt(p.h2);
+    const double ih = rsqrt(p.h2);
+    p.h = p.h2 * ih;
+    p.ih2 = ih * ih;
     p.px[0] = -qx;          p.py[0] = -qy;
     p.px[1] = s.Px1 - qx;   p.py[1] = s.Py1 - qy;
     p.px[2] = s.Px2 - qx;   p.py[2] = s.Py2 - qy;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        p.R[k] = sqrt(p.px[k] * p.px[k] + p.py[k] * p.py[k] + p.h2);
-        p.iR[k] = 1.0 / p.R[k];
+        const double r2 = p.px[k] * p.px[k] + p.py[k] * p.py[k] + p.h2;
+        p.iR[k] = rsqrt(r2);
+        p.R[k] = r2 * p.iR[k];
     }
     // van Oosterom at the lifted point, in the source frame: r_k = (px, py, -h)
     double d01 = p.px[0] * p.px[1] + p.py[0] * p.py[1] + p.h2;
@@ -117,30 +123,55 @@ __device__ __forceinline__ void pair_setup(const SrcP0& s, double ox, double oy,
     double numer = -p.h * s.area2;
     double denom = p.R[0] * p.R[1] * p.R[2] + p.R[2] * d01 + p.R[0] * d12 + p.R[1] * d02;
     double omega = 2.0 * atan2(numer, denom);
-    p.I3 = -omega / p.h;
+    p.I3 = -omega * ih;
 }
 
 // Per-edge primitive differences at orders 1 and 3 (tri_kernels.py:54-76,
 // :298-302): J1 = log(u + R), K1 = R, J3 = u / (rho^2 R), K3 = -1/R.
 struct EdgeP0 {
-    double nx, ny, tx, ty, dp, rho2;
+    double nx, ny, tx, ty, dp, ua, ub, rho2, ir2;
     double dJ1, dK1, dJ3, dK3, dL3;
 };
 
-__device__ __forceinline__ void edge_setup(const SrcP0& s, const PairP0& p, int e, EdgeP0& g) {
-    const int a = e, b = (e + 1) % 3;
-    g.tx = s.tx[e]; g.ty = s.ty[e];
-    g.nx = g.ty; g.ny = -g.tx;
-    g.dp = p.px[a] * g.nx + p.py[a] * g.ny;
-    double ua = p.px[a] * g.tx + p.py[a] * g.ty;
-    double ub = p.px[b] * g.tx + p.py[b] * g.ty;
-    g.rho2 = g.dp * g.dp + p.h2;
-    g.dJ1 = log(ub + p.R[b] + 1e-300) - log(ua + p.R[a] + 1e-300);
-    g.dK1 = p.R[b] - p.R[a];
-    double ir2 = (g.rho2 < 1e-60) ? 0.0 : 1.0 / g.rho2;
-    g.dJ3 = (ub * p.iR[b] - ua * p.iR[a]) * ir2;
-    g.dK3 = p.iR[a] - p.iR[b];
-    g.dL3 = g.dJ1 - g.rho2 * g.dJ3;
+// All three edges at once: dJ1 = log((u_b + R_b) / (u_a + R_a)) takes one
+// log per edge, and the three quotients and the three 1/rho^2 share one
+// division each through the product of their denominators.
+__device__ __forceinline__ void edges_setup(const SrcP0& s, const PairP0& p, EdgeP0 g[3]) {
+    double num[3], den[3];
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+        const int a = e, b = (e + 1) % 3;
+        g[e].tx = s.tx[e]; g[e].ty = s.ty[e];
+        g[e].nx = g[e].ty; g[e].ny = -g[e].tx;
+        g[e].dp = p.px[a] * g[e].nx + p.py[a] * g[e].ny;
+        g[e].ua = p.px[a] * g[e].tx + p.py[a] * g[e].ty;
+        g[e].ub = p.px[b] * g[e].tx + p.py[b] * g[e].ty;
+        g[e].rho2 = s.edge_ok[e] ? g[e].dp * g[e].dp + p.h2 : 1.0;
+        num[e] = s.edge_ok[e] ? g[e].ub + p.R[b] + 1e-300 : 1.0;
+        den[e] = s.edge_ok[e] ? g[e].ua + p.R[a] + 1e-300 : 1.0;
+        g[e].dK1 = p.R[b] - p.R[a];
+        g[e].dK3 = p.iR[a] - p.iR[b];
+    }
+    const double r01 = g[0].rho2 * g[1].rho2;
+    const double d01 = den[0] * den[1];
+    const bool tiny = fmin(fmin(g[0].rho2, g[1].rho2), g[2].rho2) < 1e-60;
+    const double ir = tiny ? 0.0 : 1.0 / (r01 * g[2].rho2);
+    const double id = 1.0 / (d01 * den[2]);
+    g[0].ir2 = g[1].rho2 * g[2].rho2 * ir;
+    g[1].ir2 = g[0].rho2 * g[2].rho2 * ir;
+    g[2].ir2 = r01 * ir;
+    if (tiny) {
+#pragma unroll
+        for (int e = 0; e < 3; e++) g[e].ir2 = (g[e].rho2 < 1e-60) ? 0.0 : 1.0 / g[e].rho2;
+    }
+    const double q[3] = {num[0] * den[1] * den[2] * id, num[1] * den[0] * den[2] * id, num[2] * d01 * id};
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+        const int a = e, b = (e + 1) % 3;
+        g[e].dJ1 = log(q[e]);
+        g[e].dJ3 = (g[e].ub * p.iR[b] - g[e].ua * p.iR[a]) * g[e].ir2;
+        g[e].dL3 = g[e].dJ1 - g[e].rho2 * g[e].dJ3;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -161,11 +192,12 @@ __device__ __forceinline__ void t_moments(const SrcP0& s, const double* __restri
                                           const PairP0& p, TMoments& m) {
     double BN1_001 = 0, BN2_001 = 0, BD003 = 0, BN1_003 = 0, BN2_003 = 0, BN1_103 = 0,
            BN1_013 = 0, BN2_013 = 0, BN1_203 = 0, BN1_113 = 0, BN1_023 = 0, BN2_023 = 0;
+    EdgeP0 G[3];
+    edges_setup(s, p, G);
 #pragma unroll
     for (int e = 0; e < 3; e++) {
         if (!s.edge_ok[e]) continue;
-        EdgeP0 g;
-        edge_setup(s, p, e, g);
+        const EdgeP0& g = G[e];
         double A = g.dp * g.nx, B = g.dp * g.ny;
         double v10 = A * g.dJ3 + g.tx * g.dK3;
         double v01 = B * g.dJ3 + g.ty * g.dK3;
@@ -182,7 +214,7 @@ __device__ __forceinline__ void t_moments(const SrcP0& s, const double* __restri
         BN1_023 += g.nx * v02; BN2_023 += g.ny * v02;
     }
     const double I3 = p.I3, z = p.z;
-    const double I5 = (BD003 + I3) / (3.0 * p.h2);
+    const double I5 = (BD003 + I3) * p.ih2 * (1.0 / 3.0);
     const double third = 1.0 / 3.0;
     const double m10_3 = -BN1_001, m01_3 = -BN2_001;
     const double m10_5 = -BN1_003 * third, m01_5 = -BN2_003 * third;
@@ -285,16 +317,15 @@ struct UMoments {
 
 __device__ __forceinline__ void u_moments(const SrcP0& s, const PairP0& p, UMoments& m) {
     double BD001 = 0, BN1_001 = 0, BN2_001 = 0, BN1_101 = 0, BN1_011 = 0, BN2_011 = 0;
+    EdgeP0 G[3];
+    edges_setup(s, p, G);
 #pragma unroll
     for (int e = 0; e < 3; e++) {
         if (!s.edge_ok[e]) continue;
-        const int a = e, b = (e + 1) % 3;
-        const double tx = s.tx[e], ty = s.ty[e], nx = ty, ny = -tx;
-        const double dp = p.px[a] * nx + p.py[a] * ny;
-        const double ua = p.px[a] * tx + p.py[a] * ty;
-        const double ub = p.px[b] * tx + p.py[b] * ty;
-        const double dJ1 = log(ub + p.R[b] + 1e-300) - log(ua + p.R[a] + 1e-300);
-        const double dK1 = p.R[b] - p.R[a];
+        const double tx = G[e].tx, ty = G[e].ty, nx = G[e].nx, ny = G[e].ny;
+        const double dp = G[e].dp;
+        const double dJ1 = G[e].dJ1;
+        const double dK1 = G[e].dK1;
         const double v10 = dp * nx * dJ1 + tx * dK1;
         const double v01 = dp * ny * dJ1 + ty * dK1;
         BD001 += dp * dJ1;
@@ -390,11 +421,12 @@ __device__ __forceinline__ void stress_moments(const SrcP0& s, const PairP0& p, 
     double b5_1_00 = 0, b5_1_10 = 0, b5_1_01 = 0, b5_1_20 = 0, b5_1_11 = 0, b5_1_02 = 0,
            b5_1_30 = 0, b5_1_21 = 0, b5_1_12 = 0, b5_1_03 = 0;
     double b5_2_00 = 0, b5_2_01 = 0, b5_2_02 = 0, b5_2_03 = 0;
+    EdgeP0 G[3];
+    edges_setup(s, p, G);
 #pragma unroll
     for (int e = 0; e < 3; e++) {
         if (!s.edge_ok[e]) continue;
-        EdgeP0 g;
-        edge_setup(s, p, e, g);
+        const EdgeP0& g = G[e];
         const double A = g.dp * g.nx, B = g.dp * g.ny;
         BN1m1 += g.nx * g.dJ1; BN2m1 += g.ny * g.dJ1;
         double v;
@@ -409,12 +441,11 @@ __device__ __forceinline__ void stress_moments(const SrcP0& s, const PairP0& p, 
         b3_1_02 += g.nx * v; b3_2_02 += g.ny * v;
         if (NEED7) {
             const int a = e, b = (e + 1) % 3;
-            const double ua = p.px[a] * g.tx + p.py[a] * g.ty;
-            const double ub = p.px[b] * g.tx + p.py[b] * g.ty;
+            const double ua = g.ua, ub = g.ub;
             // J5 = u (3 rho^2 + 2 u^2) / (3 rho^4 R^3), K5 = -1 / (3 R^3)
             double dJ5 = 0.0;
             if (g.rho2 >= 1e-60) {
-                const double ir2 = 1.0 / g.rho2;
+                const double ir2 = g.ir2;
                 const double ia3 = p.iR[a] * p.iR[a] * p.iR[a];
                 const double ib3 = p.iR[b] * p.iR[b] * p.iR[b];
                 dJ5 = (ub * (3.0 * g.rho2 + 2.0 * ub * ub) * ib3 -
@@ -441,7 +472,7 @@ __device__ __forceinline__ void stress_moments(const SrcP0& s, const PairP0& p, 
     }
     const double I3 = p.I3, h2 = p.h2;
     const double third = 1.0 / 3.0, fifth = 0.2;
-    const double I5 = (h2 > 1e-60) ? (BD003 + I3) / (3.0 * h2) : 0.0;
+    const double I5 = (h2 > 1e-60) ? (BD003 + I3) * p.ih2 * third : 0.0;
     M.z = p.z;
     M.I3 = I3;
     M.m3_10 = -BN1m1;
@@ -457,7 +488,7 @@ __device__ __forceinline__ void stress_moments(const SrcP0& s, const PairP0& p, 
     M.M5[1][2] = -b3_1_02 * third;
     M.M5[0][3] = (2.0 * M.m3_01 - b3_2_02) * third;
     if (NEED7) {
-        const double I7 = (h2 > 1e-60) ? (BD005 + 3.0 * I5) / (5.0 * h2) : 0.0;
+        const double I7 = (h2 > 1e-60) ? (BD005 + 3.0 * I5) * p.ih2 * fifth : 0.0;
         M.M7[0][0] = I7;
         M.M7[1][0] = -b5_1_00 * fifth;
         M.M7[0][1] = -b5_2_00 * fifth;

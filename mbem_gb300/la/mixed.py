@@ -1,0 +1,128 @@
+"""Mixed-precision operator: FP32 far field (dense, quadrature) plus FP64 near
+field (closed form, 3x3 blocks in CSR by field point).
+
+``far_near_block`` assembles one kernel block both ways; ``MixedOperator``
+holds the blocks of a system and applies it (far part in double-float
+arithmetic, near part in FP64) through the C ABI.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from .. import _native as nat
+from .. import defaults
+from .._device import ptr, stream_handle
+
+
+@dataclass
+class NearList:
+    row0: int               # first row of the block in the system (3 per field point)
+    col0: int               # first column of the block in the system
+    n_field: int
+    rowptr: torch.Tensor    # (n_field + 1,) int64
+    cols: torch.Tensor      # (nnz,) int64
+    vals: torch.Tensor      # (nnz, 9) float64
+
+    @property
+    def nnz(self) -> int:
+        return int(self.cols.numel())
+
+
+_KERNEL_ID = {"T": 0, "U": 1}
+
+
+def near_list(x_field: torch.Tensor, tri_verts: torch.Tensor, eps: torch.Tensor,
+              near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR):
+    """(rowptr, cols) of the near pairs, sources in increasing order."""
+    nf, ns = x_field.shape[0], tri_verts.shape[0]
+    dev = x_field.device
+    rowptr = torch.empty(nf + 1, dtype=torch.int64, device=dev)
+    work = torch.empty(int(nat.lib().mbem_near_list_workspace_size(nf)), dtype=torch.uint8, device=dev)
+    nnz = ctypes.c_int64(0)
+    nat.call("mbem_near_count", ptr(x_field), nf, ptr(tri_verts), ptr(eps), ns, float(near_factor),
+             ptr(rowptr), ptr(work), work.numel(), ctypes.byref(nnz), stream_handle())
+    cols = torch.empty(max(nnz.value, 1), dtype=torch.int64, device=dev)[:nnz.value]
+    nat.call("mbem_near_fill", ptr(x_field), nf, ptr(tri_verts), ptr(eps), ns, float(near_factor),
+             ptr(rowptr), ptr(cols), stream_handle())
+    return rowptr, cols
+
+
+def far_near_block(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha: float,
+                   far_out: torch.Tensor, row0: int = 0, col0: int = 0,
+                   near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, timer=None) -> NearList:
+    """Writes alpha * (far part) into ``far_out`` (FP32 (3Nf, 3Ns) view, zeros
+    at near pairs) and returns the near blocks alpha * (closed form) in FP64."""
+    k = _KERNEL_ID[kernel]
+    nf, ns = x_field.shape[0], tri_verts.shape[0]
+    if far_out.dtype != torch.float32 or far_out.stride(1) != 1 or tuple(far_out.shape) != (3 * nf, 3 * ns):
+        raise ValueError("far_out must be a float32 (3Nf, 3Ns) view with unit column stride")
+    c = nat.dbl_array(coeffs)
+    ev = None
+    if timer is not None:
+        ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        ev[0].record()
+    nat.call("mbem_far_matrix", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ns, c,
+             float(near_factor), float(alpha), ptr(far_out), far_out.stride(0), stream_handle())
+    if ev is not None:
+        ev[1].record()
+        timer.append(("far_" + kernel, nf, ns, ev[0], ev[1]))
+    rowptr, cols = near_list(x_field, tri_verts, eps, near_factor)
+    vals = torch.empty((max(cols.numel(), 1), 9), dtype=torch.float64, device=x_field.device)[:cols.numel()]
+    nat.call("mbem_near_eval", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ptr(rowptr),
+             ptr(cols), cols.numel(), c, float(alpha), ptr(vals), stream_handle())
+    return NearList(row0, col0, nf, rowptr, cols, vals)
+
+
+class MixedOperator:
+    """A = A32 (FP32 dense far field) + sum of near-block lists (FP64)."""
+
+    def __init__(self, A32: torch.Tensor, near: list[NearList]):
+        self.A32 = A32
+        self.near = near
+        self._keep = None
+
+    @property
+    def n(self) -> int:
+        return int(self.A32.shape[0])
+
+    def struct(self, n_rows=None, n_cols=None) -> nat.MixedOperator:
+        arr = (nat.NearBlocks * max(len(self.near), 1))()
+        for i, nb in enumerate(self.near):
+            arr[i] = nat.NearBlocks(nb.row0, nb.col0, nb.n_field, ptr(nb.rowptr), ptr(nb.cols), ptr(nb.vals))
+        self._keep = arr
+        return nat.MixedOperator(self.A32.shape[0] if n_rows is None else n_rows,
+                                 self.A32.shape[1] if n_cols is None else n_cols, ptr(self.A32),
+                                 self.A32.stride(0), len(self.near), arr)
+
+    def matvec(self, x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        x = x.to(torch.float64).contiguous()
+        y = out if out is not None else torch.empty(self.A32.shape[0], dtype=torch.float64, device=x.device)
+        work = torch.empty(2 * x.numel() * 4 + 64, dtype=torch.uint8, device=x.device)
+        op = self.struct()
+        nat.call("mbem_mixed_matvec", ctypes.byref(op), ptr(x), ptr(y), ptr(work), work.numel(),
+                 stream_handle())
+        return y
+
+    def rowsum3(self, row0: int, rows: int, col0: int, cols: int, near: NearList) -> torch.Tensor:
+        """(rows/3, 3, 3) calibration row sums of one block (far + its near list)."""
+        out = torch.empty((rows // 3, 3, 3), dtype=torch.float64, device=self.A32.device)
+        view = self.A32[row0:row0 + rows, col0:col0 + cols]
+        nat.call("mbem_mixed_rowsum3", ptr(view), view.stride(0), rows, cols // 3, ptr(near.rowptr),
+                 ptr(near.vals), ptr(out), stream_handle())
+        return out
+
+    def dense64(self) -> torch.Tensor:
+        """The operator as an FP64 dense matrix (tests and small systems only)."""
+        A = self.A32.to(torch.float64)
+        for nb in self.near:
+            rp = nb.rowptr.cpu().numpy()
+            f = torch.from_numpy(np.repeat(np.arange(nb.n_field), np.diff(rp))).to(A.device)
+            for i in range(3):
+                for j in range(3):
+                    A[nb.row0 + 3 * f + i, nb.col0 + 3 * nb.cols + j] += nb.vals[:, 3 * i + j]
+        return A

@@ -39,6 +39,17 @@ class SolveReport:
         return f"FGMRES {status}: {self.iterations} iters, true relres {self.true_relres:.3e}"
 
 
+def fgmres_mixed(op, b: torch.Tensor, x0: torch.Tensor | None = None,
+                 rtol: float = defaults.GMRES_RTOL, restart: int = defaults.GMRES_RESTART,
+                 maxiter: int = defaults.GMRES_MAXITER,
+                 stagnation_window: int = defaults.GMRES_STAGNATION_WINDOW,
+                 stagnation_factor: float = defaults.GMRES_STAGNATION_FACTOR,
+                 u_ranges=(), workspace: torch.Tensor | None = None):
+    """FGMRES on a ``la.mixed.MixedOperator`` (same contract as fgmres_dense)."""
+    return _fgmres(None, op, b, x0, rtol, restart, maxiter, stagnation_window, stagnation_factor,
+                   u_ranges, workspace)
+
+
 def fgmres_dense(A: torch.Tensor, b: torch.Tensor, x0: torch.Tensor | None = None,
                  rtol: float = defaults.GMRES_RTOL, restart: int = defaults.GMRES_RESTART,
                  maxiter: int = defaults.GMRES_MAXITER,
@@ -48,16 +59,23 @@ def fgmres_dense(A: torch.Tensor, b: torch.Tensor, x0: torch.Tensor | None = Non
     """Solve A x = b for a dense FP64 CUDA matrix. ``u_ranges`` = [(offset,
     size), ...] of the u-slots to deflate (empty: no deflation).
     Returns (x, SolveReport)."""
-    n = b.shape[0]
-    if A.dtype != torch.float64 or not A.is_cuda or A.shape[0] != n or A.stride(1) != 1:
+    if A.dtype != torch.float64 or not A.is_cuda or A.shape[0] != b.shape[0] or A.stride(1) != 1:
         raise ValueError("A must be a float64 CUDA matrix (n, n) with unit column stride")
-    b = b.to(dtype=torch.float64, device=A.device).contiguous()
-    x = (torch.zeros(n, dtype=torch.float64, device=A.device) if x0 is None
-         else x0.to(dtype=torch.float64, device=A.device).clone().contiguous())
+    return _fgmres(A, None, b, x0, rtol, restart, maxiter, stagnation_window, stagnation_factor,
+                   u_ranges, workspace)
+
+
+def _fgmres(A, mop, b, x0, rtol, restart, maxiter, stagnation_window, stagnation_factor, u_ranges,
+            workspace):
+    n = b.shape[0]
+    dev = (A if A is not None else mop.A32).device
+    b = b.to(dtype=torch.float64, device=dev).contiguous()
+    x = (torch.zeros(n, dtype=torch.float64, device=dev) if x0 is None
+         else x0.to(dtype=torch.float64, device=dev).clone().contiguous())
     restart = int(min(restart, maxiter))
     need = nat.lib().mbem_fgmres_workspace_size(n, restart)
     if workspace is None or workspace.numel() * workspace.element_size() < need:
-        workspace = torch.empty(need, dtype=torch.uint8, device=A.device)
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
     rng = np.ascontiguousarray(np.asarray(u_ranges, dtype=np.int64).reshape(-1))
     prm = nat.FgmresParams(restart=restart, maxiter=int(maxiter), rtol=float(rtol),
                            stagnation_window=int(stagnation_window),
@@ -68,8 +86,13 @@ def fgmres_dense(A: torch.Tensor, b: torch.Tensor, x0: torch.Tensor | None = Non
     hist = np.zeros(max(int(maxiter), 1))
     rep = nat.FgmresReport()
     rep.history = hist.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    nat.call("mbem_fgmres_dense", ptr(A), A.stride(0), n, ptr(b), ptr(x), ctypes.byref(prm),
-             ptr(workspace), need, ctypes.byref(rep), stream_handle())
+    if A is not None:
+        nat.call("mbem_fgmres_dense", ptr(A), A.stride(0), n, ptr(b), ptr(x), ctypes.byref(prm),
+                 ptr(workspace), need, ctypes.byref(rep), stream_handle())
+    else:
+        op = mop.struct()
+        nat.call("mbem_fgmres_mixed", ctypes.byref(op), ptr(b), ptr(x), ctypes.byref(prm),
+                 ptr(workspace), need, ctypes.byref(rep), stream_handle())
     report = SolveReport(converged=bool(rep.converged), iterations=int(rep.iterations),
                          true_relres=float(rep.true_relres), arnoldi_relres=float(rep.arnoldi_relres),
                          stagnated=bool(rep.stagnated), restarts=int(rep.restarts),

@@ -1,0 +1,85 @@
+"""Mixed-precision operator (FP32 quadrature far field + FP64 near blocks)
+against the FP64 closed-form operator.
+
+Stated tolerances (mixed mode): far entries within 1e-6 of the largest
+far entry of the matrix, near entries equal to the FP64 operator's to 1e-13
+of max|A|, the mixed matvec equal to the mixed operator applied in FP64 to
+1e-13, and the mixed solution within 1e-5 of the FP64 solution.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def systems(gpu):
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.model import generate_system
+    model, eps = cube_fault_model(8, 4, 1.3, 1.95)
+    system = generate_system(model)
+    a64 = DenseBackend(jump="calibrated", deflate=True, rtol=1e-12).assemble(system, eps)
+    amx = DenseBackend(jump="calibrated", deflate=True, rtol=1e-12, precision="mixed").assemble(system, eps)
+    return a64, amx
+
+
+def test_mixed_operator_entries(systems):
+    a64, amx = systems
+    A = a64.A.cpu().numpy()
+    M = amx.op.dense64().cpu().numpy()
+    nl = amx.op.near[0]
+    near = np.zeros_like(A, dtype=bool)
+    rp = nl.rowptr.cpu().numpy()
+    f = np.repeat(np.arange(nl.n_field), np.diff(rp))
+    s = nl.cols.cpu().numpy()
+    for i in range(3):
+        for j in range(3):
+            near[3 * f + i, 3 * s + j] = True
+    # the 3x3 diagonal blocks carry each operator's own calibration (the row
+    # sums of that operator), so they are compared through the null space
+    diag = np.zeros_like(near)
+    for c in range(A.shape[0] // 3):
+        diag[3 * c:3 * c + 3, 3 * c:3 * c + 3] = True
+    scale = np.abs(A).max()
+    near_err = np.abs(M - A)[near & ~diag].max() / scale
+    far_err = np.abs(M - A)[~near].max() / np.abs(A[~near]).max()
+    diag_err = np.abs(M - A)[diag].max() / scale
+    print(f"near {near_err:.2e} far {far_err:.2e} diag {diag_err:.2e} near fraction {near.mean():.3f}")
+    assert near_err < 1e-13
+    assert far_err < 1e-6
+    assert diag_err < 1e-6
+    # every row has its self block, and the calibrated mixed operator
+    # annihilates rigid translations exactly
+    assert all(f0 in s[rp[f0]:rp[f0 + 1]] for f0 in range(nl.n_field))
+    from mbem_gb300.backends.dense import translation_basis
+    Z = translation_basis(amx.layout)
+    assert np.abs(M @ Z).max() < 1e-13 * scale
+
+
+def test_mixed_matvec_is_exact_for_its_operator(systems):
+    _, amx = systems
+    x = torch.randn(amx.op.n, dtype=torch.float64, device="cuda")
+    y = amx.op.matvec(x)
+    ref = amx.op.dense64() @ x
+    assert rel_err(y.cpu().numpy(), ref.cpu().numpy()) < 1e-13
+
+
+def test_mixed_solution_against_fp64(systems):
+    a64, amx = systems
+    x64 = a64.solve_device()
+    xmx = amx.solve_device()
+    assert a64.report.converged and amx.report.converged
+    err = float((xmx - x64).norm() / x64.norm())
+    # the FP64 operator's residual of the mixed solution
+    Pb = a64.b.clone()
+    r = (a64.A @ xmx - a64.b)
+    print(f"mixed vs fp64 solution {err:.2e}; its(fp64) {a64.report.iterations} "
+          f"its(mixed) {amx.report.iterations}")
+    assert err < 1e-5
+    assert amx.report.true_relres < 1e-12
+    del Pb, r
