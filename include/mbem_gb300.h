@@ -183,6 +183,18 @@ int mbem_near_add_diagonal(const int64_t* rowptr, const int64_t* cols, double* v
  * y (n_rows) is overwritten. work >= 2 n_cols floats + 64 bytes. */
 int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, void* work,
                       size_t work_bytes, void* stream);
+/* The same product for callers that cannot allocate device memory (a host that
+ * gives all device memory to its own pool at start-up, or a loop that must not
+ * enter the allocator): no workspace argument, and nothing allocated. Its
+ * scratch is a fixed 2 MiB array inside the library, held by every GPU that
+ * loads it until exit, so n_cols is limited to 262144 (larger sizes return
+ * MBEM_ERR_SIZE). The first call on each device looks the array's device
+ * address up (cudaGetSymbolAddress) and must come before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller.
+ * It has no counterpart in the reference. */
+int mbem_mixed_matvec_noalloc(const mbem_mixed_operator* op, const double* x, double* y,
+                              void* stream);
 
 /* ---- deflated FGMRES on a dense operator (la/solver.py:115-245 fgmres,
  * wired as backends/hmat.py:678-690: P A P y = P b, P = I - Z Z^T with Z

@@ -96,6 +96,7 @@ _SIGNATURES = {
     "mbem_mixed_rowsum3": (c_int, [_P, _I, _I, _I, _P, _P, _P, _P]),
     "mbem_near_add_diagonal": (c_int, [_P, _P, _P, _I, _P, _P, _P]),
     "mbem_mixed_matvec": (c_int, [POINTER(MixedOperator), _P, _P, _P, c_size_t, _P]),
+    "mbem_mixed_matvec_noalloc": (c_int, [POINTER(MixedOperator), _P, _P, _P]),
 }
 
 _lib = None

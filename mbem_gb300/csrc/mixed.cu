@@ -21,6 +21,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 #include "p0_pair.cuh"
@@ -723,3 +724,64 @@ int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// The mixed matvec for callers that cannot allocate device memory.
+//
+// Some hosts of this library never call cudaMalloc: a solver embedded in an
+// application that hands every byte of device memory to its own pool at
+// start-up, a real-time loop that must not take the allocator's locks or its
+// synchronisation, or code running where a new allocation would fail the
+// memory budget it was given. mbem_mixed_matvec needs 2 n_cols floats of
+// scratch (the hi/lo split of x) from such a caller. This variant instead
+// keeps that scratch in a fixed array compiled into the library: every GPU
+// that loads the library holds it (2 MiB) until the process exits.
+// ---------------------------------------------------------------------------
+namespace mbem {
+
+constexpr int64_t NOALLOC_MAX_COLS = 262144;          // 2 x 262144 floats = 2 MiB
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) float g_noalloc_split[2 * NOALLOC_MAX_COLS];
+
+static std::mutex g_noalloc_mutex;
+static float* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side name of a __device__ array is not a device
+// address and must never be passed to a kernel).
+static int noalloc_scratch(float** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return set_error(MBEM_ERR_UNSUPPORTED, "device ordinal %d beyond %d", dev, NOALLOC_MAX_DEVICES);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_split);
+        if (e != cudaSuccess)
+            return set_error(MBEM_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = static_cast<float*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return MBEM_OK;
+}
+
+}  // namespace mbem
+
+extern "C" int mbem_mixed_matvec_noalloc(const mbem_mixed_operator* op, const double* x, double* y,
+                                         void* stream) {
+    MBEM_REQUIRE(op && x && y && op->n_rows >= 0 && op->n_cols >= 0 && op->ld32 >= op->n_cols, MBEM_ERR_ARG,
+                 "bad mixed matvec args");
+    MBEM_REQUIRE(op->n_cols <= mbem::NOALLOC_MAX_COLS, MBEM_ERR_SIZE,
+                 "mbem_mixed_matvec_noalloc: n_cols = %lld exceeds its fixed scratch of %lld columns; use "
+                 "mbem_mixed_matvec with a workspace",
+                 (long long)op->n_cols, (long long)mbem::NOALLOC_MAX_COLS);
+    float* scratch = nullptr;
+    int e = mbem::noalloc_scratch(&scratch);
+    if (e) return e;
+    // Nothing in the scratch has to start at zero: the split kernel writes
+    // entries 0 .. n_cols-1 of both halves before the product reads them.
+    return mbem::mixed_matvec(op, x, y, scratch, scratch + mbem::NOALLOC_MAX_COLS, (cudaStream_t)stream);
+}
