@@ -1,12 +1,17 @@
 """Time-to-solve benchmark of the dense mollified-BEM hot path on one GB300.
 
-One step = one complete solve of the workload: assemble the FP64 collocation
-matrix of the calibrated dense backend (CUDA pair kernels, straight into
+One step = one complete solve of the workload: assemble the collocation
+operator of the calibrated dense backend (CUDA pair kernels, straight into
 HBM), the calibration row sums and free-term diagonal, the fault right-hand
 side, then deflated FGMRES(50) on the device to a true relative residual of
-1e-8. ``value`` is seconds per solve with the mesh arrays already resident
-in HBM; ``e2e`` is the same through the public API from host numpy arrays
-(model -> assemble -> solve -> numpy solution), host<->device copies inside.
+1e-8. The headline (``--precision mixed``, default) is the mixed-precision
+operator (FP32 quadrature far field, FP64 closed-form near field; its
+residual evaluated in double-float); the plain FP64 path on the same
+workload is timed beside it (``fp64_path``) for the mixed/FP64 ratio the
+metric names. ``value`` is seconds per solve with the mesh arrays already
+resident in HBM; ``e2e`` is the same through the public API from host numpy
+arrays (model -> assemble -> solve -> numpy solution), host<->device copies
+inside.
 
 Workloads (mesh: traction-free cube of side 4, n x n squares per face, two
 triangles each; vertical fault 1 x 1 at the centre, uniform slip (1,0,0);
@@ -162,6 +167,23 @@ def fp64_peak_tflops():
 # our arm
 # ---------------------------------------------------------------------------
 
+def _timed_steps(step, steps, ws):
+    """Runs ``steps`` steps between barriers + syncs; returns (device s per
+    step as max over ranks, wall s per step, per-step results)."""
+    import torch
+    torch.cuda.synchronize()
+    _barrier(ws)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    start.record()
+    out = [step() for _ in range(steps)]
+    end.record()
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / steps
+    dev = _max_over_ranks(start.elapsed_time(end) / 1e3 / steps, ws)
+    return dev, wall, out
+
+
 def run_ours(args, rank, ws):
     import torch
     from mbem_gb300 import _native as nat
@@ -175,46 +197,47 @@ def run_ours(args, rank, ws):
     model, eps = cube_fault_model(cfg["n_face"], cfg["n_fault"])
     system = generate_system(model)
     n = system.layout.n_unknowns
-    backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART,
-                           precision=args.precision)
     arrays = {}     # device-resident mesh arrays, filled by the first assembly
 
-    def step(timer=None):
-        asm = backend.assemble(system, eps, arrays=arrays, timer=timer)
-        x = asm.solve_device()
-        rep = asm.report
-        asm.A = None
-        asm.op = None
-        return x, rep
+    def make_step(precision, timer=None):
+        backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART,
+                               precision=precision)
 
+        def step():
+            asm = backend.assemble(system, eps, arrays=arrays, timer=timer)
+            asm.solve_device(time_matvec=True)
+            rep = asm.report
+            nnz = sum(nl.nnz for nl in asm.op.near) if asm.op is not None else 0
+            asm.A = None
+            asm.op = None
+            return rep, nnz
+        return step
+
+    # headline: the mixed-precision path
+    timer = []
+    step = make_step(args.precision, timer)
     for _ in range(args.warmup):
         step()
-    torch.cuda.synchronize()
-    _barrier(ws)
-
-    timer = []
-    reps = []
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    timer.clear()
     launches0 = nat.lib().mbem_launch_count()
     with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        start.record()
-        for _ in range(args.steps):
-            _, rep = step(timer)
-            reps.append(rep)
-        end.record()
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
+        dev_s, wall, res = _timed_steps(step, args.steps, ws)
     launches = nat.lib().mbem_launch_count() - launches0
-    dev_s = start.elapsed_time(end) / 1e3 / args.steps
-    dev_s = _max_over_ranks(dev_s, ws)
+    rep, nnz = res[-1]
 
-    # the dominant kernel: the FP64 T-kernel assembly (one launch per block)
-    asm_ms = [s.elapsed_time(e) for (k, nf, ns, s, e) in timer]
-    pairs = [nf * ns for (k, nf, ns, s, e) in timer]
-    asm_launch_ms = float(np.mean(asm_ms))
-    pairs_per_launch = float(np.mean(pairs))
+    # the plain FP64 path on the same workload, for the ratio the metric names
+    fp64 = None
+    if args.precision != "fp64" and not args.skip_fp64:
+        timer64 = []
+        step64 = make_step("fp64", timer64)
+        step64()
+        timer64.clear()
+        dev64, wall64, res64 = _timed_steps(step64, max(1, args.fp64_steps), ws)
+        asm64 = [s.elapsed_time(e) for (k, nf, ns, s, e) in timer64 if k == "H"]
+        fp64 = {"ms_per_step": dev64 * 1e3, "iterations": res64[-1][0].iterations,
+                "true_relres": res64[-1][0].true_relres, "steps": max(1, args.fp64_steps),
+                "assembly_ms_per_step": float(np.sum(asm64)) / max(1, args.fp64_steps),
+                "speedup_mixed_vs_fp64": dev64 / dev_s}
 
     # end to end through the public API from host arrays
     e2e = None
@@ -223,6 +246,8 @@ def run_ours(args, rank, ws):
         from mbem_gb300.model import BCType, Patch, Region, RegionModel
         host_cube = M.cube(cfg["n_face"])
         host_fault = M.centre_fault(cfg["n_fault"])
+        backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART,
+                               precision=args.precision)
 
         def e2e_step():
             cube_p = Patch("cube", host_cube, BCType.FREE_TRACTION)
@@ -232,6 +257,7 @@ def run_ours(args, rank, ws):
             asm = backend.assemble(generate_system(m), eps)
             sol = asm.solve()
             asm.A = None
+            asm.op = None
             return sol
 
         e2e_step()
@@ -247,9 +273,24 @@ def run_ours(args, rank, ws):
         e2e = {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 8 * n}
 
     peaks = measured_peaks()
-    fp64 = fp64_peak_tflops()
-    flop_pair = FLOP_PER_T_PAIR
-    achieved = flop_pair * pairs_per_launch / (asm_launch_ms / 1e3) / 1e12
+    hbm_peak = peaks.get("hbm_gbs") or 6800.0
+    mv_ms = rep.matvec_ms / max(1, rep.matvecs)
+    if args.precision == "mixed":
+        # the mixed matvec: the FP32 far field once, the near blocks (72 B +
+        # an 8 B index each), x read, y written
+        mv_bytes = 4.0 * n * n + 80.0 * nnz + 16.0 * n
+        kernel = "mixed matvec (split_vec + sgemv_df_tma_kernel + near_matvec_kernel)"
+    else:
+        mv_bytes = 8.0 * n * n + 16.0 * n
+        kernel = "dgemv_vec_kernel"
+    achieved = mv_bytes / (mv_ms / 1e3) / 1e9
+    roofline = {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak,
+                "traffic": TRAFFIC_OVER_ALGORITHMIC * mv_bytes if args.precision == "mixed" else None,
+                "bytes_per_launch": mv_bytes, "launch_ms": mv_ms, "launches_per_step": rep.matvecs,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks.get("hbm_gbs")
+                else "fallback 6.8 TB/s (of fallback)"}
+    asm_ms = [s.elapsed_time(e) for (k, nf, ns, s, e) in timer]
     line = {
         "metric": METRIC,
         "value": dev_s,
@@ -266,33 +307,32 @@ def run_ours(args, rank, ws):
         "config": {"workload": args.workload, "n_face": cfg["n_face"], "n_fault": cfg["n_fault"],
                    "unknowns": n, "precision": args.precision, "solver": f"deflated FGMRES({RESTART})",
                    "rtol": RTOL, "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "inputs larger than L2 (A = %.1f GB FP64)" % (8.0 * n * n / 1e9)},
-        "iterations": reps[-1].iterations,
-        "true_relres": reps[-1].true_relres,
-        "wall_s_per_step": wall / args.steps,
+                   "l2": "inputs larger than L2 (A = %.1f GB FP32 far field)" % (4.0 * n * n / 1e9)
+                   if args.precision == "mixed" else
+                   "inputs larger than L2 (A = %.1f GB FP64)" % (8.0 * n * n / 1e9)},
+        "iterations": rep.iterations,
+        "true_relres": rep.true_relres,
+        "wall_s_per_step": wall,
+        "matvec_ms_per_step": rep.matvec_ms,
+        "assembly_kernels_ms_per_step": float(np.sum(asm_ms)) / args.steps,
+        "fp64_path": fp64,
         "e2e": e2e,
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "p0_matrix_kernel<T_DIRECT>", "bound": "fp64",
-                     "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
-                     "frac": achieved / fp64, "traffic": None,
-                     "flop_per_pair": flop_pair, "pairs_per_launch": pairs_per_launch,
-                     "launch_ms": asm_launch_ms,
-                     "peak_source": "own DFMA probe (mbem_fp64_fma_probe), measured in this run"},
-        "assembly_share": float(np.sum(asm_ms)) / 1e3 / args.steps / dev_s,
-        "measured_peaks": {k: peaks.get(k) for k in ("hbm_gbs", "bf16_tflops")},
+        "roofline": roofline,
+        "fp64_peak_tflops": fp64_peak_tflops(),
     }
     clocks = clk.summary()
     if clocks:
         line["clocks"] = clocks
     if rank == 0 and not args.skip_cpu:
-        line["cpu_baseline"] = cpu_baseline(args, reps[-1].iterations)
+        line["cpu_baseline"] = cpu_baseline(args, rep.iterations)
     return line
 
 
-# FP64 operations per T-kernel pair of the CUDA formulation, counted from
-# the source of p0_pair.cuh (t_moments + t_block; FMA = 2, add/mul = 1,
-# each sqrt/div/log/atan2 = 1).
-FLOP_PER_T_PAIR = 480.0
+# DRAM bytes over algorithmic bytes of the mixed matvec, from the ncu capture
+# of sgemv_df_tma_kernel at 20,736 unknowns (profiles/): 1.720 GB read for a
+# 1.720 GB FP32 matrix.
+TRAFFIC_OVER_ALGORITHMIC = 1.0
 
 
 # ---------------------------------------------------------------------------
@@ -384,7 +424,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=2)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -154,10 +154,18 @@ typedef struct {
 /* FP32 far-field block (kernel 0 = T with 6 coeffs, 1 = U with 3) of
  * alpha * M into out (3Nf, 3Ns) at ld_out; near pairs (centroid distance
  * below near_factor * max(eps, mean edge), or below 1.5 longest edge) are
- * written as zeros. */
+ * written as zeros. near_mask (optional, device, n_field x ceil(Ns/32)
+ * uint32) receives one bit per near pair, source s at word s/32, bit s%32. */
 int mbem_far_matrix(int kernel, const double* x_field, int64_t n_field, const double* tri_verts,
                     const double* normals, const double* eps, int64_t n_src, const double* coeffs,
-                    double near_factor, double alpha, float* out, int64_t ld_out, void* stream);
+                    double near_factor, double alpha, float* out, int64_t ld_out, uint32_t* near_mask,
+                    void* stream);
+/* Near list from that bit mask: rowptr (n_field+1) and nnz on the host
+ * (synchronises `stream`), then the source indices in increasing order. */
+int mbem_near_mask_count(const uint32_t* mask, int64_t n_field, int64_t n_src, int64_t* rowptr,
+                         void* work, size_t work_bytes, int64_t* nnz_host, void* stream);
+int mbem_near_mask_fill(const uint32_t* mask, int64_t n_field, int64_t n_src, const int64_t* rowptr,
+                        int64_t* cols, void* stream);
 /* Near list, pass 1: rowptr (n_field+1) device; nnz returned on the host
  * (the call synchronises `stream`). work >= mbem_near_list_workspace_size. */
 size_t mbem_near_list_workspace_size(int64_t n_field);
@@ -209,6 +217,7 @@ typedef struct {
     const int64_t* u_ranges;/* HOST array of 2*n_u_ranges int64 */
     int precond;            /* 0 none, 1 block-Jacobi (mbem_bj_*), 2 learned (mbem_nn_*) */
     const void* precond_state; /* the preconditioner object for precond != 0 */
+    int time_matvec;        /* 1: time every operator application with CUDA events */
 } mbem_fgmres_params;
 
 typedef struct {
@@ -219,6 +228,8 @@ typedef struct {
     double true_relres;
     double arnoldi_relres;
     double* history;        /* optional HOST array of maxiter doubles, filled if non-NULL */
+    int matvecs;            /* operator applications (A x products) */
+    double matvec_ms;       /* their total device time when params->time_matvec */
 } mbem_fgmres_report;
 
 /* Bytes of device workspace mbem_fgmres_dense / mbem_fgmres_mixed need for
@@ -240,8 +251,8 @@ int mbem_fgmres_dense(const double* A, int64_t ld, int64_t n, const double* b, d
                       const mbem_fgmres_params* params, void* work, size_t work_bytes,
                       mbem_fgmres_report* report, void* stream);
 
-/* The deflation projection v_out = P v_in (hmat.py:684-685 proj). work:
- * 3 doubles of device memory. */
+/* The deflation projection v_out = P v_in (hmat.py:684-685 proj); v_out may
+ * alias v_in. work: 384 doubles of device memory (partial sums). */
 int mbem_project_translation(const double* v_in, double* v_out, int64_t n,
                              const int64_t* u_ranges, int n_u_ranges, double* work,
                              void* stream);

@@ -39,13 +39,13 @@ class FgmresParams(Structure):
     _fields_ = [("restart", c_int), ("maxiter", c_int), ("rtol", c_double),
                 ("stagnation_window", c_int), ("stagnation_factor", c_double),
                 ("n_u_ranges", c_int), ("u_ranges", POINTER(c_int64)),
-                ("precond", c_int), ("precond_state", c_void_p)]
+                ("precond", c_int), ("precond_state", c_void_p), ("time_matvec", c_int)]
 
 
 class FgmresReport(Structure):
     _fields_ = [("converged", c_int), ("iterations", c_int), ("restarts", c_int),
                 ("stagnated", c_int), ("true_relres", c_double), ("arnoldi_relres", c_double),
-                ("history", POINTER(c_double))]
+                ("history", POINTER(c_double)), ("matvecs", c_int), ("matvec_ms", c_double)]
 
 
 class NearBlocks(Structure):
@@ -88,7 +88,9 @@ _SIGNATURES = {
                                   POINTER(FgmresReport), _P]),
     "mbem_fgmres_mixed": (c_int, [POINTER(MixedOperator), _P, _P, POINTER(FgmresParams), _P, c_size_t,
                                   POINTER(FgmresReport), _P]),
-    "mbem_far_matrix": (c_int, [c_int, _P, _I, _P, _P, _P, _I, _P, _D, _D, _P, _I, _P]),
+    "mbem_far_matrix": (c_int, [c_int, _P, _I, _P, _P, _P, _I, _P, _D, _D, _P, _I, _P, _P]),
+    "mbem_near_mask_count": (c_int, [_P, _I, _I, _P, _P, c_size_t, POINTER(c_int64), _P]),
+    "mbem_near_mask_fill": (c_int, [_P, _I, _I, _P, _P, _P]),
     "mbem_near_list_workspace_size": (c_size_t, [_I]),
     "mbem_near_count": (c_int, [_P, _I, _P, _P, _I, _D, _P, _P, c_size_t, POINTER(c_int64), _P]),
     "mbem_near_fill": (c_int, [_P, _I, _P, _P, _I, _D, _P, _P, _P]),

@@ -383,12 +383,13 @@ class AssembledDense:
         return [(s.offset, s.size) for s in self.layout.slots if s.kind == "u"]
 
     def solve_device(self, rtol: float | None = None, restart: int | None = None,
-                     maxiter: int | None = None, x0=None) -> torch.Tensor:
+                     maxiter: int | None = None, x0=None, time_matvec: bool = False) -> torch.Tensor:
         """FGMRES on the device; returns the solution vector as a CUDA tensor
         and leaves ``self.report``."""
         kw = dict(x0=x0, rtol=self.rtol if rtol is None else rtol,
                   restart=self.restart if restart is None else restart,
-                  maxiter=self.maxiter if maxiter is None else maxiter, u_ranges=self.u_ranges())
+                  maxiter=self.maxiter if maxiter is None else maxiter, u_ranges=self.u_ranges(),
+                  time_matvec=time_matvec)
         if self.op is not None:
             x, rep = fgmres_mixed(self.op, self.b, **kw)
         else:

@@ -35,6 +35,10 @@ int nodal_contract(int kind, const double* x, int64_t nf, const double* tv, cons
 int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, float* xh, float* xl,
                  cudaStream_t st);
 
+// MBEM_ERR_WAIT if a bounded pipeline wait of the mixed matvec gave up since
+// the last check; synchronises `st`.
+int mixed_wait_check(cudaStream_t st);
+
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 __host__ __device__ inline int64_t lmin(int64_t a, int64_t b) { return a < b ? a : b; }
 

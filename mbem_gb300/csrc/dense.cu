@@ -10,6 +10,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -251,18 +252,21 @@ struct URanges {
     int n;
 };
 
-constexpr int PROJ_THREADS = 1024;
+// Two passes over the whole grid: per-block partial sums of each component
+// over the u-slots (fixed block count, fixed order), then every block forms
+// the three means from the partials and subtracts them from its entries.
+constexpr int PROJ_THREADS = 256;
+constexpr int PROJ_BLOCKS = 128;     // partial sums: 3 * PROJ_BLOCKS doubles
 
 __global__ void __launch_bounds__(PROJ_THREADS)
-project_kernel(const double* __restrict__ vin, double* __restrict__ vout, int64_t n, URanges ur) {
+proj_partial_kernel(const double* __restrict__ vin, URanges ur, double* __restrict__ partial) {
     __shared__ double red[PROJ_THREADS / 32][3];
-    __shared__ double mean[3];
     double acc[3] = {0.0, 0.0, 0.0};
-    int64_t total = 0;
+    const int64_t stride = (int64_t)gridDim.x * PROJ_THREADS;
     for (int q = 0; q < ur.n; q++) {
         const int64_t off = ur.off[q], len = ur.len[q];
-        total += len;
-        for (int64_t t = threadIdx.x; t < len; t += PROJ_THREADS) acc[t % 3] += vin[off + t];
+        for (int64_t t = (int64_t)blockIdx.x * PROJ_THREADS + threadIdx.x; t < len; t += stride)
+            acc[t % 3] += vin[off + t];
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -274,18 +278,40 @@ project_kernel(const double* __restrict__ vin, double* __restrict__ vout, int64_
     __syncthreads();
     if (threadIdx.x < 3) {
         double s = 0.0;
-        for (int q = 0; q < PROJ_THREADS / 32; q++) s += red[q][threadIdx.x];
+        for (int w = 0; w < PROJ_THREADS / 32; w++) s += red[w][threadIdx.x];
+        partial[3 * blockIdx.x + threadIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(PROJ_THREADS)
+proj_apply_kernel(const double* __restrict__ vin, double* __restrict__ vout, int64_t n, URanges ur,
+                  const double* __restrict__ partial, int nparts) {
+    __shared__ double mean[3];
+    if (threadIdx.x < 3) {
+        double s = 0.0;
+        for (int b = 0; b < nparts; b++) s += partial[3 * b + threadIdx.x];
+        int64_t total = 0;
+        for (int q = 0; q < ur.n; q++) total += ur.len[q];
         // Z_k = 1/sqrt(M) on component-k u entries: Z (Z^T v) = sum / M
         mean[threadIdx.x] = (total > 0) ? s / (double)(total / 3) : 0.0;
     }
     __syncthreads();
-    if (vout != vin)
-        for (int64_t c = threadIdx.x; c < n; c += PROJ_THREADS) vout[c] = vin[c];
-    __syncthreads();
-    for (int q = 0; q < ur.n; q++) {
-        const int64_t off = ur.off[q], len = ur.len[q];
-        for (int64_t t = threadIdx.x; t < len; t += PROJ_THREADS) vout[off + t] = vin[off + t] - mean[t % 3];
+    for (int64_t c = (int64_t)blockIdx.x * PROJ_THREADS + threadIdx.x; c < n;
+         c += (int64_t)gridDim.x * PROJ_THREADS) {
+        double m = 0.0;
+        for (int q = 0; q < ur.n; q++)
+            if (c >= ur.off[q] && c < ur.off[q] + ur.len[q]) m = mean[(c - ur.off[q]) % 3];
+        vout[c] = vin[c] - m;
     }
+}
+
+// vout = P vin (vout may alias vin); partial holds 3 * PROJ_BLOCKS doubles
+static int project(const double* vin, double* vout, int64_t n, const URanges& ur, double* partial,
+                   cudaStream_t st) {
+    proj_partial_kernel<<<PROJ_BLOCKS, PROJ_THREADS, 0, st>>>(vin, ur, partial);
+    const unsigned g = (unsigned)lmin(ceil_div(n, PROJ_THREADS), 4 * 152);
+    proj_apply_kernel<<<g, PROJ_THREADS, 0, st>>>(vin, vout, n, ur, partial, PROJ_BLOCKS);
+    return launch_status("project", 2);
 }
 
 static int make_ranges(const int64_t* r, int nr, URanges& ur) {
@@ -317,6 +343,7 @@ struct FgmresWork {
     double* scal;     // 8
     float* xh;        // n (mixed operator: split of the matvec input)
     float* xl;        // n
+    double* proj;     // 3 * PROJ_BLOCKS projection partial sums
 };
 
 static size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -341,6 +368,7 @@ static size_t fgmres_layout(int64_t n, int m, char* base, FgmresWork* w) {
     tmp.scal = take(8);
     tmp.xh = reinterpret_cast<float*>(take((n + 1) / 2));
     tmp.xl = reinterpret_cast<float*>(take((n + 1) / 2));
+    tmp.proj = take(3 * PROJ_BLOCKS);
     if (w) *w = tmp;
     return off;
 }
@@ -360,17 +388,41 @@ struct Fgmres {
             if (in != out) cudaMemcpyAsync(out, in, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
             return launch_status("copy", 0);
         }
-        project_kernel<<<1, PROJ_THREADS, 0, st>>>(in, out, n, ur);
-        return launch_status("project_kernel");
+        return project(in, out, n, ur, W.proj, st);
     }
     // out = P A P in (uses W.t)
     int op(const double* in, double* out) {
         int e = proj(in, W.t);
         if (e) return e;
+        cudaEvent_t ev[2] = {nullptr, nullptr};
+        if (time_matvec) {
+            cudaEventCreate(&ev[0]);
+            cudaEventCreate(&ev[1]);
+            cudaEventRecord(ev[0], st);
+        }
         e = mop ? mixed_matvec(mop, W.t, out, W.xh, W.xl, st) : dgemv(A, ld, n, n, W.t, 1.0, 0.0, out, st);
+        matvecs++;
+        if (time_matvec) {
+            cudaEventRecord(ev[1], st);
+            pending.push_back({ev[0], ev[1]});
+        }
         if (e) return e;
         return proj(out, out);
     }
+    // accumulates the device time of the matvecs timed so far (after a sync)
+    void collect_times() {
+        for (auto& p : pending) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, p.first, p.second) == cudaSuccess) matvec_ms += ms;
+            cudaEventDestroy(p.first);
+            cudaEventDestroy(p.second);
+        }
+        pending.clear();
+    }
+    bool time_matvec = false;
+    int matvecs = 0;
+    double matvec_ms = 0.0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
     // h[0..k) (+)= V[0..k) . w
     int multidot(const double* V, int k, const double* w, double* h, int accumulate) {
         for (int i0 = 0; i0 < k; i0 += KV_MAXV) {
@@ -443,12 +495,12 @@ int mbem_dgemm_multi(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols
 
 int mbem_project_translation(const double* v_in, double* v_out, int64_t n, const int64_t* u_ranges,
                              int n_u_ranges, double* work, void* stream) {
-    (void)work;
     URanges ur;
     int e = make_ranges(u_ranges, n_u_ranges, ur);
     if (e) return e;
-    project_kernel<<<1, PROJ_THREADS, 0, (cudaStream_t)stream>>>(v_in, v_out, n, ur);
-    return launch_status("project_kernel");
+    MBEM_REQUIRE(work != nullptr, MBEM_ERR_ARG, "work is NULL (needs %d doubles)", 3 * PROJ_BLOCKS);
+    if (n == 0) return MBEM_OK;
+    return project(v_in, v_out, n, ur, work, (cudaStream_t)stream);
 }
 
 size_t mbem_fgmres_workspace_size(int64_t n, int restart) {
@@ -494,6 +546,7 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
     int e = make_ranges(prm->u_ranges, prm->n_u_ranges, F.ur);
     if (e) return e;
     F.deflate = prm->n_u_ranges > 0;
+    F.time_matvec = prm->time_matvec != 0;
     FgmresWork& W = F.W;
     cudaStream_t st = F.st;
 
@@ -621,9 +674,13 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
     if ((e = F.proj(x, x))) return e;
     cudaMemcpyAsync(&tmp, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
+    if (mop && (e = mixed_wait_check(st))) return e;
     rep->true_relres = sqrt(tmp) / bnorm;
     rep->arnoldi_relres = arnoldi;
     rep->iterations = total;
+    F.collect_times();
+    rep->matvecs = F.matvecs;
+    rep->matvec_ms = F.matvec_ms;
     rep->restarts = restarts - 1 < 0 ? 0 : restarts - 1;
     rep->converged = rep->true_relres < prm->rtol;
     rep->stagnated = (stagnated || breakdown) && !rep->converged;

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "p0_pair.cuh"
+#include "tma_pipe.cuh"
 
 namespace mbem {
 
@@ -250,7 +251,7 @@ __device__ __forceinline__ void far_block(const QuadRules& Q, const SrcFar& s, c
 // far assembly: one thread per source, FIELD_TILE field points per block
 // ---------------------------------------------------------------------------
 constexpr int FAR_THREADS = 128;
-constexpr int FAR_FIELD_TILE = 32;
+constexpr int FAR_FIELD_TILE = 64;
 
 struct FarArgs {
     const double* x_field;
@@ -264,6 +265,7 @@ struct FarArgs {
     double near_factor;
     float* out;
     int64_t ld;
+    uint32_t* near_mask;   // optional (n_field, ceil(n_src/32)) bit mask of near pairs
 };
 
 template <bool TKERNEL>
@@ -272,8 +274,20 @@ far_assemble_kernel(FarArgs a, QuadRules Q) {
     __shared__ F2 xs[FAR_FIELD_TILE][3];
     const int64_t s = (int64_t)blockIdx.x * FAR_THREADS + threadIdx.x;
     const bool active = s < a.n_src;
+    const int64_t n_words = ceil_div(a.n_src, 32);
     SrcFar src;
-    if (active) far_setup(a.tri_verts + 9 * s, TKERNEL ? a.normals + 3 * s : nullptr, a.eps[s], a.near_factor, src);
+    if (active) {
+        far_setup(a.tri_verts + 9 * s, TKERNEL ? a.normals + 3 * s : nullptr, a.eps[s], a.near_factor, src);
+    } else {
+        // inactive lanes still vote in the near-mask ballot; they never count as near
+        for (int k = 0; k < 3; k++) {
+            src.c[k].hi = src.c[k].lo = 0.0f;
+            src.e1[k] = src.e2[k] = src.n[k] = 0.0f;
+        }
+        src.area2 = src.eps2 = src.L2 = 1.0f;
+        src.rnear2 = -1.0f;
+        src.ok = false;
+    }
     for (int64_t f0 = (int64_t)blockIdx.y * FAR_FIELD_TILE; f0 < a.n_field;
          f0 += (int64_t)gridDim.y * FAR_FIELD_TILE) {
         __syncthreads();
@@ -282,13 +296,18 @@ far_assemble_kernel(FarArgs a, QuadRules Q) {
             xs[t / 3][t % 3] = split_d(f < a.n_field ? a.x_field[3 * f0 + t] : 0.0);
         }
         __syncthreads();
-        if (!active) continue;
         const int nf = (int)lmin(FAR_FIELD_TILE, a.n_field - f0);
         for (int ff = 0; ff < nf; ff++) {
             const int64_t f = f0 + ff;
             float d[3], D2;
             float blk[3][3];
-            const bool near = is_near(xs[ff], src, d, D2);
+            const bool near = is_near(xs[ff], src, d, D2) && active;
+            if (a.near_mask) {
+                const unsigned m = __ballot_sync(0xffffffffu, near);
+                // lane 0 of a warp with at least one source writes its word
+                if ((threadIdx.x & 31) == 0 && (s >> 5) < n_words) a.near_mask[f * n_words + (s >> 5)] = m;
+            }
+            if (!active) continue;
             if (near || !src.ok) {
 #pragma unroll
                 for (int i = 0; i < 3; i++)
@@ -382,6 +401,45 @@ __global__ void scan_kernel(const int64_t* __restrict__ counts, int64_t n, int64
     if (n == 0 && t == 0) rowptr[0] = 0;
 }
 
+// near list from the far kernel's bit mask: one warp per field point
+__global__ void mask_count_kernel(const uint32_t* __restrict__ mask, int64_t n_field, int64_t n_words,
+                                  int64_t* __restrict__ counts) {
+    const int64_t f = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (f >= n_field) return;
+    int64_t c = 0;
+    for (int64_t w = lane; w < n_words; w += 32) c += __popc(mask[f * n_words + w]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) counts[f] = c;
+}
+
+__global__ void mask_fill_kernel(const uint32_t* __restrict__ mask, int64_t n_field, int64_t n_words,
+                                 const int64_t* __restrict__ rowptr, int64_t* __restrict__ cols) {
+    const int64_t f = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (f >= n_field) return;
+    int64_t pos = rowptr[f];
+    for (int64_t w0 = 0; w0 < n_words; w0 += 32) {
+        const int64_t w = w0 + lane;
+        uint32_t m = (w < n_words) ? mask[f * n_words + w] : 0u;
+        const int c = __popc(m);
+        int incl = c;   // inclusive warp scan of the counts (lane order = source order)
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        int64_t p = pos + (incl - c);
+        while (m) {
+            const int b = __ffs(m) - 1;
+            cols[p++] = 32 * w + b;
+            m &= m - 1;
+        }
+        pos += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
 // near T/U blocks in FP64 (closed form), one thread per near pair
 struct NearEvalArgs {
     const double* x_field;
@@ -467,6 +525,14 @@ __global__ void near_add_diag_kernel(const int64_t* __restrict__ rowptr, const i
     atomicAdd(missing, 1);
 }
 
+// TwoSum of v into (h, l)
+__device__ __forceinline__ void ts_add(float& h, float& l, float v) {
+    const float s = __fadd_rn(h, v);
+    const float bb = __fsub_rn(s, h);
+    l = __fadd_rn(l, __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(v, bb)));
+    h = s;
+}
+
 // FP32 row sums with double-float accumulation: out[r, j] (+)= sum_c A[r, 3c+j]
 __global__ void rowsum3_f32_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_cols,
                                    double alpha, int accumulate, double* __restrict__ out) {
@@ -474,21 +540,40 @@ __global__ void rowsum3_f32_kernel(const float* __restrict__ A, int64_t ld, int6
     const int lane = threadIdx.x & 31;
     if (r >= n_rows) return;
     const float* row = A + r * ld;
-    float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
-    int j = lane % 3;
-    for (int64_t c = lane; c < n_cols; c += 32) {
+    // four independent (hi, lo) accumulators per component; a lane reads 12
+    // consecutive columns (3 float4) at a time, so element e of the chunk
+    // always belongs to component e % 3 and every index is static
+    float hi[4][3], lo[4][3];
+#pragma unroll
+    for (int t = 0; t < 4; t++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) hi[t][k] = lo[t][k] = 0.0f;
+    int64_t c_start = 0;
+    if ((reinterpret_cast<uintptr_t>(row) & 15) == 0) {
+        const int64_t n12 = n_cols / 12;
+        const float4* r4 = reinterpret_cast<const float4*>(row);
+        for (int64_t q = lane; q < n12; q += 32) {
+            const float4 a = __ldcs(r4 + 3 * q), b = __ldcs(r4 + 3 * q + 1), c = __ldcs(r4 + 3 * q + 2);
+            ts_add(hi[0][0], lo[0][0], a.x); ts_add(hi[0][1], lo[0][1], a.y); ts_add(hi[0][2], lo[0][2], a.z);
+            ts_add(hi[1][0], lo[1][0], a.w); ts_add(hi[1][1], lo[1][1], b.x); ts_add(hi[1][2], lo[1][2], b.y);
+            ts_add(hi[2][0], lo[2][0], b.z); ts_add(hi[2][1], lo[2][1], b.w); ts_add(hi[2][2], lo[2][2], c.x);
+            ts_add(hi[3][0], lo[3][0], c.y); ts_add(hi[3][1], lo[3][1], c.z); ts_add(hi[3][2], lo[3][2], c.w);
+        }
+        c_start = 12 * n12;
+    }
+    for (int64_t c = c_start + lane; c < n_cols; c += 32) {
         const float v = row[c];
-        const float s = __fadd_rn(hi[j], v);
-        const float bb = __fsub_rn(s, hi[j]);
-        lo[j] = __fadd_rn(lo[j], __fadd_rn(__fsub_rn(hi[j], __fsub_rn(s, bb)), __fsub_rn(v, bb)));
-        hi[j] = s;
-        j += 2;
-        if (j >= 3) j -= 3;
+        const int k = (int)(c % 3);
+        if (k == 0) ts_add(hi[0][0], lo[0][0], v);
+        else if (k == 1) ts_add(hi[0][1], lo[0][1], v);
+        else ts_add(hi[0][2], lo[0][2], v);
     }
     double acc[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        acc[k] = (double)hi[k] + (double)lo[k];
+        acc[k] = 0.0;
+#pragma unroll
+        for (int t = 0; t < 4; t++) acc[k] += (double)hi[t][k] + (double)lo[t][k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
     }
@@ -512,6 +597,7 @@ __global__ void split_vec_kernel(const double* __restrict__ x, int64_t n, float*
 }
 
 constexpr int SGEMV_ROWS = 4;
+constexpr int SGEMV_UNROLL = 2;
 constexpr int SGEMV_THREADS = 256;
 
 // double-float accumulate of a (FP32, exact) times x = xh + xl
@@ -533,35 +619,62 @@ sgemv_df_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int64_t
     const int64_t r0 = warp * SGEMV_ROWS;
     if (r0 >= n_rows) return;
     const int nr = (int)lmin(SGEMV_ROWS, n_rows - r0);
-    float sh[SGEMV_ROWS], sl[SGEMV_ROWS];
+    // four independent double-float accumulators per row (one per float4
+    // lane): the TwoSum chain, not HBM, bounds a single accumulator
+    float sh[SGEMV_ROWS][4], sl[SGEMV_ROWS][4];
 #pragma unroll
-    for (int i = 0; i < SGEMV_ROWS; i++) sh[i] = sl[i] = 0.0f;
+    for (int i = 0; i < SGEMV_ROWS; i++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) sh[i][k] = sl[i][k] = 0.0f;
     const int64_t n4 = n_cols / 4;
     const float4* xh4 = reinterpret_cast<const float4*>(xh);
     const float4* xl4 = reinterpret_cast<const float4*>(xl);
     const float4* rows[SGEMV_ROWS];
 #pragma unroll
     for (int i = 0; i < SGEMV_ROWS; i++) rows[i] = reinterpret_cast<const float4*>(A + (r0 + min(i, nr - 1)) * ld);
-    for (int64_t c = lane; c < n4; c += 32) {
+    // full chunks: SGEMV_UNROLL x SGEMV_ROWS independent 16-byte loads per lane
+    const int64_t full = (n4 / (32 * SGEMV_UNROLL)) * (32 * SGEMV_UNROLL);
+    for (int64_t c0 = lane; c0 < full; c0 += 32 * SGEMV_UNROLL) {
+        float4 v[SGEMV_UNROLL][SGEMV_ROWS], h[SGEMV_UNROLL], l[SGEMV_UNROLL];
+#pragma unroll
+        for (int u = 0; u < SGEMV_UNROLL; u++) {
+            const int64_t c = c0 + 32 * u;
+            h[u] = __ldg(xh4 + c);
+            l[u] = __ldg(xl4 + c);
+#pragma unroll
+            for (int i = 0; i < SGEMV_ROWS; i++) v[u][i] = __ldcs(rows[i] + c);
+        }
+#pragma unroll
+        for (int u = 0; u < SGEMV_UNROLL; u++)
+#pragma unroll
+            for (int i = 0; i < SGEMV_ROWS; i++) {
+                df_acc(sh[i][0], sl[i][0], v[u][i].x, h[u].x, l[u].x);
+                df_acc(sh[i][1], sl[i][1], v[u][i].y, h[u].y, l[u].y);
+                df_acc(sh[i][2], sl[i][2], v[u][i].z, h[u].z, l[u].z);
+                df_acc(sh[i][3], sl[i][3], v[u][i].w, h[u].w, l[u].w);
+            }
+    }
+    for (int64_t c = full + lane; c < n4; c += 32) {
         const float4 h = __ldg(xh4 + c), l = __ldg(xl4 + c);
 #pragma unroll
         for (int i = 0; i < SGEMV_ROWS; i++) {
             const float4 v = __ldcs(rows[i] + c);
-            df_acc(sh[i], sl[i], v.x, h.x, l.x);
-            df_acc(sh[i], sl[i], v.y, h.y, l.y);
-            df_acc(sh[i], sl[i], v.z, h.z, l.z);
-            df_acc(sh[i], sl[i], v.w, h.w, l.w);
+            df_acc(sh[i][0], sl[i][0], v.x, h.x, l.x);
+            df_acc(sh[i][1], sl[i][1], v.y, h.y, l.y);
+            df_acc(sh[i][2], sl[i][2], v.z, h.z, l.z);
+            df_acc(sh[i][3], sl[i][3], v.w, h.w, l.w);
         }
     }
     for (int64_t c = 4 * n4 + lane; c < n_cols; c += 32) {
 #pragma unroll
         for (int i = 0; i < SGEMV_ROWS; i++)
-            df_acc(sh[i], sl[i], A[(r0 + min(i, nr - 1)) * ld + c], xh[c], xl[c]);
+            df_acc(sh[i][0], sl[i][0], A[(r0 + min(i, nr - 1)) * ld + c], xh[c], xl[c]);
     }
     double acc[SGEMV_ROWS];
 #pragma unroll
     for (int i = 0; i < SGEMV_ROWS; i++) {
-        acc[i] = (double)sh[i] + (double)sl[i];
+        acc[i] = ((double)sh[i][0] + (double)sl[i][0]) + ((double)sh[i][1] + (double)sl[i][1]) +
+                 ((double)sh[i][2] + (double)sl[i][2]) + ((double)sh[i][3] + (double)sl[i][3]);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
     }
@@ -574,14 +687,17 @@ sgemv_df_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int64_t
     }
 }
 
-// y[3f + i] += sum_k vals[k, i, j] x[3 cols[k] + j]  (one thread per row block)
+// y[3f + i] += sum_k vals[k, i, j] x[3 cols[k] + j]: one warp per row block,
+// lanes over its near blocks, fixed-order warp reduction
 __global__ void near_matvec_kernel(const int64_t* __restrict__ rowptr, const int64_t* __restrict__ cols,
                                    const double* __restrict__ vals, int64_t n_field, const double* __restrict__ x,
                                    double* __restrict__ y) {
-    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t f = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
     if (f >= n_field) return;
     double a0 = 0, a1 = 0, a2 = 0;
-    for (int64_t k = rowptr[f]; k < rowptr[f + 1]; k++) {
+    const int64_t k1 = rowptr[f + 1];
+    for (int64_t k = rowptr[f] + lane; k < k1; k += 32) {
         const int64_t s = cols[k];
         const double x0 = x[3 * s], x1 = x[3 * s + 1], x2 = x[3 * s + 2];
         const double* v = vals + 9 * k;
@@ -589,9 +705,160 @@ __global__ void near_matvec_kernel(const int64_t* __restrict__ rowptr, const int
         a1 += v[3] * x0 + v[4] * x1 + v[5] * x2;
         a2 += v[6] * x0 + v[7] * x1 + v[8] * x2;
     }
-    y[3 * f] += a0;
-    y[3 * f + 1] += a1;
-    y[3 * f + 2] += a2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (lane == 0) {
+        y[3 * f] += a0;
+        y[3 * f + 1] += a1;
+        y[3 * f + 2] += a2;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The same product as a warp-specialised bulk-copy pipeline: one producer
+// warp streams TP_ROWS row chunks of A and the matching chunk of x (hi, lo)
+// into a TP_STAGES-deep shared-memory ring with cp.async.bulk, completing on
+// per-stage mbarriers; TP_ROWS consumer warps (one row each) read the stage
+// from shared memory and accumulate in double-float. The ring keeps
+// ~160 KB per SM in flight independent of register pressure.
+// ---------------------------------------------------------------------------
+constexpr int TP_ROWS = 16;
+constexpr int TP_CH = 1024;              // columns per chunk (4 KB per row)
+constexpr int TP_STAGES = 3;
+constexpr int TP_THREADS = 32 * (TP_ROWS + 1);
+constexpr size_t TP_SMEM = (size_t)TP_STAGES * (TP_ROWS + 2) * TP_CH * sizeof(float) + 2 * TP_STAGES * 8;
+constexpr uint32_t TP_WAIT_LIMIT = 1u << 26;
+
+// set by a pipeline wait that gave up; read (and cleared) by the host
+__device__ int g_mixed_wait_error = 0;
+
+__global__ void __launch_bounds__(TP_THREADS, 1)
+sgemv_df_tma_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_main, int64_t n_cols,
+                    const float* __restrict__ xh, const float* __restrict__ xl, double* __restrict__ y) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    float* sA = reinterpret_cast<float*>(smem);                     // [S][ROWS][CH]
+    float* sX = sA + TP_STAGES * TP_ROWS * TP_CH;                   // [S][2][CH]
+    uint64_t* full = reinterpret_cast<uint64_t*>(sX + TP_STAGES * 2 * TP_CH);
+    uint64_t* empty = full + TP_STAGES;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t r0 = (int64_t)blockIdx.x * TP_ROWS;
+    const int nrow = (int)lmin(TP_ROWS, n_rows - r0);
+    const int64_t nchunks = ceil_div(n_main, TP_CH);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TP_STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], TP_ROWS);
+        }
+        mbar_init_fence();
+    }
+    __syncthreads();
+
+    if (warp == TP_ROWS) {
+        // producer warp: lane 0 waits for the stage to drain and posts the
+        // byte count; lanes 0..nrow+1 then issue one copy each, in parallel
+        int64_t issued = 0;
+        for (int64_t k = 0; k < nchunks; k++) {
+            const int s = (int)(k % TP_STAGES);
+            int ok = 1;
+            if (lane == 0) {
+                if (k >= TP_STAGES && !mbar_wait(&empty[s], (uint32_t)(((k / TP_STAGES) - 1) & 1), TP_WAIT_LIMIT)) {
+                    atomicExch(&g_mixed_wait_error, 1);
+                    ok = 0;
+                }
+            }
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+            const int64_t c0 = k * TP_CH;
+            const uint32_t bytes = (uint32_t)lmin(TP_CH, n_main - c0) * 4u;
+            if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)(nrow + 2));
+            __syncwarp();
+            if (lane < nrow)
+                bulk_g2s(sA + ((int64_t)s * TP_ROWS + lane) * TP_CH, A + (r0 + lane) * ld + c0, bytes, &full[s]);
+            else if (lane == TP_ROWS)
+                bulk_g2s(sX + (int64_t)s * 2 * TP_CH, xh + c0, bytes, &full[s]);
+            else if (lane == TP_ROWS + 1)
+                bulk_g2s(sX + ((int64_t)s * 2 + 1) * TP_CH, xl + c0, bytes, &full[s]);
+            issued = k + 1;
+        }
+        // do not leave the block while copies into its shared memory are in flight
+        if (lane == 0)
+            for (int64_t k = (issued > TP_STAGES ? issued - TP_STAGES : 0); k < issued; k++)
+                if (!mbar_wait(&full[k % TP_STAGES], (uint32_t)((k / TP_STAGES) & 1), TP_WAIT_LIMIT))
+                    atomicExch(&g_mixed_wait_error, 1);
+        return;
+    }
+
+    // consumers: warp w owns row r0 + w
+    const bool valid = warp < nrow;
+    // eight independent double-float chains: two float4 per step, one chain
+    // per element
+    float sh[8], sl[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) sh[t] = sl[t] = 0.0f;
+    for (int64_t k = 0; k < nchunks; k++) {
+        const int s = (int)(k % TP_STAGES);
+        if (!mbar_wait(&full[s], (uint32_t)((k / TP_STAGES) & 1), TP_WAIT_LIMIT)) {
+            atomicExch(&g_mixed_wait_error, 1);
+            break;
+        }
+        if (valid) {
+            const int w4 = (int)(lmin(TP_CH, n_main - k * TP_CH) / 4);
+            const float4* a4 = reinterpret_cast<const float4*>(sA + ((int64_t)s * TP_ROWS + warp) * TP_CH);
+            const float4* h4 = reinterpret_cast<const float4*>(sX + (int64_t)s * 2 * TP_CH);
+            const float4* l4 = reinterpret_cast<const float4*>(sX + ((int64_t)s * 2 + 1) * TP_CH);
+            int q = lane;
+#pragma unroll 2
+            for (; q + 32 < w4; q += 64) {
+                const float4 a = a4[q], h = h4[q], l = l4[q];
+                const float4 b = a4[q + 32], g = h4[q + 32], m = l4[q + 32];
+                df_acc(sh[0], sl[0], a.x, h.x, l.x);
+                df_acc(sh[1], sl[1], a.y, h.y, l.y);
+                df_acc(sh[2], sl[2], a.z, h.z, l.z);
+                df_acc(sh[3], sl[3], a.w, h.w, l.w);
+                df_acc(sh[4], sl[4], b.x, g.x, m.x);
+                df_acc(sh[5], sl[5], b.y, g.y, m.y);
+                df_acc(sh[6], sl[6], b.z, g.z, m.z);
+                df_acc(sh[7], sl[7], b.w, g.w, m.w);
+            }
+            if (q < w4) {
+                const float4 a = a4[q], h = h4[q], l = l4[q];
+                df_acc(sh[0], sl[0], a.x, h.x, l.x);
+                df_acc(sh[1], sl[1], a.y, h.y, l.y);
+                df_acc(sh[2], sl[2], a.z, h.z, l.z);
+                df_acc(sh[3], sl[3], a.w, h.w, l.w);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+    }
+    if (!valid) return;
+    const int64_t r = r0 + warp;
+    for (int64_t c = n_main + lane; c < n_cols; c += 32) df_acc(sh[0], sl[0], A[r * ld + c], xh[c], xl[c]);
+    double acc = 0.0;
+#pragma unroll
+    for (int t = 0; t < 8; t++) acc += (double)sh[t] + (double)sl[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[r] = acc;
+}
+
+// MBEM_ERR_WAIT if a pipeline wait gave up since the last check (the flag is
+// cleared); synchronises the stream.
+int mixed_wait_check(cudaStream_t st) {
+    int flag = 0;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaMemcpyFromSymbol(&flag, g_mixed_wait_error, sizeof(int));
+    if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "wait check: %s", cudaGetErrorString(e));
+    if (flag) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_mixed_wait_error, &zero, sizeof(int));
+        return set_error(MBEM_ERR_WAIT, "a bulk-copy pipeline wait expired in the mixed matvec");
+    }
+    return MBEM_OK;
 }
 
 int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, float* xh, float* xl,
@@ -599,15 +866,25 @@ int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, floa
     const int64_t nr = op->n_rows, nc = op->n_cols;
     if (nr == 0) return MBEM_OK;
     split_vec_kernel<<<(unsigned)ceil_div(nc > 0 ? nc : 1, 256), 256, 0, st>>>(x, nc, xh, xl);
-    const int64_t warps = ceil_div(nr, SGEMV_ROWS);
     const bool vec = ((uintptr_t)op->A32 % 16 == 0) && (op->ld32 % 4 == 0);
     MBEM_REQUIRE(vec, MBEM_ERR_ARG, "the FP32 far matrix must be 16-byte aligned with ld32 %% 4 == 0");
-    sgemv_df_kernel<<<(unsigned)ceil_div(warps, SGEMV_THREADS / 32), SGEMV_THREADS, 0, st>>>(
-        op->A32, op->ld32, nr, nc, xh, xl, y);
+    const bool xal = ((uintptr_t)xh % 16 == 0) && ((uintptr_t)xl % 16 == 0);
+    const int64_t n_main = nc & ~(int64_t)3;
+    if (xal && n_main > 0) {
+        cudaError_t e = cudaFuncSetAttribute(sgemv_df_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)TP_SMEM);
+        if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "sgemv smem attribute: %s", cudaGetErrorString(e));
+        sgemv_df_tma_kernel<<<(unsigned)ceil_div(nr, TP_ROWS), TP_THREADS, TP_SMEM, st>>>(
+            op->A32, op->ld32, nr, n_main, nc, xh, xl, y);
+    } else {
+        const int64_t warps = ceil_div(nr, SGEMV_ROWS);
+        sgemv_df_kernel<<<(unsigned)ceil_div(warps, SGEMV_THREADS / 32), SGEMV_THREADS, 0, st>>>(
+            op->A32, op->ld32, nr, nc, xh, xl, y);
+    }
     int launches = 2;
     for (int q = 0; q < op->n_near; q++) {
         const mbem_near_blocks& nb = op->near[q];
-        near_matvec_kernel<<<(unsigned)ceil_div(nb.n_field, 128), 128, 0, st>>>(
+        near_matvec_kernel<<<(unsigned)ceil_div(nb.n_field, 8), 256, 0, st>>>(
             nb.rowptr, nb.cols, nb.vals, nb.n_field, x + nb.col0, y + nb.row0);
         launches++;
     }
@@ -622,7 +899,8 @@ extern "C" {
 
 int mbem_far_matrix(int kernel, const double* x_field, int64_t n_field, const double* tri_verts,
                     const double* normals, const double* eps, int64_t n_src, const double* coeffs,
-                    double near_factor, double alpha, float* out, int64_t ld_out, void* stream) {
+                    double near_factor, double alpha, float* out, int64_t ld_out, uint32_t* near_mask,
+                    void* stream) {
     MBEM_REQUIRE(kernel == 0 || kernel == 1, MBEM_ERR_ARG, "kernel must be 0 (T) or 1 (U)");
     MBEM_REQUIRE(n_field >= 0 && n_src >= 0 && ld_out >= 3 * n_src, MBEM_ERR_ARG, "bad far matrix shape");
     MBEM_REQUIRE(coeffs != nullptr && near_factor > 0.0, MBEM_ERR_ARG, "coeffs/near_factor");
@@ -634,6 +912,7 @@ int mbem_far_matrix(int kernel, const double* x_field, int64_t n_field, const do
     const int nc = kernel == 0 ? 6 : 3;
     for (int i = 0; i < 6; i++) a.c[i] = i < nc ? (float)coeffs[i] : 0.0f;
     a.alpha = (float)alpha; a.near_factor = near_factor; a.out = out; a.ld = ld_out;
+    a.near_mask = near_mask;
     dim3 grid((unsigned)ceil_div(n_src, FAR_THREADS), (unsigned)lmin(ceil_div(n_field, FAR_FIELD_TILE), 65535));
     if (kernel == 0)
         far_assemble_kernel<true><<<grid, FAR_THREADS, 0, (cudaStream_t)stream>>>(a, rules());
@@ -643,6 +922,33 @@ int mbem_far_matrix(int kernel, const double* x_field, int64_t n_field, const do
 }
 
 size_t mbem_near_list_workspace_size(int64_t n_field) { return (size_t)(n_field + 1) * sizeof(int64_t); }
+
+int mbem_near_mask_count(const uint32_t* mask, int64_t n_field, int64_t n_src, int64_t* rowptr, void* work,
+                         size_t work_bytes, int64_t* nnz_host, void* stream) {
+    MBEM_REQUIRE(n_field >= 0 && n_src >= 0 && rowptr && nnz_host && (n_field == 0 || mask), MBEM_ERR_ARG,
+                 "bad near-mask-count args");
+    MBEM_REQUIRE(work && work_bytes >= mbem_near_list_workspace_size(n_field), MBEM_ERR_SIZE,
+                 "near-mask-count workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    int64_t* counts = (int64_t*)work;
+    const int64_t n_words = ceil_div(n_src, 32);
+    if (n_field > 0)
+        mask_count_kernel<<<(unsigned)ceil_div(n_field, 8), 256, 0, st>>>(mask, n_field, n_words, counts);
+    scan_kernel<<<1, 1024, 0, st>>>(counts, n_field, rowptr);
+    cudaMemcpyAsync(nnz_host, rowptr + n_field, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("near_mask_count sync", 2);
+    return launch_status("near_mask_count", 2);
+}
+
+int mbem_near_mask_fill(const uint32_t* mask, int64_t n_field, int64_t n_src, const int64_t* rowptr, int64_t* cols,
+                        void* stream) {
+    MBEM_REQUIRE(n_field >= 0 && n_src >= 0 && rowptr && (n_field == 0 || mask), MBEM_ERR_ARG,
+                 "bad near-mask-fill args");
+    if (n_field == 0) return MBEM_OK;
+    mask_fill_kernel<<<(unsigned)ceil_div(n_field, 8), 256, 0, (cudaStream_t)stream>>>(
+        mask, n_field, ceil_div(n_src, 32), rowptr, cols);
+    return launch_status("mask_fill_kernel");
+}
 
 int mbem_near_count(const double* x_field, int64_t n_field, const double* tri_verts, const double* eps,
                     int64_t n_src, double near_factor, int64_t* rowptr, void* work, size_t work_bytes,

@@ -66,12 +66,25 @@ def far_near_block(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha:
     if timer is not None:
         ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
         ev[0].record()
+    # the far kernel votes the near pairs into a bit mask (one word per warp of
+    # sources), from which the near list is read without a second pass over
+    # all pairs
+    n_words = (ns + 31) // 32
+    mask = torch.empty((nf, n_words), dtype=torch.int32, device=x_field.device)
     nat.call("mbem_far_matrix", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ns, c,
-             float(near_factor), float(alpha), ptr(far_out), far_out.stride(0), stream_handle())
+             float(near_factor), float(alpha), ptr(far_out), far_out.stride(0), ptr(mask), stream_handle())
     if ev is not None:
         ev[1].record()
         timer.append(("far_" + kernel, nf, ns, ev[0], ev[1]))
-    rowptr, cols = near_list(x_field, tri_verts, eps, near_factor)
+    rowptr = torch.empty(nf + 1, dtype=torch.int64, device=x_field.device)
+    work = torch.empty(int(nat.lib().mbem_near_list_workspace_size(nf)), dtype=torch.uint8,
+                       device=x_field.device)
+    nnz = ctypes.c_int64(0)
+    nat.call("mbem_near_mask_count", ptr(mask), nf, ns, ptr(rowptr), ptr(work), work.numel(),
+             ctypes.byref(nnz), stream_handle())
+    cols = torch.empty(max(nnz.value, 1), dtype=torch.int64, device=x_field.device)[:nnz.value]
+    nat.call("mbem_near_mask_fill", ptr(mask), nf, ns, ptr(rowptr), ptr(cols), stream_handle())
+    del mask
     vals = torch.empty((max(cols.numel(), 1), 9), dtype=torch.float64, device=x_field.device)[:cols.numel()]
     nat.call("mbem_near_eval", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ptr(rowptr),
              ptr(cols), cols.numel(), c, float(alpha), ptr(vals), stream_handle())

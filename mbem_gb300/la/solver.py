@@ -33,40 +33,38 @@ class SolveReport:
     precond_summary: dict | None = None
     recycle_dim: int = 0
     setup_matvecs: int = 0
+    matvecs: int = 0                 # operator applications
+    matvec_ms: float = 0.0           # their device time (when timed)
 
     def __str__(self):
         status = "converged" if self.converged else ("STAGNATED" if self.stagnated else "NOT CONVERGED")
         return f"FGMRES {status}: {self.iterations} iters, true relres {self.true_relres:.3e}"
 
 
-def fgmres_mixed(op, b: torch.Tensor, x0: torch.Tensor | None = None,
-                 rtol: float = defaults.GMRES_RTOL, restart: int = defaults.GMRES_RESTART,
-                 maxiter: int = defaults.GMRES_MAXITER,
-                 stagnation_window: int = defaults.GMRES_STAGNATION_WINDOW,
-                 stagnation_factor: float = defaults.GMRES_STAGNATION_FACTOR,
-                 u_ranges=(), workspace: torch.Tensor | None = None):
+_DEFAULTS = dict(rtol=defaults.GMRES_RTOL, restart=defaults.GMRES_RESTART, maxiter=defaults.GMRES_MAXITER,
+                 stagnation_window=defaults.GMRES_STAGNATION_WINDOW,
+                 stagnation_factor=defaults.GMRES_STAGNATION_FACTOR, u_ranges=(), workspace=None,
+                 time_matvec=False)
+
+
+def fgmres_mixed(op, b: torch.Tensor, x0: torch.Tensor | None = None, **kw):
     """FGMRES on a ``la.mixed.MixedOperator`` (same contract as fgmres_dense)."""
-    return _fgmres(None, op, b, x0, rtol, restart, maxiter, stagnation_window, stagnation_factor,
-                   u_ranges, workspace)
+    return _fgmres(None, op, b, x0, **{**_DEFAULTS, **kw})
 
 
-def fgmres_dense(A: torch.Tensor, b: torch.Tensor, x0: torch.Tensor | None = None,
-                 rtol: float = defaults.GMRES_RTOL, restart: int = defaults.GMRES_RESTART,
-                 maxiter: int = defaults.GMRES_MAXITER,
-                 stagnation_window: int = defaults.GMRES_STAGNATION_WINDOW,
-                 stagnation_factor: float = defaults.GMRES_STAGNATION_FACTOR,
-                 u_ranges=(), workspace: torch.Tensor | None = None):
-    """Solve A x = b for a dense FP64 CUDA matrix. ``u_ranges`` = [(offset,
-    size), ...] of the u-slots to deflate (empty: no deflation).
+def fgmres_dense(A: torch.Tensor, b: torch.Tensor, x0: torch.Tensor | None = None, **kw):
+    """Solve A x = b for a dense FP64 CUDA matrix. Keywords: rtol, restart,
+    maxiter, stagnation_window, stagnation_factor, ``u_ranges`` = [(offset,
+    size), ...] of the u-slots to deflate (empty: no deflation), workspace,
+    time_matvec (CUDA-event time of every operator application).
     Returns (x, SolveReport)."""
     if A.dtype != torch.float64 or not A.is_cuda or A.shape[0] != b.shape[0] or A.stride(1) != 1:
         raise ValueError("A must be a float64 CUDA matrix (n, n) with unit column stride")
-    return _fgmres(A, None, b, x0, rtol, restart, maxiter, stagnation_window, stagnation_factor,
-                   u_ranges, workspace)
+    return _fgmres(A, None, b, x0, **{**_DEFAULTS, **kw})
 
 
 def _fgmres(A, mop, b, x0, rtol, restart, maxiter, stagnation_window, stagnation_factor, u_ranges,
-            workspace):
+            workspace, time_matvec):
     n = b.shape[0]
     dev = (A if A is not None else mop.A32).device
     b = b.to(dtype=torch.float64, device=dev).contiguous()
@@ -82,7 +80,7 @@ def _fgmres(A, mop, b, x0, rtol, restart, maxiter, stagnation_window, stagnation
                            stagnation_factor=float(stagnation_factor),
                            n_u_ranges=len(rng) // 2,
                            u_ranges=rng.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) if rng.size else None,
-                           precond=0, precond_state=None)
+                           precond=0, precond_state=None, time_matvec=int(bool(time_matvec)))
     hist = np.zeros(max(int(maxiter), 1))
     rep = nat.FgmresReport()
     rep.history = hist.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
@@ -96,5 +94,6 @@ def _fgmres(A, mop, b, x0, rtol, restart, maxiter, stagnation_window, stagnation
     report = SolveReport(converged=bool(rep.converged), iterations=int(rep.iterations),
                          true_relres=float(rep.true_relres), arnoldi_relres=float(rep.arnoldi_relres),
                          stagnated=bool(rep.stagnated), restarts=int(rep.restarts),
-                         residual_history=hist[:rep.iterations].tolist())
+                         residual_history=hist[:rep.iterations].tolist(), matvecs=int(rep.matvecs),
+                         matvec_ms=float(rep.matvec_ms))
     return x, report

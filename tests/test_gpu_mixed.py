@@ -61,6 +61,30 @@ def test_mixed_operator_entries(systems):
     assert np.abs(M @ Z).max() < 1e-13 * scale
 
 
+@pytest.mark.parametrize("ns", [129, 200, 32])
+def test_near_list_from_mask_equals_classification(gpu, ns):
+    """The far kernel's ballot mask gives the same near list as the
+    stand-alone classification pass (ragged source counts: partial words,
+    a block with a single live warp)."""
+    from mbem_gb300._device import as_cuda
+    from mbem_gb300.kernels import basis as kb
+    from mbem_gb300.la.mixed import far_near_block, near_list
+    rng = np.random.default_rng(ns)
+    c = rng.uniform(-1, 1, size=(ns, 3))
+    tv = c[:, None, :] + rng.normal(scale=0.15, size=(ns, 3, 3))
+    cr = np.cross(tv[:, 1] - tv[:, 0], tv[:, 2] - tv[:, 0])
+    nrm = cr / np.linalg.norm(cr, axis=1)[:, None]
+    x = rng.uniform(-1.2, 1.2, size=(97, 3))
+    e = rng.uniform(0.02, 0.1, ns)
+    X, T, N, E = as_cuda(x), as_cuda(tv), as_cuda(nrm), as_cuda(e)
+    far = torch.empty((3 * 97, 3 * ns), dtype=torch.float32, device="cuda")
+    nl = far_near_block("T", X, T, N, E, kb.t_coeffs(1.0, 1.0), 1.0, far)
+    rowptr, cols = near_list(X, T, E)
+    assert torch.equal(nl.rowptr, rowptr)
+    assert torch.equal(nl.cols, cols)
+    assert nl.nnz > 0
+
+
 def test_mixed_matvec_is_exact_for_its_operator(systems):
     _, amx = systems
     x = torch.randn(amx.op.n, dtype=torch.float64, device="cuda")

@@ -41,7 +41,12 @@ def test_projection_removes_translations(gpu):
     v = torch.randn(n, dtype=torch.float64, device="cuda")
     out = torch.empty_like(v)
     rng = np.array([0, 150], dtype=np.int64)
-    nat.call("mbem_project_translation", ptr(v), ptr(out), n, rng.ctypes.data, 1, None, stream_handle())
+    work = torch.empty(384, dtype=torch.float64, device="cuda")
+    nat.call("mbem_project_translation", ptr(v), ptr(out), n, rng.ctypes.data, 1, ptr(work), stream_handle())
+    # in place gives the same result
+    v2 = v.clone()
+    nat.call("mbem_project_translation", ptr(v2), ptr(v2), n, rng.ctypes.data, 1, ptr(work), stream_handle())
+    assert torch.equal(v2, out)
     o = out.cpu().numpy()
     vv = v.cpu().numpy()
     for k in range(3):
