@@ -100,7 +100,8 @@ int mbem_stress_contract(int kind, const double* x_field, int64_t n_field,
  * basis.py:406-427 assemble_traction_matrix. which: 0 "slip" (total minus
  * eigen), 1 "force", 2 "eigen", 3 "total". ids (Ns,K) int64 DEVICE array
  * scattering element-node columns onto n_cols shared columns; out
- * (3Nf, 3 n_cols) at ld_out, accumulated (out += alpha * rows). -------- */
+ * (3Nf, 3 n_cols) at ld_out, accumulated (out += alpha * rows); an id
+ * outside [0, n_cols) contributes nothing. ------------------------------ */
 int mbem_traction_matrix(const double* x_field, const double* n_field, int64_t n_pts,
                          const double* tri_verts, const double* normals, const double* eps,
                          int64_t n_src, const int64_t* ids, int64_t n_cols, double mu, double lam,
@@ -120,6 +121,14 @@ int mbem_block_rowsum3(const double* A, int64_t ld, int64_t n_rows, int64_t n_co
  * block's top-left corner; shape is a HOST (K,K) array. */
 int mbem_add_block_diagonal(double* A, int64_t ld, const double* D, int64_t n_c, int K,
                             const double* shape, void* stream);
+
+/* In place, rows (3c, 3c+1, 3c+2) of A (n_cols wide, at ld) and entries
+ * (3c..3c+2) of b (may be NULL) become F_c times themselves, F = frames
+ * (n_nodes, 3, 3) DEVICE: a traction fault's Cartesian rows into its row
+ * frame (equations.py:443-473 apply_fault_rows). A and b point at the
+ * fault's first row. */
+int mbem_rotate_row_triples(double* A, int64_t ld, int64_t n_cols, double* b, int64_t n_nodes,
+                            const double* frames, void* stream);
 
 /* y = alpha * A x + beta * y, FP64 row-major (the dense matvec of
  * la/solver.py:513-520 _as_matvec on an AssembledDense.A). */

@@ -80,6 +80,7 @@ _SIGNATURES = {
                                      _P, _I, _P]),
     "mbem_block_rowsum3": (c_int, [_P, _I, _I, _I, _D, c_int, _P, _P]),
     "mbem_add_block_diagonal": (c_int, [_P, _I, _P, _I, c_int, _P, _P]),
+    "mbem_rotate_row_triples": (c_int, [_P, _I, _I, _P, _I, _P, _P]),
     "mbem_dgemv": (c_int, [_P, _I, _I, _I, _P, _D, _D, _P, _P]),
     "mbem_dgemm_multi": (c_int, [_P, _I, _I, _I, _P, _I, _P, _P]),
     "mbem_project_translation": (c_int, [_P, _P, _I, _P, c_int, _P, _P]),

@@ -169,6 +169,8 @@ class AssembledDense:
         else:
             which = "slip" if kernel == KERNEL_HT else "force"
             ids = kb.identity_ids(order, source_patch.n_triangles)
+            if not accumulate:
+                out.zero_()          # the traction rows are always accumulated
             tn.traction_matrix(f["coll"], f["coll_n"], s["tv"], s["normals"], s["eps"], ids, ids.size,
                                material.mu, material.lam, order, which, out=out, alpha=alpha)
         if ev is not None:

@@ -41,6 +41,7 @@ int mixed_wait_check(cudaStream_t st);
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 __host__ __device__ inline int64_t lmin(int64_t a, int64_t b) { return a < b ? a : b; }
+__host__ __device__ inline int64_t lmax(int64_t a, int64_t b) { return a > b ? a : b; }
 
 }  // namespace mbem
 

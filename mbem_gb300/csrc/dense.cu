@@ -70,6 +70,33 @@ __global__ void add_block_diag_kernel(double* __restrict__ A, int64_t ld, const 
 }
 
 // ---------------------------------------------------------------------------
+// Row triples into per-node frames: rows (3c, 3c+1, 3c+2) of A (and of b)
+// become F_c times them (equations.py:467-473, the einsum of apply_fault_rows).
+// One thread per (node, column); a warp reads 32 consecutive columns.
+// ---------------------------------------------------------------------------
+__global__ void rotate_row_triples_kernel(double* __restrict__ A, int64_t ld, int64_t n_cols,
+                                          double* __restrict__ b, int64_t n_nodes,
+                                          const double* __restrict__ F) {
+    const int64_t c = blockIdx.y;
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const double* f = F + 9 * c;
+    if (j < n_cols) {
+        double* a0 = A + (3 * c) * ld + j;
+        const double x0 = a0[0], x1 = a0[ld], x2 = a0[2 * ld];
+        a0[0] = (f[0] * x0 + f[1] * x1) + f[2] * x2;
+        a0[ld] = (f[3] * x0 + f[4] * x1) + f[5] * x2;
+        a0[2 * ld] = (f[6] * x0 + f[7] * x1) + f[8] * x2;
+    }
+    if (b != nullptr && blockIdx.x == 0 && threadIdx.x == 0) {
+        double* bb = b + 3 * c;
+        const double x0 = bb[0], x1 = bb[1], x2 = bb[2];
+        bb[0] = (f[0] * x0 + f[1] * x1) + f[2] * x2;
+        bb[1] = (f[3] * x0 + f[4] * x1) + f[5] * x2;
+        bb[2] = (f[6] * x0 + f[7] * x1) + f[8] * x2;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // y = alpha A x + beta y: 4 rows per warp, 128-bit streaming loads of A
 // ---------------------------------------------------------------------------
 constexpr int GEMV_ROWS = 4;
@@ -473,6 +500,21 @@ int mbem_add_block_diagonal(double* A, int64_t ld, const double* D, int64_t n_c,
     for (int i = 0; i < K * K; i++) sk.w[i] = shape[i];
     add_block_diag_kernel<<<(unsigned)ceil_div(n_c, 128), 128, 0, (cudaStream_t)stream>>>(A, ld, D, n_c, K, sk);
     return launch_status("add_block_diag_kernel");
+}
+
+int mbem_rotate_row_triples(double* A, int64_t ld, int64_t n_cols, double* b, int64_t n_nodes,
+                            const double* frames, void* stream) {
+    MBEM_REQUIRE(n_nodes >= 0 && n_cols >= 0 && ld >= n_cols, MBEM_ERR_ARG, "bad row-triple shape");
+    MBEM_REQUIRE(n_nodes == 0 || (A && frames), MBEM_ERR_ARG, "NULL A or frames");
+    int64_t launches = 0;
+    for (int64_t c0 = 0; c0 < n_nodes; c0 += 65535) {     // grid rows per launch
+        const int64_t nc = lmin(65535, n_nodes - c0);
+        const dim3 grid((unsigned)lmax(1, ceil_div(n_cols, 256)), (unsigned)nc);
+        rotate_row_triples_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(
+            A + 3 * c0 * ld, ld, n_cols, b ? b + 3 * c0 : nullptr, nc, frames + 9 * c0);
+        launches++;
+    }
+    return launch_status("rotate_row_triples_kernel", launches);
 }
 
 int mbem_dgemv(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols, const double* x, double alpha,

@@ -188,6 +188,64 @@ struct TMoments {
     double V3[3], V5[3], t[3], W[3][3];   // global frame
 };
 
+// T-kernel moments V3, V5, t, W (global frame) from the 2-D moments of the
+// source frame (ex, ey, nh); shared by the P0 pair and the nodal tables.
+struct TScal {
+    double z, I3, I5, m10_3, m01_3, m10_5, m01_5, m20_5, m11_5, m02_5, m30_5, m21_5, m12_5, m03_5;
+};
+
+__device__ __forceinline__ void t_from_scal(const double* ex, const double* ey, const double* nh,
+                                            const double* __restrict__ nrm, const TScal& q, TMoments& m) {
+    const double z = q.z, I3 = q.I3, I5 = q.I5;
+    const double m10_3 = q.m10_3, m01_3 = q.m01_3, m10_5 = q.m10_5, m01_5 = q.m01_5;
+    const double m20_5 = q.m20_5, m11_5 = q.m11_5, m02_5 = q.m02_5;
+    const double m30_5 = q.m30_5, m21_5 = q.m21_5, m12_5 = q.m12_5, m03_5 = q.m03_5;
+    // local frame (ex, ey, nh): d = (-xi1, -xi2, z)
+    const double V3l[3] = {-m10_3, -m01_3, z * I3};
+    const double V5l[3] = {-m10_5, -m01_5, z * I5};
+    const double z2 = z * z;
+    // T3 in the local frame, T[a][b][c] = (-1)^(#0+#1) z^(#2) M5(#0,#1)
+    const double T000 = -m30_5, T001 = -m21_5, T002 = z * m20_5, T011 = -m12_5,
+                 T012 = z * m11_5, T022 = -z2 * m10_5, T111 = -m03_5, T112 = z * m02_5,
+                 T122 = -z2 * m01_5, T222 = z2 * z * I5;
+    const double tl[3] = {T000 + T011 + T022, T001 + T111 + T122, T002 + T112 + T222};
+    // local normal of the source normal passed in (may differ from nh)
+    const double nl0 = nrm[0] * ex[0] + nrm[1] * ex[1] + nrm[2] * ex[2];
+    const double nl1 = nrm[0] * ey[0] + nrm[1] * ey[1] + nrm[2] * ey[2];
+    const double nl2 = nrm[0] * nh[0] + nrm[1] * nh[1] + nrm[2] * nh[2];
+    double Wl[3][3];
+    Wl[0][0] = T000 * nl0 + T001 * nl1 + T002 * nl2;
+    Wl[0][1] = T001 * nl0 + T011 * nl1 + T012 * nl2;
+    Wl[0][2] = T002 * nl0 + T012 * nl1 + T022 * nl2;
+    Wl[1][1] = T011 * nl0 + T111 * nl1 + T112 * nl2;
+    Wl[1][2] = T012 * nl0 + T112 * nl1 + T122 * nl2;
+    Wl[2][2] = T022 * nl0 + T122 * nl1 + T222 * nl2;
+    Wl[1][0] = Wl[0][1]; Wl[2][0] = Wl[0][2]; Wl[2][1] = Wl[1][2];
+    // rotate to the global frame: v = Q^T v_l, W = Q^T W_l Q (Q rows ex, ey, nh)
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const double qi[3] = {ex[i], ey[i], nh[i]};
+        m.V3[i] = qi[0] * V3l[0] + qi[1] * V3l[1] + qi[2] * V3l[2];
+        m.V5[i] = qi[0] * V5l[0] + qi[1] * V5l[1] + qi[2] * V5l[2];
+        m.t[i] = qi[0] * tl[0] + qi[1] * tl[1] + qi[2] * tl[2];
+    }
+    double Y[3][3];  // Y = W_l Q  (3x3 local-by-global)
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            Y[a][j] = Wl[a][0] * ex[j] + Wl[a][1] * ey[j] + Wl[a][2] * nh[j];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = i; j < 3; j++) {
+            double w = ex[i] * Y[0][j] + ey[i] * Y[1][j] + nh[i] * Y[2][j];
+            m.W[i][j] = w;
+            m.W[j][i] = w;
+        }
+}
+
+
 __device__ __forceinline__ void t_moments(const SrcP0& s, const double* __restrict__ nrm,
                                           const PairP0& p, TMoments& m) {
     double BN1_001 = 0, BN2_001 = 0, BD003 = 0, BN1_003 = 0, BN2_003 = 0, BN1_103 = 0,
@@ -222,49 +280,8 @@ __device__ __forceinline__ void t_moments(const SrcP0& s, const double* __restri
     const double m02_5 = (I3 - BN2_013) * third;
     const double m30_5 = (2.0 * m10_3 - BN1_203) * third, m21_5 = (m01_3 - BN1_113) * third;
     const double m12_5 = -BN1_023 * third, m03_5 = (2.0 * m01_3 - BN2_023) * third;
-    // local frame (ex, ey, nh): d = (-xi1, -xi2, z)
-    const double V3l[3] = {-m10_3, -m01_3, z * I3};
-    const double V5l[3] = {-m10_5, -m01_5, z * I5};
-    const double z2 = z * z;
-    // T3 in the local frame, T[a][b][c] = (-1)^(#0+#1) z^(#2) M5(#0,#1)
-    const double T000 = -m30_5, T001 = -m21_5, T002 = z * m20_5, T011 = -m12_5,
-                 T012 = z * m11_5, T022 = -z2 * m10_5, T111 = -m03_5, T112 = z * m02_5,
-                 T122 = -z2 * m01_5, T222 = z2 * z * I5;
-    const double tl[3] = {T000 + T011 + T022, T001 + T111 + T122, T002 + T112 + T222};
-    // local normal of the source normal passed in (may differ from nh)
-    const double nl0 = nrm[0] * s.ex[0] + nrm[1] * s.ex[1] + nrm[2] * s.ex[2];
-    const double nl1 = nrm[0] * s.ey[0] + nrm[1] * s.ey[1] + nrm[2] * s.ey[2];
-    const double nl2 = nrm[0] * s.nh[0] + nrm[1] * s.nh[1] + nrm[2] * s.nh[2];
-    double Wl[3][3];
-    Wl[0][0] = T000 * nl0 + T001 * nl1 + T002 * nl2;
-    Wl[0][1] = T001 * nl0 + T011 * nl1 + T012 * nl2;
-    Wl[0][2] = T002 * nl0 + T012 * nl1 + T022 * nl2;
-    Wl[1][1] = T011 * nl0 + T111 * nl1 + T112 * nl2;
-    Wl[1][2] = T012 * nl0 + T112 * nl1 + T122 * nl2;
-    Wl[2][2] = T022 * nl0 + T122 * nl1 + T222 * nl2;
-    Wl[1][0] = Wl[0][1]; Wl[2][0] = Wl[0][2]; Wl[2][1] = Wl[1][2];
-    // rotate to the global frame: v = Q^T v_l, W = Q^T W_l Q (Q rows ex, ey, nh)
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const double qi[3] = {s.ex[i], s.ey[i], s.nh[i]};
-        m.V3[i] = qi[0] * V3l[0] + qi[1] * V3l[1] + qi[2] * V3l[2];
-        m.V5[i] = qi[0] * V5l[0] + qi[1] * V5l[1] + qi[2] * V5l[2];
-        m.t[i] = qi[0] * tl[0] + qi[1] * tl[1] + qi[2] * tl[2];
-    }
-    double Y[3][3];  // Y = W_l Q  (3x3 local-by-global)
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int j = 0; j < 3; j++)
-            Y[a][j] = Wl[a][0] * s.ex[j] + Wl[a][1] * s.ey[j] + Wl[a][2] * s.nh[j];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = i; j < 3; j++) {
-            double w = s.ex[i] * Y[0][j] + s.ey[i] * Y[1][j] + s.nh[i] * Y[2][j];
-            m.W[i][j] = w;
-            m.W[j][i] = w;
-        }
+    TScal q{z, I3, I5, m10_3, m01_3, m10_5, m01_5, m20_5, m11_5, m02_5, m30_5, m21_5, m12_5, m03_5};
+    t_from_scal(s.ex, s.ey, s.nh, nrm, q, m);
 }
 
 // Combined T block with six coefficients.

@@ -40,6 +40,16 @@ def c1_rows():
 
 
 @pytest.fixture(scope="session")
+def nodal_pairs():
+    return load_golden("nodal_pairs")
+
+
+@pytest.fixture(scope="session")
+def traction_small():
+    return load_golden("traction_small")
+
+
+@pytest.fixture(scope="session")
 def oracle():
     from oracle import oracle as orc
     orc.lib()

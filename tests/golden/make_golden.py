@@ -212,8 +212,80 @@ def make_c1_rows(path):
     np.savez_compressed(path, **out)
 
 
+def make_nodal_pairs(path):
+    """The order-generic public drivers (tri_nodal.py:1257-1404) at orders 1
+    and 2, and the traction rows at orders 0, 1 and 2, on the scattered
+    geometry (the collinear triangle dropped: nodal orders refuse it) plus
+    observers far enough for both Gauss rules (D > 10 L and D > 40 L)."""
+    import mbem.kernels.tri_nodal as tn
+    _, kb = _ref()
+    x, tv, n, eps, _ = pair_geometry()
+    tv, n, eps = tv[:-1], n[:-1], eps[:-1]
+    rng = np.random.default_rng(77)
+    far = rng.normal(size=(6, 3))
+    far = far / np.linalg.norm(far, axis=1)[:, None] * np.array([25.0, 30.0, 45.0, 80.0, 120.0, 200.0])[:, None]
+    x = np.ascontiguousarray(np.concatenate([x, far]))
+    nf = rng.normal(size=x.shape)
+    nf = np.ascontiguousarray(nf / np.linalg.norm(nf, axis=1)[:, None])
+    out = dict(x_field=x, n_field=nf, tri_verts=tv, normals=n, eps=eps, materials=MATERIALS)
+    t0 = time.time()
+    for order in (1, 2):
+        K = tn.n_nodes(order)
+        dens = rng.normal(size=(K * tv.shape[0], 3))
+        dens[3 * K:4 * K] = 0.0
+        out[f"density_{order}"] = dens
+        mu, lam = MATERIALS[0]
+        c = kb.t_coeffs(mu, lam)
+        g = kb.u_coeffs(mu, lam)
+        out[f"t_matrix_{order}"] = tn.t_matrix_direct(x, tv, n, eps, *c, order)
+        out[f"u_matrix_{order}"] = tn.u_matrix_direct(x, tv, eps, *g, order)
+        out[f"t_disp_{order}"] = tn.t_disp_contract(x, tv, n, eps, dens, *c, order)
+        out[f"u_disp_{order}"] = tn.u_disp_contract(x, tv, eps, dens, *g, order)
+        for m, (mu, lam) in enumerate(MATERIALS):
+            out[f"dd_stress_{order}_{m}"] = tn.dd_stress_contract(x, tv, n, eps, dens, mu, lam, order)
+            out[f"kelvin_stress_{order}_{m}"] = tn.kelvin_stress_contract(x, tv, eps, dens, mu, lam, order)
+            out[f"eigenstress_{order}_{m}"] = tn.eigenstress_contract(x, tv, n, eps, dens, mu, lam, order)
+        print(f"nodal order {order}: {time.time() - t0:.1f} s", flush=True)
+    for order in (0, 1, 2):
+        ids = kb.identity_ids(order, tv.shape[0])
+        for which in ("slip", "force", "eigen", "total"):
+            mu, lam = MATERIALS[1 if which == "slip" else 0]
+            out[f"traction_{order}_{which}"] = tn.traction_matrix(x, nf, tv, n, eps, ids, ids.size, mu, lam,
+                                                                  order, which)
+        print(f"traction order {order}: {time.time() - t0:.1f} s", flush=True)
+    np.savez_compressed(path, **out)
+
+
+def make_traction_small(path):
+    """A FAULT_TRACTION fault (solved slip under a uniform shear-traction
+    drop, order 0) in a 2x2-per-face cube: the reference's whole system with
+    traction rows, the fault-row frame and the constraint rows, and its LU
+    solution."""
+    import local_box_mesh as lbm
+    from mollified_bem import ElasticMaterial
+    from mbem.backends.dense import AssembledDense
+    from mbem.model import BCType, Patch, Region, RegionModel
+    from mbem.model.equations import generate_system
+
+    model_ref, cube, fmesh = reference_cube_model(2, 2, 1.0, 1.0)
+    mat = ElasticMaterial(mu=1.0, lam=1.0)
+    drop = np.array([-1e-3, 0.0, 0.0])
+    cube_p = Patch("cube", cube, BCType.FREE_TRACTION)
+    fault_p = Patch("fault", fmesh, BCType.FAULT_TRACTION, value=drop)
+    model = RegionModel([Region("body", mat, [cube_p], np.zeros(3), faults=[fault_p])])
+    eps = (4.0 / 2) / 2.0
+    t0 = time.time()
+    asm = AssembledDense(generate_system(model), eps, "direct", jump="calibrated", deflate=True)
+    sol = asm.solve()
+    print(f"traction_small: {time.time() - t0:.1f} s", flush=True)
+    np.savez_compressed(path, cube_vertices=cube.vertices, cube_triangles=cube.triangles,
+                        fault_vertices=fmesh.vertices, fault_triangles=fmesh.triangles, eps=eps,
+                        drop=drop, A=asm.A, b=asm.b, x_u=sol["u:cube"], x_b=sol["b:fault"])
+
+
 CASES = {"p0_pairs": make_p0_pairs, "cube_small": make_cube_small,
-         "c1_rows": make_c1_rows}
+         "c1_rows": make_c1_rows, "nodal_pairs": make_nodal_pairs,
+         "traction_small": make_traction_small}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(CASES)

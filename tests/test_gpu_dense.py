@@ -96,3 +96,30 @@ def test_half_jump_and_anchor_rules(gpu):
     for c in range(A.shape[0] // 3):
         off[3 * c:3 * c + 3, 3 * c:3 * c + 3] = 0.0
     assert np.abs(off).max() == 0.0
+
+
+def test_fault_traction_system_and_solution(gpu, traction_small):
+    """A FAULT_TRACTION fault (solved slip under a uniform shear-traction
+    drop) in a 2x2-per-face cube: the whole system (traction rows through the
+    nodal machinery at order 0, row frame, constraint rows) and the slip
+    against the reference's bordered LU."""
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.model import BCType, generate_system
+    g = traction_small
+    model, eps = cube_fault_model(2, 2, fault_kind=BCType.FAULT_TRACTION, fault_value=g["drop"])
+    assert eps == float(g["eps"])
+    cube = model.regions[0].patches[0].mesh
+    fault = model.regions[0].faults[0].mesh
+    assert np.array_equal(cube.vertices, g["cube_vertices"])
+    assert np.array_equal(fault.triangles, g["fault_triangles"])
+    asm = DenseBackend(jump="calibrated", deflate=True, rtol=1e-13).assemble(generate_system(model), eps)
+    assert rel_err(asm.A.cpu().numpy(), g["A"]) < 1e-12
+    assert rel_err(asm.b.cpu().numpy(), g["b"]) < 1e-12
+    sol = asm.solve()
+    assert asm.report.converged
+    assert rel_err(sol["u:cube"], g["x_u"]) < 1e-10
+    assert rel_err(sol["b:fault"], g["x_b"]) < 1e-10
+    # the constraint rows hold: no opening
+    nrm = model.regions[0].faults[0].collocation_normals()
+    assert np.abs(np.einsum("ij,ij->i", sol["b:fault"], nrm)).max() < 1e-12 * np.abs(sol["b:fault"]).max()

@@ -1,0 +1,151 @@
+"""CUDA nodal (P1/P2) kernels and traction rows against the reference's
+golden vectors (tri_nodal.py public drivers, orders 0/1/2).
+
+The geometry holds the near regimes of the edge primitives (small-|u|
+series, large-|u| series, closed form), a needle (height / L = 2e-3, where
+the closed form loses (L / height)^2 digits of every formulation), observers
+on vertices and edges, and observers in both far Gauss rules.
+
+Tolerance: 1e-10 of the largest entry of each output. Rounding differs
+from the reference (reciprocal multiplies, another summation order of the
+frame rotations), and the needle amplifies those ulps by (L / height)^2.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def tn(gpu):
+    from mbem_gb300.kernels import tri_nodal
+    return tri_nodal
+
+
+@pytest.fixture(scope="module")
+def coeffs():
+    from mbem_gb300.kernels import basis
+    return basis
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_nodal_matrices(tn, coeffs, nodal_pairs, order):
+    g = nodal_pairs
+    mu, lam = g["materials"][0]
+    c = coeffs.t_coeffs(mu, lam)
+    u = coeffs.u_coeffs(mu, lam)
+    x, tv, n, e = g["x_field"], g["tri_verts"], g["normals"], g["eps"]
+    T = tn.t_matrix_direct(x, tv, n, e, *c, order=order)
+    U = tn.u_matrix_direct(x, tv, e, *u, order=order)
+    assert rel_err(T, g[f"t_matrix_{order}"]) < TOL
+    assert rel_err(U, g[f"u_matrix_{order}"]) < TOL
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_nodal_basis_stacks_combine_to_direct(tn, coeffs, nodal_pairs, order):
+    g = nodal_pairs
+    mu, lam = g["materials"][0]
+    c = np.asarray(coeffs.t_coeffs(mu, lam))
+    u = np.asarray(coeffs.u_coeffs(mu, lam))
+    x, tv, n, e = g["x_field"], g["tri_verts"], g["normals"], g["eps"]
+    TB = tn.t_basis_matrices(x, tv, n, e, order=order)
+    UB = tn.u_basis_matrices(x, tv, e, order=order)
+    K = tn.n_nodes(order)
+    assert TB.shape == (6, 3 * x.shape[0], 3 * K * tv.shape[0])
+    assert rel_err(np.tensordot(c, TB, axes=1), g[f"t_matrix_{order}"]) < TOL
+    assert rel_err(np.tensordot(u, UB, axes=1), g[f"u_matrix_{order}"]) < TOL
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("m", [0, 1])
+def test_nodal_contractions(tn, coeffs, nodal_pairs, order, m):
+    g = nodal_pairs
+    x, tv, n, e = g["x_field"], g["tri_verts"], g["normals"], g["eps"]
+    d = g[f"density_{order}"]
+    mu, lam = g["materials"][m]
+    if m == 0:
+        c = coeffs.t_coeffs(mu, lam)
+        u = coeffs.u_coeffs(mu, lam)
+        assert rel_err(tn.t_disp_contract(x, tv, n, e, d, *c, order=order), g[f"t_disp_{order}"]) < TOL
+        assert rel_err(tn.u_disp_contract(x, tv, e, d, *u, order=order), g[f"u_disp_{order}"]) < TOL
+    dd = tn.dd_stress_contract(x, tv, n, e, d, mu, lam, order=order)
+    ks = tn.kelvin_stress_contract(x, tv, e, d, mu, lam, order=order)
+    es = tn.eigenstress_contract(x, tv, n, e, d, mu, lam, order=order)
+    el = tn.elastic_stress_contract(x, tv, n, e, d, mu, lam, order=order)
+    assert rel_err(dd, g[f"dd_stress_{order}_{m}"]) < TOL
+    assert rel_err(ks, g[f"kelvin_stress_{order}_{m}"]) < TOL
+    assert rel_err(es, g[f"eigenstress_{order}_{m}"]) < TOL
+    assert rel_err(el, g[f"dd_stress_{order}_{m}"] - g[f"eigenstress_{order}_{m}"]) < TOL
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_nodal_contraction_equals_matrix_times_density(tn, coeffs, nodal_pairs, order):
+    g = nodal_pairs
+    x, tv, n, e = g["x_field"], g["tri_verts"], g["normals"], g["eps"]
+    d = g[f"density_{order}"]
+    c = coeffs.t_coeffs(*g["materials"][0])
+    T = tn.t_matrix_direct(x, tv, n, e, *c, order=order)
+    v = tn.t_disp_contract(x, tv, n, e, d, *c, order=order)
+    assert rel_err(v.reshape(-1), T @ d.reshape(-1)) < 1e-12
+
+
+@pytest.mark.parametrize("order", [0, 1, 2])
+@pytest.mark.parametrize("which", ["slip", "force", "eigen", "total"])
+def test_traction_rows(tn, coeffs, nodal_pairs, order, which):
+    g = nodal_pairs
+    x, nf, tv, n, e = g["x_field"], g["n_field"], g["tri_verts"], g["normals"], g["eps"]
+    mu, lam = g["materials"][1 if which == "slip" else 0]
+    ids = coeffs.identity_ids(order, tv.shape[0])
+    R = tn.traction_matrix(x, nf, tv, n, e, ids, ids.size, mu, lam, order, which)
+    assert rel_err(R, g[f"traction_{order}_{which}"]) < TOL
+
+
+def test_traction_shared_ids_add_columns(tn, coeffs, nodal_pairs):
+    """A shared-node ids table sums the element-major columns it merges."""
+    g = nodal_pairs
+    x, nf, tv, n, e = g["x_field"], g["n_field"], g["tri_verts"], g["normals"], g["eps"]
+    mu, lam = g["materials"][0]
+    K = tn.n_nodes(1)
+    ids = coeffs.identity_ids(1, tv.shape[0]) % 7          # collisions on purpose
+    R = tn.traction_matrix(x, nf, tv, n, e, ids, 7, mu, lam, 1, "slip")
+    full = g["traction_1_total"] - g["traction_1_eigen"]
+    want = np.zeros((full.shape[0], 21))
+    for col in range(K * tv.shape[0]):
+        want[:, 3 * (col % 7):3 * (col % 7) + 3] += full[:, 3 * col:3 * col + 3]
+    assert rel_err(R, want) < TOL
+
+
+def test_traction_accumulates_into_a_block(tn, coeffs, nodal_pairs):
+    g = nodal_pairs
+    x, nf, tv, n, e = g["x_field"], g["n_field"], g["tri_verts"], g["normals"], g["eps"]
+    mu, lam = g["materials"][0]
+    ids = coeffs.identity_ids(0, tv.shape[0])
+    rows, cols = 3 * x.shape[0], 3 * ids.size
+    big = torch.ones((rows + 5, cols + 9), dtype=torch.float64, device="cuda")
+    blk = big[2:2 + rows, 4:4 + cols]
+    tn.traction_matrix(x, nf, tv, n, e, ids, ids.size, mu, lam, 0, "force", out=blk, alpha=-2.0)
+    got = big.cpu().numpy()
+    assert rel_err(got[2:2 + rows, 4:4 + cols], 1.0 - 2.0 * g["traction_0_force"]) < TOL
+    got[2:2 + rows, 4:4 + cols] = 1.0
+    assert np.all(got == 1.0)
+
+
+def test_nodal_refuses_bad_inputs(tn, coeffs, nodal_pairs):
+    g = nodal_pairs
+    x, nf, tv, n, e = g["x_field"], g["n_field"], g["tri_verts"], g["normals"], g["eps"]
+    ids = coeffs.identity_ids(1, tv.shape[0])
+    with pytest.raises(ValueError):
+        tn.traction_matrix(x, nf, tv, n, e, ids[:, :2], ids.size, 1.0, 1.0, 1)
+    with pytest.raises(ValueError):
+        tn.traction_matrix(x, nf, tv, n, e, ids, ids.size - 1, 1.0, 1.0, 1)
+    needle = np.array([[[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.5, 1e-6, 0.0]]])
+    with pytest.raises(ValueError):
+        tn.t_matrix_direct(x, needle, np.array([[0.0, 0.0, 1.0]]), e[:1], *coeffs.t_coeffs(1.0, 1.0),
+                           order=1)
+    empty = tn.t_matrix_direct(x[:0], tv, n, e, *coeffs.t_coeffs(1.0, 1.0), order=2)
+    assert empty.shape == (0, 3 * 6 * tv.shape[0])
