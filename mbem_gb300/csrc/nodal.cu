@@ -815,14 +815,19 @@ nodal_matrix_kernel(NodalArgs a, NodalSpec sp, int kind) {
 
 // contractions: one thread per field point; kind 0 T disp, 1 U disp, 2+w stress
 __global__ void __launch_bounds__(ND_THREADS)
-nodal_contract_kernel(NodalArgs a, NodalSpec sp, int kind) {
-    const int64_t f = (int64_t)blockIdx.x * ND_THREADS + threadIdx.x;
-    if (f >= a.n_field_pts) return;
+nodal_contract_kernel(NodalArgs a, NodalSpec sp, int kind, int split) {
+    // split threads per observer take interleaved sources; their partial sums
+    // are added in slice order (deterministic)
+    __shared__ double red[ND_THREADS][9];
+    const int obs_per_block = ND_THREADS / split;
+    const int lane = threadIdx.x % obs_per_block, slice = threadIdx.x / obs_per_block;
+    const int64_t f = (int64_t)blockIdx.x * obs_per_block + lane;
+    const bool active = f < a.n_field_pts;
     const int K = sp.K;
     double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     double W[4][ND_MAXK][5][5];
     NodalScratch S;
-    for (int64_t s = 0; s < a.n_src; s++) {
+    for (int64_t s = slice; active && s < a.n_src; s += split) {
         bool zero = true;
         for (int k = 0; k < K * 3 && zero; k++) zero = a.density[3 * K * s + k] == 0.0;
         if (zero) continue;
@@ -856,6 +861,14 @@ nodal_contract_kernel(NodalArgs a, NodalSpec sp, int kind) {
         }
     }
     const int nout = kind <= 1 ? 3 : 9;
+    if (split > 1) {
+        for (int i = 0; i < nout; i++) red[threadIdx.x][i] = acc[i];
+        __syncthreads();
+        if (slice != 0) return;
+        for (int k = 1; k < split; k++)
+            for (int i = 0; i < nout; i++) acc[i] += red[k * obs_per_block + lane][i];
+    }
+    if (!active) return;
     double* o = a.out + nout * f;
     for (int i = 0; i < nout; i++) {
         const double v = a.alpha * acc[i];
@@ -863,36 +876,40 @@ nodal_contract_kernel(NodalArgs a, NodalSpec sp, int kind) {
     }
 }
 
-// traction rows: out[3f+i, 3 ids[s,k] + j] += alpha * n_f . sigma(e_j density of node k)
+// traction rows: out[3f+i, 3 ids[s,k] + j] += alpha * n_f . sigma(e_j density of node k).
+// One thread per (field point, source), sources fastest so that a warp
+// writes neighbouring columns of the same rows. Entries are added
+// atomically: a shared-node ids table maps several sources onto one column
+// (the element-major table maps each entry once, so its result does not
+// depend on the order of the adds).
 __global__ void __launch_bounds__(ND_THREADS)
 nodal_traction_kernel(NodalArgs a, NodalSpec sp) {
-    const int64_t f = (int64_t)blockIdx.x * ND_THREADS + threadIdx.x;
-    if (f >= a.n_field_pts) return;
+    const int64_t idx = (int64_t)blockIdx.x * ND_THREADS + threadIdx.x;
+    if (idx >= a.n_field_pts * a.n_src) return;
+    const int64_t f = idx / a.n_src, s = idx % a.n_src;
     const int K = sp.K;
     const double* nf = a.n_field + 3 * f;
     double W[4][ND_MAXK][5][5];
     NodalScratch S;
     // which: 0 slip (dd - eigen), 1 force, 2 eigen, 3 total (dd)
     const int sw = a.which == 0 ? 3 : (a.which == 1 ? 1 : (a.which == 2 ? 2 : 0));
-    for (int64_t s = 0; s < a.n_src; s++) {
-        NodalSrc g;
-        if (!nodal_frame(a.tri_verts + 9 * s, g)) continue;
-        const double eps = a.eps[s];
-        const double z = nodal_pair_tables(sp, g, a.x_field + 3 * f, eps, W, S);
-        const double zero_n[3] = {0.0, 0.0, 0.0};
-        const double* nrm = a.normals ? a.normals + 3 * s : zero_n;
-        for (int k = 0; k < K; k++) {
-            const int64_t id = a.ids[s * K + k];
-            if (id < 0 || id >= a.n_cols) continue;        // outside the block: never written
-            const int64_t col = 3 * id;
-            for (int j = 0; j < 3; j++) {
-                const double d[3] = {j == 0 ? 1.0 : 0.0, j == 1 ? 1.0 : 0.0, j == 2 ? 1.0 : 0.0};
-                double sg[3][3];
-                node_stress(g, W, k, z, nrm, d, eps, a.mu, a.lam, sw, sg);
-                for (int i = 0; i < 3; i++) {
-                    const double t = nf[0] * sg[i][0] + nf[1] * sg[i][1] + nf[2] * sg[i][2];
-                    a.out[(3 * f + i) * a.ld + col + j] += a.alpha * t;
-                }
+    NodalSrc g;
+    if (!nodal_frame(a.tri_verts + 9 * s, g)) return;
+    const double eps = a.eps[s];
+    const double z = nodal_pair_tables(sp, g, a.x_field + 3 * f, eps, W, S);
+    const double zero_n[3] = {0.0, 0.0, 0.0};
+    const double* nrm = a.normals ? a.normals + 3 * s : zero_n;
+    for (int k = 0; k < K; k++) {
+        const int64_t id = a.ids[s * K + k];
+        if (id < 0 || id >= a.n_cols) continue;        // outside the block: never written
+        const int64_t col = 3 * id;
+        for (int j = 0; j < 3; j++) {
+            const double d[3] = {j == 0 ? 1.0 : 0.0, j == 1 ? 1.0 : 0.0, j == 2 ? 1.0 : 0.0};
+            double sg[3][3];
+            node_stress(g, W, k, z, nrm, d, eps, a.mu, a.lam, sw, sg);
+            for (int i = 0; i < 3; i++) {
+                const double t = nf[0] * sg[i][0] + nf[1] * sg[i][1] + nf[2] * sg[i][2];
+                atomicAdd(&a.out[(3 * f + i) * a.ld + col + j], a.alpha * t);
             }
         }
     }
@@ -945,7 +962,10 @@ int nodal_contract(int kind, const double* x, int64_t nf, const double* tv, cons
     for (int i = 0; i < 6; i++) a.c[i] = (coeffs && i < (kind == 0 ? 6 : 3)) ? coeffs[i] : 0.0;
     a.mu = mu; a.lam = lam; a.alpha = alpha; a.accumulate = accumulate; a.out = out;
     if (nf == 0) return MBEM_OK;
-    nodal_contract_kernel<<<(unsigned)ceil_div(nf, ND_THREADS), ND_THREADS, 0, (cudaStream_t)stream>>>(a, sp, kind);
+    int split = 1;      // about eight 64-thread blocks per SM (152 SMs)
+    while (split < 16 && nf * split < (int64_t)152 * 8 * ND_THREADS) split *= 2;
+    nodal_contract_kernel<<<(unsigned)ceil_div(nf, ND_THREADS / split), ND_THREADS, 0, (cudaStream_t)stream>>>(
+        a, sp, kind, split);
     return launch_status("nodal_contract_kernel");
 }
 
@@ -976,7 +996,8 @@ extern "C" int mbem_traction_matrix(const double* x_field, const double* n_field
     a.x_field = x_field; a.n_field = n_field; a.n_field_pts = n_pts; a.tri_verts = tri_verts;
     a.normals = normals; a.eps = eps; a.n_src = n_src; a.ids = ids; a.n_cols = n_cols;
     a.mu = mu; a.lam = lam; a.alpha = alpha; a.which = which; a.out = out; a.ld = ld_out;
-    if (n_pts == 0) return MBEM_OK;
-    nodal_traction_kernel<<<(unsigned)ceil_div(n_pts, ND_THREADS), ND_THREADS, 0, (cudaStream_t)stream>>>(a, sp);
+    if (n_pts == 0 || n_src == 0) return MBEM_OK;
+    nodal_traction_kernel<<<(unsigned)ceil_div(n_pts * n_src, ND_THREADS), ND_THREADS, 0, (cudaStream_t)stream>>>(
+        a, sp);
     return launch_status("nodal_traction_kernel");
 }

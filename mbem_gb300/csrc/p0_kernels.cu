@@ -165,6 +165,7 @@ struct ConArgs {
     double alpha;
     int accumulate;
     double* out;
+    int split;       // source slices per observer (1, 2, 4, 8 or 16)
 };
 
 struct SrcTile {
@@ -177,8 +178,16 @@ struct SrcTile {
 template <int KIND>
 __global__ void __launch_bounds__(CON_THREADS)
 p0_contract_kernel(ConArgs a) {
+    // A block holds CON_THREADS / split observers; the split threads of an
+    // observer take interleaved sources of each tile and their partial sums
+    // are added in slice order at the end (deterministic).
     __shared__ SrcTile tile[SRC_TILE];
-    const int64_t f = (int64_t)blockIdx.x * CON_THREADS + threadIdx.x;
+    __shared__ double red[CON_THREADS][9];
+    const int split = a.split;
+    const int obs_per_block = CON_THREADS / split;
+    const int lane = threadIdx.x % obs_per_block;
+    const int slice = threadIdx.x / obs_per_block;
+    const int64_t f = (int64_t)blockIdx.x * obs_per_block + lane;
     const bool active = f < a.n_field;
     double ox = 0, oy = 0, oz = 0;
     if (active) {
@@ -212,7 +221,7 @@ p0_contract_kernel(ConArgs a) {
         __syncthreads();
         if (!active) continue;
         const int ns = (int)lmin(SRC_TILE, a.n_src - s0);
-        for (int t = 0; t < ns; t++) {
+        for (int t = slice; t < ns; t += split) {
             const SrcTile& T = tile[t];
             if (!T.live) continue;
             const SrcP0& sg = T.g;
@@ -284,13 +293,29 @@ p0_contract_kernel(ConArgs a) {
             }
         }
     }
-    if (!active) return;
     const int nout = STRESS ? 9 : 3;
+    if (split > 1) {
+        __syncthreads();
+        for (int i = 0; i < nout; i++) red[threadIdx.x][i] = acc[i];
+        __syncthreads();
+        if (slice != 0) return;
+        for (int k = 1; k < split; k++)
+            for (int i = 0; i < nout; i++) acc[i] += red[k * obs_per_block + lane][i];
+    }
+    if (!active) return;
     double* o = a.out + nout * f;
     for (int i = 0; i < nout; i++) {
         const double v = a.alpha * acc[i];
         o[i] = a.accumulate ? o[i] + v : v;
     }
+}
+
+// Slices per observer so that a launch holds about four 128-thread blocks
+// per SM (152 SMs) whatever the observer count.
+static int contract_split(int64_t nf) {
+    int split = 1;
+    while (split < 16 && nf * split < (int64_t)152 * 4 * CON_THREADS) split *= 2;
+    return split;
 }
 
 static int check_common(const double* x, int64_t nf, const double* tv, const double* eps, int64_t ns,
@@ -331,7 +356,8 @@ int launch_contract(int kind, const double* x, int64_t nf, const double* tv, con
     for (int i = 0; i < 6; i++) a.c[i] = (c && i < nc) ? c[i] : 0.0;
     a.mu = mu; a.lam = lam; a.alpha = alpha; a.accumulate = accumulate; a.out = out;
     if (nf == 0) return MBEM_OK;
-    dim3 grid((unsigned)ceil_div(nf, CON_THREADS));
+    a.split = contract_split(nf);
+    dim3 grid((unsigned)ceil_div(nf, CON_THREADS / a.split));
     switch (kind) {
         case CON_T_DISP: p0_contract_kernel<CON_T_DISP><<<grid, CON_THREADS, 0, st>>>(a); break;
         case CON_U_DISP: p0_contract_kernel<CON_U_DISP><<<grid, CON_THREADS, 0, st>>>(a); break;
