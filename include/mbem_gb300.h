@@ -213,6 +213,36 @@ int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y,
 int mbem_mixed_matvec_noalloc(const mbem_mixed_operator* op, const double* x, double* y,
                               void* stream);
 
+/* ---- cluster block-Jacobi preconditioner (la/preconditioner.py:421-470,
+ * the "block_jacobi" rung; chunks from la/cluster.py:56-75 bisection, built
+ * by the caller). The chunks partition 0..n-1; chunk c holds the DOFs
+ * dofs[chunk_ptr[c] .. chunk_ptr[c+1]) (at most MBEM_BJ_MAX_DOF of them,
+ * so that a chunk's FP32 copy fits one CTA's shared memory). local[d] is
+ * the position of DOF d in its chunk and chunk_of[d] its chunk (both needed
+ * by the mixed build only). inv holds mbem_bj_inverse_bytes() of FP32
+ * inverses, written by a build, read by mbem_bj_apply. All device memory
+ * is the caller's. --------------------------------------------------- */
+#define MBEM_BJ_MAX_DOF 225
+typedef struct {
+    int64_t n;                  /* system size */
+    int64_t n_chunks;
+    int m_max;                  /* largest chunk (DOF), <= MBEM_BJ_MAX_DOF */
+    const int64_t* chunk_ptr;   /* (n_chunks + 1) device */
+    const int64_t* dofs;        /* (n) device */
+    const int32_t* local;       /* (n) device */
+    const int32_t* chunk_of;    /* (n) device */
+    float* inv;                 /* (n_chunks, m_max, m_max) device */
+} mbem_block_jacobi;
+
+size_t mbem_bj_inverse_bytes(int64_t n_chunks, int m_max);
+/* Inverts the diagonal chunks of a dense FP64 A (at ld) / of a mixed operator
+ * (FP32 far field plus its FP64 near blocks). MBEM_ERR_NUMERIC when a chunk is
+ * singular (its inverse is then the identity). */
+int mbem_bj_build_dense(const double* A, int64_t ld, const mbem_block_jacobi* bj, void* stream);
+int mbem_bj_build_mixed(const mbem_mixed_operator* op, const mbem_block_jacobi* bj, void* stream);
+/* z = M^-1 r (r, z distinct device vectors of length n). */
+int mbem_bj_apply(const mbem_block_jacobi* bj, const double* r, double* z, void* stream);
+
 /* ---- deflated FGMRES on a dense operator (la/solver.py:115-245 fgmres,
  * wired as backends/hmat.py:678-690: P A P y = P b, P = I - Z Z^T with Z
  * the rigid-translation basis of backends/dense.py:190-208). ---------- */
@@ -224,8 +254,9 @@ typedef struct {
     double stagnation_factor;
     int n_u_ranges;         /* deflation: number of (offset, size) u-slot ranges, 0 = none */
     const int64_t* u_ranges;/* HOST array of 2*n_u_ranges int64 */
-    int precond;            /* 0 none, 1 block-Jacobi (mbem_bj_*), 2 learned (mbem_nn_*) */
-    const void* precond_state; /* the preconditioner object for precond != 0 */
+    int precond;            /* 0 none, 1 block-Jacobi (state: const mbem_block_jacobi*),
+                               2 learned (state: const mbem_nn_precond*) */
+    const void* precond_state; /* the preconditioner object for precond != 0 (host pointer) */
     int time_matvec;        /* 1: time every operator application with CUDA events */
 } mbem_fgmres_params;
 

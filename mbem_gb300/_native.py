@@ -58,6 +58,13 @@ class MixedOperator(Structure):
                 ("n_near", c_int), ("near", POINTER(NearBlocks))]
 
 
+class BlockJacobi(Structure):
+    _fields_ = [("n", c_int64), ("n_chunks", c_int64), ("m_max", c_int), ("chunk_ptr", c_void_p),
+                ("dofs", c_void_p), ("local", c_void_p), ("chunk_of", c_void_p), ("inv", c_void_p)]
+
+
+BJ_MAX_DOF = 225
+
 _P = c_void_p
 _I = c_int64
 _D = c_double
@@ -84,6 +91,10 @@ _SIGNATURES = {
     "mbem_dgemv": (c_int, [_P, _I, _I, _I, _P, _D, _D, _P, _P]),
     "mbem_dgemm_multi": (c_int, [_P, _I, _I, _I, _P, _I, _P, _P]),
     "mbem_project_translation": (c_int, [_P, _P, _I, _P, c_int, _P, _P]),
+    "mbem_bj_inverse_bytes": (c_size_t, [_I, c_int]),
+    "mbem_bj_build_dense": (c_int, [_P, _I, POINTER(BlockJacobi), _P]),
+    "mbem_bj_build_mixed": (c_int, [POINTER(MixedOperator), POINTER(BlockJacobi), _P]),
+    "mbem_bj_apply": (c_int, [POINTER(BlockJacobi), _P, _P, _P]),
     "mbem_fgmres_workspace_size": (c_size_t, [_I, c_int]),
     "mbem_fgmres_dense": (c_int, [_P, _I, _I, _P, _P, POINTER(FgmresParams), _P, c_size_t,
                                   POINTER(FgmresReport), _P]),

@@ -42,8 +42,10 @@ class DenseBackend:
     def __init__(self, mode: str = "direct", jump: str = "calibrated", deflate: bool = False,
                  lu: str | None = None, rtol: float = 1e-10, restart: int = 50,
                  maxiter: int = defaults.GMRES_MAXITER, precision: str = "fp64",
-                 near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR):
-        """``precision="fp64"``: every entry by the FP64 closed form, the
+                 near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, precond: str | None = None):
+        """``precond``: None (plain FGMRES, the reference's dense-backend
+        solve) or "block_jacobi" (la/preconditioner.py:421-470 cluster
+        block-Jacobi, built on first solve). ``precision="fp64"``: every entry by the FP64 closed form, the
         reference's operator. ``"mixed"``: pairs beyond near_factor *
         max(eps, h) of the source by FP32 quadrature (stored FP32), the near
         pairs by the FP64 closed form (stored as 3x3 blocks); the solve's
@@ -64,6 +66,9 @@ class DenseBackend:
         self.maxiter = maxiter
         self.precision = precision
         self.near_factor = near_factor
+        if precond not in (None, "block_jacobi"):
+            raise ValueError(f"precond must be None or 'block_jacobi' (got {precond!r})")
+        self.precond = precond
 
     def assemble(self, system: BlockSystem, eps, arrays: dict | None = None,
                  timer: list | None = None) -> "AssembledDense":
@@ -73,7 +78,7 @@ class DenseBackend:
         (start, end) CUDA events around every kernel-block launch."""
         return AssembledDense(system, eps, jump=self.jump, deflate=self.deflate, rtol=self.rtol,
                               restart=self.restart, maxiter=self.maxiter, arrays=arrays, timer=timer,
-                              precision=self.precision, near_factor=self.near_factor)
+                              precision=self.precision, near_factor=self.near_factor, precond=self.precond)
 
 
 def require_anchor_or_deflate(system: BlockSystem, jump: str, deflate: bool):
@@ -111,7 +116,7 @@ class AssembledDense:
                  deflate: bool = False, rtol: float = 1e-10, restart: int = 50,
                  maxiter: int = defaults.GMRES_MAXITER, arrays: dict | None = None,
                  timer: list | None = None, precision: str = "fp64",
-                 near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR):
+                 near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, precond: str | None = None):
         if jump not in ("half", "calibrated"):
             raise ValueError(jump)
         require_anchor_or_deflate(system, jump, deflate)
@@ -120,6 +125,8 @@ class AssembledDense:
         self._timer = timer
         self.precision = precision
         self.near_factor = near_factor
+        self.precond = precond
+        self._bj = None
         self.op = None
         self.system = system
         self.layout = system.layout
@@ -384,14 +391,31 @@ class AssembledDense:
             return []
         return [(s.offset, s.size) for s in self.layout.slots if s.kind == "u"]
 
+    def block_jacobi(self, max_nodes: int | None = None):
+        """The cluster block-Jacobi preconditioner of this system (built once)."""
+        from ..la.precond import MAX_NODES, BlockJacobi
+        if self._bj is None or (max_nodes is not None and max_nodes != self._bj_nodes):
+            self._bj_nodes = MAX_NODES if max_nodes is None else max_nodes
+            bj = BlockJacobi.for_layout(self.layout, self._bj_nodes)
+            self._bj = bj.build_mixed(self.op) if self.op is not None else bj.build_dense(self.A)
+        return self._bj
+
     def solve_device(self, rtol: float | None = None, restart: int | None = None,
-                     maxiter: int | None = None, x0=None, time_matvec: bool = False) -> torch.Tensor:
+                     maxiter: int | None = None, x0=None, time_matvec: bool = False,
+                     precond=None) -> torch.Tensor:
         """FGMRES on the device; returns the solution vector as a CUDA tensor
-        and leaves ``self.report``."""
+        and leaves ``self.report``. ``precond``: None (the backend's
+        default), "none", "block_jacobi", or a preconditioner object
+        (``la.precond.BlockJacobi``, ``la.learned.LearnedPreconditioner``)."""
+        precond = self.precond if precond is None else precond
+        if precond == "none":
+            precond = None
+        elif precond == "block_jacobi":
+            precond = self.block_jacobi()
         kw = dict(x0=x0, rtol=self.rtol if rtol is None else rtol,
                   restart=self.restart if restart is None else restart,
                   maxiter=self.maxiter if maxiter is None else maxiter, u_ranges=self.u_ranges(),
-                  time_matvec=time_matvec)
+                  time_matvec=time_matvec, precond=precond)
         if self.op is not None:
             x, rep = fgmres_mixed(self.op, self.b, **kw)
         else:
@@ -403,10 +427,10 @@ class AssembledDense:
         return x
 
     def solve(self, rtol: float | None = None, restart: int | None = None,
-              maxiter: int | None = None, x0=None) -> dict:
+              maxiter: int | None = None, x0=None, precond=None) -> dict:
         """FGMRES on the device; returns {slot_name: (n, 3) ndarray} and
         leaves ``self.report`` (a SolveReport)."""
-        xh = self.solve_device(rtol, restart, maxiter, x0).cpu().numpy()
+        xh = self.solve_device(rtol, restart, maxiter, x0, precond=precond).cpu().numpy()
         return {s.name: xh[s.offset:s.stop].reshape(-1, 3) for s in self.layout.slots}
 
     @property

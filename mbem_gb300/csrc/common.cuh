@@ -20,6 +20,11 @@ int launch_status(const char* what, int n_launched = 1);
 // Counts kernel launches whose status is checked later.
 void count_launches(int n);
 
+// z = M^-1 r for the FGMRES preconditioners (kind 1 block-Jacobi, 2 learned).
+int bj_apply(const mbem_block_jacobi* bj, const double* r, double* z, cudaStream_t st);
+int precond_apply(int kind, const void* state, const double* r, double* z, cudaStream_t st);
+int nn_precond_apply(const void* state, const double* r, double* z, cudaStream_t st);
+
 // Nodal (P1/P2) drivers behind the public entry points when order > 0.
 // kind for nodal_matrix: 0 T direct, 1 U direct, 2 T basis, 3 U basis;
 // for nodal_contract: 0 T disp, 1 U disp, 2 + MBEM_STRESS_* for stress.

@@ -360,6 +360,7 @@ static int make_ranges(const int64_t* r, int nr, URanges& ur) {
 // ---------------------------------------------------------------------------
 struct FgmresWork {
     double* V;        // (m+1, n)
+    double* Z;        // (m, n) preconditioned directions (flexible variant)
     double* w;        // n
     double* t;        // n
     double* r;        // n
@@ -385,6 +386,7 @@ static size_t fgmres_layout(int64_t n, int m, char* base, FgmresWork* w) {
     };
     FgmresWork tmp;
     tmp.V = take((size_t)(m + 1) * n);
+    tmp.Z = take((size_t)m * n);
     tmp.w = take(n);
     tmp.t = take(n);
     tmp.r = take(n);
@@ -577,7 +579,9 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
     MBEM_REQUIRE(n > 0, MBEM_ERR_ARG, "bad system size");
     const int m = prm->restart;
     MBEM_REQUIRE(m >= 1 && m <= 1000, MBEM_ERR_ARG, "restart must be in [1, 1000]");
-    MBEM_REQUIRE(prm->precond == 0, MBEM_ERR_UNSUPPORTED, "preconditioner %d not available here", prm->precond);
+    MBEM_REQUIRE(prm->precond >= 0 && prm->precond <= 2, MBEM_ERR_ARG, "unknown preconditioner %d", prm->precond);
+    MBEM_REQUIRE(prm->precond == 0 || prm->precond_state != nullptr, MBEM_ERR_ARG, "preconditioner state is NULL");
+    const bool flexible = prm->precond != 0;
     const size_t need = fgmres_layout(n, m, nullptr, nullptr);
     MBEM_REQUIRE(work != nullptr && work_bytes >= need, MBEM_ERR_SIZE, "workspace %zu < %zu bytes", work_bytes,
                  need);
@@ -643,7 +647,14 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
         for (int j = 0; j < mm; j++) {
             double* vj = W.V + (int64_t)j * n;
             double* vn = W.V + (int64_t)(j + 1) * n;
-            if ((e = F.op(vj, W.w))) return e;                  // w = P A P v_j (no preconditioner)
+            if (flexible) {
+                // z_j = M^-1 v_j, w = P A P z_j (right preconditioning, flexible: la/solver.py:160-170)
+                double* zj = W.Z + (int64_t)j * n;
+                if ((e = precond_apply(prm->precond, prm->precond_state, vj, zj, st))) return e;
+                if ((e = F.op(zj, W.w))) return e;
+            } else if ((e = F.op(vj, W.w))) {               // w = P A P v_j
+                return e;
+            }
             if ((e = F.multidot(W.V, j + 1, W.w, W.h, 0))) return e;
             if ((e = F.multiaxpy(W.w, W.V, j + 1, W.h, -1.0))) return e;
             if ((e = F.multidot(W.V, j + 1, W.w, W.h2, 0))) return e;
@@ -702,7 +713,7 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
             }
             cudaMemcpyAsync(W.y, y.data(), jdone * sizeof(double), cudaMemcpyHostToDevice, st);
             if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
-            if ((e = F.multiaxpy(x, W.V, jdone, W.y, 1.0))) return e;
+            if ((e = F.multiaxpy(x, flexible ? W.Z : W.V, jdone, W.y, 1.0))) return e;
         }
         restarts++;
         if (stagnated) break;

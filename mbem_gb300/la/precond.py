@@ -1,0 +1,133 @@
+"""Cluster block-Jacobi preconditioner on the GPU
+(``src/mbem/la/preconditioner.py:421-470``, the "block_jacobi" rung).
+
+The chunks are the leaves of the principal-axis bisection tree of the
+node centroids of each slot (``src/mbem/la/cluster.py:56-75``
+``build_cluster_tree``: split at the median of the projection on the
+covariance's leading eigenvector, ``proj < median`` to the left). A
+leaf holds at most ``max_nodes`` nodes (3 DOF each, at most
+``MBEM_BJ_MAX_DOF`` = 225 DOF), so that the CUDA build inverts it in one
+CTA's shared memory; the reference's default chunk is 9000 DOF, factored
+by LAPACK on the host.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from .. import _native as nat
+from .._device import ptr, stream_handle
+
+MAX_NODES = nat.BJ_MAX_DOF // 3
+
+
+def cluster_leaves(points: np.ndarray, max_nodes: int) -> list:
+    """Index arrays of the leaves of the bisection tree over ``points``
+    (n, 3), each with at most ``max_nodes`` entries, in tree order."""
+    points = np.asarray(points, float)
+    leaves = []
+    stack = [np.arange(points.shape[0])]
+    while stack:
+        idx = stack.pop()
+        if idx.size <= max_nodes:
+            leaves.append(idx)
+            continue
+        pts = points[idx]
+        mean = pts.mean(axis=0)
+        cov = (pts - mean).T @ (pts - mean)
+        _, vecs = np.linalg.eigh(cov)
+        proj = (pts - mean) @ vecs[:, -1]
+        left = proj < np.median(proj)
+        if left.all() or not left.any():
+            # coincident projections: halve by position
+            order = np.argsort(proj, kind="stable")
+            left = np.zeros(idx.size, bool)
+            left[order[:idx.size // 2]] = True
+        # right pushed first so the left subtree is emitted first
+        stack.append(idx[~left])
+        stack.append(idx[left])
+    return leaves
+
+
+class BlockJacobi:
+    """M^-1 = blockdiag(A[c, c]^-1) over spatial chunks c of every slot.
+
+    ``groups``: [(dof_offset, node_points (n_nodes, 3)), ...] covering the
+    unknowns 0..n-1, each node owning DOFs offset + 3 i + (0, 1, 2)."""
+
+    PRECOND_KIND = 1
+
+    def __init__(self, n: int, groups, max_nodes: int = MAX_NODES, device="cuda"):
+        if not 1 <= max_nodes <= MAX_NODES:
+            raise ValueError(f"max_nodes must be in [1, {MAX_NODES}]")
+        chunks = []
+        for off, pts in groups:
+            for leaf in cluster_leaves(pts, max_nodes):
+                leaf = np.sort(leaf)
+                chunks.append((off + 3 * leaf[:, None] + np.arange(3)[None, :]).ravel())
+        dofs = np.concatenate(chunks) if chunks else np.zeros(0, np.int64)
+        if dofs.size != n or not np.array_equal(np.sort(dofs), np.arange(n)):
+            raise ValueError("the slots' nodes do not partition the unknowns")
+        sizes = np.array([c.size for c in chunks], np.int64)
+        ptr_h = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        local = np.empty(n, np.int32)
+        chunk_of = np.empty(n, np.int32)
+        for c, d in enumerate(chunks):
+            local[d] = np.arange(d.size, dtype=np.int32)
+            chunk_of[d] = c
+        self.n = int(n)
+        self.n_chunks = len(chunks)
+        self.m_max = int(sizes.max()) if sizes.size else 1
+        self.chunk_sizes = sizes
+        self.device = torch.device(device)
+        self._ptr = torch.from_numpy(ptr_h).to(self.device)
+        self._dofs = torch.from_numpy(dofs.astype(np.int64)).to(self.device)
+        self._local = torch.from_numpy(local).to(self.device)
+        self._chunk_of = torch.from_numpy(chunk_of).to(self.device)
+        nbytes = nat.lib().mbem_bj_inverse_bytes(self.n_chunks, self.m_max)
+        self.inv = torch.zeros(nbytes // 4, dtype=torch.float32, device=self.device)
+        self._struct = nat.BlockJacobi(n=self.n, n_chunks=self.n_chunks, m_max=self.m_max,
+                                       chunk_ptr=ptr(self._ptr), dofs=ptr(self._dofs), local=ptr(self._local),
+                                       chunk_of=ptr(self._chunk_of), inv=ptr(self.inv))
+        self.built = False
+
+    @classmethod
+    def for_layout(cls, layout, max_nodes: int = MAX_NODES, device="cuda"):
+        """Chunks over every slot of an ``UnknownLayout``, nodes at the
+        slot patch's collocation points."""
+        groups = [(s.offset, np.asarray(s.patch.collocation_points(), float)) for s in layout.slots]
+        return cls(layout.n_unknowns, groups, max_nodes, device)
+
+    def struct(self):
+        return self._struct
+
+    def build_dense(self, A: torch.Tensor):
+        if A.dtype != torch.float64 or A.stride(1) != 1 or A.shape[0] != self.n:
+            raise ValueError("A must be the (n, n) FP64 system with unit column stride")
+        nat.call("mbem_bj_build_dense", ptr(A), A.stride(0), ctypes.byref(self._struct), stream_handle())
+        self.built = True
+        return self
+
+    def build_mixed(self, op):
+        s = op.struct()
+        nat.call("mbem_bj_build_mixed", ctypes.byref(s), ctypes.byref(self._struct), stream_handle())
+        self.built = True
+        return self
+
+    def apply(self, r: torch.Tensor) -> torch.Tensor:
+        if not self.built:
+            raise RuntimeError("block-Jacobi preconditioner applied before a build")
+        r = r.to(dtype=torch.float64, device=self.device).contiguous()
+        z = torch.empty_like(r)
+        nat.call("mbem_bj_apply", ctypes.byref(self._struct), ptr(r), ptr(z), stream_handle())
+        return z
+
+    def dense_blocks_host(self, A: np.ndarray) -> list:
+        """(dofs, A[dofs, dofs]) per chunk from a host matrix (for checks)."""
+        ptr_h = self._ptr.cpu().numpy()
+        dofs = self._dofs.cpu().numpy()
+        return [(dofs[ptr_h[c]:ptr_h[c + 1]], A[np.ix_(dofs[ptr_h[c]:ptr_h[c + 1]], dofs[ptr_h[c]:ptr_h[c + 1]])])
+                for c in range(self.n_chunks)]

@@ -44,7 +44,7 @@ class SolveReport:
 _DEFAULTS = dict(rtol=defaults.GMRES_RTOL, restart=defaults.GMRES_RESTART, maxiter=defaults.GMRES_MAXITER,
                  stagnation_window=defaults.GMRES_STAGNATION_WINDOW,
                  stagnation_factor=defaults.GMRES_STAGNATION_FACTOR, u_ranges=(), workspace=None,
-                 time_matvec=False)
+                 time_matvec=False, precond=None)
 
 
 def fgmres_mixed(op, b: torch.Tensor, x0: torch.Tensor | None = None, **kw):
@@ -56,15 +56,30 @@ def fgmres_dense(A: torch.Tensor, b: torch.Tensor, x0: torch.Tensor | None = Non
     """Solve A x = b for a dense FP64 CUDA matrix. Keywords: rtol, restart,
     maxiter, stagnation_window, stagnation_factor, ``u_ranges`` = [(offset,
     size), ...] of the u-slots to deflate (empty: no deflation), workspace,
-    time_matvec (CUDA-event time of every operator application).
-    Returns (x, SolveReport)."""
+    time_matvec (CUDA-event time of every operator application), precond
+    (a right preconditioner: ``la.precond.BlockJacobi`` or
+    ``la.learned.LearnedPreconditioner``; the iteration is then flexible,
+    x = x0 + Z y with z_j = M^-1 v_j). Returns (x, SolveReport)."""
     if A.dtype != torch.float64 or not A.is_cuda or A.shape[0] != b.shape[0] or A.stride(1) != 1:
         raise ValueError("A must be a float64 CUDA matrix (n, n) with unit column stride")
     return _fgmres(A, None, b, x0, **{**_DEFAULTS, **kw})
 
 
+def _precond_args(precond):
+    """(kind, state pointer, keep-alive) for the C params."""
+    if precond is None:
+        return 0, None, None
+    kind = getattr(precond, "PRECOND_KIND", None)
+    if kind not in (1, 2):
+        raise TypeError(f"unsupported preconditioner {type(precond).__name__}")
+    if not getattr(precond, "built", True):
+        raise RuntimeError("preconditioner used before it was built")
+    st = precond.struct()
+    return kind, ctypes.cast(ctypes.byref(st), ctypes.c_void_p), st
+
+
 def _fgmres(A, mop, b, x0, rtol, restart, maxiter, stagnation_window, stagnation_factor, u_ranges,
-            workspace, time_matvec):
+            workspace, time_matvec, precond):
     n = b.shape[0]
     dev = (A if A is not None else mop.A32).device
     b = b.to(dtype=torch.float64, device=dev).contiguous()
@@ -81,6 +96,9 @@ def _fgmres(A, mop, b, x0, rtol, restart, maxiter, stagnation_window, stagnation
                            n_u_ranges=len(rng) // 2,
                            u_ranges=rng.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) if rng.size else None,
                            precond=0, precond_state=None, time_matvec=int(bool(time_matvec)))
+    kind, state, _keep = _precond_args(precond)
+    prm.precond = kind
+    prm.precond_state = state
     hist = np.zeros(max(int(maxiter), 1))
     rep = nat.FgmresReport()
     rep.history = hist.ctypes.data_as(ctypes.POINTER(ctypes.c_double))

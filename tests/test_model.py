@@ -93,3 +93,20 @@ def test_coefficients_from_mu_lam():
     C1 = 1.0 / (16 * np.pi * 1.3 * (1 - nu))
     assert np.allclose(g, [(3 - 4 * nu) * C1, 1 / (8 * np.pi * 1.3), C1], rtol=1e-15)
     assert c.shape == (6,)
+
+
+def test_cluster_leaves_partition_and_bound():
+    """Principal-axis bisection (la/cluster.py:56-75): the leaves partition
+    the points, none exceeds the bound, and each is spatially compact."""
+    from mbem_gb300.la.precond import cluster_leaves
+    from mbem_gb300.mesh import cube
+    pts = cube(12, 4.0).centroids()
+    leaves = cluster_leaves(pts, 75)
+    allidx = np.sort(np.concatenate(leaves))
+    assert np.array_equal(allidx, np.arange(pts.shape[0]))
+    assert max(l.size for l in leaves) <= 75 and min(l.size for l in leaves) >= 75 // 2 - 1
+    span = max(np.ptp(pts[l], axis=0).max() for l in leaves)
+    assert span < 2.5
+    coincident = cluster_leaves(np.zeros((10, 3)), 3)
+    assert sorted(np.concatenate(coincident).tolist()) == list(range(10))
+    assert max(l.size for l in coincident) <= 3
