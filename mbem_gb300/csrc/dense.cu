@@ -651,6 +651,9 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
                 // z_j = M^-1 v_j, w = P A P z_j (right preconditioning, flexible: la/solver.py:160-170)
                 double* zj = W.Z + (int64_t)j * n;
                 if ((e = precond_apply(prm->precond, prm->precond_state, vj, zj, st))) return e;
+                // keep z_j in the deflated complement: the update x += Z y
+                // then never feeds the null space
+                if ((e = F.proj(zj, zj))) return e;
                 if ((e = F.op(zj, W.w))) return e;
             } else if ((e = F.op(vj, W.w))) {               // w = P A P v_j
                 return e;

@@ -107,15 +107,22 @@ class BlockJacobi:
     def build_dense(self, A: torch.Tensor):
         if A.dtype != torch.float64 or A.stride(1) != 1 or A.shape[0] != self.n:
             raise ValueError("A must be the (n, n) FP64 system with unit column stride")
-        nat.call("mbem_bj_build_dense", ptr(A), A.stride(0), ctypes.byref(self._struct), stream_handle())
-        self.built = True
+        self._build("mbem_bj_build_dense", ptr(A), A.stride(0))
         return self
 
     def build_mixed(self, op):
         s = op.struct()
-        nat.call("mbem_bj_build_mixed", ctypes.byref(s), ctypes.byref(self._struct), stream_handle())
-        self.built = True
+        self._build("mbem_bj_build_mixed", ctypes.byref(s))
         return self
+
+    def _build(self, name, *args):
+        try:
+            nat.call(name, *args, ctypes.byref(self._struct), stream_handle())
+        except nat.MbemError as err:
+            # a singular chunk: its inverse is the identity, the rest stand
+            self.built = err.code == nat.ERR_NUMERIC
+            raise
+        self.built = True
 
     def apply(self, r: torch.Tensor) -> torch.Tensor:
         if not self.built:
