@@ -65,6 +65,15 @@ class BlockJacobi(Structure):
 
 BJ_MAX_DOF = 225
 
+
+class NnPrecond(Structure):
+    _fields_ = [("n_nodes", c_int64), ("k", c_int), ("nbr", c_void_p), ("w", c_void_p),
+                ("bj", POINTER(BlockJacobi)), ("work", c_void_p)]
+
+
+NN_FEAT, NN_HIDDEN = 16, 32
+NN_PARAMS = NN_HIDDEN * NN_FEAT + NN_HIDDEN + NN_HIDDEN * NN_HIDDEN + NN_HIDDEN + 9 * NN_HIDDEN + 9
+
 _P = c_void_p
 _I = c_int64
 _D = c_double
@@ -95,6 +104,16 @@ _SIGNATURES = {
     "mbem_bj_build_dense": (c_int, [_P, _I, POINTER(BlockJacobi), _P]),
     "mbem_bj_build_mixed": (c_int, [POINTER(MixedOperator), POINTER(BlockJacobi), _P]),
     "mbem_bj_apply": (c_int, [POINTER(BlockJacobi), _P, _P, _P]),
+    "mbem_nn_forward": (c_int, [_P, _I, _P, _P, _P, _P]),
+    "mbem_nn_apply_batch": (c_int, [_P, _I, c_int, _P, _P, _I, _P, _P]),
+    "mbem_nn_loss_partial_count": (c_size_t, [_I, _I]),
+    "mbem_nn_loss_grad": (c_int, [_P, _P, _P, _I, _I, _P, _P, _P, _P]),
+    "mbem_nn_edge_grad": (c_int, [_P, _I, c_int, _P, _P, _I, _P, _P]),
+    "mbem_nn_backward_workspace_size": (c_size_t, [_I]),
+    "mbem_nn_backward": (c_int, [_P, _I, _P, _P, _P, _P, _P, c_size_t, _P]),
+    "mbem_nn_adam": (c_int, [_P, _P, _P, _P, _I, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                             ctypes.c_float, c_int, _P]),
+    "mbem_nn_apply": (c_int, [POINTER(NnPrecond), _P, _P, _P]),
     "mbem_fgmres_workspace_size": (c_size_t, [_I, c_int]),
     "mbem_fgmres_dense": (c_int, [_P, _I, _I, _P, _P, POINTER(FgmresParams), _P, c_size_t,
                                   POINTER(FgmresReport), _P]),

@@ -39,3 +39,23 @@ def readout_grid(n: int = 64, y: float = 0.1, half: float = 2.0) -> np.ndarray:
     g = (np.arange(n) + 0.5) / n * (2.0 * half) - half
     X, Z = np.meshgrid(g, g, indexing="xy")
     return np.column_stack([X.ravel(), np.full(X.size, y), Z.ravel()])
+
+
+def fault_traction_model(n_face: int, n_fault: int, dip_deg: float = 90.0, mu: float = 1.0, lam: float = 1.0,
+                         drop: float = 1e-3, side: float = 4.0):
+    """The cube with a FAULT_TRACTION fault (slip solved under a uniform
+    shear-traction drop of ``drop * mu`` along strike, no normal component)
+    whose plane is the centre fault rotated about its strike (the x axis)
+    to dip ``dip_deg`` (90: vertical). Returns (model, eps), eps = half the
+    cube grid spacing."""
+    cube = M.cube(n_face, side)
+    fault = M.centre_fault(n_fault)
+    th = np.deg2rad(90.0 - dip_deg)
+    c, s = np.cos(th), np.sin(th)
+    R = np.array([[1.0, 0.0, 0.0], [0.0, c, -s], [0.0, s, c]])
+    fault.vertices = np.ascontiguousarray(fault.vertices @ R.T)
+    mat = M.ElasticMaterial(mu=mu, lam=lam)
+    cube_p = Patch("cube", cube, BCType.FREE_TRACTION)
+    fault_p = Patch("fault", fault, BCType.FAULT_TRACTION, value=np.array([-drop * mu, 0.0, 0.0]))
+    region = Region("body", mat, [cube_p], np.zeros(3), faults=[fault_p])
+    return RegionModel([region]), (side / n_face) / 2.0
