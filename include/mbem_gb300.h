@@ -243,49 +243,56 @@ int mbem_bj_build_mixed(const mbem_mixed_operator* op, const mbem_block_jacobi* 
 /* z = M^-1 r (r, z distinct device vectors of length n). */
 int mbem_bj_apply(const mbem_block_jacobi* bj, const double* r, double* z, void* stream);
 
-/* ---- learned preconditioner: z = rho + sum_j W_ij rho_j with rho the
- * block-Jacobi step and W_ij (3x3) the output of a small MLP on the geometry
- * of node i and its k nearest nodes j (no reference counterpart: the learned
- * part replaces the block-Jacobi rung of la/preconditioner.py:421-470 in
- * the solve). MLP: MBEM_NN_FEAT -> MBEM_NN_HIDDEN (tanh) -> MBEM_NN_HIDDEN
- * (tanh) -> 9; flat FP32 parameters W1 (H x F), b1, W2 (H x H), b2, W3
- * (9 x H), b3. Node i owns unknowns 3i..3i+2. ------------------------- */
+/* ---- learned preconditioner: block-Jacobi with a learned coarse space (no
+ * reference counterpart: it replaces the block-Jacobi rung of
+ * la/preconditioner.py:421-470 in the solve). Each block-Jacobi chunk c gets
+ * three coarse vectors whose 3x3 block on node i of the chunk is phi_i, the
+ * output of a small MLP on the node's geometry (phi_i = I: the chunk's
+ * translations). With Phi (n x 3C) and A_c = Phi^T A Phi:
+ *     y = A_c^-1 Phi^T r,   z = Phi y + BJ (r - (A Phi) y).
+ * MLP: MBEM_NN_FEAT -> MBEM_NN_HIDDEN (tanh) -> MBEM_NN_HIDDEN (tanh) -> 9
+ * (phi_i row-major); flat FP32 parameters W1 (H x F), b1, W2 (H x H), b2,
+ * W3 (9 x H), b3. Node i owns unknowns 3i..3i+2; every chunk holds whole
+ * nodes. ---------------------------------------------------------------- */
 #define MBEM_NN_FEAT 16
 #define MBEM_NN_HIDDEN 32
 #define MBEM_NN_PARAMS (MBEM_NN_HIDDEN * MBEM_NN_FEAT + MBEM_NN_HIDDEN + MBEM_NN_HIDDEN * MBEM_NN_HIDDEN + \
                         MBEM_NN_HIDDEN + 9 * MBEM_NN_HIDDEN + 9)
 typedef struct {
-    int64_t n_nodes;                 /* unknowns = 3 n_nodes */
-    int k;                           /* neighbours per node, the node itself first */
-    const int32_t* nbr;              /* (n_nodes, k) device */
-    const float* w;                  /* (n_nodes, k, 3, 3) device edge blocks (mbem_nn_forward) */
-    const mbem_block_jacobi* bj;     /* the block-Jacobi step (host pointer to its descriptor) */
-    double* work;                    /* (3 n_nodes) device scratch */
+    int64_t n;                       /* unknowns (a multiple of 3) */
+    int64_t n_coarse;                /* 3 x the block-Jacobi chunks */
+    const mbem_block_jacobi* bj;     /* chunks and their inverses (host pointer; chunk_of required) */
+    const float* phi;                /* (n/3, 3, 3) device: coarse blocks per node (mbem_nn_forward) */
+    const double* APhi;              /* (n, n_coarse) device: A Phi, written by mbem_nn_setup_dense */
+    const double* Ac_inv;            /* (n_coarse, n_coarse) device: A_c^-1, written by the setup */
+    double* work;                    /* mbem_nn_apply_workspace_size() bytes, device */
 } mbem_nn_precond;
 
-/* Edge blocks w (E, 9) from features (E, MBEM_NN_FEAT); act (E, 2H) keeps
- * the hidden activations for training (NULL at inference). */
-int mbem_nn_forward(const float* feat, int64_t n_edges, const float* params, float* act, float* w,
+/* out (n_items, 9) = MLP(feat (n_items, MBEM_NN_FEAT)); act (n_items, 2H)
+ * keeps the hidden activations for training (NULL at inference). */
+int mbem_nn_forward(const float* feat, int64_t n_items, const float* params, float* act, float* out,
                     void* stream);
-/* z[s] = rho[s] + W rho[s] for n_samples rows of 3 n_nodes (FP32). */
-int mbem_nn_apply_batch(const int32_t* nbr, int64_t n_nodes, int k, const float* w, const float* rho,
-                        int64_t n_samples, float* z, void* stream);
-/* loss = (1/S) sum_s |z_s - e_s|^2 inv_e2[s] into *loss (device double);
- * dz = dloss/dz. partial: mbem_nn_loss_partial_count() device doubles. */
-size_t mbem_nn_loss_partial_count(int64_t n_samples, int64_t n);
-int mbem_nn_loss_grad(const float* z, const float* e, const float* inv_e2, int64_t n_samples, int64_t n,
-                      float* dz, double* partial, double* loss, void* stream);
-/* G (E, 9): dloss/dW_e = sum_s dz[s, i] rho[s, j]^T for edge e = (i, j). */
-int mbem_nn_edge_grad(const int32_t* nbr, int64_t n_nodes, int k, const float* dz, const float* rho,
-                      int64_t n_samples, float* G, void* stream);
-/* grad (MBEM_NN_PARAMS) = dloss/dparams from G through the MLP. */
-size_t mbem_nn_backward_workspace_size(int64_t n_edges);
-int mbem_nn_backward(const float* feat, int64_t n_edges, const float* params, const float* act, const float* G,
+/* Training loss: the chunk-wise least-squares projection error of the
+ * block-Jacobi errors eps (n_samples, n) onto the coarse space, weighted by
+ * inv_e2 (1/|eps_s|^2) and averaged, into *loss (device double); dphi
+ * (n/3, 9) = dloss/dphi. partial: bj->n_chunks device doubles. */
+int mbem_nn_coarse_loss_grad(const mbem_block_jacobi* bj, const float* phi, const float* eps,
+                             const float* inv_e2, int64_t n_samples, float* dphi, double* partial,
+                             double* loss, void* stream);
+/* grad (MBEM_NN_PARAMS) = dloss/dparams from dloss/dout (n_items, 9). */
+size_t mbem_nn_backward_workspace_size(int64_t n_items);
+int mbem_nn_backward(const float* feat, int64_t n_items, const float* params, const float* act, const float* G,
                      float* grad, void* work, size_t work_bytes, void* stream);
 /* One Adam step (step >= 1) on n parameters. */
 int mbem_nn_adam(float* params, const float* grad, float* m, float* v, int64_t n, float lr, float beta1,
                  float beta2, float eps, int step, void* stream);
-/* z = M^-1 r: the block-Jacobi step, then the network's correction. */
+/* A Phi, A_c and A_c^-1 (Gauss-Jordan, partial pivoting) for a dense FP64 A;
+ * MBEM_ERR_NUMERIC when A_c is singular. */
+size_t mbem_nn_setup_workspace_size(int64_t n_coarse);
+int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, void* work, size_t work_bytes,
+                        void* stream);
+/* z = M^-1 r (r, z distinct device vectors of length n). */
+size_t mbem_nn_apply_workspace_size(int64_t n, int64_t n_coarse);
 int mbem_nn_apply(const mbem_nn_precond* nn, const double* r, double* z, void* stream);
 
 /* ---- deflated FGMRES on a dense operator (la/solver.py:115-245 fgmres,

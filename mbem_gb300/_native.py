@@ -67,8 +67,8 @@ BJ_MAX_DOF = 225
 
 
 class NnPrecond(Structure):
-    _fields_ = [("n_nodes", c_int64), ("k", c_int), ("nbr", c_void_p), ("w", c_void_p),
-                ("bj", POINTER(BlockJacobi)), ("work", c_void_p)]
+    _fields_ = [("n", c_int64), ("n_coarse", c_int64), ("bj", POINTER(BlockJacobi)), ("phi", c_void_p),
+                ("APhi", c_void_p), ("Ac_inv", c_void_p), ("work", c_void_p)]
 
 
 NN_FEAT, NN_HIDDEN = 16, 32
@@ -105,14 +105,14 @@ _SIGNATURES = {
     "mbem_bj_build_mixed": (c_int, [POINTER(MixedOperator), POINTER(BlockJacobi), _P]),
     "mbem_bj_apply": (c_int, [POINTER(BlockJacobi), _P, _P, _P]),
     "mbem_nn_forward": (c_int, [_P, _I, _P, _P, _P, _P]),
-    "mbem_nn_apply_batch": (c_int, [_P, _I, c_int, _P, _P, _I, _P, _P]),
-    "mbem_nn_loss_partial_count": (c_size_t, [_I, _I]),
-    "mbem_nn_loss_grad": (c_int, [_P, _P, _P, _I, _I, _P, _P, _P, _P]),
-    "mbem_nn_edge_grad": (c_int, [_P, _I, c_int, _P, _P, _I, _P, _P]),
+    "mbem_nn_coarse_loss_grad": (c_int, [POINTER(BlockJacobi), _P, _P, _P, _I, _P, _P, _P, _P]),
     "mbem_nn_backward_workspace_size": (c_size_t, [_I]),
     "mbem_nn_backward": (c_int, [_P, _I, _P, _P, _P, _P, _P, c_size_t, _P]),
     "mbem_nn_adam": (c_int, [_P, _P, _P, _P, _I, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                              ctypes.c_float, c_int, _P]),
+    "mbem_nn_setup_workspace_size": (c_size_t, [_I]),
+    "mbem_nn_setup_dense": (c_int, [_P, _I, POINTER(NnPrecond), _P, c_size_t, _P]),
+    "mbem_nn_apply_workspace_size": (c_size_t, [_I, _I]),
     "mbem_nn_apply": (c_int, [POINTER(NnPrecond), _P, _P, _P]),
     "mbem_fgmres_workspace_size": (c_size_t, [_I, c_int]),
     "mbem_fgmres_dense": (c_int, [_P, _I, _I, _P, _P, POINTER(FgmresParams), _P, c_size_t,

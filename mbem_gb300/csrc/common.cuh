@@ -22,6 +22,9 @@ void count_launches(int n);
 
 // z = M^-1 r for the FGMRES preconditioners (kind 1 block-Jacobi, 2 learned).
 int bj_apply(const mbem_block_jacobi* bj, const double* r, double* z, cudaStream_t st);
+// y = alpha A x + beta y (FP64 row-major at ld)
+int dgemv(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols, const double* x, double alpha,
+          double beta, double* y, cudaStream_t st);
 int precond_apply(int kind, const void* state, const double* r, double* z, cudaStream_t st);
 int nn_precond_apply(const void* state, const double* r, double* z, cudaStream_t st);
 

@@ -1,21 +1,29 @@
-// Learned preconditioner: a mesh-local network that corrects the cluster
-// block-Jacobi step with the residuals of each node's k nearest nodes.
+// Learned preconditioner: block-Jacobi with a learned coarse space.
 //
-//   rho = BJ r,   z_i = rho_i + sum_{j in nbr(i)} W_ij rho_j,
-//   W_ij = MLP(g_ij) (3x3),  g_ij = geometry of the pair (i, j)
+// The unknowns are split into the block-Jacobi chunks. Each chunk c gets
+// three coarse vectors; on node i of chunk c they take the 3x3 block phi_i,
+// the output of a small MLP on the node's geometry (its place in the chunk,
+// its normal, its slot kind, the shape of its neighbourhood). phi_i = I gives
+// the chunk translations (a Nicolaides coarse space). With Phi (n x 3C) the
+// coarse basis and A_c = Phi^T A Phi, the preconditioner is multiplicative:
 //
-// The network sees geometry only, so its edge blocks W are computed once per
-// mesh; every FGMRES apply is then one block-Jacobi apply and one sparse
-// 3x3-block product over the k-nearest-neighbour graph. z is linear in r,
-// so the preconditioner is a fixed linear map per mesh.
+//   y = A_c^-1 Phi^T r,   z = Phi y + BJ (r - (A Phi) y).
 //
-// MLP: MBEM_NN_FEAT -> MBEM_NN_HIDDEN (tanh) -> MBEM_NN_HIDDEN (tanh) -> 9.
-// Parameters, flat FP32: W1 (H x F), b1 (H), W2 (H x H), b2 (H), W3 (9 x H),
-// b3 (9). Training minimises (1/S) sum_s |z_s - e_s|^2 / |e_s|^2 over pairs
-// (r_s, e_s = A^-1 r_s) with the kernels below: forward, batched apply, loss
-// gradient, per-edge gradient, backward through the MLP, fixed-order
-// parameter-gradient reduction, Adam. Every reduction runs in a fixed order,
-// so a training run is deterministic.
+// Setup per mesh: phi (MLP forward), A Phi (one pass over A), A_c, and A_c^-1
+// by Gauss-Jordan with partial pivoting (FP64). An apply is five small
+// kernels plus the block-Jacobi apply; it never touches A.
+//
+// Training: the coarse space should hold what block-Jacobi misses, the error
+// eps = A^-1 r - BJ r of training pairs. The loss is the chunk-wise
+// least-squares projection error of eps onto the coarse space,
+//   loss = (1/S) sum_s sum_c |eps_sc - Phi_c y_sc|^2 / |eps_s|^2,
+//   y_sc = argmin_y |eps_sc - Phi_c y|,
+// whose gradient needs no derivative of y (it is the minimiser):
+//   dloss/dphi_i = -(2/S) sum_s (eps_si - phi_i y_sc) y_sc^T / |eps_s|^2.
+// MLP: MBEM_NN_FEAT -> MBEM_NN_HIDDEN (tanh) -> MBEM_NN_HIDDEN (tanh) -> 9
+// (phi_i row-major); flat FP32 parameters W1 (H x F), b1, W2 (H x H), b2,
+// W3 (9 x H), b3. Every reduction runs in a fixed order: training and setup
+// are deterministic.
 #include <math.h>
 
 #include "common.cuh"
@@ -28,13 +36,14 @@ constexpr int NP = MBEM_NN_PARAMS;
 constexpr int OFF_W1 = 0, OFF_B1 = NH * NF, OFF_W2 = OFF_B1 + NH, OFF_B2 = OFF_W2 + NH * NH,
               OFF_W3 = OFF_B2 + NH, OFF_B3 = OFF_W3 + 9 * NH;
 static_assert(OFF_B3 + 9 == NP, "parameter layout");
-constexpr int ACT = 2 * NH;          // stored activations per edge (h1, h2)
-constexpr int DEL = 2 * NH + 9;      // stored deltas per edge (d1, d2, d3)
+constexpr int ACT = 2 * NH;          // stored activations per item (h1, h2)
+constexpr int DEL = 2 * NH + 9;      // stored deltas per item (d1, d2, d3)
 constexpr int NN_THREADS = 256;
-constexpr int GRAD_CHUNK = 512;      // edges per partial parameter-gradient sum
+constexpr int GRAD_CHUNK = 512;      // items per partial parameter-gradient sum
+constexpr int CHUNK_NODES = MBEM_BJ_MAX_DOF / 3;
 
 // ---------------------------------------------------------------------------
-// forward: one thread per edge, parameters in shared memory
+// MLP forward: one thread per item (node), parameters in shared memory
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(NN_THREADS)
 nn_forward_kernel(const float* __restrict__ feat, int64_t E, const float* __restrict__ params,
@@ -78,52 +87,87 @@ nn_forward_kernel(const float* __restrict__ feat, int64_t E, const float* __rest
 }
 
 // ---------------------------------------------------------------------------
-// batched apply (training): z[s] = rho[s] + W rho[s], FP32, (S, 3 n_nodes)
+// coarse-space projection loss and its gradient: one CTA per chunk, one
+// thread per node of the chunk
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NN_THREADS)
-nn_apply_batch_kernel(const int32_t* __restrict__ nbr, int64_t n_nodes, int k, const float* __restrict__ w,
-                      const float* __restrict__ rho, int64_t S, float* __restrict__ z) {
-    const int64_t t = (int64_t)blockIdx.x * NN_THREADS + threadIdx.x;
-    if (t >= S * n_nodes) return;
-    const int64_t s = t / n_nodes, i = t % n_nodes;
-    const int64_t N = 3 * n_nodes;
-    const float* rs = rho + s * N;
-    float a0 = rs[3 * i], a1 = rs[3 * i + 1], a2 = rs[3 * i + 2];
-    for (int q = 0; q < k; q++) {
-        const int64_t j = nbr[i * k + q];
-        const float* W = w + (i * k + q) * 9;
-        const float r0 = rs[3 * j], r1 = rs[3 * j + 1], r2 = rs[3 * j + 2];
-        a0 = fmaf(W[0], r0, fmaf(W[1], r1, fmaf(W[2], r2, a0)));
-        a1 = fmaf(W[3], r0, fmaf(W[4], r1, fmaf(W[5], r2, a1)));
-        a2 = fmaf(W[6], r0, fmaf(W[7], r1, fmaf(W[8], r2, a2)));
-    }
-    float* zs = z + s * N;
-    zs[3 * i] = a0;
-    zs[3 * i + 1] = a1;
-    zs[3 * i + 2] = a2;
+__device__ __forceinline__ double block_sum(double v, double* red) {
+    // 128-thread block: warp shuffles, then the four warp sums in order
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    return ((red[0] + red[1]) + red[2]) + red[3];
 }
 
-// loss = (1/S) sum_s |z_s - e_s|^2 inv_e2[s]; dz = (2/S) (z - e) inv_e2[s].
-// Per-block partial sums in FP64, summed in block order by nn_sum_kernel.
-__global__ void __launch_bounds__(NN_THREADS)
-nn_loss_grad_kernel(const float* __restrict__ z, const float* __restrict__ e, const float* __restrict__ inv_e2,
-                    int64_t S, int64_t N, float* __restrict__ dz, double* __restrict__ partial) {
-    __shared__ double red[NN_THREADS];
-    const int64_t t = (int64_t)blockIdx.x * NN_THREADS + threadIdx.x;
-    double l = 0.0;
-    if (t < S * N) {
-        const int64_t s = t / N;
-        const float d = z[t] - e[t];
-        dz[t] = (2.0f / (float)S) * d * inv_e2[s];
-        l = (double)d * (double)d * (double)inv_e2[s] / (double)S;
+__global__ void __launch_bounds__(128)
+nn_coarse_loss_grad_kernel(const int64_t* __restrict__ chunk_ptr, const int64_t* __restrict__ dofs,
+                           const float* __restrict__ phi, const float* __restrict__ eps,
+                           const float* __restrict__ inv_e2, int64_t S, int64_t N, float* __restrict__ dphi,
+                           double* __restrict__ partial) {
+    __shared__ double red[4];
+    const int c = blockIdx.x;
+    const int64_t c0 = chunk_ptr[c];
+    const int m = (int)((chunk_ptr[c + 1] - c0) / 3);
+    const int t = threadIdx.x;
+    const bool live = t < m;
+    int64_t node = 0;
+    float P[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) P[q] = 0.0f;
+    if (live) {
+        node = dofs[c0 + 3 * t] / 3;
+#pragma unroll
+        for (int q = 0; q < 9; q++) P[q] = phi[node * 9 + q];
     }
-    red[threadIdx.x] = l;
-    __syncthreads();
-    for (int o = NN_THREADS / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
+    // G = sum_i phi_i^T phi_i (symmetric 3x3), inverted once
+    double G[6];
+    {
+        const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+        for (int q = 0; q < 6; q++) {
+            const int a = ia[q], b = ib[q];
+            double v = 0.0;
+            for (int r = 0; r < 3; r++) v += (double)P[3 * r + a] * (double)P[3 * r + b];
+            G[q] = block_sum(v, red);
+        }
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+    const double g00 = G[0], g01 = G[1], g02 = G[2], g11 = G[3], g12 = G[4], g22 = G[5];
+    const double c00 = g11 * g22 - g12 * g12, c01 = g02 * g12 - g01 * g22, c02 = g01 * g12 - g02 * g11;
+    const double c11 = g00 * g22 - g02 * g02, c12 = g01 * g02 - g00 * g12, c22 = g00 * g11 - g01 * g01;
+    const double det = g00 * c00 + g01 * c01 + g02 * c02;
+    const double id = (det != 0.0) ? 1.0 / det : 0.0;
+    double gr[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double lsum = 0.0;
+    for (int64_t s = 0; s < S; s++) {
+        float ev[3] = {0.0f, 0.0f, 0.0f};
+        if (live) {
+            const float* es = eps + s * N + 3 * node;
+            ev[0] = es[0]; ev[1] = es[1]; ev[2] = es[2];
+        }
+        double b[3];
+        for (int k = 0; k < 3; k++) {
+            const double v = (double)P[k] * ev[0] + (double)P[3 + k] * ev[1] + (double)P[6 + k] * ev[2];
+            b[k] = block_sum(v, red);
+        }
+        const double y0 = id * (c00 * b[0] + c01 * b[1] + c02 * b[2]);
+        const double y1 = id * (c01 * b[0] + c11 * b[1] + c12 * b[2]);
+        const double y2 = id * (c02 * b[0] + c12 * b[1] + c22 * b[2]);
+        if (live) {
+            const double w = (double)inv_e2[s] / (double)S;
+            for (int a = 0; a < 3; a++) {
+                const double res = ev[a] - ((double)P[3 * a] * y0 + (double)P[3 * a + 1] * y1 +
+                                            (double)P[3 * a + 2] * y2);
+                lsum += res * res * w;
+                gr[3 * a] -= 2.0 * w * res * y0;
+                gr[3 * a + 1] -= 2.0 * w * res * y1;
+                gr[3 * a + 2] -= 2.0 * w * res * y2;
+            }
+        }
+    }
+    if (live)
+        for (int q = 0; q < 9; q++) dphi[node * 9 + q] = (float)gr[q];
+    const double tot = block_sum(lsum, red);
+    if (t == 0) partial[c] = tot;
 }
 
 __global__ void nn_sum_kernel(const double* __restrict__ partial, int64_t n, double* __restrict__ out) {
@@ -133,30 +177,12 @@ __global__ void nn_sum_kernel(const double* __restrict__ partial, int64_t n, dou
     *out = s;
 }
 
-// G_e = sum_s dz[s, i] rho[s, j]^T for edge e = (i, j): one thread per edge
+// ---------------------------------------------------------------------------
+// MLP backward and Adam
+// ---------------------------------------------------------------------------
+// per-item deltas: d3 = G, d2 = (W3^T d3)(1 - h2^2), d1 = (W2^T d2)(1 - h1^2)
 __global__ void __launch_bounds__(NN_THREADS)
-nn_edge_grad_kernel(const int32_t* __restrict__ nbr, int64_t n_nodes, int k, const float* __restrict__ dz,
-                    const float* __restrict__ rho, int64_t S, float* __restrict__ G) {
-    const int64_t e = (int64_t)blockIdx.x * NN_THREADS + threadIdx.x;
-    if (e >= n_nodes * k) return;
-    const int64_t i = e / k, j = nbr[e];
-    const int64_t N = 3 * n_nodes;
-    float g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int64_t s = 0; s < S; s++) {
-        const float* d = dz + s * N + 3 * i;
-        const float* r = rho + s * N + 3 * j;
-        const float d0 = d[0], d1 = d[1], d2 = d[2], r0 = r[0], r1 = r[1], r2 = r[2];
-        g[0] = fmaf(d0, r0, g[0]); g[1] = fmaf(d0, r1, g[1]); g[2] = fmaf(d0, r2, g[2]);
-        g[3] = fmaf(d1, r0, g[3]); g[4] = fmaf(d1, r1, g[4]); g[5] = fmaf(d1, r2, g[5]);
-        g[6] = fmaf(d2, r0, g[6]); g[7] = fmaf(d2, r1, g[7]); g[8] = fmaf(d2, r2, g[8]);
-    }
-#pragma unroll
-    for (int o = 0; o < 9; o++) G[e * 9 + o] = g[o];
-}
-
-// per-edge deltas of the MLP: d3 = G, d2 = (W3^T d3)(1 - h2^2), d1 = (W2^T d2)(1 - h1^2)
-__global__ void __launch_bounds__(NN_THREADS)
-nn_backward_edges_kernel(int64_t E, const float* __restrict__ params, const float* __restrict__ act,
+nn_backward_items_kernel(int64_t E, const float* __restrict__ params, const float* __restrict__ act,
                          const float* __restrict__ G, float* __restrict__ del) {
     __shared__ float P[NP];
     for (int p = threadIdx.x; p < NP; p += NN_THREADS) P[p] = params[p];
@@ -188,8 +214,8 @@ nn_backward_edges_kernel(int64_t E, const float* __restrict__ params, const floa
     for (int o = 0; o < 9; o++) del[e * DEL + 2 * NH + o] = d3[o];
 }
 
-// partial[c][p] = sum over edges of chunk c of dL/dparam_p contributions;
-// threads of a warp take consecutive parameters (coalesced inputs)
+// partial[c][p]: the gradient contributions of the items of chunk c to
+// parameter p; the threads of a warp take consecutive parameters
 __global__ void __launch_bounds__(NN_THREADS)
 nn_param_grad_kernel(int64_t E, const float* __restrict__ feat, const float* __restrict__ act,
                      const float* __restrict__ del, float* __restrict__ partial) {
@@ -197,9 +223,7 @@ nn_param_grad_kernel(int64_t E, const float* __restrict__ feat, const float* __r
     const int64_t c = blockIdx.y;
     if (p >= NP) return;
     const int64_t e0 = c * GRAD_CHUNK, e1 = lmin(E, e0 + GRAD_CHUNK);
-    // parameter p = (delta index, input index or -1 for a bias)
-    const float* dbase;
-    int dstride = DEL, di, ii = -1, istride = 0;
+    int di, ii = -1, istride = 0;
     const float* ibase = nullptr;
     if (p < OFF_B1) { di = p / NF; ii = p % NF; ibase = feat; istride = NF; }
     else if (p < OFF_W2) { di = p - OFF_B1; }
@@ -207,12 +231,11 @@ nn_param_grad_kernel(int64_t E, const float* __restrict__ feat, const float* __r
     else if (p < OFF_W3) { di = NH + (p - OFF_B2); }
     else if (p < OFF_B3) { di = 2 * NH + (p - OFF_W3) / NH; ii = NH + (p - OFF_W3) % NH; ibase = act; istride = ACT; }
     else { di = 2 * NH + (p - OFF_B3); }
-    dbase = del;
     float s = 0.0f;
     if (ii >= 0) {
-        for (int64_t e = e0; e < e1; e++) s = fmaf(dbase[e * dstride + di], ibase[e * istride + ii], s);
+        for (int64_t e = e0; e < e1; e++) s = fmaf(del[e * DEL + di], ibase[e * istride + ii], s);
     } else {
-        for (int64_t e = e0; e < e1; e++) s += dbase[e * dstride + di];
+        for (int64_t e = e0; e < e1; e++) s += del[e * DEL + di];
     }
     partial[c * NP + p] = s;
 }
@@ -239,32 +262,205 @@ __global__ void nn_adam_kernel(float* __restrict__ params, const float* __restri
     params[p] -= lr * (mp / c1) / (sqrtf(vp / c2) + eps);
 }
 
-// inference: z = rho + W rho in FP64 (FP32 edge blocks)
-__global__ void __launch_bounds__(NN_THREADS)
-nn_apply_kernel(const int32_t* __restrict__ nbr, int64_t n_nodes, int k, const float* __restrict__ w,
-                const double* __restrict__ rho, double* __restrict__ z) {
-    const int64_t i = (int64_t)blockIdx.x * NN_THREADS + threadIdx.x;
-    if (i >= n_nodes) return;
-    double a0 = rho[3 * i], a1 = rho[3 * i + 1], a2 = rho[3 * i + 2];
-    for (int q = 0; q < k; q++) {
-        const int64_t j = nbr[i * k + q];
-        const float* W = w + (i * k + q) * 9;
-        const double r0 = rho[3 * j], r1 = rho[3 * j + 1], r2 = rho[3 * j + 2];
-        a0 += (double)W[0] * r0 + (double)W[1] * r1 + (double)W[2] * r2;
-        a1 += (double)W[3] * r0 + (double)W[4] * r1 + (double)W[5] * r2;
-        a2 += (double)W[6] * r0 + (double)W[7] * r1 + (double)W[8] * r2;
+// ---------------------------------------------------------------------------
+// setup: A Phi, A_c = Phi^T (A Phi), A_c^-1
+// ---------------------------------------------------------------------------
+constexpr int APHI_ROWS = 64;     // rows of A per CTA
+
+// APhi[r, 3c + k] = sum_{i in c} sum_a A[r, 3i + a] phi_i[a][k]; a CTA per
+// (chunk, 64-row tile), a warp per row, lanes along the chunk's columns
+__global__ void __launch_bounds__(256)
+nn_aphi_kernel(const double* __restrict__ A, int64_t ld, int64_t n, const int64_t* __restrict__ chunk_ptr,
+               const int64_t* __restrict__ dofs, const float* __restrict__ phi, int64_t n_coarse,
+               double* __restrict__ APhi) {
+    __shared__ int64_t col[MBEM_BJ_MAX_DOF];
+    __shared__ float ph[MBEM_BJ_MAX_DOF][3];
+    const int c = blockIdx.x;
+    const int64_t c0 = chunk_ptr[c];
+    const int m = (int)(chunk_ptr[c + 1] - c0);
+    for (int t = threadIdx.x; t < m; t += 256) {
+        const int64_t d = dofs[c0 + t];
+        col[t] = d;
+        const int64_t node = d / 3;
+        const int a = (int)(d % 3);
+        ph[t][0] = phi[node * 9 + 3 * a];
+        ph[t][1] = phi[node * 9 + 3 * a + 1];
+        ph[t][2] = phi[node * 9 + 3 * a + 2];
     }
-    z[3 * i] = a0;
-    z[3 * i + 1] = a1;
-    z[3 * i + 2] = a2;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t r0 = (int64_t)blockIdx.y * APHI_ROWS;
+    for (int64_t r = r0 + warp; r < lmin(n, r0 + APHI_ROWS); r += 8) {
+        const double* Ar = A + r * ld;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        for (int t = lane; t < m; t += 32) {
+            const double v = Ar[col[t]];
+            s0 += v * (double)ph[t][0];
+            s1 += v * (double)ph[t][1];
+            s2 += v * (double)ph[t][2];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        if (lane == 0) {
+            APhi[r * n_coarse + 3 * c] = s0;
+            APhi[r * n_coarse + 3 * c + 1] = s1;
+            APhi[r * n_coarse + 3 * c + 2] = s2;
+        }
+    }
+}
+
+// Ac[3c + k, q] = sum_{i in c} sum_a phi_i[a][k] APhi[3i + a, q]: a CTA per
+// (chunk, 256 columns), a thread per column
+__global__ void __launch_bounds__(256)
+nn_coarse_matrix_kernel(const double* __restrict__ APhi, int64_t n_coarse, const int64_t* __restrict__ chunk_ptr,
+                        const int64_t* __restrict__ dofs, const float* __restrict__ phi, double* __restrict__ Ac) {
+    const int c = blockIdx.x;
+    const int64_t q = (int64_t)blockIdx.y * 256 + threadIdx.x;
+    if (q >= n_coarse) return;
+    const int64_t c0 = chunk_ptr[c];
+    const int m = (int)(chunk_ptr[c + 1] - c0);
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int t = 0; t < m; t++) {
+        const int64_t d = dofs[c0 + t];
+        const int64_t node = d / 3;
+        const int a = (int)(d % 3);
+        const double v = APhi[d * n_coarse + q];
+        s0 += (double)phi[node * 9 + 3 * a] * v;
+        s1 += (double)phi[node * 9 + 3 * a + 1] * v;
+        s2 += (double)phi[node * 9 + 3 * a + 2] * v;
+    }
+    Ac[(3 * c) * n_coarse + q] = s0;
+    Ac[(3 * c + 1) * n_coarse + q] = s1;
+    Ac[(3 * c + 2) * n_coarse + q] = s2;
+}
+
+// Gauss-Jordan step k on M (m x m, FP64, in place): pivot search, row swap,
+// scaling of the pivot row; one CTA
+__global__ void __launch_bounds__(256)
+gj_pivot_kernel(double* __restrict__ M, int64_t m, int64_t k, double* __restrict__ rowk, double* __restrict__ fcol,
+                int* __restrict__ piv, int* __restrict__ bad) {
+    __shared__ double bv[256];
+    __shared__ int64_t bi[256];
+    double best = -1.0;
+    int64_t besti = k;
+    for (int64_t i = k + threadIdx.x; i < m; i += 256) {
+        const double v = fabs(M[i * m + k]);
+        if (v > best) { best = v; besti = i; }
+    }
+    bv[threadIdx.x] = best;
+    bi[threadIdx.x] = besti;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            const double ob = bv[threadIdx.x + o];
+            const int64_t oi = bi[threadIdx.x + o];
+            if (ob > bv[threadIdx.x] || (ob == bv[threadIdx.x] && oi < bi[threadIdx.x])) {
+                bv[threadIdx.x] = ob;
+                bi[threadIdx.x] = oi;
+            }
+        }
+        __syncthreads();
+    }
+    const int64_t p = bi[0];
+    if (threadIdx.x == 0) {
+        piv[k] = (int)p;
+        if (!(bv[0] > 0.0)) *bad = 1;
+    }
+    if (p != k)
+        for (int64_t j = threadIdx.x; j < m; j += 256) {
+            const double t = M[k * m + j];
+            M[k * m + j] = M[p * m + j];
+            M[p * m + j] = t;
+        }
+    __syncthreads();
+    const double pv = M[k * m + k];
+    const double d = (pv != 0.0) ? 1.0 / pv : 1.0;
+    for (int64_t j = threadIdx.x; j < m; j += 256) {
+        rowk[j] = (j == k ? 1.0 : M[k * m + j]) * d;
+        fcol[j] = M[j * m + k];
+    }
+}
+
+// rank-1 update of every row but k; row k becomes rowk
+__global__ void __launch_bounds__(256)
+gj_update_kernel(double* __restrict__ M, int64_t m, int64_t k, const double* __restrict__ rowk,
+                 const double* __restrict__ fcol) {
+    const int64_t i = blockIdx.y;
+    const int64_t j = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (j >= m) return;
+    if (i == k) {
+        M[i * m + j] = rowk[j];
+    } else {
+        const double v = (j == k) ? 0.0 : M[i * m + j];
+        M[i * m + j] = v - fcol[i] * rowk[j];
+    }
+}
+
+__global__ void gj_swap_columns_kernel(double* __restrict__ M, int64_t m, const int* __restrict__ piv) {
+    const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (i >= m) return;
+    for (int64_t k = m - 1; k >= 0; k--) {
+        const int64_t p = piv[k];
+        if (p != k) {
+            const double t = M[i * m + k];
+            M[i * m + k] = M[i * m + p];
+            M[i * m + p] = t;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// apply pieces
+// ---------------------------------------------------------------------------
+// q[3c + k] = sum_{i in c} sum_a phi_i[a][k] r[3i + a]; a CTA per chunk
+__global__ void __launch_bounds__(128)
+nn_phit_kernel(const int64_t* __restrict__ chunk_ptr, const int64_t* __restrict__ dofs,
+               const float* __restrict__ phi, const double* __restrict__ r, double* __restrict__ q) {
+    __shared__ double red[4];
+    const int c = blockIdx.x;
+    const int64_t c0 = chunk_ptr[c];
+    const int m = (int)(chunk_ptr[c + 1] - c0);
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int t = threadIdx.x; t < m; t += 128) {
+        const int64_t d = dofs[c0 + t];
+        const int64_t node = d / 3;
+        const int a = (int)(d % 3);
+        const double v = r[d];
+        s[0] += (double)phi[node * 9 + 3 * a] * v;
+        s[1] += (double)phi[node * 9 + 3 * a + 1] * v;
+        s[2] += (double)phi[node * 9 + 3 * a + 2] * v;
+    }
+    for (int k = 0; k < 3; k++) {
+        const double tot = block_sum(s[k], red);
+        if (threadIdx.x == 0) q[3 * c + k] = tot;
+    }
+}
+
+// z[d] += sum_k phi_i[a][k] y[3 c(d) + k] for d = 3i + a
+__global__ void __launch_bounds__(256)
+nn_phi_add_kernel(int64_t n, const int32_t* __restrict__ chunk_of, const float* __restrict__ phi,
+                  const double* __restrict__ y, double* __restrict__ z) {
+    const int64_t d = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (d >= n) return;
+    const int64_t node = d / 3;
+    const int a = (int)(d % 3);
+    const int64_t c = chunk_of[d];
+    const double* yc = y + 3 * c;
+    z[d] += (double)phi[node * 9 + 3 * a] * yc[0] + (double)phi[node * 9 + 3 * a + 1] * yc[1] +
+            (double)phi[node * 9 + 3 * a + 2] * yc[2];
 }
 
 static int nn_check(const mbem_nn_precond* nn) {
     MBEM_REQUIRE(nn != nullptr && nn->bj != nullptr, MBEM_ERR_ARG, "learned preconditioner descriptor is NULL");
-    MBEM_REQUIRE(nn->n_nodes >= 0 && nn->k >= 1 && 3 * nn->n_nodes == nn->bj->n, MBEM_ERR_ARG,
-                 "learned preconditioner sizes (n_nodes=%lld, k=%d, n=%lld)", (long long)nn->n_nodes, nn->k,
-                 (long long)nn->bj->n);
-    MBEM_REQUIRE(nn->n_nodes == 0 || (nn->nbr && nn->w && nn->work), MBEM_ERR_ARG, "NULL learned arrays");
+    MBEM_REQUIRE(nn->n == nn->bj->n && nn->n_coarse == 3 * nn->bj->n_chunks && nn->n % 3 == 0, MBEM_ERR_ARG,
+                 "learned preconditioner sizes (n=%lld, coarse=%lld, chunks=%lld)", (long long)nn->n,
+                 (long long)nn->n_coarse, (long long)nn->bj->n_chunks);
+    MBEM_REQUIRE(nn->n == 0 || (nn->phi && nn->APhi && nn->Ac_inv && nn->work && nn->bj->chunk_of), MBEM_ERR_ARG,
+                 "NULL learned preconditioner arrays");
     return MBEM_OK;
 }
 
@@ -272,12 +468,21 @@ int nn_precond_apply(const void* state, const double* r, double* z, cudaStream_t
     const mbem_nn_precond* nn = static_cast<const mbem_nn_precond*>(state);
     int e = nn_check(nn);
     if (e) return e;
-    MBEM_REQUIRE(z != nn->work && r != nn->work, MBEM_ERR_ARG, "r/z alias the learned preconditioner's scratch");
-    if ((e = bj_apply(nn->bj, r, nn->work, st))) return e;
-    if (nn->n_nodes == 0) return MBEM_OK;
-    nn_apply_kernel<<<(unsigned)ceil_div(nn->n_nodes, NN_THREADS), NN_THREADS, 0, st>>>(nn->nbr, nn->n_nodes, nn->k,
-                                                                                       nn->w, nn->work, z);
-    return launch_status("nn_apply_kernel");
+    if (nn->n == 0) return MBEM_OK;
+    const int64_t n = nn->n, nc = nn->n_coarse;
+    double* t = nn->work;          // n: r - (A Phi) y
+    double* q = t + n;             // nc: Phi^T r
+    double* y = q + nc;            // nc: A_c^-1 q
+    MBEM_REQUIRE(z != t && r != t, MBEM_ERR_ARG, "r/z alias the learned preconditioner's scratch");
+    const mbem_block_jacobi* bj = nn->bj;
+    nn_phit_kernel<<<(unsigned)bj->n_chunks, 128, 0, st>>>(bj->chunk_ptr, bj->dofs, nn->phi, r, q);
+    if ((e = launch_status("nn_phit_kernel"))) return e;
+    if ((e = dgemv(nn->Ac_inv, nc, nc, nc, q, 1.0, 0.0, y, st))) return e;
+    cudaMemcpyAsync(t, r, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    if ((e = dgemv(nn->APhi, nc, n, nc, y, -1.0, 1.0, t, st))) return e;
+    if ((e = bj_apply(bj, t, z, st))) return e;
+    nn_phi_add_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(n, bj->chunk_of, nn->phi, y, z);
+    return launch_status("nn_phi_add_kernel");
 }
 
 }  // namespace mbem
@@ -286,71 +491,49 @@ using namespace mbem;
 
 extern "C" {
 
-int mbem_nn_forward(const float* feat, int64_t n_edges, const float* params, float* act, float* w,
+int mbem_nn_forward(const float* feat, int64_t n_items, const float* params, float* act, float* out,
                     void* stream) {
-    MBEM_REQUIRE(n_edges >= 0 && (n_edges == 0 || (feat && params && w)), MBEM_ERR_ARG, "bad forward args");
-    if (n_edges == 0) return MBEM_OK;
-    nn_forward_kernel<<<(unsigned)ceil_div(n_edges, NN_THREADS), NN_THREADS, 0, (cudaStream_t)stream>>>(
-        feat, n_edges, params, act, w);
+    MBEM_REQUIRE(n_items >= 0 && (n_items == 0 || (feat && params && out)), MBEM_ERR_ARG, "bad forward args");
+    if (n_items == 0) return MBEM_OK;
+    nn_forward_kernel<<<(unsigned)ceil_div(n_items, NN_THREADS), NN_THREADS, 0, (cudaStream_t)stream>>>(
+        feat, n_items, params, act, out);
     return launch_status("nn_forward_kernel");
 }
 
-int mbem_nn_apply_batch(const int32_t* nbr, int64_t n_nodes, int k, const float* w, const float* rho,
-                        int64_t n_samples, float* z, void* stream) {
-    MBEM_REQUIRE(n_nodes >= 0 && k >= 1 && n_samples >= 0, MBEM_ERR_ARG, "bad batch apply sizes");
-    MBEM_REQUIRE(n_nodes * n_samples == 0 || (nbr && w && rho && z && rho != z), MBEM_ERR_ARG,
-                 "bad batch apply pointers");
-    if (n_nodes * n_samples == 0) return MBEM_OK;
-    nn_apply_batch_kernel<<<(unsigned)ceil_div(n_nodes * n_samples, NN_THREADS), NN_THREADS, 0,
-                            (cudaStream_t)stream>>>(nbr, n_nodes, k, w, rho, n_samples, z);
-    return launch_status("nn_apply_batch_kernel");
+int mbem_nn_coarse_loss_grad(const mbem_block_jacobi* bj, const float* phi, const float* eps, const float* inv_e2,
+                             int64_t n_samples, float* dphi, double* partial, double* loss, void* stream) {
+    MBEM_REQUIRE(bj && bj->n_chunks >= 1 && bj->m_max <= MBEM_BJ_MAX_DOF && phi && eps && inv_e2 && dphi &&
+                     partial && loss && n_samples >= 1,
+                 MBEM_ERR_ARG, "bad coarse-loss args");
+    MBEM_REQUIRE(bj->m_max / 3 <= 128, MBEM_ERR_ARG, "chunks of more than 128 nodes");
+    cudaStream_t st = (cudaStream_t)stream;
+    nn_coarse_loss_grad_kernel<<<(unsigned)bj->n_chunks, 128, 0, st>>>(bj->chunk_ptr, bj->dofs, phi, eps, inv_e2,
+                                                                      n_samples, bj->n, dphi, partial);
+    nn_sum_kernel<<<1, 32, 0, st>>>(partial, bj->n_chunks, loss);
+    return launch_status("nn_coarse_loss_grad_kernel", 2);
 }
 
-int mbem_nn_loss_grad(const float* z, const float* e, const float* inv_e2, int64_t n_samples, int64_t n,
-                      float* dz, double* partial, double* loss, void* stream) {
-    MBEM_REQUIRE(n_samples >= 1 && n >= 1 && z && e && inv_e2 && dz && partial && loss, MBEM_ERR_ARG,
-                 "bad loss args");
-    const int64_t blocks = ceil_div(n_samples * n, NN_THREADS);
-    nn_loss_grad_kernel<<<(unsigned)blocks, NN_THREADS, 0, (cudaStream_t)stream>>>(z, e, inv_e2, n_samples, n, dz,
-                                                                                   partial);
-    nn_sum_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(partial, blocks, loss);
-    return launch_status("nn_loss_grad_kernel", 2);
+size_t mbem_nn_backward_workspace_size(int64_t n_items) {
+    const int64_t chunks = ceil_div(n_items, GRAD_CHUNK);
+    return (size_t)n_items * DEL * sizeof(float) + (size_t)chunks * NP * sizeof(float);
 }
 
-size_t mbem_nn_loss_partial_count(int64_t n_samples, int64_t n) {
-    return (size_t)ceil_div(n_samples * n, NN_THREADS);
-}
-
-int mbem_nn_edge_grad(const int32_t* nbr, int64_t n_nodes, int k, const float* dz, const float* rho,
-                      int64_t n_samples, float* G, void* stream) {
-    MBEM_REQUIRE(n_nodes >= 1 && k >= 1 && n_samples >= 1 && nbr && dz && rho && G, MBEM_ERR_ARG,
-                 "bad edge-gradient args");
-    nn_edge_grad_kernel<<<(unsigned)ceil_div(n_nodes * k, NN_THREADS), NN_THREADS, 0, (cudaStream_t)stream>>>(
-        nbr, n_nodes, k, dz, rho, n_samples, G);
-    return launch_status("nn_edge_grad_kernel");
-}
-
-size_t mbem_nn_backward_workspace_size(int64_t n_edges) {
-    const int64_t chunks = ceil_div(n_edges, GRAD_CHUNK);
-    return (size_t)n_edges * DEL * sizeof(float) + (size_t)chunks * NP * sizeof(float);
-}
-
-int mbem_nn_backward(const float* feat, int64_t n_edges, const float* params, const float* act, const float* G,
+int mbem_nn_backward(const float* feat, int64_t n_items, const float* params, const float* act, const float* G,
                      float* grad, void* work, size_t work_bytes, void* stream) {
-    MBEM_REQUIRE(n_edges >= 1 && feat && params && act && G && grad, MBEM_ERR_ARG, "bad backward args");
-    const size_t need = mbem_nn_backward_workspace_size(n_edges);
+    MBEM_REQUIRE(n_items >= 1 && feat && params && act && G && grad, MBEM_ERR_ARG, "bad backward args");
+    const size_t need = mbem_nn_backward_workspace_size(n_items);
     MBEM_REQUIRE(work != nullptr && work_bytes >= need, MBEM_ERR_SIZE, "backward workspace %zu < %zu", work_bytes,
                  need);
     cudaStream_t st = (cudaStream_t)stream;
     float* del = static_cast<float*>(work);
-    float* partial = del + (size_t)n_edges * DEL;
-    const int64_t chunks = ceil_div(n_edges, GRAD_CHUNK);
-    MBEM_REQUIRE(chunks <= 65535, MBEM_ERR_UNSUPPORTED, "%lld edges exceed the gradient grid",
-                 (long long)n_edges);
-    nn_backward_edges_kernel<<<(unsigned)ceil_div(n_edges, NN_THREADS), NN_THREADS, 0, st>>>(n_edges, params, act,
+    float* partial = del + (size_t)n_items * DEL;
+    const int64_t chunks = ceil_div(n_items, GRAD_CHUNK);
+    MBEM_REQUIRE(chunks <= 65535, MBEM_ERR_UNSUPPORTED, "%lld items exceed the gradient grid",
+                 (long long)n_items);
+    nn_backward_items_kernel<<<(unsigned)ceil_div(n_items, NN_THREADS), NN_THREADS, 0, st>>>(n_items, params, act,
                                                                                            G, del);
     dim3 grid((unsigned)ceil_div(NP, NN_THREADS), (unsigned)chunks);
-    nn_param_grad_kernel<<<grid, NN_THREADS, 0, st>>>(n_edges, feat, act, del, partial);
+    nn_param_grad_kernel<<<grid, NN_THREADS, 0, st>>>(n_items, feat, act, del, partial);
     nn_param_reduce_kernel<<<(unsigned)ceil_div(NP, 256), 256, 0, st>>>(partial, chunks, grad);
     return launch_status("nn_backward", 3);
 }
@@ -362,6 +545,54 @@ int mbem_nn_adam(float* params, const float* grad, float* m, float* v, int64_t n
     nn_adam_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(params, grad, m, v, n, lr, beta1,
                                                                                beta2, eps, c1, c2);
     return launch_status("nn_adam_kernel");
+}
+
+size_t mbem_nn_setup_workspace_size(int64_t n_coarse) {
+    return (size_t)(2 * n_coarse + 8) * sizeof(double) + (size_t)(n_coarse + 8) * sizeof(int);
+}
+
+int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, void* work, size_t work_bytes,
+                        void* stream) {
+    int e = nn_check(nn);
+    if (e) return e;
+    MBEM_REQUIRE(A != nullptr && ld >= nn->n, MBEM_ERR_ARG, "bad dense operator");
+    const int64_t n = nn->n, nc = nn->n_coarse;
+    if (n == 0) return MBEM_OK;
+    MBEM_REQUIRE(work != nullptr && work_bytes >= mbem_nn_setup_workspace_size(nc), MBEM_ERR_SIZE,
+                 "setup workspace too small");
+    MBEM_REQUIRE(ceil_div(n, APHI_ROWS) <= 65535 && ceil_div(nc, 256) <= 65535 && nc <= 65535, MBEM_ERR_UNSUPPORTED,
+                 "learned preconditioner sizes beyond one launch");
+    cudaStream_t st = (cudaStream_t)stream;
+    const mbem_block_jacobi* bj = nn->bj;
+    double* APhi = const_cast<double*>(nn->APhi);
+    double* Ac = const_cast<double*>(nn->Ac_inv);
+    nn_aphi_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(n, APHI_ROWS)), 256, 0, st>>>(
+        A, ld, n, bj->chunk_ptr, bj->dofs, nn->phi, nc, APhi);
+    nn_coarse_matrix_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(nc, 256)), 256, 0, st>>>(
+        APhi, nc, bj->chunk_ptr, bj->dofs, nn->phi, Ac);
+    if ((e = launch_status("nn_coarse_setup", 2))) return e;
+    // A_c^-1 in place
+    double* rowk = static_cast<double*>(work);
+    double* fcol = rowk + nc;
+    int* piv = reinterpret_cast<int*>(fcol + nc + 8);
+    int* bad = piv + nc;
+    cudaMemsetAsync(bad, 0, sizeof(int), st);
+    for (int64_t k = 0; k < nc; k++) {
+        gj_pivot_kernel<<<1, 256, 0, st>>>(Ac, nc, k, rowk, fcol, piv, bad);
+        gj_update_kernel<<<dim3((unsigned)ceil_div(nc, 256), (unsigned)nc), 256, 0, st>>>(Ac, nc, k, rowk, fcol);
+    }
+    count_launches((int)(2 * nc));
+    gj_swap_columns_kernel<<<(unsigned)ceil_div(nc, 256), 256, 0, st>>>(Ac, nc, piv);
+    if ((e = launch_status("gauss_jordan"))) return e;
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("nn setup sync", 0);
+    MBEM_REQUIRE(hbad == 0, MBEM_ERR_NUMERIC, "singular coarse operator");
+    return MBEM_OK;
+}
+
+size_t mbem_nn_apply_workspace_size(int64_t n, int64_t n_coarse) {
+    return (size_t)(n + 2 * n_coarse) * sizeof(double);
 }
 
 int mbem_nn_apply(const mbem_nn_precond* nn, const double* r, double* z, void* stream) {

@@ -1,61 +1,56 @@
-"""Learned right preconditioner for FGMRES: a mesh-local network that
-corrects the cluster block-Jacobi step.
+"""Learned right preconditioner for FGMRES: cluster block-Jacobi with a
+learned coarse space.
 
-    rho = BJ r,    z_i = rho_i + sum_{j in knn(i)} W_ij rho_j,    W_ij = MLP(g_ij)
+Each block-Jacobi chunk c (``la.precond``) gets three coarse vectors; on
+node i of the chunk (unknowns 3i..3i+2 of a u-, t- or b-slot) they take the
+3x3 block phi_i = MLP(g_i), where g_i is the node's geometry: its place in
+the chunk (offset from the chunk centroid over the chunk radius), its
+normal, its slot kind, the shape of its neighbourhood (the mean offset of
+its nearest same-slot nodes, which points away from a patch edge), its size
+against the chunk's. phi_i = I gives the chunk translations (a Nicolaides
+coarse space), which is where training starts. The preconditioner is
 
-Node i owns unknowns 3i..3i+2 (a collocation node of a u-, t- or b-slot);
-knn(i) are its k nearest nodes over every slot, itself first; g_ij is the
-pair's geometry in units of node i's element size (relative position and
-distance, both normals, the slot kinds, the size ratio). The network sees
-no residual, so W is computed once per mesh (``mbem_nn_forward``) and an
-apply is one block-Jacobi apply plus one 3x3-block product over the k-NN
-graph (``mbem_nn_apply``). With the last layer at zero the preconditioner is
-block-Jacobi itself, which is where training starts.
+    y = A_c^-1 Phi^T r,   z = Phi y + BJ (r - (A Phi) y),   A_c = Phi^T A Phi,
+
+set up once per mesh (``mbem_nn_setup_dense``) and applied by
+``mbem_nn_apply`` (no pass over A).
 
 Training (all on the GPU, the library's own kernels): pairs (r, e = A^-1 r)
 from direct dense solves of smaller meshes (the bordered deflated system of
-src/mbem/backends/dense.py:384-388, LU-factored once), residuals drawn from
-smooth random fields, images A s of smooth fields and white noise;
-loss (1/S) sum_s |z_s - e_s|^2 / |e_s|^2; Adam.
+src/mbem/backends/dense.py:384-388, LU-factored once); the coarse space
+should hold what block-Jacobi misses, eps = e - BJ r, so the loss is the
+chunk-wise least-squares projection error of eps onto the coarse space;
+Adam. Residuals come from smooth random fields, images A s of smooth
+fields, and white noise.
 """
 
 from __future__ import annotations
 
 import ctypes
 import math
-from dataclasses import dataclass
 
 import numpy as np
 import torch
 
 from .. import _native as nat
 from .._device import ptr, stream_handle
-from ..model.core import BCType
 
-K_DEFAULT = 16
+NEIGHBOURS = 12
 
 
 # ---------------------------------------------------------------------------
-# mesh graph and features (host)
+# node geometry and features (host)
 # ---------------------------------------------------------------------------
-@dataclass
-class NodeGraph:
-    pos: np.ndarray       # (n, 3)
-    nrm: np.ndarray       # (n, 3)
-    h: np.ndarray         # (n,) element size (sqrt of the element area)
-    kind: np.ndarray      # (n,) 1 for a solved-slip (b) node, else 0
-    nbr: np.ndarray       # (n, k) int32, self first
-    feat: np.ndarray      # (n k, F) float32
-
-
 def layout_nodes(layout):
-    """Per global node (unknowns 3i..3i+2): position, normal, size, kind."""
+    """Per global node (unknowns 3i..3i+2): position, normal, size (sqrt of
+    the element area), kind (1 for a solved-slip b node), slot index."""
     n = layout.n_unknowns // 3
     pos = np.zeros((n, 3))
     nrm = np.zeros((n, 3))
     h = np.ones(n)
     kind = np.zeros(n)
-    for s in layout.slots:
+    slot = np.zeros(n, np.int64)
+    for si, s in enumerate(layout.slots):
         p = s.patch
         i0 = s.offset // 3
         m = s.size // 3
@@ -65,11 +60,12 @@ def layout_nodes(layout):
         K = m // p.mesh.n_triangles
         h[i0:i0 + m] = np.repeat(np.sqrt(np.asarray(areas, float)), K)
         kind[i0:i0 + m] = 1.0 if s.kind == "b" else 0.0
-    return pos, nrm, h, kind
+        slot[i0:i0 + m] = si
+    return pos, nrm, h, kind, slot
 
 
 def knn(pos: np.ndarray, k: int) -> np.ndarray:
-    """(n, k) nearest nodes by distance, each row starting with the node itself."""
+    """(n, k) nearest nodes by distance, the node itself first."""
     n = pos.shape[0]
     k = min(k, n)
     try:
@@ -79,45 +75,46 @@ def knn(pos: np.ndarray, k: int) -> np.ndarray:
     except ImportError:            # small meshes without scipy
         d2 = ((pos[:, None, :] - pos[None, :, :]) ** 2).sum(-1)
         idx = np.argsort(d2, axis=1, kind="stable")[:, :k]
-    rows = np.arange(n)
-    for i in np.flatnonzero(idx[:, 0] != rows):       # coincident nodes: put self first
-        r = [i] + [j for j in idx[i] if j != i][:k - 1]
-        idx[i] = r
-    return idx.astype(np.int32)
+    for i in np.flatnonzero(idx[:, 0] != np.arange(n)):    # coincident nodes: self first
+        idx[i] = [i] + [j for j in idx[i] if j != i][:k - 1]
+    return idx
 
 
-def edge_features(pos, nrm, h, kind, nbr) -> np.ndarray:
-    n, k = nbr.shape
-    i = np.repeat(np.arange(n), k)
-    j = nbr.reshape(-1).astype(np.int64)
-    hi = h[i][:, None]
-    d = (pos[j] - pos[i]) / hi
-    f = np.zeros((n * k, nat.NN_FEAT), np.float32)
-    f[:, 0:3] = d
-    f[:, 3] = np.linalg.norm(d, axis=1)
-    f[:, 4:7] = nrm[i]
-    f[:, 7:10] = nrm[j]
-    f[:, 10] = np.sum(nrm[i] * nrm[j], axis=1)
-    f[:, 11] = kind[i]
-    f[:, 12] = kind[j]
-    f[:, 13] = np.log(h[j] / h[i])
-    f[:, 14] = (i == j)
-    f[:, 15] = np.sum(nrm[i] * d, axis=1)
+def node_features(layout, chunks) -> np.ndarray:
+    """(n, MBEM_NN_FEAT) float32 node features; chunks: node-index arrays."""
+    pos, nrm, h, kind, slot = layout_nodes(layout)
+    n = pos.shape[0]
+    cof = np.empty(n, np.int64)
+    cen = np.zeros((len(chunks), 3))
+    rad = np.zeros(len(chunks))
+    for c, nodes in enumerate(chunks):
+        cof[nodes] = c
+        cen[c] = pos[nodes].mean(axis=0)
+        rad[c] = np.linalg.norm(pos[nodes] - cen[c], axis=1).max() + 1e-12 * max(1.0, h[nodes].max())
+    nb = knn(pos, NEIGHBOURS)
+    same = slot[nb] == slot[:, None]
+    off = ((pos[nb] - pos[:, None, :]) * same[..., None]).sum(1) / np.maximum(same.sum(1), 1)[:, None] / h[:, None]
+    rel = (pos - cen[cof]) / rad[cof][:, None]
+    f = np.zeros((n, nat.NN_FEAT), np.float32)
+    f[:, 0:3] = rel
+    f[:, 3] = np.linalg.norm(rel, axis=1)
+    f[:, 4:7] = nrm
+    f[:, 7] = kind
+    f[:, 8:11] = off
+    f[:, 11] = np.linalg.norm(off, axis=1)
+    f[:, 12] = np.sum(nrm * rel, axis=1)
+    f[:, 13] = np.log(h / rad[cof])
+    f[:, 14] = 1.0
+    f[:, 15] = same.mean(axis=1)
     return f
 
 
-def node_graph(layout, k: int = K_DEFAULT) -> NodeGraph:
-    pos, nrm, h, kind = layout_nodes(layout)
-    nbr = knn(pos, k)
-    return NodeGraph(pos, nrm, h, kind, nbr, edge_features(pos, nrm, h, kind, nbr))
-
-
 # ---------------------------------------------------------------------------
-# the network's parameters
+# the network
 # ---------------------------------------------------------------------------
 def init_params(seed: int = 0) -> np.ndarray:
-    """Glorot-uniform hidden layers, zero output layer (the identity
-    correction: the preconditioner starts as block-Jacobi)."""
+    """Glorot-uniform hidden layers, zero output weights and an identity
+    output bias: phi_i = I, the chunk translations."""
     rng = np.random.default_rng(seed)
     F, H = nat.NN_FEAT, nat.NN_HIDDEN
 
@@ -125,43 +122,52 @@ def init_params(seed: int = 0) -> np.ndarray:
         a = math.sqrt(6.0 / (i + o))
         return rng.uniform(-a, a, size=(o, i))
 
-    parts = [glorot(H, F), np.zeros(H), glorot(H, H), np.zeros(H), np.zeros((9, H)), np.zeros(9)]
+    parts = [glorot(H, F), np.zeros(H), glorot(H, H), np.zeros(H), np.zeros((9, H)), np.eye(3).ravel()]
     p = np.concatenate([x.ravel() for x in parts]).astype(np.float32)
     assert p.size == nat.NN_PARAMS
     return p
 
 
-def edge_blocks(feat: torch.Tensor, params: torch.Tensor, act: torch.Tensor | None = None) -> torch.Tensor:
-    """W (E, 9) FP32 from features (E, F) on the device."""
+def mlp_forward(feat: torch.Tensor, params: torch.Tensor, act: torch.Tensor | None = None) -> torch.Tensor:
+    """(n_items, 9) FP32 network outputs for features (n_items, F) on the device."""
     E = feat.shape[0]
-    w = torch.empty((E, 9), dtype=torch.float32, device=feat.device)
-    nat.call("mbem_nn_forward", ptr(feat), E, ptr(params), ptr(act) if act is not None else None, ptr(w),
+    out = torch.empty((E, 9), dtype=torch.float32, device=feat.device)
+    nat.call("mbem_nn_forward", ptr(feat), E, ptr(params), ptr(act) if act is not None else None, ptr(out),
              stream_handle())
-    return w
+    return out
 
 
 # ---------------------------------------------------------------------------
 # the preconditioner (inference)
 # ---------------------------------------------------------------------------
 class LearnedPreconditioner:
-    """M^-1 r = (I + W) BJ r for one assembled system. ``params``: the
-    trained network (np or torch FP32, MBEM_NN_PARAMS)."""
+    """Block-Jacobi with the learned coarse space for one assembled FP64
+    system. ``params``: the trained network (FP32, MBEM_NN_PARAMS)."""
 
     PRECOND_KIND = 2
 
-    def __init__(self, asm, params, k: int = K_DEFAULT, bj=None):
-        self.graph = node_graph(asm.layout, k)
+    def __init__(self, asm, params, bj=None):
+        if asm.A is None:
+            raise NotImplementedError("the learned preconditioner is set up on a dense FP64 system")
         self.bj = bj if bj is not None else asm.block_jacobi()
         dev = self.bj.device
+        n = self.bj.n
+        nc = 3 * self.bj.n_chunks
         self.params = torch.as_tensor(np.asarray(params, np.float32)).to(dev)
-        self.nbr = torch.from_numpy(self.graph.nbr).to(dev)
-        self.feat = torch.from_numpy(self.graph.feat).to(dev)
-        self.w = edge_blocks(self.feat, self.params)
-        n_nodes, kk = self.graph.nbr.shape
-        self.work = torch.empty(3 * n_nodes, dtype=torch.float64, device=dev)
+        self.feat = torch.from_numpy(node_features(asm.layout, self.bj.chunk_nodes())).to(dev)
+        self.phi = mlp_forward(self.feat, self.params)
+        self.APhi = torch.empty((n, nc), dtype=torch.float64, device=dev)
+        self.Ac_inv = torch.empty((nc, nc), dtype=torch.float64, device=dev)
+        self.work = torch.empty(nat.lib().mbem_nn_apply_workspace_size(n, nc) // 8, dtype=torch.float64,
+                                device=dev)
         self._bj_struct = self.bj.struct()
-        self._struct = nat.NnPrecond(n_nodes=n_nodes, k=kk, nbr=ptr(self.nbr), w=ptr(self.w),
-                                     bj=ctypes.pointer(self._bj_struct), work=ptr(self.work))
+        self._struct = nat.NnPrecond(n=n, n_coarse=nc, bj=ctypes.pointer(self._bj_struct), phi=ptr(self.phi),
+                                     APhi=ptr(self.APhi), Ac_inv=ptr(self.Ac_inv), work=ptr(self.work))
+        need = nat.lib().mbem_nn_setup_workspace_size(nc)
+        setup_work = torch.empty(need, dtype=torch.uint8, device=dev)
+        A = asm.A
+        nat.call("mbem_nn_setup_dense", ptr(A), A.stride(0), ctypes.byref(self._struct), ptr(setup_work), need,
+                 stream_handle())
         self.built = True
 
     def struct(self):
@@ -177,7 +183,7 @@ class LearnedPreconditioner:
 # ---------------------------------------------------------------------------
 # training data and training
 # ---------------------------------------------------------------------------
-def _smooth_fields(pos: np.ndarray, n_samples: int, rng, n_modes: int = 24) -> np.ndarray:
+def smooth_fields(pos: np.ndarray, n_samples: int, rng, n_modes: int = 24) -> np.ndarray:
     """(S, 3 n) random smooth fields: sums of random plane waves over the
     node positions, wavelength 0.3 .. 3 box units, per component."""
     n = pos.shape[0]
@@ -192,9 +198,9 @@ def _smooth_fields(pos: np.ndarray, n_samples: int, rng, n_modes: int = 24) -> n
     return out.reshape(n_samples, 3 * n)
 
 
-def training_pairs(asm, n_samples: int, seed: int = 0, chunk: int = 512):
-    """(rho (S, N) FP32, e (S, N) FP32) on the device for one assembled FP64
-    system: e = the deflated solution of A e = r (bordered LU), rho = BJ r."""
+def training_errors(asm, n_samples: int, seed: int = 0, chunk: int = 512) -> torch.Tensor:
+    """(S, N) FP32 block-Jacobi errors eps = A^-1 r - BJ r on the device for
+    one assembled FP64 system (A^-1: the deflated solution, bordered LU)."""
     from ..backends.dense import translation_basis
     A = asm.A
     N = A.shape[0]
@@ -211,27 +217,34 @@ def training_pairs(asm, n_samples: int, seed: int = 0, chunk: int = 512):
     LU, piv = torch.linalg.lu_factor(B)
     del B
     bj = asm.block_jacobi()
-    rho = torch.empty((n_samples, N), dtype=torch.float32, device=dev)
-    e = torch.empty((n_samples, N), dtype=torch.float32, device=dev)
+    eps = torch.empty((n_samples, N), dtype=torch.float32, device=dev)
     for s0 in range(0, n_samples, chunk):
         S = min(chunk, n_samples - s0)
-        n1 = int(0.4 * S)
-        n2 = int(0.3 * S)
-        R = np.empty((S, N))
-        R[:n1] = _smooth_fields(pos, n1, rng)
-        sm = torch.from_numpy(_smooth_fields(pos, n2, rng)).to(dev)
-        R[n1:n1 + n2] = (sm @ A.T).cpu().numpy()
-        R[n1 + n2:] = rng.normal(size=(S - n1 - n2, N))
-        Rt = torch.from_numpy(R).to(dev)
+        n1, n2 = int(0.4 * S), int(0.3 * S)
+        R = torch.empty((S, N), dtype=torch.float64, device=dev)
+        R[:n1] = torch.from_numpy(smooth_fields(pos, n1, rng)).to(dev)
+        R[n1:n1 + n2] = torch.from_numpy(smooth_fields(pos, n2, rng)).to(dev) @ A.T
+        R[n1 + n2:] = torch.from_numpy(rng.normal(size=(S - n1 - n2, N))).to(dev)
         if nz:
-            Rt = Rt - (Rt @ Z) @ Z.T            # the residuals of the deflated system
+            R = R - (R @ Z) @ Z.T                # the residuals of the deflated system
         rhs = torch.zeros((N + nz, S), dtype=torch.float64, device=dev)
-        rhs[:N] = Rt.T
+        rhs[:N] = R.T
         E = torch.linalg.lu_solve(LU, piv, rhs)[:N].T
-        e[s0:s0 + S] = E.float()
         for q in range(S):
-            rho[s0 + q] = bj.apply(Rt[q]).float()
-    return rho, e
+            E[q] -= bj.apply(R[q])
+        eps[s0:s0 + S] = E.float()
+    return eps
+
+
+class TrainingMesh:
+    """One training system: its block-Jacobi chunks, node features and
+    block-Jacobi errors, on the device."""
+
+    def __init__(self, asm, n_samples: int, seed: int = 0):
+        self.bj = asm.block_jacobi()
+        self.feat = torch.from_numpy(node_features(asm.layout, self.bj.chunk_nodes())).to(self.bj.device)
+        self.eps = training_errors(asm, n_samples, seed)
+        self.chunks = self.bj.chunk_nodes()
 
 
 class Trainer:
@@ -249,57 +262,49 @@ class Trainer:
         self.loss_dev = torch.zeros(1, dtype=torch.float64, device=self.device)
         self.history = []
 
-    def batch_grad(self, feat, nbr, rho, e):
-        """loss (device scalar) and self.grad for one batch (rho, e: (S, N))."""
-        S, N = rho.shape
-        n_nodes, k = nbr.shape
-        E = feat.shape[0]
-        act = torch.empty((E, 2 * nat.NN_HIDDEN), dtype=torch.float32, device=self.device)
-        w = edge_blocks(feat, self.params, act)
-        z = torch.empty_like(rho)
+    def batch_grad(self, feat: torch.Tensor, bj, eps: torch.Tensor) -> torch.Tensor:
+        """Loss (device scalar) of one batch of block-Jacobi errors (S, N);
+        leaves dloss/dparams in self.grad."""
+        S = eps.shape[0]
+        n_items = feat.shape[0]
+        act = torch.empty((n_items, 2 * nat.NN_HIDDEN), dtype=torch.float32, device=self.device)
+        phi = mlp_forward(feat, self.params, act)
+        inv_e2 = (1.0 / (eps.double() ** 2).sum(1)).float().contiguous()
+        dphi = torch.empty_like(phi)
+        partial = torch.empty(bj.n_chunks, dtype=torch.float64, device=self.device)
         st = stream_handle()
-        nat.call("mbem_nn_apply_batch", ptr(nbr), n_nodes, k, ptr(w), ptr(rho), S, ptr(z), st)
-        inv_e2 = (1.0 / (e.double() ** 2).sum(1)).float().contiguous()
-        dz = torch.empty_like(rho)
-        partial = torch.empty(nat.lib().mbem_nn_loss_partial_count(S, N), dtype=torch.float64, device=self.device)
-        nat.call("mbem_nn_loss_grad", ptr(z), ptr(e), ptr(inv_e2), S, N, ptr(dz), ptr(partial), ptr(self.loss_dev),
-                 st)
-        G = torch.empty((E, 9), dtype=torch.float32, device=self.device)
-        nat.call("mbem_nn_edge_grad", ptr(nbr), n_nodes, k, ptr(dz), ptr(rho), S, ptr(G), st)
-        need = nat.lib().mbem_nn_backward_workspace_size(E)
+        nat.call("mbem_nn_coarse_loss_grad", ctypes.byref(bj.struct()), ptr(phi), ptr(eps), ptr(inv_e2), S,
+                 ptr(dphi), ptr(partial), ptr(self.loss_dev), st)
+        need = nat.lib().mbem_nn_backward_workspace_size(n_items)
         work = torch.empty(need, dtype=torch.uint8, device=self.device)
-        nat.call("mbem_nn_backward", ptr(feat), E, ptr(self.params), ptr(act), ptr(G), ptr(self.grad), ptr(work),
-                 need, st)
+        nat.call("mbem_nn_backward", ptr(feat), n_items, ptr(self.params), ptr(act), ptr(dphi), ptr(self.grad),
+                 ptr(work), need, st)
         return self.loss_dev
 
-    def step(self, feat, nbr, rho, e):
-        loss = self.batch_grad(feat, nbr, rho, e)
+    def step(self, feat, bj, eps):
+        loss = self.batch_grad(feat, bj, eps)
         self.step_count += 1
         nat.call("mbem_nn_adam", ptr(self.params), ptr(self.grad), ptr(self.m), ptr(self.v), self.params.numel(),
                  self.lr, 0.9, 0.999, 1e-8, self.step_count, stream_handle())
         return loss
 
 
-def train(datasets, steps: int = 400, batch: int = 64, lr: float = 2e-3, seed: int = 0, log_every: int = 0):
-    """Trains on [(graph, rho, e), ...] (one per training mesh, batches drawn
-    round-robin over the meshes); returns (params np.float32, Trainer)."""
+def train(meshes, steps: int = 600, batch: int = 64, lr: float = 2e-3, seed: int = 0, log_every: int = 0):
+    """Trains on a list of ``TrainingMesh`` (batches drawn round-robin over
+    the meshes); returns (params np.float32, Trainer)."""
     tr = Trainer(lr=lr, seed=seed)
     rng = np.random.default_rng(seed + 1)
-    dev = tr.device
-    prepared = [(torch.from_numpy(g.feat).to(dev), torch.from_numpy(g.nbr).to(dev), rho, e)
-                for g, rho, e in datasets]
     for it in range(steps):
-        feat, nbr, rho, e = prepared[it % len(prepared)]
-        idx = torch.from_numpy(rng.choice(rho.shape[0], size=min(batch, rho.shape[0]), replace=False)).to(dev)
-        loss = tr.step(feat, nbr, rho.index_select(0, idx).contiguous(), e.index_select(0, idx).contiguous())
+        m = meshes[it % len(meshes)]
+        idx = torch.from_numpy(rng.choice(m.eps.shape[0], size=min(batch, m.eps.shape[0]),
+                                          replace=False)).to(tr.device)
+        loss = tr.step(m.feat, m.bj, m.eps.index_select(0, idx).contiguous())
         if log_every and (it % log_every == 0 or it == steps - 1):
             tr.history.append((it, float(loss.item())))
     return tr.params.cpu().numpy(), tr
 
 
-def validation_loss(params, graph, rho, e) -> float:
-    """Mean relative squared error of (I + W) rho against e."""
-    tr = Trainer(params=params)
-    feat = torch.from_numpy(graph.feat).to(tr.device)
-    nbr = torch.from_numpy(graph.nbr).to(tr.device)
-    return float(tr.batch_grad(feat, nbr, rho, e).item())
+def coarse_loss(params, mesh: TrainingMesh) -> float:
+    """The projection loss of a parameter set on all of a mesh's errors."""
+    tr = Trainer(params=params, device=mesh.bj.device)
+    return float(tr.batch_grad(mesh.feat, mesh.bj, mesh.eps).item())

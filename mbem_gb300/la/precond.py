@@ -82,6 +82,7 @@ class BlockJacobi:
         self.n_chunks = len(chunks)
         self.m_max = int(sizes.max()) if sizes.size else 1
         self.chunk_sizes = sizes
+        self._chunks = chunks
         self.device = torch.device(device)
         self._ptr = torch.from_numpy(ptr_h).to(self.device)
         self._dofs = torch.from_numpy(dofs.astype(np.int64)).to(self.device)
@@ -103,6 +104,10 @@ class BlockJacobi:
 
     def struct(self):
         return self._struct
+
+    def chunk_nodes(self) -> list:
+        """Node indices (unknowns 3i..3i+2) of every chunk, in chunk order."""
+        return [d[::3] // 3 for d in self._chunks]
 
     def build_dense(self, A: torch.Tensor):
         if A.dtype != torch.float64 or A.stride(1) != 1 or A.shape[0] != self.n:

@@ -1,16 +1,19 @@
-"""CPU oracle (FP64 numpy) of the learned preconditioner's network: forward
-pass, batched apply, loss and the gradient of the loss with respect to the
-parameters, by explicit backpropagation (no autograd).
+"""CPU oracle (FP64 numpy) of the learned preconditioner: the network's
+forward pass and the gradient of the training loss by explicit
+backpropagation (no autograd), the coarse-space loss, and the preconditioner
+apply.
 
 Test infrastructure only: the GPU kernels in mbem_gb300/csrc/nn.cu are
-checked against these functions. The network has no counterpart in the
-reference (it is the learned replacement of the block-Jacobi rung of
-src/mbem/la/preconditioner.py:421-470), so the oracle restates the
-network's definition:
+checked against these functions. The learned preconditioner has no
+counterpart in the reference (it replaces the block-Jacobi rung of
+src/mbem/la/preconditioner.py:421-470), so the oracle restates its
+definition:
 
-    W_e = MLP(g_e),  MLP: F -> H (tanh) -> H (tanh) -> 9
-    z_s,i = rho_s,i + sum_q W_(i,q) rho_s,nbr(i,q)
-    loss = (1/S) sum_s |z_s - e_s|^2 / |e_s|^2
+    phi_i = MLP(g_i)  (3x3 per node),  MLP: F -> H (tanh) -> H (tanh) -> 9
+    Phi[3i + a, 3c(i) + k] = phi_i[a, k]
+    loss = (1/S) sum_s sum_c |eps_sc - Phi_c y_sc|^2 / |eps_s|^2,
+           y_sc = argmin_y |eps_sc - Phi_c y|
+    z = Phi y + BJ (r - A Phi y),  y = (Phi^T A Phi)^-1 Phi^T r
 
 Parameter layout (flat): W1 (H, F), b1 (H), W2 (H, H), b2 (H), W3 (9, H), b3 (9).
 """
@@ -45,33 +48,46 @@ def forward(feat: np.ndarray, params: np.ndarray):
     return h2 @ W3.T + b3, h1, h2
 
 
-def apply(nbr: np.ndarray, w: np.ndarray, rho: np.ndarray) -> np.ndarray:
-    """z (S, 3 n) = rho + W rho for rho (S, 3 n)."""
-    n, k = nbr.shape
-    S = rho.shape[0]
-    r = rho.reshape(S, n, 3)
-    Wb = w.reshape(n, k, 3, 3)
-    z = r + np.einsum("iqab,sqib->sia", Wb, r[:, nbr, :].transpose(0, 2, 1, 3))
-    return z.reshape(S, 3 * n)
+def coarse_loss_grad(chunks, phi, eps):
+    """(loss, dloss/dphi (n, 9)) of the chunk-wise projection loss; chunks:
+    list of node-index arrays, phi (n, 3, 3), eps (S, 3 n)."""
+    phi = np.asarray(phi, float).reshape(-1, 3, 3)
+    n = phi.shape[0]
+    S = eps.shape[0]
+    E = np.asarray(eps, float).reshape(S, n, 3)
+    inv = 1.0 / np.sum(E.reshape(S, -1) ** 2, axis=1)
+    loss = 0.0
+    grad = np.zeros((n, 3, 3))
+    for nodes in chunks:
+        Pm = phi[nodes].reshape(-1, 3)                    # (3m, 3)
+        ec = E[:, nodes, :].reshape(S, -1)                # (S, 3m)
+        y = np.linalg.solve(Pm.T @ Pm, (ec @ Pm).T).T     # (S, 3)
+        res = ec - y @ Pm.T
+        loss += float(np.sum(np.sum(res * res, axis=1) * inv) / S)
+        g = -(2.0 / S) * np.einsum("s,sp,sk->pk", inv, res, y)    # (3m, 3)
+        grad[nodes] += g.reshape(-1, 3, 3)
+    return loss, grad.reshape(n, 9)
 
 
-def loss_and_grad(feat, params, nbr, rho, e):
-    """(loss, dloss/dparams) for one batch."""
+def loss_and_grad(feat, params, chunks, eps):
+    """(loss, dloss/dparams) of the coarse-space loss through the MLP."""
     W1, b1, W2, b2, W3, b3 = unpack(params)
-    w, h1, h2 = forward(feat, params)
-    S = rho.shape[0]
-    n, k = nbr.shape
-    z = apply(nbr, w, rho)
-    inv_e2 = 1.0 / np.sum(e * e, axis=1)
-    d = z - e
-    loss = float(np.sum(d * d * inv_e2[:, None]) / S)
-    dz = (2.0 / S) * d * inv_e2[:, None]
-    dzr = dz.reshape(S, n, 3)
-    rr = rho.reshape(S, n, 3)
-    # G_(i,q)[a, b] = sum_s dz[s, i, a] rho[s, nbr(i, q), b]
-    G = np.einsum("sia,sqib->iqab", dzr, rr[:, nbr, :].transpose(0, 2, 1, 3)).reshape(n * k, 9)
-    d3 = G
+    out, h1, h2 = forward(feat, params)
+    loss, d3 = coarse_loss_grad(chunks, out, eps)
     d2 = (d3 @ W3) * (1.0 - h2 * h2)
     d1 = (d2 @ W2) * (1.0 - h1 * h1)
     grads = [d1.T @ np.asarray(feat, float), d1.sum(0), d2.T @ h1, d2.sum(0), d3.T @ h2, d3.sum(0)]
     return loss, np.concatenate([g.ravel() for g in grads])
+
+
+def two_level_apply(A, chunks, phi, bj_solve, r):
+    """z = Phi y + BJ (r - A Phi y), y = (Phi^T A Phi)^-1 Phi^T r (dense)."""
+    phi = np.asarray(phi, float).reshape(-1, 3, 3)
+    n3 = A.shape[0]
+    Phi = np.zeros((n3, 3 * len(chunks)))
+    for c, nodes in enumerate(chunks):
+        for a in range(3):
+            Phi[3 * nodes + a, 3 * c:3 * c + 3] = phi[nodes, a, :]
+    AP = A @ Phi
+    y = np.linalg.solve(Phi.T @ AP, Phi.T @ r)
+    return Phi @ y + bj_solve(r - AP @ y)
