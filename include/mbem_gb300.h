@@ -246,9 +246,10 @@ int mbem_bj_apply(const mbem_block_jacobi* bj, const double* r, double* z, void*
 /* ---- learned preconditioner: block-Jacobi with a learned coarse space (no
  * reference counterpart: it replaces the block-Jacobi rung of
  * la/preconditioner.py:421-470 in the solve). Each block-Jacobi chunk c gets
- * three coarse vectors whose 3x3 block on node i of the chunk is phi_i, the
- * output of a small MLP on the node's geometry (phi_i = I: the chunk's
- * translations). With Phi (n x 3C) and A_c = Phi^T A Phi:
+ * six coarse vectors: its three translations and three learned vectors whose
+ * 3x3 block on node i of the chunk is phi_i, the output of a small MLP on the
+ * node's geometry; on node i the basis block is [I | phi_i] (3 x 6). With
+ * Phi (n x 6C) and A_c = Phi^T A Phi:
  *     y = A_c^-1 Phi^T r,   z = Phi y + BJ (r - (A Phi) y).
  * MLP: MBEM_NN_FEAT -> MBEM_NN_HIDDEN (tanh) -> MBEM_NN_HIDDEN (tanh) -> 9
  * (phi_i row-major); flat FP32 parameters W1 (H x F), b1, W2 (H x H), b2,
@@ -260,7 +261,7 @@ int mbem_bj_apply(const mbem_block_jacobi* bj, const double* r, double* z, void*
                         MBEM_NN_HIDDEN + 9 * MBEM_NN_HIDDEN + 9)
 typedef struct {
     int64_t n;                       /* unknowns (a multiple of 3) */
-    int64_t n_coarse;                /* 3 x the block-Jacobi chunks */
+    int64_t n_coarse;                /* 6 x the block-Jacobi chunks */
     const mbem_block_jacobi* bj;     /* chunks and their inverses (host pointer; chunk_of required) */
     const float* phi;                /* (n/3, 3, 3) device: coarse blocks per node (mbem_nn_forward) */
     const double* APhi;              /* (n, n_coarse) device: A Phi, written by mbem_nn_setup_dense */
@@ -272,8 +273,9 @@ typedef struct {
  * keeps the hidden activations for training (NULL at inference). */
 int mbem_nn_forward(const float* feat, int64_t n_items, const float* params, float* act, float* out,
                     void* stream);
-/* Training loss: the chunk-wise least-squares projection error of the
- * block-Jacobi errors eps (n_samples, n) onto the coarse space, weighted by
+/* Training loss: the chunk-wise least-squares projection error (normal
+ * equations regularised by 1e-8 trace / 6) of the block-Jacobi errors eps
+ * (n_samples, n) onto each chunk's six coarse vectors, weighted by
  * inv_e2 (1/|eps_s|^2) and averaged, into *loss (device double); dphi
  * (n/3, 9) = dloss/dphi. partial: bj->n_chunks device doubles. */
 int mbem_nn_coarse_loss_grad(const mbem_block_jacobi* bj, const float* phi, const float* eps,

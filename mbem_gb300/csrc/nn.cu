@@ -1,11 +1,12 @@
 // Learned preconditioner: block-Jacobi with a learned coarse space.
 //
-// The unknowns are split into the block-Jacobi chunks. Each chunk c gets
-// three coarse vectors; on node i of chunk c they take the 3x3 block phi_i,
-// the output of a small MLP on the node's geometry (its place in the chunk,
-// its normal, its slot kind, the shape of its neighbourhood). phi_i = I gives
-// the chunk translations (a Nicolaides coarse space). With Phi (n x 3C) the
-// coarse basis and A_c = Phi^T A Phi, the preconditioner is multiplicative:
+// The unknowns are split into the block-Jacobi chunks. Each chunk c gets six
+// coarse vectors: the chunk's three translations and three learned vectors
+// whose 3x3 block on node i of the chunk is phi_i, the output of a small MLP
+// on the node's geometry (its place in the chunk, its normal, its slot kind,
+// the shape of its neighbourhood). On node i the coarse basis is the 3x6
+// block B_i = [I | phi_i]. With Phi (n x 6C) and A_c = Phi^T A Phi, the
+// preconditioner is multiplicative:
 //
 //   y = A_c^-1 Phi^T r,   z = Phi y + BJ (r - (A Phi) y).
 //
@@ -15,11 +16,13 @@
 //
 // Training: the coarse space should hold what block-Jacobi misses, the error
 // eps = A^-1 r - BJ r of training pairs. The loss is the chunk-wise
-// least-squares projection error of eps onto the coarse space,
+// least-squares projection error of eps onto the chunk's six vectors,
 //   loss = (1/S) sum_s sum_c |eps_sc - Phi_c y_sc|^2 / |eps_s|^2,
-//   y_sc = argmin_y |eps_sc - Phi_c y|,
-// whose gradient needs no derivative of y (it is the minimiser):
-//   dloss/dphi_i = -(2/S) sum_s (eps_si - phi_i y_sc) y_sc^T / |eps_s|^2.
+//   y_sc = (G_c + delta I)^-1 Phi_c^T eps_sc,  G_c = Phi_c^T Phi_c,
+//   delta = 1e-8 trace(G_c) / 6,
+// and, y being the (regularised) minimiser, the gradient needs no
+// derivative of y:
+//   dloss/dphi_i = -(2/S) sum_s (eps_si - B_i y_sc) y_sc[3:6]^T / |eps_s|^2.
 // MLP: MBEM_NN_FEAT -> MBEM_NN_HIDDEN (tanh) -> MBEM_NN_HIDDEN (tanh) -> 9
 // (phi_i row-major); flat FP32 parameters W1 (H x F), b1, W2 (H x H), b2,
 // W3 (9 x H), b3. Every reduction runs in a fixed order: training and setup
@@ -40,7 +43,7 @@ constexpr int ACT = 2 * NH;          // stored activations per item (h1, h2)
 constexpr int DEL = 2 * NH + 9;      // stored deltas per item (d1, d2, d3)
 constexpr int NN_THREADS = 256;
 constexpr int GRAD_CHUNK = 512;      // items per partial parameter-gradient sum
-constexpr int CHUNK_NODES = MBEM_BJ_MAX_DOF / 3;
+constexpr int NCV = 6;               // coarse vectors per chunk: 3 translations + 3 learned
 
 // ---------------------------------------------------------------------------
 // MLP forward: one thread per item (node), parameters in shared memory
@@ -100,12 +103,34 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
     return ((red[0] + red[1]) + red[2]) + red[3];
 }
 
+// inverse of a symmetric positive 6x6 (Gauss-Jordan, no pivoting needed)
+__device__ void inv6(double M[6][6], double R[6][6]) {
+    for (int i = 0; i < 6; i++)
+        for (int j = 0; j < 6; j++) R[i][j] = (i == j) ? 1.0 : 0.0;
+    for (int k = 0; k < 6; k++) {
+        const double d = (M[k][k] != 0.0) ? 1.0 / M[k][k] : 0.0;
+        for (int j = 0; j < 6; j++) {
+            M[k][j] *= d;
+            R[k][j] *= d;
+        }
+        for (int i = 0; i < 6; i++) {
+            if (i == k) continue;
+            const double f = M[i][k];
+            for (int j = 0; j < 6; j++) {
+                M[i][j] -= f * M[k][j];
+                R[i][j] -= f * R[k][j];
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128)
 nn_coarse_loss_grad_kernel(const int64_t* __restrict__ chunk_ptr, const int64_t* __restrict__ dofs,
                            const float* __restrict__ phi, const float* __restrict__ eps,
                            const float* __restrict__ inv_e2, int64_t S, int64_t N, float* __restrict__ dphi,
                            double* __restrict__ partial) {
     __shared__ double red[4];
+    __shared__ double Ginv[6][6];
     const int c = blockIdx.x;
     const int64_t c0 = chunk_ptr[c];
     const int m = (int)((chunk_ptr[c + 1] - c0) / 3);
@@ -120,22 +145,34 @@ nn_coarse_loss_grad_kernel(const int64_t* __restrict__ chunk_ptr, const int64_t*
 #pragma unroll
         for (int q = 0; q < 9; q++) P[q] = phi[node * 9 + q];
     }
-    // G = sum_i phi_i^T phi_i (symmetric 3x3), inverted once
-    double G[6];
-    {
-        const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
-        for (int q = 0; q < 6; q++) {
-            const int a = ia[q], b = ib[q];
+    // G = sum_i B_i^T B_i with B_i = [I | phi_i]:
+    // [[m I, sum phi_i], [sum phi_i^T, sum phi_i^T phi_i]]
+    double sp[9], gl[9];
+    for (int q = 0; q < 9; q++) sp[q] = block_sum(live ? (double)P[q] : 0.0, red);
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) {
             double v = 0.0;
             for (int r = 0; r < 3; r++) v += (double)P[3 * r + a] * (double)P[3 * r + b];
-            G[q] = block_sum(v, red);
+            gl[3 * a + b] = block_sum(v, red);
         }
+    if (t == 0) {
+        double G[6][6];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) {
+                G[a][b] = (a == b) ? (double)m : 0.0;
+                G[a][3 + b] = sp[3 * a + b];
+                G[3 + b][a] = sp[3 * a + b];
+                G[3 + a][3 + b] = gl[3 * a + b];
+            }
+        double tr = 0.0;
+        for (int a = 0; a < 6; a++) tr += G[a][a];
+        for (int a = 0; a < 6; a++) G[a][a] += 1e-8 * tr / 6.0;
+        double R[6][6];
+        inv6(G, R);
+        for (int a = 0; a < 6; a++)
+            for (int b = 0; b < 6; b++) Ginv[a][b] = R[a][b];
     }
-    const double g00 = G[0], g01 = G[1], g02 = G[2], g11 = G[3], g12 = G[4], g22 = G[5];
-    const double c00 = g11 * g22 - g12 * g12, c01 = g02 * g12 - g01 * g22, c02 = g01 * g12 - g02 * g11;
-    const double c11 = g00 * g22 - g02 * g02, c12 = g01 * g02 - g00 * g12, c22 = g00 * g11 - g01 * g01;
-    const double det = g00 * c00 + g01 * c01 + g02 * c02;
-    const double id = (det != 0.0) ? 1.0 / det : 0.0;
+    __syncthreads();
     double gr[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     double lsum = 0.0;
     for (int64_t s = 0; s < S; s++) {
@@ -144,23 +181,27 @@ nn_coarse_loss_grad_kernel(const int64_t* __restrict__ chunk_ptr, const int64_t*
             const float* es = eps + s * N + 3 * node;
             ev[0] = es[0]; ev[1] = es[1]; ev[2] = es[2];
         }
-        double b[3];
+        double b[6];
+        for (int k = 0; k < 3; k++) b[k] = block_sum(live ? (double)ev[k] : 0.0, red);
         for (int k = 0; k < 3; k++) {
             const double v = (double)P[k] * ev[0] + (double)P[3 + k] * ev[1] + (double)P[6 + k] * ev[2];
-            b[k] = block_sum(v, red);
+            b[3 + k] = block_sum(v, red);
         }
-        const double y0 = id * (c00 * b[0] + c01 * b[1] + c02 * b[2]);
-        const double y1 = id * (c01 * b[0] + c11 * b[1] + c12 * b[2]);
-        const double y2 = id * (c02 * b[0] + c12 * b[1] + c22 * b[2]);
+        double y[6];
+        for (int a = 0; a < 6; a++) {
+            double v = 0.0;
+            for (int q = 0; q < 6; q++) v += Ginv[a][q] * b[q];
+            y[a] = v;
+        }
         if (live) {
             const double w = (double)inv_e2[s] / (double)S;
             for (int a = 0; a < 3; a++) {
-                const double res = ev[a] - ((double)P[3 * a] * y0 + (double)P[3 * a + 1] * y1 +
-                                            (double)P[3 * a + 2] * y2);
+                const double res = ev[a] - (y[a] + (double)P[3 * a] * y[3] + (double)P[3 * a + 1] * y[4] +
+                                            (double)P[3 * a + 2] * y[5]);
                 lsum += res * res * w;
-                gr[3 * a] -= 2.0 * w * res * y0;
-                gr[3 * a + 1] -= 2.0 * w * res * y1;
-                gr[3 * a + 2] -= 2.0 * w * res * y2;
+                gr[3 * a] -= 2.0 * w * res * y[3];
+                gr[3 * a + 1] -= 2.0 * w * res * y[4];
+                gr[3 * a + 2] -= 2.0 * w * res * y[5];
             }
         }
     }
@@ -267,7 +308,7 @@ __global__ void nn_adam_kernel(float* __restrict__ params, const float* __restri
 // ---------------------------------------------------------------------------
 constexpr int APHI_ROWS = 64;     // rows of A per CTA
 
-// APhi[r, 3c + k] = sum_{i in c} sum_a A[r, 3i + a] phi_i[a][k]; a CTA per
+// APhi[r, 6c + k] = sum_{i in c} sum_a A[r, 3i + a] B_i[a][k]; a CTA per
 // (chunk, 64-row tile), a warp per row, lanes along the chunk's columns
 __global__ void __launch_bounds__(256)
 nn_aphi_kernel(const double* __restrict__ A, int64_t ld, int64_t n, const int64_t* __restrict__ chunk_ptr,
@@ -275,6 +316,7 @@ nn_aphi_kernel(const double* __restrict__ A, int64_t ld, int64_t n, const int64_
                double* __restrict__ APhi) {
     __shared__ int64_t col[MBEM_BJ_MAX_DOF];
     __shared__ float ph[MBEM_BJ_MAX_DOF][3];
+    __shared__ int comp[MBEM_BJ_MAX_DOF];
     const int c = blockIdx.x;
     const int64_t c0 = chunk_ptr[c];
     const int m = (int)(chunk_ptr[c + 1] - c0);
@@ -283,6 +325,7 @@ nn_aphi_kernel(const double* __restrict__ A, int64_t ld, int64_t n, const int64_
         col[t] = d;
         const int64_t node = d / 3;
         const int a = (int)(d % 3);
+        comp[t] = a;
         ph[t][0] = phi[node * 9 + 3 * a];
         ph[t][1] = phi[node * 9 + 3 * a + 1];
         ph[t][2] = phi[node * 9 + 3 * a + 2];
@@ -292,28 +335,28 @@ nn_aphi_kernel(const double* __restrict__ A, int64_t ld, int64_t n, const int64_
     const int64_t r0 = (int64_t)blockIdx.y * APHI_ROWS;
     for (int64_t r = r0 + warp; r < lmin(n, r0 + APHI_ROWS); r += 8) {
         const double* Ar = A + r * ld;
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         for (int t = lane; t < m; t += 32) {
             const double v = Ar[col[t]];
-            s0 += v * (double)ph[t][0];
-            s1 += v * (double)ph[t][1];
-            s2 += v * (double)ph[t][2];
+            const int a = comp[t];
+            s[0] += (a == 0) ? v : 0.0;
+            s[1] += (a == 1) ? v : 0.0;
+            s[2] += (a == 2) ? v : 0.0;
+            s[3] += v * (double)ph[t][0];
+            s[4] += v * (double)ph[t][1];
+            s[5] += v * (double)ph[t][2];
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-        }
-        if (lane == 0) {
-            APhi[r * n_coarse + 3 * c] = s0;
-            APhi[r * n_coarse + 3 * c + 1] = s1;
-            APhi[r * n_coarse + 3 * c + 2] = s2;
-        }
+        for (int k = 0; k < 6; k++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < 6; k++) APhi[r * n_coarse + NCV * c + k] = s[k];
     }
 }
 
-// Ac[3c + k, q] = sum_{i in c} sum_a phi_i[a][k] APhi[3i + a, q]: a CTA per
+// Ac[6c + k, q] = sum_{i in c} sum_a B_i[a][k] APhi[3i + a, q]: a CTA per
 // (chunk, 256 columns), a thread per column
 __global__ void __launch_bounds__(256)
 nn_coarse_matrix_kernel(const double* __restrict__ APhi, int64_t n_coarse, const int64_t* __restrict__ chunk_ptr,
@@ -323,19 +366,18 @@ nn_coarse_matrix_kernel(const double* __restrict__ APhi, int64_t n_coarse, const
     if (q >= n_coarse) return;
     const int64_t c0 = chunk_ptr[c];
     const int m = (int)(chunk_ptr[c + 1] - c0);
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int t = 0; t < m; t++) {
         const int64_t d = dofs[c0 + t];
         const int64_t node = d / 3;
         const int a = (int)(d % 3);
         const double v = APhi[d * n_coarse + q];
-        s0 += (double)phi[node * 9 + 3 * a] * v;
-        s1 += (double)phi[node * 9 + 3 * a + 1] * v;
-        s2 += (double)phi[node * 9 + 3 * a + 2] * v;
+        s[a] += v;
+        s[3] += (double)phi[node * 9 + 3 * a] * v;
+        s[4] += (double)phi[node * 9 + 3 * a + 1] * v;
+        s[5] += (double)phi[node * 9 + 3 * a + 2] * v;
     }
-    Ac[(3 * c) * n_coarse + q] = s0;
-    Ac[(3 * c + 1) * n_coarse + q] = s1;
-    Ac[(3 * c + 2) * n_coarse + q] = s2;
+    for (int k = 0; k < 6; k++) Ac[(NCV * c + k) * n_coarse + q] = s[k];
 }
 
 // Gauss-Jordan step k on M (m x m, FP64, in place): pivot search, row swap,
@@ -416,7 +458,7 @@ __global__ void gj_swap_columns_kernel(double* __restrict__ M, int64_t m, const 
 // ---------------------------------------------------------------------------
 // apply pieces
 // ---------------------------------------------------------------------------
-// q[3c + k] = sum_{i in c} sum_a phi_i[a][k] r[3i + a]; a CTA per chunk
+// q[6c + k] = sum_{i in c} sum_a B_i[a][k] r[3i + a]; a CTA per chunk
 __global__ void __launch_bounds__(128)
 nn_phit_kernel(const int64_t* __restrict__ chunk_ptr, const int64_t* __restrict__ dofs,
                const float* __restrict__ phi, const double* __restrict__ r, double* __restrict__ q) {
@@ -424,23 +466,24 @@ nn_phit_kernel(const int64_t* __restrict__ chunk_ptr, const int64_t* __restrict_
     const int c = blockIdx.x;
     const int64_t c0 = chunk_ptr[c];
     const int m = (int)(chunk_ptr[c + 1] - c0);
-    double s[3] = {0.0, 0.0, 0.0};
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int t = threadIdx.x; t < m; t += 128) {
         const int64_t d = dofs[c0 + t];
         const int64_t node = d / 3;
         const int a = (int)(d % 3);
         const double v = r[d];
-        s[0] += (double)phi[node * 9 + 3 * a] * v;
-        s[1] += (double)phi[node * 9 + 3 * a + 1] * v;
-        s[2] += (double)phi[node * 9 + 3 * a + 2] * v;
+        s[a] += v;
+        s[3] += (double)phi[node * 9 + 3 * a] * v;
+        s[4] += (double)phi[node * 9 + 3 * a + 1] * v;
+        s[5] += (double)phi[node * 9 + 3 * a + 2] * v;
     }
-    for (int k = 0; k < 3; k++) {
+    for (int k = 0; k < 6; k++) {
         const double tot = block_sum(s[k], red);
-        if (threadIdx.x == 0) q[3 * c + k] = tot;
+        if (threadIdx.x == 0) q[NCV * c + k] = tot;
     }
 }
 
-// z[d] += sum_k phi_i[a][k] y[3 c(d) + k] for d = 3i + a
+// z[d] += y[6c + a] + sum_k phi_i[a][k] y[6c + 3 + k] for d = 3i + a in chunk c
 __global__ void __launch_bounds__(256)
 nn_phi_add_kernel(int64_t n, const int32_t* __restrict__ chunk_of, const float* __restrict__ phi,
                   const double* __restrict__ y, double* __restrict__ z) {
@@ -448,15 +491,14 @@ nn_phi_add_kernel(int64_t n, const int32_t* __restrict__ chunk_of, const float* 
     if (d >= n) return;
     const int64_t node = d / 3;
     const int a = (int)(d % 3);
-    const int64_t c = chunk_of[d];
-    const double* yc = y + 3 * c;
-    z[d] += (double)phi[node * 9 + 3 * a] * yc[0] + (double)phi[node * 9 + 3 * a + 1] * yc[1] +
-            (double)phi[node * 9 + 3 * a + 2] * yc[2];
+    const double* yc = y + NCV * (int64_t)chunk_of[d];
+    z[d] += yc[a] + ((double)phi[node * 9 + 3 * a] * yc[3] + (double)phi[node * 9 + 3 * a + 1] * yc[4] +
+                     (double)phi[node * 9 + 3 * a + 2] * yc[5]);
 }
 
 static int nn_check(const mbem_nn_precond* nn) {
     MBEM_REQUIRE(nn != nullptr && nn->bj != nullptr, MBEM_ERR_ARG, "learned preconditioner descriptor is NULL");
-    MBEM_REQUIRE(nn->n == nn->bj->n && nn->n_coarse == 3 * nn->bj->n_chunks && nn->n % 3 == 0, MBEM_ERR_ARG,
+    MBEM_REQUIRE(nn->n == nn->bj->n && nn->n_coarse == NCV * nn->bj->n_chunks && nn->n % 3 == 0, MBEM_ERR_ARG,
                  "learned preconditioner sizes (n=%lld, coarse=%lld, chunks=%lld)", (long long)nn->n,
                  (long long)nn->n_coarse, (long long)nn->bj->n_chunks);
     MBEM_REQUIRE(nn->n == 0 || (nn->phi && nn->APhi && nn->Ac_inv && nn->work && nn->bj->chunk_of), MBEM_ERR_ARG,

@@ -1,14 +1,15 @@
 """Learned right preconditioner for FGMRES: cluster block-Jacobi with a
 learned coarse space.
 
-Each block-Jacobi chunk c (``la.precond``) gets three coarse vectors; on
-node i of the chunk (unknowns 3i..3i+2 of a u-, t- or b-slot) they take the
-3x3 block phi_i = MLP(g_i), where g_i is the node's geometry: its place in
+Each block-Jacobi chunk c (``la.precond``) gets six coarse vectors: its
+three translations and three learned vectors, whose 3x3 block on node i of
+the chunk (unknowns 3i..3i+2 of a u-, t- or b-slot) is phi_i = MLP(g_i);
+on node i the basis block is [I | phi_i]. g_i is the node's geometry: its place in
 the chunk (offset from the chunk centroid over the chunk radius), its
 normal, its slot kind, the shape of its neighbourhood (the mean offset of
 its nearest same-slot nodes, which points away from a patch edge), its size
-against the chunk's. phi_i = I gives the chunk translations (a Nicolaides
-coarse space), which is where training starts. The preconditioner is
+against the chunk's. The translations alone are a Nicolaides coarse space;
+the learned vectors add what they miss. The preconditioner is
 
     y = A_c^-1 Phi^T r,   z = Phi y + BJ (r - (A Phi) y),   A_c = Phi^T A Phi,
 
@@ -113,8 +114,9 @@ def node_features(layout, chunks) -> np.ndarray:
 # the network
 # ---------------------------------------------------------------------------
 def init_params(seed: int = 0) -> np.ndarray:
-    """Glorot-uniform hidden layers, zero output weights and an identity
-    output bias: phi_i = I, the chunk translations."""
+    """Glorot-uniform hidden layers, small random output weights (the
+    learned vectors must not vanish, or the projection has no gradient),
+    zero output bias."""
     rng = np.random.default_rng(seed)
     F, H = nat.NN_FEAT, nat.NN_HIDDEN
 
@@ -122,7 +124,7 @@ def init_params(seed: int = 0) -> np.ndarray:
         a = math.sqrt(6.0 / (i + o))
         return rng.uniform(-a, a, size=(o, i))
 
-    parts = [glorot(H, F), np.zeros(H), glorot(H, H), np.zeros(H), np.zeros((9, H)), np.eye(3).ravel()]
+    parts = [glorot(H, F), np.zeros(H), glorot(H, H), np.zeros(H), rng.normal(0.0, 0.1, size=(9, H)), np.zeros(9)]
     p = np.concatenate([x.ravel() for x in parts]).astype(np.float32)
     assert p.size == nat.NN_PARAMS
     return p
@@ -152,7 +154,7 @@ class LearnedPreconditioner:
         self.bj = bj if bj is not None else asm.block_jacobi()
         dev = self.bj.device
         n = self.bj.n
-        nc = 3 * self.bj.n_chunks
+        nc = 6 * self.bj.n_chunks
         self.params = torch.as_tensor(np.asarray(params, np.float32)).to(dev)
         self.feat = torch.from_numpy(node_features(asm.layout, self.bj.chunk_nodes())).to(dev)
         self.phi = mlp_forward(self.feat, self.params)

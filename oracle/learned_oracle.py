@@ -10,9 +10,9 @@ src/mbem/la/preconditioner.py:421-470), so the oracle restates its
 definition:
 
     phi_i = MLP(g_i)  (3x3 per node),  MLP: F -> H (tanh) -> H (tanh) -> 9
-    Phi[3i + a, 3c(i) + k] = phi_i[a, k]
+    B_i = [I | phi_i] (3x6),  Phi[3i + a, 6c(i) + k] = B_i[a, k]
     loss = (1/S) sum_s sum_c |eps_sc - Phi_c y_sc|^2 / |eps_s|^2,
-           y_sc = argmin_y |eps_sc - Phi_c y|
+           y_sc = (G_c + 1e-8 trace(G_c)/6 I)^-1 Phi_c^T eps_sc,  G_c = Phi_c^T Phi_c
     z = Phi y + BJ (r - A Phi y),  y = (Phi^T A Phi)^-1 Phi^T r
 
 Parameter layout (flat): W1 (H, F), b1 (H), W2 (H, H), b2 (H), W3 (9, H), b3 (9).
@@ -48,6 +48,13 @@ def forward(feat: np.ndarray, params: np.ndarray):
     return h2 @ W3.T + b3, h1, h2
 
 
+def _basis(phi_nodes):
+    """(3m, 6) chunk basis [I | phi_i] stacked over the chunk's nodes."""
+    m = phi_nodes.shape[0]
+    B = np.concatenate([np.broadcast_to(np.eye(3), (m, 3, 3)), phi_nodes], axis=2)
+    return B.reshape(3 * m, 6)
+
+
 def coarse_loss_grad(chunks, phi, eps):
     """(loss, dloss/dphi (n, 9)) of the chunk-wise projection loss; chunks:
     list of node-index arrays, phi (n, 3, 3), eps (S, 3 n)."""
@@ -59,12 +66,14 @@ def coarse_loss_grad(chunks, phi, eps):
     loss = 0.0
     grad = np.zeros((n, 3, 3))
     for nodes in chunks:
-        Pm = phi[nodes].reshape(-1, 3)                    # (3m, 3)
+        Pm = _basis(phi[nodes])                           # (3m, 6)
         ec = E[:, nodes, :].reshape(S, -1)                # (S, 3m)
-        y = np.linalg.solve(Pm.T @ Pm, (ec @ Pm).T).T     # (S, 3)
+        G = Pm.T @ Pm
+        G = G + 1e-8 * np.trace(G) / 6.0 * np.eye(6)
+        y = np.linalg.solve(G, (ec @ Pm).T).T             # (S, 6)
         res = ec - y @ Pm.T
         loss += float(np.sum(np.sum(res * res, axis=1) * inv) / S)
-        g = -(2.0 / S) * np.einsum("s,sp,sk->pk", inv, res, y)    # (3m, 3)
+        g = -(2.0 / S) * np.einsum("s,sp,sk->pk", inv, res, y[:, 3:])    # (3m, 3)
         grad[nodes] += g.reshape(-1, 3, 3)
     return loss, grad.reshape(n, 9)
 
@@ -84,10 +93,11 @@ def two_level_apply(A, chunks, phi, bj_solve, r):
     """z = Phi y + BJ (r - A Phi y), y = (Phi^T A Phi)^-1 Phi^T r (dense)."""
     phi = np.asarray(phi, float).reshape(-1, 3, 3)
     n3 = A.shape[0]
-    Phi = np.zeros((n3, 3 * len(chunks)))
+    Phi = np.zeros((n3, 6 * len(chunks)))
     for c, nodes in enumerate(chunks):
         for a in range(3):
-            Phi[3 * nodes + a, 3 * c:3 * c + 3] = phi[nodes, a, :]
+            Phi[3 * nodes + a, 6 * c + a] = 1.0
+            Phi[3 * nodes + a, 6 * c + 3:6 * c + 6] = phi[nodes, a, :]
     AP = A @ Phi
     y = np.linalg.solve(Phi.T @ AP, Phi.T @ r)
     return Phi @ y + bj_solve(r - AP @ y)

@@ -26,7 +26,6 @@ def _instance(seed=0, n=29, S=5):
     rng = np.random.default_rng(seed)
     feat = rng.normal(size=(n, lo.F)).astype(np.float32)
     params = (rng.normal(size=lo.N_PARAMS) * 0.3).astype(np.float32)
-    params[-9:] += np.eye(3).ravel().astype(np.float32)
     eps = rng.normal(size=(S, 3 * n)).astype(np.float32)
     return feat, params, eps
 
@@ -81,7 +80,6 @@ def test_two_level_apply_matches_oracle(gpu):
     from mbem_gb300.la.learned import LearnedPreconditioner, init_params
     asm = _fault_system(4, 2, 60.0)
     p = init_params(3)
-    p[-9 - 9 * lo.H:-9] = np.random.default_rng(1).normal(size=9 * lo.H) * 0.1
     lp = LearnedPreconditioner(asm, p)
     A = asm.A.cpu().numpy()
     bj = lp.bj
@@ -102,23 +100,23 @@ def test_two_level_apply_matches_oracle(gpu):
 @pytest.mark.gpu
 def test_trained_coarse_space_beats_block_jacobi(gpu):
     """Train on two small meshes (dips 45 and 75 degrees), then solve a
-    held-out mesh and dip. The learned coarse space lowers the held-out
-    projection loss below the translations' (the network's start) and takes
-    fewer FGMRES iterations than block-Jacobi alone and than the untrained
-    translation coarse space; the solutions agree."""
+    held-out mesh and dip. Training lowers the held-out projection loss; the
+    trained preconditioner takes fewer FGMRES iterations than block-Jacobi
+    alone and than the same coarse space with the untrained network; the
+    solutions agree."""
     from mbem_gb300.la.learned import LearnedPreconditioner, TrainingMesh, coarse_loss, init_params, train
     meshes = [TrainingMesh(_fault_system(6, 4, 45.0), 768, seed=1), TrainingMesh(_fault_system(8, 6, 75.0), 768,
                                                                                   seed=2)]
-    params, tr = train(meshes, steps=400, batch=64, lr=2e-3, log_every=100)
+    params, tr = train(meshes, steps=600, batch=64, lr=2e-3, log_every=100)
     asm = _fault_system(9, 6, 60.0, rtol=1e-10, maxiter=500)
     held = TrainingMesh(asm, 256, seed=3)
-    assert coarse_loss(params, held) < 0.95 * coarse_loss(init_params(), held)
+    assert coarse_loss(params, held) < 0.8 * coarse_loss(init_params(), held)
     x_bj = asm.solve_device(precond="block_jacobi").clone()
     its_bj = asm.report.iterations
     asm.solve_device(precond=LearnedPreconditioner(asm, init_params()))
-    its_tr = asm.report.iterations
+    its_untrained = asm.report.iterations
     x_nn = asm.solve_device(precond=LearnedPreconditioner(asm, params))
     its_nn = asm.report.iterations
     assert asm.report.converged
     assert rel_err(x_nn.cpu().numpy(), x_bj.cpu().numpy()) < 1e-8
-    assert its_nn < its_bj and its_nn <= its_tr, (its_nn, its_tr, its_bj, tr.history)
+    assert its_nn < its_untrained < its_bj, (its_nn, its_untrained, its_bj, tr.history)
