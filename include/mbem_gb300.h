@@ -288,11 +288,15 @@ int mbem_nn_backward(const float* feat, int64_t n_items, const float* params, co
 /* One Adam step (step >= 1) on n parameters. */
 int mbem_nn_adam(float* params, const float* grad, float* m, float* v, int64_t n, float lr, float beta1,
                  float beta2, float eps, int step, void* stream);
-/* A Phi, A_c and A_c^-1 (Gauss-Jordan, partial pivoting) for a dense FP64 A;
- * MBEM_ERR_NUMERIC when A_c is singular. */
+/* A Phi, A_c and A_c^-1 (Gauss-Jordan, partial pivoting) for a dense FP64 A.
+ * shift (n_coarse, n_shift) device, or NULL: A_c += shift shift^T first, with
+ * shift = Phi^T Z for a calibrated operator whose null space Z (the rigid
+ * translations of the u-slots, A Z = 0) the coarse space contains; the
+ * solution on the complement of Z is unchanged. MBEM_ERR_NUMERIC when A_c is
+ * singular. */
 size_t mbem_nn_setup_workspace_size(int64_t n_coarse);
-int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, void* work, size_t work_bytes,
-                        void* stream);
+int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift,
+                        int n_shift, void* work, size_t work_bytes, void* stream);
 /* z = M^-1 r (r, z distinct device vectors of length n). */
 size_t mbem_nn_apply_workspace_size(int64_t n, int64_t n_coarse);
 int mbem_nn_apply(const mbem_nn_precond* nn, const double* r, double* z, void* stream);

@@ -380,6 +380,18 @@ nn_coarse_matrix_kernel(const double* __restrict__ APhi, int64_t n_coarse, const
     for (int k = 0; k < 6; k++) Ac[(NCV * c + k) * n_coarse + q] = s[k];
 }
 
+// Ac[p, q] += sum_j U[p, j] U[q, j]: the rank-n_shift shift that makes the
+// coarse operator of a calibrated (singular) system invertible
+__global__ void nn_coarse_shift_kernel(double* __restrict__ Ac, int64_t nc, const double* __restrict__ U,
+                                       int n_shift) {
+    const int64_t p = blockIdx.y;
+    const int64_t q = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (q >= nc) return;
+    double s = 0.0;
+    for (int j = 0; j < n_shift; j++) s += U[p * n_shift + j] * U[q * n_shift + j];
+    Ac[p * nc + q] += s;
+}
+
 // Gauss-Jordan step k on M (m x m, FP64, in place): pivot search, row swap,
 // scaling of the pivot row; one CTA
 __global__ void __launch_bounds__(256)
@@ -593,8 +605,8 @@ size_t mbem_nn_setup_workspace_size(int64_t n_coarse) {
     return (size_t)(2 * n_coarse + 8) * sizeof(double) + (size_t)(n_coarse + 8) * sizeof(int);
 }
 
-int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, void* work, size_t work_bytes,
-                        void* stream) {
+int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift,
+                        int n_shift, void* work, size_t work_bytes, void* stream) {
     int e = nn_check(nn);
     if (e) return e;
     MBEM_REQUIRE(A != nullptr && ld >= nn->n, MBEM_ERR_ARG, "bad dense operator");
@@ -613,6 +625,12 @@ int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, 
     nn_coarse_matrix_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(nc, 256)), 256, 0, st>>>(
         APhi, nc, bj->chunk_ptr, bj->dofs, nn->phi, Ac);
     if ((e = launch_status("nn_coarse_setup", 2))) return e;
+    MBEM_REQUIRE(n_shift >= 0 && (n_shift == 0 || shift != nullptr), MBEM_ERR_ARG, "bad coarse shift");
+    if (n_shift > 0) {
+        nn_coarse_shift_kernel<<<dim3((unsigned)ceil_div(nc, 256), (unsigned)nc), 256, 0, st>>>(Ac, nc, shift,
+                                                                                            n_shift);
+        if ((e = launch_status("nn_coarse_shift_kernel"))) return e;
+    }
     // A_c^-1 in place
     double* rowk = static_cast<double*>(work);
     double* fcol = rowk + nc;

@@ -168,9 +168,28 @@ class LearnedPreconditioner:
         need = nat.lib().mbem_nn_setup_workspace_size(nc)
         setup_work = torch.empty(need, dtype=torch.uint8, device=dev)
         A = asm.A
-        nat.call("mbem_nn_setup_dense", ptr(A), A.stride(0), ctypes.byref(self._struct), ptr(setup_work), need,
-                 stream_handle())
+        shift = self._null_shift(asm)
+        nat.call("mbem_nn_setup_dense", ptr(A), A.stride(0), ctypes.byref(self._struct),
+                 ptr(shift) if shift is not None else None, 0 if shift is None else shift.shape[1],
+                 ptr(setup_work), need, stream_handle())
         self.built = True
+
+    def _null_shift(self, asm):
+        """Phi^T Z (n_coarse, 3) for the deflated translations Z of a
+        calibrated all-Neumann system (A Z = 0), else None."""
+        if not asm.deflate:
+            return None
+        from ..backends.dense import translation_basis
+        Z = translation_basis(asm.layout)
+        if Z.shape[1] == 0:
+            return None
+        phi = self.phi.double().cpu().numpy().reshape(-1, 3, 3)
+        U = np.zeros((6 * self.bj.n_chunks, Z.shape[1]))
+        for c, nodes in enumerate(self.bj.chunk_nodes()):
+            Zc = Z[(3 * nodes[:, None] + np.arange(3)).ravel()].reshape(len(nodes), 3, -1)   # (m, 3, j)
+            U[6 * c:6 * c + 3] = Zc.sum(0)
+            U[6 * c + 3:6 * c + 6] = np.einsum("mak,maj->kj", phi[nodes], Zc)
+        return torch.from_numpy(U).to(self.phi.device)
 
     def struct(self):
         return self._struct

@@ -89,8 +89,9 @@ def loss_and_grad(feat, params, chunks, eps):
     return loss, np.concatenate([g.ravel() for g in grads])
 
 
-def two_level_apply(A, chunks, phi, bj_solve, r):
-    """z = Phi y + BJ (r - A Phi y), y = (Phi^T A Phi)^-1 Phi^T r (dense)."""
+def two_level_apply(A, chunks, phi, bj_solve, r, Z=None):
+    """z = Phi y + BJ (r - A Phi y), y = (Phi^T (A + Z Z^T) Phi)^-1 Phi^T r
+    (dense); Z: the null space of a calibrated A (A Z = 0), or None."""
     phi = np.asarray(phi, float).reshape(-1, 3, 3)
     n3 = A.shape[0]
     Phi = np.zeros((n3, 6 * len(chunks)))
@@ -99,5 +100,8 @@ def two_level_apply(A, chunks, phi, bj_solve, r):
             Phi[3 * nodes + a, 6 * c + a] = 1.0
             Phi[3 * nodes + a, 6 * c + 3:6 * c + 6] = phi[nodes, a, :]
     AP = A @ Phi
-    y = np.linalg.solve(Phi.T @ AP, Phi.T @ r)
+    Ac = Phi.T @ AP
+    if Z is not None:
+        Ac = Ac + (Phi.T @ Z) @ (Z.T @ Phi)
+    y = np.linalg.solve(Ac, Phi.T @ r)
     return Phi @ y + bj_solve(r - AP @ y)
