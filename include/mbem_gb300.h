@@ -263,7 +263,8 @@ typedef struct {
     int64_t n;                       /* unknowns (a multiple of 3) */
     int64_t n_coarse;                /* 6 x the block-Jacobi chunks */
     const mbem_block_jacobi* bj;     /* chunks and their inverses (host pointer; chunk_of required) */
-    const float* phi;                /* (n/3, 3, 3) device: coarse blocks per node (mbem_nn_forward) */
+    const float* basis;              /* (n, 6) device: the coarse basis row of every unknown, Phi[d, 6 c(d) + k]
+                                        (the [I | phi_i] blocks, orthonormalised per chunk) */
     const double* APhi;              /* (n, n_coarse) device: A Phi, written by mbem_nn_setup_dense */
     const double* Ac_inv;            /* (n_coarse, n_coarse) device: A_c^-1, written by the setup */
     double* work;                    /* mbem_nn_apply_workspace_size() bytes, device */

@@ -67,7 +67,7 @@ BJ_MAX_DOF = 225
 
 
 class NnPrecond(Structure):
-    _fields_ = [("n", c_int64), ("n_coarse", c_int64), ("bj", POINTER(BlockJacobi)), ("phi", c_void_p),
+    _fields_ = [("n", c_int64), ("n_coarse", c_int64), ("bj", POINTER(BlockJacobi)), ("basis", c_void_p),
                 ("APhi", c_void_p), ("Ac_inv", c_void_p), ("work", c_void_p)]
 
 

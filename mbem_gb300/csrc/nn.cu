@@ -10,8 +10,10 @@
 //
 //   y = A_c^-1 Phi^T r,   z = Phi y + BJ (r - (A Phi) y).
 //
-// Setup per mesh: phi (MLP forward), A Phi (one pass over A), A_c, and A_c^-1
-// by Gauss-Jordan with partial pivoting (FP64). An apply is five small
+// Setup per mesh: phi (MLP forward), the chunk bases orthonormalised (the
+// span is what matters; an orthonormal basis keeps A_c as well conditioned
+// as A), A Phi (one pass over A), A_c, and A_c^-1 by Gauss-Jordan with
+// partial pivoting (FP64). An apply is five small
 // kernels plus the block-Jacobi apply; it never touches A.
 //
 // Training: the coarse space should hold what block-Jacobi misses, the error
@@ -312,72 +314,58 @@ constexpr int APHI_ROWS = 64;     // rows of A per CTA
 // (chunk, 64-row tile), a warp per row, lanes along the chunk's columns
 __global__ void __launch_bounds__(256)
 nn_aphi_kernel(const double* __restrict__ A, int64_t ld, int64_t n, const int64_t* __restrict__ chunk_ptr,
-               const int64_t* __restrict__ dofs, const float* __restrict__ phi, int64_t n_coarse,
+               const int64_t* __restrict__ dofs, const float* __restrict__ basis, int64_t n_coarse,
                double* __restrict__ APhi) {
     __shared__ int64_t col[MBEM_BJ_MAX_DOF];
-    __shared__ float ph[MBEM_BJ_MAX_DOF][3];
-    __shared__ int comp[MBEM_BJ_MAX_DOF];
+    __shared__ float bs[MBEM_BJ_MAX_DOF][NCV];
     const int c = blockIdx.x;
     const int64_t c0 = chunk_ptr[c];
     const int m = (int)(chunk_ptr[c + 1] - c0);
     for (int t = threadIdx.x; t < m; t += 256) {
         const int64_t d = dofs[c0 + t];
         col[t] = d;
-        const int64_t node = d / 3;
-        const int a = (int)(d % 3);
-        comp[t] = a;
-        ph[t][0] = phi[node * 9 + 3 * a];
-        ph[t][1] = phi[node * 9 + 3 * a + 1];
-        ph[t][2] = phi[node * 9 + 3 * a + 2];
+#pragma unroll
+        for (int k = 0; k < NCV; k++) bs[t][k] = basis[d * NCV + k];
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t r0 = (int64_t)blockIdx.y * APHI_ROWS;
     for (int64_t r = r0 + warp; r < lmin(n, r0 + APHI_ROWS); r += 8) {
         const double* Ar = A + r * ld;
-        double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        double s[NCV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         for (int t = lane; t < m; t += 32) {
             const double v = Ar[col[t]];
-            const int a = comp[t];
-            s[0] += (a == 0) ? v : 0.0;
-            s[1] += (a == 1) ? v : 0.0;
-            s[2] += (a == 2) ? v : 0.0;
-            s[3] += v * (double)ph[t][0];
-            s[4] += v * (double)ph[t][1];
-            s[5] += v * (double)ph[t][2];
+#pragma unroll
+            for (int k = 0; k < NCV; k++) s[k] += v * (double)bs[t][k];
         }
 #pragma unroll
-        for (int k = 0; k < 6; k++)
+        for (int k = 0; k < NCV; k++)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
         if (lane == 0)
 #pragma unroll
-            for (int k = 0; k < 6; k++) APhi[r * n_coarse + NCV * c + k] = s[k];
+            for (int k = 0; k < NCV; k++) APhi[r * n_coarse + NCV * c + k] = s[k];
     }
 }
 
-// Ac[6c + k, q] = sum_{i in c} sum_a B_i[a][k] APhi[3i + a, q]: a CTA per
-// (chunk, 256 columns), a thread per column
+// Ac[6c + k, q] = sum_{d in c} basis[d][k] APhi[d, q]: a CTA per (chunk,
+// 256 columns), a thread per column
 __global__ void __launch_bounds__(256)
 nn_coarse_matrix_kernel(const double* __restrict__ APhi, int64_t n_coarse, const int64_t* __restrict__ chunk_ptr,
-                        const int64_t* __restrict__ dofs, const float* __restrict__ phi, double* __restrict__ Ac) {
+                        const int64_t* __restrict__ dofs, const float* __restrict__ basis, double* __restrict__ Ac) {
     const int c = blockIdx.x;
     const int64_t q = (int64_t)blockIdx.y * 256 + threadIdx.x;
     if (q >= n_coarse) return;
     const int64_t c0 = chunk_ptr[c];
     const int m = (int)(chunk_ptr[c + 1] - c0);
-    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    double s[NCV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int t = 0; t < m; t++) {
         const int64_t d = dofs[c0 + t];
-        const int64_t node = d / 3;
-        const int a = (int)(d % 3);
         const double v = APhi[d * n_coarse + q];
-        s[a] += v;
-        s[3] += (double)phi[node * 9 + 3 * a] * v;
-        s[4] += (double)phi[node * 9 + 3 * a + 1] * v;
-        s[5] += (double)phi[node * 9 + 3 * a + 2] * v;
+#pragma unroll
+        for (int k = 0; k < NCV; k++) s[k] += (double)basis[d * NCV + k] * v;
     }
-    for (int k = 0; k < 6; k++) Ac[(NCV * c + k) * n_coarse + q] = s[k];
+    for (int k = 0; k < NCV; k++) Ac[(NCV * c + k) * n_coarse + q] = s[k];
 }
 
 // Ac[p, q] += sum_j U[p, j] U[q, j]: the rank-n_shift shift that makes the
@@ -470,42 +458,38 @@ __global__ void gj_swap_columns_kernel(double* __restrict__ M, int64_t m, const 
 // ---------------------------------------------------------------------------
 // apply pieces
 // ---------------------------------------------------------------------------
-// q[6c + k] = sum_{i in c} sum_a B_i[a][k] r[3i + a]; a CTA per chunk
+// q[6c + k] = sum_{d in c} basis[d][k] r[d]; a CTA per chunk
 __global__ void __launch_bounds__(128)
 nn_phit_kernel(const int64_t* __restrict__ chunk_ptr, const int64_t* __restrict__ dofs,
-               const float* __restrict__ phi, const double* __restrict__ r, double* __restrict__ q) {
+               const float* __restrict__ basis, const double* __restrict__ r, double* __restrict__ q) {
     __shared__ double red[4];
     const int c = blockIdx.x;
     const int64_t c0 = chunk_ptr[c];
     const int m = (int)(chunk_ptr[c + 1] - c0);
-    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    double s[NCV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int t = threadIdx.x; t < m; t += 128) {
         const int64_t d = dofs[c0 + t];
-        const int64_t node = d / 3;
-        const int a = (int)(d % 3);
         const double v = r[d];
-        s[a] += v;
-        s[3] += (double)phi[node * 9 + 3 * a] * v;
-        s[4] += (double)phi[node * 9 + 3 * a + 1] * v;
-        s[5] += (double)phi[node * 9 + 3 * a + 2] * v;
+#pragma unroll
+        for (int k = 0; k < NCV; k++) s[k] += (double)basis[d * NCV + k] * v;
     }
-    for (int k = 0; k < 6; k++) {
+    for (int k = 0; k < NCV; k++) {
         const double tot = block_sum(s[k], red);
         if (threadIdx.x == 0) q[NCV * c + k] = tot;
     }
 }
 
-// z[d] += y[6c + a] + sum_k phi_i[a][k] y[6c + 3 + k] for d = 3i + a in chunk c
+// z[d] += sum_k basis[d][k] y[6 c(d) + k]
 __global__ void __launch_bounds__(256)
-nn_phi_add_kernel(int64_t n, const int32_t* __restrict__ chunk_of, const float* __restrict__ phi,
+nn_phi_add_kernel(int64_t n, const int32_t* __restrict__ chunk_of, const float* __restrict__ basis,
                   const double* __restrict__ y, double* __restrict__ z) {
     const int64_t d = (int64_t)blockIdx.x * 256 + threadIdx.x;
     if (d >= n) return;
-    const int64_t node = d / 3;
-    const int a = (int)(d % 3);
     const double* yc = y + NCV * (int64_t)chunk_of[d];
-    z[d] += yc[a] + ((double)phi[node * 9 + 3 * a] * yc[3] + (double)phi[node * 9 + 3 * a + 1] * yc[4] +
-                     (double)phi[node * 9 + 3 * a + 2] * yc[5]);
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < NCV; k++) s += (double)basis[d * NCV + k] * yc[k];
+    z[d] += s;
 }
 
 static int nn_check(const mbem_nn_precond* nn) {
@@ -513,7 +497,7 @@ static int nn_check(const mbem_nn_precond* nn) {
     MBEM_REQUIRE(nn->n == nn->bj->n && nn->n_coarse == NCV * nn->bj->n_chunks && nn->n % 3 == 0, MBEM_ERR_ARG,
                  "learned preconditioner sizes (n=%lld, coarse=%lld, chunks=%lld)", (long long)nn->n,
                  (long long)nn->n_coarse, (long long)nn->bj->n_chunks);
-    MBEM_REQUIRE(nn->n == 0 || (nn->phi && nn->APhi && nn->Ac_inv && nn->work && nn->bj->chunk_of), MBEM_ERR_ARG,
+    MBEM_REQUIRE(nn->n == 0 || (nn->basis && nn->APhi && nn->Ac_inv && nn->work && nn->bj->chunk_of), MBEM_ERR_ARG,
                  "NULL learned preconditioner arrays");
     return MBEM_OK;
 }
@@ -529,13 +513,13 @@ int nn_precond_apply(const void* state, const double* r, double* z, cudaStream_t
     double* y = q + nc;            // nc: A_c^-1 q
     MBEM_REQUIRE(z != t && r != t, MBEM_ERR_ARG, "r/z alias the learned preconditioner's scratch");
     const mbem_block_jacobi* bj = nn->bj;
-    nn_phit_kernel<<<(unsigned)bj->n_chunks, 128, 0, st>>>(bj->chunk_ptr, bj->dofs, nn->phi, r, q);
+    nn_phit_kernel<<<(unsigned)bj->n_chunks, 128, 0, st>>>(bj->chunk_ptr, bj->dofs, nn->basis, r, q);
     if ((e = launch_status("nn_phit_kernel"))) return e;
     if ((e = dgemv(nn->Ac_inv, nc, nc, nc, q, 1.0, 0.0, y, st))) return e;
     cudaMemcpyAsync(t, r, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
     if ((e = dgemv(nn->APhi, nc, n, nc, y, -1.0, 1.0, t, st))) return e;
     if ((e = bj_apply(bj, t, z, st))) return e;
-    nn_phi_add_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(n, bj->chunk_of, nn->phi, y, z);
+    nn_phi_add_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(n, bj->chunk_of, nn->basis, y, z);
     return launch_status("nn_phi_add_kernel");
 }
 
@@ -621,9 +605,9 @@ int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, 
     double* APhi = const_cast<double*>(nn->APhi);
     double* Ac = const_cast<double*>(nn->Ac_inv);
     nn_aphi_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(n, APHI_ROWS)), 256, 0, st>>>(
-        A, ld, n, bj->chunk_ptr, bj->dofs, nn->phi, nc, APhi);
+        A, ld, n, bj->chunk_ptr, bj->dofs, nn->basis, nc, APhi);
     nn_coarse_matrix_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(nc, 256)), 256, 0, st>>>(
-        APhi, nc, bj->chunk_ptr, bj->dofs, nn->phi, Ac);
+        APhi, nc, bj->chunk_ptr, bj->dofs, nn->basis, Ac);
     if ((e = launch_status("nn_coarse_setup", 2))) return e;
     MBEM_REQUIRE(n_shift >= 0 && (n_shift == 0 || shift != nullptr), MBEM_ERR_ARG, "bad coarse shift");
     if (n_shift > 0) {

@@ -158,12 +158,13 @@ class LearnedPreconditioner:
         self.params = torch.as_tensor(np.asarray(params, np.float32)).to(dev)
         self.feat = torch.from_numpy(node_features(asm.layout, self.bj.chunk_nodes())).to(dev)
         self.phi = mlp_forward(self.feat, self.params)
+        self.basis = torch.from_numpy(self._orthonormal_basis()).to(dev)
         self.APhi = torch.empty((n, nc), dtype=torch.float64, device=dev)
         self.Ac_inv = torch.empty((nc, nc), dtype=torch.float64, device=dev)
         self.work = torch.empty(nat.lib().mbem_nn_apply_workspace_size(n, nc) // 8, dtype=torch.float64,
                                 device=dev)
         self._bj_struct = self.bj.struct()
-        self._struct = nat.NnPrecond(n=n, n_coarse=nc, bj=ctypes.pointer(self._bj_struct), phi=ptr(self.phi),
+        self._struct = nat.NnPrecond(n=n, n_coarse=nc, bj=ctypes.pointer(self._bj_struct), basis=ptr(self.basis),
                                      APhi=ptr(self.APhi), Ac_inv=ptr(self.Ac_inv), work=ptr(self.work))
         need = nat.lib().mbem_nn_setup_workspace_size(nc)
         setup_work = torch.empty(need, dtype=torch.uint8, device=dev)
@@ -174,6 +175,18 @@ class LearnedPreconditioner:
                  ptr(setup_work), need, stream_handle())
         self.built = True
 
+    def _orthonormal_basis(self) -> np.ndarray:
+        """(n, 6) FP32: per chunk, the rows [I | phi_i] of its nodes made
+        orthonormal (QR); the span, which is what the coarse correction
+        depends on, is unchanged."""
+        phi = self.phi.double().cpu().numpy().reshape(-1, 3, 3)
+        B = np.zeros((self.bj.n, 6))
+        for nodes in self.bj.chunk_nodes():
+            Bc = np.concatenate([np.broadcast_to(np.eye(3), (len(nodes), 3, 3)), phi[nodes]], axis=2).reshape(-1, 6)
+            Q, _ = np.linalg.qr(Bc)
+            B[(3 * nodes[:, None] + np.arange(3)).ravel()] = Q
+        return np.ascontiguousarray(B, dtype=np.float32)
+
     def _null_shift(self, asm):
         """Phi^T Z (n_coarse, 3) for the deflated translations Z of a
         calibrated all-Neumann system (A Z = 0), else None."""
@@ -183,12 +196,11 @@ class LearnedPreconditioner:
         Z = translation_basis(asm.layout)
         if Z.shape[1] == 0:
             return None
-        phi = self.phi.double().cpu().numpy().reshape(-1, 3, 3)
+        B = self.basis.double().cpu().numpy()
         U = np.zeros((6 * self.bj.n_chunks, Z.shape[1]))
         for c, nodes in enumerate(self.bj.chunk_nodes()):
-            Zc = Z[(3 * nodes[:, None] + np.arange(3)).ravel()].reshape(len(nodes), 3, -1)   # (m, 3, j)
-            U[6 * c:6 * c + 3] = Zc.sum(0)
-            U[6 * c + 3:6 * c + 6] = np.einsum("mak,maj->kj", phi[nodes], Zc)
+            d = (3 * nodes[:, None] + np.arange(3)).ravel()
+            U[6 * c:6 * c + 6] = B[d].T @ Z[d]
         return torch.from_numpy(U).to(self.phi.device)
 
     def struct(self):
