@@ -302,6 +302,18 @@ int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, 
 size_t mbem_nn_apply_workspace_size(int64_t n, int64_t n_coarse);
 int mbem_nn_apply(const mbem_nn_precond* nn, const double* r, double* z, void* stream);
 
+/* ---- many right-hand sides on the tensor cores: Y (M x n_rhs, FP32, at ldy)
+ * = A (M x K, BF16 row-major at lda) X, with X passed transposed as Xt
+ * (n_rhs x K, BF16 row-major at ldx), n_rhs <= 256; tcgen05.mma with TMA
+ * operand staging and FP32 accumulation in tensor memory. The product of
+ * the multi-RHS refinement (la/lu.py:210) and of batched FGMRES. lda and ldx
+ * multiples of 8, bases 16-byte aligned. mbem_gemm_bf16_check synchronises
+ * the stream and returns MBEM_ERR_WAIT if a pipeline wait of an earlier GEMM
+ * gave up. --------------------------------------------------------------- */
+int mbem_gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K, int n_rhs,
+                   float* Y, int64_t ldy, void* stream);
+int mbem_gemm_bf16_check(void* stream);
+
 /* ---- deflated FGMRES on a dense operator (la/solver.py:115-245 fgmres,
  * wired as backends/hmat.py:678-690: P A P y = P b, P = I - Z Z^T with Z
  * the rigid-translation basis of backends/dense.py:190-208). ---------- */

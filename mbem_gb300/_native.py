@@ -100,6 +100,8 @@ _SIGNATURES = {
     "mbem_dgemv": (c_int, [_P, _I, _I, _I, _P, _D, _D, _P, _P]),
     "mbem_dgemm_multi": (c_int, [_P, _I, _I, _I, _P, _I, _P, _P]),
     "mbem_project_translation": (c_int, [_P, _P, _I, _P, c_int, _P, _P]),
+    "mbem_gemm_bf16": (c_int, [_P, _I, _P, _I, _I, _I, c_int, _P, _I, _P]),
+    "mbem_gemm_bf16_check": (c_int, [_P]),
     "mbem_bj_inverse_bytes": (c_size_t, [_I, c_int]),
     "mbem_bj_build_dense": (c_int, [_P, _I, POINTER(BlockJacobi), _P]),
     "mbem_bj_build_mixed": (c_int, [POINTER(MixedOperator), POINTER(BlockJacobi), _P]),

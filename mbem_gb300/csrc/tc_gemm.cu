@@ -1,0 +1,262 @@
+// Multi-RHS product Y = A X on the 5th-generation tensor cores (sm_103a):
+// BF16 operands staged by TMA into 128-byte-swizzled shared memory,
+// tcgen05.mma (kind::f16, FP32 accumulation) into tensor memory, read back
+// with tcgen05.ld. It serves the many-right-hand-side solves, where the
+// matvec of FGMRES becomes a true GEMM (N x N times N x n_rhs).
+//
+// Layout: A (M x K) row-major BF16 (K-major), X given transposed as
+// Xt (NR x K) row-major BF16 (K-major too), Y (M x NR) row-major FP32.
+// One CTA owns a 128-row block of Y and all NR <= 256 columns, so it reads
+// its rows of A once; Xt (a few MB) is shared through L2.
+//
+// Warp roles (6 warps): warps 0-3 read the accumulator (warp w owns TMEM
+// lanes 32w..32w+31 = rows 32w..), warp 4 issues the TMA loads, warp 5
+// allocates TMEM and issues the MMAs. A 4-stage ring of (A, B) tiles with
+// full/empty mbarriers; tcgen05.commit releases a stage when its MMAs have
+// read it. Every wait is bounded: on a timeout the kernel records an error
+// and carries on without waiting, so it always ends.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "common.cuh"
+#include "tma_pipe.cuh"
+
+namespace mbem {
+
+constexpr int TC_BM = 128;            // rows per CTA (the MMA's M)
+constexpr int TC_BK = 64;             // K per stage: one 128-byte swizzle row of BF16
+constexpr int TC_STAGES = 4;
+constexpr int TC_THREADS = 192;
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+
+__device__ int g_tc_error;
+
+// tcgen05 shared-memory matrix descriptor, K-major operand with 128-byte
+// swizzle: start address, leading-dimension offset (unused for this layout),
+// stride between 8-row groups (1024 bytes), descriptor version 1, swizzle
+// mode 2 (128B).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(16u >> 4) << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t f16_idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cta.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_addr(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+template <int BN>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
+               int64_t K, float* __restrict__ Y, int64_t ldy, int n_cols) {
+    static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "MMA N for M = 128");
+    constexpr int A_BYTES = TC_BM * TC_BK * 2;
+    constexpr int B_BYTES = BN * TC_BK * 2;
+    constexpr int STAGE = A_BYTES + B_BYTES;
+    constexpr uint32_t TMEM_COLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+    extern __shared__ __align__(1024) uint8_t tc_smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], accum;
+    __shared__ uint32_t tmem_base;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t m0 = (int64_t)blockIdx.x * TC_BM;
+    const int kb_total = (int)((K + TC_BK - 1) / TC_BK);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(&accum, 1);
+        mbar_init_fence();
+    }
+    if (warp == 5) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 4 && lane == 0) {
+        // producer
+        for (int kb = 0; kb < kb_total; kb++) {
+            const int s = kb % TC_STAGES;
+            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+            if (!mbar_wait(&empty[s], ph ^ 1u, TC_WAIT_LIMIT)) atomicExch(&g_tc_error, 1);
+            uint8_t* st = smem + s * STAGE;
+            mbar_arrive_expect_tx(&full[s], STAGE);
+            tma_load_2d(st, &mapA, kb * TC_BK, (int)m0, &full[s]);
+            tma_load_2d(st + A_BYTES, &mapB, kb * TC_BK, 0, &full[s]);
+        }
+        // the last copies have landed before the CTA can end
+        for (int kb = (kb_total > TC_STAGES ? kb_total - TC_STAGES : 0); kb < kb_total; kb++)
+            if (!mbar_wait(&full[kb % TC_STAGES], (uint32_t)(kb / TC_STAGES) & 1u, TC_WAIT_LIMIT))
+                atomicExch(&g_tc_error, 1);
+    } else if (warp == 5 && lane == 0) {
+        // MMA issuer
+        constexpr uint32_t idesc = f16_idesc(TC_BM, BN);
+        for (int kb = 0; kb < kb_total; kb++) {
+            const int s = kb % TC_STAGES;
+            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+            if (!mbar_wait(&full[s], ph, TC_WAIT_LIMIT)) atomicExch(&g_tc_error, 1);
+            tc_fence_after();
+            const uint32_t a0 = smem_addr(smem + s * STAGE), b0 = a0 + A_BYTES;
+#pragma unroll
+            for (int k = 0; k < TC_BK / 16; k++) {
+                const uint64_t ad = sw128_desc(a0 + k * 32), bd = sw128_desc(b0 + k * 32);
+                const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&empty[s]))
+                         : "memory");
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_addr(&accum))
+                     : "memory");
+    } else if (warp < 4) {
+        // epilogue: row m0 + 32 warp + lane, BN columns from TMEM
+        if (!mbar_wait(&accum, 0u, TC_WAIT_LIMIT)) atomicExch(&g_tc_error, 1);
+        tc_fence_after();
+        const int64_t row = m0 + 32 * warp + lane;
+        float* yr = Y + row * ldy;
+#pragma unroll 1
+        for (int c = 0; c < BN; c += 16) {
+            uint32_t v[16];
+            const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(ta));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row < M) {
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    if (c + j < n_cols) yr[c + j] = __uint_as_float(v[j]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 5) {
+        // every MMA has completed (the epilogue waited for the final commit)
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host: tensor maps through the driver entry point (no libcuda link)
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+static std::mutex g_encode_mutex;
+
+static int get_encode() {
+    std::lock_guard<std::mutex> lock(g_encode_mutex);
+    if (g_encode) return MBEM_OK;
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || fn == nullptr)
+        return set_error(MBEM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    return MBEM_OK;
+}
+
+// BF16 row-major (rows x cols) at ld elements, box (64 cols x box_rows), 128B swizzle
+static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int64_t ld, int box_rows) {
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+    const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(MBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return MBEM_OK;
+}
+
+template <int BN>
+static int launch_tc(const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int64_t K, float* Y, int64_t ldy,
+                     int n_cols, cudaStream_t st) {
+    const size_t smem = (size_t)TC_STAGES * (TC_BM * TC_BK * 2 + BN * TC_BK * 2) + 1024;
+    cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    tc_gemm_kernel<BN><<<(unsigned)ceil_div(M, TC_BM), TC_THREADS, smem, st>>>(ma, mb, M, K, Y, ldy, n_cols);
+    return launch_status("tc_gemm_kernel");
+}
+
+int tc_gemm_check(cudaStream_t st) {
+    int err = 0;
+    cudaMemcpyFromSymbolAsync(&err, g_tc_error, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("tc_gemm sync", 0);
+    if (err) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(int));
+        return set_error(MBEM_ERR_WAIT, "a tensor-core GEMM pipeline wait ran out");
+    }
+    return MBEM_OK;
+}
+
+}  // namespace mbem
+
+using namespace mbem;
+
+extern "C" int mbem_gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K,
+                              int n_rhs, float* Y, int64_t ldy, void* stream) {
+    MBEM_REQUIRE(M >= 0 && K >= 1 && n_rhs >= 1 && n_rhs <= 256, MBEM_ERR_ARG,
+                 "bad GEMM sizes (M=%lld, K=%lld, n_rhs=%d; n_rhs <= 256)", (long long)M, (long long)K, n_rhs);
+    MBEM_REQUIRE(A && Xt && Y && lda >= K && ldx >= K && ldy >= n_rhs, MBEM_ERR_ARG, "bad GEMM pointers/strides");
+    MBEM_REQUIRE(lda % 8 == 0 && ldx % 8 == 0 && (uintptr_t)A % 16 == 0 && (uintptr_t)Xt % 16 == 0, MBEM_ERR_ARG,
+                 "TMA needs 16-byte aligned bases and row strides (lda, ldx multiples of 8)");
+    if (M == 0) return MBEM_OK;
+    int e = get_encode();
+    if (e) return e;
+    const int bn = n_rhs <= 16 ? 16 : (n_rhs <= 32 ? 32 : (n_rhs <= 64 ? 64 : (n_rhs <= 128 ? 128 : 256)));
+    CUtensorMap ma, mb;
+    if ((e = make_map(&ma, A, M, K, lda, TC_BM))) return e;
+    if ((e = make_map(&mb, Xt, n_rhs, K, ldx, bn))) return e;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (bn) {
+        case 16: return launch_tc<16>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        case 32: return launch_tc<32>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        case 64: return launch_tc<64>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        case 128: return launch_tc<128>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        case 256: return launch_tc<256>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        default: break;
+    }
+    return set_error(MBEM_ERR_UNSUPPORTED, "no GEMM tile for %d right-hand sides", bn);
+}
+
+extern "C" int mbem_gemm_bf16_check(void* stream) { return tc_gemm_check((cudaStream_t)stream); }
