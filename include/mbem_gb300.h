@@ -312,7 +312,40 @@ int mbem_nn_apply(const mbem_nn_precond* nn, const double* r, double* z, void* s
  * gave up. --------------------------------------------------------------- */
 int mbem_gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K, int n_rhs,
                    float* Y, int64_t ldy, void* stream);
+/* The same product written transposed: Yt (n_rhs x M) at ldy, one row per
+ * right-hand side (the layout of the batched solver's vectors). */
+int mbem_gemm_bf16_t(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K, int n_rhs,
+                     float* Yt, int64_t ldy, void* stream);
 int mbem_gemm_bf16_check(void* stream);
+
+/* ---- batched GMRES for a block of k right-hand sides (k Krylov iterations
+ * sharing one GEMM per step; la/solver.py:115-245 per right-hand side).
+ * Vectors are RHS-major (k, n) row-major; a Krylov basis V is (n_vec, k, n)
+ * FP32; Hessenberg columns H are (n_vec, k) FP64. ----------------------- */
+/* BF16 copy out (rows x cols at ldo) of an FP32 (is_f64 = 0) or FP64 matrix,
+ * and of a mixed operator (FP32 far field plus its near blocks). */
+int mbem_to_bf16(const void* A, int is_f64, int64_t lda, int64_t rows, int64_t cols, uint16_t* out, int64_t ldo,
+                 void* stream);
+int mbem_mixed_to_bf16(const mbem_mixed_operator* op, uint16_t* out, int64_t ldo, void* stream);
+/* H[i, r] = V[i, r] . W[r] */
+int mbem_batch_dots(const float* V, int n_vec, const float* W, int64_t k, int64_t n, double* H, void* stream);
+/* W[r] += alpha sum_i H[i, r] V[i, r] */
+int mbem_batch_axpy(float* W, const float* V, int n_vec, const double* H, double alpha, int64_t k, int64_t n,
+                    void* stream);
+/* norms[r] = |W[r]|, V[r] = W[r] / norms[r], Vbf (NULL or (k, n) BF16) its copy; W FP32 or FP64 */
+int mbem_batch_normalize(const void* W, int w_is_f64, int64_t k, int64_t n, double* norms, float* V, uint16_t* Vbf,
+                         void* stream);
+/* X[r] += sum_i Y[i, r] V[i, r] (X FP64) */
+int mbem_batch_update(double* X, const float* V, int n_vec, const double* Y, int64_t k, int64_t n, void* stream);
+/* X[r] = P X[r]: the rigid translations of the u-ranges removed (FP32 or FP64 X) */
+int mbem_batch_project(void* X, int is_f64, int64_t k, int64_t n, const int64_t* u_ranges, int n_u_ranges,
+                       void* stream);
+/* R = B - A X for the mixed operator and k right-hand sides (k, n) FP64: the
+ * far field with FP32 entries and double-float accumulation, the near blocks
+ * in FP64. */
+size_t mbem_batch_residual_workspace_size(int64_t k, int64_t n);
+int mbem_batch_residual_mixed(const mbem_mixed_operator* op, const double* B, const double* X, int64_t k, double* R,
+                              void* work, size_t work_bytes, void* stream);
 
 /* ---- deflated FGMRES on a dense operator (la/solver.py:115-245 fgmres,
  * wired as backends/hmat.py:678-690: P A P y = P b, P = I - Z Z^T with Z

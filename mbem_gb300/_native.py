@@ -102,6 +102,16 @@ _SIGNATURES = {
     "mbem_project_translation": (c_int, [_P, _P, _I, _P, c_int, _P, _P]),
     "mbem_gemm_bf16": (c_int, [_P, _I, _P, _I, _I, _I, c_int, _P, _I, _P]),
     "mbem_gemm_bf16_check": (c_int, [_P]),
+    "mbem_gemm_bf16_t": (c_int, [_P, _I, _P, _I, _I, _I, c_int, _P, _I, _P]),
+    "mbem_to_bf16": (c_int, [_P, c_int, _I, _I, _I, _P, _I, _P]),
+    "mbem_mixed_to_bf16": (c_int, [POINTER(MixedOperator), _P, _I, _P]),
+    "mbem_batch_dots": (c_int, [_P, c_int, _P, _I, _I, _P, _P]),
+    "mbem_batch_axpy": (c_int, [_P, _P, c_int, _P, _D, _I, _I, _P]),
+    "mbem_batch_normalize": (c_int, [_P, c_int, _I, _I, _P, _P, _P, _P]),
+    "mbem_batch_update": (c_int, [_P, _P, c_int, _P, _I, _I, _P]),
+    "mbem_batch_project": (c_int, [_P, c_int, _I, _I, _P, c_int, _P]),
+    "mbem_batch_residual_workspace_size": (c_size_t, [_I, _I]),
+    "mbem_batch_residual_mixed": (c_int, [POINTER(MixedOperator), _P, _P, _I, _P, _P, c_size_t, _P]),
     "mbem_bj_inverse_bytes": (c_size_t, [_I, c_int]),
     "mbem_bj_build_dense": (c_int, [_P, _I, POINTER(BlockJacobi), _P]),
     "mbem_bj_build_mixed": (c_int, [POINTER(MixedOperator), POINTER(BlockJacobi), _P]),

@@ -57,3 +57,26 @@ __host__ __device__ inline int64_t lmax(int64_t a, int64_t b) { return a > b ? a
     do {                                                   \
         if (!(cond)) return mbem::set_error((code), __VA_ARGS__); \
     } while (0)
+
+namespace mbem {
+
+// The u-slot ranges (offset, length) whose rigid translations are deflated.
+struct URanges {
+    int64_t off[8];
+    int64_t len[8];
+    int n;
+};
+
+inline int make_ranges(const int64_t* r, int nr, URanges& ur) {
+    MBEM_REQUIRE(nr >= 0 && nr <= 8, MBEM_ERR_ARG, "at most 8 u-slot ranges (got %d)", nr);
+    ur.n = nr;
+    for (int q = 0; q < nr; q++) {
+        ur.off[q] = r[2 * q];
+        ur.len[q] = r[2 * q + 1];
+        MBEM_REQUIRE(ur.off[q] >= 0 && ur.len[q] >= 0 && ur.len[q] % 3 == 0, MBEM_ERR_ARG,
+                     "bad u-slot range (%lld, %lld)", (long long)ur.off[q], (long long)ur.len[q]);
+    }
+    return MBEM_OK;
+}
+
+}  // namespace mbem

@@ -273,12 +273,6 @@ __global__ void axpby_kernel(double* __restrict__ y, const double* __restrict__ 
 // ---------------------------------------------------------------------------
 // deflation projection: subtract, per component, the mean over the u-slots
 // ---------------------------------------------------------------------------
-struct URanges {
-    int64_t off[8];
-    int64_t len[8];
-    int n;
-};
-
 // Two passes over the whole grid: per-block partial sums of each component
 // over the u-slots (fixed block count, fixed order), then every block forms
 // the three means from the partials and subtracts them from its entries.
@@ -341,17 +335,6 @@ static int project(const double* vin, double* vout, int64_t n, const URanges& ur
     return launch_status("project", 2);
 }
 
-static int make_ranges(const int64_t* r, int nr, URanges& ur) {
-    MBEM_REQUIRE(nr >= 0 && nr <= 8, MBEM_ERR_ARG, "at most 8 u-slot ranges (got %d)", nr);
-    ur.n = nr;
-    for (int q = 0; q < nr; q++) {
-        ur.off[q] = r[2 * q];
-        ur.len[q] = r[2 * q + 1];
-        MBEM_REQUIRE(ur.off[q] >= 0 && ur.len[q] >= 0 && ur.len[q] % 3 == 0, MBEM_ERR_ARG,
-                     "bad u-slot range (%lld, %lld)", (long long)ur.off[q], (long long)ur.len[q]);
-    }
-    return MBEM_OK;
-}
 
 // ---------------------------------------------------------------------------
 // FGMRES (la/solver.py:115-245) with classical Gram-Schmidt applied twice

@@ -64,7 +64,7 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-template <int BN>
+template <int BN, bool TRANS>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
                int64_t K, float* __restrict__ Y, int64_t ldy, int n_cols) {
@@ -148,7 +148,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
         if (!mbar_wait(&accum, 0u, TC_WAIT_LIMIT)) atomicExch(&g_tc_error, 1);
         tc_fence_after();
         const int64_t row = m0 + 32 * warp + lane;
-        float* yr = Y + row * ldy;
+        float* yr = TRANS ? Y + row : Y + row * ldy;   // Y^T: element (row, c) at c ldy + row
 #pragma unroll 1
         for (int c = 0; c < BN; c += 16) {
             uint32_t v[16];
@@ -164,7 +164,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
             if (row < M) {
 #pragma unroll
                 for (int j = 0; j < 16; j++)
-                    if (c + j < n_cols) yr[c + j] = __uint_as_float(v[j]);
+                    if (c + j < n_cols) yr[TRANS ? (int64_t)(c + j) * ldy : (c + j)] = __uint_as_float(v[j]);
             }
         }
     }
@@ -208,13 +208,27 @@ static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t co
     return MBEM_OK;
 }
 
-template <int BN>
+template <int BN, bool TRANS>
 static int launch_tc(const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int64_t K, float* Y, int64_t ldy,
                      int n_cols, cudaStream_t st) {
     const size_t smem = (size_t)TC_STAGES * (TC_BM * TC_BK * 2 + BN * TC_BK * 2) + 1024;
-    cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    tc_gemm_kernel<BN><<<(unsigned)ceil_div(M, TC_BM), TC_THREADS, smem, st>>>(ma, mb, M, K, Y, ldy, n_cols);
+    cudaFuncSetAttribute(tc_gemm_kernel<BN, TRANS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    tc_gemm_kernel<BN, TRANS><<<(unsigned)ceil_div(M, TC_BM), TC_THREADS, smem, st>>>(ma, mb, M, K, Y, ldy, n_cols);
     return launch_status("tc_gemm_kernel");
+}
+
+template <bool TRANS>
+static int launch_bn(int bn, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int64_t K, float* Y,
+                     int64_t ldy, int n_rhs, cudaStream_t st) {
+    switch (bn) {
+        case 16: return launch_tc<16, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        case 32: return launch_tc<32, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        case 64: return launch_tc<64, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        case 128: return launch_tc<128, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        case 256: return launch_tc<256, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        default: break;
+    }
+    return set_error(MBEM_ERR_UNSUPPORTED, "no GEMM tile for %d right-hand sides", bn);
 }
 
 int tc_gemm_check(cudaStream_t st) {
@@ -229,15 +243,12 @@ int tc_gemm_check(cudaStream_t st) {
     return MBEM_OK;
 }
 
-}  // namespace mbem
-
-using namespace mbem;
-
-extern "C" int mbem_gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K,
-                              int n_rhs, float* Y, int64_t ldy, void* stream) {
+static int gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K, int n_rhs,
+                     float* Y, int64_t ldy, bool trans, cudaStream_t st) {
     MBEM_REQUIRE(M >= 0 && K >= 1 && n_rhs >= 1 && n_rhs <= 256, MBEM_ERR_ARG,
                  "bad GEMM sizes (M=%lld, K=%lld, n_rhs=%d; n_rhs <= 256)", (long long)M, (long long)K, n_rhs);
-    MBEM_REQUIRE(A && Xt && Y && lda >= K && ldx >= K && ldy >= n_rhs, MBEM_ERR_ARG, "bad GEMM pointers/strides");
+    MBEM_REQUIRE(A && Xt && Y && lda >= K && ldx >= K && ldy >= (trans ? M : n_rhs), MBEM_ERR_ARG,
+                 "bad GEMM pointers/strides");
     MBEM_REQUIRE(lda % 8 == 0 && ldx % 8 == 0 && (uintptr_t)A % 16 == 0 && (uintptr_t)Xt % 16 == 0, MBEM_ERR_ARG,
                  "TMA needs 16-byte aligned bases and row strides (lda, ldx multiples of 8)");
     if (M == 0) return MBEM_OK;
@@ -247,16 +258,27 @@ extern "C" int mbem_gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_
     CUtensorMap ma, mb;
     if ((e = make_map(&ma, A, M, K, lda, TC_BM))) return e;
     if ((e = make_map(&mb, Xt, n_rhs, K, ldx, bn))) return e;
-    cudaStream_t st = (cudaStream_t)stream;
-    switch (bn) {
-        case 16: return launch_tc<16>(ma, mb, M, K, Y, ldy, n_rhs, st);
-        case 32: return launch_tc<32>(ma, mb, M, K, Y, ldy, n_rhs, st);
-        case 64: return launch_tc<64>(ma, mb, M, K, Y, ldy, n_rhs, st);
-        case 128: return launch_tc<128>(ma, mb, M, K, Y, ldy, n_rhs, st);
-        case 256: return launch_tc<256>(ma, mb, M, K, Y, ldy, n_rhs, st);
-        default: break;
-    }
-    return set_error(MBEM_ERR_UNSUPPORTED, "no GEMM tile for %d right-hand sides", bn);
+    return trans ? launch_bn<true>(bn, ma, mb, M, K, Y, ldy, n_rhs, st)
+                 : launch_bn<false>(bn, ma, mb, M, K, Y, ldy, n_rhs, st);
+}
+
+int tc_gemm(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K, int n_rhs, float* Y,
+            int64_t ldy, bool trans, cudaStream_t st) {
+    return gemm_bf16(A, lda, Xt, ldx, M, K, n_rhs, Y, ldy, trans, st);
+}
+
+}  // namespace mbem
+
+using namespace mbem;
+
+extern "C" int mbem_gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K,
+                              int n_rhs, float* Y, int64_t ldy, void* stream) {
+    return gemm_bf16(A, lda, Xt, ldx, M, K, n_rhs, Y, ldy, false, (cudaStream_t)stream);
+}
+
+extern "C" int mbem_gemm_bf16_t(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K,
+                                int n_rhs, float* Yt, int64_t ldy, void* stream) {
+    return gemm_bf16(A, lda, Xt, ldx, M, K, n_rhs, Yt, ldy, true, (cudaStream_t)stream);
 }
 
 extern "C" int mbem_gemm_bf16_check(void* stream) { return tc_gemm_check((cudaStream_t)stream); }

@@ -37,3 +37,201 @@ def gemm_bf16(A: torch.Tensor, Xt: torch.Tensor, out: torch.Tensor | None = None
 def gemm_check():
     """Synchronises and raises if a tensor-core pipeline wait gave up."""
     nat.call("mbem_gemm_bf16_check", stream_handle())
+
+
+def gemm_bf16_t(A: torch.Tensor, Xt: torch.Tensor, K: int, out: torch.Tensor) -> torch.Tensor:
+    """out (n, M) FP32 = (A[:, :K] @ Xt[:, :K]^T)^T, out's rows at out.stride(0)."""
+    M = A.shape[0]
+    n = Xt.shape[0]
+    nat.call("mbem_gemm_bf16_t", ptr(A), A.stride(0), ptr(Xt), Xt.stride(0), M, K, n, ptr(out), out.stride(0),
+             stream_handle())
+    return out
+
+
+# ---------------------------------------------------------------------------
+# a block of right-hand sides: batched GMRES on the BF16 tensor-core
+# operator inside FP64-accurate iterative refinement
+# ---------------------------------------------------------------------------
+import ctypes  # noqa: E402
+from dataclasses import dataclass, field  # noqa: E402
+
+import numpy as np  # noqa: E402
+
+
+@dataclass
+class BlockReport:
+    converged: bool
+    outer: int                        # refinement steps
+    inner_iterations: list = field(default_factory=list)   # batched GMRES iterations per step
+    true_relres: np.ndarray = None    # per right-hand side |b - A x| / |b|
+    gemm_ms: float = 0.0
+
+    def __str__(self):
+        worst = float(np.max(self.true_relres)) if self.true_relres is not None else float("nan")
+        return (f"block solve {'converged' if self.converged else 'NOT CONVERGED'}: {self.outer} refinement steps, "
+                f"inner {self.inner_iterations}, worst relres {worst:.3e}")
+
+
+def _pad8(n: int) -> int:
+    return (n + 7) // 8 * 8
+
+
+class BlockSolver:
+    """Solves A X = B for up to 256 right-hand sides at once.
+
+    The refinement loop computes the residual R = P (B - A X) with the
+    accurate operator (the mixed operator's FP32 far field with double-float
+    accumulation and its FP64 near blocks, or the FP64 dense matrix), and
+    corrects X by batched GMRES on the BF16 copy of the operator, whose
+    every step is one tensor-core GEMM over the whole block. P removes the
+    rigid translations of the u-slots of a deflated system."""
+
+    def __init__(self, asm, inner_restart: int = 30, inner_rtol: float = 1e-3):
+        self.asm = asm
+        self.op = asm.op
+        self.A = asm.A
+        if self.op is None and self.A is None:
+            raise ValueError("the assembled system holds no operator")
+        dev = (self.A if self.A is not None else self.op.A32).device
+        self.device = dev
+        self.n = int(asm.b.shape[0])
+        self.ldp = _pad8(self.n)
+        self.A16 = torch.zeros((self.n, self.ldp), dtype=torch.bfloat16, device=dev)
+        st = stream_handle()
+        if self.op is not None:
+            s = self.op.struct()
+            nat.call("mbem_mixed_to_bf16", ctypes.byref(s), ptr(self.A16), self.ldp, st)
+        else:
+            nat.call("mbem_to_bf16", ptr(self.A), 1, self.A.stride(0), self.n, self.n, ptr(self.A16), self.ldp, st)
+        rng = np.ascontiguousarray(np.asarray(asm.u_ranges(), dtype=np.int64).reshape(-1))
+        self._ranges = rng
+        self.inner_restart = inner_restart
+        self.inner_rtol = inner_rtol
+
+    # -- pieces ---------------------------------------------------------
+    def project(self, X: torch.Tensor):
+        if self._ranges.size == 0:
+            return X
+        is64 = 1 if X.dtype == torch.float64 else 0
+        nat.call("mbem_batch_project", ptr(X), is64, X.shape[0], X.shape[1],
+                 self._ranges.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), len(self._ranges) // 2,
+                 stream_handle())
+        return X
+
+    def residual(self, B: torch.Tensor, X: torch.Tensor) -> torch.Tensor:
+        """P (B - A X) for (k, n) FP64 blocks with the accurate operator."""
+        k = B.shape[0]
+        R = torch.empty_like(B)
+        if self.op is not None:
+            need = nat.lib().mbem_batch_residual_workspace_size(k, self.n)
+            work = torch.empty(need // 8, dtype=torch.float64, device=self.device)
+            s = self.op.struct()
+            nat.call("mbem_batch_residual_mixed", ctypes.byref(s), ptr(B), ptr(X), k, ptr(R), ptr(work), need,
+                     stream_handle())
+        else:
+            Y = torch.empty((self.n, k), dtype=torch.float64, device=self.device)
+            Xc = X.T.contiguous()
+            nat.call("mbem_dgemm_multi", ptr(self.A), self.A.stride(0), self.n, self.n, ptr(Xc), k, ptr(Y),
+                     stream_handle())
+            R = B - Y.T
+        return self.project(R)
+
+    def inner_gmres(self, R: torch.Tensor, m: int, rtol: float):
+        """D (k, n) FP64 with |R - A16 D| small for every row, by batched
+        GMRES(m) on the BF16 operator; returns (D, iterations, gemm_ms)."""
+        k, n = R.shape
+        dev = self.device
+        st = stream_handle()
+        V = torch.empty((m + 1, k, n), dtype=torch.float32, device=dev)
+        Vbf = torch.zeros((k, self.ldp), dtype=torch.bfloat16, device=dev)
+        W = torch.empty((k, n), dtype=torch.float32, device=dev)
+        norms = torch.empty(k, dtype=torch.float64, device=dev)
+        Hd = torch.empty((m + 1, k), dtype=torch.float64, device=dev)
+        H2d = torch.empty((m + 1, k), dtype=torch.float64, device=dev)
+        Vb = Vbf if self.ldp == n else Vbf[:, :n]
+
+        def normalize(src, is64, j):
+            # V[j] = src / |src| (and its BF16 copy at row stride ldp)
+            nat.call("mbem_batch_normalize", ptr(src), is64, k, n, ptr(norms), ptr(V[j]),
+                     ptr(Vbf) if self.ldp == n else None, st)
+            if self.ldp != n:
+                Vbf[:, :n].copy_(V[j])           # row stride ldp: the GEMM's K-major operand
+            return norms.cpu().numpy().copy()
+
+        beta = normalize(R, 1, 0)
+        live = beta > 0
+        H = np.zeros((m + 1, m, k))
+        cs = np.zeros((m, k))
+        sn = np.zeros((m, k))
+        g = np.zeros((m + 1, k))
+        g[0] = beta
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        gemm_ms = 0.0
+        jdone = 0
+        for j in range(m):
+            ev0.record()
+            gemm_bf16_t(self.A16, Vbf, n, W)
+            ev1.record()
+            self.project(W)
+            nat.call("mbem_batch_dots", ptr(V), j + 1, ptr(W), k, n, ptr(Hd), st)
+            nat.call("mbem_batch_axpy", ptr(W), ptr(V), j + 1, ptr(Hd), -1.0, k, n, st)
+            nat.call("mbem_batch_dots", ptr(V), j + 1, ptr(W), k, n, ptr(H2d), st)
+            nat.call("mbem_batch_axpy", ptr(W), ptr(V), j + 1, ptr(H2d), -1.0, k, n, st)
+            hn = normalize(W, 0, j + 1)
+            h = (Hd[:j + 1] + H2d[:j + 1]).cpu().numpy()
+            gemm_ms += ev0.elapsed_time(ev1)
+            col = np.vstack([h, hn[None, :]])            # (j + 2, k)
+            for i in range(j):                           # accumulated rotations
+                a, b = col[i].copy(), col[i + 1].copy()
+                col[i] = cs[i] * a + sn[i] * b
+                col[i + 1] = -sn[i] * a + cs[i] * b
+            den = np.hypot(col[j], col[j + 1])
+            ok = den > 0
+            cs[j] = np.where(ok, np.abs(col[j]) / np.where(ok, den, 1.0), 1.0)
+            sgn = np.where(col[j] >= 0, 1.0, -1.0)
+            sn[j] = np.where(ok, sgn * col[j + 1] / np.where(ok, den, 1.0), 0.0)
+            col[j] = cs[j] * col[j] + sn[j] * col[j + 1]
+            col[j + 1] = 0.0
+            H[:j + 2, j] = col
+            g[j + 1] = -sn[j] * g[j]
+            g[j] = cs[j] * g[j]
+            jdone = j + 1
+            rel = np.where(live, np.abs(g[j + 1]) / np.where(live, beta, 1.0), 0.0)
+            if np.all(rel < rtol):
+                break
+        # back substitution per right-hand side
+        Y = np.zeros((jdone, k))
+        for i in range(jdone - 1, -1, -1):
+            s = g[i] - (H[i, i + 1:jdone].T * Y[i + 1:jdone].T).sum(axis=1) if i + 1 < jdone else g[i].copy()
+            d = H[i, i]
+            Y[i] = np.where(d != 0, s / np.where(d != 0, d, 1.0), 0.0)
+        D = torch.zeros((k, n), dtype=torch.float64, device=dev)
+        Yd = torch.from_numpy(np.ascontiguousarray(Y)).to(dev)
+        nat.call("mbem_batch_update", ptr(D), ptr(V), jdone, ptr(Yd), k, n, st)
+        return D, jdone, gemm_ms
+
+    # -- the solve ------------------------------------------------------
+    def solve(self, B: torch.Tensor, rtol: float = 1e-8, max_outer: int = 12):
+        """X (k, n) FP64 for B (k, n) FP64 on the device, and a BlockReport."""
+        B = self.project(B.to(dtype=torch.float64, device=self.device).contiguous().clone())
+        k = B.shape[0]
+        if not 1 <= k <= MAX_RHS:
+            raise ValueError(f"1..{MAX_RHS} right-hand sides per block (got {k})")
+        bnorm = torch.linalg.vector_norm(B, dim=1).cpu().numpy()
+        X = torch.zeros_like(B)
+        rep = BlockReport(converged=False, outer=0)
+        for outer in range(max_outer + 1):
+            R = self.residual(B, X)
+            rel = torch.linalg.vector_norm(R, dim=1).cpu().numpy() / np.where(bnorm > 0, bnorm, 1.0)
+            rep.true_relres = rel
+            if np.all(rel < rtol) or outer == max_outer:
+                rep.converged = bool(np.all(rel < rtol))
+                break
+            D, its, ms = self.inner_gmres(R, self.inner_restart, self.inner_rtol)
+            rep.inner_iterations.append(its)
+            rep.gemm_ms += ms
+            X += D
+            self.project(X)
+            rep.outer = outer + 1
+        gemm_check()
+        return X, rep
