@@ -59,3 +59,18 @@ def fault_traction_model(n_face: int, n_fault: int, dip_deg: float = 90.0, mu: f
     fault_p = Patch("fault", fault, BCType.FAULT_TRACTION, value=np.array([-drop * mu, 0.0, 0.0]))
     region = Region("body", mat, [cube_p], np.zeros(3), faults=[fault_p])
     return RegionModel([region]), (side / n_face) / 2.0
+
+
+def gaussian_slips(fault: Patch, n_rhs: int, length: float = 0.3, seed0: int = 0) -> np.ndarray:
+    """(n_rhs, n_dofs, 3) smooth random slip patterns on a fault's collocation
+    points: a Gaussian random field with squared-exponential covariance of
+    ``length`` and unit variance per component, Cholesky factor with 1e-10
+    jitter, one ``np.random.default_rng(seed0 + i)`` draw per pattern."""
+    pts = np.asarray(fault.collocation_points(), float)
+    d2 = ((pts[:, None, :] - pts[None, :, :]) ** 2).sum(-1)
+    C = np.exp(-0.5 * d2 / (length * length))
+    L = np.linalg.cholesky(C + 1e-10 * np.eye(pts.shape[0]))
+    out = np.empty((n_rhs, pts.shape[0], 3))
+    for i in range(n_rhs):
+        out[i] = L @ np.random.default_rng(seed0 + i).normal(size=(pts.shape[0], 3))
+    return out

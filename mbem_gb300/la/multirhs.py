@@ -235,3 +235,37 @@ class BlockSolver:
             rep.outer = outer + 1
         gemm_check()
         return X, rep
+
+
+def slip_rhs(asm, fault, slips) -> torch.Tensor:
+    """B (k, n) FP64: the right-hand sides of k slip patterns (k, n_dofs, 3)
+    on a prescribed-slip fault, every other datum of the system zero. Each
+    RHS term of the fault (equations.py:296-309: scale -sigma times the T
+    block) is assembled once in FP64 and applied to all patterns at once."""
+    from ..kernels import KERNEL_T
+    from ..kernels import basis as kb
+    from ..kernels import tri_nodal as tn
+    slips = np.asarray(slips, float)
+    k = slips.shape[0]
+    dev = asm.b.device
+    B = torch.zeros((k, asm.b.shape[0]), dtype=torch.float64, device=dev)
+    S = torch.from_numpy(np.ascontiguousarray(slips.reshape(k, -1).T)).to(dev)     # (3 n_src, k)
+    held = asm._arrays
+    if held is None:
+        asm._arrays = asm._arrays_in if asm._arrays_in is not None else {}
+    for rt in asm.system.rhs_terms:
+        if rt.source_patch is not fault:
+            continue
+        if rt.kernel != KERNEL_T:
+            raise NotImplementedError("slip right-hand sides through the T kernel only")
+        mat = asm.materials[rt.region.name]
+        f = asm._patch_arrays(rt.field_patch)
+        s = asm._patch_arrays(rt.source_patch)
+        c = kb.t_coeffs(mat.mu, mat.lam)
+        T = tn.t_matrix_direct(f["coll"], s["tv"], s["normals"], s["eps"], *c, order=rt.source_patch.order)
+        Y = torch.empty((T.shape[0], k), dtype=torch.float64, device=dev)
+        nat.call("mbem_dgemm_multi", ptr(T), T.stride(0), T.shape[0], T.shape[1], ptr(S), k, ptr(Y),
+                 stream_handle())
+        B[:, rt.row.offset:rt.row.stop] += rt.scale * Y.T
+    asm._arrays = held
+    return B

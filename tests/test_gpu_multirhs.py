@@ -113,3 +113,15 @@ def test_block_residual_mixed_matches_fp64(gpu):
     ref = B - (asm.op.dense64() @ X.T).T
     bs.project(ref)
     assert rel_err(R.cpu().numpy(), ref.cpu().numpy()) < 1e-13
+
+
+def test_slip_rhs_reproduces_the_system_rhs(gpu):
+    from mbem_gb300.cases import gaussian_slips
+    from mbem_gb300.la.multirhs import slip_rhs
+    asm = _cube("fp64")
+    fault = asm.system.model.regions[0].faults[0]
+    own = np.broadcast_to(fault.value_array().reshape(-1, 3), (fault.n_dofs, 3))[None]
+    slips = np.concatenate([own, gaussian_slips(fault, 3, seed0=4)])
+    B = slip_rhs(asm, fault, slips)
+    assert rel_err(B[0].cpu().numpy(), asm.b.cpu().numpy()) < 1e-13
+    assert slips.shape == (4, fault.n_dofs, 3) and np.all(np.abs(slips[1:].std(axis=(1, 2)) - 1.0) < 0.6)
