@@ -64,7 +64,9 @@ class BlockReport:
     outer: int                        # refinement steps
     inner_iterations: list = field(default_factory=list)   # batched GMRES iterations per step
     true_relres: np.ndarray = None    # per right-hand side |b - A x| / |b|
-    gemm_ms: float = 0.0
+    gemm_ms: float = 0.0              # tensor-core GEMM time
+    residual_ms: float = 0.0          # FP64-accurate residuals
+    inner_ms: float = 0.0             # batched GMRES (GEMM included)
 
     def __str__(self):
         worst = float(np.max(self.true_relres)) if self.true_relres is not None else float("nan")
@@ -86,7 +88,15 @@ class BlockSolver:
     every step is one tensor-core GEMM over the whole block. P removes the
     rigid translations of the u-slots of a deflated system."""
 
-    def __init__(self, asm, inner_restart: int = 30, inner_rtol: float = 1e-3):
+    def __init__(self, asm, inner_restart: int = 30, inner_rtol: float = 1e-3, terms: int = 3):
+        """``terms``: 1 = the operator in BF16 (relative error ~2^-9 per
+        product: about five refinement steps to 1e-8); 3 = A and the Krylov
+        vectors each split into BF16 high and low parts, A_hi V_hi + A_hi
+        V_lo + A_lo V_hi in one GEMM over a three-fold K (error ~2^-16: two
+        refinement steps)."""
+        if terms not in (1, 3):
+            raise ValueError("terms must be 1 or 3")
+        self.terms = terms
         self.asm = asm
         self.op = asm.op
         self.A = asm.A
@@ -94,15 +104,25 @@ class BlockSolver:
             raise ValueError("the assembled system holds no operator")
         dev = (self.A if self.A is not None else self.op.A32).device
         self.device = dev
-        self.n = int(asm.b.shape[0])
-        self.ldp = _pad8(self.n)
-        self.A16 = torch.zeros((self.n, self.ldp), dtype=torch.bfloat16, device=dev)
+        self.n = n = int(asm.b.shape[0])
+        self.ldp = _pad8(n)
+        # A16 = [A_hi | A_hi | A_lo] (terms 3) or A_hi, each block ldp wide
+        self.A16 = torch.zeros((n, terms * self.ldp), dtype=torch.bfloat16, device=dev)
+        hi = self.A16[:, :self.ldp]
         st = stream_handle()
         if self.op is not None:
             s = self.op.struct()
-            nat.call("mbem_mixed_to_bf16", ctypes.byref(s), ptr(self.A16), self.ldp, st)
+            nat.call("mbem_mixed_to_bf16", ctypes.byref(s), ptr(hi), self.A16.stride(0), st)
         else:
-            nat.call("mbem_to_bf16", ptr(self.A), 1, self.A.stride(0), self.n, self.n, ptr(self.A16), self.ldp, st)
+            nat.call("mbem_to_bf16", ptr(self.A), 1, self.A.stride(0), n, n, ptr(hi), self.A16.stride(0), st)
+        if terms == 3:
+            full = self.op.dense64() if self.op is not None else self.A
+            lo = (full - hi[:, :n].double())
+            del full
+            self.A16[:, self.ldp:self.ldp + n] = hi[:, :n]
+            nat.call("mbem_to_bf16", ptr(lo), 1, lo.stride(0), n, n, ptr(self.A16[:, 2 * self.ldp:]),
+                     self.A16.stride(0), st)
+            del lo
         rng = np.ascontiguousarray(np.asarray(asm.u_ranges(), dtype=np.int64).reshape(-1))
         self._ranges = rng
         self.inner_restart = inner_restart
@@ -143,19 +163,22 @@ class BlockSolver:
         dev = self.device
         st = stream_handle()
         V = torch.empty((m + 1, k, n), dtype=torch.float32, device=dev)
-        Vbf = torch.zeros((k, self.ldp), dtype=torch.bfloat16, device=dev)
+        Vbf = torch.zeros((k, self.terms * self.ldp), dtype=torch.bfloat16, device=dev)
+        ld = self.ldp
+        terms = self.terms
         W = torch.empty((k, n), dtype=torch.float32, device=dev)
         norms = torch.empty(k, dtype=torch.float64, device=dev)
         Hd = torch.empty((m + 1, k), dtype=torch.float64, device=dev)
         H2d = torch.empty((m + 1, k), dtype=torch.float64, device=dev)
-        Vb = Vbf if self.ldp == n else Vbf[:, :n]
 
         def normalize(src, is64, j):
-            # V[j] = src / |src| (and its BF16 copy at row stride ldp)
-            nat.call("mbem_batch_normalize", ptr(src), is64, k, n, ptr(norms), ptr(V[j]),
-                     ptr(Vbf) if self.ldp == n else None, st)
-            if self.ldp != n:
-                Vbf[:, :n].copy_(V[j])           # row stride ldp: the GEMM's K-major operand
+            # V[j] = src / |src|; the GEMM operand [V_hi | V_lo | V_hi] (or V_hi)
+            nat.call("mbem_batch_normalize", ptr(src), is64, k, n, ptr(norms), ptr(V[j]), None, st)
+            vh = V[j].to(torch.bfloat16)
+            Vbf[:, :n] = vh
+            if terms == 3:
+                Vbf[:, ld:ld + n] = (V[j] - vh.float()).to(torch.bfloat16)
+                Vbf[:, 2 * ld:2 * ld + n] = vh
             return norms.cpu().numpy().copy()
 
         beta = normalize(R, 1, 0)
@@ -170,7 +193,7 @@ class BlockSolver:
         jdone = 0
         for j in range(m):
             ev0.record()
-            gemm_bf16_t(self.A16, Vbf, n, W)
+            gemm_bf16_t(self.A16, Vbf, terms * ld, W)
             ev1.record()
             self.project(W)
             nat.call("mbem_batch_dots", ptr(V), j + 1, ptr(W), k, n, ptr(Hd), st)
@@ -220,14 +243,25 @@ class BlockSolver:
         bnorm = torch.linalg.vector_norm(B, dim=1).cpu().numpy()
         X = torch.zeros_like(B)
         rep = BlockReport(converged=False, outer=0)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        rep.residual_ms = 0.0
+        rep.inner_ms = 0.0
         for outer in range(max_outer + 1):
+            ev[0].record()
             R = self.residual(B, X)
+            ev[1].record()
+            ev[1].synchronize()
+            rep.residual_ms += ev[0].elapsed_time(ev[1])
             rel = torch.linalg.vector_norm(R, dim=1).cpu().numpy() / np.where(bnorm > 0, bnorm, 1.0)
             rep.true_relres = rel
             if np.all(rel < rtol) or outer == max_outer:
                 rep.converged = bool(np.all(rel < rtol))
                 break
+            ev[0].record()
             D, its, ms = self.inner_gmres(R, self.inner_restart, self.inner_rtol)
+            ev[1].record()
+            ev[1].synchronize()
+            rep.inner_ms += ev[0].elapsed_time(ev[1])
             rep.inner_iterations.append(its)
             rep.gemm_ms += ms
             X += D
