@@ -327,6 +327,12 @@ int mbem_gemm_bf16_check(void* stream);
 int mbem_to_bf16(const void* A, int is_f64, int64_t lda, int64_t rows, int64_t cols, uint16_t* out, int64_t ldo,
                  void* stream);
 int mbem_mixed_to_bf16(const mbem_mixed_operator* op, uint16_t* out, int64_t ldo, void* stream);
+/* The two-part split A = hi + lo (hi = bf16(A), lo = bf16(A - hi); about
+ * 2^-16 relative) of an FP32/FP64 matrix or of a mixed operator (lo may be
+ * NULL there: hi alone). */
+int mbem_to_bf16x2(const void* A, int is_f64, int64_t lda, int64_t rows, int64_t cols, uint16_t* hi, uint16_t* lo,
+                   int64_t ldo, void* stream);
+int mbem_mixed_to_bf16x2(const mbem_mixed_operator* op, uint16_t* hi, uint16_t* lo, int64_t ldo, void* stream);
 /* H[i, r] = V[i, r] . W[r] */
 int mbem_batch_dots(const float* V, int n_vec, const float* W, int64_t k, int64_t n, double* H, void* stream);
 /* W[r] += alpha sum_i H[i, r] V[i, r] */

@@ -105,6 +105,8 @@ _SIGNATURES = {
     "mbem_gemm_bf16_t": (c_int, [_P, _I, _P, _I, _I, _I, c_int, _P, _I, _P]),
     "mbem_to_bf16": (c_int, [_P, c_int, _I, _I, _I, _P, _I, _P]),
     "mbem_mixed_to_bf16": (c_int, [POINTER(MixedOperator), _P, _I, _P]),
+    "mbem_to_bf16x2": (c_int, [_P, c_int, _I, _I, _I, _P, _P, _I, _P]),
+    "mbem_mixed_to_bf16x2": (c_int, [POINTER(MixedOperator), _P, _P, _I, _P]),
     "mbem_batch_dots": (c_int, [_P, c_int, _P, _I, _I, _P, _P]),
     "mbem_batch_axpy": (c_int, [_P, _P, c_int, _P, _D, _I, _I, _P]),
     "mbem_batch_normalize": (c_int, [_P, c_int, _I, _I, _P, _P, _P, _P]),

@@ -51,6 +51,49 @@ __global__ void f64_to_bf16_kernel(const double* __restrict__ A, int64_t lda, in
         out[r * ldo + c] = to_bf16((float)A[r * lda + c]);
 }
 
+// hi = bf16(A), lo = bf16(A - hi): A = hi + lo to about 2^-16
+__global__ void f32_to_bf16x2_kernel(const float* __restrict__ A, int64_t lda, int64_t cols,
+                                     uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, int64_t ldo) {
+    const int64_t r = blockIdx.y;
+    for (int64_t c = (int64_t)blockIdx.x * BT + threadIdx.x; c < cols; c += (int64_t)gridDim.x * BT) {
+        const float v = A[r * lda + c];
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[r * ldo + c] = __bfloat16_as_ushort(h);
+        lo[r * ldo + c] = to_bf16(v - __bfloat162float(h));
+    }
+}
+
+__global__ void f64_to_bf16x2_kernel(const double* __restrict__ A, int64_t lda, int64_t cols,
+                                     uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, int64_t ldo) {
+    const int64_t r = blockIdx.y;
+    for (int64_t c = (int64_t)blockIdx.x * BT + threadIdx.x; c < cols; c += (int64_t)gridDim.x * BT) {
+        const double v = A[r * lda + c];
+        const __nv_bfloat16 h = __float2bfloat16_rn((float)v);
+        hi[r * ldo + c] = __bfloat16_as_ushort(h);
+        lo[r * ldo + c] = to_bf16((float)(v - (double)__bfloat162float(h)));
+    }
+}
+
+// the near 3x3 blocks of a mixed operator: hi (and lo, when given) of
+// A32 + near on their entries; one thread per field point
+__global__ void near_to_bf16x2_kernel(const float* __restrict__ A32, int64_t lda, mbem_near_blocks nb,
+                                      uint16_t* __restrict__ hi, uint16_t* __restrict__ lo, int64_t ldo) {
+    const int64_t f = (int64_t)blockIdx.x * BT + threadIdx.x;
+    if (f >= nb.n_field) return;
+    for (int64_t q = nb.rowptr[f]; q < nb.rowptr[f + 1]; q++) {
+        const int64_t c0 = nb.col0 + 3 * nb.cols[q];
+        for (int a = 0; a < 3; a++) {
+            const int64_t r = nb.row0 + 3 * f + a;
+            for (int b = 0; b < 3; b++) {
+                const double v = (double)A32[r * lda + c0 + b] + nb.vals[9 * q + 3 * a + b];
+                const __nv_bfloat16 h = __float2bfloat16_rn((float)v);
+                hi[r * ldo + c0 + b] = __bfloat16_as_ushort(h);
+                if (lo) lo[r * ldo + c0 + b] = to_bf16((float)(v - (double)__bfloat162float(h)));
+            }
+        }
+    }
+}
+
 // the near 3x3 blocks: out = bf16(A32 + near) on their entries; one thread
 // per (field point, near block)
 __global__ void near_to_bf16_kernel(const float* __restrict__ A32, int64_t lda, mbem_near_blocks nb,
@@ -158,7 +201,7 @@ batch_project_kernel(T* __restrict__ X, int64_t n, URanges ur) {
 // R = B - A X for a block: FP32 far field with double-float accumulation,
 // FP64 near blocks
 // ---------------------------------------------------------------------------
-constexpr int DF_ROWS = 32, DF_RHS = 32, DF_K = 32;
+constexpr int DF_ROWS = 64, DF_RHS = 64, DF_K = 16;
 
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
     const float t = __fadd_rn(hi, p);
@@ -168,51 +211,60 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float p) {
     lo = __fadd_rn(lo, e);
 }
 
-// Y[r, row] = sum_j A32[row, j] X[r, j]: a block per (32 rows, 32 RHS), a
-// thread per (2 rows, 2 RHS); every product a x_hi exact (TwoProd), a x_lo
+// Y[r, row] = sum_j A32[row, j] X[r, j]: a block per (64 rows, 64 RHS), a
+// thread per (4 rows, 4 RHS); every product a x_hi exact (TwoProd), a x_lo
 // rounded, sums in hi/lo pairs
 __global__ void __launch_bounds__(BT)
 df_gemm_kernel(const float* __restrict__ A, int64_t lda, int64_t n_rows, int64_t n_cols,
                const double* __restrict__ X, int64_t k, double* __restrict__ Y) {
-    __shared__ float As[DF_ROWS][DF_K + 1];
-    __shared__ float Xh[DF_RHS][DF_K + 1], Xl[DF_RHS][DF_K + 1];
+    __shared__ float As[DF_K][DF_ROWS + 4];
+    __shared__ float Xh[DF_K][DF_RHS + 4], Xl[DF_K][DF_RHS + 4];
     const int64_t row0 = (int64_t)blockIdx.x * DF_ROWS, rhs0 = (int64_t)blockIdx.y * DF_RHS;
-    const int tr = threadIdx.x % 16, tc = threadIdx.x / 16;    // rows 2tr, 2tr+1; RHS 2tc, 2tc+1
-    float hi[2][2] = {{0, 0}, {0, 0}}, lo[2][2] = {{0, 0}, {0, 0}};
+    const int tr = threadIdx.x % 16, tc = threadIdx.x / 16;    // rows tr + 16a, RHS tc + 16b
+    float hi[4][4], lo[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) hi[a][b] = lo[a][b] = 0.0f;
     for (int64_t j0 = 0; j0 < n_cols; j0 += DF_K) {
         for (int e = threadIdx.x; e < DF_ROWS * DF_K; e += BT) {
-            const int i = e / DF_K, j = e % DF_K;
+            const int i = e / DF_K, j = e % DF_K;      // i: row (and RHS) within the tile, j: column
             const int64_t gr = row0 + i, gc = j0 + j;
-            As[i][j] = (gr < n_rows && gc < n_cols) ? A[gr * lda + gc] : 0.0f;
+            As[j][i] = (gr < n_rows && gc < n_cols) ? A[gr * lda + gc] : 0.0f;
             const int64_t rr = rhs0 + i;
             const double xv = (rr < k && gc < n_cols) ? X[rr * n_cols + gc] : 0.0;
             const float xh = (float)xv;
-            Xh[i][j] = xh;
-            Xl[i][j] = (float)(xv - (double)xh);
+            Xh[j][i] = xh;
+            Xl[j][i] = (float)(xv - (double)xh);
         }
         __syncthreads();
 #pragma unroll 4
         for (int j = 0; j < DF_K; j++) {
+            float av[4], xh[4], xl[4];
 #pragma unroll
-            for (int a = 0; a < 2; a++) {
-                const float av = As[2 * tr + a][j];
+            for (int a = 0; a < 4; a++) av[a] = As[j][tr + 16 * a];
 #pragma unroll
-                for (int b = 0; b < 2; b++) {
-                    const float xh = Xh[2 * tc + b][j], xl = Xl[2 * tc + b][j];
-                    const float p = __fmul_rn(av, xh);
-                    const float err = __fmaf_rn(av, xh, -p);
-                    two_sum_acc(hi[a][b], lo[a][b], p);
-                    lo[a][b] = __fadd_rn(lo[a][b], __fmaf_rn(av, xl, err));
-                }
+            for (int b = 0; b < 4; b++) {
+                xh[b] = Xh[j][tc + 16 * b];
+                xl[b] = Xl[j][tc + 16 * b];
             }
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    const float p = __fmul_rn(av[a], xh[b]);
+                    const float err = __fmaf_rn(av[a], xh[b], -p);
+                    two_sum_acc(hi[a][b], lo[a][b], p);
+                    lo[a][b] = __fadd_rn(lo[a][b], __fmaf_rn(av[a], xl[b], err));
+                }
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int a = 0; a < 2; a++)
+    for (int a = 0; a < 4; a++)
 #pragma unroll
-        for (int b = 0; b < 2; b++) {
-            const int64_t gr = row0 + 2 * tr + a, rr = rhs0 + 2 * tc + b;
+        for (int b = 0; b < 4; b++) {
+            const int64_t gr = row0 + tr + 16 * a, rr = rhs0 + tc + 16 * b;
             if (gr < n_rows && rr < k) Y[rr * n_rows + gr] = (double)hi[a][b] + (double)lo[a][b];
         }
 }
@@ -264,6 +316,40 @@ int mbem_to_bf16(const void* A, int is_f64, int64_t lda, int64_t rows, int64_t c
         count_launches(1);
     }
     return launch_status("to_bf16", 0);
+}
+
+int mbem_to_bf16x2(const void* A, int is_f64, int64_t lda, int64_t rows, int64_t cols, uint16_t* hi, uint16_t* lo,
+                   int64_t ldo, void* stream) {
+    MBEM_REQUIRE(rows >= 0 && cols >= 0 && lda >= cols && ldo >= cols, MBEM_ERR_ARG, "bad BF16 split shape");
+    MBEM_REQUIRE(rows * cols == 0 || (A && hi && lo), MBEM_ERR_ARG, "NULL split pointers");
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int64_t r0 = 0; r0 < rows; r0 += 65535) {
+        const int64_t nr = lmin(65535, rows - r0);
+        const dim3 grid((unsigned)lmin(ceil_div(cols, BT), 64), (unsigned)nr);
+        if (is_f64)
+            f64_to_bf16x2_kernel<<<grid, BT, 0, st>>>((const double*)A + r0 * lda, lda, cols, hi + r0 * ldo,
+                                                     lo + r0 * ldo, ldo);
+        else
+            f32_to_bf16x2_kernel<<<grid, BT, 0, st>>>((const float*)A + r0 * lda, lda, cols, hi + r0 * ldo,
+                                                     lo + r0 * ldo, ldo);
+        count_launches(1);
+    }
+    return launch_status("to_bf16x2", 0);
+}
+
+int mbem_mixed_to_bf16x2(const mbem_mixed_operator* op, uint16_t* hi, uint16_t* lo, int64_t ldo, void* stream) {
+    MBEM_REQUIRE(op && op->A32 && hi && ldo >= op->n_cols, MBEM_ERR_ARG, "bad mixed operator or output");
+    int e = lo ? mbem_to_bf16x2(op->A32, 0, op->ld32, op->n_rows, op->n_cols, hi, lo, ldo, stream)
+               : mbem_to_bf16(op->A32, 0, op->ld32, op->n_rows, op->n_cols, hi, ldo, stream);
+    if (e) return e;
+    for (int t = 0; t < op->n_near; t++) {
+        const mbem_near_blocks& nb = op->near[t];
+        if (nb.n_field == 0) continue;
+        near_to_bf16x2_kernel<<<(unsigned)ceil_div(nb.n_field, BT), BT, 0, (cudaStream_t)stream>>>(op->A32, op->ld32,
+                                                                                                   nb, hi, lo, ldo);
+        if ((e = launch_status("near_to_bf16x2_kernel"))) return e;
+    }
+    return MBEM_OK;
 }
 
 int mbem_mixed_to_bf16(const mbem_mixed_operator* op, uint16_t* out, int64_t ldo, void* stream) {

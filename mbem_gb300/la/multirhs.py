@@ -109,20 +109,18 @@ class BlockSolver:
         # A16 = [A_hi | A_hi | A_lo] (terms 3) or A_hi, each block ldp wide
         self.A16 = torch.zeros((n, terms * self.ldp), dtype=torch.bfloat16, device=dev)
         hi = self.A16[:, :self.ldp]
+        lo = self.A16[:, 2 * self.ldp:] if terms == 3 else None
         st = stream_handle()
+        ld16 = self.A16.stride(0)
         if self.op is not None:
             s = self.op.struct()
-            nat.call("mbem_mixed_to_bf16", ctypes.byref(s), ptr(hi), self.A16.stride(0), st)
+            nat.call("mbem_mixed_to_bf16x2", ctypes.byref(s), ptr(hi), ptr(lo) if lo is not None else None, ld16, st)
+        elif lo is not None:
+            nat.call("mbem_to_bf16x2", ptr(self.A), 1, self.A.stride(0), n, n, ptr(hi), ptr(lo), ld16, st)
         else:
-            nat.call("mbem_to_bf16", ptr(self.A), 1, self.A.stride(0), n, n, ptr(hi), self.A16.stride(0), st)
+            nat.call("mbem_to_bf16", ptr(self.A), 1, self.A.stride(0), n, n, ptr(hi), ld16, st)
         if terms == 3:
-            full = self.op.dense64() if self.op is not None else self.A
-            lo = (full - hi[:, :n].double())
-            del full
             self.A16[:, self.ldp:self.ldp + n] = hi[:, :n]
-            nat.call("mbem_to_bf16", ptr(lo), 1, lo.stride(0), n, n, ptr(self.A16[:, 2 * self.ldp:]),
-                     self.A16.stride(0), st)
-            del lo
         rng = np.ascontiguousarray(np.asarray(asm.u_ranges(), dtype=np.int64).reshape(-1))
         self._ranges = rng
         self.inner_restart = inner_restart
@@ -248,7 +246,7 @@ class BlockSolver:
         rep.inner_ms = 0.0
         for outer in range(max_outer + 1):
             ev[0].record()
-            R = self.residual(B, X)
+            R = B.clone() if outer == 0 else self.residual(B, X)     # X = 0: R = P B
             ev[1].record()
             ev[1].synchronize()
             rep.residual_ms += ev[0].elapsed_time(ev[1])
