@@ -324,9 +324,154 @@ def run_ours(args, rank, ws):
     clocks = clk.summary()
     if clocks:
         line["clocks"] = clocks
+    if not args.skip_extra:
+        line["workloads"] = extra_workloads(args, peaks)
     if rank == 0 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(args, rep.iterations)
     return line
+
+
+def _sync_time(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def multi_rhs_workload(peaks, n_face=24, n_fault=16, n_rhs=256):
+    """Many right-hand sides (cube 24 x 24 per face, fault 16 x 16, 256 slip
+    patterns from a Gaussian random field): the mixed operator, its
+    three-term BF16 copy and the block solver (batched GMRES on the tcgen05
+    GEMM inside FP64-accurate refinement), against the plain FP64 path
+    solving the 256 systems one by one (FGMRES on the FP64 matrix)."""
+    import torch
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model, gaussian_slips
+    from mbem_gb300.la.multirhs import BlockSolver, gemm_bf16_t, slip_rhs
+    from mbem_gb300.model import generate_system
+    model, eps = cube_fault_model(n_face, n_fault)
+    system = generate_system(model)
+    fault = model.regions[0].faults[0]
+    slips = gaussian_slips(fault, n_rhs)
+    out = {"config": {"n_face": n_face, "n_fault": n_fault, "unknowns": system.layout.n_unknowns, "n_rhs": n_rhs,
+                      "slips": "Gaussian random field, length 0.3, unit variance, seeds 0..%d" % (n_rhs - 1)}}
+    mixed = DenseBackend(jump="calibrated", deflate=True, precision="mixed")
+    # warm-up pass, then the timed one
+    for timed in (False, True):
+        asm, t_asm = _sync_time(lambda: mixed.assemble(system, eps))
+        B, t_rhs = _sync_time(lambda: slip_rhs(asm, fault, slips))
+        bs, t_bf = _sync_time(lambda: BlockSolver(asm))
+        (X, rep), t_solve = _sync_time(lambda: bs.solve(B, rtol=RTOL))
+        if timed:
+            break
+        del bs, asm
+        torch.cuda.empty_cache()
+    total = t_asm + t_rhs + t_bf + t_solve
+    n = bs.n
+    Vbf = torch.randn((n_rhs, bs.A16.shape[1]), device="cuda").to(torch.bfloat16)
+    W = torch.empty((n_rhs, n), device="cuda")
+    K = bs.A16.shape[1]
+    for _ in range(3):
+        gemm_bf16_t(bs.A16, Vbf, K, W)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        gemm_bf16_t(bs.A16, Vbf, K, W)
+    e1.record()
+    torch.cuda.synchronize()
+    gemm_ms = e0.elapsed_time(e1) / 10
+    flops = 2.0 * n * K * n_rhs
+    bf16_peak = peaks.get("bf16_tflops") or 1900.0
+    out["mixed_block"] = {"s": total, "assembly_s": t_asm, "rhs_s": t_rhs, "bf16_copy_s": t_bf, "solve_s": t_solve,
+                          "refinement_steps": rep.outer, "inner_iterations": rep.inner_iterations,
+                          "worst_true_relres": float(np.max(rep.true_relres)), "gemm_ms_in_solve": rep.gemm_ms,
+                          "residual_ms_in_solve": rep.residual_ms}
+    out["roofline_gemm"] = {"kernel": "tc_gemm_kernel (tcgen05.mma kind::f16, TMA, TMEM)", "bound": "tensor",
+                            "achieved": flops / (gemm_ms / 1e3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                            "frac": flops / (gemm_ms / 1e3) / 1e12 / bf16_peak, "launch_ms": gemm_ms,
+                            "flops_per_launch": flops, "hbm_gbs_of_A": 2.0 * n * K / (gemm_ms / 1e3) / 1e9,
+                            "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)" if peaks.get("bf16_tflops")
+                            else "fallback 1.9 PFLOP/s (of fallback)"}
+    del bs, asm
+    torch.cuda.empty_cache()
+    # plain FP64: one FGMRES per right-hand side
+    fp64 = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART)
+    asm, t_asm = _sync_time(lambda: fp64.assemble(system, eps))
+    B, t_rhs = _sync_time(lambda: slip_rhs(asm, fault, slips))
+    its = []
+    diff = 0.0
+
+    def solve_all():
+        nonlocal diff
+        for r in range(n_rhs):
+            asm.b = B[r].clone()
+            x = asm.solve_device()
+            its.append(asm.report.iterations)
+            diff = max(diff, float(torch.linalg.vector_norm(x - X[r]) / torch.linalg.vector_norm(x)))
+    _, t_solve = _sync_time(solve_all)
+    t64 = t_asm + t_rhs + t_solve
+    out["fp64_one_by_one"] = {"s": t64, "assembly_s": t_asm, "rhs_s": t_rhs, "solve_s": t_solve,
+                              "mean_iterations": float(np.mean(its))}
+    out["speedup_vs_fp64"] = t64 / total
+    out["max_rel_diff_mixed_vs_fp64_solution"] = diff
+    del asm
+    torch.cuda.empty_cache()
+    return out
+
+
+def fault_traction_workload(n_face=32, n_fault=24, dip=90.0):
+    """The FAULT_TRACTION cube (32 x 32 per face, fault 24 x 24, uniform
+    shear drop 1e-3 mu): FGMRES with block-Jacobi, with the learned coarse
+    space (shipped parameters, trained on 12- and 16-per-face meshes), and
+    without a preconditioner."""
+    import torch
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import fault_traction_model
+    from mbem_gb300.la.learned import LearnedPreconditioner
+    from mbem_gb300.la.train_learned import load_default
+    from mbem_gb300.model import generate_system
+    model, eps = fault_traction_model(n_face, n_fault, dip)
+    system = generate_system(model)
+    params = load_default()
+    out = {"config": {"n_face": n_face, "n_fault": n_fault, "dip_deg": dip, "unknowns": system.layout.n_unknowns,
+                      "rtol": RTOL}}
+    backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART, maxiter=1000)
+    asm, t_asm = _sync_time(lambda: backend.assemble(system, eps))
+    out["assembly_s"] = t_asm
+    for name in ("block_jacobi", "learned", "block_jacobi", "learned"):     # second pass timed
+        asm._bj = None
+
+        def setup():
+            return "block_jacobi" if name == "block_jacobi" else LearnedPreconditioner(asm, params)
+
+        def bj_build():
+            asm.block_jacobi()
+        _, t_bj = _sync_time(bj_build)
+        pc, t_setup = _sync_time(setup)
+        _, t_solve = _sync_time(lambda: asm.solve_device(precond=pc))
+        out[name] = {"setup_s": t_bj + t_setup, "solve_s": t_solve, "iterations": asm.report.iterations,
+                     "true_relres": asm.report.true_relres, "converged": asm.report.converged,
+                     "time_to_solve_s": t_asm + t_bj + t_setup + t_solve}
+    _, t_plain = _sync_time(lambda: asm.solve_device(precond="none", maxiter=300))
+    out["none"] = {"solve_s": t_plain, "iterations": asm.report.iterations, "true_relres": asm.report.true_relres,
+                   "converged": asm.report.converged}
+    out["learned_vs_block_jacobi_time"] = out["block_jacobi"]["time_to_solve_s"] / out["learned"]["time_to_solve_s"]
+    del asm
+    torch.cuda.empty_cache()
+    return out
+
+
+def extra_workloads(args, peaks):
+    out = {}
+    for name, fn in (("multi_rhs_cube24_256", lambda: multi_rhs_workload(peaks)),
+                     ("fault_traction_cube32_learned", fault_traction_workload)):
+        try:
+            out[name] = fn()
+        except Exception as err:     # one workload failing must not hide the headline
+            out[name] = {"error": f"{type(err).__name__}: {err}"}
+    return out
 
 
 # DRAM bytes over algorithmic bytes of the mixed matvec, from the ncu capture
@@ -427,6 +572,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--skip-extra", action="store_true",
+                    help="skip the many-right-hand-side and FAULT_TRACTION workloads")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
