@@ -695,16 +695,15 @@ __device__ __forceinline__ void frame_rotate_sym(const NodalSrc& g, const double
 
 // stress (global, symmetric) per density d of node k: which 0 dd, 1 kelvin,
 // 2 eigen, 3 dd - eigen
-__device__ void node_stress(const NodalSrc& g, const double W[4][ND_MAXK][5][5], int k, double z,
-                            const double* nrm, const double* d, double eps, double mu, double lam, int which,
-                            double out[3][3]) {
+// stress (global, symmetric) per density d from a node's stress moments M
+// (I7 = M.M7[0][0]): which 0 dd, 1 kelvin, 2 eigen, 3 dd - eigen
+__device__ void moments_stress(const NodalSrc& g, const StressMoments& M, const double* nrm, const double* d,
+                               double eps, double mu, double lam, int which, double out[3][3]) {
     const double nu = lam / (2.0 * (lam + mu));
     const double C1 = 1.0 / (16.0 * MBEM_PI * mu * (1.0 - nu));
     const double c34 = 3.0 - 4.0 * nu;
     double loc[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     if (which != 2) {
-        StressMoments M;
-        node_smoments(W, k, z, M);
         double dl[3];
         frame_local(g, d, dl);
         if (which == 1) {
@@ -717,13 +716,84 @@ __device__ void node_stress(const NodalSrc& g, const double W[4][ND_MAXK][5][5],
     }
     frame_rotate_sym(g, loc, out);
     if (which >= 2) {
-        const double phi = (15.0 * eps * eps * eps * eps / (8.0 * MBEM_PI)) * W[3][k][0][0];
+        const double phi = (15.0 * eps * eps * eps * eps / (8.0 * MBEM_PI)) * M.M7[0][0];
         const double sgn = (which == 3) ? -1.0 : 1.0;
         const double nd = nrm[0] * d[0] + nrm[1] * d[1] + nrm[2] * d[2];
         for (int m = 0; m < 3; m++)
             for (int n = 0; n < 3; n++)
                 out[m][n] += sgn * phi * ((m == n ? lam * nd : 0.0) + mu * (d[m] * nrm[n] + d[n] * nrm[m]));
     }
+}
+
+__device__ void node_stress(const NodalSrc& g, const double W[4][ND_MAXK][5][5], int k, double z,
+                            const double* nrm, const double* d, double eps, double mu, double lam, int which,
+                            double out[3][3]) {
+    StressMoments M;
+    node_smoments(W, k, z, M);
+    moments_stress(g, M, nrm, d, eps, mu, lam, which, out);
+}
+
+// Far pairs of a P0 (one-node) density: the Gauss tables of the stress
+// moments held in registers (I3; M5 and M7 to the degrees the kernel needs),
+// the same sums as the general tables (tri_nodal.py:641-679) with N = 1.
+template <bool KELVIN>
+__device__ void far_moments_p0(const NodalSrc& g, double X1, double X2, double h2, int q0, int q1,
+                               StressMoments& M) {
+    constexpr int D5 = KELVIN ? 3 : 2;      // n = 5 degree: kelvin 3, dd 2
+    double I3 = 0.0, m3_10 = 0.0, m3_01 = 0.0;
+    double m5[D5 + 1][D5 + 1], m7[5][5];
+#pragma unroll
+    for (int a = 0; a <= D5; a++)
+#pragma unroll
+        for (int b = 0; b <= D5; b++) m5[a][b] = 0.0;
+#pragma unroll
+    for (int a = 0; a < 5; a++)
+#pragma unroll
+        for (int b = 0; b < 5; b++) m7[a][b] = 0.0;
+    for (int q = q0; q < q1; q++) {
+        const double l0 = c_rule_lam[q][0], l1 = c_rule_lam[q][1], l2 = c_rule_lam[q][2];
+        const double eta1 = l0 * g.p2d[0][0] + l1 * g.p2d[1][0] + l2 * g.p2d[2][0];
+        const double eta2 = l0 * g.p2d[0][1] + l1 * g.p2d[1][1] + l2 * g.p2d[2][1];
+        const double xi1 = eta1 - X1, xi2 = eta2 - X2;
+        const double R2 = xi1 * xi1 + xi2 * xi2 + h2;
+        const double wq = c_rule_w[q] * g.area2;
+        const double r2i = 1.0 / R2;
+        const double Rn1 = sqrt(r2i);
+        const double Rn3 = Rn1 * r2i, Rn5 = Rn3 * r2i, Rn7 = Rn5 * r2i;
+        double x1p[5], x2p[5];
+        x1p[0] = x2p[0] = 1.0;
+#pragma unroll
+        for (int a = 1; a < 5; a++) {
+            x1p[a] = x1p[a - 1] * xi1;
+            x2p[a] = x2p[a - 1] * xi2;
+        }
+        I3 += wq * Rn3;
+        if (KELVIN) {
+            m3_10 += wq * x1p[1] * x2p[0] * Rn3;
+            m3_01 += wq * x1p[0] * x2p[1] * Rn3;
+        }
+#pragma unroll
+        for (int a = 0; a <= D5; a++)
+#pragma unroll
+            for (int b = 0; a + b <= D5; b++) m5[a][b] += wq * x1p[a] * x2p[b] * Rn5;
+        if (!KELVIN) {
+#pragma unroll
+            for (int a = 0; a < 5; a++)
+#pragma unroll
+                for (int b = 0; a + b < 5; b++) m7[a][b] += wq * x1p[a] * x2p[b] * Rn7;
+        }
+    }
+    M.I3 = I3;
+    M.m3_10 = m3_10;
+    M.m3_01 = m3_01;
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) M.M5[a][b] = (a <= D5 && b <= D5) ? m5[a < D5 + 1 ? a : 0][b < D5 + 1 ? b : 0] : 0.0;
+#pragma unroll
+    for (int a = 0; a < 5; a++)
+#pragma unroll
+        for (int b = 0; b < 5; b++) M.M7[a][b] = m7[a][b];
 }
 
 // ---------------------------------------------------------------------------
@@ -896,9 +966,39 @@ nodal_traction_kernel(NodalArgs a, NodalSpec sp) {
     NodalSrc g;
     if (!nodal_frame(a.tri_verts + 9 * s, g)) return;
     const double eps = a.eps[s];
-    const double z = nodal_pair_tables(sp, g, a.x_field + 3 * f, eps, W, S);
     const double zero_n[3] = {0.0, 0.0, 0.0};
     const double* nrm = a.normals ? a.normals + 3 * s : zero_n;
+    if (K == 1) {
+        // one-node density: far pairs through the register tables
+        const double* x = a.x_field + 3 * f;
+        const double dx = x[0] - g.c[0], dy = x[1] - g.c[1], dz = x[2] - g.c[2];
+        const double D = sqrt((dx * dx + dy * dy + dz * dz) + eps * eps);
+        if (D > sp.d_star * g.L) {
+            const double z = dx * g.nh[0] + dy * g.nh[1] + dz * g.nh[2];
+            const double X1 = dx * g.ex[0] + dy * g.ex[1] + dz * g.ex[2];
+            const double X2 = dx * g.ey[0] + dy * g.ey[1] + dz * g.ey[2];
+            const double h2 = z * z + eps * eps;
+            const bool distant = D > sp.d_star_distant * g.L;
+            const int q0 = distant ? sp.q_split : 0, q1 = distant ? ND_Q : sp.q_split;
+            StressMoments M;
+            M.z = z;
+            if (sw == 1) far_moments_p0<true>(g, X1, X2, h2, q0, q1, M);
+            else far_moments_p0<false>(g, X1, X2, h2, q0, q1, M);
+            const int64_t id = a.ids[s];
+            if (id < 0 || id >= a.n_cols) return;
+            for (int j = 0; j < 3; j++) {
+                const double d[3] = {j == 0 ? 1.0 : 0.0, j == 1 ? 1.0 : 0.0, j == 2 ? 1.0 : 0.0};
+                double sg[3][3];
+                moments_stress(g, M, nrm, d, eps, a.mu, a.lam, sw, sg);
+                for (int i = 0; i < 3; i++) {
+                    const double t = nf[0] * sg[i][0] + nf[1] * sg[i][1] + nf[2] * sg[i][2];
+                    atomicAdd(&a.out[(3 * f + i) * a.ld + 3 * id + j], a.alpha * t);
+                }
+            }
+            return;
+        }
+    }
+    const double z = nodal_pair_tables(sp, g, a.x_field + 3 * f, eps, W, S);
     for (int k = 0; k < K; k++) {
         const int64_t id = a.ids[s * K + k];
         if (id < 0 || id >= a.n_cols) continue;        // outside the block: never written
