@@ -451,6 +451,8 @@ def fault_traction_workload(n_face=32, n_fault=24, dip=90.0):
         _, t_bj = _sync_time(bj_build)
         pc, t_setup = _sync_time(setup)
         _, t_solve = _sync_time(lambda: asm.solve_device(precond=pc))
+        if name == "learned":
+            out["learned_setup_parts_s"] = pc.setup_s
         out[name] = {"setup_s": t_bj + t_setup, "solve_s": t_solve, "iterations": asm.report.iterations,
                      "true_relres": asm.report.true_relres, "converged": asm.report.converged,
                      "time_to_solve_s": t_asm + t_bj + t_setup + t_solve}

@@ -289,6 +289,13 @@ int mbem_nn_backward(const float* feat, int64_t n_items, const float* params, co
 /* One Adam step (step >= 1) on n parameters. */
 int mbem_nn_adam(float* params, const float* grad, float* m, float* v, int64_t n, float lr, float beta1,
                  float beta2, float eps, int step, void* stream);
+/* basis (n, 6) FP32: every chunk's [I | phi_i] rows orthonormalised (the
+ * span is what the coarse correction depends on; an orthonormal basis keeps
+ * A_c as well conditioned as A), and U (n_coarse, 3) = basis^T Z for the
+ * rigid translations Z of the u-ranges (U may be NULL; with no u-range it
+ * is left untouched). */
+int mbem_nn_basis(const mbem_block_jacobi* bj, const float* phi, const int64_t* u_ranges, int n_u_ranges,
+                  float* basis, double* U, void* stream);
 /* A Phi, A_c and A_c^-1 (Gauss-Jordan, partial pivoting) for a dense FP64 A.
  * shift (n_coarse, n_shift) device, or NULL: A_c += shift shift^T first, with
  * shift = Phi^T Z for a calibrated operator whose null space Z (the rigid

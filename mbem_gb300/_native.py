@@ -124,6 +124,7 @@ _SIGNATURES = {
     "mbem_nn_backward": (c_int, [_P, _I, _P, _P, _P, _P, _P, c_size_t, _P]),
     "mbem_nn_adam": (c_int, [_P, _P, _P, _P, _I, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                              ctypes.c_float, c_int, _P]),
+    "mbem_nn_basis": (c_int, [POINTER(BlockJacobi), _P, _P, c_int, _P, _P, _P]),
     "mbem_nn_setup_workspace_size": (c_size_t, [_I]),
     "mbem_nn_setup_dense": (c_int, [_P, _I, POINTER(NnPrecond), _P, c_int, _P, c_size_t, _P]),
     "mbem_nn_apply_workspace_size": (c_size_t, [_I, _I]),

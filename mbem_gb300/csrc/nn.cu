@@ -492,6 +492,62 @@ nn_phi_add_kernel(int64_t n, const int32_t* __restrict__ chunk_of, const float* 
     z[d] += s;
 }
 
+// The coarse basis of every chunk: the 3m x 6 block [I | phi_i] over the
+// chunk's nodes orthonormalised by modified Gram-Schmidt (FP64 sums), and its
+// projection on the rigid translations of the u-ranges,
+// U[6c + k, j] = sum_{d in c, d in u, d % 3 = j} basis[d, k] / sqrt(u nodes).
+// A CTA of 128 threads per chunk, the chunk's rows in shared memory.
+__global__ void __launch_bounds__(128)
+nn_basis_kernel(const int64_t* __restrict__ chunk_ptr, const int64_t* __restrict__ dofs,
+                const float* __restrict__ phi, URanges ur, double inv_sqrt_u, float* __restrict__ basis,
+                double* __restrict__ U) {
+    __shared__ double Bs[MBEM_BJ_MAX_DOF][NCV];
+    __shared__ double red[4];
+    const int c = blockIdx.x;
+    const int64_t c0 = chunk_ptr[c];
+    const int m = (int)(chunk_ptr[c + 1] - c0);
+    for (int t = threadIdx.x; t < m; t += 128) {
+        const int64_t d = dofs[c0 + t];
+        const int64_t node = d / 3;
+        const int a = (int)(d % 3);
+        for (int k = 0; k < 3; k++) Bs[t][k] = (a == k) ? 1.0 : 0.0;
+        for (int k = 0; k < 3; k++) Bs[t][3 + k] = (double)phi[node * 9 + 3 * a + k];
+    }
+    __syncthreads();
+    for (int k = 0; k < NCV; k++) {
+        for (int p = 0; p < k; p++) {
+            double v = 0.0;
+            for (int t = threadIdx.x; t < m; t += 128) v += Bs[t][p] * Bs[t][k];
+            const double dot = block_sum(v, red);
+            for (int t = threadIdx.x; t < m; t += 128) Bs[t][k] -= dot * Bs[t][p];
+            __syncthreads();
+        }
+        double v = 0.0;
+        for (int t = threadIdx.x; t < m; t += 128) v += Bs[t][k] * Bs[t][k];
+        const double nrm = sqrt(block_sum(v, red));
+        const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+        for (int t = threadIdx.x; t < m; t += 128) Bs[t][k] *= inv;
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < m; t += 128) {
+        const int64_t d = dofs[c0 + t];
+        for (int k = 0; k < NCV; k++) basis[d * NCV + k] = (float)Bs[t][k];
+    }
+    if (U == nullptr) return;
+    for (int k = 0; k < NCV; k++)
+        for (int j = 0; j < 3; j++) {
+            double v = 0.0;
+            for (int t = threadIdx.x; t < m; t += 128) {
+                const int64_t d = dofs[c0 + t];
+                bool in_u = false;
+                for (int q = 0; q < ur.n; q++) in_u |= (d >= ur.off[q] && d < ur.off[q] + ur.len[q]);
+                if (in_u && d % 3 == j) v += (double)(float)Bs[t][k];
+            }
+            const double tot = block_sum(v, red);
+            if (threadIdx.x == 0) U[(NCV * c + k) * 3 + j] = tot * inv_sqrt_u;
+        }
+}
+
 static int nn_check(const mbem_nn_precond* nn) {
     MBEM_REQUIRE(nn != nullptr && nn->bj != nullptr, MBEM_ERR_ARG, "learned preconditioner descriptor is NULL");
     MBEM_REQUIRE(nn->n == nn->bj->n && nn->n_coarse == NCV * nn->bj->n_chunks && nn->n % 3 == 0, MBEM_ERR_ARG,
@@ -583,6 +639,22 @@ int mbem_nn_adam(float* params, const float* grad, float* m, float* v, int64_t n
     nn_adam_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(params, grad, m, v, n, lr, beta1,
                                                                                beta2, eps, c1, c2);
     return launch_status("nn_adam_kernel");
+}
+
+int mbem_nn_basis(const mbem_block_jacobi* bj, const float* phi, const int64_t* u_ranges, int n_u_ranges,
+                  float* basis, double* U, void* stream) {
+    MBEM_REQUIRE(bj && bj->n_chunks >= 0 && bj->m_max <= MBEM_BJ_MAX_DOF && phi && basis, MBEM_ERR_ARG,
+                 "bad coarse-basis args");
+    URanges ur;
+    int e = make_ranges(u_ranges, n_u_ranges, ur);
+    if (e) return e;
+    int64_t u_nodes = 0;
+    for (int q = 0; q < ur.n; q++) u_nodes += ur.len[q] / 3;
+    if (bj->n_chunks == 0) return MBEM_OK;
+    nn_basis_kernel<<<(unsigned)bj->n_chunks, 128, 0, (cudaStream_t)stream>>>(
+        bj->chunk_ptr, bj->dofs, phi, ur, u_nodes > 0 ? 1.0 / sqrt((double)u_nodes) : 0.0, basis,
+        u_nodes > 0 ? U : nullptr);
+    return launch_status("nn_basis_kernel");
 }
 
 size_t mbem_nn_setup_workspace_size(int64_t n_coarse) {

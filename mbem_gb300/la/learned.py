@@ -155,10 +155,18 @@ class LearnedPreconditioner:
         dev = self.bj.device
         n = self.bj.n
         nc = 6 * self.bj.n_chunks
+        import time
+        t0 = time.perf_counter()
         self.params = torch.as_tensor(np.asarray(params, np.float32)).to(dev)
         self.feat = torch.from_numpy(node_features(asm.layout, self.bj.chunk_nodes())).to(dev)
+        t1 = time.perf_counter()
         self.phi = mlp_forward(self.feat, self.params)
-        self.basis = torch.from_numpy(self._orthonormal_basis()).to(dev)
+        self.basis = torch.empty((n, 6), dtype=torch.float32, device=dev)
+        rng = np.ascontiguousarray(np.asarray(asm.u_ranges(), dtype=np.int64).reshape(-1))
+        shift = torch.zeros((nc, 3), dtype=torch.float64, device=dev) if rng.size else None
+        nat.call("mbem_nn_basis", ctypes.byref(self.bj.struct()), ptr(self.phi),
+                 rng.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) if rng.size else None, len(rng) // 2,
+                 ptr(self.basis), ptr(shift) if shift is not None else None, stream_handle())
         self.APhi = torch.empty((n, nc), dtype=torch.float64, device=dev)
         self.Ac_inv = torch.empty((nc, nc), dtype=torch.float64, device=dev)
         self.work = torch.empty(nat.lib().mbem_nn_apply_workspace_size(n, nc) // 8, dtype=torch.float64,
@@ -169,39 +177,11 @@ class LearnedPreconditioner:
         need = nat.lib().mbem_nn_setup_workspace_size(nc)
         setup_work = torch.empty(need, dtype=torch.uint8, device=dev)
         A = asm.A
-        shift = self._null_shift(asm)
         nat.call("mbem_nn_setup_dense", ptr(A), A.stride(0), ctypes.byref(self._struct),
                  ptr(shift) if shift is not None else None, 0 if shift is None else shift.shape[1],
                  ptr(setup_work), need, stream_handle())
         self.built = True
-
-    def _orthonormal_basis(self) -> np.ndarray:
-        """(n, 6) FP32: per chunk, the rows [I | phi_i] of its nodes made
-        orthonormal (QR); the span, which is what the coarse correction
-        depends on, is unchanged."""
-        phi = self.phi.double().cpu().numpy().reshape(-1, 3, 3)
-        B = np.zeros((self.bj.n, 6))
-        for nodes in self.bj.chunk_nodes():
-            Bc = np.concatenate([np.broadcast_to(np.eye(3), (len(nodes), 3, 3)), phi[nodes]], axis=2).reshape(-1, 6)
-            Q, _ = np.linalg.qr(Bc)
-            B[(3 * nodes[:, None] + np.arange(3)).ravel()] = Q
-        return np.ascontiguousarray(B, dtype=np.float32)
-
-    def _null_shift(self, asm):
-        """Phi^T Z (n_coarse, 3) for the deflated translations Z of a
-        calibrated all-Neumann system (A Z = 0), else None."""
-        if not asm.deflate:
-            return None
-        from ..backends.dense import translation_basis
-        Z = translation_basis(asm.layout)
-        if Z.shape[1] == 0:
-            return None
-        B = self.basis.double().cpu().numpy()
-        U = np.zeros((6 * self.bj.n_chunks, Z.shape[1]))
-        for c, nodes in enumerate(self.bj.chunk_nodes()):
-            d = (3 * nodes[:, None] + np.arange(3)).ravel()
-            U[6 * c:6 * c + 6] = B[d].T @ Z[d]
-        return torch.from_numpy(U).to(self.phi.device)
+        self.setup_s = {"features_host": t1 - t0, "device": time.perf_counter() - t1}
 
     def struct(self):
         return self._struct
