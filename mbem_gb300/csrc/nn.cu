@@ -380,17 +380,22 @@ __global__ void nn_coarse_shift_kernel(double* __restrict__ Ac, int64_t nc, cons
     Ac[p * nc + q] += s;
 }
 
-// Gauss-Jordan step k on M (m x m, FP64, in place): pivot search, row swap,
-// scaling of the pivot row; one CTA
+// One Gauss-Jordan step with partial pivoting, out of place (Min -> Mout, so
+// no block reads a row another block is writing): every block finds the
+// pivot p = argmax_{i >= k} |Min[i, k]| itself (same data, same order, same
+// answer), forms the scaled pivot row, and writes its share of the rows of
+// Mout; row k of Mout is the pivot row, row p the old row k (the swap).
+constexpr int GJ_ROWS = 16;       // rows of Mout per block
+
 __global__ void __launch_bounds__(256)
-gj_pivot_kernel(double* __restrict__ M, int64_t m, int64_t k, double* __restrict__ rowk, double* __restrict__ fcol,
-                int* __restrict__ piv, int* __restrict__ bad) {
+gj_step_kernel(const double* __restrict__ Min, double* __restrict__ Mout, int64_t m, int64_t k,
+               int* __restrict__ piv, int* __restrict__ bad) {
     __shared__ double bv[256];
     __shared__ int64_t bi[256];
     double best = -1.0;
     int64_t besti = k;
     for (int64_t i = k + threadIdx.x; i < m; i += 256) {
-        const double v = fabs(M[i * m + k]);
+        const double v = fabs(Min[i * m + k]);
         if (v > best) { best = v; besti = i; }
     }
     bv[threadIdx.x] = best;
@@ -408,37 +413,20 @@ gj_pivot_kernel(double* __restrict__ M, int64_t m, int64_t k, double* __restrict
         __syncthreads();
     }
     const int64_t p = bi[0];
-    if (threadIdx.x == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         piv[k] = (int)p;
         if (!(bv[0] > 0.0)) *bad = 1;
     }
-    if (p != k)
-        for (int64_t j = threadIdx.x; j < m; j += 256) {
-            const double t = M[k * m + j];
-            M[k * m + j] = M[p * m + j];
-            M[p * m + j] = t;
-        }
-    __syncthreads();
-    const double pv = M[k * m + k];
+    const double pv = Min[p * m + k];
     const double d = (pv != 0.0) ? 1.0 / pv : 1.0;
-    for (int64_t j = threadIdx.x; j < m; j += 256) {
-        rowk[j] = (j == k ? 1.0 : M[k * m + j]) * d;
-        fcol[j] = M[j * m + k];
-    }
-}
-
-// rank-1 update of every row but k; row k becomes rowk
-__global__ void __launch_bounds__(256)
-gj_update_kernel(double* __restrict__ M, int64_t m, int64_t k, const double* __restrict__ rowk,
-                 const double* __restrict__ fcol) {
-    const int64_t i = blockIdx.y;
-    const int64_t j = (int64_t)blockIdx.x * 256 + threadIdx.x;
-    if (j >= m) return;
-    if (i == k) {
-        M[i * m + j] = rowk[j];
-    } else {
-        const double v = (j == k) ? 0.0 : M[i * m + j];
-        M[i * m + j] = v - fcol[i] * rowk[j];
+    const int64_t r0 = (int64_t)blockIdx.x * GJ_ROWS;
+    for (int64_t i = r0; i < lmin(m, r0 + GJ_ROWS); i++) {
+        const int64_t src = (i == k) ? p : (i == p ? k : i);     // the row swap
+        const double fi = (i == k) ? 0.0 : Min[src * m + k];
+        for (int64_t j = threadIdx.x; j < m; j += 256) {
+            const double rk = (j == k ? 1.0 : Min[p * m + j]) * d;
+            Mout[i * m + j] = (i == k) ? rk : ((j == k ? 0.0 : Min[src * m + j]) - fi * rk);
+        }
     }
 }
 
@@ -658,7 +646,7 @@ int mbem_nn_basis(const mbem_block_jacobi* bj, const float* phi, const int64_t* 
 }
 
 size_t mbem_nn_setup_workspace_size(int64_t n_coarse) {
-    return (size_t)(2 * n_coarse + 8) * sizeof(double) + (size_t)(n_coarse + 8) * sizeof(int);
+    return (size_t)n_coarse * n_coarse * sizeof(double) + (size_t)(n_coarse + 8) * sizeof(int);
 }
 
 int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift,
@@ -687,17 +675,21 @@ int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, 
                                                                                             n_shift);
         if ((e = launch_status("nn_coarse_shift_kernel"))) return e;
     }
-    // A_c^-1 in place
-    double* rowk = static_cast<double*>(work);
-    double* fcol = rowk + nc;
-    int* piv = reinterpret_cast<int*>(fcol + nc + 8);
+    // A_c^-1: Gauss-Jordan steps ping-ponging between Ac and a buffer
+    double* buf = static_cast<double*>(work);
+    int* piv = reinterpret_cast<int*>(buf + nc * nc);
     int* bad = piv + nc;
     cudaMemsetAsync(bad, 0, sizeof(int), st);
+    double* src = Ac;
+    double* dst = buf;
     for (int64_t k = 0; k < nc; k++) {
-        gj_pivot_kernel<<<1, 256, 0, st>>>(Ac, nc, k, rowk, fcol, piv, bad);
-        gj_update_kernel<<<dim3((unsigned)ceil_div(nc, 256), (unsigned)nc), 256, 0, st>>>(Ac, nc, k, rowk, fcol);
+        gj_step_kernel<<<(unsigned)ceil_div(nc, GJ_ROWS), 256, 0, st>>>(src, dst, nc, k, piv, bad);
+        double* t = src;
+        src = dst;
+        dst = t;
     }
-    count_launches((int)(2 * nc));
+    count_launches((int)nc);
+    if (src != Ac) cudaMemcpyAsync(Ac, src, nc * nc * sizeof(double), cudaMemcpyDeviceToDevice, st);
     gj_swap_columns_kernel<<<(unsigned)ceil_div(nc, 256), 256, 0, st>>>(Ac, nc, piv);
     if ((e = launch_status("gauss_jordan"))) return e;
     int hbad = 0;
