@@ -303,6 +303,15 @@ int mbem_nn_basis(const mbem_block_jacobi* bj, const float* phi, const int64_t* 
  * solution on the complement of Z is unchanged. MBEM_ERR_NUMERIC when A_c is
  * singular. */
 size_t mbem_nn_setup_workspace_size(int64_t n_coarse);
+/* The two halves of the setup: A Phi and A_c (+ shift shift^T) into
+ * APhi / Ac_inv, then A_c inverted in place. */
+int mbem_nn_coarse_operator_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift,
+                                  int n_shift, void* stream);
+/* In-place inverse of a dense FP64 matrix (n x n, row-major, n <= 1,048,560)
+ * by Gauss-Jordan with partial pivoting, one launch per pivot;
+ * MBEM_ERR_NUMERIC when singular. */
+size_t mbem_dense_inverse_workspace_size(int64_t n);
+int mbem_dense_inverse(double* M, int64_t n, void* work, size_t work_bytes, void* stream);
 int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift,
                         int n_shift, void* work, size_t work_bytes, void* stream);
 /* z = M^-1 r (r, z distinct device vectors of length n). */

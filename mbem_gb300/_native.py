@@ -126,6 +126,9 @@ _SIGNATURES = {
                              ctypes.c_float, c_int, _P]),
     "mbem_nn_basis": (c_int, [POINTER(BlockJacobi), _P, _P, c_int, _P, _P, _P]),
     "mbem_nn_setup_workspace_size": (c_size_t, [_I]),
+    "mbem_nn_coarse_operator_dense": (c_int, [_P, _I, POINTER(NnPrecond), _P, c_int, _P]),
+    "mbem_dense_inverse_workspace_size": (c_size_t, [_I]),
+    "mbem_dense_inverse": (c_int, [_P, _I, _P, c_size_t, _P]),
     "mbem_nn_setup_dense": (c_int, [_P, _I, POINTER(NnPrecond), _P, c_int, _P, c_size_t, _P]),
     "mbem_nn_apply_workspace_size": (c_size_t, [_I, _I]),
     "mbem_nn_apply": (c_int, [POINTER(NnPrecond), _P, _P, _P]),

@@ -645,21 +645,50 @@ int mbem_nn_basis(const mbem_block_jacobi* bj, const float* phi, const int64_t* 
     return launch_status("nn_basis_kernel");
 }
 
-size_t mbem_nn_setup_workspace_size(int64_t n_coarse) {
-    return (size_t)n_coarse * n_coarse * sizeof(double) + (size_t)(n_coarse + 8) * sizeof(int);
+size_t mbem_dense_inverse_workspace_size(int64_t n) {
+    return (size_t)n * n * sizeof(double) + (size_t)(n + 8) * sizeof(int);
 }
 
-int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift,
-                        int n_shift, void* work, size_t work_bytes, void* stream) {
+int mbem_dense_inverse(double* M, int64_t n, void* work, size_t work_bytes, void* stream) {
+    MBEM_REQUIRE(n >= 0 && n <= 65535 * GJ_ROWS && (n == 0 || M), MBEM_ERR_ARG, "bad matrix for the inverse");
+    if (n == 0) return MBEM_OK;
+    MBEM_REQUIRE(work && work_bytes >= mbem_dense_inverse_workspace_size(n), MBEM_ERR_SIZE,
+                 "inverse workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    double* buf = static_cast<double*>(work);
+    int* piv = reinterpret_cast<int*>(buf + n * n);
+    int* bad = piv + n;
+    cudaMemsetAsync(bad, 0, sizeof(int), st);
+    double* src = M;
+    double* dst = buf;
+    for (int64_t k = 0; k < n; k++) {
+        gj_step_kernel<<<(unsigned)ceil_div(n, GJ_ROWS), 256, 0, st>>>(src, dst, n, k, piv, bad);
+        double* t = src;
+        src = dst;
+        dst = t;
+    }
+    count_launches((int)n);
+    if (src != M) cudaMemcpyAsync(M, src, n * n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    gj_swap_columns_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(M, n, piv);
+    int e = launch_status("gauss_jordan");
+    if (e) return e;
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inverse sync", 0);
+    MBEM_REQUIRE(hbad == 0, MBEM_ERR_NUMERIC, "singular matrix");
+    return MBEM_OK;
+}
+
+int mbem_nn_coarse_operator_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift,
+                                  int n_shift, void* stream) {
     int e = nn_check(nn);
     if (e) return e;
     MBEM_REQUIRE(A != nullptr && ld >= nn->n, MBEM_ERR_ARG, "bad dense operator");
     const int64_t n = nn->n, nc = nn->n_coarse;
     if (n == 0) return MBEM_OK;
-    MBEM_REQUIRE(work != nullptr && work_bytes >= mbem_nn_setup_workspace_size(nc), MBEM_ERR_SIZE,
-                 "setup workspace too small");
     MBEM_REQUIRE(ceil_div(n, APHI_ROWS) <= 65535 && ceil_div(nc, 256) <= 65535 && nc <= 65535, MBEM_ERR_UNSUPPORTED,
                  "learned preconditioner sizes beyond one launch");
+    MBEM_REQUIRE(n_shift >= 0 && (n_shift == 0 || shift != nullptr), MBEM_ERR_ARG, "bad coarse shift");
     cudaStream_t st = (cudaStream_t)stream;
     const mbem_block_jacobi* bj = nn->bj;
     double* APhi = const_cast<double*>(nn->APhi);
@@ -669,34 +698,21 @@ int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, 
     nn_coarse_matrix_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(nc, 256)), 256, 0, st>>>(
         APhi, nc, bj->chunk_ptr, bj->dofs, nn->basis, Ac);
     if ((e = launch_status("nn_coarse_setup", 2))) return e;
-    MBEM_REQUIRE(n_shift >= 0 && (n_shift == 0 || shift != nullptr), MBEM_ERR_ARG, "bad coarse shift");
     if (n_shift > 0) {
         nn_coarse_shift_kernel<<<dim3((unsigned)ceil_div(nc, 256), (unsigned)nc), 256, 0, st>>>(Ac, nc, shift,
                                                                                             n_shift);
         if ((e = launch_status("nn_coarse_shift_kernel"))) return e;
     }
-    // A_c^-1: Gauss-Jordan steps ping-ponging between Ac and a buffer
-    double* buf = static_cast<double*>(work);
-    int* piv = reinterpret_cast<int*>(buf + nc * nc);
-    int* bad = piv + nc;
-    cudaMemsetAsync(bad, 0, sizeof(int), st);
-    double* src = Ac;
-    double* dst = buf;
-    for (int64_t k = 0; k < nc; k++) {
-        gj_step_kernel<<<(unsigned)ceil_div(nc, GJ_ROWS), 256, 0, st>>>(src, dst, nc, k, piv, bad);
-        double* t = src;
-        src = dst;
-        dst = t;
-    }
-    count_launches((int)nc);
-    if (src != Ac) cudaMemcpyAsync(Ac, src, nc * nc * sizeof(double), cudaMemcpyDeviceToDevice, st);
-    gj_swap_columns_kernel<<<(unsigned)ceil_div(nc, 256), 256, 0, st>>>(Ac, nc, piv);
-    if ((e = launch_status("gauss_jordan"))) return e;
-    int hbad = 0;
-    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("nn setup sync", 0);
-    MBEM_REQUIRE(hbad == 0, MBEM_ERR_NUMERIC, "singular coarse operator");
     return MBEM_OK;
+}
+
+size_t mbem_nn_setup_workspace_size(int64_t n_coarse) { return mbem_dense_inverse_workspace_size(n_coarse); }
+
+int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift,
+                        int n_shift, void* work, size_t work_bytes, void* stream) {
+    int e = mbem_nn_coarse_operator_dense(A, ld, nn, shift, n_shift, stream);
+    if (e) return e;
+    return mbem_dense_inverse(const_cast<double*>(nn->Ac_inv), nn->n_coarse, work, work_bytes, stream);
 }
 
 size_t mbem_nn_apply_workspace_size(int64_t n, int64_t n_coarse) {

@@ -174,14 +174,21 @@ class LearnedPreconditioner:
         self._bj_struct = self.bj.struct()
         self._struct = nat.NnPrecond(n=n, n_coarse=nc, bj=ctypes.pointer(self._bj_struct), basis=ptr(self.basis),
                                      APhi=ptr(self.APhi), Ac_inv=ptr(self.Ac_inv), work=ptr(self.work))
-        need = nat.lib().mbem_nn_setup_workspace_size(nc)
-        setup_work = torch.empty(need, dtype=torch.uint8, device=dev)
         A = asm.A
-        nat.call("mbem_nn_setup_dense", ptr(A), A.stride(0), ctypes.byref(self._struct),
-                 ptr(shift) if shift is not None else None, 0 if shift is None else shift.shape[1],
-                 ptr(setup_work), need, stream_handle())
+        st = stream_handle()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        nat.call("mbem_nn_coarse_operator_dense", ptr(A), A.stride(0), ctypes.byref(self._struct),
+                 ptr(shift) if shift is not None else None, 0 if shift is None else shift.shape[1], st)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        need = nat.lib().mbem_dense_inverse_workspace_size(nc)
+        inv_work = torch.empty(need, dtype=torch.uint8, device=dev)
+        nat.call("mbem_dense_inverse", ptr(self.Ac_inv), nc, ptr(inv_work), need, st)
         self.built = True
-        self.setup_s = {"features_host": t1 - t0, "device": time.perf_counter() - t1}
+        t4 = time.perf_counter()
+        self.setup_s = {"features_host": t1 - t0, "basis_device": t2 - t1, "coarse_operator_device": t3 - t2,
+                        "coarse_inverse_device": t4 - t3}
 
     def struct(self):
         return self._struct
