@@ -348,6 +348,73 @@ nn_aphi_kernel(const double* __restrict__ A, int64_t ld, int64_t n, const int64_
     }
 }
 
+// APhi by streaming A's rows: a warp per row reads the row contiguously;
+// consecutive columns of one chunk (runs of equal chunk index across the
+// lanes) are summed lane by lane in order, and each run's six sums are added
+// to the row's accumulator in shared memory by the run's first lane. A warp
+// owns its row's accumulator, so the order of every sum is fixed.
+constexpr int APHI_WARPS = 8;
+
+__global__ void __launch_bounds__(APHI_WARPS * 32)
+nn_aphi_rows_kernel(const double* __restrict__ A, int64_t ld, int64_t n, const int32_t* __restrict__ chunk_of,
+                    const float* __restrict__ basis, int64_t n_coarse, double* __restrict__ APhi) {
+    extern __shared__ double acc_all[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double* acc = acc_all + (int64_t)warp * n_coarse;
+    const int64_t r = (int64_t)blockIdx.x * APHI_WARPS + warp;
+    for (int64_t q = lane; q < n_coarse; q += 32) acc[q] = 0.0;
+    __syncwarp();
+    if (r < n) {
+        const double* Ar = A + r * ld;
+        for (int64_t j0 = 0; j0 < n; j0 += 32) {
+            const int64_t j = j0 + lane;
+            const bool live = j < n;
+            const double a = live ? Ar[j] : 0.0;
+            const int c = live ? chunk_of[j] : -1;
+            double v[NCV];
+#pragma unroll
+            for (int k = 0; k < NCV; k++) v[k] = live ? a * (double)basis[j * NCV + k] : 0.0;
+            // runs of equal c: the first lane of a run collects the run in lane order
+            const int cprev = __shfl_up_sync(0xffffffffu, c, 1);
+            const bool head = (lane == 0) || (cprev != c);
+            const unsigned heads = __ballot_sync(0xffffffffu, head);
+            // the run of this lane ends before the next head
+            const unsigned after = heads & ~((2u << lane) - 1u);
+            const int run_end = after ? (__ffs(after) - 1) : 32;     // exclusive
+            // sum over [lane, run_end) by a fixed tree: after the step with
+            // offset o a lane holds [lane, min(lane + 2o, run_end))
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+#pragma unroll
+                for (int k = 0; k < NCV; k++) {
+                    const double t = __shfl_down_sync(0xffffffffu, v[k], o);
+                    if (lane + o < run_end) v[k] += t;
+                }
+            // heads add their run; heads of one chunk (two runs of it in
+            // this stretch) add one after the other in lane order
+            const int key = head ? c : -1 - lane;
+            const unsigned same = __match_any_sync(0xffffffffu, key);
+            const bool dup = head && __popc(same) > 1;
+            if (!__any_sync(0xffffffffu, dup)) {
+                if (head && c >= 0)
+#pragma unroll
+                    for (int k = 0; k < NCV; k++) acc[NCV * c + k] += v[k];
+            } else {
+                for (int l = 0; l < 32; l++) {
+                    if (lane == l && head && c >= 0)
+#pragma unroll
+                        for (int k = 0; k < NCV; k++) acc[NCV * c + k] += v[k];
+                    __syncwarp();
+                }
+            }
+            __syncwarp();
+        }
+    }
+    __syncwarp();
+    if (r < n)
+        for (int64_t q = lane; q < n_coarse; q += 32) APhi[r * n_coarse + q] = acc[q];
+}
+
 // Ac[6c + k, q] = sum_{d in c} basis[d][k] APhi[d, q]: a CTA per (chunk,
 // 256 columns), a thread per column
 __global__ void __launch_bounds__(256)
@@ -380,16 +447,16 @@ __global__ void nn_coarse_shift_kernel(double* __restrict__ Ac, int64_t nc, cons
     Ac[p * nc + q] += s;
 }
 
-// One Gauss-Jordan step with partial pivoting, out of place (Min -> Mout, so
-// no block reads a row another block is writing): every block finds the
-// pivot p = argmax_{i >= k} |Min[i, k]| itself (same data, same order, same
-// answer), forms the scaled pivot row, and writes its share of the rows of
-// Mout; row k of Mout is the pivot row, row p the old row k (the swap).
-constexpr int GJ_ROWS = 16;       // rows of Mout per block
+// Gauss-Jordan with partial pivoting, out of place per step (Min -> Mout,
+// so no thread reads an entry another is writing). gj_pivot_kernel (one
+// block) finds p = argmax_{i >= k} |Min[i, k]| and 1 / Min[p, k];
+// gj_update_kernel writes Mout, a thread per (row group, column): row k of
+// Mout is the scaled pivot row, row p the old row k (the swap).
+constexpr int GJ_ROWS = 8;        // rows of Mout per thread
 
 __global__ void __launch_bounds__(256)
-gj_step_kernel(const double* __restrict__ Min, double* __restrict__ Mout, int64_t m, int64_t k,
-               int* __restrict__ piv, int* __restrict__ bad) {
+gj_pivot_kernel(const double* __restrict__ Min, int64_t m, int64_t k, int* __restrict__ piv,
+                double* __restrict__ dinv, int* __restrict__ bad) {
     __shared__ double bv[256];
     __shared__ int64_t bi[256];
     double best = -1.0;
@@ -412,20 +479,31 @@ gj_step_kernel(const double* __restrict__ Min, double* __restrict__ Mout, int64_
         }
         __syncthreads();
     }
-    const int64_t p = bi[0];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (threadIdx.x == 0) {
+        const int64_t p = bi[0];
         piv[k] = (int)p;
+        const double pv = Min[p * m + k];
+        *dinv = (pv != 0.0) ? 1.0 / pv : 1.0;
         if (!(bv[0] > 0.0)) *bad = 1;
     }
-    const double pv = Min[p * m + k];
-    const double d = (pv != 0.0) ? 1.0 / pv : 1.0;
-    const int64_t r0 = (int64_t)blockIdx.x * GJ_ROWS;
+}
+
+__global__ void __launch_bounds__(256)
+gj_update_kernel(const double* __restrict__ Min, double* __restrict__ Mout, int64_t m, int64_t k,
+                 const int* __restrict__ piv, const double* __restrict__ dinv) {
+    const int64_t j = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (j >= m) return;
+    const int64_t p = piv[k];
+    const double d = *dinv;
+    const double rk = (j == k ? 1.0 : Min[p * m + j]) * d;
+    const int64_t r0 = (int64_t)blockIdx.y * GJ_ROWS;
     for (int64_t i = r0; i < lmin(m, r0 + GJ_ROWS); i++) {
         const int64_t src = (i == k) ? p : (i == p ? k : i);     // the row swap
-        const double fi = (i == k) ? 0.0 : Min[src * m + k];
-        for (int64_t j = threadIdx.x; j < m; j += 256) {
-            const double rk = (j == k ? 1.0 : Min[p * m + j]) * d;
-            Mout[i * m + j] = (i == k) ? rk : ((j == k ? 0.0 : Min[src * m + j]) - fi * rk);
+        if (i == k) {
+            Mout[i * m + j] = rk;
+        } else {
+            const double fi = Min[src * m + k];
+            Mout[i * m + j] = (j == k ? 0.0 : Min[src * m + j]) - fi * rk;
         }
     }
 }
@@ -646,7 +724,7 @@ int mbem_nn_basis(const mbem_block_jacobi* bj, const float* phi, const int64_t* 
 }
 
 size_t mbem_dense_inverse_workspace_size(int64_t n) {
-    return (size_t)n * n * sizeof(double) + (size_t)(n + 8) * sizeof(int);
+    return (size_t)(n * n + 1) * sizeof(double) + (size_t)(n + 8) * sizeof(int);
 }
 
 int mbem_dense_inverse(double* M, int64_t n, void* work, size_t work_bytes, void* stream) {
@@ -656,18 +734,21 @@ int mbem_dense_inverse(double* M, int64_t n, void* work, size_t work_bytes, void
                  "inverse workspace too small");
     cudaStream_t st = (cudaStream_t)stream;
     double* buf = static_cast<double*>(work);
-    int* piv = reinterpret_cast<int*>(buf + n * n);
+    double* dinv = buf + n * n;
+    int* piv = reinterpret_cast<int*>(dinv + 1);
     int* bad = piv + n;
     cudaMemsetAsync(bad, 0, sizeof(int), st);
     double* src = M;
     double* dst = buf;
+    const dim3 grid((unsigned)ceil_div(n, 256), (unsigned)ceil_div(n, GJ_ROWS));
     for (int64_t k = 0; k < n; k++) {
-        gj_step_kernel<<<(unsigned)ceil_div(n, GJ_ROWS), 256, 0, st>>>(src, dst, n, k, piv, bad);
+        gj_pivot_kernel<<<1, 256, 0, st>>>(src, n, k, piv, dinv, bad);
+        gj_update_kernel<<<grid, 256, 0, st>>>(src, dst, n, k, piv, dinv);
         double* t = src;
         src = dst;
         dst = t;
     }
-    count_launches((int)n);
+    count_launches((int)(2 * n));
     if (src != M) cudaMemcpyAsync(M, src, n * n * sizeof(double), cudaMemcpyDeviceToDevice, st);
     gj_swap_columns_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(M, n, piv);
     int e = launch_status("gauss_jordan");
@@ -693,8 +774,15 @@ int mbem_nn_coarse_operator_dense(const double* A, int64_t ld, const mbem_nn_pre
     const mbem_block_jacobi* bj = nn->bj;
     double* APhi = const_cast<double*>(nn->APhi);
     double* Ac = const_cast<double*>(nn->Ac_inv);
-    nn_aphi_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(n, APHI_ROWS)), 256, 0, st>>>(
-        A, ld, n, bj->chunk_ptr, bj->dofs, nn->basis, nc, APhi);
+    const size_t smem = (size_t)APHI_WARPS * nc * sizeof(double);
+    if (smem <= 200 * 1024) {
+        cudaFuncSetAttribute(nn_aphi_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        nn_aphi_rows_kernel<<<(unsigned)ceil_div(n, APHI_WARPS), APHI_WARPS * 32, smem, st>>>(
+            A, ld, n, bj->chunk_of, nn->basis, nc, APhi);
+    } else {
+        nn_aphi_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(n, APHI_ROWS)), 256, 0, st>>>(
+            A, ld, n, bj->chunk_ptr, bj->dofs, nn->basis, nc, APhi);
+    }
     nn_coarse_matrix_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(nc, 256)), 256, 0, st>>>(
         APhi, nc, bj->chunk_ptr, bj->dofs, nn->basis, Ac);
     if ((e = launch_status("nn_coarse_setup", 2))) return e;
