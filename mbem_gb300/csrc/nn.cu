@@ -348,73 +348,6 @@ nn_aphi_kernel(const double* __restrict__ A, int64_t ld, int64_t n, const int64_
     }
 }
 
-// APhi by streaming A's rows: a warp per row reads the row contiguously;
-// consecutive columns of one chunk (runs of equal chunk index across the
-// lanes) are summed lane by lane in order, and each run's six sums are added
-// to the row's accumulator in shared memory by the run's first lane. A warp
-// owns its row's accumulator, so the order of every sum is fixed.
-constexpr int APHI_WARPS = 8;
-
-__global__ void __launch_bounds__(APHI_WARPS * 32)
-nn_aphi_rows_kernel(const double* __restrict__ A, int64_t ld, int64_t n, const int32_t* __restrict__ chunk_of,
-                    const float* __restrict__ basis, int64_t n_coarse, double* __restrict__ APhi) {
-    extern __shared__ double acc_all[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double* acc = acc_all + (int64_t)warp * n_coarse;
-    const int64_t r = (int64_t)blockIdx.x * APHI_WARPS + warp;
-    for (int64_t q = lane; q < n_coarse; q += 32) acc[q] = 0.0;
-    __syncwarp();
-    if (r < n) {
-        const double* Ar = A + r * ld;
-        for (int64_t j0 = 0; j0 < n; j0 += 32) {
-            const int64_t j = j0 + lane;
-            const bool live = j < n;
-            const double a = live ? Ar[j] : 0.0;
-            const int c = live ? chunk_of[j] : -1;
-            double v[NCV];
-#pragma unroll
-            for (int k = 0; k < NCV; k++) v[k] = live ? a * (double)basis[j * NCV + k] : 0.0;
-            // runs of equal c: the first lane of a run collects the run in lane order
-            const int cprev = __shfl_up_sync(0xffffffffu, c, 1);
-            const bool head = (lane == 0) || (cprev != c);
-            const unsigned heads = __ballot_sync(0xffffffffu, head);
-            // the run of this lane ends before the next head
-            const unsigned after = heads & ~((2u << lane) - 1u);
-            const int run_end = after ? (__ffs(after) - 1) : 32;     // exclusive
-            // sum over [lane, run_end) by a fixed tree: after the step with
-            // offset o a lane holds [lane, min(lane + 2o, run_end))
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1)
-#pragma unroll
-                for (int k = 0; k < NCV; k++) {
-                    const double t = __shfl_down_sync(0xffffffffu, v[k], o);
-                    if (lane + o < run_end) v[k] += t;
-                }
-            // heads add their run; heads of one chunk (two runs of it in
-            // this stretch) add one after the other in lane order
-            const int key = head ? c : -1 - lane;
-            const unsigned same = __match_any_sync(0xffffffffu, key);
-            const bool dup = head && __popc(same) > 1;
-            if (!__any_sync(0xffffffffu, dup)) {
-                if (head && c >= 0)
-#pragma unroll
-                    for (int k = 0; k < NCV; k++) acc[NCV * c + k] += v[k];
-            } else {
-                for (int l = 0; l < 32; l++) {
-                    if (lane == l && head && c >= 0)
-#pragma unroll
-                        for (int k = 0; k < NCV; k++) acc[NCV * c + k] += v[k];
-                    __syncwarp();
-                }
-            }
-            __syncwarp();
-        }
-    }
-    __syncwarp();
-    if (r < n)
-        for (int64_t q = lane; q < n_coarse; q += 32) APhi[r * n_coarse + q] = acc[q];
-}
-
 // Ac[6c + k, q] = sum_{d in c} basis[d][k] APhi[d, q]: a CTA per (chunk,
 // 256 columns), a thread per column
 __global__ void __launch_bounds__(256)
@@ -774,15 +707,8 @@ int mbem_nn_coarse_operator_dense(const double* A, int64_t ld, const mbem_nn_pre
     const mbem_block_jacobi* bj = nn->bj;
     double* APhi = const_cast<double*>(nn->APhi);
     double* Ac = const_cast<double*>(nn->Ac_inv);
-    const size_t smem = (size_t)APHI_WARPS * nc * sizeof(double);
-    if (smem <= 200 * 1024) {
-        cudaFuncSetAttribute(nn_aphi_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        nn_aphi_rows_kernel<<<(unsigned)ceil_div(n, APHI_WARPS), APHI_WARPS * 32, smem, st>>>(
-            A, ld, n, bj->chunk_of, nn->basis, nc, APhi);
-    } else {
-        nn_aphi_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(n, APHI_ROWS)), 256, 0, st>>>(
-            A, ld, n, bj->chunk_ptr, bj->dofs, nn->basis, nc, APhi);
-    }
+    nn_aphi_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(n, APHI_ROWS)), 256, 0, st>>>(
+        A, ld, n, bj->chunk_ptr, bj->dofs, nn->basis, nc, APhi);
     nn_coarse_matrix_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(nc, 256)), 256, 0, st>>>(
         APhi, nc, bj->chunk_ptr, bj->dofs, nn->basis, Ac);
     if ((e = launch_status("nn_coarse_setup", 2))) return e;
