@@ -1,0 +1,62 @@
+"""One launch (or a few) of a hot kernel on a small case, for profilers:
+``python -m mbem_gb300.kernel_cases tcgemm|traction|dfgemm|nodal``.
+
+tcgemm    the block solver's GEMM: (20,736 x 62,208 BF16) x (62,208 x 256)
+traction  FAULT_TRACTION assembly, cube 16 x 16, fault 12 x 12, dip 60,
+          with its block-Jacobi build (traction rows, bj_build_kernel)
+dfgemm    the block residual of the mixed operator, cube 24, 64 RHS
+nodal     the P2 DD-minus-eigen readout of a 16 x 16 fault at 20,000 points
+"""
+
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+import torch
+
+
+def run(which: str) -> None:
+    from .backends.dense import DenseBackend
+    from .cases import cube_fault_model, fault_traction_model
+    from .model import generate_system
+    if which == "tcgemm":
+        from .la.multirhs import gemm_bf16_t
+        n, k = 20736, 256
+        A = torch.randn((n, 3 * n), device="cuda").to(torch.bfloat16)
+        X = torch.randn((k, 3 * n), device="cuda").to(torch.bfloat16)
+        W = torch.empty((k, n), device="cuda")
+        for _ in range(3):
+            gemm_bf16_t(A, X, 3 * n, W)
+    elif which == "traction":
+        model, eps = fault_traction_model(16, 12, 60.0)
+        asm = DenseBackend(jump="calibrated", deflate=True).assemble(generate_system(model), eps)
+        asm.block_jacobi()
+    elif which == "dfgemm":
+        from .la.multirhs import BlockSolver
+        model, eps = cube_fault_model(24, 16)
+        asm = DenseBackend(jump="calibrated", deflate=True, precision="mixed").assemble(generate_system(model),
+                                                                                         eps)
+        bs = BlockSolver(asm)
+        B = torch.randn((64, bs.n), dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            bs.residual(B, B)
+    elif which == "nodal":
+        from . import mesh as M
+        from .kernels import tri_nodal as tn
+        fault = M.centre_fault(16)
+        tv = fault.tri_verts()
+        nrm, _ = fault.normals_and_areas()
+        rng = np.random.default_rng(0)
+        x = rng.uniform(-1, 1, size=(20000, 3))
+        d = rng.normal(size=(6 * tv.shape[0], 3))
+        e = np.full(tv.shape[0], 0.01)
+        for _ in range(2):
+            tn.elastic_stress_contract(x, tv, nrm, e, d, 1.0, 1.0, order=2)
+    else:
+        raise SystemExit(f"unknown case {which!r}")
+    torch.cuda.synchronize()
+
+
+if __name__ == "__main__":
+    run(sys.argv[1])
