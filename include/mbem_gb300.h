@@ -332,6 +332,12 @@ int mbem_gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, int6
  * right-hand side (the layout of the batched solver's vectors). */
 int mbem_gemm_bf16_t(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K, int n_rhs,
                      float* Yt, int64_t ldy, void* stream);
+/* The transposed product with K split over the SMs (up to 8 slices whose
+ * partial sums are added in slice order): for products whose 128-row tiles
+ * do not fill the GPU evenly. work: mbem_gemm_bf16_workspace_size() bytes. */
+size_t mbem_gemm_bf16_workspace_size(int64_t M, int n_rhs);
+int mbem_gemm_bf16_t_split(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K,
+                           int n_rhs, float* Yt, int64_t ldy, void* work, size_t work_bytes, void* stream);
 int mbem_gemm_bf16_check(void* stream);
 
 /* ---- batched GMRES for a block of k right-hand sides (k Krylov iterations

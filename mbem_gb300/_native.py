@@ -103,6 +103,8 @@ _SIGNATURES = {
     "mbem_gemm_bf16": (c_int, [_P, _I, _P, _I, _I, _I, c_int, _P, _I, _P]),
     "mbem_gemm_bf16_check": (c_int, [_P]),
     "mbem_gemm_bf16_t": (c_int, [_P, _I, _P, _I, _I, _I, c_int, _P, _I, _P]),
+    "mbem_gemm_bf16_workspace_size": (c_size_t, [_I, c_int]),
+    "mbem_gemm_bf16_t_split": (c_int, [_P, _I, _P, _I, _I, _I, c_int, _P, _I, _P, c_size_t, _P]),
     "mbem_to_bf16": (c_int, [_P, c_int, _I, _I, _I, _P, _I, _P]),
     "mbem_mixed_to_bf16": (c_int, [POINTER(MixedOperator), _P, _I, _P]),
     "mbem_to_bf16x2": (c_int, [_P, c_int, _I, _I, _I, _P, _P, _I, _P]),

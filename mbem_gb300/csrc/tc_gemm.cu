@@ -67,7 +67,7 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 template <int BN, bool TRANS>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
-               int64_t K, float* __restrict__ Y, int64_t ldy, int n_cols) {
+               int64_t K, float* __restrict__ Y, int64_t ldy, int n_cols, int kb_per, int64_t split_stride) {
     static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "MMA N for M = 128");
     constexpr int A_BYTES = TC_BM * TC_BK * 2;
     constexpr int B_BYTES = BN * TC_BK * 2;
@@ -80,7 +80,12 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t m0 = (int64_t)blockIdx.x * TC_BM;
-    const int kb_total = (int)((K + TC_BK - 1) / TC_BK);
+    // this CTA's share of K (a split of K over blockIdx.y; its partial sum
+    // goes to slice blockIdx.y of Y)
+    const int kb_all = (int)((K + TC_BK - 1) / TC_BK);
+    const int kb_first = (int)blockIdx.y * kb_per;
+    const int kb_total = min(kb_per, kb_all - kb_first);
+    Y += (int64_t)blockIdx.y * split_stride;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; s++) {
@@ -109,8 +114,8 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
             if (!mbar_wait(&empty[s], ph ^ 1u, TC_WAIT_LIMIT)) atomicExch(&g_tc_error, 1);
             uint8_t* st = smem + s * STAGE;
             mbar_arrive_expect_tx(&full[s], STAGE);
-            tma_load_2d(st, &mapA, kb * TC_BK, (int)m0, &full[s]);
-            tma_load_2d(st + A_BYTES, &mapB, kb * TC_BK, 0, &full[s]);
+            tma_load_2d(st, &mapA, (kb_first + kb) * TC_BK, (int)m0, &full[s]);
+            tma_load_2d(st + A_BYTES, &mapB, (kb_first + kb) * TC_BK, 0, &full[s]);
         }
         // the last copies have landed before the CTA can end
         for (int kb = (kb_total > TC_STAGES ? kb_total - TC_STAGES : 0); kb < kb_total; kb++)
@@ -210,25 +215,54 @@ static int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t co
 
 template <int BN, bool TRANS>
 static int launch_tc(const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int64_t K, float* Y, int64_t ldy,
-                     int n_cols, cudaStream_t st) {
+                     int n_cols, int splits, int kb_per, int64_t split_stride, cudaStream_t st) {
     const size_t smem = (size_t)TC_STAGES * (TC_BM * TC_BK * 2 + BN * TC_BK * 2) + 1024;
     cudaFuncSetAttribute(tc_gemm_kernel<BN, TRANS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    tc_gemm_kernel<BN, TRANS><<<(unsigned)ceil_div(M, TC_BM), TC_THREADS, smem, st>>>(ma, mb, M, K, Y, ldy, n_cols);
+    const dim3 grid((unsigned)ceil_div(M, TC_BM), (unsigned)splits);
+    tc_gemm_kernel<BN, TRANS><<<grid, TC_THREADS, smem, st>>>(ma, mb, M, K, Y, ldy, n_cols, kb_per, split_stride);
     return launch_status("tc_gemm_kernel");
 }
 
 template <bool TRANS>
 static int launch_bn(int bn, const CUtensorMap& ma, const CUtensorMap& mb, int64_t M, int64_t K, float* Y,
-                     int64_t ldy, int n_rhs, cudaStream_t st) {
+                     int64_t ldy, int n_rhs, int splits, int kb_per, int64_t split_stride, cudaStream_t st) {
     switch (bn) {
-        case 16: return launch_tc<16, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, st);
-        case 32: return launch_tc<32, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, st);
-        case 64: return launch_tc<64, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, st);
-        case 128: return launch_tc<128, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, st);
-        case 256: return launch_tc<256, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, st);
+        case 16: return launch_tc<16, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, splits, kb_per, split_stride, st);
+        case 32: return launch_tc<32, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, splits, kb_per, split_stride, st);
+        case 64: return launch_tc<64, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, splits, kb_per, split_stride, st);
+        case 128: return launch_tc<128, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, splits, kb_per, split_stride, st);
+        case 256: return launch_tc<256, TRANS>(ma, mb, M, K, Y, ldy, n_rhs, splits, kb_per, split_stride, st);
         default: break;
     }
     return set_error(MBEM_ERR_UNSUPPORTED, "no GEMM tile for %d right-hand sides", bn);
+}
+
+// Y[i] = sum_s P[s][i] over the K splits, in split order
+__global__ void split_sum_kernel(const float* __restrict__ P, int splits, int64_t stride, int64_t rows,
+                                 int64_t cols, float* __restrict__ Y, int64_t ldy) {
+    const int64_t r = blockIdx.y;
+    const int64_t c = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (c >= cols) return;
+    float acc = 0.0f;
+    for (int s = 0; s < splits; s++) acc += P[s * stride + r * cols + c];
+    Y[r * ldy + c] = acc;
+}
+
+// K splits that fill the SMs evenly: the smallest count of waves per unit of
+// work over 1..8 splits, each split keeping at least 8 K blocks
+static int choose_splits(int64_t tiles, int kb_all, int sms) {
+    int best = 1;
+    double best_cost = 1e30;
+    for (int s = 1; s <= 8; s++) {
+        if (kb_all / s < 8 && s > 1) break;
+        const double waves = (double)ceil_div(tiles * s, sms);
+        const double cost = waves / s + 0.02 * (s - 1);     // the partial sums' traffic
+        if (cost < best_cost - 1e-12) {
+            best_cost = cost;
+            best = s;
+        }
+    }
+    return best;
 }
 
 int tc_gemm_check(cudaStream_t st) {
@@ -244,7 +278,7 @@ int tc_gemm_check(cudaStream_t st) {
 }
 
 static int gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K, int n_rhs,
-                     float* Y, int64_t ldy, bool trans, cudaStream_t st) {
+                     float* Y, int64_t ldy, bool trans, float* work, size_t work_bytes, cudaStream_t st) {
     MBEM_REQUIRE(M >= 0 && K >= 1 && n_rhs >= 1 && n_rhs <= 256, MBEM_ERR_ARG,
                  "bad GEMM sizes (M=%lld, K=%lld, n_rhs=%d; n_rhs <= 256)", (long long)M, (long long)K, n_rhs);
     MBEM_REQUIRE(A && Xt && Y && lda >= K && ldx >= K && ldy >= (trans ? M : n_rhs), MBEM_ERR_ARG,
@@ -258,14 +292,32 @@ static int gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, in
     CUtensorMap ma, mb;
     if ((e = make_map(&ma, A, M, K, lda, TC_BM))) return e;
     if ((e = make_map(&mb, Xt, n_rhs, K, ldx, bn))) return e;
-    return trans ? launch_bn<true>(bn, ma, mb, M, K, Y, ldy, n_rhs, st)
-                 : launch_bn<false>(bn, ma, mb, M, K, Y, ldy, n_rhs, st);
+    const int kb_all = (int)ceil_div(K, TC_BK);
+    int sms = 152;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int splits = 1;
+    const int64_t rows_out = trans ? n_rhs : M, cols_out = trans ? M : n_rhs;
+    const int64_t slice = rows_out * cols_out;
+    if (work != nullptr) {
+        splits = choose_splits(ceil_div(M, TC_BM), kb_all, sms);
+        while (splits > 1 && work_bytes < (size_t)splits * slice * sizeof(float)) splits--;
+    }
+    const int kb_per = (int)ceil_div(kb_all, splits);
+    splits = (int)ceil_div(kb_all, kb_per);                // every split non-empty
+    if (splits == 1)
+        return trans ? launch_bn<true>(bn, ma, mb, M, K, Y, ldy, n_rhs, 1, kb_per, 0, st)
+                     : launch_bn<false>(bn, ma, mb, M, K, Y, ldy, n_rhs, 1, kb_per, 0, st);
+    // partial sums in the workspace (dense, leading dimension = cols_out), then their sum
+    e = trans ? launch_bn<true>(bn, ma, mb, M, K, work, cols_out, n_rhs, splits, kb_per, slice, st)
+              : launch_bn<false>(bn, ma, mb, M, K, work, cols_out, n_rhs, splits, kb_per, slice, st);
+    if (e) return e;
+    split_sum_kernel<<<dim3((unsigned)ceil_div(cols_out, 256), (unsigned)rows_out), 256, 0, st>>>(
+        work, splits, slice, rows_out, cols_out, Y, ldy);
+    return launch_status("split_sum_kernel");
 }
 
-int tc_gemm(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K, int n_rhs, float* Y,
-            int64_t ldy, bool trans, cudaStream_t st) {
-    return gemm_bf16(A, lda, Xt, ldx, M, K, n_rhs, Y, ldy, trans, st);
-}
+size_t tc_gemm_workspace_size(int64_t M, int n_rhs) { return (size_t)8 * M * n_rhs * sizeof(float); }
 
 }  // namespace mbem
 
@@ -273,12 +325,21 @@ using namespace mbem;
 
 extern "C" int mbem_gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K,
                               int n_rhs, float* Y, int64_t ldy, void* stream) {
-    return gemm_bf16(A, lda, Xt, ldx, M, K, n_rhs, Y, ldy, false, (cudaStream_t)stream);
+    return gemm_bf16(A, lda, Xt, ldx, M, K, n_rhs, Y, ldy, false, nullptr, 0, (cudaStream_t)stream);
 }
 
 extern "C" int mbem_gemm_bf16_t(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K,
                                 int n_rhs, float* Yt, int64_t ldy, void* stream) {
-    return gemm_bf16(A, lda, Xt, ldx, M, K, n_rhs, Yt, ldy, true, (cudaStream_t)stream);
+    return gemm_bf16(A, lda, Xt, ldx, M, K, n_rhs, Yt, ldy, true, nullptr, 0, (cudaStream_t)stream);
+}
+
+extern "C" size_t mbem_gemm_bf16_workspace_size(int64_t M, int n_rhs) { return tc_gemm_workspace_size(M, n_rhs); }
+
+extern "C" int mbem_gemm_bf16_t_split(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K,
+                                      int n_rhs, float* Yt, int64_t ldy, void* work, size_t work_bytes,
+                                      void* stream) {
+    return gemm_bf16(A, lda, Xt, ldx, M, K, n_rhs, Yt, ldy, true, static_cast<float*>(work), work_bytes,
+                     (cudaStream_t)stream);
 }
 
 extern "C" int mbem_gemm_bf16_check(void* stream) { return tc_gemm_check((cudaStream_t)stream); }

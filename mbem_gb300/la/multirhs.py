@@ -39,12 +39,28 @@ def gemm_check():
     nat.call("mbem_gemm_bf16_check", stream_handle())
 
 
-def gemm_bf16_t(A: torch.Tensor, Xt: torch.Tensor, K: int, out: torch.Tensor) -> torch.Tensor:
-    """out (n, M) FP32 = (A[:, :K] @ Xt[:, :K]^T)^T, out's rows at out.stride(0)."""
+_split_work = {}
+
+
+def gemm_bf16_t(A: torch.Tensor, Xt: torch.Tensor, K: int, out: torch.Tensor, split: bool = True) -> torch.Tensor:
+    """out (n, M) FP32 = (A[:, :K] @ Xt[:, :K]^T)^T, out's rows at out.stride(0);
+    with ``split`` K is divided over the SMs when the row tiles alone
+    would leave them unevenly loaded."""
     M = A.shape[0]
     n = Xt.shape[0]
-    nat.call("mbem_gemm_bf16_t", ptr(A), A.stride(0), ptr(Xt), Xt.stride(0), M, K, n, ptr(out), out.stride(0),
-             stream_handle())
+    if not split:
+        nat.call("mbem_gemm_bf16_t", ptr(A), A.stride(0), ptr(Xt), Xt.stride(0), M, K, n, ptr(out),
+                 out.stride(0), stream_handle())
+        return out
+    need = nat.lib().mbem_gemm_bf16_workspace_size(M, n)
+    key = (A.device.index, need)
+    work = _split_work.get(key)
+    if work is None:
+        work = torch.empty(need // 4, dtype=torch.float32, device=A.device)
+        _split_work.clear()
+        _split_work[key] = work
+    nat.call("mbem_gemm_bf16_t_split", ptr(A), A.stride(0), ptr(Xt), Xt.stride(0), M, K, n, ptr(out),
+             out.stride(0), ptr(work), need, stream_handle())
     return out
 
 

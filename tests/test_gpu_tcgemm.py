@@ -37,3 +37,17 @@ def test_gemm_bf16_large_and_strided(gpu):
     R = _ref(A, Xt)
     assert float((out[:, :256] - R).abs().max() / R.abs().max()) < 3e-5
     assert torch.all(out[:, 256:] == 7.0)
+
+
+@pytest.mark.parametrize("M,K,n", [(1000, 4096, 256), (20736, 1024, 64), (200, 640, 16)])
+def test_gemm_split_k(gpu, M, K, n):
+    """The K-split product (partial sums in slice order) equals the product."""
+    from mbem_gb300.la.multirhs import gemm_bf16_t, gemm_check
+    g = torch.Generator(device="cuda").manual_seed(M + K + n)
+    A = torch.randn((M, K), generator=g, device="cuda").to(torch.bfloat16)
+    Xt = torch.randn((n, K), generator=g, device="cuda").to(torch.bfloat16)
+    out = torch.empty((n, M), device="cuda")
+    gemm_bf16_t(A, Xt, K, out, split=True)
+    gemm_check()
+    ref = (A.float() @ Xt.float().T).T
+    assert float((out - ref).abs().max() / ref.abs().max()) < 3e-5
