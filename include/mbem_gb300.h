@@ -375,6 +375,27 @@ size_t mbem_batch_residual_workspace_size(int64_t k, int64_t n);
 int mbem_batch_residual_mixed(const mbem_mixed_operator* op, const double* B, const double* X, int64_t k, double* R,
                               void* work, size_t work_bytes, void* stream);
 
+/* ---- mixed-precision stress readout of a nodal slip density (the elastic
+ * stress, DD minus the exact eigenstress: evaluate.py:383-407 with
+ * subtract_anelastic, tri_nodal.py:1131-1172): far pairs by FP32 quadrature
+ * of the mollified point kernel (3x3, 5x5, 8x8 collapsed Gauss rules for
+ * D / L above 12, above 6, below), near pairs (D <= near_factor max(eps, L))
+ * by the FP64 nodal machinery. Two calls: prepare writes the per-source
+ * records (mbem_readout_record_bytes), the per-observer near counts (n_obs)
+ * and their scan rowptr (n_obs + 1), and returns the number of near pairs in
+ * *n_near (host); evaluate takes near-pair buffers of that size (pair_obs
+ * int64, pair_src int32, pair_out 9 doubles each) and writes out (n_obs, 3, 3)
+ * (+)= alpha * stress. ------------------------------------------------- */
+size_t mbem_readout_record_bytes(int64_t n_src);
+int mbem_readout_prepare(const double* x, int64_t n_obs, const double* tri_verts, const double* normals,
+                         const double* eps, int64_t n_src, const double* density, int order, double near_factor,
+                         float* records, int64_t* counts, int64_t* rowptr, int64_t* n_near, void* stream);
+int mbem_readout_evaluate(const double* x, int64_t n_obs, const double* tri_verts, const double* normals,
+                          const double* eps, int64_t n_src, const double* density, double mu, double lam, int order,
+                          const float* records, const int64_t* rowptr, int64_t n_near, int64_t* pair_obs,
+                          int32_t* pair_src, double* pair_out, double alpha, int accumulate, double* out,
+                          void* stream);
+
 /* ---- deflated FGMRES on a dense operator (la/solver.py:115-245 fgmres,
  * wired as backends/hmat.py:678-690: P A P y = P b, P = I - Z Z^T with Z
  * the rigid-translation basis of backends/dense.py:190-208). ---------- */

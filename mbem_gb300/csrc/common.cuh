@@ -34,6 +34,11 @@ int nn_precond_apply(const void* state, const double* r, double* z, cudaStream_t
 int nodal_matrix(int kind, const double* x, int64_t nf, const double* tv, const double* normals,
                  const double* eps, int64_t ns, const double* coeffs, int order, double alpha,
                  int accumulate, double* out, int64_t ld, void* stream);
+// FP64 elastic (DD minus eigen) stress of listed (observer, source) pairs of a
+// nodal slip density, nine components per pair (the near pairs of a readout).
+int nodal_pairs_stress(const double* x, const double* tv, const double* normals, const double* eps,
+                       const double* density, double mu, double lam, int order, const int64_t* pair_obs,
+                       const int32_t* pair_src, int64_t n_pairs, double* out, cudaStream_t st);
 int nodal_contract(int kind, const double* x, int64_t nf, const double* tv, const double* normals,
                    const double* eps, int64_t ns, const double* density, const double* coeffs,
                    double mu, double lam, int order, double alpha, int accumulate, double* out,

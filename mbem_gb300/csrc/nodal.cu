@@ -1015,6 +1015,54 @@ nodal_traction_kernel(NodalArgs a, NodalSpec sp) {
     }
 }
 
+// Listed (observer, source) pairs of a readout: the FP64 elastic stress
+// (DD minus eigen) of the source's nodal slip density at the observer, nine
+// components per pair; the mixed-precision readout sends its near pairs here.
+__global__ void __launch_bounds__(ND_THREADS)
+nodal_pairs_stress_kernel(NodalArgs a, NodalSpec sp, const int64_t* __restrict__ pair_obs,
+                          const int32_t* __restrict__ pair_src, int64_t n_pairs, double* __restrict__ out) {
+    const int64_t p = (int64_t)blockIdx.x * ND_THREADS + threadIdx.x;
+    if (p >= n_pairs) return;
+    const int64_t f = pair_obs[p], s = pair_src[p];
+    double acc[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    NodalSrc g;
+    if (nodal_frame(a.tri_verts + 9 * s, g)) {
+        double W[4][ND_MAXK][5][5];
+        NodalScratch S;
+        const double eps = a.eps[s];
+        const double z = nodal_pair_tables(sp, g, a.x_field + 3 * f, eps, W, S);
+        const double* nrm = a.normals + 3 * s;
+        for (int k = 0; k < sp.K; k++) {
+            const double* d = a.density + 3 * (sp.K * s + k);
+            if (d[0] == 0.0 && d[1] == 0.0 && d[2] == 0.0) continue;
+            double sg[3][3];
+            node_stress(g, W, k, z, nrm, d, eps, a.mu, a.lam, 3, sg);
+            for (int m = 0; m < 3; m++)
+                for (int n = 0; n < 3; n++) acc[m][n] += sg[m][n];
+        }
+    }
+    for (int m = 0; m < 3; m++)
+        for (int n = 0; n < 3; n++) out[9 * p + 3 * m + n] = acc[m][n];
+}
+
+int nodal_pairs_stress(const double* x, const double* tv, const double* normals, const double* eps,
+                       const double* density, double mu, double lam, int order, const int64_t* pair_obs,
+                       const int32_t* pair_src, int64_t n_pairs, double* out, cudaStream_t st) {
+    MBEM_REQUIRE(order >= 0 && order <= 2, MBEM_ERR_ARG, "order must be 0, 1 or 2");
+    int e = ensure_rules();
+    if (e) return e;
+    const NodalSpec sp = make_spec(order, KF_H);
+    MBEM_REQUIRE(sp.valid, MBEM_ERR_UNSUPPORTED, "nodal degrees beyond the P2 tables");
+    if (n_pairs == 0) return MBEM_OK;
+    NodalArgs a;
+    memset(&a, 0, sizeof(a));
+    a.x_field = x; a.tri_verts = tv; a.normals = normals; a.eps = eps; a.density = density;
+    a.mu = mu; a.lam = lam;
+    nodal_pairs_stress_kernel<<<(unsigned)ceil_div(n_pairs, ND_THREADS), ND_THREADS, 0, st>>>(a, sp, pair_obs, pair_src,
+                                                                                          n_pairs, out);
+    return launch_status("nodal_pairs_stress_kernel");
+}
+
 static int flags_for_matrix(int kind) { return (kind == 0 || kind == 2) ? KF_T : KF_U; }
 
 int nodal_matrix(int kind, const double* x, int64_t nf, const double* tv, const double* normals,

@@ -239,3 +239,62 @@ def traction_matrix(x_field, n_field, tri_verts, normals, eps_arr, ids, n_cols, 
              ptr(ids_d), int(n_cols), float(mu), float(lam), order, _TRACTION_KINDS[which],
              float(alpha), ptr(res), res.stride(0), stream_handle())
     return res if out is not None else out_like(res, is_torch(x_field, tri_verts))
+
+
+def elastic_stress_readout(x_field, tri_verts, normals, eps_arr, density, mu, lam, order=0, near_factor=3.0,
+                           out=None, alpha=1.0, accumulate=False):
+    """The elastic stress (DD minus eigen) of a nodal slip density at many
+    points, mixed precision (FP32 quadrature far field, FP64 near pairs):
+    ``elastic_stress_contract``'s result to ~1e-6. The observers are ordered
+    along a Morton curve for the launch (neighbouring threads then take the
+    same quadrature rule), the result in the caller's order."""
+    import torch
+    K = n_nodes(order)
+    if order:
+        _check_shape(tri_verts)
+    x, tv, e, n = _geom(x_field, tri_verts, eps_arr, normals)
+    d = _density(density, K * tv.shape[0])
+    N = x.shape[0]
+    dev = x.device
+    # Morton order of the observers
+    lo = x.min(dim=0).values
+    span = torch.clamp(x.max(dim=0).values - lo, min=1e-300)
+    q = ((x - lo) / span * 1023.0).round().to(torch.int64).clamp(0, 1023)
+
+    def spread(v):
+        v = (v | (v << 16)) & 0x030000FF
+        v = (v | (v << 8)) & 0x0300F00F
+        v = (v | (v << 4)) & 0x030C30C3
+        return (v | (v << 2)) & 0x09249249
+    code = spread(q[:, 0]) | (spread(q[:, 1]) << 1) | (spread(q[:, 2]) << 2)
+    perm = torch.argsort(code)
+    xs = x.index_select(0, perm).contiguous()
+    ns = tv.shape[0]
+    rec = torch.empty(nat.lib().mbem_readout_record_bytes(ns) // 4, dtype=torch.float32, device=dev)
+    counts = torch.empty(max(N, 1), dtype=torch.int64, device=dev)
+    rowptr = torch.empty(N + 1, dtype=torch.int64, device=dev)
+    n_near = ctypes.c_int64(0)
+    st = stream_handle()
+    nat.call("mbem_readout_prepare", ptr(xs), N, ptr(tv), ptr(n), ptr(e), ns, ptr(d), order, float(near_factor),
+             ptr(rec), ptr(counts), ptr(rowptr), ctypes.byref(n_near), st)
+    m = max(int(n_near.value), 1)
+    pair_obs = torch.empty(m, dtype=torch.int64, device=dev)
+    pair_src = torch.empty(m, dtype=torch.int32, device=dev)
+    pair_out = torch.empty((m, 9), dtype=torch.float64, device=dev)
+    res = torch.empty((N, 3, 3), dtype=torch.float64, device=dev)
+    nat.call("mbem_readout_evaluate", ptr(xs), N, ptr(tv), ptr(n), ptr(e), ns, ptr(d), float(mu), float(lam), order,
+             ptr(rec), ptr(rowptr), int(n_near.value), ptr(pair_obs), ptr(pair_src), ptr(pair_out), 1.0, 0,
+             ptr(res), st)
+    full = torch.empty_like(res)
+    full[perm] = res
+    if out is not None:
+        o = out if isinstance(out, torch.Tensor) else None
+        if o is None:
+            raise TypeError("out must be a CUDA tensor")
+        if accumulate:
+            o += alpha * full
+        else:
+            o.copy_(alpha * full)
+        return o
+    full = alpha * full if alpha != 1.0 else full
+    return out_like(full, is_torch(x_field, tri_verts, density))

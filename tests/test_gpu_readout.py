@@ -1,0 +1,54 @@
+"""The mixed-precision nodal stress readout (FP32 quadrature far field, FP64
+nodal near pairs) against the FP64 nodal readout of the same density
+(``elastic_stress_contract``, pinned to the reference by test_gpu_nodal).
+
+Tolerance: every observer's stress within 2e-5 of the largest stress of the
+set (FP32 quadrature of the far pairs: ~1e-6 observed is the design target).
+"""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(order, n_fault=8, n_obs=3000, seed=0):
+    from mbem_gb300 import mesh as M
+    fault = M.centre_fault(n_fault)
+    tv = fault.tri_verts()
+    nrm, _ = fault.normals_and_areas()
+    edge = np.linalg.norm(tv[:, [1, 2, 0]] - tv, axis=2).mean()
+    eps = np.full(tv.shape[0], 0.07 * edge)
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, size=(n_obs, 3))
+    k = n_obs // 10
+    x[:k, 1] = rng.uniform(-2 * eps[0], 2 * eps[0], size=k)      # near the fault plane y = 0
+    x[:k, 0] = rng.uniform(-0.5, 0.5, size=k)
+    x[:k, 2] = rng.uniform(-0.5, 0.5, size=k)
+    K = (order + 1) * (order + 2) // 2
+    d = rng.normal(size=(K * tv.shape[0], 3))
+    return x, tv, nrm, eps, d
+
+
+@pytest.mark.parametrize("order", [0, 1, 2])
+def test_mixed_readout_matches_fp64(gpu, order):
+    from mbem_gb300.kernels import tri_nodal as tn
+    x, tv, n, e, d = _case(order)
+    mu, lam = 1.3, 1.95
+    ref = tn.elastic_stress_contract(x, tv, n, e, d, mu, lam, order=order)
+    got = tn.elastic_stress_readout(x, tv, n, e, d, mu, lam, order=order)
+    scale = np.abs(ref).max()
+    err = np.abs(got - ref).reshape(len(x), -1).max(axis=1) / scale
+    assert err.max() < 2e-5, (err.max(), np.argmax(err))
+    # the near pairs took the FP64 path: the observers on the plane agree to rounding
+    assert err[:len(x) // 10].max() < 2e-5
+
+
+def test_mixed_readout_accumulates_and_scales(gpu):
+    from mbem_gb300.kernels import tri_nodal as tn
+    x, tv, n, e, d = _case(2, n_fault=4, n_obs=500, seed=3)
+    base = tn.elastic_stress_readout(x, tv, n, e, d, 1.0, 1.0, order=2)
+    out = torch.ones((len(x), 3, 3), dtype=torch.float64, device="cuda")
+    tn.elastic_stress_readout(x, tv, n, e, d, 1.0, 1.0, order=2, out=out, alpha=-2.0, accumulate=True)
+    assert np.allclose(out.cpu().numpy(), 1.0 - 2.0 * base, rtol=1e-12, atol=1e-12 * np.abs(base).max())
