@@ -465,10 +465,50 @@ def fault_traction_workload(n_face=32, n_fault=24, dip=90.0):
     return out
 
 
+def p2_readout_workload(n_fault=64, n_obs=1_000_000, n_check=2000):
+    """Stress readout of a P2 fault (64 x 64, 8,192 triangles, 49,152 nodal
+    slips from default_rng(5)) at 1 M points uniform in [-1, 1]^3, 10 % of
+    them redrawn within 2 eps of the fault plane; eps = 0.07 x the smallest
+    mean edge. Mixed precision (FP32 quadrature far pairs, FP64 near pairs)
+    for all points; the FP64 nodal readout on n_check of them gives the error
+    and, scaled by the point count, the FP64 time."""
+    import torch
+    from mbem_gb300 import mesh as M
+    from mbem_gb300.kernels import tri_nodal as tn
+    fault = M.centre_fault(n_fault)
+    tv = fault.tri_verts()
+    nrm, _ = fault.normals_and_areas()
+    edge = np.linalg.norm(tv[:, [1, 2, 0]] - tv, axis=2).mean(axis=1)
+    eps_val = 0.07 * float(edge.min())
+    eps = np.full(tv.shape[0], eps_val)
+    slip = np.random.default_rng(5).normal(size=(6 * tv.shape[0], 3))
+    rng = np.random.default_rng(11)
+    x = rng.uniform(-1.0, 1.0, size=(n_obs, 3))
+    k = n_obs // 10
+    x[:k, 1] = rng.uniform(-2 * eps_val, 2 * eps_val, size=k)
+    dev = "cuda"
+    xt, tvt, nt, et, st_ = (torch.from_numpy(a).to(dev) for a in (x, tv, nrm, eps, slip))
+    for _ in range(2):      # warm-up, then timed
+        res, t_mixed = _sync_time(lambda: tn.elastic_stress_readout(xt, tvt, nt, et, st_, 1.0, 1.0, order=2))
+    idx = np.concatenate([np.arange(0, k, k // (n_check // 2)), np.arange(k, n_obs, (n_obs - k) // (n_check // 2))])
+    ref, t64 = _sync_time(lambda: tn.elastic_stress_contract(xt[idx], tvt, nt, et, st_, 1.0, 1.0, order=2))
+    got = res[idx]
+    scale = float(ref.abs().max())
+    err = (got - ref).abs().reshape(len(idx), -1).max(dim=1).values / scale
+    return {"config": {"n_fault": n_fault, "triangles": int(tv.shape[0]), "nodal_slips": int(6 * tv.shape[0]),
+                       "observers": n_obs, "eps": eps_val, "near_plane_fraction": 0.1},
+            "mixed_s": t_mixed, "pairs_per_s": n_obs * tv.shape[0] / t_mixed,
+            "fp64_s_for_check_points": t64, "fp64_s_extrapolated": t64 * n_obs / len(idx),
+            "speedup_vs_fp64": t64 * n_obs / len(idx) / t_mixed,
+            "check_points": int(len(idx)), "max_err_rel_to_max_stress": float(err.max()),
+            "median_err_rel_to_max_stress": float(err.median())}
+
+
 def extra_workloads(args, peaks):
     out = {}
     for name, fn in (("multi_rhs_cube24_256", lambda: multi_rhs_workload(peaks)),
-                     ("fault_traction_cube32_learned", fault_traction_workload)):
+                     ("fault_traction_cube32_learned", fault_traction_workload),
+                     ("p2_readout_1m", p2_readout_workload)):
         try:
             out[name] = fn()
         except Exception as err:     # one workload failing must not hide the headline
