@@ -494,14 +494,17 @@ def p2_readout_workload(n_fault=64, n_obs=1_000_000, n_check=2000):
     ref, t64 = _sync_time(lambda: tn.elastic_stress_contract(xt[idx], tvt, nt, et, st_, 1.0, 1.0, order=2))
     got = res[idx]
     scale = float(ref.abs().max())
-    err = (got - ref).abs().reshape(len(idx), -1).max(dim=1).values / scale
+    dev_abs = (got - ref).abs().reshape(len(idx), -1).max(dim=1).values
+    err = dev_abs / scale
+    own = dev_abs / torch.clamp(ref.abs().reshape(len(idx), -1).max(dim=1).values, min=1e-12 * scale)
     return {"config": {"n_fault": n_fault, "triangles": int(tv.shape[0]), "nodal_slips": int(6 * tv.shape[0]),
                        "observers": n_obs, "eps": eps_val, "near_plane_fraction": 0.1},
             "mixed_s": t_mixed, "pairs_per_s": n_obs * tv.shape[0] / t_mixed,
             "fp64_s_for_check_points": t64, "fp64_s_extrapolated": t64 * n_obs / len(idx),
             "speedup_vs_fp64": t64 * n_obs / len(idx) / t_mixed,
             "check_points": int(len(idx)), "max_err_rel_to_max_stress": float(err.max()),
-            "median_err_rel_to_max_stress": float(err.median())}
+            "median_err_rel_to_max_stress": float(err.median()),
+            "max_err_rel_to_own_stress": float(own.max()), "median_err_rel_to_own_stress": float(own.median())}
 
 
 def extra_workloads(args, peaks):

@@ -78,12 +78,18 @@ def _warn_near_boundary(points: np.ndarray, region: Region) -> None:
 
 def evaluate_stress(model: RegionModel, region, solution: dict, points, eps,
                     subtract_anelastic: bool = True, warn_near: bool = True, parts: bool = False,
-                    near=None):
+                    near=None, precision: str = "fp64"):
     """Stress (N, 3, 3) at ``points`` of ``region``; with ``parts`` also the
     summed eigenstress. ``near`` (continuous near-field recovery) is not part
-    of the GPU path."""
+    of the GPU path. ``precision="mixed"``: the double layers' elastic stress
+    by FP32 quadrature for the far pairs and FP64 for the near ones (within
+    ~1e-6 of the FP64 readout; subtract_anelastic only)."""
     if near is not None:
         raise NotImplementedError("near-field recovery (near=) is not on the GPU readout path")
+    if precision not in ("fp64", "mixed"):
+        raise ValueError(f"precision must be 'fp64' or 'mixed' (got {precision!r})")
+    if precision == "mixed" and not subtract_anelastic:
+        raise NotImplementedError("the mixed readout evaluates the elastic stress (subtract_anelastic=True)")
     region = _region(model, region)
     torch_in = is_torch(points)
     pts = as_cuda(points).reshape(-1, 3)
@@ -97,7 +103,10 @@ def evaluate_stress(model: RegionModel, region, solution: dict, points, eps,
     def double_layer(patch, jump, sigma):
         tv, nrm, e = _src(patch, eps)
         d = as_cuda(np.asarray(jump, float).reshape(-1, 3))
-        if subtract_anelastic:
+        if subtract_anelastic and precision == "mixed":
+            tn.elastic_stress_readout(pts, tv, nrm, e, d, mu, lam, patch.order, out=sig, alpha=-sigma,
+                                      accumulate=True)
+        elif subtract_anelastic:
             tn.elastic_stress_contract(pts, tv, nrm, e, d, mu, lam, patch.order, out=sig,
                                        alpha=-sigma, accumulate=True)
         else:

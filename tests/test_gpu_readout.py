@@ -52,3 +52,18 @@ def test_mixed_readout_accumulates_and_scales(gpu):
     out = torch.ones((len(x), 3, 3), dtype=torch.float64, device="cuda")
     tn.elastic_stress_readout(x, tv, n, e, d, 1.0, 1.0, order=2, out=out, alpha=-2.0, accumulate=True)
     assert np.allclose(out.cpu().numpy(), 1.0 - 2.0 * base, rtol=1e-12, atol=1e-12 * np.abs(base).max())
+
+
+def test_evaluate_stress_mixed_matches_fp64(gpu, cube_small):
+    """evaluate_stress(precision="mixed") on the small cube's solution."""
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.evaluate import evaluate_stress
+    from mbem_gb300.model import generate_system
+    g = cube_small
+    model, eps = cube_fault_model(int(g["n_face"]), int(g["n_fault"]), float(g["mu"]), float(g["lam"]))
+    asm = DenseBackend(jump="calibrated", deflate=True, rtol=1e-12).assemble(generate_system(model), eps)
+    sol = asm.solve()
+    ref = evaluate_stress(model, "body", sol, g["points"], eps, warn_near=False)
+    got = evaluate_stress(model, "body", sol, g["points"], eps, warn_near=False, precision="mixed")
+    assert np.abs(got - ref).max() < 2e-5 * np.abs(ref).max()
