@@ -6,7 +6,9 @@ HBM), the calibration row sums and free-term diagonal, the fault right-hand
 side, then deflated FGMRES(50) on the device to a true relative residual of
 1e-8. The headline (``--precision mixed``, default) is the mixed-precision
 operator (FP32 quadrature far field, FP64 closed-form near field; its
-residual evaluated in double-float); the plain FP64 path on the same
+residual evaluated in double-float), solved by flexible FGMRES whose
+preconditioner is a GMRES solve on the far field rounded to BF16 (written by
+the same assembly pass); the plain FP64 path on the same
 workload is timed beside it (``fp64_path``) for the mixed/FP64 ratio the
 metric names. ``value`` is seconds per solve with the mesh arrays already
 resident in HBM; ``e2e`` is the same through the public API from host numpy
@@ -187,6 +189,7 @@ def _timed_steps(step, steps, ws):
 def run_ours(args, rank, ws):
     import torch
     from mbem_gb300 import _native as nat
+    from mbem_gb300 import defaults
     from mbem_gb300.backends.dense import DenseBackend
     from mbem_gb300.cases import cube_fault_model
     from mbem_gb300.model import generate_system
@@ -201,7 +204,7 @@ def run_ours(args, rank, ws):
 
     def make_step(precision, timer=None):
         backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART,
-                               precision=precision)
+                               precision=precision, precond=_precond_for(precision))
 
         def step():
             asm = backend.assemble(system, eps, arrays=arrays, timer=timer)
@@ -219,10 +222,13 @@ def run_ours(args, rank, ws):
     for _ in range(args.warmup):
         step()
     timer.clear()
+    from mbem_gb300.la.mixed import inner_stats
+    inner_stats(timing=True)
     launches0 = nat.lib().mbem_launch_count()
     with ClockSampler(local) as clk:
         dev_s, wall, res = _timed_steps(step, args.steps, ws)
     launches = nat.lib().mbem_launch_count() - launches0
+    inner_steps, inner_solves, inner_ms = inner_stats(timing=False)
     rep, nnz = res[-1]
 
     # the plain FP64 path on the same workload, for the ratio the metric names
@@ -247,7 +253,7 @@ def run_ours(args, rank, ws):
         host_cube = M.cube(cfg["n_face"])
         host_fault = M.centre_fault(cfg["n_fault"])
         backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART,
-                               precision=args.precision)
+                               precision=args.precision, precond=_precond_for(args.precision))
 
         def e2e_step():
             cube_p = Patch("cube", host_cube, BCType.FREE_TRACTION)
@@ -284,12 +290,25 @@ def run_ours(args, rank, ws):
         mv_bytes = 8.0 * n * n + 16.0 * n
         kernel = "dgemv_vec_kernel"
     achieved = mv_bytes / (mv_ms / 1e3) / 1e9
+    peak_source = ("MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks.get("hbm_gbs")
+                   else "fallback 6.8 TB/s (of fallback)")
     roofline = {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak,
                 "traffic": TRAFFIC_OVER_ALGORITHMIC * mv_bytes if args.precision == "mixed" else None,
                 "bytes_per_launch": mv_bytes, "launch_ms": mv_ms, "launches_per_step": rep.matvecs,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks.get("hbm_gbs")
-                else "fallback 6.8 TB/s (of fallback)"}
+                "peak_source": peak_source}
+    roofline_outer = None
+    if args.precision == "mixed" and inner_steps > 0:
+        # the inner BF16 product dominates the solve: the BF16 far field once
+        # (2 B an entry), the FP64 near blocks, x (FP32) read, y written
+        b16 = 2.0 * n * n + 80.0 * nnz + 12.0 * n
+        ms16 = inner_ms / inner_steps
+        a16 = b16 / (ms16 / 1e3) / 1e9
+        roofline_outer = roofline
+        roofline = {"kernel": "BF16 inner matvec (d2f + sgemv_bf16_tma_kernel + near_matvec_kernel)",
+                    "bound": "hbm", "achieved": a16, "peak": hbm_peak, "unit": "GB/s", "frac": a16 / hbm_peak,
+                    "traffic": TRAFFIC_OVER_ALGORITHMIC * b16, "bytes_per_launch": b16, "launch_ms": ms16,
+                    "launches_per_step": inner_steps / args.steps, "peak_source": peak_source}
     asm_ms = [s.elapsed_time(e) for (k, nf, ns, s, e) in timer]
     line = {
         "metric": METRIC,
@@ -305,12 +324,17 @@ def run_ours(args, rank, ws):
         "dtype": "f64",
         "data": "synthetic (seeded mesh generators; no dataset)",
         "config": {"workload": args.workload, "n_face": cfg["n_face"], "n_fault": cfg["n_fault"],
-                   "unknowns": n, "precision": args.precision, "solver": f"deflated FGMRES({RESTART})",
+                   "unknowns": n, "precision": args.precision,
+                   "solver": f"deflated FGMRES({RESTART})" + (
+                       f", BF16 inner GMRES (<= {defaults.MIXED_INNER_ITERATIONS} steps to "
+                       f"{defaults.MIXED_INNER_RTOL:g}) as flexible preconditioner"
+                       if args.precision == "mixed" else ""),
                    "rtol": RTOL, "parallelism": "replicas" if ws > 1 else "single",
                    "l2": "inputs larger than L2 (A = %.1f GB FP32 far field)" % (4.0 * n * n / 1e9)
                    if args.precision == "mixed" else
                    "inputs larger than L2 (A = %.1f GB FP64)" % (8.0 * n * n / 1e9)},
         "iterations": rep.iterations,
+        "inner_steps_per_step": inner_steps / args.steps,
         "true_relres": rep.true_relres,
         "wall_s_per_step": wall,
         "matvec_ms_per_step": rep.matvec_ms,
@@ -319,6 +343,7 @@ def run_ours(args, rank, ws):
         "e2e": e2e,
         "gpu_launches": int(launches),
         "roofline": roofline,
+        "roofline_outer_matvec": roofline_outer,
         "fp64_peak_tflops": fp64_peak_tflops(),
     }
     clocks = clk.summary()
@@ -327,8 +352,17 @@ def run_ours(args, rank, ws):
     if not args.skip_extra:
         line["workloads"] = extra_workloads(args, peaks)
     if rank == 0 and not args.skip_cpu:
-        line["cpu_baseline"] = cpu_baseline(args, rep.iterations)
+        # the reference's own solve is plain FGMRES: its iteration count is
+        # that of the FP64 path (the headline's outer count is not)
+        line["cpu_baseline"] = cpu_baseline(args, fp64["iterations"] if fp64 else
+                                            PLAIN_ITERATIONS.get(args.workload, ITER_GUESS))
     return line
+
+
+def _precond_for(precision):
+    """The headline solve's preconditioner: the BF16 inner solve for the
+    mixed operator, none for FP64 (the reference's plain FGMRES)."""
+    return "bf16_inner" if precision == "mixed" else None
 
 
 def _sync_time(fn):
@@ -579,10 +613,11 @@ def run_reference(args, rank, ws):
     from oracle import oracle as orc
     orc.lib()
     vals = []
+    its = PLAIN_ITERATIONS.get(args.workload, ITER_GUESS)
     for _ in range(args.warmup):
-        cpu_baseline(args, ITER_GUESS)
+        cpu_baseline(args, its)
     for _ in range(args.steps):
-        vals.append(cpu_baseline(args, ITER_GUESS))
+        vals.append(cpu_baseline(args, its))
     v = float(np.mean([b["value"] for b in vals]))
     base = vals[-1]
     cfg = WORKLOADS[args.workload]
@@ -598,9 +633,12 @@ def run_reference(args, rank, ws):
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-# FGMRES(50) iterations of the reference on the calibrated cube (the
-# reference took 20 to 1e-8 at n = 12); the CPU arm has no solve of its own
-# to count, so it uses this figure for the matvec count.
+# FGMRES(50) iterations to 1e-8 of the reference's plain solve on the
+# calibrated cube: 20 at n = 12 (the reference itself), 27 at n = 48 (the
+# FP64 path here, whose counts equal the reference's at n = 12); n = 24 is
+# taken between them. The CPU arm has no solve of its own to count, so it
+# uses these for the matvec count.
+PLAIN_ITERATIONS = {"cube12": 20, "cube24": 24, "cube48": 27}
 ITER_GUESS = 20
 
 

@@ -169,6 +169,12 @@ int mbem_far_matrix(int kernel, const double* x_field, int64_t n_field, const do
                     const double* normals, const double* eps, int64_t n_src, const double* coeffs,
                     double near_factor, double alpha, float* out, int64_t ld_out, uint32_t* near_mask,
                     void* stream);
+/* The same, also writing out16 = BF16(out) (round to nearest even) at ld16:
+ * the inner operator's copy, made by the assembly with no extra pass. */
+int mbem_far_matrix_bf16(int kernel, const double* x_field, int64_t n_field, const double* tri_verts,
+                         const double* normals, const double* eps, int64_t n_src, const double* coeffs,
+                         double near_factor, double alpha, float* out, int64_t ld_out, uint16_t* out16,
+                         int64_t ld16, uint32_t* near_mask, void* stream);
 /* Near list from that bit mask: rowptr (n_field+1) and nnz on the host
  * (synchronises `stream`), then the source indices in increasing order. */
 int mbem_near_mask_count(const uint32_t* mask, int64_t n_field, int64_t n_src, int64_t* rowptr,
@@ -212,6 +218,43 @@ int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y,
  * It has no counterpart in the reference. */
 int mbem_mixed_matvec_noalloc(const mbem_mixed_operator* op, const double* x, double* y,
                               void* stream);
+
+/* ---- BF16 inner operator and inner solve (the mixed-precision
+ * preconditioner). A16 is the mixed operator's FP32 far field rounded to
+ * BF16 (round to nearest even; BF16 keeps FP32's exponent range, so no block
+ * scales are needed); the near blocks stay FP64.
+ * y = A16 x + near blocks x, FP32 row sums; work: n_cols floats. */
+int mbem_bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_cols, int n_near,
+                     const mbem_near_blocks* near, const double* x, double* y, void* work, size_t work_bytes,
+                     void* stream);
+
+/* z = the iterate after `iterations` steps of GMRES from zero on
+ * P (A16 + near) P z = P r (P: the deflation of params->u_ranges), as a
+ * flexible right preconditioner of FGMRES on the accurate operator: the inner
+ * steps read 2 bytes per far entry, the outer ones 4. The Arnoldi steps run
+ * on the device; the host reads the Hessenberg matrix once per application
+ * (rtol = 0) or one column per step (rtol > 0, to stop early). */
+#define MBEM_INNER_MAX_ITERS 64
+typedef struct {
+    int64_t n;                      /* system size (square) */
+    const uint16_t* A16;            /* (n, ld16) row-major BF16, 16-byte aligned */
+    int64_t ld16;                   /* multiple of 8 */
+    int n_near;
+    const mbem_near_blocks* near;   /* HOST array of n_near FP64 near-block lists */
+    int iterations;                 /* at most this many steps, 1..MBEM_INNER_MAX_ITERS */
+    double rtol;                    /* > 0: stop once the inner residual estimate is below rtol |P r|
+                                       (one host read per step); 0: all steps, one read in total */
+    int n_u_ranges;                 /* deflation ranges, as in mbem_fgmres_params */
+    const int64_t* u_ranges;
+    void* work;                     /* mbem_inner_bf16_workspace_size(n, iterations) bytes */
+    size_t work_bytes;
+} mbem_inner_bf16;
+size_t mbem_inner_bf16_workspace_size(int64_t n, int iterations);
+int mbem_inner_bf16_apply(const mbem_inner_bf16* p, const double* r, double* z, void* stream);
+/* Inner steps, applications and (when timed) the device time of their BF16
+ * products in ms since the last call; resets them and sets whether the
+ * following applications time their products with CUDA events. */
+void mbem_inner_bf16_stats(int timing, int64_t* steps, int64_t* applies, double* matvec_ms);
 
 /* ---- cluster block-Jacobi preconditioner (la/preconditioner.py:421-470,
  * the "block_jacobi" rung; chunks from la/cluster.py:56-75 bisection, built
@@ -408,9 +451,11 @@ typedef struct {
     int n_u_ranges;         /* deflation: number of (offset, size) u-slot ranges, 0 = none */
     const int64_t* u_ranges;/* HOST array of 2*n_u_ranges int64 */
     int precond;            /* 0 none, 1 block-Jacobi (state: const mbem_block_jacobi*),
-                               2 learned (state: const mbem_nn_precond*) */
+                               2 learned (state: const mbem_nn_precond*),
+                               3 BF16 inner solve (state: const mbem_inner_bf16*) */
     const void* precond_state; /* the preconditioner object for precond != 0 (host pointer) */
     int time_matvec;        /* 1: time every operator application with CUDA events */
+    int x_is_zero;          /* 1: x is zero on entry (skips the first product); 0: x is the initial guess */
 } mbem_fgmres_params;
 
 typedef struct {

@@ -39,7 +39,8 @@ class FgmresParams(Structure):
     _fields_ = [("restart", c_int), ("maxiter", c_int), ("rtol", c_double),
                 ("stagnation_window", c_int), ("stagnation_factor", c_double),
                 ("n_u_ranges", c_int), ("u_ranges", POINTER(c_int64)),
-                ("precond", c_int), ("precond_state", c_void_p), ("time_matvec", c_int)]
+                ("precond", c_int), ("precond_state", c_void_p), ("time_matvec", c_int),
+                ("x_is_zero", c_int)]
 
 
 class FgmresReport(Structure):
@@ -70,6 +71,14 @@ class NnPrecond(Structure):
     _fields_ = [("n", c_int64), ("n_coarse", c_int64), ("bj", POINTER(BlockJacobi)), ("basis", c_void_p),
                 ("APhi", c_void_p), ("Ac_inv", c_void_p), ("work", c_void_p)]
 
+
+class InnerBf16(Structure):
+    _fields_ = [("n", c_int64), ("A16", c_void_p), ("ld16", c_int64), ("n_near", c_int),
+                ("near", POINTER(NearBlocks)), ("iterations", c_int), ("rtol", c_double), ("n_u_ranges", c_int),
+                ("u_ranges", c_void_p), ("work", c_void_p), ("work_bytes", c_size_t)]
+
+
+INNER_MAX_ITERS = 64
 
 NN_FEAT, NN_HIDDEN = 16, 32
 NN_PARAMS = NN_HIDDEN * NN_FEAT + NN_HIDDEN + NN_HIDDEN * NN_HIDDEN + NN_HIDDEN + 9 * NN_HIDDEN + 9
@@ -144,6 +153,7 @@ _SIGNATURES = {
     "mbem_fgmres_mixed": (c_int, [POINTER(MixedOperator), _P, _P, POINTER(FgmresParams), _P, c_size_t,
                                   POINTER(FgmresReport), _P]),
     "mbem_far_matrix": (c_int, [c_int, _P, _I, _P, _P, _P, _I, _P, _D, _D, _P, _I, _P, _P]),
+    "mbem_far_matrix_bf16": (c_int, [c_int, _P, _I, _P, _P, _P, _I, _P, _D, _D, _P, _I, _P, _I, _P, _P]),
     "mbem_near_mask_count": (c_int, [_P, _I, _I, _P, _P, c_size_t, POINTER(c_int64), _P]),
     "mbem_near_mask_fill": (c_int, [_P, _I, _I, _P, _P, _P]),
     "mbem_near_list_workspace_size": (c_size_t, [_I]),
@@ -153,6 +163,10 @@ _SIGNATURES = {
     "mbem_mixed_rowsum3": (c_int, [_P, _I, _I, _I, _P, _P, _P, _P]),
     "mbem_near_add_diagonal": (c_int, [_P, _P, _P, _I, _P, _P, _P]),
     "mbem_mixed_matvec": (c_int, [POINTER(MixedOperator), _P, _P, _P, c_size_t, _P]),
+    "mbem_bf16_matvec": (c_int, [_P, _I, _I, _I, c_int, POINTER(NearBlocks), _P, _P, _P, c_size_t, _P]),
+    "mbem_inner_bf16_workspace_size": (c_size_t, [_I, c_int]),
+    "mbem_inner_bf16_apply": (c_int, [POINTER(InnerBf16), _P, _P, _P]),
+    "mbem_inner_bf16_stats": (None, [c_int, POINTER(c_int64), POINTER(c_int64), POINTER(c_double)]),
     "mbem_mixed_matvec_noalloc": (c_int, [POINTER(MixedOperator), _P, _P, _P]),
 }
 

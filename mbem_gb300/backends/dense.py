@@ -44,8 +44,11 @@ class DenseBackend:
                  maxiter: int = defaults.GMRES_MAXITER, precision: str = "fp64",
                  near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, precond: str | None = None):
         """``precond``: None (plain FGMRES, the reference's dense-backend
-        solve) or "block_jacobi" (la/preconditioner.py:421-470 cluster
-        block-Jacobi, built on first solve). ``precision="fp64"``: every entry by the FP64 closed form, the
+        solve), "block_jacobi" (la/preconditioner.py:421-470 cluster
+        block-Jacobi, built on first solve) or, with ``precision="mixed"``,
+        "bf16_inner" (a few GMRES steps on the far field rounded to BF16 as a
+        flexible preconditioner; the outer FGMRES keeps the FP32 operator).
+        ``precision="fp64"``: every entry by the FP64 closed form, the
         reference's operator. ``"mixed"``: pairs beyond near_factor *
         max(eps, h) of the source by FP32 quadrature (stored FP32), the near
         pairs by the FP64 closed form (stored as 3x3 blocks); the solve's
@@ -66,8 +69,10 @@ class DenseBackend:
         self.maxiter = maxiter
         self.precision = precision
         self.near_factor = near_factor
-        if precond not in (None, "block_jacobi"):
-            raise ValueError(f"precond must be None or 'block_jacobi' (got {precond!r})")
+        if precond not in (None, "block_jacobi", "bf16_inner"):
+            raise ValueError(f"precond must be None, 'block_jacobi' or 'bf16_inner' (got {precond!r})")
+        if precond == "bf16_inner" and precision != "mixed":
+            raise ValueError("precond='bf16_inner' needs precision='mixed'")
         self.precond = precond
 
     def assemble(self, system: BlockSystem, eps, arrays: dict | None = None,
@@ -127,6 +132,7 @@ class AssembledDense:
         self.near_factor = near_factor
         self.precond = precond
         self._bj = None
+        self._inner = None
         self.op = None
         self.system = system
         self.layout = system.layout
@@ -193,7 +199,7 @@ class AssembledDense:
         return res.reshape(rows // 3, 3, 3)
 
     # -- mixed precision: FP32 far field + FP64 near blocks -------------
-    def _mixed_block(self, far_out, q, p, kernel, material, alpha, row0, col0):
+    def _mixed_block(self, far_out, q, p, kernel, material, alpha, row0, col0, far16_out=None):
         from ..la.mixed import far_near_block
         if p.order != 0 or q.order != 0:
             raise NotImplementedError("the mixed-precision operator is P0 (order 0) only")
@@ -204,10 +210,10 @@ class AssembledDense:
         if kernel == KERNEL_T:
             coeffs = kb.t_coeffs(material.mu, material.lam)
             return far_near_block("T", f["coll"], s["tv"], s["normals"], s["eps"], coeffs, alpha, far_out,
-                                  row0, col0, self.near_factor, self._timer)
+                                  row0, col0, self.near_factor, self._timer, far16_out)
         coeffs = kb.u_coeffs(material.mu, material.lam)
         return far_near_block("U", f["coll"], s["tv"], s["normals"], s["eps"], coeffs, alpha, far_out, row0,
-                              col0, self.near_factor, self._timer)
+                              col0, self.near_factor, self._timer, far16_out)
 
     def _build_mixed(self):
         from ..la.mixed import MixedOperator
@@ -220,14 +226,19 @@ class AssembledDense:
         if any(v > 1 for v in counts.values()):
             raise NotImplementedError("mixed precision: two terms on one block")
         covered = sum(t.row.size * t.col.size for t in self.system.terms)
-        A32 = (torch.empty if covered == n * n else torch.zeros)((n, n), dtype=torch.float32, device=dev)
-        op = MixedOperator(A32, [])
+        alloc = torch.empty if covered == n * n else torch.zeros
+        A32 = alloc((n, n), dtype=torch.float32, device=dev)
+        # the BF16 inner operator's copy, written by the same far-field pass
+        A16 = (alloc((n, (n + 7) // 8 * 8), dtype=torch.bfloat16, device=dev)
+               if self.precond == "bf16_inner" else None)
+        op = MixedOperator(A32, [], A16)
         placed = {}
         for t in self.system.terms:
             mat = self.materials[t.region.name]
             view = A32[t.row.offset:t.row.stop, t.col.offset:t.col.stop]
+            view16 = None if A16 is None else A16[t.row.offset:t.row.stop, t.col.offset:t.col.stop]
             nl = self._mixed_block(view, t.field_patch, t.source_patch, t.kernel, mat, t.scale, t.row.offset,
-                                   t.col.offset)
+                                   t.col.offset, view16)
             op.near.append(nl)
             placed[(id(t.field_patch), id(t.source_patch), t.kernel, id(mat))] = (t, nl)
 
@@ -400,6 +411,22 @@ class AssembledDense:
             self._bj = bj.build_mixed(self.op) if self.op is not None else bj.build_dense(self.A)
         return self._bj
 
+    def bf16_inner(self, iterations: int | None = None, rtol: float | None = None):
+        """The BF16 inner-solve preconditioner of the mixed operator (the
+        BF16 copy of the far field is made once)."""
+        from ..la.mixed import Bf16Inner
+        if self.op is None:
+            raise ValueError("the BF16 inner solve needs the mixed-precision operator")
+        it = defaults.MIXED_INNER_ITERATIONS if iterations is None else iterations
+        tol = defaults.MIXED_INNER_RTOL if rtol is None else rtol
+        if self._inner is None:
+            self._inner = Bf16Inner(self.op, it, self.u_ranges(), tol)
+        self._inner.set_iterations(it)
+        if not 0.0 <= tol < 1.0:
+            raise ValueError(f"rtol must be in [0, 1) (got {tol})")
+        self._inner.rtol = float(tol)
+        return self._inner
+
     def solve_device(self, rtol: float | None = None, restart: int | None = None,
                      maxiter: int | None = None, x0=None, time_matvec: bool = False,
                      precond=None) -> torch.Tensor:
@@ -412,6 +439,8 @@ class AssembledDense:
             precond = None
         elif precond == "block_jacobi":
             precond = self.block_jacobi()
+        elif precond == "bf16_inner":
+            precond = self.bf16_inner()
         kw = dict(x0=x0, rtol=self.rtol if rtol is None else rtol,
                   restart=self.restart if restart is None else restart,
                   maxiter=self.maxiter if maxiter is None else maxiter, u_ranges=self.u_ranges(),

@@ -20,7 +20,8 @@ int launch_status(const char* what, int n_launched = 1);
 // Counts kernel launches whose status is checked later.
 void count_launches(int n);
 
-// z = M^-1 r for the FGMRES preconditioners (kind 1 block-Jacobi, 2 learned).
+// z = M^-1 r for the FGMRES preconditioners (kind 1 block-Jacobi, 2 learned,
+// 3 BF16 inner solve).
 int bj_apply(const mbem_block_jacobi* bj, const double* r, double* z, cudaStream_t st);
 // y = alpha A x + beta y (FP64 row-major at ld)
 int dgemv(const double* A, int64_t ld, int64_t n_rows, int64_t n_cols, const double* x, double alpha,
@@ -47,6 +48,13 @@ int nodal_contract(int kind, const double* x, int64_t nf, const double* tv, cons
 // y = A x for the mixed operator; xh, xl: n floats each (scratch).
 int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, float* xh, float* xl,
                  cudaStream_t st);
+
+// y = A16 x + near blocks x (BF16 far field, FP32 sums; FP64 near blocks);
+// xf: n_cols floats of scratch (16-byte aligned).
+int bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_cols, int n_near,
+                const mbem_near_blocks* near, const double* x, double* y, float* xf, cudaStream_t st);
+// z = the BF16 inner GMRES solve of r (precond kind 3).
+int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t st);
 
 // MBEM_ERR_WAIT if a bounded pipeline wait of the mixed matvec gave up since
 // the last check; synchronises `st`.

@@ -431,6 +431,12 @@ struct Fgmres {
         }
         pending.clear();
     }
+    ~Fgmres() {
+        for (auto& p : pending) {
+            cudaEventDestroy(p.first);
+            cudaEventDestroy(p.second);
+        }
+    }
     bool time_matvec = false;
     int matvecs = 0;
     double matvec_ms = 0.0;
@@ -457,6 +463,185 @@ struct Fgmres {
     }
     int norm2(const double* v, double* out_dev) { return multidot(v, 1, v, out_dev, 0); }
 };
+
+// ---------------------------------------------------------------------------
+// The BF16 inner solve (precond kind 3): up to `k` GMRES steps from zero on
+// P (A16 + near) P. The Arnoldi steps (CGS2, as in FGMRES) write each
+// Hessenberg column straight into device memory. With rtol = 0 the k steps
+// run with no host synchronisation and the host reads the (k+1) x k matrix
+// once; with rtol > 0 it reads each new column, applies the Givens rotations
+// as it goes and stops once the residual estimate is below rtol |P r|. Then
+// z = V y from the small least-squares solution. A column whose new norm is
+// zero (an invariant Krylov space) ends the basis.
+// ---------------------------------------------------------------------------
+__global__ void add_vec_kernel(double* __restrict__ h, const double* __restrict__ d, int k) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < k) h[i] += d[i];
+}
+
+// inner steps and applications since the last mbem_inner_bf16_stats call,
+// and (when timing is on) the device time of their BF16 products
+static int64_t g_inner_steps = 0, g_inner_applies = 0;
+static int g_inner_timing = 0;
+static double g_inner_matvec_ms = 0.0;
+
+struct InnerWork {
+    double* V;        // (k+1, n)
+    double* w;        // n
+    double* partial;  // nblocks * (k+1)
+    double* H;        // k columns of (k+2): h[0..j], |w|^2 at j+1; then beta^2
+    double* h2;       // k+1
+    double* y;        // k
+    float* xf;        // n
+    double* proj;     // 3 * PROJ_BLOCKS
+};
+
+static size_t inner_layout(int64_t n, int k, char* base, InnerWork* w) {
+    const int64_t nb = ceil_div(n, KV_COLS);
+    size_t off = 0;
+    auto take = [&](size_t count) {
+        char* p = base ? base + off : nullptr;
+        off += align_up(count * sizeof(double));
+        return reinterpret_cast<double*>(p);
+    };
+    InnerWork t;
+    t.V = take((size_t)(k + 1) * n);
+    t.w = take(n);
+    t.partial = take((size_t)nb * (k + 2));
+    t.H = take((size_t)(k + 1) * (k + 2));
+    t.h2 = take(k + 1);
+    t.y = take(k);
+    t.xf = reinterpret_cast<float*>(take((n + 1) / 2));
+    t.proj = take(3 * PROJ_BLOCKS);
+    if (w) *w = t;
+    return off;
+}
+
+int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t st) {
+    const mbem_inner_bf16* p = static_cast<const mbem_inner_bf16*>(state);
+    MBEM_REQUIRE(p && p->A16 && p->n > 0 && p->ld16 >= p->n, MBEM_ERR_ARG, "bad BF16 inner solve");
+    const int k = p->iterations;
+    MBEM_REQUIRE(k >= 1 && k <= MBEM_INNER_MAX_ITERS, MBEM_ERR_ARG, "inner iterations must be in [1, %d]",
+                 MBEM_INNER_MAX_ITERS);
+    MBEM_REQUIRE(p->rtol >= 0.0 && p->rtol < 1.0, MBEM_ERR_ARG, "inner rtol must be in [0, 1)");
+    const int64_t n = p->n;
+    const size_t need = inner_layout(n, k, nullptr, nullptr);
+    MBEM_REQUIRE(p->work && p->work_bytes >= need, MBEM_ERR_SIZE, "inner workspace %zu < %zu bytes",
+                 p->work_bytes, need);
+    InnerWork I;
+    inner_layout(n, k, (char*)p->work, &I);
+    Fgmres F;
+    F.A = nullptr; F.mop = nullptr; F.ld = 0; F.n = n; F.st = st;
+    F.nb = ceil_div(n, KV_COLS);
+    int e = make_ranges(p->u_ranges, p->n_u_ranges, F.ur);
+    if (e) return e;
+    F.deflate = p->n_u_ranges > 0;
+    F.W.partial = I.partial;
+    F.W.proj = I.proj;
+    const int ldh = k + 2;
+    double* beta2 = I.H + (size_t)k * ldh;
+    const unsigned gn = (unsigned)ceil_div(n, 256);
+    const bool adaptive = p->rtol > 0.0;
+
+    if ((e = F.proj(r, I.w))) return e;
+    if ((e = F.norm2(I.w, beta2))) return e;
+    scale_by_rnorm_kernel<<<gn, 256, 0, st>>>(I.w, I.V, n, beta2);
+    count_launches(1);
+    cudaMemsetAsync(z, 0, n * sizeof(double), st);
+    double beta = -1.0;
+    if (adaptive) {
+        cudaMemcpyAsync(&beta, beta2, sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
+        beta = sqrt(beta);
+        if (!(beta > 0.0)) return launch_status("inner solve zero rhs", 0);
+    }
+    // Givens least squares min |beta e1 - Hbar y| (la/solver.py:188-210),
+    // one column at a time; returns true when the basis ends at column j
+    std::vector<double> R((size_t)k * k, 0.0), g(k + 1, 0.0), cs(k), sn(k), y(k, 0.0);
+    int used = 0;
+    auto absorb = [&](int j, const double* hc) -> bool {
+        std::vector<double> col(j + 2);
+        for (int i = 0; i <= j; i++) col[i] = hc[i];
+        col[j + 1] = sqrt(fmax(hc[j + 1], 0.0));
+        for (int i = 0; i < j; i++) {
+            const double a = col[i], b = col[i + 1];
+            col[i] = cs[i] * a + sn[i] * b;
+            col[i + 1] = -sn[i] * a + cs[i] * b;
+        }
+        const double den = sqrt(col[j] * col[j] + col[j + 1] * col[j + 1]);
+        if (den == 0.0) return true;
+        cs[j] = col[j] / den;
+        sn[j] = col[j + 1] / den;
+        col[j] = den;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        for (int i = 0; i <= j; i++) R[(size_t)i * k + j] = col[i];
+        used = j + 1;
+        if (col[j + 1] == 0.0) return true;                         // invariant Krylov space: exact
+        return adaptive && fabs(g[j + 1]) < p->rtol * beta;
+    };
+    if (adaptive) g[0] = beta;
+    std::vector<double> hcol(k + 2);
+    for (int j = 0; j < k; j++) {
+        const double* vj = I.V + (int64_t)j * n;
+        double* hc = I.H + (size_t)j * ldh;
+        if (g_inner_timing) {
+            cudaEvent_t ev[2];
+            cudaEventCreate(&ev[0]);
+            cudaEventCreate(&ev[1]);
+            cudaEventRecord(ev[0], st);
+            e = bf16_matvec(p->A16, p->ld16, n, n, p->n_near, p->near, vj, I.w, I.xf, st);
+            cudaEventRecord(ev[1], st);
+            F.pending.push_back({ev[0], ev[1]});
+            if (e) return e;
+        } else if ((e = bf16_matvec(p->A16, p->ld16, n, n, p->n_near, p->near, vj, I.w, I.xf, st))) {
+            return e;
+        }
+        if ((e = F.proj(I.w, I.w))) return e;
+        if ((e = F.multidot(I.V, j + 1, I.w, hc, 0))) return e;
+        if ((e = F.multiaxpy(I.w, I.V, j + 1, hc, -1.0))) return e;
+        if ((e = F.multidot(I.V, j + 1, I.w, I.h2, 0))) return e;
+        if ((e = F.multiaxpy(I.w, I.V, j + 1, I.h2, -1.0))) return e;
+        add_vec_kernel<<<1, 64, 0, st>>>(hc, I.h2, j + 1);
+        count_launches(1);
+        if ((e = F.norm2(I.w, hc + (j + 1)))) return e;
+        if (adaptive) {
+            cudaMemcpyAsync(hcol.data(), hc, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
+            if (absorb(j, hcol.data())) break;
+        }
+        if (j + 1 < k) {
+            scale_by_rnorm_kernel<<<gn, 256, 0, st>>>(I.w, I.V + (int64_t)(j + 1) * n, n, hc + (j + 1));
+            count_launches(1);
+        }
+    }
+    if (!adaptive) {
+        std::vector<double> H((size_t)(k + 1) * ldh);
+        cudaMemcpyAsync(H.data(), I.H, H.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
+        beta = sqrt(H[(size_t)k * ldh]);
+        if (!(beta > 0.0)) return launch_status("inner solve zero rhs", 0);
+        g[0] = beta;
+        for (int j = 0; j < k; j++)
+            if (absorb(j, H.data() + (size_t)j * ldh)) break;
+    }
+    for (int i = used - 1; i >= 0; i--) {
+        double s2 = g[i];
+        for (int q = i + 1; q < used; q++) s2 -= R[(size_t)i * k + q] * y[q];
+        y[i] = s2 / R[(size_t)i * k + i];
+    }
+    g_inner_steps += used;
+    g_inner_applies += 1;
+    if (!adaptive && cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
+    F.collect_times();
+    g_inner_matvec_ms += F.matvec_ms;
+    if (used == 0) return launch_status("inner solve", 0);
+    cudaMemcpyAsync(I.y, y.data(), used * sizeof(double), cudaMemcpyHostToDevice, st);
+    if ((e = F.multiaxpy(z, I.V, used, I.y, 1.0))) return e;
+    // the host vector y must outlive the copy
+    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
+    return launch_status("inner solve", 0);
+}
 
 }  // namespace mbem
 
@@ -530,6 +715,24 @@ int mbem_project_translation(const double* v_in, double* v_out, int64_t n, const
     return project(v_in, v_out, n, ur, work, (cudaStream_t)stream);
 }
 
+size_t mbem_inner_bf16_workspace_size(int64_t n, int iterations) {
+    return inner_layout(n, iterations < 1 ? 1 : iterations, nullptr, nullptr);
+}
+
+void mbem_inner_bf16_stats(int timing, int64_t* steps, int64_t* applies, double* matvec_ms) {
+    if (steps) *steps = g_inner_steps;
+    if (applies) *applies = g_inner_applies;
+    if (matvec_ms) *matvec_ms = g_inner_matvec_ms;
+    g_inner_steps = g_inner_applies = 0;
+    g_inner_matvec_ms = 0.0;
+    g_inner_timing = timing != 0;
+}
+
+int mbem_inner_bf16_apply(const mbem_inner_bf16* p, const double* r, double* z, void* stream) {
+    MBEM_REQUIRE(r != nullptr && z != nullptr && r != z, MBEM_ERR_ARG, "r and z must be distinct device vectors");
+    return inner_bf16_apply(p, r, z, (cudaStream_t)stream);
+}
+
 size_t mbem_fgmres_workspace_size(int64_t n, int restart) {
     return fgmres_layout(n, restart, nullptr, nullptr);
 }
@@ -562,7 +765,7 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
     MBEM_REQUIRE(n > 0, MBEM_ERR_ARG, "bad system size");
     const int m = prm->restart;
     MBEM_REQUIRE(m >= 1 && m <= 1000, MBEM_ERR_ARG, "restart must be in [1, 1000]");
-    MBEM_REQUIRE(prm->precond >= 0 && prm->precond <= 2, MBEM_ERR_ARG, "unknown preconditioner %d", prm->precond);
+    MBEM_REQUIRE(prm->precond >= 0 && prm->precond <= 3, MBEM_ERR_ARG, "unknown preconditioner %d", prm->precond);
     MBEM_REQUIRE(prm->precond == 0 || prm->precond_state != nullptr, MBEM_ERR_ARG, "preconditioner state is NULL");
     const bool flexible = prm->precond != 0;
     const size_t need = fgmres_layout(n, m, nullptr, nullptr);
@@ -608,18 +811,29 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
     // termination independent of that argument
     const int max_cycles = maxiter + 2;
     int cycles = 0;
+    // prm->x_is_zero: the caller's x is zero on entry, so the first residual
+    // is P b with no product; the true residual of the current x, once
+    // computed at a cycle start, is reused as the final one when the loop
+    // ends there
+    bool x_zero = prm->x_is_zero != 0;
+    double rnorm2_final = -1.0;
     while (total < maxiter && !stagnated && !breakdown && cycles++ < max_cycles) {
-        // r = P b - P A P x
-        if ((e = F.op(x, W.w))) return e;
+        // r = P b - P A P x (P b itself while x is zero)
         if ((e = F.proj(b, W.r))) return e;
-        axpby_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.w, n, -1.0, 1.0);
-        count_launches(1);
+        if (!x_zero) {
+            if ((e = F.op(x, W.w))) return e;
+            axpby_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.w, n, -1.0, 1.0);
+            count_launches(1);
+        }
         if ((e = F.norm2(W.r, W.scal))) return e;
         cudaMemcpyAsync(&tmp, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
         const double beta = sqrt(tmp);
         arnoldi = beta / bnorm;
-        if (arnoldi < prm->rtol) break;
+        if (arnoldi < prm->rtol) {
+            rnorm2_final = tmp;
+            break;
+        }
         const int mm = min(m, maxiter - total);
         std::fill(H.begin(), H.end(), 0.0);
         std::fill(g.begin(), g.end(), 0.0);
@@ -700,18 +914,27 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
             cudaMemcpyAsync(W.y, y.data(), jdone * sizeof(double), cudaMemcpyHostToDevice, st);
             if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
             if ((e = F.multiaxpy(x, flexible ? W.Z : W.V, jdone, W.y, 1.0))) return e;
+            x_zero = false;
         }
         restarts++;
         if (stagnated) break;
     }
     // true residual (solver.py:234) and the zero-mean representative P x
-    if ((e = F.op(x, W.w))) return e;
-    if ((e = F.proj(b, W.r))) return e;
-    axpby_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.w, n, -1.0, 1.0);
-        count_launches(1);
-    if ((e = F.norm2(W.r, W.scal))) return e;
+    // (P A P x = P A P (P x): projecting x leaves the residual unchanged)
+    if (rnorm2_final < 0.0) {
+        if ((e = F.proj(b, W.r))) return e;
+        if (!x_zero) {
+            if ((e = F.op(x, W.w))) return e;
+            axpby_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.w, n, -1.0, 1.0);
+            count_launches(1);
+        }
+        if ((e = F.norm2(W.r, W.scal))) return e;
+        cudaMemcpyAsync(&tmp, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
+    } else {
+        tmp = rnorm2_final;
+    }
     if ((e = F.proj(x, x))) return e;
-    cudaMemcpyAsync(&tmp, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
     if (mop && (e = mixed_wait_check(st))) return e;
     rep->true_relres = sqrt(tmp) / bnorm;

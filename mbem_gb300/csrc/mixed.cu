@@ -18,6 +18,7 @@
 // double-float (error-free products and sums on the FP32 pipes), so the
 // operator is applied to ~1e-14 relative accuracy at the HBM roofline; the
 // near blocks are applied in FP64.
+#include <cuda_bf16.h>
 #include <math.h>
 #include <string.h>
 
@@ -266,6 +267,8 @@ struct FarArgs {
     float* out;
     int64_t ld;
     uint32_t* near_mask;   // optional (n_field, ceil(n_src/32)) bit mask of near pairs
+    uint16_t* out16;       // optional BF16 copy of out (round to nearest even)
+    int64_t ld16;
 };
 
 template <bool TKERNEL>
@@ -321,6 +324,15 @@ far_assemble_kernel(FarArgs a, QuadRules Q) {
                 float* row = a.out + (3 * f + i) * a.ld + 3 * s;
 #pragma unroll
                 for (int j = 0; j < 3; j++) row[j] = a.alpha * blk[i][j];
+            }
+            if (a.out16) {
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    uint16_t* row = a.out16 + (3 * f + i) * a.ld16 + 3 * s;
+#pragma unroll
+                    for (int j = 0; j < 3; j++)
+                        row[j] = __bfloat16_as_ushort(__float2bfloat16_rn(a.alpha * blk[i][j]));
+                }
             }
         }
     }
@@ -722,14 +734,15 @@ __global__ void near_matvec_kernel(const int64_t* __restrict__ rowptr, const int
 // The same product as a warp-specialised bulk-copy pipeline: one producer
 // warp streams TP_ROWS row chunks of A and the matching chunk of x (hi, lo)
 // into a TP_STAGES-deep shared-memory ring with cp.async.bulk, completing on
-// per-stage mbarriers; TP_ROWS consumer warps (one row each) read the stage
-// from shared memory and accumulate in double-float. The ring keeps
-// ~160 KB per SM in flight independent of register pressure.
+// per-stage mbarriers; TP_WARPS consumer warps (two rows each, so every x
+// value read from shared memory serves two rows) accumulate in double-float.
+// The ring keeps ~216 KB per SM in flight independent of register pressure.
 // ---------------------------------------------------------------------------
 constexpr int TP_ROWS = 16;
+constexpr int TP_WARPS = TP_ROWS / 2;
 constexpr int TP_CH = 1024;              // columns per chunk (4 KB per row)
 constexpr int TP_STAGES = 3;
-constexpr int TP_THREADS = 32 * (TP_ROWS + 1);
+constexpr int TP_THREADS = 32 * (TP_WARPS + 1);
 constexpr size_t TP_SMEM = (size_t)TP_STAGES * (TP_ROWS + 2) * TP_CH * sizeof(float) + 2 * TP_STAGES * 8;
 constexpr uint32_t TP_WAIT_LIMIT = 1u << 26;
 
@@ -751,13 +764,13 @@ sgemv_df_tma_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int
     if (threadIdx.x == 0) {
         for (int s = 0; s < TP_STAGES; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], TP_ROWS);
+            mbar_init(&empty[s], TP_WARPS);
         }
         mbar_init_fence();
     }
     __syncthreads();
 
-    if (warp == TP_ROWS) {
+    if (warp == TP_WARPS) {
         // producer warp: lane 0 waits for the stage to drain and posts the
         // byte count; lanes 0..nrow+1 then issue one copy each, in parallel
         int64_t issued = 0;
@@ -792,58 +805,63 @@ sgemv_df_tma_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int
         return;
     }
 
-    // consumers: warp w owns row r0 + w
-    const bool valid = warp < nrow;
-    // eight independent double-float chains: two float4 per step, one chain
-    // per element
-    float sh[8], sl[8];
+    // consumers: warp w owns rows r0 + 2w and r0 + 2w + 1; four double-float
+    // chains per row (one per float4 component)
+    const int ra = 2 * warp, rb = 2 * warp + 1;
+    const bool va = ra < nrow, vb = rb < nrow;
+    const int rb_eff = vb ? rb : ra;          // an invalid second row re-reads the first
+    float ah[4], al[4], bh[4], bl[4];
 #pragma unroll
-    for (int t = 0; t < 8; t++) sh[t] = sl[t] = 0.0f;
+    for (int t = 0; t < 4; t++) ah[t] = al[t] = bh[t] = bl[t] = 0.0f;
     for (int64_t k = 0; k < nchunks; k++) {
         const int s = (int)(k % TP_STAGES);
         if (!mbar_wait(&full[s], (uint32_t)((k / TP_STAGES) & 1), TP_WAIT_LIMIT)) {
             atomicExch(&g_mixed_wait_error, 1);
             break;
         }
-        if (valid) {
+        if (va) {
             const int w4 = (int)(lmin(TP_CH, n_main - k * TP_CH) / 4);
-            const float4* a4 = reinterpret_cast<const float4*>(sA + ((int64_t)s * TP_ROWS + warp) * TP_CH);
+            const float4* pa = reinterpret_cast<const float4*>(sA + ((int64_t)s * TP_ROWS + ra) * TP_CH);
+            const float4* pb = reinterpret_cast<const float4*>(sA + ((int64_t)s * TP_ROWS + rb_eff) * TP_CH);
             const float4* h4 = reinterpret_cast<const float4*>(sX + (int64_t)s * 2 * TP_CH);
             const float4* l4 = reinterpret_cast<const float4*>(sX + ((int64_t)s * 2 + 1) * TP_CH);
-            int q = lane;
 #pragma unroll 2
-            for (; q + 32 < w4; q += 64) {
-                const float4 a = a4[q], h = h4[q], l = l4[q];
-                const float4 b = a4[q + 32], g = h4[q + 32], m = l4[q + 32];
-                df_acc(sh[0], sl[0], a.x, h.x, l.x);
-                df_acc(sh[1], sl[1], a.y, h.y, l.y);
-                df_acc(sh[2], sl[2], a.z, h.z, l.z);
-                df_acc(sh[3], sl[3], a.w, h.w, l.w);
-                df_acc(sh[4], sl[4], b.x, g.x, m.x);
-                df_acc(sh[5], sl[5], b.y, g.y, m.y);
-                df_acc(sh[6], sl[6], b.z, g.z, m.z);
-                df_acc(sh[7], sl[7], b.w, g.w, m.w);
-            }
-            if (q < w4) {
-                const float4 a = a4[q], h = h4[q], l = l4[q];
-                df_acc(sh[0], sl[0], a.x, h.x, l.x);
-                df_acc(sh[1], sl[1], a.y, h.y, l.y);
-                df_acc(sh[2], sl[2], a.z, h.z, l.z);
-                df_acc(sh[3], sl[3], a.w, h.w, l.w);
+            for (int q = lane; q < w4; q += 32) {
+                const float4 h = h4[q], l = l4[q], a = pa[q], b = pb[q];
+                df_acc(ah[0], al[0], a.x, h.x, l.x);
+                df_acc(ah[1], al[1], a.y, h.y, l.y);
+                df_acc(ah[2], al[2], a.z, h.z, l.z);
+                df_acc(ah[3], al[3], a.w, h.w, l.w);
+                df_acc(bh[0], bl[0], b.x, h.x, l.x);
+                df_acc(bh[1], bl[1], b.y, h.y, l.y);
+                df_acc(bh[2], bl[2], b.z, h.z, l.z);
+                df_acc(bh[3], bl[3], b.w, h.w, l.w);
             }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);
     }
-    if (!valid) return;
-    const int64_t r = r0 + warp;
-    for (int64_t c = n_main + lane; c < n_cols; c += 32) df_acc(sh[0], sl[0], A[r * ld + c], xh[c], xl[c]);
-    double acc = 0.0;
+    if (!va) return;
+    const int64_t rowa = r0 + ra, rowb = r0 + rb_eff;
+    for (int64_t c = n_main + lane; c < n_cols; c += 32) {
+        df_acc(ah[0], al[0], A[rowa * ld + c], xh[c], xl[c]);
+        df_acc(bh[0], bl[0], A[rowb * ld + c], xh[c], xl[c]);
+    }
+    double sa = 0.0, sb = 0.0;
 #pragma unroll
-    for (int t = 0; t < 8; t++) acc += (double)sh[t] + (double)sl[t];
+    for (int t = 0; t < 4; t++) {
+        sa += (double)ah[t] + (double)al[t];
+        sb += (double)bh[t] + (double)bl[t];
+    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) y[r] = acc;
+    for (int o = 16; o > 0; o >>= 1) {
+        sa += __shfl_xor_sync(0xffffffffu, sa, o);
+        sb += __shfl_xor_sync(0xffffffffu, sb, o);
+    }
+    if (lane == 0) {
+        y[rowa] = sa;
+        if (vb) y[rowb] = sb;
+    }
 }
 
 // MBEM_ERR_WAIT if a pipeline wait gave up since the last check (the flag is
@@ -891,6 +909,158 @@ int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, floa
     return launch_status("mixed_matvec", launches);
 }
 
+// ---------------------------------------------------------------------------
+// The inner operator of the mixed solve: y = A16 x + near blocks x, with A16
+// the far field rounded to BF16. Rows stream through a warp-specialised
+// bulk-copy ring (as sgemv_df_tma_kernel) at half the bytes. Each consumer
+// warp owns two rows, so every FP32 x value read from shared memory serves
+// two rows; lanes read 8-byte BF16 quads and 16-byte x quads at unit stride
+// (no bank conflicts). x is rounded to FP32 once per product; rows sum in
+// FP32 over four chains each (the operator is a preconditioner: its 2^-9
+// entry rounding, not the summation, sets its accuracy).
+// ---------------------------------------------------------------------------
+constexpr int BP_ROWS = 16;
+constexpr int BP_WARPS = BP_ROWS / 2;    // consumer warps, two rows each
+constexpr int BP_CH = 2048;              // columns per chunk (4 KB of BF16 per row)
+constexpr int BP_STAGES = 3;
+constexpr int BP_THREADS = 32 * (BP_WARPS + 1);
+constexpr size_t BP_SMEM = (size_t)BP_STAGES * (BP_ROWS * BP_CH * 2 + BP_CH * 4) + 2 * BP_STAGES * 8;
+
+__global__ void d2f_kernel(const double* __restrict__ x, int64_t n, float* __restrict__ xf) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) xf[i] = (float)x[i];
+}
+
+__device__ __forceinline__ float bf16_lo(uint32_t u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
+
+__global__ void __launch_bounds__(BP_THREADS, 1)
+sgemv_bf16_tma_kernel(const uint16_t* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_main, int64_t n_cols,
+                      const float* __restrict__ xf, double* __restrict__ y) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint16_t* sA = reinterpret_cast<uint16_t*>(smem);                                // [S][ROWS][CH]
+    float* sX = reinterpret_cast<float*>(sA + (size_t)BP_STAGES * BP_ROWS * BP_CH);   // [S][CH]
+    uint64_t* full = reinterpret_cast<uint64_t*>(sX + BP_STAGES * BP_CH);
+    uint64_t* empty = full + BP_STAGES;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t r0 = (int64_t)blockIdx.x * BP_ROWS;
+    const int nrow = (int)lmin(BP_ROWS, n_rows - r0);
+    const int64_t nchunks = ceil_div(n_main, BP_CH);
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < BP_STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], BP_WARPS);
+        }
+        mbar_init_fence();
+    }
+    __syncthreads();
+
+    if (warp == BP_WARPS) {
+        int64_t issued = 0;
+        for (int64_t k = 0; k < nchunks; k++) {
+            const int s = (int)(k % BP_STAGES);
+            int ok = 1;
+            if (lane == 0) {
+                if (k >= BP_STAGES && !mbar_wait(&empty[s], (uint32_t)(((k / BP_STAGES) - 1) & 1), TP_WAIT_LIMIT)) {
+                    atomicExch(&g_mixed_wait_error, 1);
+                    ok = 0;
+                }
+            }
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) break;
+            const int64_t c0 = k * BP_CH;
+            const uint32_t cols = (uint32_t)lmin(BP_CH, n_main - c0);
+            if (lane == 0) mbar_arrive_expect_tx(&full[s], cols * 2u * (uint32_t)nrow + cols * 4u);
+            __syncwarp();
+            if (lane < nrow)
+                bulk_g2s(sA + ((int64_t)s * BP_ROWS + lane) * BP_CH, A + (r0 + lane) * ld + c0, cols * 2u, &full[s]);
+            else if (lane == BP_ROWS)
+                bulk_g2s(sX + (int64_t)s * BP_CH, xf + c0, cols * 4u, &full[s]);
+            issued = k + 1;
+        }
+        if (lane == 0)
+            for (int64_t k = (issued > BP_STAGES ? issued - BP_STAGES : 0); k < issued; k++)
+                if (!mbar_wait(&full[k % BP_STAGES], (uint32_t)((k / BP_STAGES) & 1), TP_WAIT_LIMIT))
+                    atomicExch(&g_mixed_wait_error, 1);
+        return;
+    }
+
+    // consumer warp w: rows 2w (always < nrow when the warp has work) and 2w + 1
+    const int ra = 2 * warp, rb = 2 * warp + 1;
+    const bool va = ra < nrow, vb = rb < nrow;
+    const int rb_eff = vb ? rb : ra;          // an invalid second row re-reads the first
+    float a[4] = {0.f, 0.f, 0.f, 0.f}, b[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int64_t k = 0; k < nchunks; k++) {
+        const int s = (int)(k % BP_STAGES);
+        if (!mbar_wait(&full[s], (uint32_t)((k / BP_STAGES) & 1), TP_WAIT_LIMIT)) {
+            atomicExch(&g_mixed_wait_error, 1);
+            break;
+        }
+        if (va) {
+            const int w4 = (int)(lmin(BP_CH, n_main - k * BP_CH) / 4);
+            const uint2* pa = reinterpret_cast<const uint2*>(sA + ((int64_t)s * BP_ROWS + ra) * BP_CH);
+            const uint2* pb = reinterpret_cast<const uint2*>(sA + ((int64_t)s * BP_ROWS + rb_eff) * BP_CH);
+            const float4* x4 = reinterpret_cast<const float4*>(sX + (int64_t)s * BP_CH);
+#pragma unroll 4
+            for (int q = lane; q < w4; q += 32) {
+                const float4 u = x4[q];
+                const uint2 p = pa[q], r = pb[q];
+                a[0] = fmaf(bf16_lo(p.x), u.x, a[0]);
+                a[1] = fmaf(bf16_hi(p.x), u.y, a[1]);
+                a[2] = fmaf(bf16_lo(p.y), u.z, a[2]);
+                a[3] = fmaf(bf16_hi(p.y), u.w, a[3]);
+                b[0] = fmaf(bf16_lo(r.x), u.x, b[0]);
+                b[1] = fmaf(bf16_hi(r.x), u.y, b[1]);
+                b[2] = fmaf(bf16_lo(r.y), u.z, b[2]);
+                b[3] = fmaf(bf16_hi(r.y), u.w, b[3]);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+    }
+    if (!va) return;
+    const int64_t rowa = r0 + ra, rowb = r0 + rb_eff;
+    for (int64_t c = n_main + lane; c < n_cols; c += 32) {
+        const float xc = xf[c];
+        a[0] = fmaf(__uint_as_float((uint32_t)A[rowa * ld + c] << 16), xc, a[0]);
+        b[0] = fmaf(__uint_as_float((uint32_t)A[rowb * ld + c] << 16), xc, b[0]);
+    }
+    double sa = ((double)a[0] + (double)a[1]) + ((double)a[2] + (double)a[3]);
+    double sb = ((double)b[0] + (double)b[1]) + ((double)b[2] + (double)b[3]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sa += __shfl_xor_sync(0xffffffffu, sa, o);
+        sb += __shfl_xor_sync(0xffffffffu, sb, o);
+    }
+    if (lane == 0) {
+        y[rowa] = sa;
+        if (vb) y[rowb] = sb;
+    }
+}
+
+int bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_cols, int n_near,
+                const mbem_near_blocks* near, const double* x, double* y, float* xf, cudaStream_t st) {
+    MBEM_REQUIRE(A16 && x && y && xf && n_rows >= 0 && n_cols >= 0 && ld16 >= n_cols, MBEM_ERR_ARG,
+                 "bad BF16 matvec args");
+    MBEM_REQUIRE((uintptr_t)A16 % 16 == 0 && ld16 % 8 == 0 && (uintptr_t)xf % 16 == 0, MBEM_ERR_ARG,
+                 "the BF16 matrix and the scratch must be 16-byte aligned with ld16 %% 8 == 0");
+    MBEM_REQUIRE(n_near >= 0 && (n_near == 0 || near), MBEM_ERR_ARG, "bad near blocks");
+    if (n_rows == 0) return MBEM_OK;
+    d2f_kernel<<<(unsigned)ceil_div(n_cols > 0 ? n_cols : 1, 256), 256, 0, st>>>(x, n_cols, xf);
+    cudaError_t e = cudaFuncSetAttribute(sgemv_bf16_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)BP_SMEM);
+    if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "bf16 gemv smem attribute: %s", cudaGetErrorString(e));
+    const int64_t n_main = n_cols & ~(int64_t)7;
+    sgemv_bf16_tma_kernel<<<(unsigned)ceil_div(n_rows, BP_ROWS), BP_THREADS, BP_SMEM, st>>>(
+        A16, ld16, n_rows, n_main, n_cols, xf, y);
+    for (int q = 0; q < n_near; q++) {
+        const mbem_near_blocks& nb = near[q];
+        near_matvec_kernel<<<(unsigned)ceil_div(nb.n_field, 8), 256, 0, st>>>(
+            nb.rowptr, nb.cols, nb.vals, nb.n_field, x + nb.col0, y + nb.row0);
+    }
+    return launch_status("bf16_matvec", 2 + n_near);
+}
+
 }  // namespace mbem
 
 using namespace mbem;
@@ -901,8 +1071,17 @@ int mbem_far_matrix(int kernel, const double* x_field, int64_t n_field, const do
                     const double* normals, const double* eps, int64_t n_src, const double* coeffs,
                     double near_factor, double alpha, float* out, int64_t ld_out, uint32_t* near_mask,
                     void* stream) {
+    return mbem_far_matrix_bf16(kernel, x_field, n_field, tri_verts, normals, eps, n_src, coeffs, near_factor,
+                                alpha, out, ld_out, nullptr, 0, near_mask, stream);
+}
+
+int mbem_far_matrix_bf16(int kernel, const double* x_field, int64_t n_field, const double* tri_verts,
+                         const double* normals, const double* eps, int64_t n_src, const double* coeffs,
+                         double near_factor, double alpha, float* out, int64_t ld_out, uint16_t* out16,
+                         int64_t ld16, uint32_t* near_mask, void* stream) {
     MBEM_REQUIRE(kernel == 0 || kernel == 1, MBEM_ERR_ARG, "kernel must be 0 (T) or 1 (U)");
     MBEM_REQUIRE(n_field >= 0 && n_src >= 0 && ld_out >= 3 * n_src, MBEM_ERR_ARG, "bad far matrix shape");
+    MBEM_REQUIRE(out16 == nullptr || ld16 >= 3 * n_src, MBEM_ERR_ARG, "bad BF16 copy stride");
     MBEM_REQUIRE(coeffs != nullptr && near_factor > 0.0, MBEM_ERR_ARG, "coeffs/near_factor");
     MBEM_REQUIRE(kernel == 1 || n_src == 0 || normals, MBEM_ERR_ARG, "normals is NULL");
     if (n_field == 0 || n_src == 0) return MBEM_OK;
@@ -913,6 +1092,7 @@ int mbem_far_matrix(int kernel, const double* x_field, int64_t n_field, const do
     for (int i = 0; i < 6; i++) a.c[i] = i < nc ? (float)coeffs[i] : 0.0f;
     a.alpha = (float)alpha; a.near_factor = near_factor; a.out = out; a.ld = ld_out;
     a.near_mask = near_mask;
+    a.out16 = out16; a.ld16 = ld16;
     dim3 grid((unsigned)ceil_div(n_src, FAR_THREADS), (unsigned)lmin(ceil_div(n_field, FAR_FIELD_TILE), 65535));
     if (kernel == 0)
         far_assemble_kernel<true><<<grid, FAR_THREADS, 0, (cudaStream_t)stream>>>(a, rules());
@@ -1016,6 +1196,14 @@ int mbem_near_add_diagonal(const int64_t* rowptr, const int64_t* cols, double* v
     near_add_diag_kernel<<<(unsigned)ceil_div(n_field, 128), 128, 0, (cudaStream_t)stream>>>(rowptr, cols, vals,
                                                                                           n_field, D, missing);
     return launch_status("near_add_diag_kernel");
+}
+
+int mbem_bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_cols, int n_near,
+                     const mbem_near_blocks* near, const double* x, double* y, void* work, size_t work_bytes,
+                     void* stream) {
+    MBEM_REQUIRE(work && work_bytes >= (size_t)n_cols * sizeof(float), MBEM_ERR_SIZE,
+                 "BF16 matvec workspace too small (needs %lld bytes)", (long long)(n_cols * sizeof(float)));
+    return bf16_matvec(A16, ld16, n_rows, n_cols, n_near, near, x, y, (float*)work, (cudaStream_t)stream);
 }
 
 int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, void* work, size_t work_bytes,

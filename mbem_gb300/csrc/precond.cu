@@ -223,6 +223,7 @@ int bj_apply(const mbem_block_jacobi* bj, const double* r, double* z, cudaStream
 int precond_apply(int kind, const void* state, const double* r, double* z, cudaStream_t st) {
     if (kind == 1) return bj_apply(static_cast<const mbem_block_jacobi*>(state), r, z, st);
     if (kind == 2) return nn_precond_apply(state, r, z, st);
+    if (kind == 3) return inner_bf16_apply(state, r, z, st);
     return set_error(MBEM_ERR_ARG, "unknown preconditioner %d", kind);
 }
 

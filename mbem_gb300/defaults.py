@@ -46,3 +46,5 @@ PRECOND_BJ_CHUNK_DOF = 9000
 # ---- GPU mixed-precision path ----
 MIXED_BLOCK = 64                      # BF16 scale block (rows x columns)
 MIXED_NEAR_RADIUS_FACTOR = 3.0        # near field: centroid distance < 3 max(eps, h)
+MIXED_INNER_ITERATIONS = 40           # at most this many BF16 inner GMRES steps per outer step
+MIXED_INNER_RTOL = 1e-5               # ... or until the inner residual estimate is this small

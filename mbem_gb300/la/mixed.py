@@ -54,9 +54,12 @@ def near_list(x_field: torch.Tensor, tri_verts: torch.Tensor, eps: torch.Tensor,
 
 def far_near_block(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha: float,
                    far_out: torch.Tensor, row0: int = 0, col0: int = 0,
-                   near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, timer=None) -> NearList:
+                   near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, timer=None,
+                   far16_out: torch.Tensor | None = None) -> NearList:
     """Writes alpha * (far part) into ``far_out`` (FP32 (3Nf, 3Ns) view, zeros
-    at near pairs) and returns the near blocks alpha * (closed form) in FP64."""
+    at near pairs) and returns the near blocks alpha * (closed form) in FP64.
+    ``far16_out``: an optional BF16 view of the same shape that receives the
+    far part rounded to BF16 in the same pass."""
     k = _KERNEL_ID[kernel]
     nf, ns = x_field.shape[0], tri_verts.shape[0]
     if far_out.dtype != torch.float32 or far_out.stride(1) != 1 or tuple(far_out.shape) != (3 * nf, 3 * ns):
@@ -71,8 +74,15 @@ def far_near_block(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha:
     # all pairs
     n_words = (ns + 31) // 32
     mask = torch.empty((nf, n_words), dtype=torch.int32, device=x_field.device)
-    nat.call("mbem_far_matrix", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ns, c,
-             float(near_factor), float(alpha), ptr(far_out), far_out.stride(0), ptr(mask), stream_handle())
+    if far16_out is not None:
+        if far16_out.dtype != torch.bfloat16 or far16_out.stride(1) != 1 or far16_out.shape != far_out.shape:
+            raise ValueError("far16_out must be a bfloat16 view shaped like far_out with unit column stride")
+        nat.call("mbem_far_matrix_bf16", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ns, c,
+                 float(near_factor), float(alpha), ptr(far_out), far_out.stride(0), ptr(far16_out),
+                 far16_out.stride(0), ptr(mask), stream_handle())
+    else:
+        nat.call("mbem_far_matrix", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ns, c,
+                 float(near_factor), float(alpha), ptr(far_out), far_out.stride(0), ptr(mask), stream_handle())
     if ev is not None:
         ev[1].record()
         timer.append(("far_" + kernel, nf, ns, ev[0], ev[1]))
@@ -94,9 +104,10 @@ def far_near_block(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha:
 class MixedOperator:
     """A = A32 (FP32 dense far field) + sum of near-block lists (FP64)."""
 
-    def __init__(self, A32: torch.Tensor, near: list[NearList]):
+    def __init__(self, A32: torch.Tensor, near: list[NearList], A16: torch.Tensor | None = None):
         self.A32 = A32
         self.near = near
+        self.A16 = A16          # optional BF16 copy of A32 (n, ld16), made by the assembly
         self._keep = None
 
     @property
@@ -139,3 +150,87 @@ class MixedOperator:
                 for j in range(3):
                     A[nb.row0 + 3 * f + i, nb.col0 + 3 * nb.cols + j] += nb.vals[:, 3 * i + j]
         return A
+
+
+class Bf16Inner:
+    """The mixed solve's inner preconditioner: GMRES from zero on the
+    deflated operator with the far field rounded to BF16 (2 bytes per entry)
+    and the near blocks in FP64, for at most ``iterations`` steps or until
+    its residual estimate falls below ``rtol`` (0: always all steps). Used as a flexible right
+    preconditioner of FGMRES on the accurate mixed operator (FP32 far field,
+    double-float sums), whose true residual decides convergence."""
+
+    PRECOND_KIND = 3
+
+    def __init__(self, op: MixedOperator, iterations: int = defaults.MIXED_INNER_ITERATIONS,
+                 u_ranges=(), rtol: float = defaults.MIXED_INNER_RTOL):
+        if not 1 <= iterations <= nat.INNER_MAX_ITERS:
+            raise ValueError(f"iterations must be in [1, {nat.INNER_MAX_ITERS}] (got {iterations})")
+        if not 0.0 <= rtol < 1.0:
+            raise ValueError(f"rtol must be in [0, 1) (got {rtol})")
+        n = op.n
+        self.rtol = float(rtol)
+        self.op = op
+        self.iterations = int(iterations)
+        if op.A16 is not None:
+            self.A16 = op.A16
+            self.ld16 = op.A16.stride(0)
+        else:
+            self.ld16 = (n + 7) // 8 * 8
+            self.A16 = torch.empty((n, self.ld16), dtype=torch.bfloat16, device=op.A32.device)
+            nat.call("mbem_to_bf16", ptr(op.A32), 0, op.A32.stride(0), n, n, ptr(self.A16), self.ld16,
+                     stream_handle())
+        self.u_ranges = np.asarray(u_ranges, dtype=np.int64).reshape(-1, 2)
+        self.work = None
+        self.set_iterations(iterations)
+        self.built = True
+        self._keep = None
+
+    def set_iterations(self, iterations: int) -> None:
+        """Changes the inner step count (and grows the workspace to match)."""
+        if not 1 <= iterations <= nat.INNER_MAX_ITERS:
+            raise ValueError(f"iterations must be in [1, {nat.INNER_MAX_ITERS}] (got {iterations})")
+        size = int(nat.lib().mbem_inner_bf16_workspace_size(self.n, iterations))
+        if self.work is None or self.work.numel() < size:
+            self.work = torch.empty(size, dtype=torch.uint8, device=self.op.A32.device)
+        self.iterations = int(iterations)
+
+    @property
+    def n(self) -> int:
+        return self.op.n
+
+    def struct(self) -> nat.InnerBf16:
+        arr = (nat.NearBlocks * max(len(self.op.near), 1))()
+        for i, nb in enumerate(self.op.near):
+            arr[i] = nat.NearBlocks(nb.row0, nb.col0, nb.n_field, ptr(nb.rowptr), ptr(nb.cols), ptr(nb.vals))
+        ur = np.ascontiguousarray(self.u_ranges.ravel())
+        self._keep = (arr, ur)
+        return nat.InnerBf16(self.n, ptr(self.A16), self.ld16, len(self.op.near), arr, self.iterations,
+                             self.rtol, len(self.u_ranges), ur.ctypes.data if ur.size else None, ptr(self.work),
+                             self.work.numel())
+
+    def matvec(self, x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """(A16 + near) x: the inner operator itself."""
+        x = x.to(torch.float64).contiguous()
+        y = out if out is not None else torch.empty(self.n, dtype=torch.float64, device=x.device)
+        arr = self.struct()
+        work = torch.empty(4 * x.numel() + 64, dtype=torch.uint8, device=x.device)
+        nat.call("mbem_bf16_matvec", ptr(self.A16), self.ld16, self.n, self.n, arr.n_near, arr.near, ptr(x),
+                 ptr(y), ptr(work), work.numel(), stream_handle())
+        return y
+
+    def apply(self, r: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        r = r.to(torch.float64).contiguous()
+        z = out if out is not None else torch.empty_like(r)
+        st = self.struct()
+        nat.call("mbem_inner_bf16_apply", ctypes.byref(st), ptr(r), ptr(z), stream_handle())
+        return z
+
+
+def inner_stats(timing: bool = False) -> tuple[int, int, float]:
+    """(inner steps, inner solves, device ms of their BF16 products when they
+    were timed) since the last call; ``timing`` switches the timing of the
+    following inner solves on or off."""
+    a, b, t = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_double(0.0)
+    nat.lib().mbem_inner_bf16_stats(int(timing), ctypes.byref(a), ctypes.byref(b), ctypes.byref(t))
+    return int(a.value), int(b.value), float(t.value)

@@ -70,7 +70,7 @@ def _precond_args(precond):
     if precond is None:
         return 0, None, None
     kind = getattr(precond, "PRECOND_KIND", None)
-    if kind not in (1, 2):
+    if kind not in (1, 2, 3):
         raise TypeError(f"unsupported preconditioner {type(precond).__name__}")
     if not getattr(precond, "built", True):
         raise RuntimeError("preconditioner used before it was built")
@@ -95,7 +95,8 @@ def _fgmres(A, mop, b, x0, rtol, restart, maxiter, stagnation_window, stagnation
                            stagnation_factor=float(stagnation_factor),
                            n_u_ranges=len(rng) // 2,
                            u_ranges=rng.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) if rng.size else None,
-                           precond=0, precond_state=None, time_matvec=int(bool(time_matvec)))
+                           precond=0, precond_state=None, time_matvec=int(bool(time_matvec)),
+                           x_is_zero=int(x0 is None))
     kind, state, _keep = _precond_args(precond)
     prm.precond = kind
     prm.precond_state = state

@@ -107,3 +107,64 @@ def test_mixed_solution_against_fp64(systems):
     assert err < 1e-5
     assert amx.report.true_relres < 1e-12
     del Pb, r
+
+
+def test_bf16_matvec_against_rounded_operator(systems):
+    """The BF16 inner operator equals bf16(A_far) x + near x, summed in FP32
+    (tolerance 1e-5 of max|y|), and is within 2^-8 of the mixed operator."""
+    from mbem_gb300.la.mixed import Bf16Inner
+    _, amx = systems
+    inner = Bf16Inner(amx.op, 4, amx.u_ranges())
+    x = torch.randn(amx.op.n, dtype=torch.float64, device="cuda")
+    y = inner.matvec(x)
+    n = amx.op.n
+    A16 = inner.A16[:, :n].to(torch.float64)
+    ref = A16 @ x.to(torch.float32).to(torch.float64)
+    for nb in amx.op.near:
+        rp = nb.rowptr.cpu().numpy()
+        f = torch.from_numpy(np.repeat(np.arange(nb.n_field), np.diff(rp))).to(x.device)
+        v = nb.vals.view(-1, 3, 3)
+        contrib = torch.einsum("kij,kj->ki", v, x[nb.col0:].view(-1, 3)[nb.cols])
+        ref.view(-1, 3)[nb.row0 // 3:].index_add_(0, f, contrib)
+    assert rel_err(y.cpu().numpy(), ref.cpu().numpy()) < 1e-5
+    y32 = amx.op.matvec(x)
+    assert float((y - y32).norm() / y32.norm()) < 2.0 ** -8
+
+
+def test_bf16_inner_preconditioned_solve(systems):
+    """FGMRES on the mixed operator with the BF16 inner solve as flexible
+    preconditioner: same convergence test (the mixed operator's true
+    residual), the solution within 1e-9 of the unpreconditioned one, and
+    fewer outer iterations."""
+    _, amx = systems
+    x0 = amx.solve_device(precond="none")
+    its0 = amx.report.iterations
+    x1 = amx.solve_device(precond=amx.bf16_inner(6))
+    rep = amx.report
+    assert rep.converged and rep.true_relres < 1e-12
+    assert float((x1 - x0).norm() / x0.norm()) < 1e-9
+    assert rep.iterations < its0
+
+
+def test_fused_bf16_copy_equals_conversion(gpu):
+    """precond="bf16_inner" makes the far-field assembly write the BF16 copy
+    in the same pass: it equals the rounding of the FP32 far field bit for
+    bit, and the preconditioned solve converges to the plain solution."""
+    from mbem_gb300 import _native as nat
+    from mbem_gb300._device import ptr, stream_handle
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.model import generate_system
+    model, eps = cube_fault_model(8, 4, 1.3, 1.95)
+    asm = DenseBackend(jump="calibrated", deflate=True, rtol=1e-12, precision="mixed",
+                       precond="bf16_inner").assemble(generate_system(model), eps)
+    n = asm.op.n
+    assert asm.op.A16 is not None
+    ref = torch.empty_like(asm.op.A16)
+    nat.call("mbem_to_bf16", ptr(asm.op.A32), 0, asm.op.A32.stride(0), n, n, ptr(ref), ref.stride(0),
+             stream_handle())
+    assert torch.equal(asm.op.A16[:, :n].view(torch.int16), ref[:, :n].view(torch.int16))
+    x1 = asm.solve_device()
+    assert asm.report.converged and asm.report.true_relres < 1e-12
+    x0 = asm.solve_device(precond="none")
+    assert float((x1 - x0).norm() / x0.norm()) < 1e-9
