@@ -256,6 +256,54 @@ int mbem_inner_bf16_apply(const mbem_inner_bf16* p, const double* r, double* z, 
  * following applications time their products with CUDA events. */
 void mbem_inner_bf16_stats(int timing, int64_t* steps, int64_t* applies, double* matvec_ms);
 
+/* ---- many unevenly sized meshes in one solve. Each mesh keeps its mixed
+ * operator (FP32 far field + FP64 near blocks by field point, the calibrated
+ * diagonal inside them); the batch vectors hold the meshes' unknowns one
+ * after another, each segment rounded up to MBEM_MM_SEGMENT entries (padding
+ * zero). One persistent launch applies every mesh's operator; deflated
+ * GMRES(restart) runs on all meshes in lockstep with per-mesh reductions and
+ * Givens rotations on the device, each restart cycle one CUDA graph launch
+ * (use_graph = 1) or the same kernels launched one by one (0). ---------- */
+#define MBEM_MM_SEGMENT 512
+#define MBEM_MM_MAX_RESTART 64
+typedef struct {
+    const float* A32;        /* (n, ld32) FP32 far field, 16-byte aligned, ld32 % 4 == 0 */
+    int64_t ld32;
+    int64_t n;               /* unknowns (a multiple of 3) */
+    int64_t offset;          /* segment start: 0 for the first mesh, then the previous
+                                offset + n rounded up to MBEM_MM_SEGMENT */
+    const int64_t* rowptr;   /* near blocks by field point: (n/3 + 1) row pointers, */
+    const int64_t* cols;     /* source node per block (columns 3c..3c+2), */
+    const double* vals;      /* 3x3 FP64 values per block, row-major */
+    int64_t u_off, u_len;    /* deflated u-slot range within the segment (u_len = 0: none) */
+} mbem_mm_mesh;
+
+typedef struct {
+    int* iterations;         /* HOST arrays of n_mesh entries, filled by the solve */
+    double* relres;          /* true relative residual at the last check */
+    int* converged;
+    int cycles;              /* restart cycles run */
+} mbem_mm_report;
+
+typedef struct mbem_mm_solver mbem_mm_solver;
+/* batch vector length (-1 if the layout is invalid) and workspace bytes (0 if invalid) */
+int64_t mbem_mm_total(const mbem_mm_mesh* meshes, int n_mesh);
+size_t mbem_mm_workspace_size(const mbem_mm_mesh* meshes, int n_mesh, int restart);
+/* work: device memory (256-byte aligned) that the solver keeps; the meshes'
+ * arrays must outlive it. */
+int mbem_mm_create(const mbem_mm_mesh* meshes, int n_mesh, int restart, void* work, size_t work_bytes,
+                   void* stream, mbem_mm_solver** out);
+void mbem_mm_destroy(mbem_mm_solver* solver);
+/* y = A x on every mesh (batch vectors) */
+int mbem_mm_matvec(mbem_mm_solver* solver, const double* x, double* y, void* stream);
+/* x = the deflated solution of every mesh to rtol (true residual), at most
+ * max_cycles restart cycles; graph capture needs a stream other than the
+ * legacy default stream. */
+int mbem_mm_solve(mbem_mm_solver* solver, const double* b, double* x, double rtol, int max_cycles, int use_graph,
+                  mbem_mm_report* report, void* stream);
+/* MBEM_ERR_WAIT if a bounded wait of the batched matvec gave up since the last check */
+int mbem_mm_check(void* stream);
+
 /* ---- cluster block-Jacobi preconditioner (la/preconditioner.py:421-470,
  * the "block_jacobi" rung; chunks from la/cluster.py:56-75 bisection, built
  * by the caller). The chunks partition 0..n-1; chunk c holds the DOFs

@@ -80,6 +80,20 @@ class InnerBf16(Structure):
 
 INNER_MAX_ITERS = 64
 
+
+class MmMesh(Structure):
+    _fields_ = [("A32", c_void_p), ("ld32", c_int64), ("n", c_int64), ("offset", c_int64), ("rowptr", c_void_p),
+                ("cols", c_void_p), ("vals", c_void_p), ("u_off", c_int64), ("u_len", c_int64)]
+
+
+class MmReport(Structure):
+    _fields_ = [("iterations", POINTER(c_int)), ("relres", POINTER(c_double)), ("converged", POINTER(c_int)),
+                ("cycles", c_int)]
+
+
+MM_SEGMENT = 512
+MM_MAX_RESTART = 64
+
 NN_FEAT, NN_HIDDEN = 16, 32
 NN_PARAMS = NN_HIDDEN * NN_FEAT + NN_HIDDEN + NN_HIDDEN * NN_HIDDEN + NN_HIDDEN + 9 * NN_HIDDEN + 9
 
@@ -168,6 +182,13 @@ _SIGNATURES = {
     "mbem_inner_bf16_apply": (c_int, [POINTER(InnerBf16), _P, _P, _P]),
     "mbem_inner_bf16_stats": (None, [c_int, POINTER(c_int64), POINTER(c_int64), POINTER(c_double)]),
     "mbem_mixed_matvec_noalloc": (c_int, [POINTER(MixedOperator), _P, _P, _P]),
+    "mbem_mm_total": (c_int64, [POINTER(MmMesh), c_int]),
+    "mbem_mm_workspace_size": (c_size_t, [POINTER(MmMesh), c_int, c_int]),
+    "mbem_mm_create": (c_int, [POINTER(MmMesh), c_int, c_int, _P, c_size_t, _P, POINTER(c_void_p)]),
+    "mbem_mm_destroy": (None, [_P]),
+    "mbem_mm_matvec": (c_int, [_P, _P, _P, _P]),
+    "mbem_mm_solve": (c_int, [_P, _P, _P, c_double, c_int, c_int, POINTER(MmReport), _P]),
+    "mbem_mm_check": (c_int, [_P]),
 }
 
 _lib = None

@@ -86,6 +86,13 @@ class DenseBackend:
                               precision=self.precision, near_factor=self.near_factor, precond=self.precond)
 
 
+def _f32_matrix(rows: int, cols: int, dev, zero: bool = False) -> torch.Tensor:
+    """An FP32 (rows, cols) matrix whose rows start on 16-byte boundaries
+    (leading dimension rounded up to 4), as the streaming matvecs need."""
+    ld = (cols + 3) // 4 * 4
+    return (torch.zeros if zero else torch.empty)((rows, ld), dtype=torch.float32, device=dev)[:, :cols]
+
+
 def require_anchor_or_deflate(system: BlockSystem, jump: str, deflate: bool):
     """The calibrated jump on an un-anchored model needs deflation
     (dense.py:101-121)."""
@@ -227,7 +234,7 @@ class AssembledDense:
             raise NotImplementedError("mixed precision: two terms on one block")
         covered = sum(t.row.size * t.col.size for t in self.system.terms)
         alloc = torch.empty if covered == n * n else torch.zeros
-        A32 = alloc((n, n), dtype=torch.float32, device=dev)
+        A32 = _f32_matrix(n, n, dev, zero=covered != n * n)
         # the BF16 inner operator's copy, written by the same far-field pass
         A16 = (alloc((n, (n + 7) // 8 * 8), dtype=torch.bfloat16, device=dev)
                if self.precond == "bf16_inner" else None)
@@ -252,7 +259,7 @@ class AssembledDense:
                 return MixedOperator(A32[t.row.offset:t.row.stop, t.col.offset:t.col.stop], [
                     type(nl)(0, 0, nl.n_field, nl.rowptr, nl.cols, nl.vals)]), t.scale
             if key not in temp:
-                far = torch.empty((3 * q.n_dofs, 3 * p.n_nodes), dtype=torch.float32, device=dev)
+                far = _f32_matrix(3 * q.n_dofs, 3 * p.n_nodes, dev)
                 nl = self._mixed_block(far, q, p, kernel, mat, 1.0, 0, 0)
                 temp[key] = (MixedOperator(far, [nl]), 1.0)
             return temp[key]

@@ -25,6 +25,7 @@
 #include <mutex>
 #include <vector>
 
+#include "dfloat.cuh"
 #include "p0_pair.cuh"
 #include "tma_pipe.cuh"
 
@@ -101,17 +102,6 @@ static const QuadRules& rules() {
 // ---------------------------------------------------------------------------
 // double-float helpers
 // ---------------------------------------------------------------------------
-struct F2 {
-    float hi, lo;
-};
-
-__device__ __forceinline__ F2 split_d(double v) {
-    F2 r;
-    r.hi = (float)v;
-    r.lo = (float)(v - (double)r.hi);
-    return r;
-}
-
 // (a_hi + a_lo) - (b_hi + b_lo) rounded to FP32 with the hi difference exact
 // (Knuth's TwoSum; the _rn intrinsics keep the compiler from contracting or
 // reassociating the error-free steps)
@@ -611,17 +601,6 @@ __global__ void split_vec_kernel(const double* __restrict__ x, int64_t n, float*
 constexpr int SGEMV_ROWS = 4;
 constexpr int SGEMV_UNROLL = 2;
 constexpr int SGEMV_THREADS = 256;
-
-// double-float accumulate of a (FP32, exact) times x = xh + xl
-__device__ __forceinline__ void df_acc(float& sh, float& sl, float a, float xh, float xl) {
-    const float p = __fmul_rn(a, xh);
-    const float e = __fmaf_rn(a, xh, -p);      // exact product error (TwoProd)
-    const float q = __fmaf_rn(a, xl, e);
-    const float s = __fadd_rn(sh, p);          // TwoSum of sh + p
-    const float bb = __fsub_rn(s, sh);
-    sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb)), q));
-    sh = s;
-}
 
 __global__ void __launch_bounds__(SGEMV_THREADS)
 sgemv_df_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_cols,

@@ -27,3 +27,28 @@ def test_library_exports_every_declared_symbol():
     for name in header_symbols():
         assert hasattr(lib, name), name
     assert lib.mbem_version() >= 1
+
+
+def test_multi_mesh_layout_rules():
+    """The batch layout check is host code: segments follow one another,
+    each rounded up to MBEM_MM_SEGMENT; anything else is refused."""
+    import ctypes
+    lib = _native.lib()
+
+    def meshes(sizes, offsets):
+        arr = (_native.MmMesh * len(sizes))()
+        for i, (n, o) in enumerate(zip(sizes, offsets)):
+            # placeholder (never dereferenced) 16-byte aligned pointers
+            arr[i] = _native.MmMesh(4096, (n + 3) // 4 * 4, n, o, 4096, 4096, 4096, 0, n)
+        return arr
+
+    seg = _native.MM_SEGMENT
+    sizes = [300, 2400, 9]
+    offs = [0, seg, seg + 5 * seg]
+    assert lib.mbem_mm_total(meshes(sizes, offs), 3) == seg + 5 * seg + seg
+    assert lib.mbem_mm_workspace_size(meshes(sizes, offs), 3, 50) > 0
+    assert lib.mbem_mm_total(meshes(sizes, [0, seg, 7 * seg]), 3) == -1          # a gap
+    assert lib.mbem_mm_total(meshes([300, 2400], [0, 300]), 2) == -1             # not rounded up
+    assert lib.mbem_mm_total(meshes([301], [0]), 1) == -1                        # not a multiple of 3
+    assert lib.mbem_mm_workspace_size(meshes(sizes, offs), 3, _native.MM_MAX_RESTART + 1) == 0
+    assert ctypes.sizeof(_native.MmMesh) == 72
