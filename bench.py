@@ -216,6 +216,20 @@ def run_ours(args, rank, ws):
             return rep, nnz
         return step
 
+    # the tile shapes of the operator products, chosen by the autotuner on
+    # this workload before the warm-up (a one-time setup, like a compile)
+    tuned = None
+    if args.precision == "mixed" and not args.skip_tune:
+        from mbem_gb300 import autotune
+        tb = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART, precision="mixed",
+                          precond=_precond_for("mixed"))
+        t0 = time.perf_counter()
+        tasm = tb.assemble(system, eps, arrays=arrays)
+        tuned = autotune.tune_mixed_operator(tasm, autotune.Autotuner(cache_path=""))
+        del tasm
+        tuned["s"] = time.perf_counter() - t0
+        torch.cuda.empty_cache()
+
     # headline: the mixed-precision path
     timer = []
     step = make_step(args.precision, timer)
@@ -344,6 +358,7 @@ def run_ours(args, rank, ws):
         "gpu_launches": int(launches),
         "roofline": roofline,
         "roofline_outer_matvec": roofline_outer,
+        "autotune": tuned,
         "fp64_peak_tflops": fp64_peak_tflops(),
     }
     clocks = clk.summary()
@@ -400,7 +415,14 @@ def multi_rhs_workload(peaks, n_face=24, n_fault=16, n_rhs=256):
         (X, rep), t_solve = _sync_time(lambda: bs.solve(B, rtol=RTOL))
         if timed:
             break
-        del bs, asm
+        # after the warm-up pass: the GEMM's K split, tuned on the solver's own operator
+        from mbem_gb300 import autotune
+        Vt = torch.randn((n_rhs, bs.A16.shape[1]), device="cuda").to(torch.bfloat16)
+        Wt = torch.empty((n_rhs, bs.n), device="cuda")
+        out["autotune"] = autotune.Autotuner(cache_path="").tune(
+            "gemm_split", f"M={bs.n},K={bs.A16.shape[1]},k={n_rhs}",
+            lambda: gemm_bf16_t(bs.A16, Vt, bs.A16.shape[1], Wt)).summary()
+        del Vt, Wt, bs, asm
         torch.cuda.empty_cache()
     total = t_asm + t_rhs + t_bf + t_solve
     n = bs.n
@@ -568,6 +590,10 @@ def multi_mesh_workload(peaks, n_mesh=64, lo=8, hi=32, seed=7):
     n_total = sum(a.op.n for a in systems)
     mb = MeshBatch(systems, restart=RESTART)
     B = mb.gather([a.b for a in systems])
+    from mbem_gb300 import autotune
+    t0 = time.perf_counter()
+    tuned = autotune.tune_mesh_batch(mb, autotune.Autotuner(cache_path=""))
+    tuned["s"] = time.perf_counter() - t0
     mb.solve(B, rtol=RTOL)                      # warm-up: captures the cycle graph
     launches0 = nat.lib().mbem_launch_count()
     (X, rep), t_batch = _sync_time(lambda: mb.solve(B, rtol=RTOL))
@@ -598,6 +624,7 @@ def multi_mesh_workload(peaks, n_mesh=64, lo=8, hi=32, seed=7):
                       "largest": max(a.op.n for a in systems), "smallest": min(a.op.n for a in systems),
                       "far_field_gb": mv_bytes / 1e9, "rtol": RTOL, "restart": RESTART},
            "assembly_s": t_asm,
+           "autotune": tuned,
            "batched": {"s": t_batch, "cycles": rep.cycles, "converged": rep.all_converged,
                        "iterations_max": max(rep.iterations), "iterations_mean": float(np.mean(rep.iterations)),
                        "worst_relres": max(rep.relres), "gpu_launches": int(launches)},
@@ -728,6 +755,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--skip-tune", action="store_true", help="keep the default tile shapes")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--skip-extra", action="store_true",

@@ -256,6 +256,21 @@ int mbem_inner_bf16_apply(const mbem_inner_bf16* p, const double* r, double* z, 
  * following applications time their products with CUDA events. */
 void mbem_inner_bf16_stats(int timing, int64_t* steps, int64_t* applies, double* matvec_ms);
 
+/* ---- tile configurations of the tunable kernel families (the autotuner's
+ * knobs). Each family has mbem_tune_count() candidates; the choice is
+ * process-wide (configuration 0 until set) and applies to the next launch. */
+enum {
+    MBEM_TUNE_MIXED_MATVEC = 0,   /* FP32 double-float matvec: rows x chunk x stages */
+    MBEM_TUNE_BF16_MATVEC = 1,    /* BF16 inner matvec: rows x chunk x stages */
+    MBEM_TUNE_MM_MATVEC = 2,      /* persistent multi-mesh matvec: chunk x stages */
+    MBEM_TUNE_GEMM_SPLIT = 3,     /* tensor-core GEMM K split: cost model or fixed */
+    MBEM_TUNE_FAMILIES = 4
+};
+int mbem_tune_count(int family);
+int mbem_tune_get(int family);
+int mbem_tune_set(int family, int config);
+int mbem_tune_describe(int family, int config, char* buf, int len);
+
 /* ---- many unevenly sized meshes in one solve. Each mesh keeps its mixed
  * operator (FP32 far field + FP64 near blocks by field point, the calibrated
  * diagonal inside them); the batch vectors hold the meshes' unknowns one

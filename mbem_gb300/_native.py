@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, Structure, c_double, c_int, c_int64, c_size_t, c_void_p
+from ctypes import POINTER, Structure, c_char_p, c_double, c_int, c_int64, c_size_t, c_void_p
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libmbem_gb300.so")
@@ -93,6 +93,8 @@ class MmReport(Structure):
 
 MM_SEGMENT = 512
 MM_MAX_RESTART = 64
+
+TUNE_MIXED_MATVEC, TUNE_BF16_MATVEC, TUNE_MM_MATVEC, TUNE_GEMM_SPLIT = 0, 1, 2, 3
 
 NN_FEAT, NN_HIDDEN = 16, 32
 NN_PARAMS = NN_HIDDEN * NN_FEAT + NN_HIDDEN + NN_HIDDEN * NN_HIDDEN + NN_HIDDEN + 9 * NN_HIDDEN + 9
@@ -182,6 +184,10 @@ _SIGNATURES = {
     "mbem_inner_bf16_apply": (c_int, [POINTER(InnerBf16), _P, _P, _P]),
     "mbem_inner_bf16_stats": (None, [c_int, POINTER(c_int64), POINTER(c_int64), POINTER(c_double)]),
     "mbem_mixed_matvec_noalloc": (c_int, [POINTER(MixedOperator), _P, _P, _P]),
+    "mbem_tune_count": (c_int, [c_int]),
+    "mbem_tune_get": (c_int, [c_int]),
+    "mbem_tune_set": (c_int, [c_int, c_int]),
+    "mbem_tune_describe": (c_int, [c_int, c_int, c_char_p, c_int]),
     "mbem_mm_total": (c_int64, [POINTER(MmMesh), c_int]),
     "mbem_mm_workspace_size": (c_size_t, [POINTER(MmMesh), c_int, c_int]),
     "mbem_mm_create": (c_int, [POINTER(MmMesh), c_int, c_int, _P, c_size_t, _P, POINTER(c_void_p)]),

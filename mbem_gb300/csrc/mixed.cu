@@ -28,6 +28,7 @@
 #include "dfloat.cuh"
 #include "p0_pair.cuh"
 #include "tma_pipe.cuh"
+#include "tune.cuh"
 
 namespace mbem {
 
@@ -717,20 +718,20 @@ __global__ void near_matvec_kernel(const int64_t* __restrict__ rowptr, const int
 // value read from shared memory serves two rows) accumulate in double-float.
 // The ring keeps ~216 KB per SM in flight independent of register pressure.
 // ---------------------------------------------------------------------------
-constexpr int TP_ROWS = 16;
-constexpr int TP_WARPS = TP_ROWS / 2;
-constexpr int TP_CH = 1024;              // columns per chunk (4 KB per row)
-constexpr int TP_STAGES = 3;
-constexpr int TP_THREADS = 32 * (TP_WARPS + 1);
-constexpr size_t TP_SMEM = (size_t)TP_STAGES * (TP_ROWS + 2) * TP_CH * sizeof(float) + 2 * TP_STAGES * 8;
+// Tile shape (template): TP_ROWS rows per CTA, TP_CH columns per chunk,
+// TP_STAGES ring stages; the tuned choice is in tune.cuh.
 constexpr uint32_t TP_WAIT_LIMIT = 1u << 26;
+template <int R, int CH, int S>
+constexpr size_t tp_smem() { return (size_t)S * (R + 2) * CH * sizeof(float) + 2 * S * 8; }
 
 // set by a pipeline wait that gave up; read (and cleared) by the host
 __device__ int g_mixed_wait_error = 0;
 
-__global__ void __launch_bounds__(TP_THREADS, 1)
+template <int TP_ROWS, int TP_CH, int TP_STAGES>
+__global__ void __launch_bounds__(32 * (TP_ROWS / 2 + 1))
 sgemv_df_tma_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_main, int64_t n_cols,
                     const float* __restrict__ xh, const float* __restrict__ xl, double* __restrict__ y) {
+    constexpr int TP_WARPS = TP_ROWS / 2;
     extern __shared__ __align__(128) unsigned char smem[];
     float* sA = reinterpret_cast<float*>(smem);                     // [S][ROWS][CH]
     float* sX = sA + TP_STAGES * TP_ROWS * TP_CH;                   // [S][2][CH]
@@ -751,7 +752,7 @@ sgemv_df_tma_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int
 
     if (warp == TP_WARPS) {
         // producer warp: lane 0 waits for the stage to drain and posts the
-        // byte count; lanes 0..nrow+1 then issue one copy each, in parallel
+        // byte count; the lanes then issue the nrow + 2 copies in parallel
         int64_t issued = 0;
         for (int64_t k = 0; k < nchunks; k++) {
             const int s = (int)(k % TP_STAGES);
@@ -768,12 +769,14 @@ sgemv_df_tma_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int
             const uint32_t bytes = (uint32_t)lmin(TP_CH, n_main - c0) * 4u;
             if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)(nrow + 2));
             __syncwarp();
-            if (lane < nrow)
-                bulk_g2s(sA + ((int64_t)s * TP_ROWS + lane) * TP_CH, A + (r0 + lane) * ld + c0, bytes, &full[s]);
-            else if (lane == TP_ROWS)
-                bulk_g2s(sX + (int64_t)s * 2 * TP_CH, xh + c0, bytes, &full[s]);
-            else if (lane == TP_ROWS + 1)
-                bulk_g2s(sX + ((int64_t)s * 2 + 1) * TP_CH, xl + c0, bytes, &full[s]);
+            for (int t = lane; t < TP_ROWS + 2; t += 32) {
+                if (t < nrow)
+                    bulk_g2s(sA + ((int64_t)s * TP_ROWS + t) * TP_CH, A + (r0 + t) * ld + c0, bytes, &full[s]);
+                else if (t == TP_ROWS)
+                    bulk_g2s(sX + (int64_t)s * 2 * TP_CH, xh + c0, bytes, &full[s]);
+                else if (t == TP_ROWS + 1)
+                    bulk_g2s(sX + ((int64_t)s * 2 + 1) * TP_CH, xl + c0, bytes, &full[s]);
+            }
             issued = k + 1;
         }
         // do not leave the block while copies into its shared memory are in flight
@@ -843,6 +846,40 @@ sgemv_df_tma_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int
     }
 }
 
+template <int R, int CH, int S>
+static int df_tma_launch(const float* A, int64_t ld, int64_t nr, int64_t n_main, int64_t nc, const float* xh,
+                         const float* xl, double* y, cudaStream_t st) {
+    constexpr size_t smem = tp_smem<R, CH, S>();
+    static_assert(smem <= 232448, "ring exceeds 227 KB of shared memory");
+    const cudaError_t e = cudaFuncSetAttribute(sgemv_df_tma_kernel<R, CH, S>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "sgemv smem attribute: %s", cudaGetErrorString(e));
+    sgemv_df_tma_kernel<R, CH, S><<<(unsigned)ceil_div(nr, R), 32 * (R / 2 + 1), smem, st>>>(A, ld, nr, n_main, nc,
+                                                                                             xh, xl, y);
+    return MBEM_OK;
+}
+
+// the FP32 double-float matvec with tile configuration `cfg` of kDfTiles
+static int launch_df_tma(int cfg, const float* A, int64_t ld, int64_t nr, int64_t n_main, int64_t nc,
+                         const float* xh, const float* xl, double* y, cudaStream_t st) {
+#define MBEM_DF_CASE(i)                                                                                  \
+    case i:                                                                                              \
+        return df_tma_launch<kDfTiles[i].rows, kDfTiles[i].ch, kDfTiles[i].stages>(A, ld, nr, n_main, nc, \
+                                                                                   xh, xl, y, st);
+    static_assert(count_of(kDfTiles) == 6, "one case per configuration");
+    switch (cfg) {
+        MBEM_DF_CASE(0)
+        MBEM_DF_CASE(1)
+        MBEM_DF_CASE(2)
+        MBEM_DF_CASE(3)
+        MBEM_DF_CASE(4)
+        MBEM_DF_CASE(5)
+        default: break;
+    }
+#undef MBEM_DF_CASE
+    return set_error(MBEM_ERR_ARG, "no FP32 matvec tile configuration %d", cfg);
+}
+
 // MBEM_ERR_WAIT if a pipeline wait gave up since the last check (the flag is
 // cleared); synchronises the stream.
 int mixed_wait_check(cudaStream_t st) {
@@ -868,11 +905,8 @@ int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, floa
     const bool xal = ((uintptr_t)xh % 16 == 0) && ((uintptr_t)xl % 16 == 0);
     const int64_t n_main = nc & ~(int64_t)3;
     if (xal && n_main > 0) {
-        cudaError_t e = cudaFuncSetAttribute(sgemv_df_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)TP_SMEM);
-        if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "sgemv smem attribute: %s", cudaGetErrorString(e));
-        sgemv_df_tma_kernel<<<(unsigned)ceil_div(nr, TP_ROWS), TP_THREADS, TP_SMEM, st>>>(
-            op->A32, op->ld32, nr, n_main, nc, xh, xl, y);
+        int e = launch_df_tma(tune_get(MBEM_TUNE_MIXED_MATVEC), op->A32, op->ld32, nr, n_main, nc, xh, xl, y, st);
+        if (e) return e;
     } else {
         const int64_t warps = ceil_div(nr, SGEMV_ROWS);
         sgemv_df_kernel<<<(unsigned)ceil_div(warps, SGEMV_THREADS / 32), SGEMV_THREADS, 0, st>>>(
@@ -898,12 +932,11 @@ int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, floa
 // FP32 over four chains each (the operator is a preconditioner: its 2^-9
 // entry rounding, not the summation, sets its accuracy).
 // ---------------------------------------------------------------------------
-constexpr int BP_ROWS = 16;
-constexpr int BP_WARPS = BP_ROWS / 2;    // consumer warps, two rows each
-constexpr int BP_CH = 2048;              // columns per chunk (4 KB of BF16 per row)
-constexpr int BP_STAGES = 3;
-constexpr int BP_THREADS = 32 * (BP_WARPS + 1);
-constexpr size_t BP_SMEM = (size_t)BP_STAGES * (BP_ROWS * BP_CH * 2 + BP_CH * 4) + 2 * BP_STAGES * 8;
+// Tile shape (template): BP_ROWS rows per CTA (BP_ROWS / 2 consumer warps),
+// BP_CH columns per chunk, BP_STAGES ring stages; the tuned choice is in
+// tune.cuh.
+template <int R, int CH, int S>
+constexpr size_t bp_smem() { return (size_t)S * (R * CH * 2 + CH * 4) + 2 * S * 8; }
 
 __global__ void d2f_kernel(const double* __restrict__ x, int64_t n, float* __restrict__ xf) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -913,9 +946,11 @@ __global__ void d2f_kernel(const double* __restrict__ x, int64_t n, float* __res
 __device__ __forceinline__ float bf16_lo(uint32_t u) { return __uint_as_float(u << 16); }
 __device__ __forceinline__ float bf16_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
 
-__global__ void __launch_bounds__(BP_THREADS, 1)
+template <int BP_ROWS, int BP_CH, int BP_STAGES>
+__global__ void __launch_bounds__(32 * (BP_ROWS / 2 + 1))
 sgemv_bf16_tma_kernel(const uint16_t* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_main, int64_t n_cols,
                       const float* __restrict__ xf, double* __restrict__ y) {
+    constexpr int BP_WARPS = BP_ROWS / 2;
     extern __shared__ __align__(128) unsigned char smem[];
     uint16_t* sA = reinterpret_cast<uint16_t*>(smem);                                // [S][ROWS][CH]
     float* sX = reinterpret_cast<float*>(sA + (size_t)BP_STAGES * BP_ROWS * BP_CH);   // [S][CH]
@@ -951,10 +986,12 @@ sgemv_bf16_tma_kernel(const uint16_t* __restrict__ A, int64_t ld, int64_t n_rows
             const uint32_t cols = (uint32_t)lmin(BP_CH, n_main - c0);
             if (lane == 0) mbar_arrive_expect_tx(&full[s], cols * 2u * (uint32_t)nrow + cols * 4u);
             __syncwarp();
-            if (lane < nrow)
-                bulk_g2s(sA + ((int64_t)s * BP_ROWS + lane) * BP_CH, A + (r0 + lane) * ld + c0, cols * 2u, &full[s]);
-            else if (lane == BP_ROWS)
-                bulk_g2s(sX + (int64_t)s * BP_CH, xf + c0, cols * 4u, &full[s]);
+            for (int t = lane; t < BP_ROWS + 1; t += 32) {
+                if (t < nrow)
+                    bulk_g2s(sA + ((int64_t)s * BP_ROWS + t) * BP_CH, A + (r0 + t) * ld + c0, cols * 2u, &full[s]);
+                else if (t == BP_ROWS)
+                    bulk_g2s(sX + (int64_t)s * BP_CH, xf + c0, cols * 4u, &full[s]);
+            }
             issued = k + 1;
         }
         if (lane == 0)
@@ -1017,6 +1054,40 @@ sgemv_bf16_tma_kernel(const uint16_t* __restrict__ A, int64_t ld, int64_t n_rows
     }
 }
 
+template <int R, int CH, int S>
+static int bf16_tma_launch(const uint16_t* A, int64_t ld, int64_t nr, int64_t n_main, int64_t nc, const float* xf,
+                           double* y, cudaStream_t st) {
+    constexpr size_t smem = bp_smem<R, CH, S>();
+    static_assert(smem <= 232448, "ring exceeds 227 KB of shared memory");
+    const cudaError_t e = cudaFuncSetAttribute(sgemv_bf16_tma_kernel<R, CH, S>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "bf16 gemv smem attribute: %s", cudaGetErrorString(e));
+    sgemv_bf16_tma_kernel<R, CH, S><<<(unsigned)ceil_div(nr, R), 32 * (R / 2 + 1), smem, st>>>(A, ld, nr, n_main,
+                                                                                               nc, xf, y);
+    return MBEM_OK;
+}
+
+// the BF16 matvec with tile configuration `cfg` of kBf16Tiles
+static int launch_bf16_tma(int cfg, const uint16_t* A, int64_t ld, int64_t nr, int64_t n_main, int64_t nc,
+                           const float* xf, double* y, cudaStream_t st) {
+#define MBEM_BF_CASE(i)                                                                                        \
+    case i:                                                                                                    \
+        return bf16_tma_launch<kBf16Tiles[i].rows, kBf16Tiles[i].ch, kBf16Tiles[i].stages>(A, ld, nr, n_main, nc, \
+                                                                                           xf, y, st);
+    static_assert(count_of(kBf16Tiles) == 6, "one case per configuration");
+    switch (cfg) {
+        MBEM_BF_CASE(0)
+        MBEM_BF_CASE(1)
+        MBEM_BF_CASE(2)
+        MBEM_BF_CASE(3)
+        MBEM_BF_CASE(4)
+        MBEM_BF_CASE(5)
+        default: break;
+    }
+#undef MBEM_BF_CASE
+    return set_error(MBEM_ERR_ARG, "no BF16 matvec tile configuration %d", cfg);
+}
+
 int bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_cols, int n_near,
                 const mbem_near_blocks* near, const double* x, double* y, float* xf, cudaStream_t st) {
     MBEM_REQUIRE(A16 && x && y && xf && n_rows >= 0 && n_cols >= 0 && ld16 >= n_cols, MBEM_ERR_ARG,
@@ -1026,12 +1097,9 @@ int bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_col
     MBEM_REQUIRE(n_near >= 0 && (n_near == 0 || near), MBEM_ERR_ARG, "bad near blocks");
     if (n_rows == 0) return MBEM_OK;
     d2f_kernel<<<(unsigned)ceil_div(n_cols > 0 ? n_cols : 1, 256), 256, 0, st>>>(x, n_cols, xf);
-    cudaError_t e = cudaFuncSetAttribute(sgemv_bf16_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)BP_SMEM);
-    if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "bf16 gemv smem attribute: %s", cudaGetErrorString(e));
     const int64_t n_main = n_cols & ~(int64_t)7;
-    sgemv_bf16_tma_kernel<<<(unsigned)ceil_div(n_rows, BP_ROWS), BP_THREADS, BP_SMEM, st>>>(
-        A16, ld16, n_rows, n_main, n_cols, xf, y);
+    int e = launch_bf16_tma(tune_get(MBEM_TUNE_BF16_MATVEC), A16, ld16, n_rows, n_main, n_cols, xf, y, st);
+    if (e) return e;
     for (int q = 0; q < n_near; q++) {
         const mbem_near_blocks& nb = near[q];
         near_matvec_kernel<<<(unsigned)ceil_div(nb.n_field, 8), 256, 0, st>>>(

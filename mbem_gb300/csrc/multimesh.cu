@@ -31,21 +31,21 @@
 #include "common.cuh"
 #include "dfloat.cuh"
 #include "tma_pipe.cuh"
+#include "tune.cuh"
 
 namespace mbem {
 
 constexpr int MM_SEG = MBEM_MM_SEGMENT;  // segment alignment = reduction chunk (columns)
 constexpr int MM_ROWS = 16;              // rows per work item
 constexpr int MM_WARPS = MM_ROWS / 2;    // consumer warps, two rows each
-constexpr int MM_CH = 1024;              // columns per ring chunk
-constexpr int MM_STAGES = 3;
 constexpr int MM_THREADS = 32 * (MM_WARPS + 1);
-constexpr size_t MM_SMEM = (size_t)MM_STAGES * (MM_ROWS + 2) * MM_CH * sizeof(float) + 2 * MM_STAGES * 8;
+// ring chunk (columns) and stages: template parameters, chosen from kMmTiles
+template <int CH, int S>
+constexpr size_t mm_smem() { return (size_t)S * (MM_ROWS + 2) * CH * sizeof(float) + 2 * S * 8; }
 constexpr uint32_t MM_WAIT_LIMIT = 1u << 26;
 constexpr int MM_RED = MM_SEG / 2;       // reduction threads per chunk (two columns each)
 constexpr int MM_MAXV = MBEM_MM_MAX_RESTART;
 
-static_assert(MM_SEG % MM_CH == 0 || MM_CH % MM_SEG == 0, "segment and ring chunk must nest");
 
 // set by a ring wait that gave up; read (and cleared) by the host
 __device__ int g_mm_wait_error = 0;
@@ -58,7 +58,8 @@ struct MMItem {
 // ---------------------------------------------------------------------------
 // the persistent batched operator: y[seg m] = A_m x[seg m] for active meshes
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(MM_THREADS, 1)
+template <int MM_CH, int MM_STAGES>
+__global__ void __launch_bounds__(MM_THREADS)
 mm_matvec_kernel(const mbem_mm_mesh* __restrict__ meshes, const MMItem* __restrict__ items, int64_t n_items,
                  const int* __restrict__ active, const float* __restrict__ xh, const float* __restrict__ xl,
                  double* __restrict__ y) {
@@ -492,6 +493,7 @@ struct mbem_mm_solver {
     double* mean = nullptr;     // n_mesh x 3
     cudaGraphExec_t cycle = nullptr;
     double cycle_rtol = -1.0;
+    int cycle_cfg = -1;            // tile configuration captured in the cycle
     long long cycle_kernels = 0;   // kernel nodes in the captured cycle
 };
 
@@ -594,12 +596,39 @@ size_t mm_layout(int n_mesh, int restart, const MMCounts& k, char* base, mbem_mm
 
 unsigned blocks(int64_t n, int t = 256) { return (unsigned)ceil_div(n > 0 ? n : 1, t); }
 
+template <int CH, int S>
+int mm_far_launch(mbem_mm_solver* s, double* y, const int* on, cudaStream_t st) {
+    constexpr size_t smem = mm_smem<CH, S>();
+    static_assert(smem <= 232448, "ring exceeds 227 KB of shared memory");
+    // one CTA per SM, or two where two rings fit
+    const unsigned grid = (unsigned)(s->grid * (2 * smem <= 232448 ? 2 : 1));
+    mm_matvec_kernel<CH, S><<<grid, MM_THREADS, smem, st>>>(s->d_meshes, s->d_items, s->n_items, on, s->xh,
+                                                           s->xl, y);
+    return MBEM_OK;
+}
+
+template <int CH, int S>
+cudaError_t mm_far_attribute() {
+    return cudaFuncSetAttribute(mm_matvec_kernel<CH, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)mm_smem<CH, S>());
+}
+
+#define MBEM_MM_CASES(X) X(0) X(1) X(2) X(3)
+static_assert(count_of(kMmTiles) == 4, "one case per configuration");
+
 // y = A x on the meshes flagged in `on`
 int mm_apply(mbem_mm_solver* s, const double* x, double* y, const int* on, cudaStream_t st) {
     mm_split_kernel<<<blocks(s->n_total), 256, 0, st>>>(x, s->n_total, s->xh, s->xl);
     mm_near_kernel<<<blocks(s->n_total * 32), 256, 0, st>>>(s->d_meshes, s->chunk_mesh, on, x, y, s->n_total);
-    mm_matvec_kernel<<<(unsigned)s->grid, MM_THREADS, MM_SMEM, st>>>(s->d_meshes, s->d_items, s->n_items, on,
-                                                                      s->xh, s->xl, y);
+    int e = set_error(MBEM_ERR_ARG, "no multi-mesh tile configuration %d", tune_get(MBEM_TUNE_MM_MATVEC));
+    switch (tune_get(MBEM_TUNE_MM_MATVEC)) {
+#define MBEM_MM_CASE(i) \
+        case i: e = mm_far_launch<kMmTiles[i].ch, kMmTiles[i].stages>(s, y, on, st); break;
+        MBEM_MM_CASES(MBEM_MM_CASE)
+#undef MBEM_MM_CASE
+        default: break;
+    }
+    if (e) return e;
     return launch_status("mm_matvec_kernel", 3);
 }
 
@@ -691,7 +720,12 @@ int mbem_mm_create(const mbem_mm_mesh* meshes, int n_mesh, int restart, void* wo
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     s->grid = sms > 0 ? sms : 1;
-    cudaError_t ce = cudaFuncSetAttribute(mm_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MM_SMEM);
+    // shared-memory limits of every tile configuration, set before any capture
+    cudaError_t ce = cudaSuccess;
+#define MBEM_MM_ATTR(i) \
+    if (ce == cudaSuccess) ce = mm_far_attribute<kMmTiles[i].ch, kMmTiles[i].stages>();
+    MBEM_MM_CASES(MBEM_MM_ATTR)
+#undef MBEM_MM_ATTR
     if (ce != cudaSuccess) {
         delete s;
         return set_error(MBEM_ERR_CUDA, "multi-mesh matvec smem attribute: %s", cudaGetErrorString(ce));
@@ -811,7 +845,7 @@ int mbem_mm_solve(mbem_mm_solver* s, const double* B, double* X, double rtol, in
         mm_cycle_start_kernel<<<blocks(nm, 64), 64, 0, st>>>(nm, m, s->rn2, s->g, s->jdone, s->active);
         mm_scale_kernel<<<blocks(nt), 256, 0, st>>>(s->R, s->V, s->rn2, 1, s->chunk_mesh, s->active, nt);
         if (use_graph) {
-            if (s->cycle == nullptr || s->cycle_rtol != rtol) {
+            if (s->cycle == nullptr || s->cycle_rtol != rtol || s->cycle_cfg != tune_get(MBEM_TUNE_MM_MATVEC)) {
                 if (s->cycle) {
                     cudaGraphExecDestroy(s->cycle);
                     s->cycle = nullptr;
@@ -838,6 +872,7 @@ int mbem_mm_solve(mbem_mm_solver* s, const double* B, double* X, double rtol, in
                     return set_error(MBEM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
                 }
                 s->cycle_rtol = rtol;
+                s->cycle_cfg = tune_get(MBEM_TUNE_MM_MATVEC);
             }
             cudaError_t ce = cudaGraphLaunch(s->cycle, st);
             if (ce != cudaSuccess) return set_error(MBEM_ERR_CUDA, "graph launch: %s", cudaGetErrorString(ce));

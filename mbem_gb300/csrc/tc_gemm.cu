@@ -21,6 +21,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "tune.cuh"
 #include "tma_pipe.cuh"
 
 namespace mbem {
@@ -300,7 +301,8 @@ static int gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, in
     const int64_t rows_out = trans ? n_rhs : M, cols_out = trans ? M : n_rhs;
     const int64_t slice = rows_out * cols_out;
     if (work != nullptr) {
-        splits = choose_splits(ceil_div(M, TC_BM), kb_all, sms);
+        const int forced = kGemmSplits[tune_get(MBEM_TUNE_GEMM_SPLIT)];
+        splits = forced > 0 ? (int)lmin(forced, kb_all) : choose_splits(ceil_div(M, TC_BM), kb_all, sms);
         while (splits > 1 && work_bytes < (size_t)splits * slice * sizeof(float)) splits--;
     }
     const int kb_per = (int)ceil_div(kb_all, splits);
