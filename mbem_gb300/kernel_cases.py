@@ -1,11 +1,15 @@
 """One launch (or a few) of a hot kernel on a small case, for profilers:
-``python -m mbem_gb300.kernel_cases tcgemm|traction|dfgemm|nodal``.
+``python -m mbem_gb300.kernel_cases <case>``.
 
 tcgemm    the block solver's GEMM: (20,736 x 62,208 BF16) x (62,208 x 256)
 traction  FAULT_TRACTION assembly, cube 16 x 16, fault 12 x 12, dip 60,
           with its block-Jacobi build (traction rows, bj_build_kernel)
 dfgemm    the block residual of the mixed operator, cube 24, 64 RHS
 nodal     the P2 DD-minus-eigen readout of a 16 x 16 fault at 20,000 points
+mixedmv   the FP32 double-float operator product, cube 24 (20,736 unknowns)
+bf16mv    the BF16 inner product of the mixed solve, cube 24
+mm        the persistent multi-mesh product: 8 cubes, grids drawn in [8, 20]
+readout   the mixed P2 stress readout: fault 32 x 32, 100,000 observers
 """
 
 from __future__ import annotations
@@ -53,6 +57,37 @@ def run(which: str) -> None:
         e = np.full(tv.shape[0], 0.01)
         for _ in range(2):
             tn.elastic_stress_contract(x, tv, nrm, e, d, 1.0, 1.0, order=2)
+    elif which in ("mixedmv", "bf16mv"):
+        from .la.mixed import Bf16Inner
+        model, eps = cube_fault_model(24, 16)
+        asm = DenseBackend(jump="calibrated", deflate=True, precision="mixed",
+                           precond="bf16_inner").assemble(generate_system(model), eps)
+        x = torch.randn(asm.op.n, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        inner = Bf16Inner(asm.op, 1, asm.u_ranges())
+        for _ in range(3):
+            (asm.op.matvec if which == "mixedmv" else inner.matvec)(x, out=y)
+    elif which == "mm":
+        from .la.multimesh import MeshBatch, random_cube_batch
+        be = DenseBackend(jump="calibrated", deflate=True, precision="mixed")
+        systems = [be.assemble(generate_system(m), e)
+                   for m, e in (cube_fault_model(nf, nq) for nf, nq in random_cube_batch(8, 8, 20, 3))]
+        mb = MeshBatch(systems)
+        x = torch.randn(mb.n_total, dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            mb.matvec(x)
+    elif which == "readout":
+        from . import mesh as M
+        from .kernels import tri_nodal as tn
+        fault = M.centre_fault(32)
+        tv = fault.tri_verts()
+        nrm, _ = fault.normals_and_areas()
+        rng = np.random.default_rng(0)
+        x = rng.uniform(-1, 1, size=(100000, 3))
+        d = rng.normal(size=(6 * tv.shape[0], 3))
+        e = np.full(tv.shape[0], 0.004)
+        for _ in range(2):
+            tn.elastic_stress_readout(x, tv, nrm, e, d, 1.0, 1.0, order=2)
     else:
         raise SystemExit(f"unknown case {which!r}")
     torch.cuda.synchronize()
