@@ -642,10 +642,46 @@ def multi_mesh_workload(peaks, n_mesh=64, lo=8, hi=32, seed=7):
     return out
 
 
+def p1_variant_workload(n_face=24, n_fault=16):
+    """The P1 variant of the 83k-unknown box: cube 24 x 24 per face at order 1
+    (three nodes per triangle, 62,208 unknowns), fault 16 x 16 at P0; the
+    mixed operator (nodal FP32 far quadrature, FP64 nodal near blocks) with
+    the BF16 inner solve against the plain FP64 nodal path, both from mesh
+    arrays to a 1e-8 true residual."""
+    import torch
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.model import generate_system
+    model, eps = cube_fault_model(n_face, n_fault, cube_order=1)
+    system = generate_system(model)
+    out = {"config": {"n_face": n_face, "n_fault": n_fault, "cube_order": 1, "fault_order": 0,
+                      "unknowns": system.layout.n_unknowns, "rtol": RTOL}}
+    res = {}
+    for name, kw in (("mixed", dict(precision="mixed", precond="bf16_inner")), ("fp64", dict())):
+        be = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART, **kw)
+        arrays = {}
+        for timed in (False, True):
+            asm, t_asm = _sync_time(lambda: be.assemble(system, eps, arrays=arrays))
+            x, t_solve = _sync_time(lambda: asm.solve_device())
+            if not timed:
+                del asm, x
+                torch.cuda.empty_cache()
+        rep = asm.report
+        res[name] = x.clone()
+        out[name] = {"s": t_asm + t_solve, "assembly_s": t_asm, "solve_s": t_solve, "iterations": rep.iterations,
+                     "true_relres": rep.true_relres, "converged": rep.converged}
+        del asm, x
+        torch.cuda.empty_cache()
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["s"] / out["mixed"]["s"]
+    out["max_rel_diff_mixed_vs_fp64_solution"] = float((res["mixed"] - res["fp64"]).norm() / res["fp64"].norm())
+    return out
+
+
 def extra_workloads(args, peaks):
     out = {}
     for name, fn in (("multi_rhs_cube24_256", lambda: multi_rhs_workload(peaks)),
                      ("multi_mesh_64_cubes", lambda: multi_mesh_workload(peaks)),
+                     ("p1_variant_cube24", p1_variant_workload),
                      ("fault_traction_cube32_learned", fault_traction_workload),
                      ("p2_readout_1m", p2_readout_workload)):
         try:

@@ -175,6 +175,24 @@ int mbem_far_matrix_bf16(int kernel, const double* x_field, int64_t n_field, con
                          const double* normals, const double* eps, int64_t n_src, const double* coeffs,
                          double near_factor, double alpha, float* out, int64_t ld_out, uint16_t* out16,
                          int64_t ld16, uint32_t* near_mask, void* stream);
+/* The same for a nodal source density of order 0/1/2: columns 3 (K s + k) + j
+ * (K = 1, 3, 6), node k's block by the far quadrature weighted with its
+ * Lagrange shape function; the near mask is per (field point, source). */
+int mbem_far_matrix_nodal(int kernel, int order, const double* x_field, int64_t n_field, const double* tri_verts,
+                          const double* normals, const double* eps, int64_t n_src, const double* coeffs,
+                          double near_factor, double alpha, float* out, int64_t ld_out, uint16_t* out16,
+                          int64_t ld16, uint32_t* near_mask, void* stream);
+/* FP64 nodal (order 1/2) blocks of the listed near pairs (rowptr/cols by
+ * field point over sources, nnz pairs): node k of pair q into
+ * vals[(K q + k) * 9 .. + 9], i.e. the near list by nodes (columns K s + k). */
+int mbem_near_eval_nodal(int kernel, int order, const double* x_field, int64_t n_field, const double* tri_verts,
+                         const double* normals, const double* eps, const int64_t* rowptr, const int64_t* cols,
+                         int64_t nnz, const double* coeffs, double alpha, double* vals, void* stream);
+/* The calibrated diagonal D (n_field x 3 x 3) of collocation point c = K s + kc
+ * added to the near blocks of its element's nodes K s + k with the collocation
+ * shape weights shape[kc * K + k]; *missing counts absent self blocks. */
+int mbem_near_add_diagonal_nodal(const int64_t* rowptr, const int64_t* cols, double* vals, int64_t n_field,
+                                 const double* D, int K, const double* shape, int* missing, void* stream);
 /* Near list from that bit mask: rowptr (n_field+1) and nnz on the host
  * (synchronises `stream`), then the source indices in increasing order. */
 int mbem_near_mask_count(const uint32_t* mask, int64_t n_field, int64_t n_src, int64_t* rowptr,

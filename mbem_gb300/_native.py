@@ -170,6 +170,9 @@ _SIGNATURES = {
                                   POINTER(FgmresReport), _P]),
     "mbem_far_matrix": (c_int, [c_int, _P, _I, _P, _P, _P, _I, _P, _D, _D, _P, _I, _P, _P]),
     "mbem_far_matrix_bf16": (c_int, [c_int, _P, _I, _P, _P, _P, _I, _P, _D, _D, _P, _I, _P, _I, _P, _P]),
+    "mbem_far_matrix_nodal": (c_int, [c_int, c_int, _P, _I, _P, _P, _P, _I, _P, _D, _D, _P, _I, _P, _I, _P, _P]),
+    "mbem_near_eval_nodal": (c_int, [c_int, c_int, _P, _I, _P, _P, _P, _P, _P, _I, _P, _D, _P, _P]),
+    "mbem_near_add_diagonal_nodal": (c_int, [_P, _P, _P, _I, _P, c_int, _P, _P, _P]),
     "mbem_near_mask_count": (c_int, [_P, _I, _I, _P, _P, c_size_t, POINTER(c_int64), _P]),
     "mbem_near_mask_fill": (c_int, [_P, _I, _I, _P, _P, _P]),
     "mbem_near_list_workspace_size": (c_size_t, [_I]),

@@ -208,8 +208,6 @@ class AssembledDense:
     # -- mixed precision: FP32 far field + FP64 near blocks -------------
     def _mixed_block(self, far_out, q, p, kernel, material, alpha, row0, col0, far16_out=None):
         from ..la.mixed import far_near_block
-        if p.order != 0 or q.order != 0:
-            raise NotImplementedError("the mixed-precision operator is P0 (order 0) only")
         if kernel not in (KERNEL_T, KERNEL_U):
             raise NotImplementedError("traction rows are not in the mixed-precision operator")
         f = self._patch_arrays(q)
@@ -217,10 +215,10 @@ class AssembledDense:
         if kernel == KERNEL_T:
             coeffs = kb.t_coeffs(material.mu, material.lam)
             return far_near_block("T", f["coll"], s["tv"], s["normals"], s["eps"], coeffs, alpha, far_out,
-                                  row0, col0, self.near_factor, self._timer, far16_out)
+                                  row0, col0, self.near_factor, self._timer, far16_out, p.order)
         coeffs = kb.u_coeffs(material.mu, material.lam)
         return far_near_block("U", f["coll"], s["tv"], s["normals"], s["eps"], coeffs, alpha, far_out, row0,
-                              col0, self.near_factor, self._timer, far16_out)
+                              col0, self.near_factor, self._timer, far16_out, p.order)
 
     def _build_mixed(self):
         from ..la.mixed import MixedOperator
@@ -277,8 +275,14 @@ class AssembledDense:
             if D is None:
                 continue
             Dd = (as_cuda(np.ascontiguousarray(D)) if not isinstance(D, torch.Tensor) else D.contiguous())
-            nat.call("mbem_near_add_diagonal", ptr(nl.rowptr), ptr(nl.cols), ptr(nl.vals), nl.n_field, ptr(Dd),
-                     ptr(missing), stream_handle())
+            shape = np.ascontiguousarray(t.field_patch.collocation_shape(), dtype=float)
+            if shape.shape[0] == 1:
+                nat.call("mbem_near_add_diagonal", ptr(nl.rowptr), ptr(nl.cols), ptr(nl.vals), nl.n_field,
+                         ptr(Dd), ptr(missing), stream_handle())
+            else:
+                # the free term on the element's own nodes by the collocation shape
+                nat.call("mbem_near_add_diagonal_nodal", ptr(nl.rowptr), ptr(nl.cols), ptr(nl.vals), nl.n_field,
+                         ptr(Dd), shape.shape[0], nat.dbl_array(shape.ravel()), ptr(missing), stream_handle())
         if int(missing.item()) != 0:
             raise RuntimeError("mixed precision: a collocation row has no self block in its near list")
         b = torch.zeros(n, dtype=torch.float64, device=dev)

@@ -35,8 +35,8 @@ namespace mbem {
 // ---------------------------------------------------------------------------
 // quadrature rules: collapsed Gauss-Legendre n x n on (0,0),(1,0),(0,1)
 // ---------------------------------------------------------------------------
-constexpr int QR_MIN = 3, QR_MAX = 6;
-constexpr int QR_POINTS = 9 + 16 + 25 + 36;
+constexpr int QR_MIN = 3, QR_MAX = 8;      // P0 uses n = 3..6; nodal densities up to 8
+constexpr int QR_POINTS = 9 + 16 + 25 + 36 + 49 + 64;
 
 struct QuadRules {
     float a[QR_POINTS];    // xi1 - 1/3
@@ -239,6 +239,112 @@ __device__ __forceinline__ void far_block(const QuadRules& Q, const SrcFar& s, c
     }
 }
 
+// Nodal (P1/P2) far blocks: the moments of far_block weighted by the
+// source's Lagrange shape functions at each quadrature point; node k's block
+// follows far_block's formula with node k's moments. Barycentric coordinates
+// of a point: l2 = a + 1/3, l3 = b + 1/3, l1 = 1 - l2 - l3 (tri_verts vertex
+// order); nodes P1 v1 v2 v3, P2 v1 v2 v3 m12 m23 m31.
+template <int ORDER>
+__device__ __forceinline__ void far_shape(float a, float b, float* N) {
+    const float l2 = a + (1.0f / 3.0f), l3 = b + (1.0f / 3.0f), l1 = 1.0f - l2 - l3;
+    if (ORDER == 1) {
+        N[0] = l1; N[1] = l2; N[2] = l3;
+    } else {
+        N[0] = l1 * (2.0f * l1 - 1.0f); N[1] = l2 * (2.0f * l2 - 1.0f); N[2] = l3 * (2.0f * l3 - 1.0f);
+        N[3] = 4.0f * l1 * l2; N[4] = 4.0f * l2 * l3; N[5] = 4.0f * l3 * l1;
+    }
+}
+
+template <bool TKERNEL, int ORDER>
+__device__ __forceinline__ void far_block_nodal(const QuadRules& Q, const SrcFar& s, const float dc[3], float D2,
+                                                const float c[6], float out[][3][3]) {
+    constexpr int K = ORDER == 1 ? 3 : 6;
+    // the shape functions raise the integrand's degree: ORDER more points a
+    // direction than the P0 rule at the same D / L
+    const int nq = min(far_rule(D2, s.L2) + ORDER, QR_MAX);
+    const int q0 = Q.off[nq], q1 = q0 + nq * nq;
+    float V3[K][3], V5[K][3], t[K][3], W[K][6], I1[K], I3[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        I1[k] = I3[k] = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 3; i++) V3[k][i] = V5[k][i] = t[k][i] = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 6; i++) W[k][i] = 0.0f;
+    }
+    for (int q = q0; q < q1; q++) {
+        const float a = Q.a[q], b = Q.b[q];
+        const float dx = dc[0] - (a * s.e1[0] + b * s.e2[0]);
+        const float dy = dc[1] - (a * s.e1[1] + b * s.e2[1]);
+        const float dz = dc[2] - (a * s.e1[2] + b * s.e2[2]);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float iR = rsqrtf(r2 + s.eps2);
+        const float w = Q.w[q];
+        const float iR2 = iR * iR;
+        const float w3 = w * iR2 * iR;
+        float N[K];
+        far_shape<ORDER>(a, b, N);
+        if (TKERNEL) {
+            const float w5 = w3 * iR2;
+            const float wt = w5 * r2;
+            const float wn = w5 * (dx * s.n[0] + dy * s.n[1] + dz * s.n[2]);
+            const float ux = wn * dx, uy = wn * dy, uz = wn * dz;
+            const float base[15] = {w3 * dx, w3 * dy, w3 * dz, w5 * dx, w5 * dy, w5 * dz, wt * dx, wt * dy, wt * dz,
+                                    ux * dx, ux * dy, ux * dz, uy * dy, uy * dz, uz * dz};
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    V3[k][i] = fmaf(N[k], base[i], V3[k][i]);
+                    V5[k][i] = fmaf(N[k], base[3 + i], V5[k][i]);
+                    t[k][i] = fmaf(N[k], base[6 + i], t[k][i]);
+                }
+#pragma unroll
+                for (int i = 0; i < 6; i++) W[k][i] = fmaf(N[k], base[9 + i], W[k][i]);
+            }
+        } else {
+            const float ux = w3 * dx, uy = w3 * dy, uz = w3 * dz;
+            const float base[8] = {w * iR, w3, ux * dx, ux * dy, ux * dz, uy * dy, uy * dz, uz * dz};
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                I1[k] = fmaf(N[k], base[0], I1[k]);
+                I3[k] = fmaf(N[k], base[1], I3[k]);
+#pragma unroll
+                for (int i = 0; i < 6; i++) W[k][i] = fmaf(N[k], base[2 + i], W[k][i]);
+            }
+        }
+    }
+    const float A = s.area2;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const float Wk[3][3] = {{W[k][0], W[k][1], W[k][2]}, {W[k][1], W[k][3], W[k][4]}, {W[k][2], W[k][4], W[k][5]}};
+        if (TKERNEL) {
+            const float* n = s.n;
+            const float nV3 = n[0] * V3[k][0] + n[1] * V3[k][1] + n[2] * V3[k][2];
+            const float nV5 = n[0] * V5[k][0] + n[1] * V5[k][1] + n[2] * V5[k][2];
+            const float ca = c[0] + 4.0f * c[1] + 2.0f * c[4];
+            const float cb = c[3] + c[4];
+            const float ce3 = c[2] * s.eps2, ce6 = c[5] * s.eps2;
+            const float gam = cb * nV3 + ce6 * nV5;
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                const float al = ca * V3[k][i] - 3.0f * c[1] * t[k][i] + ce3 * V5[k][i];
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    const float be = cb * V3[k][j] + ce6 * V5[k][j];
+                    out[k][i][j] = A * (n[j] * al + n[i] * be - 6.0f * c[4] * Wk[i][j] + (i == j ? gam : 0.0f));
+                }
+            }
+        } else {
+            const float dg = c[0] * I1[k] + c[1] * s.eps2 * I3[k];
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) out[k][i][j] = A * (c[2] * Wk[i][j] + (i == j ? dg : 0.0f));
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // far assembly: one thread per source, FIELD_TILE field points per block
 // ---------------------------------------------------------------------------
@@ -262,9 +368,10 @@ struct FarArgs {
     int64_t ld16;
 };
 
-template <bool TKERNEL>
+template <bool TKERNEL, int ORDER>
 __global__ void __launch_bounds__(FAR_THREADS)
 far_assemble_kernel(FarArgs a, QuadRules Q) {
+    constexpr int K = ORDER == 0 ? 1 : (ORDER == 1 ? 3 : 6);
     __shared__ F2 xs[FAR_FIELD_TILE][3];
     const int64_t s = (int64_t)blockIdx.x * FAR_THREADS + threadIdx.x;
     const bool active = s < a.n_src;
@@ -294,7 +401,7 @@ far_assemble_kernel(FarArgs a, QuadRules Q) {
         for (int ff = 0; ff < nf; ff++) {
             const int64_t f = f0 + ff;
             float d[3], D2;
-            float blk[3][3];
+            float blk[K][3][3];
             const bool near = is_near(xs[ff], src, d, D2) && active;
             if (a.near_mask) {
                 const unsigned m = __ballot_sync(0xffffffffu, near);
@@ -304,25 +411,34 @@ far_assemble_kernel(FarArgs a, QuadRules Q) {
             if (!active) continue;
             if (near || !src.ok) {
 #pragma unroll
-                for (int i = 0; i < 3; i++)
+                for (int k = 0; k < K; k++)
 #pragma unroll
-                    for (int j = 0; j < 3; j++) blk[i][j] = 0.0f;
+                    for (int i = 0; i < 3; i++)
+#pragma unroll
+                        for (int j = 0; j < 3; j++) blk[k][i][j] = 0.0f;
+            } else if (ORDER == 0) {
+                far_block<TKERNEL>(Q, src, d, D2, a.c, blk[0]);
             } else {
-                far_block<TKERNEL>(Q, src, d, D2, a.c, blk);
+                far_block_nodal<TKERNEL, ORDER>(Q, src, d, D2, a.c, blk);
             }
+            // columns 3 (K s + k) + j
 #pragma unroll
             for (int i = 0; i < 3; i++) {
-                float* row = a.out + (3 * f + i) * a.ld + 3 * s;
+                float* row = a.out + (3 * f + i) * a.ld + 3 * K * s;
 #pragma unroll
-                for (int j = 0; j < 3; j++) row[j] = a.alpha * blk[i][j];
+                for (int k = 0; k < K; k++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++) row[3 * k + j] = a.alpha * blk[k][i][j];
             }
             if (a.out16) {
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
-                    uint16_t* row = a.out16 + (3 * f + i) * a.ld16 + 3 * s;
+                    uint16_t* row = a.out16 + (3 * f + i) * a.ld16 + 3 * K * s;
 #pragma unroll
-                    for (int j = 0; j < 3; j++)
-                        row[j] = __bfloat16_as_ushort(__float2bfloat16_rn(a.alpha * blk[i][j]));
+                    for (int k = 0; k < K; k++)
+#pragma unroll
+                        for (int j = 0; j < 3; j++)
+                            row[3 * k + j] = __bfloat16_as_ushort(__float2bfloat16_rn(a.alpha * blk[k][i][j]));
                 }
             }
         }
@@ -513,6 +629,10 @@ __global__ void near_rowsum_kernel(const int64_t* __restrict__ rowptr, const dou
 }
 
 // add D[c] to the diagonal (self) block of row c, shape weights at P0 = 1
+struct ShapeKxK {
+    double w[36];
+};
+
 __global__ void near_add_diag_kernel(const int64_t* __restrict__ rowptr, const int64_t* __restrict__ cols,
                                      double* __restrict__ vals, int64_t n_field, const double* __restrict__ D,
                                      int* __restrict__ missing) {
@@ -526,6 +646,32 @@ __global__ void near_add_diag_kernel(const int64_t* __restrict__ rowptr, const i
         }
     }
     atomicAdd(missing, 1);
+}
+
+// the calibrated diagonal of collocation point c spread over its element's
+// K nodes by the collocation shape: vals of (c, node K s + k) += shape[kc][k] D_c
+__global__ void near_add_diag_nodal_kernel(const int64_t* __restrict__ rowptr, const int64_t* __restrict__ cols,
+                                           double* __restrict__ vals, int64_t n_field, const double* __restrict__ D,
+                                           int K, ShapeKxK shape, int* __restrict__ missing) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_field) return;
+    const int64_t s = c / K;
+    const int kc = (int)(c % K);
+    for (int k = 0; k < K; k++) {
+        const double w = shape.w[kc * K + k];
+        if (w == 0.0) continue;
+        const int64_t node = K * s + k;
+        bool found = false;
+        for (int64_t q = rowptr[c]; q < rowptr[c + 1]; q++) {
+            if (cols[q] == node) {
+#pragma unroll
+                for (int e = 0; e < 9; e++) vals[9 * q + e] += w * D[9 * c + e];
+                found = true;
+                break;
+            }
+        }
+        if (!found) atomicAdd(missing, 1);
+    }
 }
 
 // TwoSum of v into (h, l)
@@ -1126,9 +1272,19 @@ int mbem_far_matrix_bf16(int kernel, const double* x_field, int64_t n_field, con
                          const double* normals, const double* eps, int64_t n_src, const double* coeffs,
                          double near_factor, double alpha, float* out, int64_t ld_out, uint16_t* out16,
                          int64_t ld16, uint32_t* near_mask, void* stream) {
+    return mbem_far_matrix_nodal(kernel, 0, x_field, n_field, tri_verts, normals, eps, n_src, coeffs, near_factor,
+                                 alpha, out, ld_out, out16, ld16, near_mask, stream);
+}
+
+int mbem_far_matrix_nodal(int kernel, int order, const double* x_field, int64_t n_field, const double* tri_verts,
+                          const double* normals, const double* eps, int64_t n_src, const double* coeffs,
+                          double near_factor, double alpha, float* out, int64_t ld_out, uint16_t* out16,
+                          int64_t ld16, uint32_t* near_mask, void* stream) {
     MBEM_REQUIRE(kernel == 0 || kernel == 1, MBEM_ERR_ARG, "kernel must be 0 (T) or 1 (U)");
-    MBEM_REQUIRE(n_field >= 0 && n_src >= 0 && ld_out >= 3 * n_src, MBEM_ERR_ARG, "bad far matrix shape");
-    MBEM_REQUIRE(out16 == nullptr || ld16 >= 3 * n_src, MBEM_ERR_ARG, "bad BF16 copy stride");
+    MBEM_REQUIRE(order >= 0 && order <= 2, MBEM_ERR_ARG, "order must be 0, 1 or 2 (got %d)", order);
+    const int64_t Kn = order == 0 ? 1 : (order == 1 ? 3 : 6);
+    MBEM_REQUIRE(n_field >= 0 && n_src >= 0 && ld_out >= 3 * Kn * n_src, MBEM_ERR_ARG, "bad far matrix shape");
+    MBEM_REQUIRE(out16 == nullptr || ld16 >= 3 * Kn * n_src, MBEM_ERR_ARG, "bad BF16 copy stride");
     MBEM_REQUIRE(coeffs != nullptr && near_factor > 0.0, MBEM_ERR_ARG, "coeffs/near_factor");
     MBEM_REQUIRE(kernel == 1 || n_src == 0 || normals, MBEM_ERR_ARG, "normals is NULL");
     if (n_field == 0 || n_src == 0) return MBEM_OK;
@@ -1141,10 +1297,16 @@ int mbem_far_matrix_bf16(int kernel, const double* x_field, int64_t n_field, con
     a.near_mask = near_mask;
     a.out16 = out16; a.ld16 = ld16;
     dim3 grid((unsigned)ceil_div(n_src, FAR_THREADS), (unsigned)lmin(ceil_div(n_field, FAR_FIELD_TILE), 65535));
-    if (kernel == 0)
-        far_assemble_kernel<true><<<grid, FAR_THREADS, 0, (cudaStream_t)stream>>>(a, rules());
-    else
-        far_assemble_kernel<false><<<grid, FAR_THREADS, 0, (cudaStream_t)stream>>>(a, rules());
+    const cudaStream_t st = (cudaStream_t)stream;
+    const QuadRules& Q = rules();
+    switch (kernel * 3 + order) {
+        case 0: far_assemble_kernel<true, 0><<<grid, FAR_THREADS, 0, st>>>(a, Q); break;
+        case 1: far_assemble_kernel<true, 1><<<grid, FAR_THREADS, 0, st>>>(a, Q); break;
+        case 2: far_assemble_kernel<true, 2><<<grid, FAR_THREADS, 0, st>>>(a, Q); break;
+        case 3: far_assemble_kernel<false, 0><<<grid, FAR_THREADS, 0, st>>>(a, Q); break;
+        case 4: far_assemble_kernel<false, 1><<<grid, FAR_THREADS, 0, st>>>(a, Q); break;
+        default: far_assemble_kernel<false, 2><<<grid, FAR_THREADS, 0, st>>>(a, Q); break;
+    }
     return launch_status("far_assemble_kernel");
 }
 
@@ -1243,6 +1405,20 @@ int mbem_near_add_diagonal(const int64_t* rowptr, const int64_t* cols, double* v
     near_add_diag_kernel<<<(unsigned)ceil_div(n_field, 128), 128, 0, (cudaStream_t)stream>>>(rowptr, cols, vals,
                                                                                           n_field, D, missing);
     return launch_status("near_add_diag_kernel");
+}
+
+int mbem_near_add_diagonal_nodal(const int64_t* rowptr, const int64_t* cols, double* vals, int64_t n_field,
+                                 const double* D, int K, const double* shape, int* missing, void* stream) {
+    MBEM_REQUIRE(rowptr && D && missing && shape, MBEM_ERR_ARG, "bad near-diag args");
+    MBEM_REQUIRE(K == 1 || K == 3 || K == 6, MBEM_ERR_ARG, "K must be 1, 3 or 6 (got %d)", K);
+    MBEM_REQUIRE(n_field % K == 0, MBEM_ERR_ARG, "field points must be whole elements");
+    if (n_field == 0) return MBEM_OK;
+    ShapeKxK sh;
+    memset(&sh, 0, sizeof(sh));
+    for (int i = 0; i < K * K; i++) sh.w[i] = shape[i];
+    near_add_diag_nodal_kernel<<<(unsigned)ceil_div(n_field, 128), 128, 0, (cudaStream_t)stream>>>(
+        rowptr, cols, vals, n_field, D, K, sh, missing);
+    return launch_status("near_add_diag_nodal_kernel");
 }
 
 int mbem_bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_cols, int n_near,

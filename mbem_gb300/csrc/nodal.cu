@@ -1065,6 +1065,57 @@ int nodal_pairs_stress(const double* x, const double* tv, const double* normals,
 
 static int flags_for_matrix(int kind) { return (kind == 0 || kind == 2) ? KF_T : KF_U; }
 
+// The FP64 nodal blocks of listed near pairs (the mixed operator's near
+// field at order 1/2): pair q = (field point f, source s) from a CSR by field
+// point; node k's 3x3 block goes to vals[(K q + k) * 9], the layout of the
+// node-level near list (columns K s + k).
+__global__ void __launch_bounds__(ND_THREADS)
+nodal_near_eval_kernel(NodalArgs a, NodalSpec sp, int kind, const int64_t* __restrict__ rowptr,
+                       const int64_t* __restrict__ cols, int64_t nnz, double* __restrict__ vals) {
+    const int64_t q = (int64_t)blockIdx.x * ND_THREADS + threadIdx.x;
+    if (q >= nnz) return;
+    int64_t lo = 0, hi = a.n_field_pts;
+    while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (rowptr[mid] <= q) lo = mid;
+        else hi = mid;
+    }
+    const int64_t f = lo, s = cols[q];
+    const int K = sp.K;
+    NodalSrc g;
+    const bool ok = nodal_frame(a.tri_verts + 9 * s, g);
+    double W[4][ND_MAXK][5][5];
+    NodalScratch S;
+    double z = 0.0;
+    if (ok) z = nodal_pair_tables(sp, g, a.x_field + 3 * f, a.eps[s], W, S);
+    const double eps2 = a.eps[s] * a.eps[s];
+    const double* nrm = a.normals ? a.normals + 3 * s : nullptr;
+    for (int k = 0; k < K; k++) {
+        double* out = vals + 9 * (K * q + k);
+        if (!ok) {
+            for (int e = 0; e < 9; e++) out[e] = 0.0;
+            continue;
+        }
+        if (kind == 0) {
+            TScal ts;
+            node_tscal(W, k, z, ts);
+            TMoments m;
+            t_from_scal(g.ex, g.ey, g.nh, nrm, ts, m);
+            double blk[3][3];
+            t_block(m, nrm, a.c, eps2, blk);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) out[3 * i + j] = a.alpha * blk[i][j];
+        } else {
+            double I1 = 0.0, I3 = 0.0, T2[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            node_u(g, W, k, z, I1, I3, T2);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    out[3 * i + j] =
+                        a.alpha * (a.c[0] * (i == j ? I1 : 0.0) + a.c[1] * (i == j ? eps2 * I3 : 0.0) + a.c[2] * T2[i][j]);
+        }
+    }
+}
+
 int nodal_matrix(int kind, const double* x, int64_t nf, const double* tv, const double* normals,
                  const double* eps, int64_t ns, const double* coeffs, int order, double alpha, int accumulate,
                  double* out, int64_t ld, void* stream) {
@@ -1118,6 +1169,32 @@ int nodal_contract(int kind, const double* x, int64_t nf, const double* tv, cons
 }
 
 }  // namespace mbem
+
+extern "C" int mbem_near_eval_nodal(int kernel, int order, const double* x_field, int64_t n_field,
+                                    const double* tri_verts, const double* normals, const double* eps,
+                                    const int64_t* rowptr, const int64_t* cols, int64_t nnz, const double* coeffs,
+                                    double alpha, double* vals, void* stream) {
+    using namespace mbem;
+    MBEM_REQUIRE(kernel == 0 || kernel == 1, MBEM_ERR_ARG, "kernel must be 0 (T) or 1 (U)");
+    MBEM_REQUIRE(order == 1 || order == 2, MBEM_ERR_ARG, "nodal order must be 1 or 2 (order 0: mbem_near_eval)");
+    MBEM_REQUIRE(kernel == 1 || normals, MBEM_ERR_ARG, "normals is NULL");
+    MBEM_REQUIRE(coeffs && n_field >= 0 && nnz >= 0 && (nnz == 0 || (rowptr && cols && vals)), MBEM_ERR_ARG,
+                 "bad nodal near-eval args");
+    if (nnz == 0) return MBEM_OK;
+    int e = ensure_rules();
+    if (e) return e;
+    const NodalSpec sp = make_spec(order, kernel == 0 ? KF_T : KF_U);
+    MBEM_REQUIRE(sp.valid, MBEM_ERR_UNSUPPORTED, "nodal degrees beyond the P2 tables");
+    NodalArgs a;
+    memset(&a, 0, sizeof(a));
+    a.x_field = x_field; a.n_field_pts = n_field; a.tri_verts = tri_verts; a.normals = normals; a.eps = eps;
+    const int nc = kernel == 0 ? 6 : 3;
+    for (int i = 0; i < 6; i++) a.c[i] = i < nc ? coeffs[i] : 0.0;
+    a.alpha = alpha;
+    nodal_near_eval_kernel<<<(unsigned)ceil_div(nnz, ND_THREADS), ND_THREADS, 0, (cudaStream_t)stream>>>(
+        a, sp, kernel, rowptr, cols, nnz, vals);
+    return launch_status("nodal_near_eval_kernel");
+}
 
 extern "C" int mbem_traction_matrix(const double* x_field, const double* n_field, int64_t n_pts,
                                     const double* tri_verts, const double* normals, const double* eps,

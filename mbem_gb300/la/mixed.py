@@ -55,15 +55,18 @@ def near_list(x_field: torch.Tensor, tri_verts: torch.Tensor, eps: torch.Tensor,
 def far_near_block(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha: float,
                    far_out: torch.Tensor, row0: int = 0, col0: int = 0,
                    near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, timer=None,
-                   far16_out: torch.Tensor | None = None) -> NearList:
-    """Writes alpha * (far part) into ``far_out`` (FP32 (3Nf, 3Ns) view, zeros
-    at near pairs) and returns the near blocks alpha * (closed form) in FP64.
+                   far16_out: torch.Tensor | None = None, order: int = 0) -> NearList:
+    """Writes alpha * (far part) into ``far_out`` (FP32 (3Nf, 3 K Ns) view,
+    zeros at near pairs; K = 1, 3, 6 nodes per source for order 0, 1, 2) and
+    returns the near blocks alpha * (closed form; the nodal closed form at
+    order 1/2) in FP64, listed by field point over source nodes.
     ``far16_out``: an optional BF16 view of the same shape that receives the
     far part rounded to BF16 in the same pass."""
     k = _KERNEL_ID[kernel]
     nf, ns = x_field.shape[0], tri_verts.shape[0]
-    if far_out.dtype != torch.float32 or far_out.stride(1) != 1 or tuple(far_out.shape) != (3 * nf, 3 * ns):
-        raise ValueError("far_out must be a float32 (3Nf, 3Ns) view with unit column stride")
+    K = {0: 1, 1: 3, 2: 6}[int(order)]
+    if far_out.dtype != torch.float32 or far_out.stride(1) != 1 or tuple(far_out.shape) != (3 * nf, 3 * K * ns):
+        raise ValueError("far_out must be a float32 (3Nf, 3 K Ns) view with unit column stride")
     c = nat.dbl_array(coeffs)
     ev = None
     if timer is not None:
@@ -77,12 +80,10 @@ def far_near_block(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha:
     if far16_out is not None:
         if far16_out.dtype != torch.bfloat16 or far16_out.stride(1) != 1 or far16_out.shape != far_out.shape:
             raise ValueError("far16_out must be a bfloat16 view shaped like far_out with unit column stride")
-        nat.call("mbem_far_matrix_bf16", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ns, c,
-                 float(near_factor), float(alpha), ptr(far_out), far_out.stride(0), ptr(far16_out),
-                 far16_out.stride(0), ptr(mask), stream_handle())
-    else:
-        nat.call("mbem_far_matrix", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ns, c,
-                 float(near_factor), float(alpha), ptr(far_out), far_out.stride(0), ptr(mask), stream_handle())
+    nat.call("mbem_far_matrix_nodal", k, int(order), ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ns,
+             c, float(near_factor), float(alpha), ptr(far_out), far_out.stride(0),
+             ptr(far16_out) if far16_out is not None else None,
+             far16_out.stride(0) if far16_out is not None else 0, ptr(mask), stream_handle())
     if ev is not None:
         ev[1].record()
         timer.append(("far_" + kernel, nf, ns, ev[0], ev[1]))
@@ -95,10 +96,17 @@ def far_near_block(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha:
     cols = torch.empty(max(nnz.value, 1), dtype=torch.int64, device=x_field.device)[:nnz.value]
     nat.call("mbem_near_mask_fill", ptr(mask), nf, ns, ptr(rowptr), ptr(cols), stream_handle())
     del mask
-    vals = torch.empty((max(cols.numel(), 1), 9), dtype=torch.float64, device=x_field.device)[:cols.numel()]
-    nat.call("mbem_near_eval", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ptr(rowptr),
-             ptr(cols), cols.numel(), c, float(alpha), ptr(vals), stream_handle())
-    return NearList(row0, col0, nf, rowptr, cols, vals)
+    nnz = cols.numel()
+    vals = torch.empty((max(K * nnz, 1), 9), dtype=torch.float64, device=x_field.device)[:K * nnz]
+    if K == 1:
+        nat.call("mbem_near_eval", k, ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps), ptr(rowptr),
+                 ptr(cols), nnz, c, float(alpha), ptr(vals), stream_handle())
+        return NearList(row0, col0, nf, rowptr, cols, vals)
+    nat.call("mbem_near_eval_nodal", k, int(order), ptr(x_field), nf, ptr(tri_verts), ptr(normals), ptr(eps),
+             ptr(rowptr), ptr(cols), nnz, c, float(alpha), ptr(vals), stream_handle())
+    # the list by source nodes: pair q's node k is entry K q + k, column K s + k
+    node_cols = (cols.view(-1, 1) * K + torch.arange(K, device=cols.device)).reshape(-1).contiguous()
+    return NearList(row0, col0, nf, (rowptr * K).contiguous(), node_cols, vals)
 
 
 class MixedOperator:
