@@ -10,6 +10,9 @@ mixedmv   the FP32 double-float operator product, cube 24 (20,736 unknowns)
 bf16mv    the BF16 inner product of the mixed solve, cube 24
 mm        the persistent multi-mesh product: 8 cubes, grids drawn in [8, 20]
 readout   the mixed P2 stress readout: fault 32 x 32, 100,000 observers
+asm64     the FP64 P0 assembly of cube 12 (p0_matrix_kernel) and the FP64 P1
+          assembly of cube 8 (nodal_matrix_kernel)
+asm32     the mixed P0 assembly of cube 24 (far_assemble_kernel)
 """
 
 from __future__ import annotations
@@ -88,6 +91,13 @@ def run(which: str) -> None:
         e = np.full(tv.shape[0], 0.004)
         for _ in range(2):
             tn.elastic_stress_readout(x, tv, nrm, e, d, 1.0, 1.0, order=2)
+    elif which == "asm64":
+        for nf, nq, order in ((12, 8, 0), (8, 6, 1)):
+            model, eps = cube_fault_model(nf, nq, cube_order=order)
+            DenseBackend(jump="calibrated", deflate=True).assemble(generate_system(model), eps)
+    elif which == "asm32":
+        model, eps = cube_fault_model(24, 16)
+        DenseBackend(jump="calibrated", deflate=True, precision="mixed").assemble(generate_system(model), eps)
     else:
         raise SystemExit(f"unknown case {which!r}")
     torch.cuda.synchronize()
