@@ -274,6 +274,24 @@ int mbem_inner_bf16_apply(const mbem_inner_bf16* p, const double* r, double* z, 
  * following applications time their products with CUDA events. */
 void mbem_inner_bf16_stats(int timing, int64_t* steps, int64_t* applies, double* matvec_ms);
 
+/* ---- dense LU with partial pivoting in FP32 (la/lu.py Factor with FP32
+ * factors; the caller refines in FP64). In place on A (n x n at lda);
+ * piv[k] = the row exchanged with row k at step k (0-based, LAPACK order);
+ * *info (device int) = first zero pivot + 1, or 0. work: device memory of
+ * mbem_lu_workspace_size(n, SM count) bytes. The panel runs as a cooperative
+ * launch with bounded grid barriers (MBEM_ERR_WAIT if one runs out). */
+size_t mbem_lu_workspace_size(int64_t n, int sms);
+int mbem_lu_factor_f32(float* A, int64_t lda, int64_t n, int32_t* piv, void* work, size_t work_bytes, int* info,
+                       void* stream);
+/* x = A^-1 b from the factors (b, x FP64 device vectors; perm[i] = the
+ * original row at position i after all interchanges; xf: n floats). */
+/* Device ms of the factorisations' phases since the last call (panel,
+ * interchanges, triangular solve, operand split, tensor-core update); resets
+ * them and switches the phase timing of later factorisations on or off. */
+void mbem_lu_stats(int timing, double* phase_ms);
+int mbem_lu_solve_f32(const float* LU, int64_t lda, int64_t n, const int32_t* perm, const double* b, double* x,
+                      float* xf, void* stream);
+
 /* ---- tile configurations of the tunable kernel families (the autotuner's
  * knobs). Each family has mbem_tune_count() candidates; the choice is
  * process-wide (configuration 0 until set) and applies to the next launch. */

@@ -57,8 +57,12 @@ class DenseBackend:
             raise ValueError(mode)
         if jump not in ("half", "calibrated"):
             raise ValueError(jump)
-        if lu is not None:
-            raise ValueError("the GPU dense backend solves by FGMRES; lu= is not used")
+        if lu not in (None, "gpu", "single"):
+            raise ValueError(f"lu must be None (FGMRES), 'gpu' or 'single' (FP32 factors on the GPU, refined "
+                             f"in FP64); got {lu!r}")
+        if lu is not None and precision != "fp64":
+            raise ValueError("lu= factors the FP64 operator (precision='fp64')")
+        self.lu = lu
         if precision not in ("fp64", "mixed"):
             raise ValueError(f"precision must be 'fp64' or 'mixed' (got {precision!r})")
         self.mode = "direct"
@@ -83,7 +87,8 @@ class DenseBackend:
         (start, end) CUDA events around every kernel-block launch."""
         return AssembledDense(system, eps, jump=self.jump, deflate=self.deflate, rtol=self.rtol,
                               restart=self.restart, maxiter=self.maxiter, arrays=arrays, timer=timer,
-                              precision=self.precision, near_factor=self.near_factor, precond=self.precond)
+                              precision=self.precision, near_factor=self.near_factor, precond=self.precond,
+                              lu=self.lu)
 
 
 def _f32_matrix(rows: int, cols: int, dev, zero: bool = False) -> torch.Tensor:
@@ -128,11 +133,14 @@ class AssembledDense:
                  deflate: bool = False, rtol: float = 1e-10, restart: int = 50,
                  maxiter: int = defaults.GMRES_MAXITER, arrays: dict | None = None,
                  timer: list | None = None, precision: str = "fp64",
-                 near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, precond: str | None = None):
+                 near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, precond: str | None = None,
+                 lu: str | None = None):
         if jump not in ("half", "calibrated"):
             raise ValueError(jump)
         require_anchor_or_deflate(system, jump, deflate)
         require_cuda()
+        self.lu = lu
+        self._factor = None
         self._arrays_in = arrays
         self._timer = timer
         self.precision = precision
@@ -438,6 +446,55 @@ class AssembledDense:
         self._inner.rtol = float(tol)
         return self._inner
 
+    def factor(self):
+        """The FP32 GPU LU of this operator (the bordered one [[A, Z], [Z^T, 0]]
+        with deflation, backends/dense.py:538-566), refined against the FP64
+        operator; built once."""
+        from ..la.lu import Factor
+        if self._factor is not None:
+            return self._factor
+        if self.A is None:
+            raise ValueError("lu= needs the FP64 operator (precision='fp64')")
+        A = self.A
+        n = A.shape[0]
+        Z = translation_basis(self.layout) if self.deflate else np.zeros((n, 0))
+        m = Z.shape[1]
+        if m == 0:
+            self._factor = Factor(A)
+            return self._factor
+        Zd = as_cuda(np.ascontiguousarray(Z))
+        B32 = torch.zeros((n + m, n + m), dtype=torch.float32, device=A.device)
+        B32[:n, :n] = A
+        B32[:n, n:] = Zd
+        B32[n:, :n] = Zd.T
+
+        def bordered(x):
+            y = torch.empty_like(x)
+            nat.call("mbem_dgemv", ptr(A), A.stride(0), n, n, ptr(x), 1.0, 0.0, ptr(y), stream_handle())
+            y[:n] += Zd @ x[n:]
+            y[n:] = Zd.T @ x[:n]
+            return y
+        self._factor = Factor(None, bordered, lu32=B32)
+        return self._factor
+
+    def _solve_lu(self) -> torch.Tensor:
+        f = self.factor()
+        n = self.A.shape[0]
+        rhs = torch.zeros(f.n, dtype=torch.float64, device=self.A.device)
+        rhs[:n] = self.b
+        x = f.solve(rhs)[:n].contiguous()
+        # the deflated true residual |P (b - A x)| / |P b|, as FGMRES reports it
+        r = self.b - self.A @ x
+        pb = self.b.clone()
+        for off, size in self.u_ranges():
+            r[off:off + size].view(-1, 3).sub_(r[off:off + size].view(-1, 3).mean(dim=0))
+            pb[off:off + size].view(-1, 3).sub_(pb[off:off + size].view(-1, 3).mean(dim=0))
+        rel = float(r.norm() / pb.norm()) if float(pb.norm()) > 0 else 0.0
+        self.report = DenseSolveReport(converged=rel < max(self.rtol, 1e-12), iterations=int(f.report["passes"]),
+                                       true_relres=rel, arnoldi_relres=float(f.report["left"]))
+        self._x = x
+        return x
+
     def solve_device(self, rtol: float | None = None, restart: int | None = None,
                      maxiter: int | None = None, x0=None, time_matvec: bool = False,
                      precond=None) -> torch.Tensor:
@@ -445,6 +502,8 @@ class AssembledDense:
         and leaves ``self.report``. ``precond``: None (the backend's
         default), "none", "block_jacobi", or a preconditioner object
         (``la.precond.BlockJacobi``, ``la.learned.LearnedPreconditioner``)."""
+        if self.lu is not None and precond is None:
+            return self._solve_lu()
         precond = self.precond if precond is None else precond
         if precond == "none":
             precond = None

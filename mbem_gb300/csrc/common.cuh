@@ -56,6 +56,12 @@ int bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_col
 // z = the BF16 inner GMRES solve of r (precond kind 3).
 int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t st);
 
+// C[M x N] -= A[M x K] B[N x K]^T on the tensor cores (BF16 operands, FP32 C).
+int gemm_bf16_sub(const void* A, int64_t lda, const void* Bt, int64_t ldb, int64_t M, int64_t N, int64_t K, float* C,
+                  int64_t ldc, cudaStream_t st);
+// MBEM_ERR_WAIT if a tensor-core wait gave up since the last check (synchronises).
+int tc_gemm_check(cudaStream_t st);
+
 // MBEM_ERR_WAIT if a bounded pipeline wait of the mixed matvec gave up since
 // the last check; synchronises `st`.
 int mixed_wait_check(cudaStream_t st);

@@ -65,31 +65,46 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-template <int BN, bool TRANS>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+// SUB: Y[M x N] -= A B^T over column tiles of BN (blockIdx.y = the tile,
+// n_cols = N, the whole of K in each CTA); else Y (or its slice of the K
+// split blockIdx.y) = A B^T for n_cols <= BN columns.
+// ring stages: the update (short K, two CTAs an SM) keeps two
+template <bool SUB>
+constexpr int tc_stages() { return SUB ? 2 : TC_STAGES; }
+
+template <int BN, bool TRANS, bool SUB = false>
+__global__ void __launch_bounds__(TC_THREADS, SUB ? 2 : 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t M,
                int64_t K, float* __restrict__ Y, int64_t ldy, int n_cols, int kb_per, int64_t split_stride) {
     static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "MMA N for M = 128");
+    constexpr int NS = tc_stages<SUB>();
     constexpr int A_BYTES = TC_BM * TC_BK * 2;
     constexpr int B_BYTES = BN * TC_BK * 2;
     constexpr int STAGE = A_BYTES + B_BYTES;
     constexpr uint32_t TMEM_COLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
     extern __shared__ __align__(1024) uint8_t tc_smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], accum;
+    __shared__ __align__(8) uint64_t full[NS], empty[NS], accum;
     __shared__ uint32_t tmem_base;
+
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t m0 = (int64_t)blockIdx.x * TC_BM;
     // this CTA's share of K (a split of K over blockIdx.y; its partial sum
     // goes to slice blockIdx.y of Y)
     const int kb_all = (int)((K + TC_BK - 1) / TC_BK);
-    const int kb_first = (int)blockIdx.y * kb_per;
-    const int kb_total = min(kb_per, kb_all - kb_first);
-    Y += (int64_t)blockIdx.y * split_stride;
+    const int kb_first = SUB ? 0 : (int)blockIdx.y * kb_per;
+    const int kb_total = SUB ? kb_all : min(kb_per, kb_all - kb_first);
+    const int n0 = SUB ? (int)blockIdx.y * BN : 0;
+    if (SUB) {
+        Y += n0;
+        n_cols = min(BN, n_cols - n0);
+    } else {
+        Y += (int64_t)blockIdx.y * split_stride;
+    }
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < TC_STAGES; s++) {
+        for (int s = 0; s < NS; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
@@ -110,24 +125,24 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     if (warp == 4 && lane == 0) {
         // producer
         for (int kb = 0; kb < kb_total; kb++) {
-            const int s = kb % TC_STAGES;
-            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+            const int s = kb % NS;
+            const uint32_t ph = (uint32_t)(kb / NS) & 1u;
             if (!mbar_wait(&empty[s], ph ^ 1u, TC_WAIT_LIMIT)) atomicExch(&g_tc_error, 1);
             uint8_t* st = smem + s * STAGE;
             mbar_arrive_expect_tx(&full[s], STAGE);
             tma_load_2d(st, &mapA, (kb_first + kb) * TC_BK, (int)m0, &full[s]);
-            tma_load_2d(st + A_BYTES, &mapB, (kb_first + kb) * TC_BK, 0, &full[s]);
+            tma_load_2d(st + A_BYTES, &mapB, (kb_first + kb) * TC_BK, n0, &full[s]);
         }
         // the last copies have landed before the CTA can end
-        for (int kb = (kb_total > TC_STAGES ? kb_total - TC_STAGES : 0); kb < kb_total; kb++)
-            if (!mbar_wait(&full[kb % TC_STAGES], (uint32_t)(kb / TC_STAGES) & 1u, TC_WAIT_LIMIT))
+        for (int kb = (kb_total > NS ? kb_total - NS : 0); kb < kb_total; kb++)
+            if (!mbar_wait(&full[kb % NS], (uint32_t)(kb / NS) & 1u, TC_WAIT_LIMIT))
                 atomicExch(&g_tc_error, 1);
     } else if (warp == 5 && lane == 0) {
         // MMA issuer
         constexpr uint32_t idesc = f16_idesc(TC_BM, BN);
         for (int kb = 0; kb < kb_total; kb++) {
-            const int s = kb % TC_STAGES;
-            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+            const int s = kb % NS;
+            const uint32_t ph = (uint32_t)(kb / NS) & 1u;
             if (!mbar_wait(&full[s], ph, TC_WAIT_LIMIT)) atomicExch(&g_tc_error, 1);
             tc_fence_after();
             const uint32_t a0 = smem_addr(smem + s * STAGE), b0 = a0 + A_BYTES;
@@ -151,8 +166,66 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
                      : "memory");
     } else if (warp < 4) {
         // epilogue: row m0 + 32 warp + lane, BN columns from TMEM
+        if (SUB) {
+            // while the MMAs run: this warp's 32 rows of the Y tile into L2
+            const int64_t prow = m0 + 32 * warp + lane;
+            if (prow < M) {
+                const char* p0 = reinterpret_cast<const char*>(Y + prow * ldy);
+                for (int off = 0; off < n_cols * 4; off += 128)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(p0 + off));
+            }
+        }
         if (!mbar_wait(&accum, 0u, TC_WAIT_LIMIT)) atomicExch(&g_tc_error, 1);
         tc_fence_after();
+        if (SUB) {
+            // 32 columns at a time: TMEM -> registers -> this warp's block in
+            // shared memory -> Y, one row per pass with the lanes along it.
+            // Every MMA has completed (accum), so no copy or MMA still reads
+            // the ring.
+            const int64_t rbase = m0 + 32 * warp;
+            constexpr int CW = BN >= 64 ? 64 : 32;      // columns a pass
+            constexpr int LDE = CW + 1;
+            float* epi = reinterpret_cast<float*>(smem) + warp * 32 * LDE;
+#pragma unroll 1
+            for (int c = 0; c < BN; c += CW) {
+#pragma unroll
+                for (int h = 0; h < CW; h += 16) {
+                    uint32_t v[16];
+                    const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(c + h);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+                        "%12, %13, %14, %15}, [%16];"
+                        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                          "=r"(v[14]), "=r"(v[15])
+                        : "r"(ta));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                    for (int q = 0; q < 16; q++) epi[lane * LDE + h + q] = __uint_as_float(v[q]);
+                }
+                __syncwarp();
+                // the warp's 32 rows x CW columns: CW / 32 columns a lane, all
+                // loads in flight before the first subtraction
+                constexpr int PER = CW / 32;
+                float yv[32 * PER];
+#pragma unroll
+                for (int r = 0; r < 32; r++)
+#pragma unroll
+                    for (int t = 0; t < PER; t++) {
+                        const int col = c + 32 * t + lane;
+                        yv[r * PER + t] = (rbase + r < M && col < n_cols) ? Y[(rbase + r) * ldy + col] : 0.0f;
+                    }
+#pragma unroll
+                for (int r = 0; r < 32; r++)
+#pragma unroll
+                    for (int t = 0; t < PER; t++) {
+                        const int col = c + 32 * t + lane;
+                        if (rbase + r < M && col < n_cols)
+                            Y[(rbase + r) * ldy + col] = yv[r * PER + t] - epi[r * LDE + 32 * t + lane];
+                    }
+                __syncwarp();
+            }
+        } else {
         const int64_t row = m0 + 32 * warp + lane;
         float* yr = TRANS ? Y + row : Y + row * ldy;   // Y^T: element (row, c) at c ldy + row
 #pragma unroll 1
@@ -172,6 +245,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
                 for (int j = 0; j < 16; j++)
                     if (c + j < n_cols) yr[TRANS ? (int64_t)(c + j) * ldy : (c + j)] = __uint_as_float(v[j]);
             }
+        }
         }
     }
     tc_fence_before();
@@ -320,6 +394,40 @@ static int gemm_bf16(const void* A, int64_t lda, const void* Xt, int64_t ldx, in
 }
 
 size_t tc_gemm_workspace_size(int64_t M, int n_rhs) { return (size_t)8 * M * n_rhs * sizeof(float); }
+
+// C[M x N] -= A[M x K] B[N x K]^T (BF16 operands, FP32 C at ldc): column
+// tiles of 256 (fewer for a narrow N) over grid.y
+int gemm_bf16_sub(const void* A, int64_t lda, const void* Bt, int64_t ldb, int64_t M, int64_t N, int64_t K, float* C,
+                  int64_t ldc, cudaStream_t st) {
+    MBEM_REQUIRE(M >= 0 && N >= 0 && K >= 1 && A && Bt && C && lda >= K && ldb >= K && ldc >= N, MBEM_ERR_ARG,
+                 "bad GEMM-update arguments");
+    MBEM_REQUIRE(lda % 8 == 0 && ldb % 8 == 0 && (uintptr_t)A % 16 == 0 && (uintptr_t)Bt % 16 == 0, MBEM_ERR_ARG,
+                 "TMA needs 16-byte aligned bases and row strides (lda, ldb multiples of 8)");
+    MBEM_REQUIRE(N <= (int64_t)65535 * 256 && M <= (int64_t)0x7fffffff, MBEM_ERR_ARG, "GEMM update too large");
+    if (M == 0 || N == 0) return MBEM_OK;
+    int e = get_encode();
+    if (e) return e;
+    const int bn = N >= 256 ? 256 : (N > 128 ? 256 : (N > 64 ? 128 : (N > 32 ? 64 : (N > 16 ? 32 : 16))));
+    CUtensorMap ma, mb;
+    if ((e = make_map(&ma, A, M, K, lda, TC_BM))) return e;
+    if ((e = make_map(&mb, Bt, N, K, ldb, bn))) return e;
+    const dim3 grid((unsigned)ceil_div(M, TC_BM), (unsigned)ceil_div(N, bn));
+#define MBEM_SUB_LAUNCH(B)                                                                                    \
+    {                                                                                                         \
+        const size_t smem = (size_t)tc_stages<true>() * (TC_BM * TC_BK * 2 + B * TC_BK * 2) + 1024;          \
+        cudaFuncSetAttribute(tc_gemm_kernel<B, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        tc_gemm_kernel<B, false, true><<<grid, TC_THREADS, smem, st>>>(ma, mb, M, K, C, ldc, (int)N, 0, 0); \
+    }
+    switch (bn) {
+        case 16: MBEM_SUB_LAUNCH(16) break;
+        case 32: MBEM_SUB_LAUNCH(32) break;
+        case 64: MBEM_SUB_LAUNCH(64) break;
+        case 128: MBEM_SUB_LAUNCH(128) break;
+        default: MBEM_SUB_LAUNCH(256) break;
+    }
+#undef MBEM_SUB_LAUNCH
+    return launch_status("tc_gemm_kernel<sub>");
+}
 
 }  // namespace mbem
 

@@ -43,6 +43,11 @@ TRACTION_VALUE_NORMAL_TOL = 1e-12
 # ---- block-Jacobi preconditioner (defaults.py:712) ----
 PRECOND_BJ_CHUNK_DOF = 9000
 
+# ---- dense LU (defaults.py:1243-1261) ----
+LU_REFINE_TOL = 1.0e-10                # stop when what is left after a correction is this small
+LU_REFINE_PASSES = 4                   # at most this many corrections
+LU_REFINE_RATE = 1.0e-2                # corrections that contract worse than this: not single-precision material
+
 # ---- GPU mixed-precision path ----
 MIXED_BLOCK = 64                      # BF16 scale block (rows x columns)
 MIXED_NEAR_RADIUS_FACTOR = 3.0        # near field: centroid distance < 3 max(eps, h)

@@ -1,0 +1,142 @@
+"""A dense operator factored once on the GPU: LU with partial pivoting in
+FP32, every solve refined in FP64 (the reference's ``la/lu.py`` ``Factor``
+with ``how="gpu"``: src/mbem/la/lu.py:110-258).
+
+``Factor(A)`` factors a float64 CUDA matrix (kept: the refinement reads it)
+in single precision with the library's blocked GPU LU
+(``mbem_lu_factor_f32``); ``solve(B)`` returns ``A^-1 B`` in double by the
+reference's refinement: solve from the single factors, the residual in
+double, correct, stopped on the SIZE OF THE CORRECTION (what is left after a
+correction ``d`` that contracted at ``rho`` is ``rho / (1 - rho) |d|``,
+lu.py:22-31). Where the corrections do not contract the matrix is not
+single-precision material and ``solve`` raises (the reference falls back to
+LAPACK in double on the host; this path has no host fallback).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import time
+
+import numpy as np
+import torch
+
+from .. import _native as nat
+from .. import defaults
+from .._device import ptr, stream_handle
+
+
+class SingleFactorError(RuntimeError):
+    """The refinement from single-precision factors did not contract."""
+
+
+class Factor:
+    """``A`` (n, n) float64 CUDA, factored in FP32 on the device.
+    ``matvec(x) -> A x`` in FP64 overrides the product the refinement uses
+    (for an operator held in another form, e.g. a bordered one)."""
+
+    def __init__(self, A: torch.Tensor, matvec=None, lu32: torch.Tensor | None = None):
+        if A is not None and (A.dtype != torch.float64 or not A.is_cuda or A.dim() != 2
+                              or A.shape[0] != A.shape[1]):
+            raise ValueError("Factor: a square float64 CUDA matrix")
+        if A is not None and not torch.isfinite(A).all():
+            raise ValueError("factor: the matrix must not contain infs or NaNs")
+        self._A = A
+        self._matvec = matvec
+        if lu32 is None:
+            lu32 = A.to(torch.float32).contiguous()
+        self.n = n = int(lu32.shape[0])
+        self.report = {"how": "gpu"}
+        dev = lu32.device
+        t0 = time.perf_counter()
+        self.LU = lu32
+        self.piv = torch.empty(n, dtype=torch.int32, device=dev)
+        info = torch.zeros(1, dtype=torch.int32, device=dev)
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        size = int(nat.lib().mbem_lu_workspace_size(n, sms))
+        work = torch.empty(size, dtype=torch.uint8, device=dev)
+        nat.call("mbem_lu_factor_f32", ptr(self.LU), self.LU.stride(0), n, ptr(self.piv), ptr(work), size,
+                 ptr(info), stream_handle())
+        self.info = int(info.item())
+        # the pivots as one permutation: position i holds original row perm[i]
+        piv = self.piv.cpu().numpy()
+        perm = np.arange(n, dtype=np.int64)
+        for k, p in enumerate(piv):
+            if p != k:
+                perm[k], perm[p] = perm[p], perm[k]
+        self.perm = torch.from_numpy(perm.astype(np.int32)).to(dev)
+        self._xf = torch.empty(n, dtype=torch.float32, device=dev)
+        torch.cuda.synchronize(dev)
+        self.report["factor_s"] = time.perf_counter() - t0
+        if self.info:
+            raise np.linalg.LinAlgError(f"factor: the matrix is singular (zero pivot at column {self.info - 1})")
+
+    @property
+    def nbytes(self) -> int:
+        return 4 * self.n ** 2
+
+    def _single(self, b: torch.Tensor) -> torch.Tensor:
+        """A^-1 b from the single factors, as double (one column)."""
+        x = torch.empty_like(b)
+        nat.call("mbem_lu_solve_f32", ptr(self.LU), self.LU.stride(0), self.n, ptr(self.perm), ptr(b), ptr(x),
+                 ptr(self._xf), stream_handle())
+        return x
+
+    def _apply(self, x: torch.Tensor) -> torch.Tensor:
+        if self._matvec is not None:
+            return self._matvec(x)
+        y = torch.empty_like(x)
+        nat.call("mbem_dgemv", ptr(self._A), self._A.stride(0), self.n, self.n, ptr(x), 1.0, 0.0, ptr(y),
+                 stream_handle())
+        return y
+
+    def solve(self, B: torch.Tensor) -> torch.Tensor:
+        """A^-1 B for B (n,) or (n, k) float64 CUDA, refined in double."""
+        B = B.to(torch.float64)
+        cols = B.reshape(self.n, -1)
+        out = torch.empty_like(cols)
+        passes, worst_left, worst_size = 0, 0.0, 0.0
+        for j in range(cols.shape[1]):
+            b = cols[:, j].contiguous()
+            x = self._single(b)
+            xn = float(x.norm())
+            if xn == 0.0:
+                out[:, j] = x
+                continue
+            tol, before = defaults.LU_REFINE_TOL, None
+            done, rate, size, left, k = False, 0.0, 0.0, 0.0, 0
+            while not done and k < defaults.LU_REFINE_PASSES:
+                d = self._single((b - self._apply(x)).contiguous())
+                x += d
+                k += 1
+                now = float(d.norm()) / float(x.norm())
+                rate = now if before is None else (now / before if before > 0.0 else 0.0)
+                size, before = now, now
+                left = rate / (1.0 - rate) * size if rate < 1.0 else float("inf")
+                done = left <= tol or size <= tol
+                if rate > defaults.LU_REFINE_RATE:
+                    break
+            if not done:
+                raise SingleFactorError(
+                    f"dense LU in single precision: the refinement did not contract (rate {rate:.1e}, "
+                    f"{left:.1e} left after {k} corrections); the matrix is too ill-conditioned for "
+                    f"single-precision factors")
+            passes = max(passes, k)
+            if left >= worst_left:
+                worst_left, worst_size = left, size
+            out[:, j] = x
+        self.report["passes"] = max(passes, self.report.get("passes", 0))
+        self.report["correction"], self.report["left"] = worst_size, worst_left
+        return out.reshape(B.shape)
+
+
+def factor(A: torch.Tensor, matvec=None) -> Factor:
+    return Factor(A, matvec)
+
+
+def phase_stats(timing: bool = False) -> dict:
+    """Device ms of the factorisations' phases since the last call; switches
+    the phase timing of later factorisations on or off."""
+    arr = (ctypes.c_double * 5)()
+    nat.lib().mbem_lu_stats(int(timing), arr)
+    return dict(zip(("panel", "interchanges", "trsm", "split", "update"), list(arr)))
