@@ -285,6 +285,13 @@ int mbem_lu_factor_f32(float* A, int64_t lda, int64_t n, int32_t* piv, void* wor
                        void* stream);
 /* x = A^-1 b from the factors (b, x FP64 device vectors; perm[i] = the
  * original row at position i after all interchanges; xf: n floats). */
+/* X = A^-1 B for k right-hand sides (row-major FP64 n x k at ldb / ldx) from
+ * the FP32 factors: blocked triangular solves with tensor-core updates
+ * (FP32-accurate); work: mbem_lu_solve_many_workspace_size(n, k) bytes. */
+size_t mbem_lu_solve_many_workspace_size(int64_t n, int64_t k);
+int mbem_lu_solve_many_f32(const float* LU, int64_t lda, int64_t n, const int32_t* perm, const double* B,
+                           int64_t ldb, int64_t k, double* X, int64_t ldx, void* work, size_t work_bytes,
+                           void* stream);
 /* Device ms of the factorisations' phases since the last call (panel,
  * interchanges, triangular solve, operand split, tensor-core update); resets
  * them and switches the phase timing of later factorisations on or off. */
@@ -481,6 +488,11 @@ size_t mbem_gemm_bf16_workspace_size(int64_t M, int n_rhs);
 int mbem_gemm_bf16_t_split(const void* A, int64_t lda, const void* Xt, int64_t ldx, int64_t M, int64_t K,
                            int n_rhs, float* Yt, int64_t ldy, void* work, size_t work_bytes, void* stream);
 int mbem_gemm_bf16_check(void* stream);
+/* C[M x N] -= A[M x K] Bt[N x K]^T on the tensor cores (BF16 row-major
+ * operands, lda and ldb multiples of 8; FP32 C at ldc): the update of the
+ * blocked LU and its solves. */
+int mbem_gemm_bf16_sub(const void* A, int64_t lda, const void* Bt, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                       float* C, int64_t ldc, void* stream);
 
 /* ---- batched GMRES for a block of k right-hand sides (k Krylov iterations
  * sharing one GEMM per step; la/solver.py:115-245 per right-hand side).

@@ -187,10 +187,13 @@ _SIGNATURES = {
     "mbem_inner_bf16_apply": (c_int, [POINTER(InnerBf16), _P, _P, _P]),
     "mbem_inner_bf16_stats": (None, [c_int, POINTER(c_int64), POINTER(c_int64), POINTER(c_double)]),
     "mbem_mixed_matvec_noalloc": (c_int, [POINTER(MixedOperator), _P, _P, _P]),
+    "mbem_gemm_bf16_sub": (c_int, [_P, _I, _P, _I, _I, _I, _I, _P, _I, _P]),
     "mbem_lu_workspace_size": (c_size_t, [_I, c_int]),
     "mbem_lu_factor_f32": (c_int, [_P, _I, _I, _P, _P, c_size_t, _P, _P]),
     "mbem_lu_solve_f32": (c_int, [_P, _I, _I, _P, _P, _P, _P, _P]),
     "mbem_lu_stats": (None, [c_int, POINTER(c_double)]),
+    "mbem_lu_solve_many_workspace_size": (c_size_t, [_I, _I]),
+    "mbem_lu_solve_many_f32": (c_int, [_P, _I, _I, _P, _P, _I, _I, _P, _I, _P, c_size_t, _P]),
     "mbem_tune_count": (c_int, [c_int]),
     "mbem_tune_get": (c_int, [c_int]),
     "mbem_tune_set": (c_int, [c_int, c_int]),

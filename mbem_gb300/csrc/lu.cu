@@ -10,7 +10,8 @@
 //      every CTA picks the same pivot (largest |value|, then lowest row),
 //      swaps and eliminates its own rows;
 //   2. the panel's row interchanges applied to the other columns;
-//   3. U12 = L11^-1 A12 (unit lower triangle, one column a thread);
+//   3. U12 = L11^-1 A12 (unit lower triangle, one column a thread:
+//      lu_block_trsm_kernel, also the diagonal blocks of the solves);
 //   4. A22 -= L21 U12 on the tensor cores: both operands split into three
 //      BF16 pieces, the six piece products of order <= 2 in one tcgen05 GEMM
 //      (FP32 accumulation in TMEM) subtracted from A22 in its epilogue.
@@ -240,32 +241,6 @@ __global__ void lu_swap_kernel(float* __restrict__ A, int64_t lda, int64_t n, in
     }
 }
 
-// U12 = L11^-1 A12: one thread a column, the unit lower triangle in shared memory
-__global__ void __launch_bounds__(128)
-lu_trsm_kernel(float* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nbw) {
-    __shared__ float L[LU_NB][LU_NB + 1];
-    for (int e = threadIdx.x; e < LU_NB * LU_NB; e += blockDim.x) {
-        const int r = e / LU_NB, c = e % LU_NB;
-        L[r][c] = (r < nbw && c < nbw) ? A[(k + r) * lda + k + c] : 0.0f;
-    }
-    __syncthreads();
-    const int64_t col = k + nbw + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= n) return;
-    float x[LU_NB];
-#pragma unroll
-    for (int r = 0; r < LU_NB; r++) x[r] = r < nbw ? A[(k + r) * lda + col] : 0.0f;
-#pragma unroll
-    for (int r = 1; r < LU_NB; r++) {
-        float s = x[r];
-#pragma unroll
-        for (int c = 0; c < r; c++) s = fmaf(-L[r][c], x[c], s);
-        x[r] = s;
-    }
-#pragma unroll
-    for (int r = 0; r < LU_NB; r++)
-        if (r < nbw) A[(k + r) * lda + col] = x[r];
-}
-
 // ---- the trailing update on the tensor cores --------------------------------
 // FP32 x = hi + mid + lo in three BF16 pieces (24 significant bits); the
 // product of two such is taken over the six pieces pairs of order <= 2
@@ -285,30 +260,34 @@ __device__ __forceinline__ void bf16_pieces(float x, uint16_t& hi, uint16_t& mid
     lo = __bfloat16_as_ushort(__float2bfloat16_rn(r2));
 }
 
-// Ls[r][6 x 64]: the pieces of L21 = A[k + nbw + r][k .. k + nbw)
-__global__ void lu_split_l_kernel(const float* __restrict__ A, int64_t lda, int64_t k, int nbw, int64_t M,
-                                  uint16_t* __restrict__ Ls) {
+// Ls[r][6 x 64]: the pieces of rows row0 + r (r < M) of a row-major FP32
+// matrix at columns col0 .. col0 + nbw (L21 in the factorisation, the L or U
+// panel of a blocked solve)
+__global__ void lu_split_rows_kernel(const float* __restrict__ A, int64_t lda, int64_t row0, int64_t col0, int nbw,
+                                     int64_t M, uint16_t* __restrict__ Ls) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= M * LU_NB) return;
     const int64_t r = e / LU_NB;
     const int kk = (int)(e % LU_NB);
-    const float x = kk < nbw ? A[(k + nbw + r) * lda + k + kk] : 0.0f;
+    const float x = kk < nbw ? A[(row0 + r) * lda + col0 + kk] : 0.0f;
     uint16_t h, m, l;
     bf16_pieces(x, h, m, l);
     uint16_t* o = Ls + r * LU_K6 + kk;
     o[0] = h; o[LU_NB] = h; o[2 * LU_NB] = h; o[3 * LU_NB] = m; o[4 * LU_NB] = m; o[5 * LU_NB] = l;
 }
 
-// Us[j][6 x 64]: the pieces of column j of U12 = A[k .. k + nbw)[k + nbw + j]
-// (a 64 x 32 tile through shared memory: coalesced reads and writes)
+// Us[j][6 x 64]: the pieces of column col0 + j (j < N) of rows row0 ..
+// row0 + nbw of a row-major FP32 matrix (U12 in the factorisation, a block of
+// right-hand sides in a solve); a 64 x 32 tile through shared memory keeps
+// reads and writes coalesced
 __global__ void __launch_bounds__(256)
-lu_split_u_kernel(const float* __restrict__ A, int64_t lda, int64_t k, int nbw, int64_t N,
-                  uint16_t* __restrict__ Us) {
+lu_split_cols_kernel(const float* __restrict__ A, int64_t lda, int64_t row0, int64_t col0, int nbw, int64_t N,
+                     uint16_t* __restrict__ Us) {
     __shared__ float T[LU_NB][33];
     const int64_t j0 = (int64_t)blockIdx.x * 32;
     for (int e = threadIdx.x; e < LU_NB * 32; e += 256) {
         const int kk = e / 32, j = e % 32;
-        T[kk][j] = (kk < nbw && j0 + j < N) ? A[(k + kk) * lda + k + nbw + j0 + j] : 0.0f;
+        T[kk][j] = (kk < nbw && j0 + j < N) ? A[(row0 + kk) * lda + col0 + j0 + j] : 0.0f;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < LU_NB * 32; e += 256) {
@@ -319,6 +298,62 @@ lu_split_u_kernel(const float* __restrict__ A, int64_t lda, int64_t k, int nbw, 
         uint16_t* o = Us + (j0 + j) * LU_K6 + kk;
         o[0] = h; o[LU_NB] = m; o[2 * LU_NB] = l; o[3 * LU_NB] = h; o[4 * LU_NB] = m; o[5 * LU_NB] = h;
     }
+}
+
+// X[r0 .. r0 + nb) (ncols columns at ldx) = T^-1 X with T the nb x nb
+// diagonal block of LU at (r0, r0): its unit lower triangle (lower) or its
+// upper triangle; one thread a column
+__global__ void __launch_bounds__(128)
+lu_block_trsm_kernel(const float* __restrict__ LU, int64_t lda, float* __restrict__ X, int64_t ldx, int64_t ncols,
+                     int64_t r0, int nb, int lower) {
+    __shared__ float T[LU_NB][LU_NB + 1];
+    for (int e = threadIdx.x; e < LU_NB * LU_NB; e += blockDim.x) {
+        const int r = e / LU_NB, c = e % LU_NB;
+        T[r][c] = (r < nb && c < nb) ? LU[(r0 + r) * lda + r0 + c] : (r == c ? 1.0f : 0.0f);
+    }
+    __syncthreads();
+    const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= ncols) return;
+    float x[LU_NB];
+#pragma unroll
+    for (int r = 0; r < LU_NB; r++) x[r] = r < nb ? X[(r0 + r) * ldx + col] : 0.0f;
+    if (lower) {
+#pragma unroll
+        for (int r = 1; r < LU_NB; r++) {
+            float v = x[r];
+#pragma unroll
+            for (int c = 0; c < r; c++) v = fmaf(-T[r][c], x[c], v);
+            x[r] = v;
+        }
+    } else {
+#pragma unroll
+        for (int r = LU_NB - 1; r >= 0; r--) {
+            float v = x[r];
+#pragma unroll
+            for (int c = r + 1; c < LU_NB; c++) v = fmaf(-T[r][c], x[c], v);
+            x[r] = v / T[r][r];
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < LU_NB; r++)
+        if (r < nb) X[(r0 + r) * ldx + col] = x[r];
+}
+
+// X32[i][j] = B[perm[i]][j] (FP64 to FP32) and back
+__global__ void lu_gather_rows_kernel(const double* __restrict__ B, int64_t ldb, const int32_t* __restrict__ perm,
+                                      int64_t n, int64_t k, float* __restrict__ X, int64_t ldx) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * k) return;
+    const int64_t i = e / k, j = e % k;
+    X[i * ldx + j] = (float)B[(int64_t)perm[i] * ldb + j];
+}
+
+__global__ void lu_widen_rows_kernel(const float* __restrict__ X, int64_t ldx, int64_t n, int64_t k,
+                                     double* __restrict__ Y, int64_t ldy) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * k) return;
+    const int64_t i = e / k, j = e % k;
+    Y[i * ldy + j] = (double)X[i * ldx + j];
 }
 
 // ---- solves ---------------------------------------------------------------
@@ -451,11 +486,13 @@ int mbem_lu_factor_f32(float* A, int64_t lda, int64_t n, int32_t* piv, void* wor
         mark();
         const int64_t rest = n - k - nbw;
         if (rest > 0) {
-            lu_trsm_kernel<<<(unsigned)ceil_div(rest, 128), 128, 0, st>>>(A, lda, n, k, nbw);
+            lu_block_trsm_kernel<<<(unsigned)ceil_div(rest, 128), 128, 0, st>>>(A, lda, A + k + nbw, lda, rest, k, nbw,
+                                                                               1);
             mark();
             // A22 -= L21 U12 on the tensor cores (six BF16 piece products, FP32 accumulation)
-            lu_split_l_kernel<<<(unsigned)ceil_div(rest * LU_NB, 256), 256, 0, st>>>(A, lda, k, nbw, rest, Ls);
-            lu_split_u_kernel<<<(unsigned)ceil_div(rest, 32), 256, 0, st>>>(A, lda, k, nbw, rest, Us);
+            lu_split_rows_kernel<<<(unsigned)ceil_div(rest * LU_NB, 256), 256, 0, st>>>(A, lda, k + nbw, k, nbw, rest,
+                                                                                       Ls);
+            lu_split_cols_kernel<<<(unsigned)ceil_div(rest, 32), 256, 0, st>>>(A, lda, k, k + nbw, nbw, rest, Us);
             launches += 3;
             mark();
             int ge = gemm_bf16_sub(Ls, LU_K6, Us, LU_K6, rest, rest, LU_K6, A + (k + nbw) * lda + k + nbw, lda, st);
@@ -527,6 +564,63 @@ int mbem_lu_solve_f32(const float* LU, int64_t lda, int64_t n, const int32_t* pe
     }
     lu_widen_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(xf, n, x);
     return launch_status("lu_solve", (int)launches + 1);
+}
+
+size_t mbem_lu_solve_many_workspace_size(int64_t n, int64_t k) {
+    return ((size_t)n * k * sizeof(float) + 255) / 256 * 256 + ((size_t)n * LU_K6 * 2 + 255) / 256 * 256 +
+           ((size_t)k * LU_K6 * 2 + 255) / 256 * 256;
+}
+
+// X = (P L U)^-1 B for k right-hand sides (B, X row-major FP64 n x k at ldb,
+// ldx): blocked triangular solves, each 64-row block's triangle by
+// lu_block_trsm_kernel and the update of the rows below (forward) or above
+// (backward) as a tensor-core GEMM of six BF16 piece products.
+int mbem_lu_solve_many_f32(const float* LU, int64_t lda, int64_t n, const int32_t* perm, const double* B,
+                           int64_t ldb, int64_t k, double* X, int64_t ldx, void* work, size_t work_bytes,
+                           void* stream) {
+    MBEM_REQUIRE(LU && perm && B && X && n >= 1 && k >= 1 && lda >= n && ldb >= k && ldx >= k, MBEM_ERR_ARG,
+                 "bad LU multi-solve arguments");
+    const size_t need = mbem_lu_solve_many_workspace_size(n, k);
+    MBEM_REQUIRE(work && work_bytes >= need, MBEM_ERR_SIZE, "LU multi-solve workspace %zu < %zu bytes", work_bytes,
+                 need);
+    cudaStream_t st = (cudaStream_t)stream;
+    char* w = (char*)work;
+    float* X32 = (float*)w;
+    w += ((size_t)n * k * sizeof(float) + 255) / 256 * 256;
+    uint16_t* Lp = (uint16_t*)w;
+    w += ((size_t)n * LU_K6 * 2 + 255) / 256 * 256;
+    uint16_t* Xp = (uint16_t*)w;
+    const unsigned g_nk = (unsigned)ceil_div(n * k, 256);
+    lu_gather_rows_kernel<<<g_nk, 256, 0, st>>>(B, ldb, perm, n, k, X32, k);
+    int64_t launches = 1;
+    int e;
+    for (int64_t r0 = 0; r0 < n; r0 += LU_NB) {
+        const int nb = (int)lmin(LU_NB, n - r0);
+        lu_block_trsm_kernel<<<(unsigned)ceil_div(k, 128), 128, 0, st>>>(LU, lda, X32, k, k, r0, nb, 1);
+        launches++;
+        const int64_t below = n - r0 - nb;
+        if (below > 0) {
+            lu_split_rows_kernel<<<(unsigned)ceil_div(below * LU_NB, 256), 256, 0, st>>>(LU, lda, r0 + nb, r0, nb,
+                                                                                        below, Lp);
+            lu_split_cols_kernel<<<(unsigned)ceil_div(k, 32), 256, 0, st>>>(X32, k, r0, 0, nb, k, Xp);
+            launches += 2;
+            if ((e = gemm_bf16_sub(Lp, LU_K6, Xp, LU_K6, below, k, LU_K6, X32 + (r0 + nb) * k, k, st))) return e;
+        }
+    }
+    for (int64_t r0 = ((n - 1) / LU_NB) * LU_NB; r0 >= 0; r0 -= LU_NB) {
+        const int nb = (int)lmin(LU_NB, n - r0);
+        lu_block_trsm_kernel<<<(unsigned)ceil_div(k, 128), 128, 0, st>>>(LU, lda, X32, k, k, r0, nb, 0);
+        launches++;
+        if (r0 > 0) {
+            lu_split_rows_kernel<<<(unsigned)ceil_div(r0 * LU_NB, 256), 256, 0, st>>>(LU, lda, 0, r0, nb, r0, Lp);
+            lu_split_cols_kernel<<<(unsigned)ceil_div(k, 32), 256, 0, st>>>(X32, k, r0, 0, nb, k, Xp);
+            launches += 2;
+            if ((e = gemm_bf16_sub(Lp, LU_K6, Xp, LU_K6, r0, k, LU_K6, X32, k, st))) return e;
+        }
+    }
+    lu_widen_rows_kernel<<<g_nk, 256, 0, st>>>(X32, k, n, k, X, ldx);
+    if ((e = launch_status("lu_solve_many", (int)launches + 1))) return e;
+    return tc_gemm_check(st);
 }
 
 }  // extern "C"

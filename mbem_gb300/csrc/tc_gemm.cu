@@ -453,3 +453,8 @@ extern "C" int mbem_gemm_bf16_t_split(const void* A, int64_t lda, const void* Xt
 }
 
 extern "C" int mbem_gemm_bf16_check(void* stream) { return tc_gemm_check((cudaStream_t)stream); }
+
+extern "C" int mbem_gemm_bf16_sub(const void* A, int64_t lda, const void* Bt, int64_t ldb, int64_t M, int64_t N,
+                                  int64_t K, float* C, int64_t ldc, void* stream) {
+    return gemm_bf16_sub(A, lda, Bt, ldb, M, N, K, C, ldc, (cudaStream_t)stream);
+}

@@ -13,6 +13,8 @@ readout   the mixed P2 stress readout: fault 32 x 32, 100,000 observers
 asm64     the FP64 P0 assembly of cube 12 (p0_matrix_kernel) and the FP64 P1
           assembly of cube 8 (nodal_matrix_kernel)
 asm32     the mixed P0 assembly of cube 24 (far_assemble_kernel)
+lu        the FP32 GPU LU of an 8,192 x 8,192 matrix (lu_panel_kernel, the
+          tensor-core trailing update) and one refined solve
 """
 
 from __future__ import annotations
@@ -98,6 +100,13 @@ def run(which: str) -> None:
     elif which == "asm32":
         model, eps = cube_fault_model(24, 16)
         DenseBackend(jump="calibrated", deflate=True, precision="mixed").assemble(generate_system(model), eps)
+    elif which == "lu":
+        from .la.lu import Factor
+        n = 8192
+        g = torch.Generator(device="cpu").manual_seed(0)
+        A = (torch.randn(n, n, generator=g, dtype=torch.float64)
+             + n ** 0.5 * torch.eye(n, dtype=torch.float64)).cuda()
+        Factor(A).solve(torch.ones(n, dtype=torch.float64, device="cuda"))
     else:
         raise SystemExit(f"unknown case {which!r}")
     torch.cuda.synchronize()

@@ -220,7 +220,9 @@ def smooth_fields(pos: np.ndarray, n_samples: int, rng, n_modes: int = 24) -> np
 
 def training_errors(asm, n_samples: int, seed: int = 0, chunk: int = 512) -> torch.Tensor:
     """(S, N) FP32 block-Jacobi errors eps = A^-1 r - BJ r on the device for
-    one assembled FP64 system (A^-1: the deflated solution, bordered LU)."""
+    one assembled FP64 system (A^-1: the deflated solution, the bordered
+    system factored by the project's GPU LU and solved with FP64
+    refinement)."""
     from ..backends.dense import translation_basis
     A = asm.A
     N = A.shape[0]
@@ -234,8 +236,8 @@ def training_errors(asm, n_samples: int, seed: int = 0, chunk: int = 512) -> tor
     if nz:
         B[:N, N:] = Z
         B[N:, :N] = Z.T
-    LU, piv = torch.linalg.lu_factor(B)
-    del B
+    from .lu import Factor, solve_many
+    fac = Factor(B)                          # the project's GPU LU (FP32 factors, FP64 refinement)
     bj = asm.block_jacobi()
     eps = torch.empty((n_samples, N), dtype=torch.float32, device=dev)
     for s0 in range(0, n_samples, chunk):
@@ -249,7 +251,7 @@ def training_errors(asm, n_samples: int, seed: int = 0, chunk: int = 512) -> tor
             R = R - (R @ Z) @ Z.T                # the residuals of the deflated system
         rhs = torch.zeros((N + nz, S), dtype=torch.float64, device=dev)
         rhs[:N] = R.T
-        E = torch.linalg.lu_solve(LU, piv, rhs)[:N].T
+        E = solve_many(fac, rhs)[:N].T.contiguous()
         for q in range(S):
             E[q] -= bj.apply(R[q])
         eps[s0:s0 + S] = E.float()

@@ -130,6 +130,60 @@ class Factor:
         return out.reshape(B.shape)
 
 
+def _many(f: "Factor", B: torch.Tensor) -> torch.Tensor:
+    """A^-1 B (n, k) from the single factors, as double."""
+    n, k = B.shape
+    X = torch.empty_like(B)
+    size = int(nat.lib().mbem_lu_solve_many_workspace_size(n, k))
+    work = torch.empty(size, dtype=torch.uint8, device=B.device)
+    nat.call("mbem_lu_solve_many_f32", ptr(f.LU), f.LU.stride(0), n, ptr(f.perm), ptr(B), B.stride(0), k, ptr(X),
+             X.stride(0), ptr(work), size, stream_handle())
+    return X
+
+
+def solve_many(f: "Factor", B: torch.Tensor, matmat=None) -> torch.Tensor:
+    """A^-1 B for B (n, k) float64 CUDA: the blocked multi-column solve from
+    the single factors, refined in double by the reference's rule on the
+    worst column (``matmat(X) -> A X`` in FP64; default: the kept matrix)."""
+    B = B.to(torch.float64).contiguous()
+    if matmat is None:
+        if f._A is None:
+            raise ValueError("solve_many needs the FP64 matrix or a matmat")
+
+        def matmat(X):
+            Y = torch.empty_like(X)
+            nat.call("mbem_dgemm_multi", ptr(f._A), f._A.stride(0), f.n, f.n, ptr(X), X.shape[1], ptr(Y),
+                     stream_handle())
+            return Y
+    X = _many(f, B)
+    live = X.norm(dim=0) > 0.0
+    if not bool(live.any()):
+        return X
+    tol, before = defaults.LU_REFINE_TOL, None
+    done, rate, size, left, k = False, 0.0, 0.0, 0.0, 0
+    while not done and k < defaults.LU_REFINE_PASSES:
+        D = _many(f, (B - matmat(X)).contiguous())
+        X += D
+        k += 1
+        now = D[:, live].norm(dim=0) / X[:, live].norm(dim=0)
+        if before is None:
+            rate = float(now.max())
+        else:
+            rate = float(torch.where(before > 0, now / before, torch.zeros_like(now)).max())
+        size, before = float(now.max()), now
+        left = rate / (1.0 - rate) * size if rate < 1.0 else float("inf")
+        done = left <= tol or size <= tol
+        if rate > defaults.LU_REFINE_RATE:
+            break
+    if not done:
+        raise SingleFactorError(
+            f"dense LU in single precision: the refinement did not contract (rate {rate:.1e}, {left:.1e} left "
+            f"after {k} corrections)")
+    f.report["passes"] = max(k, f.report.get("passes", 0))
+    f.report["correction"], f.report["left"] = size, left
+    return X
+
+
 def factor(A: torch.Tensor, matvec=None) -> Factor:
     return Factor(A, matvec)
 

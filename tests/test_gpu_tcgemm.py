@@ -51,3 +51,27 @@ def test_gemm_split_k(gpu, M, K, n):
     gemm_check()
     ref = (A.float() @ Xt.float().T).T
     assert float((out - ref).abs().max() / ref.abs().max()) < 3e-5
+
+
+@pytest.mark.parametrize("M,N,K", [(300, 7, 384), (1000, 64, 384), (936, 64, 384), (520, 130, 384), (200, 256, 192),
+                                   (777, 33, 64), (128, 16, 384), (1500, 300, 384)])
+def test_gemm_sub_update(gpu, M, N, K):
+    """C -= A Bt^T (the LU update) against FP64 products of the same BF16
+    operands: FP32 accumulation, tolerance 1e-5 of max|A Bt^T|; rows and
+    columns outside C untouched."""
+    from mbem_gb300 import _native as nat
+    from mbem_gb300._device import ptr, stream_handle
+    g = torch.Generator(device="cpu").manual_seed(M + N)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+    Bt = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+    ldc = N + 5
+    C0 = torch.randn(M + 3, ldc, generator=g).cuda()
+    C = C0.clone()
+    nat.call("mbem_gemm_bf16_sub", ptr(A), A.stride(0), ptr(Bt), Bt.stride(0), M, N, K, ptr(C), ldc, stream_handle())
+    torch.cuda.synchronize()
+    P = A.double() @ Bt.double().T
+    ref = C0.double().clone()
+    ref[:M, :N] -= P
+    err = float((C.double() - ref).abs().max() / P.abs().max())
+    assert err < 1e-5, err
+    assert torch.equal(C[M:], C0[M:]) and torch.equal(C[:, N:], C0[:, N:])
