@@ -446,6 +446,12 @@ class AssembledDense:
         self._inner.rtol = float(tol)
         return self._inner
 
+    def condense(self, refine: bool = True):
+        """Every unknown but the FAULT_TRACTION faults' slip eliminated
+        (dense.py:580-646): a ``backends.condense.Condensed``."""
+        from .condense import condense
+        return condense(self, refine)
+
     def factor(self):
         """The FP32 GPU LU of this operator (the bordered one [[A, Z], [Z^T, 0]]
         with deflation, backends/dense.py:538-566), refined against the FP64

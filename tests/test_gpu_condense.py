@@ -1,0 +1,70 @@
+"""AssembledDense.condense (dense.py:580-646) on the GPU: the Schur
+complement onto the FAULT_TRACTION slip coordinates against the same
+algebra in FP64 torch (1e-10 of max|S|), and the condensed solution
+x = x0 + X beta, beta = S^-1 (-L), equal to the direct solve of the whole
+system (1e-8)."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _anchored_model(n_face=4, n_fault=3):
+    from mbem_gb300 import mesh as M
+    from mbem_gb300.model import BCType, Patch, Region, RegionModel
+    cube_p = Patch("cube", M.cube(n_face), BCType.PRESCRIBED_DISPLACEMENT, value=np.zeros(3))
+    fault_p = Patch("fault", M.centre_fault(n_fault), BCType.FAULT_TRACTION, value=np.array([-1e-3, 0.0, 0.0]))
+    region = Region("body", M.ElasticMaterial(mu=1.0, lam=1.0), [cube_p], np.zeros(3), faults=[fault_p])
+    return RegionModel([region]), (4.0 / n_face) / 2.0
+
+
+def test_condense_against_fp64_and_direct_solve(gpu):
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.model import generate_system
+    model, eps = _anchored_model()
+    asm = DenseBackend(jump="calibrated", deflate=False, lu="gpu").assemble(generate_system(model), eps)
+    c = asm.condense()
+    f = model.regions[0].faults[0]
+    assert c.n == 2 * f.n_dofs and len(c.faults) == 1 and c.faults[0].name == "fault"
+    # the same algebra in FP64
+    A, b = asm.A, asm.b
+    N = A.shape[0]
+    slot = asm.layout.slot(f, "b")
+    on = np.zeros(N, bool)
+    on[slot.offset:slot.stop] = True
+    rest = torch.from_numpy(np.flatnonzero(~on)).cuda()
+    fc = c.faults[0]
+    rows = torch.from_numpy((slot.offset + 3 * fc.free[:, None] + np.arange(2)[None, :]).ravel()).cuda()
+    E = torch.from_numpy(c.X[slot.offset:slot.stop]).cuda()
+    AE = A[:, slot.offset:slot.stop] @ E
+    Xr = -torch.linalg.solve(A[rest][:, rest], AE[rest])
+    S_ref = AE[rows] + A[rows][:, rest] @ Xr
+    x0r = torch.linalg.solve(A[rest][:, rest], b[rest])
+    L_ref = -b[rows] + A[rows][:, rest] @ x0r
+    assert np.abs(c.S - S_ref.cpu().numpy()).max() < 1e-10 * np.abs(c.S).max()
+    assert np.abs(c.L - L_ref.cpu().numpy()).max() < 1e-10 * np.abs(c.L).max()
+    # the condensed solution is the whole system's solution
+    beta = np.linalg.solve(c.S, -c.L)
+    x = c.x0 + c.X @ beta
+    x_ref = asm.solve_device().cpu().numpy()
+    assert np.abs(x - x_ref).max() < 1e-8 * np.abs(x_ref).max()
+    # coordinates <-> Cartesian round trip on the free nodes
+    v = np.random.default_rng(0).normal(size=fc.stop - fc.start)
+    assert np.allclose(fc.coordinates(fc.cartesian(v)), v)
+    assert c.dragged(1e3).shape == (c.n,)
+
+
+def test_condense_refusals(gpu):
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model, fault_traction_model
+    from mbem_gb300.model import generate_system
+    model, eps = cube_fault_model(3, 2)
+    asm = DenseBackend(jump="calibrated", deflate=True).assemble(generate_system(model), eps)
+    with pytest.raises(ValueError, match="no FAULT_TRACTION"):
+        asm.condense()
+    model, eps = fault_traction_model(3, 2)
+    asm = DenseBackend(jump="calibrated", deflate=True).assemble(generate_system(model), eps)
+    with pytest.raises(ValueError, match="deflate"):
+        asm.condense()
