@@ -104,7 +104,7 @@ class BlockSolver:
     every step is one tensor-core GEMM over the whole block. P removes the
     rigid translations of the u-slots of a deflated system."""
 
-    def __init__(self, asm, inner_restart: int = 30, inner_rtol: float = 1e-3, terms: int = 3):
+    def __init__(self, asm, inner_restart: int = 30, inner_rtol: float = 3e-5, terms: int = 3):
         """``terms``: 1 = the operator in BF16 (relative error ~2^-9 per
         product: about five refinement steps to 1e-8); 3 = A and the Krylov
         vectors each split into BF16 high and low parts, A_hi V_hi + A_hi
