@@ -80,7 +80,7 @@ class DenseBackend:
         self.precond = precond
 
     def assemble(self, system: BlockSystem, eps, arrays: dict | None = None,
-                 timer: list | None = None) -> "AssembledDense":
+                 timer: list | None = None, fault_drag: dict | None = None) -> "AssembledDense":
         """``arrays``: an optional caller-held dict of per-patch device arrays,
         reused across assemblies of the same model (no host-to-device copy
         when it is already filled). ``timer``: an optional list that receives
@@ -88,7 +88,19 @@ class DenseBackend:
         return AssembledDense(system, eps, jump=self.jump, deflate=self.deflate, rtol=self.rtol,
                               restart=self.restart, maxiter=self.maxiter, arrays=arrays, timer=timer,
                               precision=self.precision, near_factor=self.near_factor, precond=self.precond,
-                              lu=self.lu)
+                              lu=self.lu, fault_drag=fault_drag)
+
+
+def _checked_drag(system: BlockSystem, drag) -> dict:
+    """``{fault name: kappa}`` naming only FAULT_TRACTION faults of the model
+    (dense.py:247-257: a drag on a prescribed slip would be silently nothing)."""
+    drag = dict(drag or {})
+    known = {f.name for _r, f in system.traction_faults()}
+    unknown = set(drag) - known
+    if unknown:
+        raise KeyError(f"fault_drag names {sorted(unknown)}, which are not FAULT_TRACTION faults of the model "
+                       f"(those are {sorted(known)})")
+    return drag
 
 
 def _f32_matrix(rows: int, cols: int, dev, zero: bool = False) -> torch.Tensor:
@@ -134,11 +146,12 @@ class AssembledDense:
                  maxiter: int = defaults.GMRES_MAXITER, arrays: dict | None = None,
                  timer: list | None = None, precision: str = "fp64",
                  near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, precond: str | None = None,
-                 lu: str | None = None):
+                 lu: str | None = None, fault_drag: dict | None = None):
         if jump not in ("half", "calibrated"):
             raise ValueError(jump)
         require_anchor_or_deflate(system, jump, deflate)
         require_cuda()
+        self.fault_drag = _checked_drag(system, fault_drag)
         self.lu = lu
         self._factor = None
         self._arrays_in = arrays
@@ -410,7 +423,7 @@ class AssembledDense:
                 bview -= torch.einsum("nij,nj->ni", C, u_c)
         if self.system.traction_faults():
             from .fault_rows import apply_fault_rows
-            apply_fault_rows(A, b, self.system)
+            apply_fault_rows(A, b, self.system, self.fault_drag)
         self._arrays = None
         self.A = A
         self.b = b

@@ -68,3 +68,25 @@ def test_condense_refusals(gpu):
     asm = DenseBackend(jump="calibrated", deflate=True).assemble(generate_system(model), eps)
     with pytest.raises(ValueError, match="deflate"):
         asm.condense()
+
+
+def test_drag_solve_equals_condensed_drag(gpu):
+    """An operator built with a fault drag kappa solves for the slip that the
+    drag-free condensed body gives by (kappa - S) beta = L (dense.py:333-340)."""
+    from mbem_gb300.backends.dense import AssembledDense
+    from mbem_gb300.model import generate_system
+    model, eps = _anchored_model()
+    system = generate_system(model)
+    c = AssembledDense(system, eps, jump="calibrated", deflate=False, lu="gpu").condense()
+    kappa = 0.7
+    dr = AssembledDense(system, eps, jump="calibrated", deflate=False, lu="gpu", fault_drag={"fault": kappa})
+    x = dr.solve_device().cpu().numpy()
+    fc = c.faults[0]
+    slot = system.layout.slot(model.regions[0].faults[0], "b")
+    beta_solve = fc.coordinates(x[slot.offset:slot.stop].reshape(-1, 3))
+    beta = c.dragged(kappa)
+    assert np.abs(beta_solve - beta).max() < 1e-8 * np.abs(beta).max()
+    with pytest.raises(ValueError, match="drag"):
+        dr.condense()
+    with pytest.raises(KeyError):
+        AssembledDense(system, eps, jump="calibrated", deflate=False, fault_drag={"cube": 1.0})
