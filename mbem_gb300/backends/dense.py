@@ -459,6 +459,27 @@ class AssembledDense:
         self._inner.rtol = float(tol)
         return self._inner
 
+    def rebuild_for_materials(self, material_map: dict, fault_drag: dict | None = None) -> "AssembledDense":
+        """A new AssembledDense of the same model with updated region
+        materials (dense.py:650-688): ``material_map`` maps region name ->
+        material; ``fault_drag`` replaces the faults' drag (``{}`` removes
+        it), ``None`` keeps this one's. The geometry arrays of this assembly
+        are reused; the blocks are re-assembled (direct mode)."""
+        new = AssembledDense.__new__(AssembledDense)
+        new.__dict__.update(self.__dict__)
+        new.materials = dict(self.materials)
+        for name, mat in material_map.items():
+            if name not in new.materials:
+                raise KeyError(f"unknown region '{name}'")
+            new.materials[name] = mat
+        new.fault_drag = self.fault_drag if fault_drag is None else _checked_drag(self.system, fault_drag)
+        new.report = None
+        new.A = new.b = new.op = new._x = None
+        new._bj = new._inner = new._factor = None
+        new.calib = None
+        new._build()
+        return new
+
     def condense(self, refine: bool = True):
         """Every unknown but the FAULT_TRACTION faults' slip eliminated
         (dense.py:580-646): a ``backends.condense.Condensed``."""

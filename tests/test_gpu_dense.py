@@ -123,3 +123,23 @@ def test_fault_traction_system_and_solution(gpu, traction_small):
     # the constraint rows hold: no opening
     nrm = model.regions[0].faults[0].collocation_normals()
     assert np.abs(np.einsum("ij,ij->i", sol["b:fault"], nrm)).max() < 1e-12 * np.abs(sol["b:fault"]).max()
+
+
+def test_rebuild_for_materials_equals_fresh_assembly(gpu):
+    """rebuild_for_materials (dense.py:650-688): the same operator as a fresh
+    assembly of the model with the new material (1e-14); unknown regions refused."""
+    from mbem_gb300 import mesh as M
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.model import generate_system
+    model, eps = cube_fault_model(4, 2, 1.0, 1.0)
+    asm = DenseBackend(jump="calibrated", deflate=True).assemble(generate_system(model), eps)
+    new_mat = M.ElasticMaterial(mu=2.5, lam=1.7)
+    re = asm.rebuild_for_materials({"body": new_mat})
+    model2, _ = cube_fault_model(4, 2, 2.5, 1.7)
+    fresh = DenseBackend(jump="calibrated", deflate=True).assemble(generate_system(model2), eps)
+    assert float((re.A - fresh.A).abs().max() / fresh.A.abs().max()) < 1e-14
+    assert float((re.b - fresh.b).abs().max() / fresh.b.abs().max()) < 1e-14
+    assert float((asm.A - fresh.A).abs().max()) > 0.0          # the original is untouched
+    with pytest.raises(KeyError):
+        asm.rebuild_for_materials({"nowhere": new_mat})
