@@ -32,6 +32,12 @@
 
 namespace mbem {
 
+constexpr uint32_t TP_WAIT_LIMIT = 1u << 26;
+
+// set by a bulk-copy wait that gave up (matvec ring or assembly tile); read
+// (and cleared) by the host
+__device__ int g_mixed_wait_error = 0;
+
 // ---------------------------------------------------------------------------
 // quadrature rules: collapsed Gauss-Legendre n x n on (0,0),(1,0),(0,1)
 // ---------------------------------------------------------------------------
@@ -372,10 +378,35 @@ template <bool TKERNEL, int ORDER>
 __global__ void __launch_bounds__(FAR_THREADS)
 far_assemble_kernel(FarArgs a, QuadRules Q) {
     constexpr int K = ORDER == 0 ? 1 : (ORDER == 1 ? 3 : 6);
+    constexpr uint32_t TILE_BYTES = FAR_FIELD_TILE * 3 * sizeof(double);
     __shared__ F2 xs[FAR_FIELD_TILE][3];
+    // the field tile arrives by one bulk copy (cp.async.bulk) while the
+    // threads set up their sources; a ragged last tile or an unaligned base
+    // falls back to plain loads
+    __shared__ __align__(16) double xraw[FAR_FIELD_TILE * 3];
+    __shared__ __align__(8) uint64_t tbar;
     const int64_t s = (int64_t)blockIdx.x * FAR_THREADS + threadIdx.x;
     const bool active = s < a.n_src;
     const int64_t n_words = ceil_div(a.n_src, 32);
+    bool bulk_ok = ((uintptr_t)a.x_field % 16) == 0;
+    if (threadIdx.x == 0) {
+        mbar_init(&tbar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    bool in_flight = false;
+    auto issue = [&](int64_t t0) -> bool {
+        if (!bulk_ok || t0 + FAR_FIELD_TILE > a.n_field) return false;
+        if (threadIdx.x == 0) {
+            mbar_arrive_expect_tx(&tbar, TILE_BYTES);
+            bulk_g2s(xraw, a.x_field + 3 * t0, TILE_BYTES, &tbar);
+        }
+        return true;
+    };
+    const int64_t first = (int64_t)blockIdx.y * FAR_FIELD_TILE;
+    bool pending = first < a.n_field && issue(first);
+    in_flight = pending;
     SrcFar src;
     if (active) {
         far_setup(a.tri_verts + 9 * s, TKERNEL ? a.normals + 3 * s : nullptr, a.eps[s], a.near_factor, src);
@@ -389,12 +420,23 @@ far_assemble_kernel(FarArgs a, QuadRules Q) {
         src.rnear2 = -1.0f;
         src.ok = false;
     }
-    for (int64_t f0 = (int64_t)blockIdx.y * FAR_FIELD_TILE; f0 < a.n_field;
-         f0 += (int64_t)gridDim.y * FAR_FIELD_TILE) {
+    for (int64_t f0 = first; f0 < a.n_field; f0 += (int64_t)gridDim.y * FAR_FIELD_TILE) {
         __syncthreads();
+        const bool bulk = (f0 == first) ? pending : issue(f0);
+        bool got = false;
+        if (bulk) {
+            if (mbar_wait(&tbar, phase, TP_WAIT_LIMIT)) {
+                got = true;
+                in_flight = false;
+            } else {
+                atomicExch(&g_mixed_wait_error, 1);
+                bulk_ok = false;                  // plain loads from here on
+            }
+            phase ^= 1u;
+        }
         for (int t = threadIdx.x; t < FAR_FIELD_TILE * 3; t += FAR_THREADS) {
             const int64_t f = f0 + t / 3;
-            xs[t / 3][t % 3] = split_d(f < a.n_field ? a.x_field[3 * f0 + t] : 0.0);
+            xs[t / 3][t % 3] = split_d(got ? xraw[t] : (f < a.n_field ? a.x_field[3 * f0 + t] : 0.0));
         }
         __syncthreads();
         const int nf = (int)lmin(FAR_FIELD_TILE, a.n_field - f0);
@@ -443,6 +485,8 @@ far_assemble_kernel(FarArgs a, QuadRules Q) {
             }
         }
     }
+    // a copy whose wait ran out must land before the block's shared memory goes
+    if (in_flight && threadIdx.x == 0) mbar_wait(&tbar, phase ^ 1u, TP_WAIT_LIMIT);
 }
 
 // ---------------------------------------------------------------------------
@@ -866,12 +910,9 @@ __global__ void near_matvec_kernel(const int64_t* __restrict__ rowptr, const int
 // ---------------------------------------------------------------------------
 // Tile shape (template): TP_ROWS rows per CTA, TP_CH columns per chunk,
 // TP_STAGES ring stages; the tuned choice is in tune.cuh.
-constexpr uint32_t TP_WAIT_LIMIT = 1u << 26;
 template <int R, int CH, int S>
 constexpr size_t tp_smem() { return (size_t)S * (R + 2) * CH * sizeof(float) + 2 * S * 8; }
 
-// set by a pipeline wait that gave up; read (and cleared) by the host
-__device__ int g_mixed_wait_error = 0;
 
 template <int TP_ROWS, int TP_CH, int TP_STAGES>
 __global__ void __launch_bounds__(32 * (TP_ROWS / 2 + 1))
@@ -1036,7 +1077,7 @@ int mixed_wait_check(cudaStream_t st) {
     if (flag) {
         const int zero = 0;
         cudaMemcpyToSymbol(g_mixed_wait_error, &zero, sizeof(int));
-        return set_error(MBEM_ERR_WAIT, "a bulk-copy pipeline wait expired in the mixed matvec");
+        return set_error(MBEM_ERR_WAIT, "a bulk-copy wait expired in a mixed-operator kernel");
     }
     return MBEM_OK;
 }
