@@ -15,6 +15,8 @@ asm64     the FP64 P0 assembly of cube 12 (p0_matrix_kernel) and the FP64 P1
 asm32     the mixed P0 assembly of cube 24 (far_assemble_kernel)
 lu        the FP32 GPU LU of an 8,192 x 8,192 matrix (lu_panel_kernel, the
           tensor-core trailing update) and one refined solve
+learned   FAULT_TRACTION cube 16 x 16, fault 12 x 12: the learned two-level
+          preconditioner's setup and its FGMRES solve
 """
 
 from __future__ import annotations
@@ -100,6 +102,13 @@ def run(which: str) -> None:
     elif which == "asm32":
         model, eps = cube_fault_model(24, 16)
         DenseBackend(jump="calibrated", deflate=True, precision="mixed").assemble(generate_system(model), eps)
+    elif which == "learned":
+        from .la.learned import LearnedPreconditioner
+        from .la.train_learned import load_default
+        model, eps = fault_traction_model(16, 12, 90.0)
+        asm = DenseBackend(jump="calibrated", deflate=True, rtol=1e-8).assemble(generate_system(model), eps)
+        pc = LearnedPreconditioner(asm, load_default())
+        asm.solve_device(precond=pc)
     elif which == "lu":
         from .la.lu import Factor
         n = 8192
