@@ -578,7 +578,9 @@ def multi_mesh_workload(peaks, n_mesh=64, lo=8, hi=32, seed=7):
     from mbem_gb300.model import generate_system
 
     shapes = random_cube_batch(n_mesh, lo, hi, seed)
-    be = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART, precision="mixed")
+    # every operator with its BF16 copy (the mixed batch solve's inner operator)
+    be = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART, precision="mixed",
+                      precond="bf16_inner")
     systems = []
 
     def assemble_all():
@@ -599,6 +601,9 @@ def multi_mesh_workload(peaks, n_mesh=64, lo=8, hi=32, seed=7):
     (X, rep), t_batch = _sync_time(lambda: mb.solve(B, rtol=RTOL))
     launches = nat.lib().mbem_launch_count() - launches0
     (Xn, repn), t_nograph = _sync_time(lambda: mb.solve(B, rtol=RTOL, graph=False))
+    # the mixed batch solve: lockstep BF16 inner solves inside refinement
+    mb.solve_mixed(B, rtol=RTOL)
+    (Xm, repm), t_mixed = _sync_time(lambda: mb.solve_mixed(B, rtol=RTOL))
     # the batched operator alone: one persistent launch over every mesh
     Xr = torch.randn(mb.n_total, dtype=torch.float64, device="cuda")
     mb.matvec(Xr)
@@ -606,19 +611,25 @@ def multi_mesh_workload(peaks, n_mesh=64, lo=8, hi=32, seed=7):
     _, t_mv = _sync_time(lambda: [mb.matvec(Xr) for _ in range(reps)])
     mv_s = t_mv / reps
     mv_bytes = sum(4.0 * a.op.n * a.op.n for a in systems)
-    # one system after another, same operators, the single-system FGMRES
+    # one system after another, same operators: the single-system FGMRES
+    # (plain, the batched GMRES's algorithm) and the single-system mixed
+    # solve (BF16 inner, the mixed batch solve's algorithm)
     single_its = []
 
-    def one_by_one():
+    def one_by_one(precond):
         single_its.clear()
         out = []
         for a in systems:
-            out.append(a.solve_device(rtol=RTOL))
+            out.append(a.solve_device(rtol=RTOL, precond=precond))
             single_its.append(a.report.iterations)
         return out
-    one_by_one()
-    xs, t_single = _sync_time(one_by_one)
+    one_by_one("none")
+    xs, t_single = _sync_time(lambda: one_by_one("none"))
+    plain_its = list(single_its)
     diff = max(float((x - y).norm() / y.norm()) for x, y in zip(mb.scatter(X), xs))
+    one_by_one("bf16_inner")
+    xsm, t_single_mixed = _sync_time(lambda: one_by_one("bf16_inner"))
+    diff_mixed = max(float((x - y).norm() / y.norm()) for x, y in zip(mb.scatter(Xm), xs))
     hbm = peaks.get("hbm_gbs") or 6800.0
     out = {"config": {"meshes": n_mesh, "per_face_grids": [s[0] for s in shapes], "unknowns_total": n_total,
                       "largest": max(a.op.n for a in systems), "smallest": min(a.op.n for a in systems),
@@ -629,15 +640,23 @@ def multi_mesh_workload(peaks, n_mesh=64, lo=8, hi=32, seed=7):
                        "iterations_max": max(rep.iterations), "iterations_mean": float(np.mean(rep.iterations)),
                        "worst_relres": max(rep.relres), "gpu_launches": int(launches)},
            "batched_without_graph_s": t_nograph,
-           "one_by_one_fgmres": {"s": t_single, "iterations_max": max(single_its),
-                                 "iterations_mean": float(np.mean(single_its))},
+           "batched_mixed": {"s": t_mixed, "refinement_steps": repm.cycles, "converged": repm.all_converged,
+                             "inner_steps_max": max(repm.iterations),
+                             "inner_steps_mean": float(np.mean(repm.iterations)),
+                             "worst_relres": max(repm.relres),
+                             "max_rel_diff_vs_plain_single_solves": diff_mixed},
+           "one_by_one_mixed": {"s": t_single_mixed},
+           "speedup_batched_mixed_vs_one_by_one_mixed": t_single_mixed / t_mixed,
+           "speedup_batched_mixed_vs_one_by_one_plain": t_single / t_mixed,
+           "one_by_one_fgmres": {"s": t_single, "iterations_max": max(plain_its),
+                                 "iterations_mean": float(np.mean(plain_its))},
            "speedup_batched_vs_one_by_one": t_single / t_batch,
            "max_rel_diff_batched_vs_single": diff,
            "roofline_batched_matvec": {"kernel": "mm_matvec_kernel (persistent, all meshes)", "bound": "hbm",
                                        "achieved": mv_bytes / mv_s / 1e9, "peak": hbm, "unit": "GB/s",
                                        "frac": mv_bytes / mv_s / 1e9 / hbm, "launch_ms": mv_s * 1e3,
                                        "bytes_per_launch": mv_bytes}}
-    del mb, systems[:], X, Xn, xs
+    del mb, systems[:], X, Xn, Xm, xs, xsm
     torch.cuda.empty_cache()
     return out
 

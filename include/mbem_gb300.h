@@ -334,6 +334,9 @@ typedef struct {
     const int64_t* cols;     /* source node per block (columns 3c..3c+2), */
     const double* vals;      /* 3x3 FP64 values per block, row-major */
     int64_t u_off, u_len;    /* deflated u-slot range within the segment (u_len = 0: none) */
+    const uint16_t* A16;     /* optional BF16 copy of the far field (n, ld16), 16-byte aligned,
+                                ld16 % 8 == 0: the inner operator of mbem_mm_solve_mixed */
+    int64_t ld16;
 } mbem_mm_mesh;
 
 typedef struct {
@@ -359,6 +362,13 @@ int mbem_mm_matvec(mbem_mm_solver* solver, const double* x, double* y, void* str
  * legacy default stream. */
 int mbem_mm_solve(mbem_mm_solver* solver, const double* b, double* x, double rtol, int max_cycles, int use_graph,
                   mbem_mm_report* report, void* stream);
+/* The mixed-precision batch solve: refinement on the accurate operator whose
+ * corrections are lockstep GMRES solves on the BF16 far fields (every mesh's
+ * A16) to inner_rtol of each residual; at most max_outer refinement steps and
+ * max_cycles restart cycles an inner solve. report->iterations: inner steps;
+ * report->cycles: refinement steps. */
+int mbem_mm_solve_mixed(mbem_mm_solver* solver, const double* b, double* x, double rtol, double inner_rtol,
+                        int max_outer, int max_cycles, int use_graph, mbem_mm_report* report, void* stream);
 /* MBEM_ERR_WAIT if a bounded wait of the batched matvec gave up since the last check */
 int mbem_mm_check(void* stream);
 

@@ -83,7 +83,8 @@ INNER_MAX_ITERS = 64
 
 class MmMesh(Structure):
     _fields_ = [("A32", c_void_p), ("ld32", c_int64), ("n", c_int64), ("offset", c_int64), ("rowptr", c_void_p),
-                ("cols", c_void_p), ("vals", c_void_p), ("u_off", c_int64), ("u_len", c_int64)]
+                ("cols", c_void_p), ("vals", c_void_p), ("u_off", c_int64), ("u_len", c_int64), ("A16", c_void_p),
+                ("ld16", c_int64)]
 
 
 class MmReport(Structure):
@@ -205,6 +206,7 @@ _SIGNATURES = {
     "mbem_mm_matvec": (c_int, [_P, _P, _P, _P]),
     "mbem_mm_solve": (c_int, [_P, _P, _P, c_double, c_int, c_int, POINTER(MmReport), _P]),
     "mbem_mm_check": (c_int, [_P]),
+    "mbem_mm_solve_mixed": (c_int, [_P, _P, _P, c_double, c_double, c_int, c_int, c_int, POINTER(MmReport), _P]),
 }
 
 _lib = None

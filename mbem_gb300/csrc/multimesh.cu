@@ -193,6 +193,131 @@ mm_matvec_kernel(const mbem_mm_mesh* __restrict__ meshes, const MMItem* __restri
     }
 }
 
+// The same walk over the BF16 copies of the far fields (the inner operator
+// of the mixed batch solve): 2-byte rows and FP32 x through the ring, FP32
+// sums (four chains a row, two rows a warp), the FP64 near part added.
+constexpr int M16_CH = 2048, M16_STAGES = 3;
+constexpr size_t M16_SMEM = (size_t)M16_STAGES * (MM_ROWS * M16_CH * 2 + M16_CH * 4) + 2 * M16_STAGES * 8;
+
+__global__ void __launch_bounds__(MM_THREADS)
+mm_matvec16_kernel(const mbem_mm_mesh* __restrict__ meshes, const MMItem* __restrict__ items, int64_t n_items,
+                   const int* __restrict__ active, const float* __restrict__ xf, double* __restrict__ y) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint16_t* sA = reinterpret_cast<uint16_t*>(smem);                                 // [S][ROWS][CH]
+    float* sX = reinterpret_cast<float*>(sA + (size_t)M16_STAGES * MM_ROWS * M16_CH);  // [S][CH]
+    uint64_t* full = reinterpret_cast<uint64_t*>(sX + M16_STAGES * M16_CH);
+    uint64_t* empty = full + M16_STAGES;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < M16_STAGES; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], MM_WARPS);
+        }
+        mbar_init_fence();
+    }
+    __syncthreads();
+    int64_t g = 0;
+    if (warp == MM_WARPS) {
+        bool ok = true;
+        for (int64_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
+            const MMItem item = items[it];
+            if (!active[item.mesh]) continue;
+            const mbem_mm_mesh M = meshes[item.mesh];
+            const int nrow = (int)lmin(MM_ROWS, M.n - item.row0);
+            const int64_t n_main = M.n & ~(int64_t)7;
+            const int64_t nch = ceil_div(n_main, M16_CH);
+            for (int64_t k = 0; k < nch; k++, g++) {
+                const int s = (int)(g % M16_STAGES);
+                int okl = 1;
+                if (lane == 0 && g >= M16_STAGES &&
+                    !mbar_wait(&empty[s], (uint32_t)(((g / M16_STAGES) - 1) & 1), MM_WAIT_LIMIT)) {
+                    atomicExch(&g_mm_wait_error, 1);
+                    okl = 0;
+                }
+                okl = __shfl_sync(0xffffffffu, okl, 0);
+                if (!okl) {
+                    ok = false;
+                    break;
+                }
+                const int64_t c0 = k * M16_CH;
+                const uint32_t cols = (uint32_t)lmin(M16_CH, n_main - c0);
+                if (lane == 0) mbar_arrive_expect_tx(&full[s], cols * 2u * (uint32_t)nrow + cols * 4u);
+                __syncwarp();
+                if (lane < nrow)
+                    bulk_g2s(sA + ((int64_t)s * MM_ROWS + lane) * M16_CH, M.A16 + (item.row0 + lane) * M.ld16 + c0,
+                             cols * 2u, &full[s]);
+                else if (lane == MM_ROWS)
+                    bulk_g2s(sX + (int64_t)s * M16_CH, xf + M.offset + c0, cols * 4u, &full[s]);
+            }
+        }
+        if (lane == 0)
+            for (int64_t q = (g > M16_STAGES ? g - M16_STAGES : 0); q < g; q++)
+                if (!mbar_wait(&full[q % M16_STAGES], (uint32_t)((q / M16_STAGES) & 1), MM_WAIT_LIMIT))
+                    atomicExch(&g_mm_wait_error, 1);
+        return;
+    }
+    const int ra = 2 * warp, rb = 2 * warp + 1;
+    for (int64_t it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const MMItem item = items[it];
+        if (!active[item.mesh]) continue;
+        const mbem_mm_mesh M = meshes[item.mesh];
+        const int nrow = (int)lmin(MM_ROWS, M.n - item.row0);
+        const int64_t n_main = M.n & ~(int64_t)7;
+        const int64_t nch = ceil_div(n_main, M16_CH);
+        const bool va = ra < nrow, vb = rb < nrow;
+        const int rb_eff = vb ? rb : ra;
+        const double near_a = (va && lane == 0) ? y[M.offset + item.row0 + ra] : 0.0;
+        const double near_b = (vb && lane == 0) ? y[M.offset + item.row0 + rb] : 0.0;
+        float a4[4] = {0.f, 0.f, 0.f, 0.f}, b4[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int64_t k = 0; k < nch; k++, g++) {
+            const int s = (int)(g % M16_STAGES);
+            if (!mbar_wait(&full[s], (uint32_t)((g / M16_STAGES) & 1), MM_WAIT_LIMIT)) {
+                atomicExch(&g_mm_wait_error, 1);
+                return;
+            }
+            if (va) {
+                const int w4 = (int)(lmin(M16_CH, n_main - k * M16_CH) / 4);
+                const uint2* pa = reinterpret_cast<const uint2*>(sA + ((int64_t)s * MM_ROWS + ra) * M16_CH);
+                const uint2* pb = reinterpret_cast<const uint2*>(sA + ((int64_t)s * MM_ROWS + rb_eff) * M16_CH);
+                const float4* x4 = reinterpret_cast<const float4*>(sX + (int64_t)s * M16_CH);
+#pragma unroll 4
+                for (int q = lane; q < w4; q += 32) {
+                    const float4 u = x4[q];
+                    const uint2 p = pa[q], r = pb[q];
+                    a4[0] = fmaf(__uint_as_float(p.x << 16), u.x, a4[0]);
+                    a4[1] = fmaf(__uint_as_float(p.x & 0xffff0000u), u.y, a4[1]);
+                    a4[2] = fmaf(__uint_as_float(p.y << 16), u.z, a4[2]);
+                    a4[3] = fmaf(__uint_as_float(p.y & 0xffff0000u), u.w, a4[3]);
+                    b4[0] = fmaf(__uint_as_float(r.x << 16), u.x, b4[0]);
+                    b4[1] = fmaf(__uint_as_float(r.x & 0xffff0000u), u.y, b4[1]);
+                    b4[2] = fmaf(__uint_as_float(r.y << 16), u.z, b4[2]);
+                    b4[3] = fmaf(__uint_as_float(r.y & 0xffff0000u), u.w, b4[3]);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[s]);
+        }
+        if (!va) continue;
+        const int64_t rowa = item.row0 + ra, rowb = item.row0 + rb_eff;
+        const float* xs = xf + M.offset;
+        for (int64_t c = n_main + lane; c < M.n; c += 32) {
+            a4[0] = fmaf(__uint_as_float((uint32_t)M.A16[rowa * M.ld16 + c] << 16), xs[c], a4[0]);
+            b4[0] = fmaf(__uint_as_float((uint32_t)M.A16[rowb * M.ld16 + c] << 16), xs[c], b4[0]);
+        }
+        double sa = ((double)a4[0] + (double)a4[1]) + ((double)a4[2] + (double)a4[3]);
+        double sb = ((double)b4[0] + (double)b4[1]) + ((double)b4[2] + (double)b4[3]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sa += __shfl_xor_sync(0xffffffffu, sa, o);
+            sb += __shfl_xor_sync(0xffffffffu, sb, o);
+        }
+        if (lane == 0) {
+            y[M.offset + rowa] = sa + near_a;
+            if (vb) y[M.offset + rowb] = sb + near_b;
+        }
+    }
+}
+
 // y[row] = the row's FP64 near blocks times x (one warp per batch row; the
 // padding and inactive meshes are skipped). mm_matvec_kernel adds the far
 // part to it.
@@ -491,10 +616,15 @@ struct mbem_mm_solver {
     double* rn2 = nullptr;      // n_mesh
     double* bnorm = nullptr;    // n_mesh
     double* mean = nullptr;     // n_mesh x 3
-    cudaGraphExec_t cycle = nullptr;
-    double cycle_rtol = -1.0;
-    int cycle_cfg = -1;            // tile configuration captured in the cycle
-    long long cycle_kernels = 0;   // kernel nodes in the captured cycle
+    double* Bfull = nullptr;    // the outer right-hand side (mixed solve)
+    double* D = nullptr;        // an inner correction (mixed solve)
+    bool has16 = false;         // every mesh has its BF16 far field
+    int op16 = 0;               // the operator of the next products: 1 = BF16 inner
+    // the captured restart cycle of each operator (0 FP32, 1 BF16)
+    cudaGraphExec_t cycle[2] = {nullptr, nullptr};
+    double cycle_rtol[2] = {-1.0, -1.0};
+    int cycle_cfg[2] = {-1, -1};      // tile configuration captured in the cycle
+    long long cycle_kernels[2] = {0, 0};
 };
 
 namespace {
@@ -516,6 +646,9 @@ int mm_check(const mbem_mm_mesh* meshes, int n_mesh, int restart, MMCounts* out)
         MBEM_REQUIRE(M.A32 && (uintptr_t)M.A32 % 16 == 0 && M.ld32 >= M.n && M.ld32 % 4 == 0, MBEM_ERR_ARG,
                      "mesh %d: the FP32 far field must be 16-byte aligned with ld32 >= n, ld32 %% 4 == 0", m);
         MBEM_REQUIRE(M.rowptr && M.cols && M.vals, MBEM_ERR_ARG, "mesh %d: NULL near blocks", m);
+        MBEM_REQUIRE(M.A16 == nullptr || ((uintptr_t)M.A16 % 16 == 0 && M.ld16 >= M.n && M.ld16 % 8 == 0),
+                     MBEM_ERR_ARG, "mesh %d: the BF16 far field must be 16-byte aligned with ld16 >= n, ld16 %% 8 == 0",
+                     m);
         MBEM_REQUIRE(M.offset == end, MBEM_ERR_ARG,
                      "mesh %d: offset %lld must be %lld (segments follow one another, each rounded up to %d)", m,
                      (long long)M.offset, (long long)end, MM_SEG);
@@ -564,6 +697,8 @@ size_t mm_layout(int n_mesh, int restart, const MMCounts& k, char* base, mbem_mm
     char* p_rn2 = take(nm * sizeof(double));
     char* p_bn = take(nm * sizeof(double));
     char* p_mean = take(nm * 3 * sizeof(double));
+    char* p_bfull = take(nt * sizeof(double));
+    char* p_d = take(nt * sizeof(double));
     if (s) {
         s->d_meshes = (mbem_mm_mesh*)p_meshes;
         s->d_items = (MMItem*)p_items;
@@ -590,6 +725,8 @@ size_t mm_layout(int n_mesh, int restart, const MMCounts& k, char* base, mbem_mm
         s->rn2 = (double*)p_rn2;
         s->bnorm = (double*)p_bn;
         s->mean = (double*)p_mean;
+        s->Bfull = (double*)p_bfull;
+        s->D = (double*)p_d;
     }
     return off;
 }
@@ -616,10 +753,16 @@ cudaError_t mm_far_attribute() {
 #define MBEM_MM_CASES(X) X(0) X(1) X(2) X(3)
 static_assert(count_of(kMmTiles) == 4, "one case per configuration");
 
-// y = A x on the meshes flagged in `on`
+// y = A x on the meshes flagged in `on` (s->op16: the BF16 inner operator)
 int mm_apply(mbem_mm_solver* s, const double* x, double* y, const int* on, cudaStream_t st) {
     mm_split_kernel<<<blocks(s->n_total), 256, 0, st>>>(x, s->n_total, s->xh, s->xl);
     mm_near_kernel<<<blocks(s->n_total * 32), 256, 0, st>>>(s->d_meshes, s->chunk_mesh, on, x, y, s->n_total);
+    if (s->op16) {
+        // xh = x rounded to FP32
+        mm_matvec16_kernel<<<(unsigned)s->grid, MM_THREADS, M16_SMEM, st>>>(s->d_meshes, s->d_items, s->n_items, on,
+                                                                            s->xh, y);
+        return launch_status("mm_matvec16_kernel", 3);
+    }
     int e = set_error(MBEM_ERR_ARG, "no multi-mesh tile configuration %d", tune_get(MBEM_TUNE_MM_MATVEC));
     switch (tune_get(MBEM_TUNE_MM_MATVEC)) {
 #define MBEM_MM_CASE(i) \
@@ -715,6 +858,9 @@ int mbem_mm_create(const mbem_mm_mesh* meshes, int n_mesh, int restart, void* wo
     s->n_chunks = k.n_chunks;
     s->n_items = k.n_items;
     s->meshes.assign(meshes, meshes + n_mesh);
+    s->has16 = true;
+    for (int m = 0; m < n_mesh; m++)
+        if (meshes[m].A16 == nullptr) s->has16 = false;
     mm_layout(n_mesh, restart, k, (char*)work, s);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -726,6 +872,8 @@ int mbem_mm_create(const mbem_mm_mesh* meshes, int n_mesh, int restart, void* wo
     if (ce == cudaSuccess) ce = mm_far_attribute<kMmTiles[i].ch, kMmTiles[i].stages>();
     MBEM_MM_CASES(MBEM_MM_ATTR)
 #undef MBEM_MM_ATTR
+    if (ce == cudaSuccess)
+        ce = cudaFuncSetAttribute(mm_matvec16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M16_SMEM);
     if (ce != cudaSuccess) {
         delete s;
         return set_error(MBEM_ERR_CUDA, "multi-mesh matvec smem attribute: %s", cudaGetErrorString(ce));
@@ -766,7 +914,8 @@ int mbem_mm_create(const mbem_mm_mesh* meshes, int n_mesh, int restart, void* wo
 
 void mbem_mm_destroy(mbem_mm_solver* s) {
     if (!s) return;
-    if (s->cycle) cudaGraphExecDestroy(s->cycle);
+    for (int op = 0; op < 2; op++)
+        if (s->cycle[op]) cudaGraphExecDestroy(s->cycle[op]);
     delete s;
 }
 
@@ -790,31 +939,29 @@ static int mm_wait_check(cudaStream_t st) {
 
 int mbem_mm_check(void* stream) { return mm_wait_check((cudaStream_t)stream); }
 
-int mbem_mm_solve(mbem_mm_solver* s, const double* B, double* X, double rtol, int max_cycles, int use_graph,
-                  mbem_mm_report* rep, void* stream) {
-    MBEM_REQUIRE(s && B && X && rep, MBEM_ERR_ARG, "bad multi-mesh solve args");
-    MBEM_REQUIRE(rtol > 0.0 && rtol < 1.0 && max_cycles >= 1, MBEM_ERR_ARG, "bad rtol / max_cycles");
-    MBEM_REQUIRE(rep->iterations && rep->relres && rep->converged, MBEM_ERR_ARG,
-                 "report arrays (n_mesh each) are NULL");
-    cudaStream_t st = (cudaStream_t)stream;
+// The lockstep deflated GMRES(restart) core: every mesh not flagged in
+// `conv` solves (its operator: s->op16) for the right-hand side in s->Bz
+// from X = 0 to rtol of its own |P b|, at most max_cycles restart cycles.
+// relres: each mesh's true relative residual at its last check; conv: set
+// for the meshes that reached rtol (or have b = 0).
+static int mm_gmres(mbem_mm_solver* s, double* X, double rtol, int max_cycles, int use_graph, std::vector<int>& conv,
+                    std::vector<double>& relres, int& cycles, cudaStream_t st) {
     const int nm = s->n_mesh, m = s->restart;
     const int64_t nt = s->n_total;
+    const int op = s->op16 ? 1 : 0;
     int e;
     std::vector<double> bn2(nm), rn2(nm), bnorm(nm);
-    std::vector<int> act(nm), conv(nm, 0);
-    // B with zero padding; its projected norm per mesh
-    mm_masked_copy_kernel<<<blocks(nt), 256, 0, st>>>(B, s->Bz, s->d_meshes, s->chunk_mesh, nt);
+    std::vector<int> act(nm);
     cudaMemcpyAsync(s->R, s->Bz, sizeof(double) * nt, cudaMemcpyDeviceToDevice, st);
     if ((e = mm_project(s, s->R, s->all_on, st))) return e;
     if ((e = mm_dots(s, s->R, 1, s->R, s->all_on, 0, s->rn2, 1, st))) return e;
     cudaMemcpyAsync(bn2.data(), s->rn2, sizeof(double) * nm, cudaMemcpyDeviceToHost, st);
     cudaMemsetAsync(X, 0, sizeof(double) * nt, st);
-    cudaMemsetAsync(s->iters, 0, sizeof(int) * nm, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("multi-mesh solve", 0);
     for (int q = 0; q < nm; q++) bnorm[q] = sqrt(bn2[q]);
     cudaMemcpyAsync(s->bnorm, bnorm.data(), sizeof(double) * nm, cudaMemcpyHostToDevice, st);
     bool x_zero = true;
-    int cycles = 0;
+    cycles = 0;
     for (;;) {
         // r = P (b - A x) on the meshes not yet converged (P b while x == 0)
         for (int q = 0; q < nm; q++) act[q] = conv[q] ? 0 : 1;
@@ -833,8 +980,8 @@ int mbem_mm_solve(mbem_mm_solver* s, const double* B, double* X, double rtol, in
         bool any = false;
         for (int q = 0; q < nm; q++) {
             if (conv[q]) continue;
-            rep->relres[q] = bnorm[q] > 0.0 ? sqrt(rn2[q]) / bnorm[q] : 0.0;
-            if (bnorm[q] == 0.0 || rep->relres[q] < rtol) conv[q] = 1;
+            relres[q] = bnorm[q] > 0.0 ? sqrt(rn2[q]) / bnorm[q] : 0.0;
+            if (bnorm[q] == 0.0 || relres[q] < rtol) conv[q] = 1;
             else any = true;
         }
         if (!any || cycles >= max_cycles) break;
@@ -845,10 +992,11 @@ int mbem_mm_solve(mbem_mm_solver* s, const double* B, double* X, double rtol, in
         mm_cycle_start_kernel<<<blocks(nm, 64), 64, 0, st>>>(nm, m, s->rn2, s->g, s->jdone, s->active);
         mm_scale_kernel<<<blocks(nt), 256, 0, st>>>(s->R, s->V, s->rn2, 1, s->chunk_mesh, s->active, nt);
         if (use_graph) {
-            if (s->cycle == nullptr || s->cycle_rtol != rtol || s->cycle_cfg != tune_get(MBEM_TUNE_MM_MATVEC)) {
-                if (s->cycle) {
-                    cudaGraphExecDestroy(s->cycle);
-                    s->cycle = nullptr;
+            if (s->cycle[op] == nullptr || s->cycle_rtol[op] != rtol ||
+                s->cycle_cfg[op] != tune_get(MBEM_TUNE_MM_MATVEC)) {
+                if (s->cycle[op]) {
+                    cudaGraphExecDestroy(s->cycle[op]);
+                    s->cycle[op] = nullptr;
                 }
                 cudaGraph_t graph = nullptr;
                 const unsigned long long before = mbem_launch_count();
@@ -858,25 +1006,25 @@ int mbem_mm_solve(mbem_mm_solver* s, const double* B, double* X, double rtol, in
                 for (int j = 0; j < m && es == MBEM_OK; j++) es = mm_step(s, j, rtol, st);
                 ce = cudaStreamEndCapture(st, &graph);
                 // captured launches run when the graph does: count them per replay
-                s->cycle_kernels = (long long)(mbem_launch_count() - before);
-                count_launches((int)-s->cycle_kernels);
+                s->cycle_kernels[op] = (long long)(mbem_launch_count() - before);
+                count_launches((int)-s->cycle_kernels[op]);
                 if (es) {
                     if (graph) cudaGraphDestroy(graph);
                     return es;
                 }
                 if (ce != cudaSuccess) return set_error(MBEM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
-                ce = cudaGraphInstantiate(&s->cycle, graph, 0);
+                ce = cudaGraphInstantiate(&s->cycle[op], graph, 0);
                 cudaGraphDestroy(graph);
                 if (ce != cudaSuccess) {
-                    s->cycle = nullptr;
+                    s->cycle[op] = nullptr;
                     return set_error(MBEM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
                 }
-                s->cycle_rtol = rtol;
-                s->cycle_cfg = tune_get(MBEM_TUNE_MM_MATVEC);
+                s->cycle_rtol[op] = rtol;
+                s->cycle_cfg[op] = tune_get(MBEM_TUNE_MM_MATVEC);
             }
-            cudaError_t ce = cudaGraphLaunch(s->cycle, st);
+            cudaError_t ce = cudaGraphLaunch(s->cycle[op], st);
             if (ce != cudaSuccess) return set_error(MBEM_ERR_CUDA, "graph launch: %s", cudaGetErrorString(ce));
-            count_launches((int)s->cycle_kernels);
+            count_launches((int)s->cycle_kernels[op]);
         } else {
             for (int j = 0; j < m; j++)
                 if ((e = mm_step(s, j, rtol, st))) return e;
@@ -889,6 +1037,13 @@ int mbem_mm_solve(mbem_mm_solver* s, const double* B, double* X, double rtol, in
         x_zero = false;
         cycles++;
     }
+    return MBEM_OK;
+}
+
+static int mm_finish(mbem_mm_solver* s, double* X, const std::vector<int>& conv, const std::vector<double>& relres,
+                     int cycles, mbem_mm_report* rep, cudaStream_t st) {
+    const int nm = s->n_mesh;
+    int e;
     // the zero-mean representative P x
     if ((e = mm_project(s, X, s->all_on, st))) return e;
     std::vector<int> its(nm);
@@ -897,9 +1052,101 @@ int mbem_mm_solve(mbem_mm_solver* s, const double* B, double* X, double rtol, in
     for (int q = 0; q < nm; q++) {
         rep->iterations[q] = its[q];
         rep->converged[q] = conv[q];
+        rep->relres[q] = relres[q];
     }
     rep->cycles = cycles;
     return MBEM_OK;
+}
+
+int mbem_mm_solve(mbem_mm_solver* s, const double* B, double* X, double rtol, int max_cycles, int use_graph,
+                  mbem_mm_report* rep, void* stream) {
+    MBEM_REQUIRE(s && B && X && rep, MBEM_ERR_ARG, "bad multi-mesh solve args");
+    MBEM_REQUIRE(rtol > 0.0 && rtol < 1.0 && max_cycles >= 1, MBEM_ERR_ARG, "bad rtol / max_cycles");
+    MBEM_REQUIRE(rep->iterations && rep->relres && rep->converged, MBEM_ERR_ARG,
+                 "report arrays (n_mesh each) are NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int nm = s->n_mesh;
+    const int64_t nt = s->n_total;
+    std::vector<int> conv(nm, 0);
+    std::vector<double> relres(nm, 0.0);
+    int cycles = 0;
+    s->op16 = 0;
+    mm_masked_copy_kernel<<<blocks(nt), 256, 0, st>>>(B, s->Bz, s->d_meshes, s->chunk_mesh, nt);
+    cudaMemsetAsync(s->iters, 0, sizeof(int) * nm, st);
+    int e = mm_gmres(s, X, rtol, max_cycles, use_graph, conv, relres, cycles, st);
+    if (e) return e;
+    return mm_finish(s, X, conv, relres, cycles, rep, st);
+}
+
+// The mixed-precision batch solve: refinement on the accurate operator (FP32
+// far field with double-float sums, FP64 near blocks) whose corrections are
+// lockstep GMRES solves on the BF16 far fields to inner_rtol of each
+// residual. rep->iterations: the inner steps of each mesh; rep->relres: the
+// true residual of the accurate operator; rep->cycles: refinement steps.
+int mbem_mm_solve_mixed(mbem_mm_solver* s, const double* B, double* X, double rtol, double inner_rtol, int max_outer,
+                        int max_cycles, int use_graph, mbem_mm_report* rep, void* stream) {
+    MBEM_REQUIRE(s && B && X && rep, MBEM_ERR_ARG, "bad multi-mesh solve args");
+    MBEM_REQUIRE(s->has16, MBEM_ERR_ARG, "the mixed batch solve needs every mesh's BF16 far field (A16)");
+    MBEM_REQUIRE(rtol > 0.0 && rtol < 1.0 && inner_rtol > 0.0 && inner_rtol < 1.0 && max_outer >= 1 &&
+                     max_cycles >= 1,
+                 MBEM_ERR_ARG, "bad tolerances or step limits");
+    MBEM_REQUIRE(rep->iterations && rep->relres && rep->converged, MBEM_ERR_ARG,
+                 "report arrays (n_mesh each) are NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int nm = s->n_mesh;
+    const int64_t nt = s->n_total;
+    int e;
+    std::vector<int> conv(nm, 0), act(nm);
+    std::vector<double> relres(nm, 0.0), bn2(nm), rn2(nm);
+    // B with zero padding, |P B| per mesh
+    mm_masked_copy_kernel<<<blocks(nt), 256, 0, st>>>(B, s->Bfull, s->d_meshes, s->chunk_mesh, nt);
+    cudaMemcpyAsync(s->Bz, s->Bfull, sizeof(double) * nt, cudaMemcpyDeviceToDevice, st);
+    if ((e = mm_project(s, s->Bz, s->all_on, st))) return e;
+    if ((e = mm_dots(s, s->Bz, 1, s->Bz, s->all_on, 0, s->rn2, 1, st))) return e;
+    cudaMemcpyAsync(bn2.data(), s->rn2, sizeof(double) * nm, cudaMemcpyDeviceToHost, st);
+    cudaMemsetAsync(X, 0, sizeof(double) * nt, st);
+    cudaMemsetAsync(s->iters, 0, sizeof(int) * nm, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("multi-mesh solve", 0);
+    int outer = 0;
+    for (;;) {
+        // the accurate residual P (B - A X) of the meshes not yet converged
+        if (outer > 0) {
+            for (int q = 0; q < nm; q++) act[q] = conv[q] ? 0 : 1;
+            cudaMemcpyAsync(s->active, act.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
+            s->op16 = 0;
+            if ((e = mm_apply(s, X, s->W, s->active, st))) return e;
+            cudaMemcpyAsync(s->Bz, s->Bfull, sizeof(double) * nt, cudaMemcpyDeviceToDevice, st);
+            mm_axpby_kernel<<<blocks(nt), 256, 0, st>>>(s->Bz, s->W, -1.0, 1.0, s->chunk_mesh, s->active, nt);
+            if ((e = mm_project(s, s->Bz, s->active, st))) return e;
+            if ((e = mm_dots(s, s->Bz, 1, s->Bz, s->active, 0, s->rn2, 1, st))) return e;
+            cudaMemcpyAsync(rn2.data(), s->rn2, sizeof(double) * nm, cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("multi-mesh solve", 0);
+        } else {
+            rn2 = bn2;
+        }
+        bool any = false;
+        for (int q = 0; q < nm; q++) {
+            if (conv[q]) continue;
+            relres[q] = bn2[q] > 0.0 ? sqrt(rn2[q] / bn2[q]) : 0.0;
+            if (bn2[q] == 0.0 || relres[q] < rtol) conv[q] = 1;
+            else any = true;
+        }
+        if (!any || outer >= max_outer) break;
+        // the correction: the BF16 operator's GMRES for the residual (in s->Bz)
+        std::vector<int> iconv = conv;
+        std::vector<double> irel(nm, 0.0);
+        int icycles = 0;
+        s->op16 = 1;
+        e = mm_gmres(s, s->D, inner_rtol, max_cycles, use_graph, iconv, irel, icycles, st);
+        s->op16 = 0;
+        if (e) return e;
+        for (int q = 0; q < nm; q++) act[q] = conv[q] ? 0 : 1;
+        cudaMemcpyAsync(s->active, act.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
+        mm_axpby_kernel<<<blocks(nt), 256, 0, st>>>(X, s->D, 1.0, 1.0, s->chunk_mesh, s->active, nt);
+        if ((e = launch_status("mm_refine", 1))) return e;
+        outer++;
+    }
+    return mm_finish(s, X, conv, relres, outer, rep, st);
 }
 
 }  // extern "C"

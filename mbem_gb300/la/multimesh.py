@@ -86,8 +86,10 @@ class MeshBatch:
             rowptr, cols, vals = _merged_near(op)
             self._keep.append((rowptr, cols, vals))
             n = op.n
+            A16 = op.A16
             meshes[i] = nat.MmMesh(ptr(op.A32), op.A32.stride(0), n, off, ptr(rowptr), ptr(cols), ptr(vals),
-                                   int(u_off), int(u_len))
+                                   int(u_off), int(u_len), ptr(A16) if A16 is not None else None,
+                                   A16.stride(0) if A16 is not None else 0)
             self.offsets.append(off)
             self.sizes.append(n)
             off += -(-n // nat.MM_SEGMENT) * nat.MM_SEGMENT
@@ -136,6 +138,34 @@ class MeshBatch:
         Y = torch.zeros_like(X)
         self._run(lambda: nat.call("mbem_mm_matvec", self._handle, ptr(X), ptr(Y), stream_handle()))
         return Y
+
+    @property
+    def has_bf16(self) -> bool:
+        """Every mesh carries the BF16 copy of its far field (assembled with
+        precond="bf16_inner"): the mixed solve is available."""
+        return all(a.op.A16 is not None for a in self.systems)
+
+    def solve_mixed(self, B: torch.Tensor | None = None, rtol: float = 1e-8, inner_rtol: float = 1e-5,
+                    max_outer: int = 6, max_cycles: int = 4, graph: bool = True):
+        """(X, BatchReport): refinement on the accurate operators whose
+        corrections are lockstep GMRES solves on the BF16 far fields (2 bytes
+        an entry) to ``inner_rtol`` of each residual. BatchReport.cycles:
+        refinement steps; iterations: the inner steps of each mesh."""
+        if not self.has_bf16:
+            raise ValueError("the mixed batch solve needs every system assembled with precond='bf16_inner'")
+        if B is None:
+            B = self.gather([asm.b for asm in self.systems])
+        B = B.to(torch.float64).contiguous()
+        X = torch.empty_like(B)
+        nm = self.n_mesh
+        its = (ctypes.c_int * nm)()
+        rel = (ctypes.c_double * nm)()
+        conv = (ctypes.c_int * nm)()
+        rep = nat.MmReport(its, rel, conv, 0)
+        self._run(lambda: nat.call("mbem_mm_solve_mixed", self._handle, ptr(B), ptr(X), float(rtol),
+                                   float(inner_rtol), int(max_outer), int(max_cycles), int(bool(graph)),
+                                   ctypes.byref(rep), stream_handle()))
+        return X, BatchReport(list(its), list(rel), [bool(c) for c in conv], int(rep.cycles))
 
     def solve(self, B: torch.Tensor | None = None, rtol: float = 1e-8, max_cycles: int = 40,
               graph: bool = True):

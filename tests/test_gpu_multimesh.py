@@ -82,3 +82,24 @@ def test_batched_restart_cycles_and_zero_rhs(batch):
     assert rep2.all_converged and rep2.cycles > 1
     for a, x in zip(systems, mb2.scatter(X2)):
         assert _deflated_relres(a, x) < 1e-9
+
+
+def test_mixed_batch_solve(gpu):
+    """The mixed batch solve (BF16 inner solves inside refinement on the
+    accurate operators): every mesh's true residual of the accurate operator
+    below rtol, solutions within 1e-9 of the single-system solves."""
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.la.multimesh import MeshBatch
+    from mbem_gb300.model import generate_system
+    be = DenseBackend(jump="calibrated", deflate=True, rtol=1e-10, precision="mixed", precond="bf16_inner")
+    systems = [be.assemble(generate_system(m), e) for m, e in (cube_fault_model(nf, nq) for nf, nq in SHAPES)]
+    mb = MeshBatch(systems)
+    assert mb.has_bf16
+    for graph in (True, False):
+        X, rep = mb.solve_mixed(rtol=1e-10, graph=graph)
+        assert rep.all_converged and max(rep.relres) < 1e-10 and rep.cycles >= 1
+        for a, x in zip(systems, mb.scatter(X)):
+            x1 = a.solve_device(rtol=1e-11, precond="none")
+            assert float((x - x1).norm() / x1.norm()) < 1e-9
+            assert _deflated_relres(a, x) < 1e-10

@@ -39,7 +39,7 @@ def test_multi_mesh_layout_rules():
         arr = (_native.MmMesh * len(sizes))()
         for i, (n, o) in enumerate(zip(sizes, offsets)):
             # placeholder (never dereferenced) 16-byte aligned pointers
-            arr[i] = _native.MmMesh(4096, (n + 3) // 4 * 4, n, o, 4096, 4096, 4096, 0, n)
+            arr[i] = _native.MmMesh(4096, (n + 3) // 4 * 4, n, o, 4096, 4096, 4096, 0, n, None, 0)
         return arr
 
     seg = _native.MM_SEGMENT
@@ -51,4 +51,4 @@ def test_multi_mesh_layout_rules():
     assert lib.mbem_mm_total(meshes([300, 2400], [0, 300]), 2) == -1             # not rounded up
     assert lib.mbem_mm_total(meshes([301], [0]), 1) == -1                        # not a multiple of 3
     assert lib.mbem_mm_workspace_size(meshes(sizes, offs), 3, _native.MM_MAX_RESTART + 1) == 0
-    assert ctypes.sizeof(_native.MmMesh) == 72
+    assert ctypes.sizeof(_native.MmMesh) == 88
