@@ -9,6 +9,7 @@ nodal     the P2 DD-minus-eigen readout of a 16 x 16 fault at 20,000 points
 mixedmv   the FP32 double-float operator product, cube 24 (20,736 unknowns)
 bf16mv    the BF16 inner product of the mixed solve, cube 24
 mm        the persistent multi-mesh product: 8 cubes, grids drawn in [8, 20]
+mm16      its BF16 inner operator (mm_matvec16_kernel) on the same 8 cubes
 readout   the mixed P2 stress readout: fault 32 x 32, 100,000 observers
 asm64     the FP64 P0 assembly of cube 12 (p0_matrix_kernel) and the FP64 P1
           assembly of cube 8 (nodal_matrix_kernel)
@@ -74,15 +75,19 @@ def run(which: str) -> None:
         inner = Bf16Inner(asm.op, 1, asm.u_ranges())
         for _ in range(3):
             (asm.op.matvec if which == "mixedmv" else inner.matvec)(x, out=y)
-    elif which == "mm":
+    elif which in ("mm", "mm16"):
         from .la.multimesh import MeshBatch, random_cube_batch
-        be = DenseBackend(jump="calibrated", deflate=True, precision="mixed")
+        be = DenseBackend(jump="calibrated", deflate=True, precision="mixed",
+                          precond="bf16_inner" if which == "mm16" else None)
         systems = [be.assemble(generate_system(m), e)
                    for m, e in (cube_fault_model(nf, nq) for nf, nq in random_cube_batch(8, 8, 20, 3))]
         mb = MeshBatch(systems)
-        x = torch.randn(mb.n_total, dtype=torch.float64, device="cuda")
-        for _ in range(3):
-            mb.matvec(x)
+        if which == "mm":
+            x = torch.randn(mb.n_total, dtype=torch.float64, device="cuda")
+            for _ in range(3):
+                mb.matvec(x)
+        else:
+            mb.solve_mixed(rtol=1e-8)
     elif which == "readout":
         from . import mesh as M
         from .kernels import tri_nodal as tn
