@@ -292,9 +292,10 @@ size_t mbem_lu_solve_many_workspace_size(int64_t n, int64_t k);
 int mbem_lu_solve_many_f32(const float* LU, int64_t lda, int64_t n, const int32_t* perm, const double* B,
                            int64_t ldb, int64_t k, double* X, int64_t ldx, void* work, size_t work_bytes,
                            void* stream);
-/* Device ms of the factorisations' phases since the last call (panel,
- * interchanges, triangular solve, operand split, tensor-core update); resets
- * them and switches the phase timing of later factorisations on or off. */
+/* Device ms of the factorisations' phases since the last call (phase_ms[3]:
+ * the panels with their interchanges, the U block rows, the tensor-core
+ * trailing updates); resets them and switches the phase timing of later
+ * factorisations on or off. */
 void mbem_lu_stats(int timing, double* phase_ms);
 int mbem_lu_solve_f32(const float* LU, int64_t lda, int64_t n, const int32_t* perm, const double* b, double* x,
                       float* xf, void* stream);

@@ -2,14 +2,17 @@
 // factorisation behind the reference's la/lu.py `Factor(how="single"|"gpu")`
 // (FP32 factors, FP64 iterative refinement by the caller).
 //
-// Right-looking, blocked by LU_NB columns:
+// Right-looking, in outer blocks of four LU_NB-column panels:
 //   1. panel: rows k..n-1 of columns k..k+NB-1 factored by ONE cooperative
 //      launch; each CTA holds a contiguous slice of the panel rows in shared
 //      memory, and every column takes one grid barrier (bounded spin on a
 //      generation counter): local arg-max, candidates published, barrier,
 //      every CTA picks the same pivot (largest |value|, then lowest row),
 //      swaps and eliminates its own rows;
-//   2. the panel's row interchanges applied to the other columns;
+//   2. the panel's row interchanges applied to the other columns (a later
+//      panel of a block is first brought up to date by the earlier ones:
+//      their U rows on its columns, each followed by the update of the rows
+//      below, left-looking);
 //   3. U12 = L11^-1 A12 (unit lower triangle, one column a thread:
 //      lu_block_trsm_kernel, also the diagonal blocks of the solves);
 //   4. A22 -= L21 U12 on the tensor cores: both operands split into three
@@ -33,16 +36,17 @@
 namespace mbem {
 
 constexpr int LU_NB = 64;                 // panel width
+constexpr int LU_OB = 256;                // outer block: four panels, one trailing update
 constexpr int LU_PT = 256;                // panel threads
 constexpr int LU_LDS = LU_NB + 1;         // padded shared-memory row (no bank conflicts)
 constexpr uint32_t LU_WAIT_LIMIT = 1u << 24;
 
 __device__ int g_lu_wait_error = 0;
 
-// optional device time of the factorisation's phases (panel, interchanges,
-// triangular solve, operand split, tensor-core update), in ms
+// optional device time of the factorisation's phases (the panels with their
+// interchanges, the U block rows, the trailing updates), in ms
 static int g_lu_timing = 0;
-static double g_lu_phase_ms[5] = {0, 0, 0, 0, 0};
+static double g_lu_phase_ms[3] = {0, 0, 0};
 
 struct PanelArgs {
     float* A;
@@ -260,44 +264,60 @@ __device__ __forceinline__ void bf16_pieces(float x, uint16_t& hi, uint16_t& mid
     lo = __bfloat16_as_ushort(__float2bfloat16_rn(r2));
 }
 
-// Ls[r][6 x 64]: the pieces of rows row0 + r (r < M) of a row-major FP32
-// matrix at columns col0 .. col0 + nbw (L21 in the factorisation, the L or U
-// panel of a blocked solve)
+// Ls[r][6 x W]: the pieces of rows row0 + r (r < M) of a row-major FP32
+// matrix at columns col0 .. col0 + nbw (W = 64 or 128; L21 in the
+// factorisation, the L or U panel of a blocked solve)
+template <int W>
 __global__ void lu_split_rows_kernel(const float* __restrict__ A, int64_t lda, int64_t row0, int64_t col0, int nbw,
                                      int64_t M, uint16_t* __restrict__ Ls) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= M * LU_NB) return;
-    const int64_t r = e / LU_NB;
-    const int kk = (int)(e % LU_NB);
+    if (e >= M * W) return;
+    const int64_t r = e / W;
+    const int kk = (int)(e % W);
     const float x = kk < nbw ? A[(row0 + r) * lda + col0 + kk] : 0.0f;
     uint16_t h, m, l;
     bf16_pieces(x, h, m, l);
-    uint16_t* o = Ls + r * LU_K6 + kk;
-    o[0] = h; o[LU_NB] = h; o[2 * LU_NB] = h; o[3 * LU_NB] = m; o[4 * LU_NB] = m; o[5 * LU_NB] = l;
+    uint16_t* o = Ls + r * (6 * W) + kk;
+    o[0] = h; o[W] = h; o[2 * W] = h; o[3 * W] = m; o[4 * W] = m; o[5 * W] = l;
 }
 
-// Us[j][6 x 64]: the pieces of column col0 + j (j < N) of rows row0 ..
+// Us[j][6 x W]: the pieces of column col0 + j (j < N) of rows row0 ..
 // row0 + nbw of a row-major FP32 matrix (U12 in the factorisation, a block of
-// right-hand sides in a solve); a 64 x 32 tile through shared memory keeps
+// right-hand sides in a solve); a W x 32 tile through shared memory keeps
 // reads and writes coalesced
+template <int W>
 __global__ void __launch_bounds__(256)
 lu_split_cols_kernel(const float* __restrict__ A, int64_t lda, int64_t row0, int64_t col0, int nbw, int64_t N,
                      uint16_t* __restrict__ Us) {
-    __shared__ float T[LU_NB][33];
+    __shared__ float T[W][33];
     const int64_t j0 = (int64_t)blockIdx.x * 32;
-    for (int e = threadIdx.x; e < LU_NB * 32; e += 256) {
+    for (int e = threadIdx.x; e < W * 32; e += 256) {
         const int kk = e / 32, j = e % 32;
         T[kk][j] = (kk < nbw && j0 + j < N) ? A[(row0 + kk) * lda + col0 + j0 + j] : 0.0f;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < LU_NB * 32; e += 256) {
-        const int j = e / LU_NB, kk = e % LU_NB;
+    for (int e = threadIdx.x; e < W * 32; e += 256) {
+        const int j = e / W, kk = e % W;
         if (j0 + j >= N) continue;
         uint16_t h, m, l;
         bf16_pieces(T[kk][j], h, m, l);
-        uint16_t* o = Us + (j0 + j) * LU_K6 + kk;
-        o[0] = h; o[LU_NB] = m; o[2 * LU_NB] = l; o[3 * LU_NB] = h; o[4 * LU_NB] = m; o[5 * LU_NB] = h;
+        uint16_t* o = Us + (j0 + j) * (6 * W) + kk;
+        o[0] = h; o[W] = m; o[2 * W] = l; o[3 * W] = h; o[4 * W] = m; o[5 * W] = h;
     }
+}
+
+// C[M x N] (at ldc) -= rows (row0 .., M) x columns (col0 .., w) of A times
+// rows (urow0 .., w) x columns (ucol0 .., N) of A, all in A (at lda): the
+// six-piece tensor-core product, panel width W
+template <int W>
+static int lu_block_update(float* A, int64_t lda, int64_t row0, int64_t col0, int64_t M, int w, int64_t urow0,
+                           int64_t ucol0, int64_t N, float* C, int64_t ldc, uint16_t* Ls, uint16_t* Us,
+                           cudaStream_t st) {
+    if (M <= 0 || N <= 0) return MBEM_OK;
+    lu_split_rows_kernel<W><<<(unsigned)ceil_div(M * W, 256), 256, 0, st>>>(A, lda, row0, col0, w, M, Ls);
+    lu_split_cols_kernel<W><<<(unsigned)ceil_div(N, 32), 256, 0, st>>>(A, lda, urow0, ucol0, w, N, Us);
+    count_launches(2);
+    return gemm_bf16_sub(Ls, 6 * W, Us, 6 * W, M, N, 6 * W, C, ldc, st);
 }
 
 // X[r0 .. r0 + nb) (ncols columns at ldx) = T^-1 X with T the nb x nb
@@ -418,7 +438,7 @@ extern "C" {
 size_t mbem_lu_workspace_size(int64_t n, int sms) {
     const size_t G = (size_t)(sms > 0 ? sms : 1);
     return 2 * G * sizeof(float) + 2 * G * sizeof(int64_t) + 2 * G * LU_NB * sizeof(float) +
-           2 * LU_NB * sizeof(float) + 4 * sizeof(unsigned) + 2 * (size_t)n * LU_K6 * sizeof(uint16_t) + 8 * 256;
+           2 * LU_NB * sizeof(float) + 4 * sizeof(unsigned) + 2 * (size_t)n * 6 * LU_OB * sizeof(uint16_t) + 8 * 256;
 }
 
 int mbem_lu_factor_f32(float* A, int64_t lda, int64_t n, int32_t* piv, void* work, size_t work_bytes, int* info,
@@ -449,14 +469,15 @@ int mbem_lu_factor_f32(float* A, int64_t lda, int64_t n, int32_t* piv, void* wor
     unsigned* bar = (unsigned*)take(4 * sizeof(unsigned));
     a.bar_count = bar;
     a.bar_gen = bar + 1;
-    uint16_t* Ls = (uint16_t*)take((size_t)n * LU_K6 * sizeof(uint16_t));
-    uint16_t* Us = (uint16_t*)take((size_t)n * LU_K6 * sizeof(uint16_t));
+    uint16_t* Ls = (uint16_t*)take((size_t)n * 6 * LU_OB * sizeof(uint16_t));
+    uint16_t* Us = (uint16_t*)take((size_t)n * 6 * LU_OB * sizeof(uint16_t));
     if ((size_t)(w - (char*)work) > work_bytes) return set_error(MBEM_ERR_SIZE, "LU workspace layout");
     cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned), st);
     cudaMemsetAsync(info, 0, sizeof(int), st);
     cudaError_t ce = cudaFuncSetAttribute(lu_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (ce != cudaSuccess) return set_error(MBEM_ERR_CUDA, "LU smem attribute: %s", cudaGetErrorString(ce));
     int64_t launches = 0;
+    int e = MBEM_OK;
     std::vector<cudaEvent_t> evs;
     auto mark = [&]() {
         if (!g_lu_timing) return;
@@ -465,56 +486,84 @@ int mbem_lu_factor_f32(float* A, int64_t lda, int64_t n, int32_t* piv, void* wor
         cudaEventRecord(e2, st);
         evs.push_back(e2);
     };
-    for (int64_t k = 0; k < n; k += LU_NB) {
-        mark();
-        const int nbw = (int)lmin(LU_NB, n - k);
+    // outer blocks of LU_OB columns (four panels): each panel brought up to
+    // date and factored (its interchanges applied) in turn, the block's U
+    // rows by 64-row triangular solves, then one trailing update with
+    // K = 6 x LU_OB
+    auto panel = [&](int64_t k, int nbw) -> int {
         a.k = k;
         const int64_t m = n - k;
         const int G = sms;
         const size_t smem = (size_t)ceil_div(m, G) * LU_LDS * sizeof(float);
         void* args[] = {&a};
-        ce = cudaLaunchCooperativeKernel((const void*)lu_panel_kernel, dim3((unsigned)G), dim3(LU_PT), args, smem,
-                                         st);
-        if (ce != cudaSuccess) return set_error(MBEM_ERR_CUDA, "LU panel launch: %s", cudaGetErrorString(ce));
-        launches++;
-        mark();
+        cudaError_t le = cudaLaunchCooperativeKernel((const void*)lu_panel_kernel, dim3((unsigned)G), dim3(LU_PT),
+                                                     args, smem, st);
+        if (le != cudaSuccess) return set_error(MBEM_ERR_CUDA, "LU panel launch: %s", cudaGetErrorString(le));
         const int64_t others = n - nbw;
-        if (others > 0) {
-            lu_swap_kernel<<<(unsigned)ceil_div(others, 256), 256, 0, st>>>(A, lda, n, k, nbw, piv);
-            launches++;
+        if (others > 0) lu_swap_kernel<<<(unsigned)ceil_div(others, 256), 256, 0, st>>>(A, lda, n, k, nbw, piv);
+        launches += 2;
+        return MBEM_OK;
+    };
+    auto trsm = [&](int64_t r0, int nb, int64_t col0, int64_t ncols) {
+        if (ncols <= 0) return;
+        lu_block_trsm_kernel<<<(unsigned)ceil_div(ncols, 128), 128, 0, st>>>(A, lda, A + col0, lda, ncols, r0, nb, 1);
+        launches++;
+    };
+    for (int64_t k = 0; k < n; k += LU_OB) {
+        const int ob = (int)lmin(LU_OB, n - k);
+        const int np = (int)ceil_div(ob, LU_NB);                 // panels in this block
+        mark();
+        for (int pnl = 0; pnl < np; pnl++) {
+            const int64_t cp = k + (int64_t)pnl * LU_NB;            // the panel's first column (and row)
+            const int wp = (int)lmin(LU_NB, k + ob - cp);
+            // left-looking within the block: the earlier panels' U rows on
+            // this panel's columns, each followed by its update of the rows below
+            for (int q = 0; q < pnl; q++) {
+                const int64_t cq = k + (int64_t)q * LU_NB;
+                trsm(cq, LU_NB, cp, wp);
+                if ((e = lu_block_update<LU_NB>(A, lda, cq + LU_NB, cq, n - cq - LU_NB, LU_NB, cq, cp, wp,
+                                                A + (cq + LU_NB) * lda + cp, lda, Ls, Us, st)))
+                    return e;
+            }
+            if ((e = panel(cp, wp))) return e;
         }
         mark();
-        const int64_t rest = n - k - nbw;
+        const int64_t rest = n - k - ob;
         if (rest > 0) {
-            lu_block_trsm_kernel<<<(unsigned)ceil_div(rest, 128), 128, 0, st>>>(A, lda, A + k + nbw, lda, rest, k, nbw,
-                                                                               1);
+            // U12 (rows k .. k + ob): panel by panel, each one's rows solved,
+            // then its update of the block's later rows
+            for (int q = 0; q < np; q++) {
+                const int64_t cq = k + (int64_t)q * LU_NB;
+                const int wq = (int)lmin(LU_NB, k + ob - cq);
+                trsm(cq, wq, k + ob, rest);
+                const int64_t below = k + ob - cq - wq;
+                if (below > 0 &&
+                    (e = lu_block_update<LU_NB>(A, lda, cq + wq, cq, below, wq, cq, k + ob, rest,
+                                                A + (cq + wq) * lda + k + ob, lda, Ls, Us, st)))
+                    return e;
+            }
             mark();
-            // A22 -= L21 U12 on the tensor cores (six BF16 piece products, FP32 accumulation)
-            lu_split_rows_kernel<<<(unsigned)ceil_div(rest * LU_NB, 256), 256, 0, st>>>(A, lda, k + nbw, k, nbw, rest,
-                                                                                       Ls);
-            lu_split_cols_kernel<<<(unsigned)ceil_div(rest, 32), 256, 0, st>>>(A, lda, k, k + nbw, nbw, rest, Us);
-            launches += 3;
-            mark();
-            int ge = gemm_bf16_sub(Ls, LU_K6, Us, LU_K6, rest, rest, LU_K6, A + (k + nbw) * lda + k + nbw, lda, st);
-            if (ge) return ge;
+            // A22 -= L21 U12 on the tensor cores (six BF16 piece products, K = 6 x LU_OB)
+            if ((e = lu_block_update<LU_OB>(A, lda, k + ob, k, rest, ob, k, k + ob, rest,
+                                            A + (k + ob) * lda + k + ob, lda, Ls, Us, st)))
+                return e;
         } else {
-            mark();
             mark();
         }
     }
     mark();
     if (g_lu_timing && !evs.empty()) {
         cudaEventSynchronize(evs.back());
-        // marks per panel: start, after panel, after swap, after trsm, after split; then the next start
-        for (size_t i = 0; i + 5 < evs.size(); i += 5)
-            for (int ph = 0; ph < 5; ph++) {
+        // marks per outer block: start, after its panels, after its U rows; then the next start
+        for (size_t i = 0; i + 3 < evs.size(); i += 3)
+            for (int ph = 0; ph < 3; ph++) {
                 float ms = 0.f;
                 cudaEventElapsedTime(&ms, evs[i + ph], evs[i + ph + 1]);
                 g_lu_phase_ms[ph] += ms;
             }
         for (auto e2 : evs) cudaEventDestroy(e2);
     }
-    int e = launch_status("lu_factor", (int)launches);
+    e = launch_status("lu_factor", (int)launches);
     if (e) return e;
     if ((e = tc_gemm_check(st))) return e;
     int flag = 0;
@@ -531,8 +580,8 @@ int mbem_lu_factor_f32(float* A, int64_t lda, int64_t n, int32_t* piv, void* wor
 
 void mbem_lu_stats(int timing, double* phase_ms) {
     if (phase_ms)
-        for (int i = 0; i < 5; i++) phase_ms[i] = g_lu_phase_ms[i];
-    for (int i = 0; i < 5; i++) g_lu_phase_ms[i] = 0.0;
+        for (int i = 0; i < 3; i++) phase_ms[i] = g_lu_phase_ms[i];
+    for (int i = 0; i < 3; i++) g_lu_phase_ms[i] = 0.0;
     g_lu_timing = timing != 0;
 }
 
@@ -600,9 +649,9 @@ int mbem_lu_solve_many_f32(const float* LU, int64_t lda, int64_t n, const int32_
         launches++;
         const int64_t below = n - r0 - nb;
         if (below > 0) {
-            lu_split_rows_kernel<<<(unsigned)ceil_div(below * LU_NB, 256), 256, 0, st>>>(LU, lda, r0 + nb, r0, nb,
-                                                                                        below, Lp);
-            lu_split_cols_kernel<<<(unsigned)ceil_div(k, 32), 256, 0, st>>>(X32, k, r0, 0, nb, k, Xp);
+            lu_split_rows_kernel<LU_NB><<<(unsigned)ceil_div(below * LU_NB, 256), 256, 0, st>>>(LU, lda, r0 + nb, r0,
+                                                                                               nb, below, Lp);
+            lu_split_cols_kernel<LU_NB><<<(unsigned)ceil_div(k, 32), 256, 0, st>>>(X32, k, r0, 0, nb, k, Xp);
             launches += 2;
             if ((e = gemm_bf16_sub(Lp, LU_K6, Xp, LU_K6, below, k, LU_K6, X32 + (r0 + nb) * k, k, st))) return e;
         }
@@ -612,8 +661,9 @@ int mbem_lu_solve_many_f32(const float* LU, int64_t lda, int64_t n, const int32_
         lu_block_trsm_kernel<<<(unsigned)ceil_div(k, 128), 128, 0, st>>>(LU, lda, X32, k, k, r0, nb, 0);
         launches++;
         if (r0 > 0) {
-            lu_split_rows_kernel<<<(unsigned)ceil_div(r0 * LU_NB, 256), 256, 0, st>>>(LU, lda, 0, r0, nb, r0, Lp);
-            lu_split_cols_kernel<<<(unsigned)ceil_div(k, 32), 256, 0, st>>>(X32, k, r0, 0, nb, k, Xp);
+            lu_split_rows_kernel<LU_NB><<<(unsigned)ceil_div(r0 * LU_NB, 256), 256, 0, st>>>(LU, lda, 0, r0, nb, r0,
+                                                                                            Lp);
+            lu_split_cols_kernel<LU_NB><<<(unsigned)ceil_div(k, 32), 256, 0, st>>>(X32, k, r0, 0, nb, k, Xp);
             launches += 2;
             if ((e = gemm_bf16_sub(Lp, LU_K6, Xp, LU_K6, r0, k, LU_K6, X32, k, st))) return e;
         }

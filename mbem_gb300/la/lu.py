@@ -191,6 +191,6 @@ def factor(A: torch.Tensor, matvec=None) -> Factor:
 def phase_stats(timing: bool = False) -> dict:
     """Device ms of the factorisations' phases since the last call; switches
     the phase timing of later factorisations on or off."""
-    arr = (ctypes.c_double * 5)()
+    arr = (ctypes.c_double * 3)()
     nat.lib().mbem_lu_stats(int(timing), arr)
-    return dict(zip(("panel", "interchanges", "trsm", "split", "update"), list(arr)))
+    return dict(zip(("panels", "block_rows", "update"), list(arr)))
