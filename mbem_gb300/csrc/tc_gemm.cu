@@ -65,12 +65,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// SUB: Y[M x N] -= A B^T over column tiles of BN (blockIdx.y = the tile,
-// n_cols = N, the whole of K in each CTA); else Y (or its slice of the K
+// SUB: Y[M x N] -= A B^T over 128 x BN tiles (a grid of row tiles x column
+// tiles, visited in row-tile groups; n_cols = N, the whole of K in each CTA); else Y (or its slice of the K
 // split blockIdx.y) = A B^T for n_cols <= BN columns.
 // ring stages: the update (short K, two CTAs an SM) keeps two
 template <bool SUB>
 constexpr int tc_stages() { return SUB ? 2 : TC_STAGES; }
+// row tiles in one raster group of the update (16 x 128 rows of A with the
+// column tiles of 304 resident CTAs: about 20 MB of operands at K = 1,536)
+constexpr int TC_GROUP_M = 16;
 
 template <int BN, bool TRANS, bool SUB = false>
 __global__ void __launch_bounds__(TC_THREADS, SUB ? 2 : 1)
@@ -89,13 +92,27 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
 
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t m0 = (int64_t)blockIdx.x * TC_BM;
+    // SUB: the (row tile, column tile) of this CTA in groups of
+    // TC_GROUP_M row tiles, column-major within a group, so the CTAs
+    // resident at one time share a few operand row panels in L2 instead of
+    // each column tile streaming all of A
+    int64_t mt = blockIdx.x, nt = blockIdx.y;
+    if (SUB) {
+        const int64_t lin = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
+        const int64_t per_group = (int64_t)TC_GROUP_M * gridDim.y;
+        const int64_t first = lin / per_group * TC_GROUP_M;
+        const int64_t gsize = min((int64_t)TC_GROUP_M, (int64_t)gridDim.x - first);
+        const int64_t local = lin % per_group;
+        mt = first + local % gsize;
+        nt = local / gsize;
+    }
+    const int64_t m0 = mt * TC_BM;
     // this CTA's share of K (a split of K over blockIdx.y; its partial sum
     // goes to slice blockIdx.y of Y)
     const int kb_all = (int)((K + TC_BK - 1) / TC_BK);
     const int kb_first = SUB ? 0 : (int)blockIdx.y * kb_per;
     const int kb_total = SUB ? kb_all : min(kb_per, kb_all - kb_first);
-    const int n0 = SUB ? (int)blockIdx.y * BN : 0;
+    const int n0 = SUB ? (int)nt * BN : 0;
     if (SUB) {
         Y += n0;
         n_cols = min(BN, n_cols - n0);
