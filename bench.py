@@ -740,9 +740,80 @@ def dense_lu_workload(n_face=35):
     return out
 
 
+def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024):
+    """The volume sampler on the cube 24 x 24 per face with the 16 x 16
+    fault, solved (mixed, 1e-8): a grid of (n_grid + 2 pad_cells)^3 points
+    half a cell off every face (some outside the body); region codes
+    (solid-angle closure over the 6,912 cube triangles plus the on-patch
+    distance test), the clearances (distances to the cube and the fault),
+    and the sampled displacement, elastic stress, strain, eigenstress and
+    scalars, with the stress from the mixed and from the FP64 readout. The
+    oracle's classification of n_cpu points on the host cores beside it."""
+    import torch
+    from mbem_gb300 import volume as V
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.geometry import MeshGeometry
+    from mbem_gb300.model import generate_system
+    from oracle import geometry_oracle as go
+    model, eps = cube_fault_model(n_face, n_fault)
+    asm = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, precision="mixed",
+                       precond="bf16_inner").assemble(generate_system(model), eps)
+    sol = asm.solve()
+    del asm
+    torch.cuda.empty_cache()
+    h = 4.0 / n_grid
+    grid = V.make_grid(model, h, pad=pad_cells * h)
+    n = grid.points.shape[0]
+    cube = model.regions[0].patches[0]
+    # warm-up on a small grid
+    small = V.make_grid(model, 0.5)
+    V.sample(model, sol, eps, small, V.classify(model, small), precision="mixed")
+    code, t_cls = _sync_time(lambda: V.classify(model, grid))
+    (c_h, c_eps, c_f), t_clr = _sync_time(lambda: V.clearance(model, grid, eps))
+    f_mixed, t_mixed = _sync_time(lambda: V.sample(model, sol, eps, grid, code, precision="mixed"))
+    f_fp64, t_fp64 = _sync_time(lambda: V.sample(model, sol, eps, grid, code))
+    inside = code > 0
+    diff = float(np.abs(f_mixed["sigma"][inside] - f_fp64["sigma"][inside]).max()
+                 / np.abs(f_fp64["sigma"][inside]).max())
+    # the two geometry kernels alone (CUDA events on the launching stream)
+    pts = torch.from_numpy(grid.points).cuda()
+    geo = MeshGeometry(cube.mesh)
+    pairs = n * geo.n_tri
+    kt = {}
+    for name, fn in (("solid_angle_kernel", lambda: geo.solid_angle(pts)),
+                     ("mesh_distance_kernel", lambda: geo.distance(pts))):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 3
+        kt[name] = {"ms": ms, "point_triangle_pairs_per_s": pairs / (ms * 1e-3)}
+    # the oracle's classification on a bounded sample of the grid
+    sel = np.random.default_rng(0).choice(n, size=min(n_cpu, n), replace=False)
+    t0 = time.perf_counter()
+    cpu_code = go.classify([[(cube.tri_verts(), 1.0)]], grid.points[sel])
+    t_cpu = time.perf_counter() - t0
+    return {"config": {"n_face": n_face, "n_fault": n_fault, "grid": list(grid.dims), "points": n,
+                       "points_inside": int(inside.sum()), "cube_triangles": geo.n_tri,
+                       "fault_triangles": model.regions[0].faults[0].mesh.n_triangles},
+            "classify_s": t_cls, "clearance_s": t_clr, "sample_mixed_s": t_mixed, "sample_fp64_s": t_fp64,
+            "points_per_s_mixed": n / (t_cls + t_clr + t_mixed),
+            "max_rel_diff_stress_mixed_vs_fp64": diff,
+            "geometry_kernels": kt,
+            "cpu_oracle_classify": {"points": int(sel.size), "s": t_cpu, "points_per_s": sel.size / t_cpu,
+                                    "threads": 1, "kind": "port (numpy)",
+                                    "agrees_with_gpu": bool(np.array_equal(cpu_code, code[sel]))}}
+
+
 def extra_workloads(args, peaks):
     out = {}
-    for name, fn in (("multi_rhs_cube24_256", lambda: multi_rhs_workload(peaks)),
+    for name, fn in (("volume_cube24_grid66", volume_workload),
+                     ("multi_rhs_cube24_256", lambda: multi_rhs_workload(peaks)),
                      ("multi_mesh_64_cubes", lambda: multi_mesh_workload(peaks)),
                      ("p1_variant_cube24", p1_variant_workload),
                      ("dense_lu_cube35", dense_lu_workload),

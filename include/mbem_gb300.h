@@ -617,6 +617,28 @@ int mbem_project_translation(const double* v_in, double* v_out, int64_t n,
                              const int64_t* u_ranges, int n_u_ranges, double* work,
                              void* stream);
 
+/* ---- Mesh geometry for a batch of points (the volume sampler) -----------
+ * Replaces src/mbem/geometry.py:8-57 (solid_angle_batch, the
+ * _solid_angle_rows kernel behind RegionModel.point_in_region,
+ * src/mbem/model/core.py:994-1025) and src/mbem/geometry.py:60-105
+ * (point_triangle_distance, distance_to_mesh). tri_verts: (n_tri, 3, 3)
+ * FP64; points: (n_pts, 3) FP64; records: mbem_geom_record_bytes(n_tri)
+ * bytes of 16-byte aligned device memory that mbem_geom_prepare fills once
+ * per mesh. Far pairs run in FP32 on hi/lo split coordinates, near pairs
+ * (within 4 circumradii) in FP64; the solid-angle sum is within ~1e-6 sr
+ * of the FP64 sum. ------------------------------------------------------ */
+size_t mbem_geom_record_bytes(int64_t n_tri);
+int mbem_geom_prepare(const double* tri_verts, int64_t n_tri, float* records, void* stream);
+/* total[i] (+)= weight * sum_t Omega_t(points[i]) (accumulate 0: =). */
+int mbem_solid_angle_sum(const float* records, const double* tri_verts, int64_t n_tri, const double* points,
+                         int64_t n_pts, double weight, int accumulate, double* total, void* stream);
+/* dist[i], idx[i]: the exact distance from points[i] to the nearest triangle
+ * and its index, over every triangle of the mesh (ties: nearer centroid,
+ * then lower index). max_edge: the mesh's longest edge (sets the FP32
+ * candidate margin). n_tri >= 1. */
+int mbem_mesh_distance(const float* records, const double* tri_verts, int64_t n_tri, const double* points,
+                       int64_t n_pts, double max_edge, double* dist, int64_t* idx, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

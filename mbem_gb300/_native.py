@@ -143,6 +143,10 @@ _SIGNATURES = {
     "mbem_batch_residual_workspace_size": (c_size_t, [_I, _I]),
     "mbem_batch_residual_mixed": (c_int, [POINTER(MixedOperator), _P, _P, _I, _P, _P, c_size_t, _P]),
     "mbem_readout_record_bytes": (c_size_t, [_I]),
+    "mbem_geom_record_bytes": (c_size_t, [_I]),
+    "mbem_geom_prepare": (c_int, [_P, _I, _P, _P]),
+    "mbem_solid_angle_sum": (c_int, [_P, _P, _I, _P, _I, _D, c_int, _P, _P]),
+    "mbem_mesh_distance": (c_int, [_P, _P, _I, _P, _I, _D, _P, _P, _P]),
     "mbem_readout_prepare": (c_int, [_P, _I, _P, _P, _P, _I, _P, c_int, _D, _P, _P, _P, POINTER(c_int64), _P]),
     "mbem_readout_evaluate": (c_int, [_P, _I, _P, _P, _P, _I, _P, _D, _D, c_int, _P, _P, _I, _P, _P, _P, _D, c_int,
                                       _P, _P]),

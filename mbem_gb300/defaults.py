@@ -23,6 +23,10 @@ HALF_JUMP_MAX_EPS_OVER_H = 0.5
 EIGEN_NEAR_RADIUS_EPS = 20.0
 NEAR_BOUNDARY_H_RATIO = 0.5
 
+# ---- volume sampler (defaults.py:833) ----
+VOLUME_CHUNK = 50_000                 # the reference's chunk (host memory bound)
+VOLUME_CHUNK_DEVICE = 1 << 18         # points a readout launch takes here (~100 MB of device state)
+
 # ---- nodal kernels (defaults.py:916-932) ----
 NODAL_D_STAR = 10.0
 NODAL_FAR_GAUSS_N = 12

@@ -18,6 +18,9 @@ lu        the FP32 GPU LU of an 8,192 x 8,192 matrix (lu_panel_kernel, the
           tensor-core trailing update) and one refined solve
 learned   FAULT_TRACTION cube 16 x 16, fault 12 x 12: the learned two-level
           preconditioner's setup and its FGMRES solve
+volume    the volume sampler's geometry on cube 24 (6,912 triangles): region
+          codes and clearances of a 40^3 grid (solid_angle_kernel,
+          mesh_distance_kernel)
 """
 
 from __future__ import annotations
@@ -121,6 +124,12 @@ def run(which: str) -> None:
         A = (torch.randn(n, n, generator=g, dtype=torch.float64)
              + n ** 0.5 * torch.eye(n, dtype=torch.float64)).cuda()
         Factor(A).solve(torch.ones(n, dtype=torch.float64, device="cuda"))
+    elif which == "volume":
+        from . import volume as V
+        model, eps = cube_fault_model(24, 16)
+        grid = V.make_grid(model, 4.0 / 40)
+        V.classify(model, grid)
+        V.clearance(model, grid, eps)
     else:
         raise SystemExit(f"unknown case {which!r}")
     torch.cuda.synchronize()

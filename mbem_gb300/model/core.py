@@ -237,6 +237,9 @@ def solid_angle_sum(mesh, x) -> float:
 _CLOSED_THRESHOLD = 2.0 * np.pi
 _OPEN_FLOOR = 1e-3
 _CLOSURE_TOL = 1e-6
+# a point this close to a patch, in units of the nearest element's mean
+# edge, lies ON it (core.py:89)
+_ON_PATCH_TOL = 1e-9
 
 
 class RegionModel:
@@ -313,6 +316,33 @@ class RegionModel:
 
     def buoyancy(self, region, patch):
         return None
+
+    def point_in_region(self, region, points, closure: bool = False):
+        """Which of ``points`` lie strictly inside ``region``: ``(N,) bool``
+        (core.py:994-1025). The Gauss closure identity read as a classifier,
+        sum_p sigma(R, p) Omega_p(x) = 4 pi iff x is inside R, within
+        _CLOSURE_TOL x 4 pi; the solid angles are summed on the GPU.
+        ``closure=True`` also returns the sum. A full-space region holds every
+        point. Numpy in, numpy out; torch in, CUDA tensors out."""
+        import torch
+
+        from .._device import as_cuda, is_torch, out_like
+        from ..geometry import MeshGeometry
+
+        region = region if not isinstance(region, str) else next(r for r in self.regions if r.name == region)
+        torch_in = is_torch(points)
+        pts = as_cuda(points).reshape(-1, 3)
+        if region.is_full_space:
+            total = torch.full((pts.shape[0],), 4.0 * np.pi, dtype=torch.float64, device=pts.device)
+        else:
+            total = torch.zeros(pts.shape[0], dtype=torch.float64, device=pts.device)
+            for p in region.patches:
+                MeshGeometry(p.mesh).solid_angle(pts, float(self._sigma[(region.name, p.name)]), out=total,
+                                                 accumulate=True)
+        inside = (total - 4.0 * np.pi).abs() <= _CLOSURE_TOL * 4.0 * np.pi
+        if closure:
+            return out_like(inside, torch_in), out_like(total, torch_in)
+        return out_like(inside, torch_in)
 
     def is_anchored(self) -> bool:
         return any(p.bc is BCType.PRESCRIBED_DISPLACEMENT for r in self.regions for p in r.patches)

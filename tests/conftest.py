@@ -50,6 +50,11 @@ def traction_small():
 
 
 @pytest.fixture(scope="session")
+def volume_small():
+    return load_golden("volume_small")
+
+
+@pytest.fixture(scope="session")
 def oracle():
     from oracle import oracle as orc
     orc.lib()

@@ -283,9 +283,60 @@ def make_traction_small(path):
                         drop=drop, A=asm.A, b=asm.b, x_u=sol["u:cube"], x_b=sol["b:fault"])
 
 
+def make_volume_small(path):
+    """The volume sampler on the small cube + fault system (3 x 3 per face,
+    fault 2 x 2, eps = h/2): a padded grid with points outside the body, its
+    region codes, clearances and sampled fields; a section grid; and, on
+    scattered points (some on a face, some just off one), the closure sums
+    of point_in_region, the exact distances to both meshes and on_patch."""
+    from mbem import volume
+    from mbem.backends.dense import AssembledDense
+    from mbem.geometry import distance_to_mesh
+    from mbem.model.equations import generate_system
+
+    t0 = time.time()
+    model, cube, fmesh = reference_cube_model(3, 2, 1.0, 1.0)
+    eps = (4.0 / 3) / 2.0
+    asm = AssembledDense(generate_system(model), eps, "direct", jump="calibrated", deflate=True)
+    sol = asm.solve()
+    region = model.regions[0]
+    grid = volume.make_grid(model, 1.0, pad=1.0)
+    section = volume.section_grid(model, "y", 0.1, 0.5)
+    code = volume.classify(model, grid)
+    c_h, c_eps, c_fault = volume.clearance(model, grid, eps)
+    fields = volume.sample(model, sol, eps, grid, code, eigenstress=True)
+    half = {k: 0.5 * fields[k] for k in volume.PRIMARY}
+    diff = volume.difference(fields, half, code > 0)
+    vti = volume.as_vti_arrays(grid, fields, code, c_h, c_eps, c_fault)
+    rng = np.random.default_rng(11)
+    sc = rng.uniform(-3.0, 3.0, size=(48, 3))
+    near = np.array([[2.0 - 1e-3, 0.3, 0.2], [2.0 + 1e-3, 0.3, 0.2], [0.1, -2.0 + 1e-6, 0.4],
+                     [0.2, 0.3, 1.999999], [1.9, 1.95, -1.97], [0.0, 1e-3, 0.0], [0.3, -0.05, 0.45]])
+    on_face = np.array([[2.0, 0.3, 0.1], [-0.7, -2.0, 1.2], [0.5, 0.25, 2.0], [2.0, 2.0, 0.4]])
+    sc_pts = np.concatenate([sc, near])
+    inside, total = model.point_in_region(region, sc_pts, closure=True)
+    all_pts = np.concatenate([sc_pts, on_face])
+    d_cube, i_cube = distance_to_mesh(all_pts, cube)
+    d_fault, i_fault = distance_to_mesh(all_pts, fmesh)
+    onp = volume.on_patch(all_pts, region.patches[0])
+    out = dict(cube_vertices=cube.vertices, cube_triangles=cube.triangles,
+               fault_vertices=fmesh.vertices, fault_triangles=fmesh.triangles, eps=eps,
+               x=sol["u:cube"], grid_points=grid.points, grid_origin=np.array(grid.origin),
+               grid_dims=np.array(grid.dims), section_points=section.points,
+               section_origin=np.array(section.origin), section_dims=np.array(section.dims),
+               code=code, c_h=c_h, c_eps=c_eps, c_fault=c_fault,
+               sc_points=sc_pts, sc_inside=inside, sc_total=total, all_points=all_pts,
+               d_cube=d_cube, i_cube=i_cube, d_fault=d_fault, i_fault=i_fault, on_patch=onp,
+               vti_keys=np.array(sorted(vti)), vti_sigma_xy=vti["sigma_xy"], vti_u=vti["u"])
+    out.update({f"f_{k}": v for k, v in fields.items()})
+    out.update({f"d_{k}": v for k, v in diff.items()})
+    np.savez_compressed(path, **out)
+    print(f"volume_small: {time.time() - t0:.1f} s", flush=True)
+
+
 CASES = {"p0_pairs": make_p0_pairs, "cube_small": make_cube_small,
          "c1_rows": make_c1_rows, "nodal_pairs": make_nodal_pairs,
-         "traction_small": make_traction_small}
+         "traction_small": make_traction_small, "volume_small": make_volume_small}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(CASES)

@@ -52,3 +52,16 @@ def test_multi_mesh_layout_rules():
     assert lib.mbem_mm_total(meshes([301], [0]), 1) == -1                        # not a multiple of 3
     assert lib.mbem_mm_workspace_size(meshes(sizes, offs), 3, _native.MM_MAX_RESTART + 1) == 0
     assert ctypes.sizeof(_native.MmMesh) == 88
+
+
+def test_geometry_entry_points_check_their_arguments():
+    """Host-side checks of the mesh-geometry entry points (no kernel runs:
+    each call is refused, or has no points, before any launch)."""
+    lib = _native.lib()
+    assert lib.mbem_geom_record_bytes(10) == 10 * 32 * 4
+    assert lib.mbem_geom_record_bytes(0) == 0
+    fake = 4096                       # never dereferenced
+    assert lib.mbem_mesh_distance(fake, fake, 0, fake, 5, 1.0, fake, fake, None) == _native.ERR_ARG
+    assert lib.mbem_mesh_distance(fake + 4, fake, 3, fake, 5, 1.0, fake, fake, None) == _native.ERR_ARG
+    assert lib.mbem_solid_angle_sum(fake, fake, 3, fake, 0, 1.0, 0, fake, None) == _native.OK
+    assert lib.mbem_geom_prepare(None, 3, fake, None) == _native.ERR_ARG
