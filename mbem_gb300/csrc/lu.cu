@@ -250,8 +250,12 @@ __global__ void lu_swap_kernel(float* __restrict__ A, int64_t lda, int64_t n, in
 // product of two such is taken over the six pieces pairs of order <= 2
 // (hi.hi, hi.mid, hi.lo, mid.hi, mid.mid, lo.hi), the dropped ones below
 // 2^-24 relative: FP32 accuracy with FP32 accumulation in TMEM.
-// The operands: L21 rows as [hi hi hi mid mid lo], U12 columns as
-// [hi mid lo hi mid hi], 6 x 64 = LU_K6 BF16 each.
+// The operands: L21 rows as [lo hi mid mid hi hi], U12 columns as
+// [hi lo mid hi mid hi], 6 x W BF16 each: along K the products run from the
+// smallest (lo.hi, hi.lo, mid.mid ~2^-16) through mid.hi, hi.mid (~2^-8)
+// to hi.hi, so the accumulator is small while the corrections are added and
+// the rounding of each accumulation step, relative to the running sum,
+// falls mostly on the last W terms.
 constexpr int LU_K6 = 6 * LU_NB;
 
 __device__ __forceinline__ void bf16_pieces(float x, uint16_t& hi, uint16_t& mid, uint16_t& lo) {
@@ -278,7 +282,7 @@ __global__ void lu_split_rows_kernel(const float* __restrict__ A, int64_t lda, i
     uint16_t h, m, l;
     bf16_pieces(x, h, m, l);
     uint16_t* o = Ls + r * (6 * W) + kk;
-    o[0] = h; o[W] = h; o[2 * W] = h; o[3 * W] = m; o[4 * W] = m; o[5 * W] = l;
+    o[0] = l; o[W] = h; o[2 * W] = m; o[3 * W] = m; o[4 * W] = h; o[5 * W] = h;
 }
 
 // Us[j][6 x W]: the pieces of column col0 + j (j < N) of rows row0 ..
@@ -302,7 +306,7 @@ lu_split_cols_kernel(const float* __restrict__ A, int64_t lda, int64_t row0, int
         uint16_t h, m, l;
         bf16_pieces(T[kk][j], h, m, l);
         uint16_t* o = Us + (j0 + j) * (6 * W) + kk;
-        o[0] = h; o[W] = m; o[2 * W] = l; o[3 * W] = h; o[4 * W] = m; o[5 * W] = h;
+        o[0] = h; o[W] = l; o[2 * W] = m; o[3 * W] = h; o[4 * W] = m; o[5 * W] = h;
     }
 }
 
