@@ -11,10 +11,11 @@
 // hi + lo floats, so a - p is formed to ~1e-7 of |a - p| whatever the
 // coordinates' magnitude, with the triple product taken against the
 // triangle's own 2A n (a . (b x c) = a . ((b - a) x (c - a))); nearer pairs
-// run the reference's FP64 arithmetic. The FP64 pipe of this part is a
-// thirtieth of its FP32 pipe, and almost every pair of a volume grid is far.
+// run the reference's FP64 arithmetic. The FP64 rate of this part is about a
+// sixtieth of its FP32 rate, and almost every pair of a volume grid is far.
 //
-// Solid angle: FP32 far terms summed four at a time into an FP64 total.
+// Solid angle: the FP32 far terms of a tile of 128 triangles in a
+// compensated (Kahan) FP32 sum, added to an FP64 total once a tile.
 // Error analysis: each far term carries ~1e-7 x 2A/D^2 from a - p and 2 ulp
 // from atan2f; over a closed surface the sum is within ~1e-6 steradian of
 // the FP64 sum (the classifier's band is 1e-6 x 4 pi = 1.26e-5).
@@ -37,7 +38,10 @@ namespace {
 
 constexpr int GEOM_THREADS = 128;     // observers a CTA and records a tile
 constexpr int GEOM_REC = 32;          // floats a record
-constexpr float GEOM_NEAR_K = 4.0f;   // FP64 inside this many circumradii
+// FP64 inside this many circumradii: beyond, every vertex is at least one
+// circumradius away and the triangle subtends under 60 degrees, so the
+// van Oosterom denominator is a sum of positive terms (no cancellation)
+constexpr float GEOM_NEAR_K = 2.0f;
 
 // record: [0..8] vertex hi (a b c), [9..17] vertex lo, [18..20] b - a,
 // [21..23] c - a, [24..26] (b - a) x (c - a), [27..29] centroid (hi),
@@ -129,8 +133,8 @@ __global__ void __launch_bounds__(GEOM_THREADS) solid_angle_kernel(const float* 
         __syncthreads();
         const int cnt = (int)lmin(GEOM_THREADS, nt - t0);
         if (!live) continue;
+        float part = 0.0f, comp = 0.0f;      // Kahan sum of the tile's far terms
         for (int j0 = 0; j0 < cnt; j0 += 4) {
-            float part = 0.0f;
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 const int j = j0 + u;
@@ -153,10 +157,13 @@ __global__ void __launch_bounds__(GEOM_THREADS) solid_angle_kernel(const float* 
                 const float numer = ax * r[24] + ay * r[25] + az * r[26];
                 const float denom = ra * rb * rc + rc * (ax * bx + ay * by + az * bz) +
                                     ra * (bx * cx + by * cy + bz * cz) + rb * (ax * cx + ay * cy + az * cz);
-                part += 2.0f * atan2f(numer, denom);
+                const float y = 2.0f * atan2f(numer, denom) - comp;
+                const float t = part + y;
+                comp = (t - part) - y;
+                part = t;
             }
-            sum += (double)part;
         }
+        sum += (double)part - (double)comp;
     }
     if (live) total[i] = (accumulate ? total[i] : 0.0) + weight * sum;
 }
