@@ -2,7 +2,7 @@
 bookkeeping (TEST INFRASTRUCTURE, not the product).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py``
-use this module, as the checker. It follows, step by step:
+use this module, to check the CUDA path. It follows, step by step:
 
 - ``solid_angle_sum``: the van Oosterom signed solid angle summed over a
   mesh (src/mbem/geometry.py:8-47), chunked over the points;

@@ -1,7 +1,7 @@
 """ctypes front end of the C oracle (TEST INFRASTRUCTURE, not the product).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py``
-use this module, as the checker or the timed CPU baseline. It restates the
+use this module, to check the CUDA path or as the timed CPU baseline. It restates the
 reference's P0 kernels (``src/mbem/kernels/tri_kernels.py``) in plain C with
 OpenMP (``p0_oracle.c``); ``tests/test_oracle.py`` pins it to golden vectors
 that the reference itself produced (``tests/golden/``).

@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the P0 mollified-triangle kernels (TEST INFRASTRUCTURE).
  *
- * This file is the checker, not the product: only tests/, the smoke check of
+ * This file checks the CUDA path and is not the product: only tests/, the smoke check of
  * __graft_entry__ and the cpu_baseline / reference leg of bench.py load it.
  * It restates, in plain C with OpenMP, the algorithm of the reference's
  * numba kernels in src/mbem/kernels/tri_kernels.py, function by function and

@@ -2,7 +2,7 @@
 
 The oracle restates the reference's P0 kernels (tri_kernels.py) in C; these
 tests pin it to the reference's own outputs (tests/golden/, made by
-make_golden.py), entry by entry, before it is trusted as the checker of the
+make_golden.py), entry by entry, before it is trusted to check the
 CUDA path at sizes the reference cannot reach here.
 """
 
