@@ -747,7 +747,8 @@ def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024):
     (solid-angle closure over the 6,912 cube triangles plus the on-patch
     distance test), the clearances (distances to the cube and the fault),
     and the sampled displacement, elastic stress, strain, eigenstress and
-    scalars, with the stress from the mixed and from the FP64 readout. The
+    scalars, with the stress and displacement from the mixed and from the
+    FP64 readouts. The
     oracle's classification of n_cpu points on the host cores beside it."""
     import torch
     from mbem_gb300 import volume as V
@@ -776,6 +777,7 @@ def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024):
     inside = code > 0
     diff = float(np.abs(f_mixed["sigma"][inside] - f_fp64["sigma"][inside]).max()
                  / np.abs(f_fp64["sigma"][inside]).max())
+    diff_u = float(np.abs(f_mixed["u"][inside] - f_fp64["u"][inside]).max() / np.abs(f_fp64["u"][inside]).max())
     # the two geometry kernels alone (CUDA events on the launching stream)
     pts = torch.from_numpy(grid.points).cuda()
     geo = MeshGeometry(cube.mesh)
@@ -803,7 +805,7 @@ def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024):
                        "fault_triangles": model.regions[0].faults[0].mesh.n_triangles},
             "classify_s": t_cls, "clearance_s": t_clr, "sample_mixed_s": t_mixed, "sample_fp64_s": t_fp64,
             "points_per_s_mixed": n / (t_cls + t_clr + t_mixed),
-            "max_rel_diff_stress_mixed_vs_fp64": diff,
+            "max_rel_diff_stress_mixed_vs_fp64": diff, "max_rel_diff_u_mixed_vs_fp64": diff_u,
             "geometry_kernels": kt,
             "cpu_oracle_classify": {"points": int(sel.size), "s": t_cpu, "points_per_s": sel.size / t_cpu,
                                     "threads": 1, "kind": "port (numpy)",

@@ -617,6 +617,16 @@ int mbem_project_translation(const double* v_in, double* v_out, int64_t n,
                              const int64_t* u_ranges, int n_u_ranges, double* work,
                              void* stream);
 
+/* Mixed-precision displacement of a P0 slip density at many observers
+ * (tri_nodal.py:1310-1319 t_disp_contract at order 0; evaluate.py:194-250):
+ * out[f] (+)= alpha sum_s T(x_f, s) d_s. Far pairs by the FP32 quadrature of
+ * the mixed operator's far field, near pairs (centroid distance below
+ * near_factor max(eps, h) or 1.5 L) by the FP64 closed form. coeffs: the six
+ * t_coeffs (host). Within ~1e-6 of the FP64 contraction. */
+int mbem_t_disp_readout(const double* x, int64_t n_obs, const double* tri_verts, const double* normals,
+                        const double* eps, int64_t n_src, const double* density, const double* coeffs,
+                        double near_factor, double alpha, int accumulate, double* out, void* stream);
+
 /* ---- Mesh geometry for a batch of points (the volume sampler) -----------
  * Replaces src/mbem/geometry.py:8-57 (solid_angle_batch, the
  * _solid_angle_rows kernel behind RegionModel.point_in_region,

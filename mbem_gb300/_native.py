@@ -143,6 +143,7 @@ _SIGNATURES = {
     "mbem_batch_residual_workspace_size": (c_size_t, [_I, _I]),
     "mbem_batch_residual_mixed": (c_int, [POINTER(MixedOperator), _P, _P, _I, _P, _P, c_size_t, _P]),
     "mbem_readout_record_bytes": (c_size_t, [_I]),
+    "mbem_t_disp_readout": (c_int, [_P, _I, _P, _P, _P, _I, _P, _P, _D, _D, c_int, _P, _P]),
     "mbem_geom_record_bytes": (c_size_t, [_I]),
     "mbem_geom_prepare": (c_int, [_P, _I, _P, _P]),
     "mbem_solid_angle_sum": (c_int, [_P, _P, _I, _P, _I, _D, c_int, _P, _P]),

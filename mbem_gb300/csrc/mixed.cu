@@ -1295,6 +1295,106 @@ int bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_col
     return launch_status("bf16_matvec", 2 + n_near);
 }
 
+// ---------------------------------------------------------------------------
+// Mixed P0 displacement readout: out[f] (+)= alpha sum_s T(x_f, s) d_s for a
+// slip density d (tri_nodal.py:1310-1319 at order 0). Far pairs by the FP32
+// quadrature of the mixed operator (far_block<true>: the T block of the
+// mollified point kernel, <= ~1.5e-7 of the closed form by the D / L rule),
+// contracted with the density in FP32 and summed over a tile of sources in
+// FP32, over tiles in FP64; near pairs (is_near, the operator's own test)
+// by the FP64 closed form of p0_pair.cuh, inline. One thread an observer,
+// DR_TILE sources staged in shared memory at a time.
+// ---------------------------------------------------------------------------
+constexpr int DR_THREADS = 128, DR_TILE = 32;
+
+struct DispReadoutArgs {
+    const double* x;
+    int64_t n_obs;
+    const double* tri_verts;
+    const double* normals;
+    const double* eps;
+    const double* density;
+    int64_t n_src;
+    double c[6];
+    float cf[6];
+    double near_factor;
+    double alpha;
+    int accumulate;
+    double* out;
+};
+
+struct DrSrc {
+    SrcFar f;
+    float d[3];
+    int live;        // non-degenerate, non-zero density
+};
+
+__global__ void __launch_bounds__(DR_THREADS) disp_readout_kernel(DispReadoutArgs a, QuadRules Q) {
+    __shared__ DrSrc tile[DR_TILE];
+    const int64_t i = (int64_t)blockIdx.x * DR_THREADS + threadIdx.x;
+    const bool live = i < a.n_obs;
+    double ox = 0.0, oy = 0.0, oz = 0.0;
+    if (live) {
+        ox = a.x[3 * i];
+        oy = a.x[3 * i + 1];
+        oz = a.x[3 * i + 2];
+    }
+    const F2 xo[3] = {split_d(ox), split_d(oy), split_d(oz)};
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int64_t s0 = 0; s0 < a.n_src; s0 += DR_TILE) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < DR_TILE; t += DR_THREADS) {
+            const int64_t s = s0 + t;
+            DrSrc& S = tile[t];
+            if (s < a.n_src) {
+                far_setup(a.tri_verts + 9 * s, a.normals + 3 * s, a.eps[s], a.near_factor, S.f);
+                const double* d = a.density + 3 * s;
+                S.d[0] = (float)d[0];
+                S.d[1] = (float)d[1];
+                S.d[2] = (float)d[2];
+                S.live = S.f.ok && !(d[0] == 0.0 && d[1] == 0.0 && d[2] == 0.0);
+            } else {
+                S.live = 0;
+            }
+        }
+        __syncthreads();
+        if (!live) continue;
+        const int ns = (int)lmin(DR_TILE, a.n_src - s0);
+        float part[3] = {0.0f, 0.0f, 0.0f};
+        for (int t = 0; t < ns; t++) {
+            const DrSrc& S = tile[t];
+            if (!S.live) continue;
+            float dc[3], D2;
+            if (is_near(xo, S.f, dc, D2)) {
+                const int64_t s = s0 + t;
+                SrcP0 g;
+                src_setup(a.tri_verts + 9 * s, a.eps[s], g);
+                if (!g.ok) continue;
+                PairP0 p;
+                pair_setup(g, ox, oy, oz, p);
+                TMoments m;
+                const double* n = a.normals + 3 * s;
+                t_moments(g, n, p, m);
+                double blk[3][3];
+                t_block(m, n, a.c, g.eps2, blk);
+                const double* d = a.density + 3 * s;
+#pragma unroll
+                for (int r = 0; r < 3; r++) acc[r] += blk[r][0] * d[0] + blk[r][1] * d[1] + blk[r][2] * d[2];
+            } else {
+                float blk[3][3];
+                far_block<true>(Q, S.f, dc, D2, a.cf, blk);
+#pragma unroll
+                for (int r = 0; r < 3; r++) part[r] += blk[r][0] * S.d[0] + blk[r][1] * S.d[1] + blk[r][2] * S.d[2];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 3; r++) acc[r] += (double)part[r];
+    }
+    if (!live) return;
+#pragma unroll
+    for (int r = 0; r < 3; r++) a.out[3 * i + r] = (a.accumulate ? a.out[3 * i + r] : 0.0) + a.alpha * acc[r];
+}
+
 }  // namespace mbem
 
 using namespace mbem;
@@ -1468,6 +1568,34 @@ int mbem_bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t 
     MBEM_REQUIRE(work && work_bytes >= (size_t)n_cols * sizeof(float), MBEM_ERR_SIZE,
                  "BF16 matvec workspace too small (needs %lld bytes)", (long long)(n_cols * sizeof(float)));
     return bf16_matvec(A16, ld16, n_rows, n_cols, n_near, near, x, y, (float*)work, (cudaStream_t)stream);
+}
+
+int mbem_t_disp_readout(const double* x, int64_t n_obs, const double* tri_verts, const double* normals,
+                        const double* eps, int64_t n_src, const double* density, const double* coeffs,
+                        double near_factor, double alpha, int accumulate, double* out, void* stream) {
+    MBEM_REQUIRE(n_obs >= 0 && n_src >= 0 && near_factor > 0.0 && coeffs, MBEM_ERR_ARG, "bad readout sizes");
+    MBEM_REQUIRE((n_obs == 0 || (x && out)) && (n_src == 0 || (tri_verts && normals && eps && density)),
+                 MBEM_ERR_ARG, "NULL readout arrays");
+    if (n_obs == 0) return MBEM_OK;
+    MBEM_REQUIRE(ceil_div(n_obs, DR_THREADS) < (int64_t)INT32_MAX, MBEM_ERR_SIZE, "too many observers");
+    DispReadoutArgs a;
+    a.x = x;
+    a.n_obs = n_obs;
+    a.tri_verts = tri_verts;
+    a.normals = normals;
+    a.eps = eps;
+    a.density = density;
+    a.n_src = n_src;
+    for (int k = 0; k < 6; k++) {
+        a.c[k] = coeffs[k];
+        a.cf[k] = (float)coeffs[k];
+    }
+    a.near_factor = near_factor;
+    a.alpha = alpha;
+    a.accumulate = accumulate;
+    a.out = out;
+    disp_readout_kernel<<<(unsigned)ceil_div(n_obs, DR_THREADS), DR_THREADS, 0, (cudaStream_t)stream>>>(a, rules());
+    return launch_status("disp_readout_kernel");
 }
 
 int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, void* work, size_t work_bytes,

@@ -137,10 +137,16 @@ def evaluate_stress(model: RegionModel, region, solution: dict, points, eps,
 
 
 def evaluate_displacement(model: RegionModel, region, solution: dict, points, eps, warn_near=True,
-                          near=None):
-    """Displacement (N, 3) at interior ``points`` (evaluate.py:194-250)."""
+                          near=None, precision: str = "fp64"):
+    """Displacement (N, 3) at interior ``points`` (evaluate.py:194-250).
+    ``precision="mixed"``: the P0 double layers (boundary u and fault slip)
+    by FP32 quadrature for the far pairs and the FP64 closed form for the
+    near ones (within ~1e-6 of the FP64 readout); single layers and P1/P2
+    double layers stay FP64."""
     if near is not None:
         raise NotImplementedError("near-field recovery (near=) is not on the GPU readout path")
+    if precision not in ("fp64", "mixed"):
+        raise ValueError(f"precision must be 'fp64' or 'mixed' (got {precision!r})")
     region = _region(model, region)
     torch_in = is_torch(points)
     pts = as_cuda(points).reshape(-1, 3)
@@ -148,13 +154,19 @@ def evaluate_displacement(model: RegionModel, region, solution: dict, points, ep
     mat = region.material
     c = kb.t_coeffs(mat.mu, mat.lam)
     g = kb.u_coeffs(mat.mu, mat.lam)
+    def double_layer(patch, tv, nrm, e, jump, sigma):
+        d = as_cuda(np.asarray(jump, float).reshape(-1, 3))
+        if precision == "mixed" and patch.order == 0:
+            tn.t_disp_readout(pts, tv, nrm, e, d, *c, 0, out=u, alpha=-sigma, accumulate=True)
+        else:
+            tn.t_disp_contract(pts, tv, nrm, e, d, *c, patch.order, out=u, alpha=-sigma, accumulate=True)
+
     for p in region.patches:
         sigma = float(model.orientation(region, p))
         tv, nrm, e = _src(p, eps)
         u_p = _density(model, p, "u", solution)
         if np.any(u_p):
-            tn.t_disp_contract(pts, tv, nrm, e, as_cuda(np.asarray(u_p, float).reshape(-1, 3)), *c,
-                               p.order, out=u, alpha=-sigma, accumulate=True)
+            double_layer(p, tv, nrm, e, u_p, sigma)
         t_p = _density(model, p, "t", solution)
         if np.any(t_p):
             tn.u_disp_contract(pts, tv, e, as_cuda(np.asarray(t_p, float).reshape(-1, 3)), *g, p.order,
@@ -164,6 +176,5 @@ def evaluate_displacement(model: RegionModel, region, solution: dict, points, ep
         slip = _density(model, f, "slip", solution)
         if np.any(slip):
             tv, nrm, e = _src(f, eps)
-            tn.t_disp_contract(pts, tv, nrm, e, as_cuda(np.asarray(slip, float).reshape(-1, 3)), *c,
-                               f.order, out=u, alpha=-sigma, accumulate=True)
+            double_layer(f, tv, nrm, e, slip, sigma)
     return out_like(u, torch_in)

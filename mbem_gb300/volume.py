@@ -244,8 +244,8 @@ def sample(model, solution: dict, eps, grid: Grid, code: np.ndarray, chunk: int 
     ``sigma`` (elastic), ``strain``, ``eigenstress`` (with ``eigenstress``)
     and the derived scalars, each ``(N, ...)``, NaN where ``code`` is 0.
     Each point is read with its own region's material and patch set.
-    ``precision="mixed"`` takes the elastic stress from the FP32-far /
-    FP64-near readout."""
+    ``precision="mixed"`` takes the elastic stress and the P0 displacement
+    from the FP32-far / FP64-near readouts."""
     if near is not None:
         raise NotImplementedError("near-field recovery (near=) is not on the GPU readout path")
     chunk = chunk or defaults.VOLUME_CHUNK_DEVICE
@@ -267,7 +267,8 @@ def sample(model, solution: dict, eps, grid: Grid, code: np.ndarray, chunk: int 
         for s in range(0, where.numel(), chunk):
             sel = where[s:s + chunk]
             pts = pts_all[sel].contiguous()
-            out["u"][sel] = evaluate_displacement(model, r, solution, pts, eps, warn_near=False)
+            out["u"][sel] = evaluate_displacement(model, r, solution, pts, eps, warn_near=False,
+                                                  precision=precision)
             got = evaluate_stress(model, r, solution, pts, eps, subtract_anelastic=True, warn_near=False,
                                   parts=eigenstress, precision=precision)
             sig = got[0] if eigenstress else got

@@ -135,3 +135,49 @@ def test_region_codes_of_a_large_grid(gpu):
     _, total = model.point_in_region("body", pts, closure=True)
     total = total.cpu().numpy()
     assert np.abs(np.where(box, total - 4.0 * np.pi, total)).max() < SOLID_ANGLE_ATOL
+
+
+# the mixed displacement readout: FP32-far quadrature against the FP64
+# contraction, relative to the largest displacement of the set
+DISP_MIXED_TOL = 2e-6
+
+
+def test_mixed_displacement_readout_against_fp64(gpu):
+    """Cube 24 (6,912 triangles) + fault 16 (512): 8,192 observers, a
+    quarter within 0.02 .. 0.5 h of a face, both double layers."""
+    from mbem_gb300.evaluate import evaluate_displacement
+    from mbem_gb300.kernels import basis as kb
+    from mbem_gb300.kernels import tri_nodal as tn
+    model, eps = cube_fault_model(24, 16)
+    rng = np.random.default_rng(9)
+    pts = rng.uniform(-1.95, 1.95, size=(8192, 3))
+    h = 4.0 / 24
+    k = rng.integers(0, 3, 2048)
+    pts[:2048][np.arange(2048), k] = rng.choice([-2.0, 2.0], 2048) * (1.0 - rng.uniform(0.02, 0.5, 2048) * h / 2.0)
+    c = kb.t_coeffs(1.0, 1.0)
+    for patch in (model.regions[0].patches[0], model.regions[0].faults[0]):
+        tv = patch.tri_verts()
+        nrm, _ = patch.mesh.normals_and_areas()
+        e = np.full(tv.shape[0], eps)
+        d = rng.normal(size=(tv.shape[0], 3))
+        ref = tn.t_disp_contract(pts, tv, nrm, e, d, *c)
+        got = tn.t_disp_readout(pts, tv, nrm, e, d, *c)
+        assert rel_err(got, ref) < DISP_MIXED_TOL
+        acc = tn.t_disp_readout(pts, tv, nrm, e, d, *c, out=torch.from_numpy(ref).cuda(), alpha=-1.0,
+                                accumulate=True)
+        assert np.abs(acc.cpu().numpy()).max() < DISP_MIXED_TOL * np.abs(ref).max()
+    sol = {"u:cube": rng.normal(size=(6912, 3)) * 1e-2}
+    u64 = evaluate_displacement(model, "body", sol, pts, eps, warn_near=False)
+    u32 = evaluate_displacement(model, "body", sol, pts, eps, warn_near=False, precision="mixed")
+    assert rel_err(u32, u64) < DISP_MIXED_TOL
+
+
+def test_mixed_sample_matches_reference(gpu, volume_small):
+    g = volume_small
+    model, eps = cube_fault_model(3, 2)
+    grid = V.make_grid(model, 1.0, pad=1.0)
+    inside = g["code"] > 0
+    f = V.sample(model, _solution(g), eps, grid, g["code"], precision="mixed")
+    assert rel_err(f["u"][inside], g["f_u"][inside]) < DISP_MIXED_TOL
+    assert rel_err(f["sigma"][inside], g["f_sigma"][inside]) < 1e-5
+    assert np.isnan(f["u"][~inside]).all()

@@ -120,3 +120,11 @@ def test_eigenvalues_3x3_match_lapack():
     Z = np.zeros((2, 3, 3))
     Z[1] = np.diag([3.0, 1.0, 2.0])
     assert np.array_equal(V.eigvalsh3(torch.from_numpy(Z)).numpy(), [[0, 0, 0], [1, 2, 3]])
+
+
+def test_mixed_displacement_readout_is_p0_only():
+    from mbem_gb300.kernels import tri_nodal as tn
+    import pytest
+    with pytest.raises(NotImplementedError):
+        tn.t_disp_readout(np.zeros((1, 3)), np.zeros((1, 3, 3)), np.zeros((1, 3)), np.ones(1), np.zeros((3, 3)),
+                          1, 1, 1, 1, 1, 1, order=1)
