@@ -778,6 +778,8 @@ def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024):
     diff = float(np.abs(f_mixed["sigma"][inside] - f_fp64["sigma"][inside]).max()
                  / np.abs(f_fp64["sigma"][inside]).max())
     diff_u = float(np.abs(f_mixed["u"][inside] - f_fp64["u"][inside]).max() / np.abs(f_fp64["u"][inside]).max())
+    diff_e = float(np.abs(f_mixed["eigenstress"][inside] - f_fp64["eigenstress"][inside]).max()
+                   / np.abs(f_fp64["eigenstress"][inside]).max())
     # the two geometry kernels alone (CUDA events on the launching stream)
     pts = torch.from_numpy(grid.points).cuda()
     geo = MeshGeometry(cube.mesh)
@@ -806,6 +808,7 @@ def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024):
             "classify_s": t_cls, "clearance_s": t_clr, "sample_mixed_s": t_mixed, "sample_fp64_s": t_fp64,
             "points_per_s_mixed": n / (t_cls + t_clr + t_mixed),
             "max_rel_diff_stress_mixed_vs_fp64": diff, "max_rel_diff_u_mixed_vs_fp64": diff_u,
+            "max_rel_diff_eigenstress_mixed_vs_fp64": diff_e,
             "geometry_kernels": kt,
             "cpu_oracle_classify": {"points": int(sel.size), "s": t_cpu, "points_per_s": sel.size / t_cpu,
                                     "threads": 1, "kind": "port (numpy)",

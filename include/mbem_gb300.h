@@ -560,6 +560,16 @@ int mbem_readout_evaluate(const double* x, int64_t n_obs, const double* tri_vert
                           const float* records, const int64_t* rowptr, int64_t n_near, int64_t* pair_obs,
                           int32_t* pair_src, double* pair_out, double alpha, int accumulate, double* out,
                           void* stream);
+/* As mbem_readout_evaluate, and with eig_out (n_obs, 3, 3) also the
+ * eigenstress of the same pairs (+)= alpha (evaluate_stress(parts=True)):
+ * far pairs from the same quadrature points, near pairs by the FP64 nodal
+ * closed form into pair_eig (9 doubles a near pair). eig_out NULL: the
+ * elastic stress alone. */
+int mbem_readout_evaluate_parts(const double* x, int64_t n_obs, const double* tri_verts, const double* normals,
+                                const double* eps, int64_t n_src, const double* density, double mu, double lam,
+                                int order, const float* records, const int64_t* rowptr, int64_t n_near,
+                                int64_t* pair_obs, int32_t* pair_src, double* pair_out, double* pair_eig,
+                                double alpha, int accumulate, double* out, double* eig_out, void* stream);
 
 /* ---- deflated FGMRES on a dense operator (la/solver.py:115-245 fgmres,
  * wired as backends/hmat.py:678-690: P A P y = P b, P = I - Z Z^T with Z

@@ -151,6 +151,8 @@ _SIGNATURES = {
     "mbem_readout_prepare": (c_int, [_P, _I, _P, _P, _P, _I, _P, c_int, _D, _P, _P, _P, POINTER(c_int64), _P]),
     "mbem_readout_evaluate": (c_int, [_P, _I, _P, _P, _P, _I, _P, _D, _D, c_int, _P, _P, _I, _P, _P, _P, _D, c_int,
                                       _P, _P]),
+    "mbem_readout_evaluate_parts": (c_int, [_P, _I, _P, _P, _P, _I, _P, _D, _D, c_int, _P, _P, _I, _P, _P, _P, _P,
+                                            _D, c_int, _P, _P, _P]),
     "mbem_bj_inverse_bytes": (c_size_t, [_I, c_int]),
     "mbem_bj_build_dense": (c_int, [_P, _I, POINTER(BlockJacobi), _P]),
     "mbem_bj_build_mixed": (c_int, [POINTER(MixedOperator), POINTER(BlockJacobi), _P]),

@@ -36,10 +36,12 @@ int nodal_matrix(int kind, const double* x, int64_t nf, const double* tv, const 
                  const double* eps, int64_t ns, const double* coeffs, int order, double alpha,
                  int accumulate, double* out, int64_t ld, void* stream);
 // FP64 elastic (DD minus eigen) stress of listed (observer, source) pairs of a
-// nodal slip density, nine components per pair (the near pairs of a readout).
+// nodal slip density, nine components per pair (the near pairs of a readout);
+// with out_eig, also the pairs' eigenstress.
 int nodal_pairs_stress(const double* x, const double* tv, const double* normals, const double* eps,
                        const double* density, double mu, double lam, int order, const int64_t* pair_obs,
-                       const int32_t* pair_src, int64_t n_pairs, double* out, cudaStream_t st);
+                       const int32_t* pair_src, int64_t n_pairs, double* out, cudaStream_t st,
+                       double* out_eig = nullptr);
 int nodal_contract(int kind, const double* x, int64_t nf, const double* tv, const double* normals,
                    const double* eps, int64_t ns, const double* density, const double* coeffs,
                    double mu, double lam, int order, double alpha, int accumulate, double* out,

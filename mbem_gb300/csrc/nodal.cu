@@ -1020,11 +1020,13 @@ nodal_traction_kernel(NodalArgs a, NodalSpec sp) {
 // components per pair; the mixed-precision readout sends its near pairs here.
 __global__ void __launch_bounds__(ND_THREADS)
 nodal_pairs_stress_kernel(NodalArgs a, NodalSpec sp, const int64_t* __restrict__ pair_obs,
-                          const int32_t* __restrict__ pair_src, int64_t n_pairs, double* __restrict__ out) {
+                          const int32_t* __restrict__ pair_src, int64_t n_pairs, double* __restrict__ out,
+                          double* __restrict__ out_eig) {
     const int64_t p = (int64_t)blockIdx.x * ND_THREADS + threadIdx.x;
     if (p >= n_pairs) return;
     const int64_t f = pair_obs[p], s = pair_src[p];
     double acc[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double acc_e[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
     NodalSrc g;
     if (nodal_frame(a.tri_verts + 9 * s, g)) {
         double W[4][ND_MAXK][5][5];
@@ -1039,15 +1041,23 @@ nodal_pairs_stress_kernel(NodalArgs a, NodalSpec sp, const int64_t* __restrict__
             node_stress(g, W, k, z, nrm, d, eps, a.mu, a.lam, 3, sg);
             for (int m = 0; m < 3; m++)
                 for (int n = 0; n < 3; n++) acc[m][n] += sg[m][n];
+            if (out_eig) {
+                node_stress(g, W, k, z, nrm, d, eps, a.mu, a.lam, 2, sg);
+                for (int m = 0; m < 3; m++)
+                    for (int n = 0; n < 3; n++) acc_e[m][n] += sg[m][n];
+            }
         }
     }
     for (int m = 0; m < 3; m++)
         for (int n = 0; n < 3; n++) out[9 * p + 3 * m + n] = acc[m][n];
+    if (out_eig)
+        for (int m = 0; m < 3; m++)
+            for (int n = 0; n < 3; n++) out_eig[9 * p + 3 * m + n] = acc_e[m][n];
 }
 
 int nodal_pairs_stress(const double* x, const double* tv, const double* normals, const double* eps,
                        const double* density, double mu, double lam, int order, const int64_t* pair_obs,
-                       const int32_t* pair_src, int64_t n_pairs, double* out, cudaStream_t st) {
+                       const int32_t* pair_src, int64_t n_pairs, double* out, cudaStream_t st, double* out_eig) {
     MBEM_REQUIRE(order >= 0 && order <= 2, MBEM_ERR_ARG, "order must be 0, 1 or 2");
     int e = ensure_rules();
     if (e) return e;
@@ -1059,7 +1069,7 @@ int nodal_pairs_stress(const double* x, const double* tv, const double* normals,
     a.x_field = x; a.tri_verts = tv; a.normals = normals; a.eps = eps; a.density = density;
     a.mu = mu; a.lam = lam;
     nodal_pairs_stress_kernel<<<(unsigned)ceil_div(n_pairs, ND_THREADS), ND_THREADS, 0, st>>>(a, sp, pair_obs, pair_src,
-                                                                                          n_pairs, out);
+                                                                                          n_pairs, out, out_eig);
     return launch_status("nodal_pairs_stress_kernel");
 }
 

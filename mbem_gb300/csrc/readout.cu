@@ -214,9 +214,11 @@ struct RoMat {
 };
 
 // elastic stress of one quadrature point (d = x - y, slip u, normal v),
-// weight folded in; sym holds xx, yy, zz, xy, xz, yz
+// weight folded in; sym holds xx, yy, zz, xy, xz, yz; with EIG the
+// eigenstress integrand goes to sym_e as well
+template <bool EIG>
 __device__ __forceinline__ void point_stress(const float d[3], const float u[3], const float v[3], float w,
-                                             float eps2, const RoMat& m, float sym[6]) {
+                                             float eps2, const RoMat& m, float sym[6], float sym_e[6]) {
     const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
     const float ir = rsqrtf(dd + eps2);
     const float ir2 = ir * ir;
@@ -252,15 +254,19 @@ __device__ __forceinline__ void point_stress(const float d[3], const float u[3],
         const float sig = -(lam * delta * trB + mu * BB);
         const float eig = phi * (lam * delta * uv + mu * symuv);
         sym[t] = fmaf(w, sig - eig, sym[t]);
+        if (EIG) sym_e[t] = fmaf(w, eig, sym_e[t]);
     }
 }
 
 // far pairs by quadrature, near pairs listed; a thread per observer, sources
-// staged RO_TILE at a time in shared memory
+// staged RO_TILE at a time in shared memory; with EIG the eigenstress of the
+// far pairs goes to eig_out as well
+template <bool EIG>
 __global__ void __launch_bounds__(RO_THREADS)
 readout_far_kernel(const double* __restrict__ x, int64_t n_obs, const float* __restrict__ rec, int64_t n_src,
                    RoMat mat, const int64_t* __restrict__ rowptr, int64_t* __restrict__ pair_obs,
-                   int32_t* __restrict__ pair_src, double alpha, int accumulate, double* __restrict__ out) {
+                   int32_t* __restrict__ pair_src, double alpha, int accumulate, double* __restrict__ out,
+                   double* __restrict__ eig_out) {
     extern __shared__ __align__(16) float tile[];
     const int64_t f = (int64_t)blockIdx.x * RO_THREADS + threadIdx.x;
     const bool live = f < n_obs;
@@ -268,6 +274,7 @@ readout_far_kernel(const double* __restrict__ x, int64_t n_obs, const float* __r
     if (live)
         for (int k = 0; k < 3; k++) xo[k] = x[3 * f + k];
     double acc[6] = {0, 0, 0, 0, 0, 0};
+    double acc_e[6] = {0, 0, 0, 0, 0, 0};
     int64_t slot = live ? rowptr[f] : 0;
     const int64_t slot_end = live ? rowptr[f + 1] : 0;
     for (int64_t s0 = 0; s0 < n_src; s0 += RO_TILE) {
@@ -299,20 +306,30 @@ readout_far_kernel(const double* __restrict__ x, int64_t n_obs, const float* __r
             else { q0 = RO_Q0 + RO_Q1; q1 = RO_Q; }
             const float nv[3] = {r[6], r[7], r[8]};
             float sym[6] = {0, 0, 0, 0, 0, 0};
+            float sym_e[6] = {0, 0, 0, 0, 0, 0};
             for (int q = q0; q < q1; q++) {
                 const float* pq = r + RO_HDR + 7 * q;
                 const float d[3] = {dc[0] - pq[0], dc[1] - pq[1], dc[2] - pq[2]};
                 const float u[3] = {pq[4], pq[5], pq[6]};
-                point_stress(d, u, nv, pq[3], eps2, mat, sym);
+                point_stress<EIG>(d, u, nv, pq[3], eps2, mat, sym, sym_e);
             }
 #pragma unroll
             for (int k = 0; k < 6; k++) acc[k] += (double)sym[k];
+            if (EIG) {
+#pragma unroll
+                for (int k = 0; k < 6; k++) acc_e[k] += (double)sym_e[k];
+            }
         }
     }
     if (!live) return;
     double* o = out + 9 * f;
     const double v9[9] = {acc[0], acc[3], acc[4], acc[3], acc[1], acc[5], acc[4], acc[5], acc[2]};
     for (int k = 0; k < 9; k++) o[k] = accumulate ? o[k] + alpha * v9[k] : alpha * v9[k];
+    if (EIG) {
+        double* oe = eig_out + 9 * f;
+        const double e9[9] = {acc_e[0], acc_e[3], acc_e[4], acc_e[3], acc_e[1], acc_e[5], acc_e[4], acc_e[5], acc_e[2]};
+        for (int k = 0; k < 9; k++) oe[k] = accumulate ? oe[k] + alpha * e9[k] : alpha * e9[k];
+    }
 }
 
 // out[f] += alpha * sum of its near pairs' stresses, in list order
@@ -393,10 +410,21 @@ int mbem_readout_evaluate(const double* x, int64_t n_obs, const double* tri_vert
                           const float* records, const int64_t* rowptr, int64_t n_near, int64_t* pair_obs,
                           int32_t* pair_src, double* pair_out, double alpha, int accumulate, double* out,
                           void* stream) {
+    return mbem_readout_evaluate_parts(x, n_obs, tri_verts, normals, eps, n_src, density, mu, lam, order, records,
+                                       rowptr, n_near, pair_obs, pair_src, pair_out, nullptr, alpha, accumulate, out,
+                                       nullptr, stream);
+}
+
+int mbem_readout_evaluate_parts(const double* x, int64_t n_obs, const double* tri_verts, const double* normals,
+                                const double* eps, int64_t n_src, const double* density, double mu, double lam,
+                                int order, const float* records, const int64_t* rowptr, int64_t n_near,
+                                int64_t* pair_obs, int32_t* pair_src, double* pair_out, double* pair_eig,
+                                double alpha, int accumulate, double* out, double* eig_out, void* stream) {
     MBEM_REQUIRE(n_obs >= 0 && n_src >= 0 && n_near >= 0 && mu > 0.0 && lam + mu > 0.0, MBEM_ERR_ARG,
                  "bad readout arguments");
     MBEM_REQUIRE(n_obs == 0 || (x && rowptr && out), MBEM_ERR_ARG, "NULL readout arrays");
     MBEM_REQUIRE(n_near == 0 || (pair_obs && pair_src && pair_out), MBEM_ERR_ARG, "NULL near-pair arrays");
+    MBEM_REQUIRE(!eig_out || n_near == 0 || pair_eig, MBEM_ERR_ARG, "the eigenstress needs its near-pair array");
     if (n_obs == 0) return MBEM_OK;
     cudaStream_t st = (cudaStream_t)stream;
     const double nu = lam / (2.0 * (lam + mu));
@@ -408,16 +436,26 @@ int mbem_readout_evaluate(const double* x, int64_t n_obs, const double* tri_vert
     m.cblob_per_eps2 = (float)(2.0 * (1.0 - nu));
     m.phi_per_eps4 = (float)(15.0 / (8.0 * MBEM_PI));
     const size_t smem = (size_t)RO_TILE * RO_REC_PAD * sizeof(float);
-    cudaFuncSetAttribute(readout_far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    readout_far_kernel<<<(unsigned)ceil_div(n_obs, RO_THREADS), RO_THREADS, smem, st>>>(
-        x, n_obs, records, n_src, m, rowptr, pair_obs, pair_src, alpha, accumulate, out);
+    const unsigned grid = (unsigned)ceil_div(n_obs, RO_THREADS);
+    if (eig_out) {
+        cudaFuncSetAttribute(readout_far_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        readout_far_kernel<true><<<grid, RO_THREADS, smem, st>>>(x, n_obs, records, n_src, m, rowptr, pair_obs,
+                                                                 pair_src, alpha, accumulate, out, eig_out);
+    } else {
+        cudaFuncSetAttribute(readout_far_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        readout_far_kernel<false><<<grid, RO_THREADS, smem, st>>>(x, n_obs, records, n_src, m, rowptr, pair_obs,
+                                                                  pair_src, alpha, accumulate, out, nullptr);
+    }
     int e = launch_status("readout_far_kernel");
     if (e) return e;
     if (n_near == 0) return MBEM_OK;
     if ((e = nodal_pairs_stress(x, tri_verts, normals, eps, density, mu, lam, order, pair_obs, pair_src, n_near,
-                                pair_out, st)))
+                                pair_out, st, eig_out ? pair_eig : nullptr)))
         return e;
     readout_near_add_kernel<<<(unsigned)ceil_div(n_obs, 256), 256, 0, st>>>(rowptr, n_obs, pair_out, alpha, out);
+    if ((e = launch_status("readout_near_add_kernel"))) return e;
+    if (!eig_out) return MBEM_OK;
+    readout_near_add_kernel<<<(unsigned)ceil_div(n_obs, 256), 256, 0, st>>>(rowptr, n_obs, pair_eig, alpha, eig_out);
     return launch_status("readout_near_add_kernel");
 }
 

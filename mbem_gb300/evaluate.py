@@ -104,8 +104,17 @@ def evaluate_stress(model: RegionModel, region, solution: dict, points, eps,
         tv, nrm, e = _src(patch, eps)
         d = as_cuda(np.asarray(jump, float).reshape(-1, 3))
         if subtract_anelastic and precision == "mixed":
-            tn.elastic_stress_readout(pts, tv, nrm, e, d, mu, lam, patch.order, out=sig, alpha=-sigma,
-                                      accumulate=True)
+            # the eigenstress (parts) from the same quadrature and near pairs:
+            # eig += sigma E, sig -= sigma (S_H - E)
+            if parts:
+                e_tmp = torch.zeros_like(eig)
+                tn.elastic_stress_readout(pts, tv, nrm, e, d, mu, lam, patch.order, out=sig, alpha=-sigma,
+                                          accumulate=True, eig_out=e_tmp)
+                eig.sub_(e_tmp)
+            else:
+                tn.elastic_stress_readout(pts, tv, nrm, e, d, mu, lam, patch.order, out=sig, alpha=-sigma,
+                                          accumulate=True)
+            return
         elif subtract_anelastic:
             tn.elastic_stress_contract(pts, tv, nrm, e, d, mu, lam, patch.order, out=sig,
                                        alpha=-sigma, accumulate=True)

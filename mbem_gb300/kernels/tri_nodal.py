@@ -259,12 +259,14 @@ def traction_matrix(x_field, n_field, tri_verts, normals, eps_arr, ids, n_cols, 
 
 
 def elastic_stress_readout(x_field, tri_verts, normals, eps_arr, density, mu, lam, order=0, near_factor=3.0,
-                           out=None, alpha=1.0, accumulate=False):
+                           out=None, alpha=1.0, accumulate=False, eig_out=None):
     """The elastic stress (DD minus eigen) of a nodal slip density at many
     points, mixed precision (FP32 quadrature far field, FP64 near pairs):
     ``elastic_stress_contract``'s result to ~1e-6. The observers are ordered
     along a Morton curve for the launch (neighbouring threads then take the
-    same quadrature rule), the result in the caller's order."""
+    same quadrature rule), the result in the caller's order. ``eig_out`` (a
+    CUDA (N, 3, 3) tensor) receives alpha times the eigenstress of the same
+    pairs, (+)= as ``out`` (``eigenstress_contract``'s result to ~1e-6)."""
     import torch
     K = n_nodes(order)
     if order:
@@ -299,9 +301,25 @@ def elastic_stress_readout(x_field, tri_verts, normals, eps_arr, density, mu, la
     pair_src = torch.empty(m, dtype=torch.int32, device=dev)
     pair_out = torch.empty((m, 9), dtype=torch.float64, device=dev)
     res = torch.empty((N, 3, 3), dtype=torch.float64, device=dev)
-    nat.call("mbem_readout_evaluate", ptr(xs), N, ptr(tv), ptr(n), ptr(e), ns, ptr(d), float(mu), float(lam), order,
-             ptr(rec), ptr(rowptr), int(n_near.value), ptr(pair_obs), ptr(pair_src), ptr(pair_out), 1.0, 0,
-             ptr(res), st)
+    eig = None
+    if eig_out is not None:
+        if not (isinstance(eig_out, torch.Tensor) and eig_out.is_cuda and eig_out.shape == (N, 3, 3)):
+            raise TypeError("eig_out must be a CUDA (N, 3, 3) tensor")
+        pair_eig = torch.empty((m, 9), dtype=torch.float64, device=dev)
+        eig = torch.empty((N, 3, 3), dtype=torch.float64, device=dev)
+        nat.call("mbem_readout_evaluate_parts", ptr(xs), N, ptr(tv), ptr(n), ptr(e), ns, ptr(d), float(mu),
+                 float(lam), order, ptr(rec), ptr(rowptr), int(n_near.value), ptr(pair_obs), ptr(pair_src),
+                 ptr(pair_out), ptr(pair_eig), 1.0, 0, ptr(res), ptr(eig), st)
+        full_e = torch.empty_like(eig)
+        full_e[perm] = eig
+        if accumulate:
+            eig_out += alpha * full_e
+        else:
+            eig_out.copy_(alpha * full_e)
+    else:
+        nat.call("mbem_readout_evaluate", ptr(xs), N, ptr(tv), ptr(n), ptr(e), ns, ptr(d), float(mu), float(lam),
+                 order, ptr(rec), ptr(rowptr), int(n_near.value), ptr(pair_obs), ptr(pair_src), ptr(pair_out), 1.0,
+                 0, ptr(res), st)
     full = torch.empty_like(res)
     full[perm] = res
     if out is not None:

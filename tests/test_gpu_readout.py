@@ -67,3 +67,40 @@ def test_evaluate_stress_mixed_matches_fp64(gpu, cube_small):
     ref = evaluate_stress(model, "body", sol, g["points"], eps, warn_near=False)
     got = evaluate_stress(model, "body", sol, g["points"], eps, warn_near=False, precision="mixed")
     assert np.abs(got - ref).max() < 2e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("order", [0, 2])
+def test_mixed_readout_eigenstress_part_matches_fp64(gpu, order):
+    """eig_out: the eigenstress of the same pairs from the same pass, against
+    the FP64 eigenstress contraction (tolerance relative to its largest
+    value, which sits on the fault plane)."""
+    from mbem_gb300.kernels import tri_nodal as tn
+    x, tv, n, e, d = _case(order, n_obs=2000, seed=5)
+    mu, lam = 1.3, 1.95
+    ref_e = tn.eigenstress_contract(x, tv, n, e, d, mu, lam, order=order)
+    ref_s = tn.elastic_stress_readout(x, tv, n, e, d, mu, lam, order=order)
+    eig = torch.zeros((len(x), 3, 3), dtype=torch.float64, device="cuda")
+    got_s = tn.elastic_stress_readout(x, tv, n, e, d, mu, lam, order=order, eig_out=eig)
+    assert np.abs(eig.cpu().numpy() - ref_e).max() < 2e-5 * np.abs(ref_e).max()
+    # the elastic part agrees with the launch without eig_out to FP32 rounding
+    assert np.abs(got_s - ref_s).max() < 1e-6 * np.abs(ref_s).max()
+    acc = torch.ones_like(eig)
+    tn.elastic_stress_readout(x, tv, n, e, d, mu, lam, order=order, eig_out=acc, alpha=-2.0, accumulate=True)
+    assert np.allclose(acc.cpu().numpy(), 1.0 - 2.0 * eig.cpu().numpy(), rtol=1e-12,
+                       atol=1e-12 * np.abs(ref_e).max())
+
+
+def test_evaluate_stress_mixed_parts_match_fp64(gpu, cube_small):
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model
+    from mbem_gb300.evaluate import evaluate_stress
+    from mbem_gb300.model import generate_system
+    g = cube_small
+    model, eps = cube_fault_model(int(g["n_face"]), int(g["n_fault"]), float(g["mu"]), float(g["lam"]))
+    asm = DenseBackend(jump="calibrated", deflate=True, rtol=1e-12).assemble(generate_system(model), eps)
+    sol = asm.solve()
+    rs, re = evaluate_stress(model, "body", sol, g["points"], eps, warn_near=False, parts=True)
+    gs, ge = evaluate_stress(model, "body", sol, g["points"], eps, warn_near=False, parts=True, precision="mixed")
+    assert np.abs(gs - rs).max() < 2e-5 * np.abs(rs).max()
+    assert np.abs(ge - re).max() < 2e-5 * np.abs(re).max()
+    assert np.abs(ge - g["stress_eigen"]).max() < 2e-5 * np.abs(g["stress_eigen"]).max()
