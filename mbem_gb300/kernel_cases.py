@@ -21,6 +21,9 @@ learned   FAULT_TRACTION cube 16 x 16, fault 12 x 12: the learned two-level
 volume    the volume sampler's geometry on cube 24 (6,912 triangles): region
           codes and clearances of a 40^3 grid (solid_angle_kernel,
           mesh_distance_kernel)
+vsample   the mixed readout of the same 40^3 grid after a mixed solve of cube 24
+          + fault 16: readout_far_kernel<EIG> (stress and eigenstress) and
+          disp_readout_kernel, each over the cube and the fault
 """
 
 from __future__ import annotations
@@ -130,6 +133,13 @@ def run(which: str) -> None:
         grid = V.make_grid(model, 4.0 / 40)
         V.classify(model, grid)
         V.clearance(model, grid, eps)
+    elif which == "vsample":
+        from . import volume as V
+        model, eps = cube_fault_model(24, 16)
+        sol = DenseBackend(jump="calibrated", deflate=True, rtol=1e-8, precision="mixed",
+                           precond="bf16_inner").assemble(generate_system(model), eps).solve()
+        grid = V.make_grid(model, 4.0 / 40)
+        V.sample(model, sol, eps, grid, V.classify(model, grid), precision="mixed")
     else:
         raise SystemExit(f"unknown case {which!r}")
     torch.cuda.synchronize()
