@@ -54,6 +54,8 @@ class MeshGeometry:
         if self.n_tri == 0:
             raise ValueError("the distance to a mesh needs at least one triangle")
         pts = points.reshape(-1, 3).contiguous()
+        if not bool(torch.isfinite(pts).all()):
+            raise ValueError("the distance to a mesh needs finite points")
         d = torch.empty(pts.shape[0], dtype=torch.float64, device=pts.device)
         idx = torch.empty(pts.shape[0], dtype=torch.int64, device=pts.device)
         nat.call("mbem_mesh_distance", ptr(self.records), ptr(self.tv), self.n_tri, ptr(pts), pts.shape[0],

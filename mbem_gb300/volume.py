@@ -252,7 +252,10 @@ def sample(model, solution: dict, eps, grid: Grid, code: np.ndarray, chunk: int 
     pts_all = _points(grid.points)
     dev = pts_all.device
     n = pts_all.shape[0]
-    code_t = torch.as_tensor(np.asarray(code), device=dev)
+    code = np.asarray(code)
+    if code.shape != (n,):
+        raise ValueError(f"code must hold one region code a grid point ({n}), got shape {code.shape}")
+    code_t = torch.as_tensor(code, device=dev)
     nan = float("nan")
     out = {"u": torch.full((n, 3), nan, dtype=torch.float64, device=dev),
            "sigma": torch.full((n, 3, 3), nan, dtype=torch.float64, device=dev),

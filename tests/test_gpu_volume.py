@@ -120,6 +120,10 @@ def test_sample_matches_reference(gpu, volume_small):
     assert rel_err(mixed["sigma"][inside], g["f_sigma"][inside]) < 1e-5
     with pytest.raises(NotImplementedError):
         V.sample(model, _solution(g), eps, grid, code, near=object())
+    with pytest.raises(ValueError):
+        V.sample(model, _solution(g), eps, grid, code[:-1])
+    with pytest.raises(ValueError):
+        G.distance_to_mesh(np.array([[0.0, np.nan, 0.0]]), model.regions[0].patches[0].mesh)
 
 
 def test_region_codes_of_a_large_grid(gpu):
