@@ -55,6 +55,11 @@ def volume_small():
 
 
 @pytest.fixture(scope="session")
+def volume_regions():
+    return load_golden("volume_regions")
+
+
+@pytest.fixture(scope="session")
 def oracle():
     from oracle import oracle as orc
     orc.lib()

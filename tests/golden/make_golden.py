@@ -334,9 +334,55 @@ def make_volume_small(path):
     print(f"volume_small: {time.time() - t0:.1f} s", flush=True)
 
 
+def make_volume_regions(path):
+    """Region codes and clearances of the reference's volume module on a
+    two-region model: a traction-free host cube of side 4 (3 x 3 per face)
+    with an inclusion cube of side 2 (2 x 2 per face) whose surface is an
+    INTERFACE patch of both regions. Points: a padded grid, points ON the
+    interface (faces, an edge, a corner), 1e-6 either side of it, and on the
+    outer surface; with each region's closure sums."""
+    import local_box_mesh as lbm
+    from mollified_bem import ElasticMaterial
+    from mbem import volume
+    from mbem.model import BCType, Patch, Region, RegionModel
+
+    def box(a, n):
+        return lbm._concatenate_meshes([
+            lbm.make_rectangular_patch((-a, a), (-a, a), a, n, n, normal_up=True),
+            lbm.make_rectangular_patch((-a, a), (-a, a), -a, n, n, normal_up=False),
+            lbm.make_vertical_panel("x", a, (-a, a), (-a, a), n, n, +1),
+            lbm.make_vertical_panel("x", -a, (-a, a), (-a, a), n, n, -1),
+            lbm.make_vertical_panel("y", a, (-a, a), (-a, a), n, n, +1),
+            lbm.make_vertical_panel("y", -a, (-a, a), (-a, a), n, n, -1)])
+
+    t0 = time.time()
+    outer, inner = box(2.0, 3), box(1.0, 2)
+    host_p = Patch("outer", outer, BCType.FREE_TRACTION)
+    iface = Patch("iface", inner, BCType.INTERFACE)
+    host = Region("host", ElasticMaterial(mu=1.0, lam=1.0), [host_p, iface], np.array([1.5, 1.5, 1.5]))
+    incl = Region("incl", ElasticMaterial(mu=2.0, lam=3.0), [iface], np.zeros(3))
+    model = RegionModel([host, incl])
+    grid = volume.make_grid(model, 0.5, pad=0.5)
+    extra = np.array([[1.0, 0.3, 0.2], [0.5, -1.0, 0.7], [0.2, 0.1, 1.0], [-1.0, -1.0, 0.3], [1.0, 1.0, 1.0],
+                      [1.0 - 1e-6, 0.3, 0.2], [1.0 + 1e-6, 0.3, 0.2], [0.2, 0.1, -1.0 + 1e-6],
+                      [0.2, 0.1, -1.0 - 1e-6], [2.0, 0.4, -0.3], [-0.6, 2.0, 1.1], [0.0, 0.0, 0.0]])
+    pts = np.concatenate([grid.points, extra])
+    g2 = volume.Grid(origin=grid.origin, spacing=grid.spacing, dims=(pts.shape[0], 1, 1), points=pts)
+    code = volume.classify(model, g2)
+    c_h, c_eps, c_fault = volume.clearance(model, g2, 0.1)
+    totals = np.stack([model.point_in_region(r, pts, closure=True)[1] for r in model.regions])
+    sig = np.array([model.orientation(host, host_p), model.orientation(host, iface), model.orientation(incl, iface)])
+    np.savez_compressed(path, outer_vertices=outer.vertices, outer_triangles=outer.triangles,
+                        inner_vertices=inner.vertices, inner_triangles=inner.triangles, points=pts,
+                        n_grid=grid.points.shape[0], code=code, c_h=c_h, c_eps=c_eps, c_fault=c_fault,
+                        totals=totals, orientation=sig)
+    print(f"volume_regions: {time.time() - t0:.1f} s", flush=True)
+
+
 CASES = {"p0_pairs": make_p0_pairs, "cube_small": make_cube_small,
          "c1_rows": make_c1_rows, "nodal_pairs": make_nodal_pairs,
-         "traction_small": make_traction_small, "volume_small": make_volume_small}
+         "traction_small": make_traction_small, "volume_small": make_volume_small,
+         "volume_regions": make_volume_regions}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(CASES)

@@ -185,3 +185,24 @@ def test_mixed_sample_matches_reference(gpu, volume_small):
     assert rel_err(f["u"][inside], g["f_u"][inside]) < DISP_MIXED_TOL
     assert rel_err(f["sigma"][inside], g["f_sigma"][inside]) < 1e-5
     assert np.isnan(f["u"][~inside]).all()
+
+
+def test_two_region_codes_and_clearances_match_reference(gpu, volume_regions):
+    """Host cube + inclusion behind an INTERFACE patch (the reference's own
+    volume module wrote the codes): points on the interface, on its edge and
+    corner, 1e-6 either side of it, on the outer surface."""
+    from test_volume import two_region_model
+    g = volume_regions
+    model, _, _ = two_region_model(g)
+    grid = V.Grid(origin=(0.0, 0.0, 0.0), spacing=(0.5,) * 3, dims=(g["points"].shape[0], 1, 1),
+                  points=g["points"])
+    code = V.classify(model, grid)
+    assert np.array_equal(code, g["code"])
+    c_h, c_eps, c_fault = V.clearance(model, grid, 0.1)
+    assert rel_err(c_h, g["c_h"]) < 1e-13 and rel_err(c_eps, g["c_eps"]) < 1e-13
+    assert np.isinf(c_fault).all()
+    # closure sums off the surfaces (on a surface the sum is rounding's choice)
+    off = (g["c_h"] > 1e-6)
+    for r, reg in enumerate(model.regions):
+        _, total = model.point_in_region(reg, g["points"], closure=True)
+        assert np.abs(total[off] - g["totals"][r][off]).max() < SOLID_ANGLE_ATOL

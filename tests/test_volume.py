@@ -128,3 +128,37 @@ def test_mixed_displacement_readout_is_p0_only():
     with pytest.raises(NotImplementedError):
         tn.t_disp_readout(np.zeros((1, 3)), np.zeros((1, 3, 3)), np.zeros((1, 3)), np.ones(1), np.zeros((3, 3)),
                           1, 1, 1, 1, 1, 1, order=1)
+
+
+def two_region_model(g):
+    """Host cube with an inclusion bounded by an INTERFACE patch, from the
+    fixture's own meshes."""
+    from mbem_gb300.mesh import ElasticMaterial, TriMesh
+    from mbem_gb300.model import BCType, Patch, Region, RegionModel
+    outer = TriMesh(g["outer_vertices"], g["outer_triangles"])
+    inner = TriMesh(g["inner_vertices"], g["inner_triangles"])
+    host_p = Patch("outer", outer, BCType.FREE_TRACTION)
+    iface = Patch("iface", inner, BCType.INTERFACE)
+    host = Region("host", ElasticMaterial(1.0, 1.0), [host_p, iface], np.array([1.5, 1.5, 1.5]))
+    incl = Region("incl", ElasticMaterial(2.0, 3.0), [iface], np.zeros(3))
+    return RegionModel([host, incl]), host_p, iface
+
+
+def test_two_region_oracle_and_orientation_match_reference(volume_regions):
+    """Region codes with an interface: points ON it go to the first region
+    that owns it; the orientation signs of the interface are opposite."""
+    g = volume_regions
+    model, host_p, iface = two_region_model(g)
+    host, incl = model.regions
+    sig = [model.orientation(host, host_p), model.orientation(host, iface), model.orientation(incl, iface)]
+    assert sig == list(g["orientation"])
+    outer = _tv(g, "outer")
+    inner = _tv(g, "inner")
+    regions = [[(outer, sig[0]), (inner, sig[1])], [(inner, sig[2])]]
+    assert np.array_equal(go.classify(regions, g["points"]), g["code"])
+    for r, patches in enumerate(regions):
+        assert np.abs(go.closure(patches, g["points"])[1] - g["totals"][r]).max() < 1e-12
+    c_h, c_eps, c_f = go.clearance(g["points"], [(outer, np.full(len(outer), 0.1)), (inner, np.full(len(inner), 0.1)),
+                                                 (inner, np.full(len(inner), 0.1))], [])
+    assert rel_err(c_h, g["c_h"]) < 1e-14 and rel_err(c_eps, g["c_eps"]) < 1e-14
+    assert np.isinf(g["c_fault"]).all() and np.isinf(c_f).all()
