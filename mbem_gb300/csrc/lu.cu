@@ -269,8 +269,8 @@ __device__ __forceinline__ void bf16_pieces(float x, uint16_t& hi, uint16_t& mid
 }
 
 // Ls[r][6 x W]: the pieces of rows row0 + r (r < M) of a row-major FP32
-// matrix at columns col0 .. col0 + nbw (W = 64 or 128; L21 in the
-// factorisation, the L or U panel of a blocked solve)
+// matrix at columns col0 .. col0 + nbw (W = 64, a panel, or 256, an outer
+// block; L21 in the factorisation, the L or U panel of a blocked solve)
 template <int W>
 __global__ void lu_split_rows_kernel(const float* __restrict__ A, int64_t lda, int64_t row0, int64_t col0, int nbw,
                                      int64_t M, uint16_t* __restrict__ Ls) {
