@@ -191,7 +191,7 @@ def test_two_region_codes_and_clearances_match_reference(gpu, volume_regions):
     """Host cube + inclusion behind an INTERFACE patch (the reference's own
     volume module wrote the codes): points on the interface, on its edge and
     corner, 1e-6 either side of it, on the outer surface."""
-    from test_volume import two_region_model
+    from volume_models import two_region_model
     g = volume_regions
     model, _, _ = two_region_model(g)
     grid = V.Grid(origin=(0.0, 0.0, 0.0), spacing=(0.5,) * 3, dims=(g["points"].shape[0], 1, 1),

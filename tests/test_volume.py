@@ -10,6 +10,7 @@ from conftest import rel_err
 from mbem_gb300 import volume as V
 from mbem_gb300.cases import cube_fault_model
 from oracle import geometry_oracle as go
+from volume_models import two_region_model
 
 
 def _tv(g, name):
@@ -128,20 +129,6 @@ def test_mixed_displacement_readout_is_p0_only():
     with pytest.raises(NotImplementedError):
         tn.t_disp_readout(np.zeros((1, 3)), np.zeros((1, 3, 3)), np.zeros((1, 3)), np.ones(1), np.zeros((3, 3)),
                           1, 1, 1, 1, 1, 1, order=1)
-
-
-def two_region_model(g):
-    """Host cube with an inclusion bounded by an INTERFACE patch, from the
-    fixture's own meshes."""
-    from mbem_gb300.mesh import ElasticMaterial, TriMesh
-    from mbem_gb300.model import BCType, Patch, Region, RegionModel
-    outer = TriMesh(g["outer_vertices"], g["outer_triangles"])
-    inner = TriMesh(g["inner_vertices"], g["inner_triangles"])
-    host_p = Patch("outer", outer, BCType.FREE_TRACTION)
-    iface = Patch("iface", inner, BCType.INTERFACE)
-    host = Region("host", ElasticMaterial(1.0, 1.0), [host_p, iface], np.array([1.5, 1.5, 1.5]))
-    incl = Region("incl", ElasticMaterial(2.0, 3.0), [iface], np.zeros(3))
-    return RegionModel([host, incl]), host_p, iface
 
 
 def test_two_region_oracle_and_orientation_match_reference(volume_regions):
