@@ -740,7 +740,7 @@ def dense_lu_workload(n_face=35):
     return out
 
 
-def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024):
+def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024, cpu=True):
     """The volume sampler on the cube 24 x 24 per face with the 16 x 16
     fault, solved (mixed, 1e-8): a grid of (n_grid + 2 pad_cells)^3 points
     half a cell off every face (some outside the body); region codes
@@ -748,15 +748,14 @@ def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024):
     distance test), the clearances (distances to the cube and the fault),
     and the sampled displacement, elastic stress, strain, eigenstress and
     scalars, with the stress and displacement from the mixed and from the
-    FP64 readouts. The
-    oracle's classification of n_cpu points on the host cores beside it."""
+    FP64 readouts. With ``cpu``, the CPU baseline of the classification
+    (volume_cpu_baseline) beside it."""
     import torch
     from mbem_gb300 import volume as V
     from mbem_gb300.backends.dense import DenseBackend
     from mbem_gb300.cases import cube_fault_model
     from mbem_gb300.geometry import MeshGeometry
     from mbem_gb300.model import generate_system
-    from oracle import geometry_oracle as go
     model, eps = cube_fault_model(n_face, n_fault)
     asm = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, precision="mixed",
                        precond="bf16_inner").assemble(generate_system(model), eps)
@@ -797,27 +796,22 @@ def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / 3
         kt[name] = {"ms": ms, "point_triangle_pairs_per_s": pairs / (ms * 1e-3)}
-    # the oracle's classification on a bounded sample of the grid
-    sel = np.random.default_rng(0).choice(n, size=min(n_cpu, n), replace=False)
-    t0 = time.perf_counter()
-    cpu_code = go.classify([[(cube.tri_verts(), 1.0)]], grid.points[sel])
-    t_cpu = time.perf_counter() - t0
-    return {"config": {"n_face": n_face, "n_fault": n_fault, "grid": list(grid.dims), "points": n,
+    out = {"config": {"n_face": n_face, "n_fault": n_fault, "grid": list(grid.dims), "points": n,
                        "points_inside": int(inside.sum()), "cube_triangles": geo.n_tri,
                        "fault_triangles": model.regions[0].faults[0].mesh.n_triangles},
             "classify_s": t_cls, "clearance_s": t_clr, "sample_mixed_s": t_mixed, "sample_fp64_s": t_fp64,
             "points_per_s_mixed": n / (t_cls + t_clr + t_mixed),
             "max_rel_diff_stress_mixed_vs_fp64": diff, "max_rel_diff_u_mixed_vs_fp64": diff_u,
             "max_rel_diff_eigenstress_mixed_vs_fp64": diff_e,
-            "geometry_kernels": kt,
-            "cpu_oracle_classify": {"points": int(sel.size), "s": t_cpu, "points_per_s": sel.size / t_cpu,
-                                    "threads": 1, "kind": "port (numpy)",
-                                    "agrees_with_gpu": bool(np.array_equal(cpu_code, code[sel]))}}
+            "geometry_kernels": kt}
+    if cpu:
+        out["cpu_baseline"] = volume_cpu_baseline(grid.points, code, cube.tri_verts(), n_cpu)
+    return out
 
 
 def extra_workloads(args, peaks):
     out = {}
-    for name, fn in (("volume_cube24_grid66", volume_workload),
+    for name, fn in (("volume_cube24_grid66", lambda: volume_workload(cpu=not args.skip_cpu)),
                      ("multi_rhs_cube24_256", lambda: multi_rhs_workload(peaks)),
                      ("multi_mesh_64_cubes", lambda: multi_mesh_workload(peaks)),
                      ("p1_variant_cube24", p1_variant_workload),
@@ -883,6 +877,21 @@ def cpu_baseline(args, iterations):
             "sample": f"T-kernel assembly of {s1} of {Ns} source columns x {x.shape[0]} field points "
                       f"({dt:.2f} s, extrapolated x{Ns / s1:.1f}) + FP64 matvec on {rows} of {n} rows "
                       f"x {iterations + 2} matvecs; host {os.uname().machine}"}
+
+
+def volume_cpu_baseline(points, code, tri_verts, n_cpu=1024):
+    """The CPU baseline of the volume sampler's classification: the numpy
+    restatement (one host core) on a bounded random sample of the grid,
+    with its agreement with the GPU codes of the same points."""
+    from oracle import geometry_oracle as go
+    n = points.shape[0]
+    sel = np.random.default_rng(0).choice(n, size=min(n_cpu, n), replace=False)
+    t0 = time.perf_counter()
+    cpu_code = go.classify([[(tri_verts, 1.0)]], points[sel])
+    t_cpu = time.perf_counter() - t0
+    return {"value": sel.size / t_cpu, "unit": "points/s", "cores": 1, "kind": "port",
+            "sample": f"region codes of {sel.size} of {n} grid points (numpy, {t_cpu:.2f} s)",
+            "agrees_with_gpu": bool(np.array_equal(cpu_code, code[sel]))}
 
 
 def run_reference(args, rank, ws):
