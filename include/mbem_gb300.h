@@ -221,18 +221,31 @@ int mbem_mixed_rowsum3(const float* A32, int64_t ld, int64_t n_rows, int64_t n_c
 int mbem_near_add_diagonal(const int64_t* rowptr, const int64_t* cols, double* vals, int64_t n_field,
                            const double* D, int* missing, void* stream);
 /* y = A x for the mixed operator (far in double-float, near in FP64);
- * y (n_rows) is overwritten. work >= 2 n_cols floats + 64 bytes. */
+ * y (n_rows) is overwritten. work >= 2 n_cols floats + 64 bytes.
+ * The product streams the far field through a bulk-copy ring whose waits are
+ * bounded: a wait that runs out sets a device flag and the product returns
+ * MBEM_OK with a partial y. The flag is read (and cleared) only by
+ * mbem_mixed_wait_check or by the next FGMRES solve on a mixed operator. */
 int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, void* work,
                       size_t work_bytes, void* stream);
+/* MBEM_ERR_WAIT if a bulk-copy wait of a mixed-operator kernel (product or
+ * assembly) gave up since the last check, else MBEM_OK; clears the flag.
+ * Synchronises `stream`. No counterpart in the reference (its products
+ * cannot time out). */
+int mbem_mixed_wait_check(void* stream);
 /* The same product for callers that cannot allocate device memory (a host that
  * gives all device memory to its own pool at start-up, or a loop that must not
  * enter the allocator): no workspace argument, and nothing allocated. Its
  * scratch is a fixed 2 MiB array inside the library, held by every GPU that
  * loads it until exit, so n_cols is limited to 262144 (larger sizes return
  * MBEM_ERR_SIZE). The first call on each device looks the array's device
- * address up (cudaGetSymbolAddress) and must come before any stream capture.
+ * address up (cudaGetSymbolAddress) and must come before any stream capture;
+ * the address is cached per CUDA context, so after cudaDeviceReset the first
+ * call in the new context again comes before any capture.
  * All calls share the array: calls that overlap on the GPU (other streams,
  * other host threads) race and must be serialised by the caller.
+ * An expired bulk-copy wait is reported as for mbem_mixed_matvec: run
+ * mbem_mixed_wait_check after the product to see it.
  * It has no counterpart in the reference. */
 int mbem_mixed_matvec_noalloc(const mbem_mixed_operator* op, const double* x, double* y,
                               void* stream);

@@ -195,6 +195,7 @@ _SIGNATURES = {
     "mbem_inner_bf16_apply": (c_int, [POINTER(InnerBf16), _P, _P, _P]),
     "mbem_inner_bf16_stats": (None, [c_int, POINTER(c_int64), POINTER(c_int64), POINTER(c_double)]),
     "mbem_mixed_matvec_noalloc": (c_int, [POINTER(MixedOperator), _P, _P, _P]),
+    "mbem_mixed_wait_check": (c_int, [_P]),
     "mbem_gemm_bf16_sub": (c_int, [_P, _I, _P, _I, _I, _I, _I, _P, _I, _P]),
     "mbem_lu_workspace_size": (c_size_t, [_I, c_int]),
     "mbem_lu_factor_f32": (c_int, [_P, _I, _I, _P, _P, c_size_t, _P, _P]),

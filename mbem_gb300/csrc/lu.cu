@@ -192,12 +192,19 @@ lu_panel_kernel(PanelArgs a) {
             }
             __syncthreads();
         }
-        const int64_t p = s_p;
+        // no candidate at all: every remaining entry of the column is NaN
+        // (|NaN| compares false), e.g. after Inf - Inf in an earlier update.
+        // The column is then a zero pivot: row gj stays in place, nothing is
+        // eliminated and info reports it.
+        const bool none = s_p < 0;
+        const int64_t p = none ? gj : s_p;
         const int win = s_win;
-        for (int c = tid; c < LU_NB; c += LU_PT) prow[c] = __ldcg(a.cand_rows + ((int64_t)buf * G + win) * LU_NB + c);
+        for (int c = tid; c < LU_NB; c += LU_PT)
+            prow[c] = none ? __ldcg(a.rowj + buf * LU_NB + c)
+                           : __ldcg(a.cand_rows + ((int64_t)buf * G + win) * LU_NB + c);
         __syncthreads();
         if (tid == 0) {
-            s_pv = prow[j];
+            s_pv = none ? 0.0f : prow[j];
             if (b == 0) a.piv[gj] = (int32_t)p;
             if (b == 0 && s_pv == 0.0f) atomicCAS(a.info, 0, (int)(gj + 1));
         }
@@ -236,7 +243,7 @@ __global__ void lu_swap_kernel(float* __restrict__ A, int64_t lda, int64_t n, in
     const int64_t c = t < k ? t : t + nbw;     // skip the panel's own columns
     for (int i = 0; i < nbw; i++) {
         const int64_t p = piv[k + i];
-        if (p == k + i) continue;
+        if (p <= k + i || p >= n) continue;      // no interchange (a pivot is never above its row)
         float* x = A + (k + i) * lda + c;
         float* y = A + p * lda + c;
         const float v = *x;
@@ -454,6 +461,9 @@ int mbem_lu_factor_f32(float* A, int64_t lda, int64_t n, int32_t* piv, void* wor
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     MBEM_REQUIRE(coop, MBEM_ERR_UNSUPPORTED, "the device cannot launch cooperative kernels");
+    // the pivot search reads one CTA's candidate per panel thread
+    MBEM_REQUIRE(sms <= LU_PT, MBEM_ERR_UNSUPPORTED, "the LU panel supports at most %d SMs (the device has %d)",
+                 LU_PT, sms);
     const size_t need = mbem_lu_workspace_size(n, sms);
     MBEM_REQUIRE(work && work_bytes >= need, MBEM_ERR_SIZE, "LU workspace %zu < %zu bytes", work_bytes, need);
     // the panel slice of each CTA must fit in shared memory

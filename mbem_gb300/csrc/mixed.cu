@@ -1609,6 +1609,10 @@ int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y,
     return mixed_matvec(op, x, y, xh, xl, (cudaStream_t)stream);
 }
 
+int mbem_mixed_wait_check(void* stream) {
+    return mixed_wait_check((cudaStream_t)stream);
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -1626,31 +1630,64 @@ int mbem_mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y,
 namespace mbem {
 
 constexpr int64_t NOALLOC_MAX_COLS = 262144;          // 2 x 262144 floats = 2 MiB
-constexpr int NOALLOC_MAX_DEVICES = 64;
 
 static __device__ __align__(256) float g_noalloc_split[2 * NOALLOC_MAX_COLS];
 
 static std::mutex g_noalloc_mutex;
-static float* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the host-side name of a __device__ array is not a device
-// address and must never be passed to a kernel).
+// The array's device address differs between CUDA contexts (a driver-API
+// context that is not the device's primary one, or the primary context made
+// again after cudaDeviceReset), so it is cached per context: the current
+// context's handle is read through the driver entry point (no libcuda link).
+struct NoallocEntry {
+    void* ctx;
+    float* ptr;
+};
+constexpr int NOALLOC_CACHE = 64;
+static NoallocEntry g_noalloc_cache[NOALLOC_CACHE];
+static int g_noalloc_used = 0;
+typedef int (*CtxGetCurrentFn)(void**);
+static CtxGetCurrentFn g_ctx_get_current = nullptr;
+
+static void* noalloc_current_context() {
+    if (g_ctx_get_current == nullptr) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPoint("cuCtxGetCurrent", &fn, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || fn == nullptr)
+            return nullptr;
+        g_ctx_get_current = (CtxGetCurrentFn)fn;
+    }
+    void* ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != 0) return nullptr;
+    return ctx;
+}
+
+// Device address of the scratch array in the current context, looked up once
+// per context (the host-side name of a __device__ array is not a device
+// address and must never be passed to a kernel). Without a readable context
+// handle the address is looked up on every call.
 static int noalloc_scratch(float** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
-        return set_error(MBEM_ERR_UNSUPPORTED, "device ordinal %d beyond %d", dev, NOALLOC_MAX_DEVICES);
+    // makes the device's primary context current on this thread if no
+    // context is (it allocates nothing)
+    e = cudaSetDevice(dev);
+    if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (g_noalloc_ptr[dev] == nullptr) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_split);
-        if (e != cudaSuccess)
-            return set_error(MBEM_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-        g_noalloc_ptr[dev] = static_cast<float*>(p);
-    }
-    *out = g_noalloc_ptr[dev];
+    void* ctx = noalloc_current_context();
+    if (ctx != nullptr)
+        for (int i = 0; i < g_noalloc_used; i++)
+            if (g_noalloc_cache[i].ctx == ctx) {
+                *out = g_noalloc_cache[i].ptr;
+                return MBEM_OK;
+            }
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_split);
+    if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    if (ctx != nullptr && g_noalloc_used < NOALLOC_CACHE) g_noalloc_cache[g_noalloc_used++] = {ctx, (float*)p};
+    *out = static_cast<float*>(p);
     return MBEM_OK;
 }
 

@@ -1,10 +1,12 @@
-"""CPU assembly of a BlockSystem with the C oracle (test infrastructure).
+"""CPU assembly of a BlockSystem with the C oracle (TEST INFRASTRUCTURE, not
+the product).
 
 Walks the terms that ``mbem_gb300.model.generate_system`` emits exactly as
-the reference's AssembledDense._build does (dense.py:480-528): blocks, the
-calibrated diagonal from the blocks' row sums, the RHS products. Used to
-check the host-side model logic on a machine without a GPU, and as the
-oracle system at sizes the reference cannot hold.
+the reference's AssembledDense._build does (``src/mbem/backends/dense.py:480-528``):
+blocks, the calibrated diagonal from the blocks' row sums, the RHS products.
+Used by ``tests/`` to check the host-side model logic on a machine without a
+GPU and as the oracle system at sizes the reference cannot hold, and by the
+CPU legs of ``bench.py`` for the port's own complete solve.
 """
 
 from __future__ import annotations

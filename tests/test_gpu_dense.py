@@ -69,7 +69,7 @@ def test_c1_config_rows_solution_and_readout(gpu, c1_rows):
 
 def test_gpu_system_matches_oracle_system(gpu, oracle):
     """A larger cube (n = 6: 432 + 32 elements) against the oracle assembly."""
-    from cpu_system import assemble
+    from oracle.cpu_system import assemble
     from mbem_gb300.backends.dense import DenseBackend
     from mbem_gb300.cases import cube_fault_model
     from mbem_gb300.model import generate_system

@@ -57,6 +57,34 @@ def test_singular_matrix_is_refused(gpu):
         Factor(A.cuda())
 
 
+@pytest.mark.parametrize("n, col", [(130, 77), (300, 0), (300, 299)])
+def test_all_nan_column_is_a_zero_pivot(gpu, n, col):
+    """A column whose remaining entries are all NaN has no pivot candidate
+    (|NaN| compares false): the C ABI reports it in info as a zero pivot,
+    keeps every pivot index inside the matrix and swaps nothing."""
+    from mbem_gb300 import _native as nat
+    from mbem_gb300._device import ptr, stream_handle
+    A = torch.randn(n, n, dtype=torch.float32, device="cuda")
+    A[:, col] = float("nan")
+    piv = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    size = int(nat.lib().mbem_lu_workspace_size(n, sms))
+    work = torch.empty(size, dtype=torch.uint8, device="cuda")
+    nat.call("mbem_lu_factor_f32", ptr(A), A.stride(0), n, ptr(piv), ptr(work), size, ptr(info), stream_handle())
+    torch.cuda.synchronize()
+    assert int(info.item()) == col + 1
+    p = piv.cpu().numpy()
+    assert p[col] == col
+    assert np.all(p >= np.arange(n)) and np.all(p < n)
+    # the factorisation through the Python front end refuses it
+    from mbem_gb300.la.lu import Factor
+    B = torch.randn(n, n, dtype=torch.float32, device="cuda")
+    B[:, col] = float("nan")
+    with pytest.raises(np.linalg.LinAlgError):
+        Factor(None, lambda x: x, lu32=B)
+
+
 def test_dense_backend_lu_solve(gpu, cube_small):
     """DenseBackend(lu="gpu"): the bordered deflated system factored on the
     GPU, the same solution as the reference (the golden) and FGMRES."""

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from conftest import rel_err
-from cpu_system import assemble, deflated_solve
+from oracle.cpu_system import assemble, deflated_solve
 from mbem_gb300 import mesh as M
 from mbem_gb300.backends.dense import require_anchor_or_deflate, translation_basis
 from mbem_gb300.cases import cube_fault_model
