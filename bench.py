@@ -55,7 +55,8 @@ WORKLOADS = {
 }
 RTOL = 1e-8
 RESTART = 50
-METRIC = "time-to-solve at 1e-8 rel. residual (FP64 true residual, assembly included)"
+METRIC = ("time-to-solve at 1e-8 rel. residual (true residual of the solved operator, evaluated in FP64; "
+          "assembly included)")
 
 
 def _dist():

@@ -312,6 +312,12 @@ int mbem_lu_solve_many_f32(const float* LU, int64_t lda, int64_t n, const int32_
 void mbem_lu_stats(int timing, double* phase_ms);
 int mbem_lu_solve_f32(const float* LU, int64_t lda, int64_t n, const int32_t* perm, const double* b, double* x,
                       float* xf, void* stream);
+/* x = A^-T b from the same factors (A^T = U^T L^T P): the second product of
+ * the 1-norm condition estimator, which the reference takes from LAPACK's
+ * gecon on its factors or onenormest on single-precision ones
+ * (src/mbem/la/lu.py:241-258). */
+int mbem_lu_solve_t_f32(const float* LU, int64_t lda, int64_t n, const int32_t* perm, const double* b, double* x,
+                        float* xf, void* stream);
 
 /* ---- tile configurations of the tunable kernel families (the autotuner's
  * knobs). Each family has mbem_tune_count() candidates; the choice is

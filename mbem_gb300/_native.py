@@ -200,6 +200,7 @@ _SIGNATURES = {
     "mbem_lu_workspace_size": (c_size_t, [_I, c_int]),
     "mbem_lu_factor_f32": (c_int, [_P, _I, _I, _P, _P, c_size_t, _P, _P]),
     "mbem_lu_solve_f32": (c_int, [_P, _I, _I, _P, _P, _P, _P, _P]),
+    "mbem_lu_solve_t_f32": (c_int, [_P, _I, _I, _P, _P, _P, _P, _P]),
     "mbem_lu_stats": (None, [c_int, POINTER(c_double)]),
     "mbem_lu_solve_many_workspace_size": (c_size_t, [_I, _I]),
     "mbem_lu_solve_many_f32": (c_int, [_P, _I, _I, _P, _P, _I, _I, _P, _I, _P, c_size_t, _P]),

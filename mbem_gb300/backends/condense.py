@@ -27,10 +27,12 @@ from ..model.equations import traction_row_frame
 
 @dataclass
 class FaultCoordinates:
-    """Where one solved fault sits in a ``Condensed`` vector: ``start:stop``
-    holds, node by node over the ``free`` (unlocked) dof nodes, the
-    components along the rows of ``frame`` (strike and dip, or all three with
-    ``allow_opening``) (dense.py:275-302)."""
+    """One FAULT_TRACTION fault's share of the condensed unknowns
+    (dense.py:275-302). Entries ``start`` to ``stop`` of a condensed vector
+    belong to this fault: for each dof node in ``free`` (the nodes that are
+    not locked), in order, its slip measured along each row of ``frame`` for
+    that node. The rows are strike and dip, plus the normal when the fault may
+    open."""
     name: str
     free: np.ndarray            # (n_free,) dof nodes
     frame: np.ndarray           # (n_free, n_comp, 3)
@@ -122,7 +124,7 @@ def condense(asm, refine: bool = True) -> Condensed:
     x0 = torch.zeros(N, dtype=torch.float64, device=dev)
     S = AE[rows_d].clone()
     L = -b[rows_d].clone()
-    cond = float("nan")
+    cond = 1.0
     if rest.numel():
         A_rr = A[rest][:, rest].contiguous()
         fac = Factor(A_rr)
@@ -134,6 +136,13 @@ def condense(asm, refine: bool = True) -> Condensed:
         S = S + A_fr @ X[rest]
         L = L + A_fr @ x0[rest]
         asm.lu_report = dict(fac.report)
+        cond = fac.cond()
         del fac, A_rr
+    # the eliminated block's condition estimate in the report, as the
+    # reference's condense leaves it (dense.py:641)
+    from .dense import DenseSolveReport
+    asm.report = DenseSolveReport(converged=True, iterations=0, true_relres=float("nan"),
+                                  arnoldi_relres=float("nan"), cond_estimate=cond,
+                                  lu=getattr(asm, "lu_report", None))
     return Condensed(S=S.cpu().numpy(), L=L.cpu().numpy(), X=X.cpu().numpy(), x0=x0.cpu().numpy(),
                      faults=tuple(coords), layout=asm.layout, cond_estimate=cond)

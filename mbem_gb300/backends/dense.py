@@ -137,7 +137,20 @@ def translation_basis(layout) -> np.ndarray:
 
 @dataclass
 class DenseSolveReport(SolveReport):
-    """The FGMRES report of a dense GPU solve (``SolveReport`` fields)."""
+    """The report of a dense GPU solve: ``SolveReport`` fields, and for an LU
+    solve the 1-norm condition estimate of the factored operator
+    (dense.py:260-271 ``cond_estimate``; NaN for an FGMRES solve) and the
+    factorisation's report (``lu``)."""
+    cond_estimate: float = float("nan")
+    lu: dict | None = None
+
+
+def warn_condition(cond: float) -> None:
+    """The reference's warning above COND_WARN_THRESHOLD (dense.py:555-562)."""
+    if cond > defaults.COND_WARN_THRESHOLD:
+        warnings.warn(f"dense solve: condition estimate {cond:.2e} exceeds {defaults.COND_WARN_THRESHOLD:.0e}; "
+                      f"the solution may miss the {defaults.SOLUTION_RTOL:.0e} accuracy target (thin panels, "
+                      f"near-fluid material, un-anchored calibrated jump, or discretization resonance)")
 
 
 class AssembledDense:
@@ -151,6 +164,8 @@ class AssembledDense:
             raise ValueError(jump)
         require_anchor_or_deflate(system, jump, deflate)
         require_cuda()
+        from .diagnostics import warn_assembly
+        warn_assembly(system, eps, jump)
         self.fault_drag = _checked_drag(system, fault_drag)
         self.lu = lu
         self._factor = None
@@ -530,8 +545,11 @@ class AssembledDense:
             r[off:off + size].view(-1, 3).sub_(r[off:off + size].view(-1, 3).mean(dim=0))
             pb[off:off + size].view(-1, 3).sub_(pb[off:off + size].view(-1, 3).mean(dim=0))
         rel = float(r.norm() / pb.norm()) if float(pb.norm()) > 0 else 0.0
+        cond = f.cond()
         self.report = DenseSolveReport(converged=rel < max(self.rtol, 1e-12), iterations=int(f.report["passes"]),
-                                       true_relres=rel, arnoldi_relres=float(f.report["left"]))
+                                       true_relres=rel, arnoldi_relres=float(f.report["left"]), cond_estimate=cond,
+                                       lu=dict(f.report))
+        warn_condition(cond)
         self._x = x
         return x
 

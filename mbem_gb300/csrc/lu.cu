@@ -440,6 +440,58 @@ __global__ void lu_widen_kernel(const float* __restrict__ x, int64_t n, double* 
     if (i < n) out[i] = (double)x[i];
 }
 
+// ---- solves with the transpose: A^T = U^T L^T P ------------------------------
+// One diagonal block of U^T w = c (ut = 1: lower, the diagonal of U) or of
+// L^T z = w (ut = 0: upper, unit diagonal), x[r0..r0+nb) in place; the
+// block's triangle is read transposed from LU
+__global__ void lu_tri_block_t_kernel(const float* __restrict__ A, int64_t lda, float* __restrict__ x, int64_t r0,
+                                      int nb, int ut) {
+    __shared__ float xs[LU_NB];
+    __shared__ float T[LU_NB][LU_NB + 1];          // T[r][c] = A[r0 + c][r0 + r]
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) xs[i] = x[r0 + i];
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) T[e % nb][e / nb] = A[(r0 + e / nb) * lda + r0 + e % nb];
+    __syncthreads();
+    const int t = threadIdx.x;
+    if (ut) {
+        for (int c = 0; c < nb; c++) {
+            if (t == c) xs[c] = xs[c] / T[c][c];
+            __syncthreads();
+            if (t > c && t < nb) xs[t] = fmaf(-T[t][c], xs[c], xs[t]);
+            __syncthreads();
+        }
+    } else {
+        for (int c = nb - 1; c > 0; c--) {
+            if (t < c) xs[t] = fmaf(-T[t][c], xs[c], xs[t]);
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) x[r0 + i] = xs[i];
+}
+
+// x[r] -= sum_c A[c0 + c][r] x[c0 + c] for r in [i0, i1): the transposed
+// block's product, one thread a row (a warp reads 32 consecutive columns of
+// each row c0 + c)
+__global__ void lu_gemv_update_t_kernel(const float* __restrict__ A, int64_t lda, float* __restrict__ x, int64_t i0,
+                                        int64_t i1, int64_t c0, int nb) {
+    const int64_t r = i0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= i1) return;
+    float s = 0.0f;
+    for (int c = 0; c < nb; c++) s = fmaf(A[(c0 + c) * lda + r], x[c0 + c], s);
+    x[r] -= s;
+}
+
+__global__ void lu_narrow_kernel(const double* __restrict__ b, int64_t n, float* __restrict__ x) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = (float)b[i];
+}
+
+// out[perm[i]] = x[i]: y = P^T z, widened to FP64
+__global__ void lu_scatter_widen_kernel(const float* __restrict__ x, const int32_t* __restrict__ perm, int64_t n,
+                                        double* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[perm[i]] = (double)x[i];
+}
+
 }  // namespace mbem
 
 using namespace mbem;
@@ -627,6 +679,35 @@ int mbem_lu_solve_f32(const float* LU, int64_t lda, int64_t n, const int32_t* pe
     }
     lu_widen_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(xf, n, x);
     return launch_status("lu_solve", (int)launches + 1);
+}
+
+// x = (P L U)^-T b = P^T L^-T U^-T b for one right-hand side (the
+// condition estimator's second product); arguments as mbem_lu_solve_f32.
+int mbem_lu_solve_t_f32(const float* LU, int64_t lda, int64_t n, const int32_t* perm, const double* b, double* x,
+                        float* xf, void* stream) {
+    MBEM_REQUIRE(LU && perm && b && x && xf && n >= 1 && lda >= n, MBEM_ERR_ARG, "bad LU solve arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    lu_narrow_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(b, n, xf);
+    int64_t launches = 1;
+    // U^T w = b, forward by blocks
+    for (int64_t r0 = 0; r0 < n; r0 += LU_NB) {
+        const int nb = (int)lmin(LU_NB, n - r0);
+        lu_tri_block_t_kernel<<<1, LU_NB, 0, st>>>(LU, lda, xf, r0, nb, 1);
+        if (r0 + nb < n)
+            lu_gemv_update_t_kernel<<<(unsigned)ceil_div(n - r0 - nb, 256), 256, 0, st>>>(LU, lda, xf, r0 + nb, n,
+                                                                                          r0, nb);
+        launches += 2;
+    }
+    // L^T z = w, backward by blocks
+    for (int64_t r0 = ((n - 1) / LU_NB) * LU_NB; r0 >= 0; r0 -= LU_NB) {
+        const int nb = (int)lmin(LU_NB, n - r0);
+        lu_tri_block_t_kernel<<<1, LU_NB, 0, st>>>(LU, lda, xf, r0, nb, 0);
+        if (r0 > 0)
+            lu_gemv_update_t_kernel<<<(unsigned)ceil_div(r0, 256), 256, 0, st>>>(LU, lda, xf, 0, r0, r0, nb);
+        launches += 2;
+    }
+    lu_scatter_widen_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(xf, perm, n, x);
+    return launch_status("lu_solve_t", (int)launches + 1);
 }
 
 size_t mbem_lu_solve_many_workspace_size(int64_t n, int64_t k) {

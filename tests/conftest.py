@@ -85,3 +85,8 @@ def rel_err(a, b) -> float:
     b = np.asarray(b, float)
     scale = np.abs(b).max()
     return float(np.abs(a - b).max() / (scale if scale > 0 else 1.0))
+
+
+@pytest.fixture(scope="session")
+def condense_small():
+    return load_golden("condense_small")

@@ -283,6 +283,45 @@ def make_traction_small(path):
                         drop=drop, A=asm.A, b=asm.b, x_u=sol["u:cube"], x_b=sol["b:fault"])
 
 
+def make_condense_small(path):
+    """``AssembledDense.condense()`` of the reference on an anchored body: a
+    3x3-per-face cube with prescribed (zero) displacement and a 3x3
+    FAULT_TRACTION fault under a shear drop. Two cases: strike and dip
+    enforced with the fault elements at |x| > 0.3 locked ("tangential"), and
+    all three components enforced with no lock ("opening"). Stored per case:
+    S, L, X, x0, the free nodes, the frame rows, the coordinate range and the
+    LAPACK condition estimate of the eliminated block."""
+    import local_box_mesh as lbm  # noqa: F401  (the reference's generators, through reference_cube_model)
+    from mollified_bem import ElasticMaterial
+    from mbem.backends.dense import AssembledDense
+    from mbem.model import BCType, Patch, Region, RegionModel
+    from mbem.model.equations import generate_system
+
+    _, cube, fmesh = reference_cube_model(3, 3, 1.0, 1.0)
+    mat = ElasticMaterial(mu=1.0, lam=1.0)
+    eps = (4.0 / 3) / 2.0
+    cent = fmesh.vertices[fmesh.triangles].mean(axis=1)
+    locked = np.abs(cent[:, 0]) > 0.3
+    out = dict(cube_vertices=cube.vertices, cube_triangles=cube.triangles, fault_vertices=fmesh.vertices,
+               fault_triangles=fmesh.triangles, eps=eps, locked=locked)
+    cases = {"tangential": dict(value=np.array([-1e-3, 0.0, 0.0]), allow_opening=False, locked=locked),
+             "opening": dict(value=np.array([-1e-3, 2e-4, 0.0]), allow_opening=True, locked=None)}
+    for tag, kw in cases.items():
+        t0 = time.time()
+        cube_p = Patch("cube", cube, BCType.PRESCRIBED_DISPLACEMENT, value=np.zeros(3))
+        fault_p = Patch("fault", fmesh, BCType.FAULT_TRACTION, **kw)
+        model = RegionModel([Region("body", mat, [cube_p], np.zeros(3), faults=[fault_p])])
+        asm = AssembledDense(generate_system(model), eps, "direct", jump="calibrated", deflate=False)
+        c = asm.condense()
+        (fc,) = c.faults
+        out.update({f"{tag}_S": c.S, f"{tag}_L": c.L, f"{tag}_X": c.X, f"{tag}_x0": c.x0,
+                    f"{tag}_free": fc.free, f"{tag}_frame": fc.frame, f"{tag}_range": np.array([fc.start, fc.stop]),
+                    f"{tag}_cond": c.cond_estimate, f"{tag}_value": kw["value"],
+                    f"{tag}_x": asm.solve()["b:fault"]})
+        print(f"condense_small {tag}: {time.time() - t0:.1f} s", flush=True)
+    np.savez_compressed(path, **out)
+
+
 def make_volume_small(path):
     """The volume sampler on the small cube + fault system (3 x 3 per face,
     fault 2 x 2, eps = h/2): a padded grid with points outside the body, its
@@ -381,7 +420,8 @@ def make_volume_regions(path):
 
 CASES = {"p0_pairs": make_p0_pairs, "cube_small": make_cube_small,
          "c1_rows": make_c1_rows, "nodal_pairs": make_nodal_pairs,
-         "traction_small": make_traction_small, "volume_small": make_volume_small,
+         "traction_small": make_traction_small, "condense_small": make_condense_small,
+         "volume_small": make_volume_small,
          "volume_regions": make_volume_regions}
 
 if __name__ == "__main__":

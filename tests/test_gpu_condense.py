@@ -90,3 +90,41 @@ def test_drag_solve_equals_condensed_drag(gpu):
         dr.condense()
     with pytest.raises(KeyError):
         AssembledDense(system, eps, jump="calibrated", deflate=False, fault_drag={"cube": 1.0})
+
+
+@pytest.mark.parametrize("tag", ["tangential", "opening"])
+def test_condense_against_reference_golden(gpu, condense_small, tag):
+    """The reference's own ``AssembledDense.condense()`` (dense.py:580-646)
+    on an anchored 3x3-per-face cube with a 3x3 FAULT_TRACTION fault
+    (tests/golden/condense_small.npz): strike and dip with locked elements,
+    and all three components without. The free nodes, frame rows and
+    coordinate ranges equal the reference's exactly; S, L, X and x0 agree to
+    1e-10 of their largest entries; the condensed slip equals the reference's
+    solve."""
+    from mbem_gb300 import mesh as M
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.model import BCType, Patch, Region, RegionModel, generate_system
+    g = condense_small
+    cube = M.cube(3)
+    fault = M.centre_fault(3)
+    assert np.array_equal(cube.vertices, g["cube_vertices"]) and np.array_equal(cube.triangles, g["cube_triangles"])
+    assert np.array_equal(fault.vertices, g["fault_vertices"])
+    locked = g["locked"] if tag == "tangential" else None
+    cube_p = Patch("cube", cube, BCType.PRESCRIBED_DISPLACEMENT, value=np.zeros(3))
+    fault_p = Patch("fault", fault, BCType.FAULT_TRACTION, value=g[f"{tag}_value"],
+                    allow_opening=tag == "opening", locked=locked)
+    model = RegionModel([Region("body", M.ElasticMaterial(1.0, 1.0), [cube_p], np.zeros(3), faults=[fault_p])])
+    eps = float(g["eps"])
+    asm = DenseBackend(jump="calibrated", deflate=False, lu="gpu").assemble(generate_system(model), eps)
+    c = asm.condense()
+    (fc,) = c.faults
+    assert np.array_equal(fc.free, g[f"{tag}_free"])
+    assert [fc.start, fc.stop] == list(g[f"{tag}_range"])
+    assert np.abs(fc.frame - g[f"{tag}_frame"]).max() < 1e-15
+    for key, got in (("S", c.S), ("L", c.L), ("X", c.X), ("x0", c.x0)):
+        ref = g[f"{tag}_{key}"]
+        assert got.shape == ref.shape, key
+        assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max(), key
+    beta = np.linalg.solve(c.S, -c.L)
+    slip = fc.cartesian(beta)
+    assert np.abs(slip - g[f"{tag}_x"]).max() < 1e-9 * np.abs(g[f"{tag}_x"]).max()

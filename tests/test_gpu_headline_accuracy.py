@@ -4,7 +4,9 @@
   their rows of the FP64 operator the GPU backend assembles (the closed form
   of every pair, times the term's sign, plus the calibrated diagonal from the
   full row sums) against the same rows built by the C oracle, which is pinned
-  to the reference's goldens. Tolerance 1e-12 of the rows' largest entry.
+  to the reference's goldens. Tolerance 1e-12 of the rows' largest entry
+  (observed 2.9e-13: the GPU's rewritten pair algebra against the
+  reference's formulation), 1e-11 on the calibrated diagonal blocks.
 - The cube-24 workload (20,736 unknowns) solved through the mixed operator
   with the BF16 inner solve, against the FP64 path on the same system: the
   solutions within the mixed mode's stated 1e-5, and the FP64 operator's own
@@ -47,9 +49,19 @@ def test_cube48_sampled_rows_against_oracle(gpu, oracle):
     sigma = float(model.orientation(model.regions[0], cube))
     ref = term.scale * H
     D = -sigma * H.reshape(64, 3, -1, 3).sum(axis=2)                    # calibrated diagonal
+    diag = np.zeros(ref.shape, dtype=bool)
     for k, c in enumerate(sel):
         ref[3 * k:3 * k + 3, 3 * c:3 * c + 3] += D[k]
-    assert rel_err(got, ref) < 1e-12
+        diag[3 * k:3 * k + 3, 3 * c:3 * c + 3] = True
+    scale = np.abs(ref).max()
+    off = np.abs(got - ref)[~diag].max() / scale
+    # the diagonal blocks hold minus a row sum over 27,648 blocks, taken in
+    # another order on the GPU: rounding of that sum, ~1e-16 x sqrt(82,944)
+    # x the row's sum of magnitudes
+    on = np.abs(got - ref)[diag].max() / scale
+    print(f"cube 48 rows: off-diagonal {off:.2e}, calibrated diagonal {on:.2e} of max")
+    assert off < 1e-12
+    assert on < 1e-11
 
 
 def test_mixed_solution_against_fp64_path_cube24(gpu):
@@ -84,4 +96,6 @@ def test_mixed_solution_against_fp64_path_cube24(gpu):
     print(f"cube 24: mixed vs FP64 solution {diff:.3e}; FP64 operator residual at the mixed solution "
           f"{relres64:.3e}")
     assert diff < 1e-5
-    assert relres64 < 1e-6
+    # FP32 evaluation of the far pairs (~2e-7 relative a block from the
+    # rounding of its ~10 FP32 steps) sets this floor; measured 9.6e-8 at cube 48
+    assert relres64 < 3e-7
