@@ -17,12 +17,12 @@ from . import tri_nodal as tn
 from .tri_nodal import n_nodes  # noqa: F401
 
 
-def _mu_lam(material=None, mu=None, lam=None):
-    if material is not None:
-        return material.mu, material.lam
-    if mu is None or lam is None:
-        raise ValueError("provide either material or (mu, lam)")
-    return mu, lam
+def _material_pair(material=None, mu=None, lam=None):
+    """(mu, lam) from a material, or the pair given directly."""
+    pair = (material.mu, material.lam) if material is not None else (mu, lam)
+    if None in pair:
+        raise ValueError("a basis combination needs a material or both Lame parameters (mu, lam)")
+    return pair
 
 
 def u_coeffs(mu, lam) -> np.ndarray:
@@ -45,135 +45,134 @@ def t_coeffs(mu, lam) -> np.ndarray:
     return np.array([c34 * cL, -cL, blob * cL, c34 * cM, -cM, blob * cM])
 
 
-def _source_arrays(mesh_source):
-    tri_verts = np.asarray(mesh_source.vertices, float)[np.asarray(mesh_source.triangles)]
-    normals, _ = mesh_source.normals_and_areas()
-    return np.ascontiguousarray(tri_verts), np.ascontiguousarray(normals)
-
-
-def _field_points(mesh_or_points):
-    if hasattr(mesh_or_points, "centroids"):
-        return np.ascontiguousarray(mesh_or_points.centroids())
-    return np.ascontiguousarray(np.asarray(mesh_or_points, dtype=float))
-
-
 class MeshArrays:
-    """Assembly-scoped memo of mesh-derived arrays keyed by ``id()`` (the
-    reference's basis.py:91-146 scope rule: never a module cache)."""
+    """Arrays derived from meshes and patches, computed once per object for
+    the life of ONE assembly (the reference's rule, basis.py:91-146): keyed
+    by ``id()``, so an instance must not outlive the meshes it has seen, and
+    is never a module-level cache."""
 
     def __init__(self):
-        self._src: dict = {}
-        self._pts: dict = {}
-        self._coll: dict = {}
+        self._memo: dict = {}
+
+    def _get(self, kind: str, obj, make):
+        key = (kind, id(obj))
+        if key not in self._memo:
+            self._memo[key] = make()
+        return self._memo[key]
 
     def source_arrays(self, mesh_source):
-        key = id(mesh_source)
-        if key not in self._src:
-            self._src[key] = _source_arrays(mesh_source)
-        return self._src[key]
+        """(tri_verts (N, 3, 3), normals (N, 3)), both C-contiguous FP64."""
+        def make():
+            corners = np.take(np.asarray(mesh_source.vertices, float), np.asarray(mesh_source.triangles), axis=0)
+            return np.ascontiguousarray(corners), np.ascontiguousarray(mesh_source.normals_and_areas()[0])
+        return self._get("src", mesh_source, make)
 
     def field_points(self, mesh_or_points):
-        if not hasattr(mesh_or_points, "centroids"):
-            return _field_points(mesh_or_points)
-        key = id(mesh_or_points)
-        if key not in self._pts:
-            self._pts[key] = _field_points(mesh_or_points)
-        return self._pts[key]
+        """A mesh's centroids, or an (N, 3) point array as given."""
+        if hasattr(mesh_or_points, "centroids"):
+            return self._get("pts", mesh_or_points, lambda: np.ascontiguousarray(mesh_or_points.centroids()))
+        return np.ascontiguousarray(np.asarray(mesh_or_points, dtype=float))
 
     def collocation_points(self, patch):
-        key = id(patch)
-        if key not in self._coll:
-            self._coll[key] = np.ascontiguousarray(patch.collocation_points())
-        return self._coll[key]
+        return self._get("coll", patch, lambda: np.ascontiguousarray(patch.collocation_points()))
 
     def collocation_normals(self, patch):
-        key = ("n", id(patch))
-        if key not in self._coll:
-            self._coll[key] = np.ascontiguousarray(patch.collocation_normals())
-        return self._coll[key]
+        return self._get("colln", patch, lambda: np.ascontiguousarray(patch.collocation_normals()))
+
+
+# Barycentric coordinates of the Lagrange nodes in the kernels' node order:
+# P0 the centroid; P1 the vertices v1 v2 v3; P2 the vertices, then the edge
+# midpoints m12 m23 m31 (node k of element s is density row K s + k).
+_NODE_BARY = {
+    0: np.full((1, 3), 1.0 / 3.0),
+    1: np.eye(3),
+    2: np.vstack([np.eye(3), 0.5 * (np.eye(3) + np.roll(np.eye(3), -1, axis=0))]),
+}
+# the vertex pairs of the P2 midpoint nodes
+_MID_PAIRS = ((0, 1), (1, 2), (2, 0))
 
 
 def lagrange_nodes(order: int, shrink: float = 0.0) -> np.ndarray:
-    """Barycentric node coordinates (K, 3) in the kernels' node order (P0
-    centroid; P1 v1 v2 v3; P2 v1 v2 v3 m12 m23 m31), pulled toward the
-    centroid by ``shrink`` (basis.py lagrange_nodes)."""
-    K = n_nodes(order)
-    if order == 0:
-        lam = np.full((1, 3), 1.0 / 3.0)
-    elif order == 1:
-        lam = np.eye(3)
-    else:
-        lam = np.array([[1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0],
-                        [0.5, 0.5, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5]])
+    """(K, 3) barycentric node coordinates, each moved toward the centroid
+    by the fraction ``shrink`` (a collocation point; 0 leaves the nodes)."""
+    if order not in _NODE_BARY:
+        raise ValueError(f"order must be 0, 1 or 2 (got {order!r})")
     t = float(shrink)
-    if t:
-        lam = (1.0 - t) * lam + t / 3.0
-    assert lam.shape == (K, 3)
-    return lam
+    return _NODE_BARY[order] * (1.0 - t) + t / 3.0
 
 
 def lagrange_shape(order: int, lam) -> np.ndarray:
-    """Shape functions N_k (M, K) at barycentric points (M, 3)."""
-    lam = np.atleast_2d(np.asarray(lam, float))
-    l1, l2, l3 = lam[:, 0], lam[:, 1], lam[:, 2]
-    if n_nodes(order) == 1:
-        return np.ones((lam.shape[0], 1))
+    """(M, K) values of the element's shape functions at barycentric points
+    ``lam`` (M, 3): 1 at P0; the coordinates themselves at P1; at P2
+    l_i (2 l_i - 1) on the vertices and 4 l_a l_b on the midpoints."""
+    L = np.atleast_2d(np.asarray(lam, float))
+    if order == 0:
+        return np.ones((L.shape[0], 1))
     if order == 1:
-        return np.stack([l1, l2, l3], axis=1)
-    return np.stack([l1 * (2.0 * l1 - 1.0), l2 * (2.0 * l2 - 1.0), l3 * (2.0 * l3 - 1.0),
-                     4.0 * l1 * l2, 4.0 * l2 * l3, 4.0 * l3 * l1], axis=1)
+        return L.copy()
+    vertex = L * (2.0 * L - 1.0)
+    mid = np.column_stack([4.0 * L[:, i] * L[:, j] for i, j in _MID_PAIRS])
+    return np.hstack([vertex, mid])
 
 
 def as_eps_array(eps, n_source: int) -> np.ndarray:
-    """Promote scalar eps to (N_src,); refuse wrong shapes and non-positive or
-    non-finite entries (basis.py:187-204)."""
-    arr = np.asarray(eps, dtype=float)
-    if arr.ndim == 0:
-        arr = np.full(n_source, float(arr))
-    elif arr.shape != (n_source,):
-        raise ValueError(f"eps array shape {arr.shape} != ({n_source},)")
-    bad = ~(np.isfinite(arr) & (arr > 0.0))
-    if bad.any():
-        raise ValueError(f"eps must be finite and > 0: {int(bad.sum())} bad of {arr.size}, "
-                         f"min = {arr.min()}")
-    return np.ascontiguousarray(arr)
+    """One eps per source element (N_src,): a scalar is repeated. Refused:
+    another length, and any entry that is not a finite positive number (the
+    kernels use eps^2, so a negative eps would pass as |eps| while the
+    eigenstress term that tests eps > 0 vanished; eps = 0 divides by zero
+    in the closed form)."""
+    given = np.asarray(eps, dtype=float)
+    if given.ndim != 0 and given.shape != (n_source,):
+        raise ValueError(f"eps has shape {given.shape}; expected a scalar or ({n_source},), one per source element")
+    arr = np.ascontiguousarray(np.broadcast_to(given, (n_source,)), dtype=float)
+    ok = np.isfinite(arr) & (arr > 0.0)
+    if not ok.all():
+        raise ValueError(f"eps must be finite and > 0 for every source element: {int((~ok).sum())} of "
+                         f"{arr.size} are not (smallest {arr.min()})")
+    return arr
 
 
 def element_sizes(mesh) -> np.ndarray:
-    """Per-triangle size: mean edge length (N_src,)."""
-    tv = np.asarray(mesh.vertices, float)[np.asarray(mesh.triangles)]
-    e = np.stack([tv[:, 1] - tv[:, 0], tv[:, 2] - tv[:, 1], tv[:, 0] - tv[:, 2]])
-    return np.linalg.norm(e, axis=2).mean(axis=0)
+    """(N_src,) size of each triangle: the mean of its three edge lengths."""
+    corners = np.take(np.asarray(mesh.vertices, float), np.asarray(mesh.triangles), axis=0)
+    edges = np.roll(corners, -1, axis=1) - corners
+    return np.sqrt((edges * edges).sum(axis=2)).mean(axis=1)
 
 
 def resolve_eps(eps, mesh) -> np.ndarray:
-    """An eps spec (scalar, (N_src,) array or "auto") for one mesh."""
-    if isinstance(eps, str):
-        if eps != "auto":
-            raise ValueError(f"unknown eps spec {eps!r} (only 'auto')")
+    """(N_src,) eps of one mesh from a spec: a scalar, one value per
+    element, or "auto" (EPS_OVER_H times each element's size, so eps / h
+    stays fixed under grading and refinement)."""
+    if not isinstance(eps, str):
+        return as_eps_array(eps, mesh.n_triangles)
+    if eps == "auto":
         return np.ascontiguousarray(defaults.EPS_OVER_H * element_sizes(mesh))
-    return as_eps_array(eps, mesh.n_triangles)
+    raise ValueError(f"eps spec {eps!r} is not understood: give a number, an array or 'auto'")
 
 
 def resolve_patch_eps(spec, patch) -> np.ndarray:
-    """The eps spec of one patch (a dict is keyed by patch name); on a fault
-    "auto" is the single value FAULT_EPS_OVER_H * min(h) (basis.py:234-258)."""
+    """(N_src,) eps of one patch or fault. A dict spec maps patch names to
+    specs and must hold this patch. On a fault "auto" means ONE width for the
+    whole fault, FAULT_EPS_OVER_H times its smallest element size (a uniform
+    slip smeared unequally would be a source of its own)."""
     from ..model.core import FAULT_KINDS
 
     if isinstance(spec, dict):
-        if patch.name not in spec:
-            raise ValueError(f"eps dict has no entry for patch {patch.name!r} (keys: {sorted(spec)})")
-        spec = spec[patch.name]
-    if isinstance(spec, str) and spec == "auto" and patch.bc in FAULT_KINDS:
-        h = element_sizes(patch.mesh)
-        return np.full(h.size, defaults.FAULT_EPS_OVER_H * float(h.min()))
+        try:
+            spec = spec[patch.name]
+        except KeyError:
+            raise ValueError(f"the eps dict names {sorted(spec)} but not patch {patch.name!r}") from None
+    if patch.bc in FAULT_KINDS and isinstance(spec, str) and spec == "auto":
+        width = defaults.FAULT_EPS_OVER_H * float(element_sizes(patch.mesh).min())
+        return np.full(patch.mesh.n_triangles, width)
     return resolve_eps(spec, patch.mesh)
 
 
 def identity_ids(order: int, n_source: int) -> np.ndarray:
-    """Element-major column ids (N_s, K): ids[s, k] = K s + k."""
+    """(N_src, K) column ids of the discontinuous layout: element s, node k
+    owns column K s + k, the kernels' own order."""
     K = n_nodes(order)
-    return np.ascontiguousarray(np.arange(K * n_source, dtype=np.int64).reshape(n_source, K))
+    return np.ascontiguousarray(np.add.outer(K * np.arange(n_source, dtype=np.int64), np.arange(K, dtype=np.int64)))
 
 
 @dataclass
@@ -182,7 +181,7 @@ class UBasis:
     stack: object
 
     def combine(self, material=None, mu=None, lam=None):
-        c = u_coeffs(*_mu_lam(material, mu, lam))
+        c = u_coeffs(*_material_pair(material, mu, lam))
         return sum(float(ci) * self.stack[i] for i, ci in enumerate(c))
 
 
@@ -192,7 +191,7 @@ class TBasis:
     stack: object
 
     def combine(self, material=None, mu=None, lam=None):
-        c = t_coeffs(*_mu_lam(material, mu, lam))
+        c = t_coeffs(*_material_pair(material, mu, lam))
         return sum(float(ci) * self.stack[i] for i, ci in enumerate(c))
 
 

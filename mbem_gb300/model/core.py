@@ -83,18 +83,21 @@ class Patch:
         self._refuse_degenerate()
 
     def _refuse_degenerate(self) -> None:
-        tv = np.asarray(self.mesh.vertices, float)[np.asarray(self.mesh.triangles)]
-        edges = tv[:, [1, 2, 0], :] - tv
-        L = np.linalg.norm(edges, axis=2).max(axis=1)
-        two_area = np.linalg.norm(np.cross(tv[:, 1] - tv[:, 0], tv[:, 2] - tv[:, 0]), axis=1)
-        h_over_L = two_area / np.where(L > 0.0, L, 1.0) ** 2
-        bad = np.nonzero(h_over_L <= defaults.MIN_TRIANGLE_HEIGHT_OVER_L)[0]
-        if bad.size:
-            worst = int(bad[np.argmin(h_over_L[bad])])
-            raise ValueError(f"patch '{self.name}': {bad.size} of {tv.shape[0]} elements are "
-                             f"degenerate (height / longest edge at or below "
-                             f"{defaults.MIN_TRIANGLE_HEIGHT_OVER_L:g}; worst "
-                             f"{h_over_L[worst]:.1e} at element {worst})")
+        """Collapsed elements are a mesher failure (core.py:227-254): their
+        height over longest edge, 2 area / L_max^2, must exceed
+        MIN_TRIANGLE_HEIGHT_OVER_L, or the kernels have no frame to integrate
+        over and "auto" eps no size."""
+        corners = np.take(np.asarray(self.mesh.vertices, float), np.asarray(self.mesh.triangles), axis=0)
+        sides = np.roll(corners, -1, axis=1) - corners
+        longest2 = (sides * sides).sum(axis=2).max(axis=1)
+        twice_area = np.linalg.norm(np.cross(sides[:, 0], -sides[:, 2]), axis=1)
+        quality = twice_area / np.where(longest2 > 0.0, longest2, 1.0)
+        limit = defaults.MIN_TRIANGLE_HEIGHT_OVER_L
+        flat = np.flatnonzero(quality <= limit)
+        if flat.size:
+            k = int(flat[quality[flat].argmin()])
+            raise ValueError(f"patch '{self.name}' has {flat.size} degenerate element(s) among {quality.size}: "
+                             f"height over longest edge must exceed {limit:g}, element {k} has {quality[k]:.1e}")
 
     # ---- sizes and node tables ----
     @property
@@ -152,36 +155,48 @@ class Patch:
         return lagrange_shape(self.order, lagrange_nodes(self.order, t))
 
     def value_array(self) -> np.ndarray:
-        """The prescribed datum at the dof nodes (n_dofs, 3)."""
-        K = n_nodes(self.order)
-        if self.value is None:
-            v = np.zeros((self.n_nodes, 3))
-        elif callable(self.value):
-            normals, _ = self.mesh.normals_and_areas()
-            try:
-                v = self.value(self.nodes(), np.repeat(normals, K, axis=0))
-            except TypeError:
-                v = self.value(self.nodes())
-            v = np.asarray(v, dtype=float)
-            if v.shape != (self.n_nodes, 3):
-                raise ValueError(f"patch '{self.name}': callable value returned {v.shape}, "
-                                 f"expected {(self.n_nodes, 3)}")
-        else:
-            v = np.asarray(self.value, dtype=float)
-            if not (K > 1 and v.shape == (self.n_nodes, 3)):
-                v = np.broadcast_to(v, (self.n_triangles, 3))
-                if K > 1:
-                    v = np.repeat(v, K, axis=0)
-        v = np.ascontiguousarray(v)
+        """The prescribed datum at the dof nodes (n_dofs, 3) (core.py:355-419):
+        None is zero; a callable is asked at the nodes (with their normals
+        when it takes them); an array is one vector for the patch, one per
+        element (repeated over its nodes) or, at order 1/2, one per node."""
+        v = self._node_values()
         if self.bc is BCType.FAULT_TRACTION and not self.allow_opening:
-            scale = float(np.max(np.abs(v))) if v.size else 0.0
-            if scale:
-                nn = np.abs(np.einsum("ij,ij->i", v, self.collocation_normals())).max()
-                if nn > defaults.TRACTION_VALUE_NORMAL_TOL * scale:
-                    raise ValueError(f"fault '{self.name}': the traction value has a normal "
-                                     f"component ({nn:.2e} against |value| {scale:.2e}) but "
-                                     f"allow_opening=False enforces the tangential components only")
+            self._check_tangential(v)
         return v
+
+    def _node_values(self) -> np.ndarray:
+        K = n_nodes(self.order)
+        want = (self.n_nodes, 3)
+        if self.value is None:
+            return np.zeros(want)
+        if callable(self.value):
+            normals = np.repeat(self.mesh.normals_and_areas()[0], K, axis=0)
+            try:
+                got = self.value(self.nodes(), normals)
+            except TypeError:                 # a callable of the points alone
+                got = self.value(self.nodes())
+            got = np.asarray(got, dtype=float)
+            if got.shape != want:
+                raise ValueError(f"patch '{self.name}': its value callable gave an array of shape {got.shape}; "
+                                 f"one vector per dof node, {want}, is needed")
+            return np.ascontiguousarray(got)
+        given = np.asarray(self.value, dtype=float)
+        if K > 1 and given.shape == want:
+            return np.ascontiguousarray(given)
+        per_element = np.broadcast_to(given, (self.n_triangles, 3))
+        return np.ascontiguousarray(np.repeat(per_element, K, axis=0))
+
+    def _check_tangential(self, v: np.ndarray) -> None:
+        """Without allow_opening only strike and dip are enforced, so a
+        traction value with a normal part would be dropped unseen: refused."""
+        size = float(np.abs(v).max()) if v.size else 0.0
+        if size == 0.0:
+            return
+        normal_part = float(np.abs((v * self.collocation_normals()).sum(axis=1)).max())
+        if normal_part > defaults.TRACTION_VALUE_NORMAL_TOL * size:
+            raise ValueError(f"fault '{self.name}': allow_opening=False enforces only the tangential traction, "
+                             f"but the value has a normal part {normal_part:.2e} (largest entry {size:.2e}); "
+                             f"remove it or set allow_opening=True")
 
     def density(self) -> np.ndarray:
         if self.bc is BCType.FAULT_TRACTION:
@@ -253,16 +268,22 @@ class RegionModel:
         self.validate()
 
     def _infer_sigma(self, region: Region, patch: Patch) -> int:
+        """The sign rule (core.py:713-729): +1 when the patch is seen from
+        the region's probe point with a positive solid angle (outward
+        normals), -1 when negative. A closed patch that does not enclose the
+        probe bounds a cavity: its sign is the opposite of the solid angle it
+        subtends at its own vertex centroid. An override wins."""
         if patch.name in region.orientation_overrides:
             return int(region.orientation_overrides[patch.name])
-        omega = solid_angle_sum(patch.mesh, region.probe_point)
-        if abs(omega) > _CLOSED_THRESHOLD or abs(omega) > _OPEN_FLOOR:
-            return 1 if omega > 0 else -1
-        omega_in = solid_angle_sum(patch.mesh, np.asarray(patch.mesh.vertices).mean(axis=0))
-        if abs(omega_in) < _CLOSED_THRESHOLD:
-            raise ValueError(f"cannot infer orientation of patch '{patch.name}' for region "
-                             f"'{region.name}'; supply orientation_overrides")
-        return -1 if omega_in > 0 else 1
+        seen = solid_angle_sum(patch.mesh, region.probe_point)
+        if abs(seen) > _OPEN_FLOOR:
+            return int(np.sign(seen))
+        from_inside = solid_angle_sum(patch.mesh, np.asarray(patch.mesh.vertices, float).mean(axis=0))
+        if abs(from_inside) >= _CLOSED_THRESHOLD:
+            return -int(np.sign(from_inside))
+        raise ValueError(f"patch '{patch.name}' of region '{region.name}': its orientation cannot be inferred "
+                         f"({seen:.3e} sr from the probe point, and it does not enclose its own vertex centroid); "
+                         f"give it in orientation_overrides")
 
     def orientation(self, region: Region, patch: Patch) -> int:
         """sigma(region, patch): inferred for boundary patches,
@@ -275,38 +296,44 @@ class RegionModel:
         return self._sigma[(region.name, patch.name)]
 
     def validate(self) -> None:
-        names = [r.name for r in self.regions]
-        if len(set(names)) != len(names):
-            raise ValueError("region names must be unique")
-        incidence: dict = {}
+        """The model's consistency (core.py:751-820): unique region names,
+        faults only in Region.faults, every region with something to solve,
+        each boundary patch in one region and each interface in two with
+        opposite signs, and every bounded region closed around its probe."""
+        if len({r.name for r in self.regions}) != len(self.regions):
+            raise ValueError("two regions share a name; region names must be unique")
+        owners: dict = {}
         for r in self.regions:
             if r.is_full_space and not r.faults:
-                raise ValueError(f"region '{r.name}' has neither boundary patches nor faults")
+                raise ValueError(f"region '{r.name}' has no boundary patch and no fault: nothing to solve")
             for p in r.patches:
                 if p.bc in FAULT_KINDS:
-                    raise ValueError(f"patch '{p.name}' is a fault; list it in Region.faults")
-                incidence.setdefault(id(p), []).append(r)
+                    raise ValueError(f"'{p.name}' is a fault ({p.bc.name}): list it in Region.faults")
+                owners.setdefault(id(p), (p, []))[1].append(r)
             for f in r.faults:
                 if f.bc not in FAULT_KINDS:
-                    raise ValueError(f"fault '{f.name}' must be FAULT or FAULT_TRACTION")
+                    raise ValueError(f"'{f.name}' is listed as a fault of '{r.name}' but is {f.bc.name}")
         for r in self.regions:
-            total = 0.0
+            if r.is_full_space:
+                continue
+            closure = 0.0
             for p in r.patches:
-                s = self._infer_sigma(r, p)
-                self._sigma[(r.name, p.name)] = s
-                total += s * solid_angle_sum(p.mesh, r.probe_point)
-            if r.patches and abs(total - 4.0 * np.pi) > 1e-3 * 4.0 * np.pi:
-                raise ValueError(f"region '{r.name}': boundary does not close around its probe "
-                                 f"point (sum sigma Omega = {total:.6f}, expected 4 pi)")
-        for pid, regs in incidence.items():
-            p = next(q for r in regs for q in r.patches if id(q) == pid)
-            if p.bc is BCType.INTERFACE:
-                if len(regs) != 2:
-                    raise ValueError(f"interface '{p.name}' must bound exactly two regions")
-                if self._sigma[(regs[0].name, p.name)] != -self._sigma[(regs[1].name, p.name)]:
-                    raise ValueError(f"interface '{p.name}' gets the same sign from both regions")
-            elif len(regs) != 1:
-                raise ValueError(f"patch '{p.name}' ({p.bc.name}) is shared by {len(regs)} regions")
+                self._sigma[(r.name, p.name)] = self._infer_sigma(r, p)
+                closure += self._sigma[(r.name, p.name)] * solid_angle_sum(p.mesh, r.probe_point)
+            if abs(closure / (4.0 * np.pi) - 1.0) > 1e-3:
+                raise ValueError(f"region '{r.name}' is not closed around its probe point: the signed solid "
+                                 f"angles sum to {closure:.6f} sr, not 4 pi")
+        for p, regs in owners.values():
+            if p.bc is not BCType.INTERFACE:
+                if len(regs) != 1:
+                    raise ValueError(f"{p.bc.name} patch '{p.name}' belongs to {len(regs)} regions; it must "
+                                     f"belong to one")
+                continue
+            if len(regs) != 2:
+                raise ValueError(f"interface '{p.name}' belongs to {len(regs)} regions; it must belong to two")
+            a, b = (self._sigma[(q.name, p.name)] for q in regs)
+            if a != -b:
+                raise ValueError(f"interface '{p.name}' has the same orientation in both of its regions")
 
     def value_of(self, patch: Patch) -> np.ndarray:
         return patch.value_array()

@@ -1,5 +1,5 @@
-"""One launch (or a few) of a hot kernel on a small case, for profilers:
-``python -m mbem_gb300.kernel_cases <case>``.
+"""One launch (or a few) of a hot kernel on a small case, for profilers
+(test tooling, not part of the package): ``python tests/kernel_cases.py <case>``.
 
 tcgemm    the block solver's GEMM: (20,736 x 62,208 BF16) x (62,208 x 256)
 traction  FAULT_TRACTION assembly, cube 16 x 16, fault 12 x 12, dip 60,
@@ -28,18 +28,21 @@ vsample   the mixed readout of the same 40^3 grid after a mixed solve of cube 24
 
 from __future__ import annotations
 
+import os
 import sys
 
 import numpy as np
 import torch
 
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
 
 def run(which: str) -> None:
-    from .backends.dense import DenseBackend
-    from .cases import cube_fault_model, fault_traction_model
-    from .model import generate_system
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.cases import cube_fault_model, fault_traction_model
+    from mbem_gb300.model import generate_system
     if which == "tcgemm":
-        from .la.multirhs import gemm_bf16_t
+        from mbem_gb300.la.multirhs import gemm_bf16_t
         n, k = 20736, 256
         A = torch.randn((n, 3 * n), device="cuda").to(torch.bfloat16)
         X = torch.randn((k, 3 * n), device="cuda").to(torch.bfloat16)
@@ -51,7 +54,7 @@ def run(which: str) -> None:
         asm = DenseBackend(jump="calibrated", deflate=True).assemble(generate_system(model), eps)
         asm.block_jacobi()
     elif which == "dfgemm":
-        from .la.multirhs import BlockSolver
+        from mbem_gb300.la.multirhs import BlockSolver
         model, eps = cube_fault_model(24, 16)
         asm = DenseBackend(jump="calibrated", deflate=True, precision="mixed").assemble(generate_system(model),
                                                                                          eps)
@@ -60,8 +63,8 @@ def run(which: str) -> None:
         for _ in range(2):
             bs.residual(B, B)
     elif which == "nodal":
-        from . import mesh as M
-        from .kernels import tri_nodal as tn
+        from mbem_gb300 import mesh as M
+        from mbem_gb300.kernels import tri_nodal as tn
         fault = M.centre_fault(16)
         tv = fault.tri_verts()
         nrm, _ = fault.normals_and_areas()
@@ -72,7 +75,7 @@ def run(which: str) -> None:
         for _ in range(2):
             tn.elastic_stress_contract(x, tv, nrm, e, d, 1.0, 1.0, order=2)
     elif which in ("mixedmv", "bf16mv"):
-        from .la.mixed import Bf16Inner
+        from mbem_gb300.la.mixed import Bf16Inner
         model, eps = cube_fault_model(24, 16)
         asm = DenseBackend(jump="calibrated", deflate=True, precision="mixed",
                            precond="bf16_inner").assemble(generate_system(model), eps)
@@ -82,7 +85,7 @@ def run(which: str) -> None:
         for _ in range(3):
             (asm.op.matvec if which == "mixedmv" else inner.matvec)(x, out=y)
     elif which in ("mm", "mm16"):
-        from .la.multimesh import MeshBatch, random_cube_batch
+        from mbem_gb300.la.multimesh import MeshBatch, random_cube_batch
         be = DenseBackend(jump="calibrated", deflate=True, precision="mixed",
                           precond="bf16_inner" if which == "mm16" else None)
         systems = [be.assemble(generate_system(m), e)
@@ -95,8 +98,8 @@ def run(which: str) -> None:
         else:
             mb.solve_mixed(rtol=1e-8)
     elif which == "readout":
-        from . import mesh as M
-        from .kernels import tri_nodal as tn
+        from mbem_gb300 import mesh as M
+        from mbem_gb300.kernels import tri_nodal as tn
         fault = M.centre_fault(32)
         tv = fault.tri_verts()
         nrm, _ = fault.normals_and_areas()
@@ -114,27 +117,27 @@ def run(which: str) -> None:
         model, eps = cube_fault_model(24, 16)
         DenseBackend(jump="calibrated", deflate=True, precision="mixed").assemble(generate_system(model), eps)
     elif which == "learned":
-        from .la.learned import LearnedPreconditioner
-        from .la.train_learned import load_default
+        from mbem_gb300.la.learned import LearnedPreconditioner
+        from mbem_gb300.la.train_learned import load_default
         model, eps = fault_traction_model(16, 12, 90.0)
         asm = DenseBackend(jump="calibrated", deflate=True, rtol=1e-8).assemble(generate_system(model), eps)
         pc = LearnedPreconditioner(asm, load_default())
         asm.solve_device(precond=pc)
     elif which == "lu":
-        from .la.lu import Factor
+        from mbem_gb300.la.lu import Factor
         n = 8192
         g = torch.Generator(device="cpu").manual_seed(0)
         A = (torch.randn(n, n, generator=g, dtype=torch.float64)
              + n ** 0.5 * torch.eye(n, dtype=torch.float64)).cuda()
         Factor(A).solve(torch.ones(n, dtype=torch.float64, device="cuda"))
     elif which == "volume":
-        from . import volume as V
+        from mbem_gb300 import volume as V
         model, eps = cube_fault_model(24, 16)
         grid = V.make_grid(model, 4.0 / 40)
         V.classify(model, grid)
         V.clearance(model, grid, eps)
     elif which == "vsample":
-        from . import volume as V
+        from mbem_gb300 import volume as V
         model, eps = cube_fault_model(24, 16)
         sol = DenseBackend(jump="calibrated", deflate=True, rtol=1e-8, precision="mixed",
                            precond="bf16_inner").assemble(generate_system(model), eps).solve()

@@ -1,5 +1,5 @@
 """The profile summaries cite commands that still run: every
-``python -m mbem_gb300.kernel_cases <case>`` names a case the module
+``python tests/kernel_cases.py <case>`` names a case the script
 handles, every ``bench.py`` flag is one bench.py accepts, and every summary
 gives its command (no GPU)."""
 
@@ -23,11 +23,11 @@ def test_every_summary_gives_a_command():
 
 
 def test_cited_kernel_cases_exist():
-    src = open(os.path.join(ROOT, "mbem_gb300", "kernel_cases.py")).read()
+    src = open(os.path.join(ROOT, "tests", "kernel_cases.py")).read()
     known = set(re.findall(r'which == "([a-z0-9]+)"', src)) | set(re.findall(r'which in \(([^)]*)\)', src))
     known = {k.strip(' "') for item in known for k in item.split(",")}
     for name, text in _summaries().items():
-        for case in re.findall(r"mbem_gb300\.kernel_cases ([a-z0-9]+)", text):
+        for case in re.findall(r"tests/kernel_cases\.py ([a-z0-9]+)", text):
             assert case in known, f"{name}: kernel case {case!r} is not in kernel_cases.py"
 
 
