@@ -279,6 +279,10 @@ typedef struct {
     const int64_t* u_ranges;
     void* work;                     /* mbem_inner_bf16_workspace_size(n, iterations) bytes */
     size_t work_bytes;
+    int precond;                    /* 0: none; 1: block-Jacobi, 2: learned two-level (as in
+                                       mbem_fgmres_params), a fixed right preconditioner M of the
+                                       inner GMRES: steps on A16 M, result z = P M (V y) */
+    const void* precond_state;      /* mbem_block_jacobi* / mbem_nn_precond* (host pointer) */
 } mbem_inner_bf16;
 size_t mbem_inner_bf16_workspace_size(int64_t n, int iterations);
 int mbem_inner_bf16_apply(const mbem_inner_bf16* p, const double* r, double* z, void* stream);
@@ -447,8 +451,28 @@ typedef struct {
     const double* APhi;              /* (n, n_coarse) device: A Phi, written by mbem_nn_setup_dense */
     const double* Ac_inv;            /* (n_coarse, n_coarse) device: A_c^-1, written by the setup */
     double* work;                    /* mbem_nn_apply_workspace_size() bytes, device */
+    const float* APhi32;             /* or (n, ld32) FP32 A Phi and (n_coarse, ld32) FP32 A_c^-1 (written by */
+    const float* Ac_inv32;           /* mbem_nn_setup_mixed; APhi and Ac_inv NULL then) */
+    int64_t ld32;                    /* their leading dimension: >= n_coarse, a multiple of 4 */
 } mbem_nn_precond;
 
+/* M (n x n, row-major FP32 at ld >= n, device) = M^-1 in place: Gauss-Jordan with
+ * partial pivoting, 16 pivot columns a step (a one-CTA panel, then one
+ * rank-16 update of the other columns); n <= 3418 (the panel lives in shared
+ * memory). MBEM_ERR_NUMERIC when a column has no usable pivot. Synchronises
+ * `stream`. No counterpart in the reference (it solves its small systems with
+ * LAPACK on the host). */
+/* The learned preconditioner on the mixed operator: A Phi (FP32) from the
+ * BF16 inner operator (its A16 far field and FP64 near blocks), A_c = Phi^T A
+ * Phi (+ U U^T from `shift`, n_shift columns, for a calibrated system's
+ * translation null space) and A_c^-1 by mbem_dense_inverse_f32. Requires
+ * nn->APhi32 (n x ld32) and nn->Ac_inv32 (n_coarse x ld32); work: at least
+ * mbem_dense_inverse_f32_workspace_size(n_coarse) bytes. Synchronises
+ * `stream`. No counterpart in the reference. */
+int mbem_nn_setup_mixed(const mbem_inner_bf16* inner, const mbem_nn_precond* nn, const double* shift, int n_shift,
+                        void* work, size_t work_bytes, void* stream);
+size_t mbem_dense_inverse_f32_workspace_size(int64_t n);
+int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t work_bytes, void* stream);
 /* out (n_items, 9) = MLP(feat (n_items, MBEM_NN_FEAT)); act (n_items, 2H)
  * keeps the hidden activations for training (NULL at inference). */
 int mbem_nn_forward(const float* feat, int64_t n_items, const float* params, float* act, float* out,

@@ -69,13 +69,15 @@ BJ_MAX_DOF = 225
 
 class NnPrecond(Structure):
     _fields_ = [("n", c_int64), ("n_coarse", c_int64), ("bj", POINTER(BlockJacobi)), ("basis", c_void_p),
-                ("APhi", c_void_p), ("Ac_inv", c_void_p), ("work", c_void_p)]
+                ("APhi", c_void_p), ("Ac_inv", c_void_p), ("work", c_void_p), ("APhi32", c_void_p),
+                ("Ac_inv32", c_void_p), ("ld32", c_int64)]
 
 
 class InnerBf16(Structure):
     _fields_ = [("n", c_int64), ("A16", c_void_p), ("ld16", c_int64), ("n_near", c_int),
                 ("near", POINTER(NearBlocks)), ("iterations", c_int), ("rtol", c_double), ("n_u_ranges", c_int),
-                ("u_ranges", c_void_p), ("work", c_void_p), ("work_bytes", c_size_t)]
+                ("u_ranges", c_void_p), ("work", c_void_p), ("work_bytes", c_size_t), ("precond", c_int),
+                ("precond_state", c_void_p)]
 
 
 INNER_MAX_ITERS = 64
@@ -200,6 +202,9 @@ _SIGNATURES = {
     "mbem_lu_workspace_size": (c_size_t, [_I, c_int]),
     "mbem_lu_factor_f32": (c_int, [_P, _I, _I, _P, _P, c_size_t, _P, _P]),
     "mbem_lu_solve_f32": (c_int, [_P, _I, _I, _P, _P, _P, _P, _P]),
+    "mbem_nn_setup_mixed": (c_int, [_P, _P, _P, c_int, _P, c_size_t, _P]),
+    "mbem_dense_inverse_f32_workspace_size": (c_size_t, [_I]),
+    "mbem_dense_inverse_f32": (c_int, [_P, _I, _I, _P, c_size_t, _P]),
     "mbem_lu_solve_t_f32": (c_int, [_P, _I, _I, _P, _P, _P, _P, _P]),
     "mbem_lu_stats": (None, [c_int, POINTER(c_double)]),
     "mbem_lu_solve_many_workspace_size": (c_size_t, [_I, _I]),

@@ -48,6 +48,9 @@ class DenseBackend:
         block-Jacobi, built on first solve) or, with ``precision="mixed"``,
         "bf16_inner" (a few GMRES steps on the far field rounded to BF16 as a
         flexible preconditioner; the outer FGMRES keeps the FP32 operator).
+        "bf16_learned" adds to that inner solve, as its right preconditioner,
+        the learned two-level preconditioner (block-Jacobi with the learned
+        coarse space, ``la.learned``) set up on the BF16 inner operator.
         ``precision="fp64"``: every entry by the FP64 closed form, the
         reference's operator. ``"mixed"``: pairs beyond near_factor *
         max(eps, h) of the source by FP32 quadrature (stored FP32), the near
@@ -73,10 +76,11 @@ class DenseBackend:
         self.maxiter = maxiter
         self.precision = precision
         self.near_factor = near_factor
-        if precond not in (None, "block_jacobi", "bf16_inner"):
-            raise ValueError(f"precond must be None, 'block_jacobi' or 'bf16_inner' (got {precond!r})")
-        if precond == "bf16_inner" and precision != "mixed":
-            raise ValueError("precond='bf16_inner' needs precision='mixed'")
+        if precond not in (None, "block_jacobi", "bf16_inner", "bf16_learned"):
+            raise ValueError(f"precond must be None, 'block_jacobi', 'bf16_inner' or 'bf16_learned' "
+                             f"(got {precond!r})")
+        if precond in ("bf16_inner", "bf16_learned") and precision != "mixed":
+            raise ValueError(f"precond={precond!r} needs precision='mixed'")
         self.precond = precond
 
     def assemble(self, system: BlockSystem, eps, arrays: dict | None = None,
@@ -271,7 +275,7 @@ class AssembledDense:
         A32 = _f32_matrix(n, n, dev, zero=covered != n * n)
         # the BF16 inner operator's copy, written by the same far-field pass
         A16 = (alloc((n, (n + 7) // 8 * 8), dtype=torch.bfloat16, device=dev)
-               if self.precond == "bf16_inner" else None)
+               if self.precond in ("bf16_inner", "bf16_learned") else None)
         op = MixedOperator(A32, [], A16)
         placed = {}
         for t in self.system.terms:
@@ -474,6 +478,17 @@ class AssembledDense:
         self._inner.rtol = float(tol)
         return self._inner
 
+    def bf16_learned(self, params=None):
+        """The BF16 inner solve with the learned two-level preconditioner of
+        its operator as right preconditioner (set up once per assembly)."""
+        from ..la.learned import LearnedPreconditioner
+        from ..la.train_learned import load_default
+        inner = self.bf16_inner()
+        if getattr(self, "_learned", None) is None or params is not None:
+            self._learned = LearnedPreconditioner(self, load_default() if params is None else params)
+        inner.set_preconditioner(self._learned)
+        return inner
+
     def rebuild_for_materials(self, material_map: dict, fault_drag: dict | None = None) -> "AssembledDense":
         """A new AssembledDense of the same model with updated region
         materials (dense.py:650-688): ``material_map`` maps region name ->
@@ -490,7 +505,7 @@ class AssembledDense:
         new.fault_drag = self.fault_drag if fault_drag is None else _checked_drag(self.system, fault_drag)
         new.report = None
         new.A = new.b = new.op = new._x = None
-        new._bj = new._inner = new._factor = None
+        new._bj = new._inner = new._factor = new._learned = None
         new.calib = None
         new._build()
         return new
@@ -569,6 +584,9 @@ class AssembledDense:
             precond = self.block_jacobi()
         elif precond == "bf16_inner":
             precond = self.bf16_inner()
+            precond.set_preconditioner(None)
+        elif precond == "bf16_learned":
+            precond = self.bf16_learned()
         kw = dict(x0=x0, rtol=self.rtol if rtol is None else rtol,
                   restart=self.restart if restart is None else restart,
                   maxiter=self.maxiter if maxiter is None else maxiter, u_ranges=self.u_ranges(),

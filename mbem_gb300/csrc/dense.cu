@@ -494,6 +494,7 @@ struct InnerWork {
     double* y;        // k
     float* xf;        // n
     double* proj;     // 3 * PROJ_BLOCKS
+    double* t;        // n: M v_j (right preconditioner), then V y
 };
 
 static size_t inner_layout(int64_t n, int k, char* base, InnerWork* w) {
@@ -513,6 +514,7 @@ static size_t inner_layout(int64_t n, int k, char* base, InnerWork* w) {
     t.y = take(k);
     t.xf = reinterpret_cast<float*>(take((n + 1) / 2));
     t.proj = take(3 * PROJ_BLOCKS);
+    t.t = take(n);
     if (w) *w = t;
     return off;
 }
@@ -524,6 +526,8 @@ int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t
     MBEM_REQUIRE(k >= 1 && k <= MBEM_INNER_MAX_ITERS, MBEM_ERR_ARG, "inner iterations must be in [1, %d]",
                  MBEM_INNER_MAX_ITERS);
     MBEM_REQUIRE(p->rtol >= 0.0 && p->rtol < 1.0, MBEM_ERR_ARG, "inner rtol must be in [0, 1)");
+    MBEM_REQUIRE(p->precond == 0 || ((p->precond == 1 || p->precond == 2) && p->precond_state != nullptr),
+                 MBEM_ERR_ARG, "inner preconditioner must be 0, or 1 / 2 with a state");
     const int64_t n = p->n;
     const size_t need = inner_layout(n, k, nullptr, nullptr);
     MBEM_REQUIRE(p->work && p->work_bytes >= need, MBEM_ERR_SIZE, "inner workspace %zu < %zu bytes",
@@ -585,6 +589,12 @@ int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t
     for (int j = 0; j < k; j++) {
         const double* vj = I.V + (int64_t)j * n;
         double* hc = I.H + (size_t)j * ldh;
+        if (p->precond) {
+            // right preconditioning: the step multiplies A16 by P M v_j
+            if ((e = precond_apply(p->precond, p->precond_state, vj, I.t, st))) return e;
+            if ((e = F.proj(I.t, I.t))) return e;
+            vj = I.t;
+        }
         if (g_inner_timing) {
             cudaEvent_t ev[2];
             cudaEventCreate(&ev[0]);
@@ -637,7 +647,15 @@ int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t
     g_inner_matvec_ms += F.matvec_ms;
     if (used == 0) return launch_status("inner solve", 0);
     cudaMemcpyAsync(I.y, y.data(), used * sizeof(double), cudaMemcpyHostToDevice, st);
-    if ((e = F.multiaxpy(z, I.V, used, I.y, 1.0))) return e;
+    if (p->precond) {
+        // z = P M (V y)
+        cudaMemsetAsync(I.w, 0, n * sizeof(double), st);
+        if ((e = F.multiaxpy(I.w, I.V, used, I.y, 1.0))) return e;
+        if ((e = precond_apply(p->precond, p->precond_state, I.w, z, st))) return e;
+        if ((e = F.proj(z, z))) return e;
+    } else if ((e = F.multiaxpy(z, I.V, used, I.y, 1.0))) {
+        return e;
+    }
     // the host vector y must outlive the copy
     if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
     return launch_status("inner solve", 0);

@@ -455,6 +455,274 @@ __global__ void gj_swap_columns_kernel(double* __restrict__ M, int64_t m, const 
 }
 
 // ---------------------------------------------------------------------------
+// A Phi for the BF16 inner operator of the mixed solve (A16 far field plus
+// its FP64 near blocks), stored FP32 at ldp: a CTA per (group of
+// APHI16_GROUP chunks, APHI16_ROWS rows) holds the group's columns and basis
+// rows in shared memory and a warp per row gathers the row's entries on
+// those columns, chunk by chunk (each chunk's columns ascending, so a warp's
+// loads run along the mesh's element runs); every APhi entry has one writer.
+// The near blocks follow as FP32 atomic adds (nn_aphi_near_kernel).
+// ---------------------------------------------------------------------------
+constexpr int APHI16_GROUP = 8, APHI16_ROWS = 128;
+
+__global__ void __launch_bounds__(256)
+nn_aphi_bf16_kernel(const uint16_t* __restrict__ A16, int64_t ld16, int64_t n, const int64_t* __restrict__ chunk_ptr,
+                    const int64_t* __restrict__ dofs, int64_t n_chunks, const float* __restrict__ basis,
+                    float* __restrict__ APhi, int64_t ldp) {
+    extern __shared__ float gsm[];
+    const int64_t cb = (int64_t)blockIdx.x * APHI16_GROUP;
+    const int64_t ce = lmin(n_chunks, cb + APHI16_GROUP);
+    const int64_t d0 = chunk_ptr[cb];
+    const int m = (int)(chunk_ptr[ce] - d0);
+    float* bs = gsm;                                            // [m][NCV]
+    int* col = reinterpret_cast<int*>(gsm + (size_t)m * NCV);   // [m]
+    for (int t = threadIdx.x; t < m; t += 256) {
+        const int64_t d = dofs[d0 + t];
+        col[t] = (int)d;
+#pragma unroll
+        for (int k = 0; k < NCV; k++) bs[t * NCV + k] = basis[d * NCV + k];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t r1 = lmin(n, ((int64_t)blockIdx.y + 1) * APHI16_ROWS);
+    for (int64_t r = (int64_t)blockIdx.y * APHI16_ROWS + warp; r < r1; r += 8) {
+        const uint16_t* Ar = A16 + r * ld16;
+        for (int64_t c = cb; c < ce; c++) {
+            const int lo = (int)(chunk_ptr[c] - d0), hi = (int)(chunk_ptr[c + 1] - d0);
+            float acc[NCV] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int t = lo + lane; t < hi; t += 32) {
+                const float v = __uint_as_float((uint32_t)Ar[col[t]] << 16);
+#pragma unroll
+                for (int k = 0; k < NCV; k++) acc[k] = fmaf(v, bs[t * NCV + k], acc[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < NCV; k++)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+            if (lane < NCV) {
+                float v = acc[0];
+#pragma unroll
+                for (int k = 1; k < NCV; k++) v = lane == k ? acc[k] : v;
+                APhi[r * ldp + NCV * c + lane] = v;
+            }
+        }
+    }
+}
+
+// APhi[row0 + 3f + i, 6 c(s) + k] += sum_j vals[e][i][j] basis[col0 + 3s + j][k]
+// for every near block e = (f, s) of one list; a warp per field point
+__global__ void __launch_bounds__(256)
+nn_aphi_near_kernel(mbem_near_blocks nb, const int32_t* __restrict__ chunk_of, const float* __restrict__ basis,
+                    float* __restrict__ APhi, int64_t ldp) {
+    const int64_t f = ((int64_t)blockIdx.x * 256 + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (f >= nb.n_field) return;
+    for (int64_t e = nb.rowptr[f] + lane; e < nb.rowptr[f + 1]; e += 32) {
+        const int64_t d = nb.col0 + 3 * nb.cols[e];
+        const int64_t c = chunk_of[d];
+        const double* v = nb.vals + 9 * e;
+        for (int i = 0; i < 3; i++) {
+            float* out = APhi + (nb.row0 + 3 * f + i) * ldp + NCV * c;
+#pragma unroll
+            for (int k = 0; k < NCV; k++) {
+                const double s = v[3 * i] * basis[d * NCV + k] + v[3 * i + 1] * basis[(d + 1) * NCV + k] +
+                                 v[3 * i + 2] * basis[(d + 2) * NCV + k];
+                atomicAdd(out + k, (float)s);
+            }
+        }
+    }
+}
+
+// Ac[6c + k, q] = sum_{d in c} basis[d][k] APhi[d, q] from the FP32 A Phi;
+// a CTA per (chunk, 256 columns), a thread per column, FP32 output at ldc
+__global__ void __launch_bounds__(256)
+nn_coarse_matrix_f32_kernel(const float* __restrict__ APhi, int64_t ldp, int64_t n_coarse,
+                            const int64_t* __restrict__ chunk_ptr, const int64_t* __restrict__ dofs,
+                            const float* __restrict__ basis, float* __restrict__ Ac, int64_t ldc) {
+    const int c = blockIdx.x;
+    const int64_t q = (int64_t)blockIdx.y * 256 + threadIdx.x;
+    if (q >= n_coarse) return;
+    const int64_t c0 = chunk_ptr[c];
+    const int m = (int)(chunk_ptr[c + 1] - c0);
+    double s[NCV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int t = 0; t < m; t++) {
+        const int64_t d = dofs[c0 + t];
+        const double v = APhi[d * ldp + q];
+#pragma unroll
+        for (int k = 0; k < NCV; k++) s[k] += (double)basis[d * NCV + k] * v;
+    }
+    for (int k = 0; k < NCV; k++) Ac[(NCV * c + k) * ldc + q] = (float)s[k];
+}
+
+// Ac[p, q] += sum_j U[p, j] U[q, j] (FP32 coarse matrix at ldc)
+__global__ void nn_coarse_shift_f32_kernel(float* __restrict__ Ac, int64_t ldc, int64_t nc,
+                                           const double* __restrict__ U, int n_shift) {
+    const int64_t p = blockIdx.y;
+    const int64_t q = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (q >= nc) return;
+    double s = 0.0;
+    for (int j = 0; j < n_shift; j++) s += U[p * n_shift + j] * U[q * n_shift + j];
+    Ac[p * ldc + q] += (float)s;
+}
+
+// out[i] = a[i] - b[i]
+__global__ void nn_sub_kernel(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out,
+                              int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (i < n) out[i] = a[i] - b[i];
+}
+
+// ---------------------------------------------------------------------------
+// Blocked Gauss-Jordan inverse in FP32 (the coarse matrix of the mixed-operator
+// preconditioner). Pivot columns are taken GJB_BLOCK at a time:
+//  - the panel kernel (one CTA, the panel's n x b values in shared memory)
+//    runs the b pivot steps with partial pivoting over the rows not yet used
+//    as pivots; the panel then holds, in GJ form, [B^-1 ; -A_RB B^-1] for
+//    the pivot rows B and the other rows R;
+//  - the swap kernel applies the b row interchanges to every other column
+//    and copies the pivot rows X_B aside;
+//  - the update kernel: X_B <- B^-1 X_B, X_R <- X_R + (-A_RB B^-1) X_B, i.e.
+//    every row gets P[i, :] X_B (pivot rows replaced, others added to).
+// The column interchanges are undone at the end (gj_swap_columns_f32_kernel).
+// A column with no usable pivot (all zero or NaN) sets *bad.
+// ---------------------------------------------------------------------------
+constexpr int GJB_BLOCK = 16;
+constexpr int GJB_PANEL_THREADS = 1024;
+
+__global__ void __launch_bounds__(GJB_PANEL_THREADS)
+gjb_panel_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b, int* __restrict__ piv,
+                 int* __restrict__ bad) {
+    extern __shared__ float P[];                  // [n][GJB_BLOCK], then the column's factors f[n]
+    float* fcol = P + n * GJB_BLOCK;
+    __shared__ float rv[GJB_PANEL_THREADS / 32];
+    __shared__ int ri[GJB_PANEL_THREADS / 32];
+    __shared__ int s_p;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int64_t e = tid; e < n * GJB_BLOCK; e += GJB_PANEL_THREADS) {
+        const int64_t i = e / GJB_BLOCK;
+        const int c = (int)(e % GJB_BLOCK);
+        P[e] = c < b ? M[i * ld + k0 + c] : 0.0f;
+    }
+    __syncthreads();
+    for (int t = 0; t < b; t++) {
+        const int64_t k = k0 + t;
+        float bv = -1.0f;
+        int bi = -1;
+        for (int64_t i = k + tid; i < n; i += GJB_PANEL_THREADS) {
+            const float v = fabsf(P[i * GJB_BLOCK + t]);
+            if (v > bv) { bv = v; bi = (int)i; }           // NaN never wins
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > bv || (ov == bv && oi >= 0 && (bi < 0 || oi < bi))) { bv = ov; bi = oi; }
+        }
+        if (lane == 0) { rv[wid] = bv; ri[wid] = bi; }
+        __syncthreads();
+        if (tid == 0) {
+            float v = rv[0];
+            int i0 = ri[0];
+            for (int w = 1; w < GJB_PANEL_THREADS / 32; w++)
+                if (rv[w] > v || (rv[w] == v && ri[w] >= 0 && (i0 < 0 || ri[w] < i0))) { v = rv[w]; i0 = ri[w]; }
+            if (i0 < 0 || !(v > 0.0f)) {
+                atomicExch(bad, 1);
+                i0 = (int)k;
+            }
+            s_p = i0;
+            piv[k] = i0;
+        }
+        __syncthreads();
+        const int64_t p = s_p;
+        if (p != k && tid < GJB_BLOCK) {
+            const float a = P[k * GJB_BLOCK + tid];
+            P[k * GJB_BLOCK + tid] = P[p * GJB_BLOCK + tid];
+            P[p * GJB_BLOCK + tid] = a;
+        }
+        __syncthreads();
+        const float pv = P[k * GJB_BLOCK + t];
+        const float inv = pv != 0.0f ? 1.0f / pv : 0.0f;
+        __syncthreads();
+        if (tid < GJB_BLOCK) P[k * GJB_BLOCK + tid] = (tid == t) ? inv : P[k * GJB_BLOCK + tid] * inv;
+        // every row's factor read before any row is changed
+        for (int64_t i = tid; i < n; i += GJB_PANEL_THREADS) fcol[i] = P[i * GJB_BLOCK + t];
+        __syncthreads();
+        for (int64_t e = tid; e < n * GJB_BLOCK; e += GJB_PANEL_THREADS) {
+            const int64_t i = e / GJB_BLOCK;
+            const int c = (int)(e % GJB_BLOCK);
+            if (i == k) continue;
+            const float f = fcol[i];
+            P[e] = (c == t) ? -f * inv : fmaf(-f, P[k * GJB_BLOCK + c], P[e]);
+        }
+        __syncthreads();
+    }
+    for (int64_t e = tid; e < n * GJB_BLOCK; e += GJB_PANEL_THREADS) {
+        const int64_t i = e / GJB_BLOCK;
+        const int c = (int)(e % GJB_BLOCK);
+        if (c < b) M[i * ld + k0 + c] = P[e];
+    }
+}
+
+// the panel's row interchanges on every other column, then X_B (b x n) aside
+__global__ void gjb_swap_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b,
+                                const int* __restrict__ piv, float* __restrict__ XB) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n || (j >= k0 && j < k0 + b)) return;
+    for (int t = 0; t < b; t++) {
+        const int64_t p = piv[k0 + t];
+        if (p != k0 + t && p > k0 + t && p < n) {
+            const float a = M[(k0 + t) * ld + j];
+            M[(k0 + t) * ld + j] = M[p * ld + j];
+            M[p * ld + j] = a;
+        }
+    }
+    for (int t = 0; t < b; t++) XB[(int64_t)t * n + j] = M[(k0 + t) * ld + j];
+}
+
+// M[i, j] = (i pivot row ? 0 : M[i, j]) + sum_t P[i, t] XB[t, j] for every
+// column j outside the panel; a CTA per 32 rows x 128 columns
+constexpr int GJB_TR = 32, GJB_TC = 128;
+__global__ void __launch_bounds__(256)
+gjb_update_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b, const float* __restrict__ XB) {
+    __shared__ float Ps[GJB_TR][GJB_BLOCK];
+    __shared__ float Xs[GJB_BLOCK][GJB_TC];
+    const int64_t i0 = (int64_t)blockIdx.y * GJB_TR, j0 = (int64_t)blockIdx.x * GJB_TC;
+    for (int e = threadIdx.x; e < GJB_TR * GJB_BLOCK; e += 256) {
+        const int r = e / GJB_BLOCK, t = e % GJB_BLOCK;
+        Ps[r][t] = (i0 + r < n && t < b) ? M[(i0 + r) * ld + k0 + t] : 0.0f;
+    }
+    for (int e = threadIdx.x; e < GJB_BLOCK * GJB_TC; e += 256) {
+        const int t = e / GJB_TC, c = e % GJB_TC;
+        Xs[t][c] = (t < b && j0 + c < n) ? XB[(int64_t)t * n + j0 + c] : 0.0f;
+    }
+    __syncthreads();
+    const int c = threadIdx.x % GJB_TC;
+    const int64_t j = j0 + c;
+    if (j >= n || (j >= k0 && j < k0 + b)) return;
+    for (int r = threadIdx.x / GJB_TC; r < GJB_TR; r += 256 / GJB_TC) {
+        const int64_t i = i0 + r;
+        if (i >= n) break;
+        float acc = (i >= k0 && i < k0 + b) ? 0.0f : M[i * ld + j];
+#pragma unroll
+        for (int t = 0; t < GJB_BLOCK; t++) acc = fmaf(Ps[r][t], Xs[t][c], acc);
+        M[i * ld + j] = acc;
+    }
+}
+
+__global__ void gj_swap_columns_f32_kernel(float* __restrict__ M, int64_t m, int64_t ld, const int* __restrict__ piv) {
+    const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (i >= m) return;
+    for (int64_t k = m - 1; k >= 0; k--) {
+        const int64_t p = piv[k];
+        if (p != k && p >= 0 && p < m) {
+            const float t = M[i * ld + k];
+            M[i * ld + k] = M[i * ld + p];
+            M[i * ld + p] = t;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // apply pieces
 // ---------------------------------------------------------------------------
 // q[6c + k] = sum_{d in c} basis[d][k] r[d]; a CTA per chunk
@@ -552,8 +820,11 @@ static int nn_check(const mbem_nn_precond* nn) {
     MBEM_REQUIRE(nn->n == nn->bj->n && nn->n_coarse == NCV * nn->bj->n_chunks && nn->n % 3 == 0, MBEM_ERR_ARG,
                  "learned preconditioner sizes (n=%lld, coarse=%lld, chunks=%lld)", (long long)nn->n,
                  (long long)nn->n_coarse, (long long)nn->bj->n_chunks);
-    MBEM_REQUIRE(nn->n == 0 || (nn->basis && nn->APhi && nn->Ac_inv && nn->work && nn->bj->chunk_of), MBEM_ERR_ARG,
+    const bool f64 = nn->APhi && nn->Ac_inv, f32 = nn->APhi32 && nn->Ac_inv32;
+    MBEM_REQUIRE(nn->n == 0 || (nn->basis && (f64 || f32) && nn->work && nn->bj->chunk_of), MBEM_ERR_ARG,
                  "NULL learned preconditioner arrays");
+    MBEM_REQUIRE(!f32 || (nn->ld32 >= nn->n_coarse && nn->ld32 % 4 == 0), MBEM_ERR_ARG,
+                 "FP32 coarse arrays need ld32 >= n_coarse, a multiple of 4");
     return MBEM_OK;
 }
 
@@ -570,9 +841,23 @@ int nn_precond_apply(const void* state, const double* r, double* z, cudaStream_t
     const mbem_block_jacobi* bj = nn->bj;
     nn_phit_kernel<<<(unsigned)bj->n_chunks, 128, 0, st>>>(bj->chunk_ptr, bj->dofs, nn->basis, r, q);
     if ((e = launch_status("nn_phit_kernel"))) return e;
-    if ((e = dgemv(nn->Ac_inv, nc, nc, nc, q, 1.0, 0.0, y, st))) return e;
-    cudaMemcpyAsync(t, r, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
-    if ((e = dgemv(nn->APhi, nc, n, nc, y, -1.0, 1.0, t, st))) return e;
+    if (nn->APhi32 != nullptr) {
+        // FP32 A Phi and A_c^-1 (the mixed operator's setup): the streaming
+        // FP32 products with double-float sums, scratch after y
+        float* xh = reinterpret_cast<float*>(y + nc);
+        float* xl = xh + ((lmax(n, nc) + 15) / 16) * 16;
+        mbem_mixed_operator op;
+        op.n_rows = nc; op.n_cols = nc; op.A32 = nn->Ac_inv32; op.ld32 = nn->ld32; op.n_near = 0; op.near = nullptr;
+        if ((e = mixed_matvec(&op, q, y, xh, xl, st))) return e;
+        op.n_rows = n; op.A32 = nn->APhi32;
+        if ((e = mixed_matvec(&op, y, t, xh, xl, st))) return e;
+        nn_sub_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(r, t, t, n);
+        if ((e = launch_status("nn_sub_kernel"))) return e;
+    } else {
+        if ((e = dgemv(nn->Ac_inv, nc, nc, nc, q, 1.0, 0.0, y, st))) return e;
+        cudaMemcpyAsync(t, r, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        if ((e = dgemv(nn->APhi, nc, n, nc, y, -1.0, 1.0, t, st))) return e;
+    }
     if ((e = bj_apply(bj, t, z, st))) return e;
     nn_phi_add_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(n, bj->chunk_of, nn->basis, y, z);
     return launch_status("nn_phi_add_kernel");
@@ -693,6 +978,47 @@ int mbem_dense_inverse(double* M, int64_t n, void* work, size_t work_bytes, void
     return MBEM_OK;
 }
 
+size_t mbem_dense_inverse_f32_workspace_size(int64_t n) {
+    return (size_t)GJB_BLOCK * n * sizeof(float) + (size_t)(n + 8) * sizeof(int) + 256;
+}
+
+int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t work_bytes, void* stream) {
+    MBEM_REQUIRE(n >= 0 && ld >= n && (n == 0 || M), MBEM_ERR_ARG, "bad matrix for the inverse");
+    if (n == 0) return MBEM_OK;
+    const size_t panel = (size_t)n * (GJB_BLOCK + 1) * sizeof(float);
+    constexpr size_t kSmem = 227 * 1024;
+    MBEM_REQUIRE(panel <= kSmem && ceil_div(n, GJB_TR) <= 65535, MBEM_ERR_UNSUPPORTED,
+                 "the FP32 inverse holds its n x %d panel in shared memory: n <= %d", GJB_BLOCK,
+                 (int)(kSmem / ((GJB_BLOCK + 1) * sizeof(float))));
+    MBEM_REQUIRE(work && work_bytes >= mbem_dense_inverse_f32_workspace_size(n), MBEM_ERR_SIZE,
+                 "inverse workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    float* XB = static_cast<float*>(work);
+    int* piv = reinterpret_cast<int*>(XB + (size_t)GJB_BLOCK * n);
+    int* bad = piv + n;
+    cudaMemsetAsync(bad, 0, sizeof(int), st);
+    cudaError_t ce = cudaFuncSetAttribute(gjb_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+    if (ce != cudaSuccess) return set_error(MBEM_ERR_CUDA, "inverse smem attribute: %s", cudaGetErrorString(ce));
+    const dim3 ug((unsigned)ceil_div(n, GJB_TC), (unsigned)ceil_div(n, GJB_TR));
+    int launches = 0;
+    for (int64_t k0 = 0; k0 < n; k0 += GJB_BLOCK) {
+        const int b = (int)lmin(GJB_BLOCK, n - k0);
+        gjb_panel_kernel<<<1, GJB_PANEL_THREADS, panel, st>>>(M, n, ld, k0, b, piv, bad);
+        gjb_swap_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(M, n, ld, k0, b, piv, XB);
+        gjb_update_kernel<<<ug, 256, 0, st>>>(M, n, ld, k0, b, XB);
+        launches += 3;
+    }
+    gj_swap_columns_f32_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(M, n, ld, piv);
+    count_launches(launches + 1);
+    int e = launch_status("gauss_jordan_f32");
+    if (e) return e;
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inverse sync", 0);
+    MBEM_REQUIRE(hbad == 0, MBEM_ERR_NUMERIC, "singular matrix");
+    return MBEM_OK;
+}
+
 int mbem_nn_coarse_operator_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift,
                                   int n_shift, void* stream) {
     int e = nn_check(nn);
@@ -730,7 +1056,49 @@ int mbem_nn_setup_dense(const double* A, int64_t ld, const mbem_nn_precond* nn, 
 }
 
 size_t mbem_nn_apply_workspace_size(int64_t n, int64_t n_coarse) {
-    return (size_t)(n + 2 * n_coarse) * sizeof(double);
+    // t (n), q, y (n_coarse) doubles, then the hi/lo split of the FP32 path
+    return (size_t)(n + 2 * n_coarse) * sizeof(double) + 2 * (size_t)((lmax(n, n_coarse) + 15) / 16 * 16) * 4 + 64;
+}
+
+int mbem_nn_setup_mixed(const mbem_inner_bf16* inner, const mbem_nn_precond* nn, const double* shift, int n_shift,
+                        void* work, size_t work_bytes, void* stream) {
+    int e = nn_check(nn);
+    if (e) return e;
+    MBEM_REQUIRE(inner && inner->A16 && inner->n == nn->n && inner->ld16 >= inner->n, MBEM_ERR_ARG,
+                 "bad BF16 inner operator");
+    MBEM_REQUIRE(nn->APhi32 && nn->Ac_inv32, MBEM_ERR_ARG, "the mixed setup writes FP32 APhi32 and Ac_inv32");
+    MBEM_REQUIRE(n_shift >= 0 && (n_shift == 0 || shift != nullptr), MBEM_ERR_ARG, "bad coarse shift");
+    const int64_t n = nn->n, nc = nn->n_coarse, ldp = nn->ld32;
+    if (n == 0) return MBEM_OK;
+    const mbem_block_jacobi* bj = nn->bj;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t groups = ceil_div(bj->n_chunks, APHI16_GROUP);
+    MBEM_REQUIRE(groups <= 65535 * 32 && ceil_div(n, APHI16_ROWS) <= 65535 && nc <= 65535, MBEM_ERR_UNSUPPORTED,
+                 "learned preconditioner sizes beyond one launch");
+    const size_t smem = (size_t)APHI16_GROUP * MBEM_BJ_MAX_DOF * (NCV * sizeof(float) + sizeof(int));
+    cudaError_t ce = cudaFuncSetAttribute(nn_aphi_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (ce != cudaSuccess) return set_error(MBEM_ERR_CUDA, "APhi smem attribute: %s", cudaGetErrorString(ce));
+    float* APhi = const_cast<float*>(nn->APhi32);
+    float* Ac = const_cast<float*>(nn->Ac_inv32);
+    nn_aphi_bf16_kernel<<<dim3((unsigned)groups, (unsigned)ceil_div(n, APHI16_ROWS)), 256, smem, st>>>(
+        inner->A16, inner->ld16, n, bj->chunk_ptr, bj->dofs, bj->n_chunks, nn->basis, APhi, ldp);
+    if ((e = launch_status("nn_aphi_bf16_kernel"))) return e;
+    for (int q = 0; q < inner->n_near; q++) {
+        const mbem_near_blocks& nb = inner->near[q];
+        if (nb.n_field == 0) continue;
+        nn_aphi_near_kernel<<<(unsigned)ceil_div(nb.n_field * 32, 256), 256, 0, st>>>(nb, bj->chunk_of, nn->basis,
+                                                                                    APhi, ldp);
+        if ((e = launch_status("nn_aphi_near_kernel"))) return e;
+    }
+    nn_coarse_matrix_f32_kernel<<<dim3((unsigned)bj->n_chunks, (unsigned)ceil_div(nc, 256)), 256, 0, st>>>(
+        APhi, ldp, nc, bj->chunk_ptr, bj->dofs, nn->basis, Ac, ldp);
+    if ((e = launch_status("nn_coarse_matrix_f32_kernel"))) return e;
+    if (n_shift > 0) {
+        nn_coarse_shift_f32_kernel<<<dim3((unsigned)ceil_div(nc, 256), (unsigned)nc), 256, 0, st>>>(Ac, ldp, nc, shift,
+                                                                                                n_shift);
+        if ((e = launch_status("nn_coarse_shift_f32_kernel"))) return e;
+    }
+    return mbem_dense_inverse_f32(Ac, nc, ldp, work, work_bytes, stream);
 }
 
 int mbem_nn_apply(const mbem_nn_precond* nn, const double* r, double* z, void* stream) {

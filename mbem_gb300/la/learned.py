@@ -149,8 +149,9 @@ class LearnedPreconditioner:
     PRECOND_KIND = 2
 
     def __init__(self, asm, params, bj=None):
-        if asm.A is None:
-            raise NotImplementedError("the learned preconditioner is set up on a dense FP64 system")
+        mixed = asm.A is None
+        if mixed and getattr(asm, "op", None) is None:
+            raise NotImplementedError("the learned preconditioner needs a dense FP64 system or a mixed operator")
         self.bj = bj if bj is not None else asm.block_jacobi()
         dev = self.bj.device
         n = self.bj.n
@@ -167,15 +168,18 @@ class LearnedPreconditioner:
         nat.call("mbem_nn_basis", ctypes.byref(self.bj.struct()), ptr(self.phi),
                  rng.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) if rng.size else None, len(rng) // 2,
                  ptr(self.basis), ptr(shift) if shift is not None else None, stream_handle())
-        self.APhi = torch.empty((n, nc), dtype=torch.float64, device=dev)
-        self.Ac_inv = torch.empty((nc, nc), dtype=torch.float64, device=dev)
-        self.work = torch.empty(nat.lib().mbem_nn_apply_workspace_size(n, nc) // 8, dtype=torch.float64,
+        self.work = torch.empty(nat.lib().mbem_nn_apply_workspace_size(n, nc) // 8 + 1, dtype=torch.float64,
                                 device=dev)
         self._bj_struct = self.bj.struct()
+        st = stream_handle()
+        if mixed:
+            self._setup_mixed(asm, n, nc, shift, dev, st, t0, t1)
+            return
+        self.APhi = torch.empty((n, nc), dtype=torch.float64, device=dev)
+        self.Ac_inv = torch.empty((nc, nc), dtype=torch.float64, device=dev)
         self._struct = nat.NnPrecond(n=n, n_coarse=nc, bj=ctypes.pointer(self._bj_struct), basis=ptr(self.basis),
                                      APhi=ptr(self.APhi), Ac_inv=ptr(self.Ac_inv), work=ptr(self.work))
         A = asm.A
-        st = stream_handle()
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         nat.call("mbem_nn_coarse_operator_dense", ptr(A), A.stride(0), ctypes.byref(self._struct),
@@ -189,6 +193,33 @@ class LearnedPreconditioner:
         t4 = time.perf_counter()
         self.setup_s = {"features_host": t1 - t0, "basis_device": t2 - t1, "coarse_operator_device": t3 - t2,
                         "coarse_inverse_device": t4 - t3}
+
+    def _setup_mixed(self, asm, n, nc, shift, dev, st, t0, t1):
+        """The mixed operator's setup: A Phi (FP32) from its BF16 inner
+        operator, A_c and its FP32 inverse (mbem_nn_setup_mixed)."""
+        import time
+        inner = asm.bf16_inner()
+        ld32 = (nc + 3) // 4 * 4
+        self.APhi = self.Ac_inv = None
+        self.APhi32 = torch.empty((n, ld32), dtype=torch.float32, device=dev)
+        self.Ac_inv32 = torch.empty((nc, ld32), dtype=torch.float32, device=dev)
+        self._struct = nat.NnPrecond(n=n, n_coarse=nc, bj=ctypes.pointer(self._bj_struct), basis=ptr(self.basis),
+                                     APhi=None, Ac_inv=None, work=ptr(self.work), APhi32=ptr(self.APhi32),
+                                     Ac_inv32=ptr(self.Ac_inv32), ld32=ld32)
+        need = int(nat.lib().mbem_dense_inverse_f32_workspace_size(nc))
+        inv_work = torch.empty(need, dtype=torch.uint8, device=dev)
+        saved = inner.precond
+        inner.precond = None
+        ist = inner.struct()
+        inner.precond = saved
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        nat.call("mbem_nn_setup_mixed", ctypes.byref(ist), ctypes.byref(self._struct),
+                 ptr(shift) if shift is not None else None, 0 if shift is None else shift.shape[1], ptr(inv_work),
+                 need, st)
+        self.built = True
+        t3 = time.perf_counter()
+        self.setup_s = {"features_host": t1 - t0, "basis_device": t2 - t1, "coarse_operator_and_inverse": t3 - t2}
 
     def struct(self):
         return self._struct

@@ -190,9 +190,20 @@ class Bf16Inner:
                      stream_handle())
         self.u_ranges = np.asarray(u_ranges, dtype=np.int64).reshape(-1, 2)
         self.work = None
+        self.precond = None
         self.set_iterations(iterations)
         self.built = True
         self._keep = None
+
+    def set_preconditioner(self, precond) -> None:
+        """A fixed right preconditioner M of the inner GMRES (None: none):
+        ``la.precond.BlockJacobi`` or ``la.learned.LearnedPreconditioner``
+        built on this operator; the inner steps then multiply A16 by M."""
+        kind = getattr(precond, "PRECOND_KIND", None) if precond is not None else 0
+        if kind not in (0, 1, 2):
+            raise TypeError(f"the inner solve takes a block-Jacobi or learned preconditioner, not "
+                            f"{type(precond).__name__}")
+        self.precond = precond
 
     def set_iterations(self, iterations: int) -> None:
         """Changes the inner step count (and grows the workspace to match)."""
@@ -212,10 +223,15 @@ class Bf16Inner:
         for i, nb in enumerate(self.op.near):
             arr[i] = nat.NearBlocks(nb.row0, nb.col0, nb.n_field, ptr(nb.rowptr), ptr(nb.cols), ptr(nb.vals))
         ur = np.ascontiguousarray(self.u_ranges.ravel())
-        self._keep = (arr, ur)
+        kind, state = 0, None
+        if self.precond is not None:
+            kind = self.precond.PRECOND_KIND
+            pst = self.precond.struct()
+            state = ctypes.cast(ctypes.byref(pst), ctypes.c_void_p)
+        self._keep = (arr, ur, state, pst if self.precond is not None else None)
         return nat.InnerBf16(self.n, ptr(self.A16), self.ld16, len(self.op.near), arr, self.iterations,
                              self.rtol, len(self.u_ranges), ur.ctypes.data if ur.size else None, ptr(self.work),
-                             self.work.numel())
+                             self.work.numel(), kind, state)
 
     def matvec(self, x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """(A16 + near) x: the inner operator itself."""
