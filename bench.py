@@ -206,9 +206,9 @@ def run_ours(args, rank, ws):
     n = system.layout.n_unknowns
     arrays = {}     # device-resident mesh arrays, filled by the first assembly
 
-    def make_step(precision, timer=None):
+    def make_step(precision, timer=None, precond=None):
         backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART,
-                               precision=precision, precond=_precond_for(precision))
+                               precision=precision, precond=precond or _precond_for(precision, args.precond))
 
         def step():
             asm = backend.assemble(system, eps, arrays=arrays, timer=timer)
@@ -226,7 +226,7 @@ def run_ours(args, rank, ws):
     if args.precision == "mixed" and not args.skip_tune:
         from mbem_gb300 import autotune
         tb = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART, precision="mixed",
-                          precond=_precond_for("mixed"))
+                          precond="bf16_inner")
         t0 = time.perf_counter()
         tasm = tb.assemble(system, eps, arrays=arrays)
         tuned = autotune.tune_mixed_operator(tasm, autotune.Autotuner(cache_path=""))
@@ -264,6 +264,21 @@ def run_ours(args, rank, ws):
                 "assembly_ms_per_step": float(np.sum(asm64)) / max(1, args.fp64_steps),
                 "speedup_mixed_vs_fp64": dev64 / dev_s}
 
+    # the other mixed variant (with / without the learned two-level
+    # preconditioner inside the BF16 inner solve), timed the same way
+    other = None
+    if args.precision == "mixed" and not args.skip_variant:
+        alt = "bf16_inner" if args.precond == "bf16_learned" else "bf16_learned"
+        stepv = make_step("mixed", precond=alt)
+        stepv()
+        inner_stats(timing=False)
+        devv, wallv, resv = _timed_steps(stepv, max(1, args.fp64_steps), ws)
+        sv, av, _ = inner_stats(timing=False)
+        other = {"precond": alt, "ms_per_step": devv * 1e3, "outer_iterations": resv[-1][0].iterations,
+                 "inner_steps_per_step": sv / max(1, args.fp64_steps), "true_relres": resv[-1][0].true_relres,
+                 "headline_speedup_over_it": devv / dev_s,
+                 "max_rel_diff_vs_headline_solution": float((resv[-1][2] - x_last).norm() / x_last.norm())}
+        del resv
     # the headline solution against the reference's FP64 system
     accuracy = None
     if args.precision == "mixed" and not args.skip_fp64:
@@ -278,7 +293,7 @@ def run_ours(args, rank, ws):
         host_cube = M.cube(cfg["n_face"])
         host_fault = M.centre_fault(cfg["n_fault"])
         backend = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART,
-                               precision=args.precision, precond=_precond_for(args.precision))
+                               precision=args.precision, precond=_precond_for(args.precision, args.precond))
 
         def e2e_step():
             cube_p = Patch("cube", host_cube, BCType.FREE_TRACTION)
@@ -353,7 +368,9 @@ def run_ours(args, rank, ws):
                    "unknowns": n, "precision": args.precision,
                    "solver": f"deflated FGMRES({RESTART})" + (
                        f", BF16 inner GMRES (<= {defaults.MIXED_INNER_ITERATIONS} steps to "
-                       f"{defaults.MIXED_INNER_RTOL:g}) as flexible preconditioner"
+                       f"{defaults.MIXED_INNER_RTOL:g}) as flexible preconditioner" + (
+                           ", right-preconditioned by the learned two-level preconditioner (block-Jacobi + "
+                           "learned coarse space, set up in the step)" if args.precond == "bf16_learned" else "")
                        if args.precision == "mixed" else ""),
                    "rtol": RTOL, "parallelism": "replicas" if ws > 1 else "single",
                    "l2": "inputs larger than L2 (A = %.1f GB FP32 far field)" % (4.0 * n * n / 1e9)
@@ -367,6 +384,7 @@ def run_ours(args, rank, ws):
         "assembly_kernels_ms_per_step": float(np.sum(asm_ms)) / args.steps,
         "fp64_path": fp64,
         "accuracy_vs_fp64_system": accuracy,
+        "mixed_variant": other,
         "e2e": e2e,
         "gpu_launches": int(launches),
         "roofline": roofline,
@@ -450,10 +468,12 @@ def headline_accuracy(model, system, eps, x_mixed, arrays, n_readout=32):
                     "solved to the same tolerance (FP64 readout)"}
 
 
-def _precond_for(precision):
-    """The headline solve's preconditioner: the BF16 inner solve for the
-    mixed operator, none for FP64 (the reference's plain FGMRES)."""
-    return "bf16_inner" if precision == "mixed" else None
+def _precond_for(precision, choice="bf16_learned"):
+    """The headline solve's preconditioner: for the mixed operator the BF16
+    inner solve, with (``bf16_learned``) or without (``bf16_inner``) the
+    learned two-level preconditioner inside it; none for FP64 (the
+    reference's plain FGMRES)."""
+    return choice if precision == "mixed" else None
 
 
 def _sync_time(fn):
@@ -1104,6 +1124,9 @@ def main():
     ap.add_argument("--skip-tune", action="store_true", help="keep the default tile shapes")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--precond", default="bf16_learned", choices=["bf16_learned", "bf16_inner"],
+                    help="the mixed headline's preconditioner (the other is timed beside it)")
+    ap.add_argument("--skip-variant", action="store_true", help="skip timing the other mixed preconditioner")
     ap.add_argument("--skip-extra", action="store_true",
                     help="skip the many-right-hand-side and FAULT_TRACTION workloads")
     args = ap.parse_args()

@@ -52,6 +52,10 @@ int mbem_version(void);
 const char* mbem_last_error(void);
 /* Kernels this library has launched since it was loaded (all threads). */
 unsigned long long mbem_launch_count(void);
+/* The FP32 pipe's FMA throughput: 16 independent FFMA chains a thread
+ * (packed = 0) or 8 FFMA2 (float2) chains (packed = 1), `iters` steps; the
+ * same 32 FLOPs a thread a step either way (bench roofline denominator). */
+int mbem_fp32_fma_probe(float* out, int64_t iters, int blocks, int threads, int packed, void* stream);
 /* FP64 pipe throughput probe: blocks*threads threads each run 8 independent
  * DFMA chains of `iters` steps (16*iters FLOP per thread); time it with
  * events for the FP64 roofline denominator. No reference counterpart. */
@@ -458,7 +462,7 @@ typedef struct {
 
 /* M (n x n, row-major FP32 at ld >= n, device) = M^-1 in place: Gauss-Jordan with
  * partial pivoting, 16 pivot columns a step (a one-CTA panel, then one
- * rank-16 update of the other columns); n <= 3418 (the panel lives in shared
+ * rank-16 update of the other columns); n <= 3403 (the panel lives in shared
  * memory). MBEM_ERR_NUMERIC when a column has no usable pivot. Synchronises
  * `stream`. No counterpart in the reference (it solves its small systems with
  * LAPACK on the host). */
@@ -471,6 +475,11 @@ typedef struct {
  * `stream`. No counterpart in the reference. */
 int mbem_nn_setup_mixed(const mbem_inner_bf16* inner, const mbem_nn_precond* nn, const double* shift, int n_shift,
                         void* work, size_t work_bytes, void* stream);
+/* idx (n, k) int64: the k nearest of n points (n, 3) FP32 (centred), the
+ * point itself first, by squared distance then index; k <= 16. The node
+ * neighbourhoods of the learned preconditioner's features. No counterpart in
+ * the reference. */
+int mbem_knn(const float* points, int64_t n, int k, int64_t* idx, void* stream);
 size_t mbem_dense_inverse_f32_workspace_size(int64_t n);
 int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t work_bytes, void* stream);
 /* out (n_items, 9) = MLP(feat (n_items, MBEM_NN_FEAT)); act (n_items, 2H)

@@ -111,6 +111,7 @@ _SIGNATURES = {
     "mbem_version": (c_int, []),
     "mbem_last_error": (ctypes.c_char_p, []),
     "mbem_launch_count": (ctypes.c_ulonglong, []),
+    "mbem_fp32_fma_probe": (c_int, [_P, _I, c_int, c_int, c_int, _P]),
     "mbem_fp64_fma_probe": (c_int, [_P, _I, c_int, c_int, _P]),
     "mbem_t_matrix_direct": (c_int, [_P, _I, _P, _P, _P, _I, _P, c_int, _D, c_int, _P, _I, _P]),
     "mbem_u_matrix_direct": (c_int, [_P, _I, _P, _P, _I, _P, c_int, _D, c_int, _P, _I, _P]),
@@ -203,6 +204,7 @@ _SIGNATURES = {
     "mbem_lu_factor_f32": (c_int, [_P, _I, _I, _P, _P, c_size_t, _P, _P]),
     "mbem_lu_solve_f32": (c_int, [_P, _I, _I, _P, _P, _P, _P, _P]),
     "mbem_nn_setup_mixed": (c_int, [_P, _P, _P, c_int, _P, c_size_t, _P]),
+    "mbem_knn": (c_int, [_P, _I, c_int, _P, _P]),
     "mbem_dense_inverse_f32_workspace_size": (c_size_t, [_I]),
     "mbem_dense_inverse_f32": (c_int, [_P, _I, _I, _P, c_size_t, _P]),
     "mbem_lu_solve_t_f32": (c_int, [_P, _I, _I, _P, _P, _P, _P, _P]),

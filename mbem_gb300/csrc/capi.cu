@@ -49,9 +49,50 @@ __global__ void fp64_fma_probe_kernel(double* out, int64_t iters) {
     if (s == 12345.678) out[0] = s;   // keeps the chains live; never true
 }
 
+// Independent FP32 FMA chains for the FP32 pipe's throughput: 16 scalar
+// chains (FFMA) or 8 float2 chains (packed FFMA2), the same FLOPs per thread.
+template <bool PACKED>
+__global__ void fp32_fma_probe_kernel(float* out, int64_t iters) {
+    float s = 0.0f;
+    if (PACKED) {
+        float2 a[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = make_float2(1.0f + 1e-6f * (threadIdx.x + k), 1.0f - 1e-6f * k);
+        const float2 m = make_float2(0.9999999f, 0.9999998f), c = make_float2(1e-7f, 2e-7f);
+        for (int64_t i = 0; i < iters; i++) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) a[k] = __ffma2_rn(a[k], m, c);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) s += a[k].x + a[k].y;
+    } else {
+        float a[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) a[k] = 1.0f + 1e-6f * (threadIdx.x + k);
+        const float m = 0.9999999f, c = 1e-7f;
+        for (int64_t i = 0; i < iters; i++) {
+#pragma unroll
+            for (int k = 0; k < 16; k++) a[k] = fmaf(a[k], m, c);
+        }
+#pragma unroll
+        for (int k = 0; k < 16; k++) s += a[k];
+    }
+    if (s == 12345.678f) out[0] = s;   // keeps the chains live; never true
+}
+
 }  // namespace mbem
 
 extern "C" {
+
+int mbem_fp32_fma_probe(float* out, int64_t iters, int blocks, int threads, int packed, void* stream) {
+    MBEM_REQUIRE(out && iters > 0 && blocks > 0 && threads > 0 && threads <= 1024, MBEM_ERR_ARG,
+                 "bad probe launch");
+    if (packed)
+        mbem::fp32_fma_probe_kernel<true><<<blocks, threads, 0, (cudaStream_t)stream>>>(out, iters);
+    else
+        mbem::fp32_fma_probe_kernel<false><<<blocks, threads, 0, (cudaStream_t)stream>>>(out, iters);
+    return mbem::launch_status("fp32_fma_probe_kernel");
+}
 
 unsigned long long mbem_launch_count(void) { return mbem::g_launches.load(); }
 

@@ -455,6 +455,55 @@ __global__ void gj_swap_columns_kernel(double* __restrict__ M, int64_t m, const 
 }
 
 // ---------------------------------------------------------------------------
+// k nearest nodes of every node (the learned features' neighbourhoods): one
+// thread a query node scanning all nodes through shared-memory tiles, keeping
+// its k best in registers (squared FP32 distances of coordinates centred on
+// the mesh's mean; ties to the lower index). The node itself comes first.
+// ---------------------------------------------------------------------------
+constexpr int KNN_MAX = 16, KNN_TILE = 1024;
+
+__global__ void __launch_bounds__(256)
+knn_kernel(const float* __restrict__ p, int64_t n, int k, int64_t* __restrict__ idx_out) {
+    __shared__ float tile[KNN_TILE * 3];
+    const int64_t q = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    float qx = 0.f, qy = 0.f, qz = 0.f;
+    if (q < n) { qx = p[3 * q]; qy = p[3 * q + 1]; qz = p[3 * q + 2]; }
+    float bd[KNN_MAX];
+    int bi[KNN_MAX];
+#pragma unroll
+    for (int t = 0; t < KNN_MAX; t++) { bd[t] = INFINITY; bi[t] = 0x7fffffff; }
+    for (int64_t j0 = 0; j0 < n; j0 += KNN_TILE) {
+        const int m = (int)lmin(KNN_TILE, n - j0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < 3 * m; t += 256) tile[t] = p[3 * j0 + t];
+        __syncthreads();
+        if (q >= n) continue;
+        for (int j = 0; j < m; j++) {
+            const float dx = tile[3 * j] - qx, dy = tile[3 * j + 1] - qy, dz = tile[3 * j + 2] - qz;
+            const int jj = (int)(j0 + j);
+            float d = (jj == q) ? -1.0f : fmaf(dx, dx, fmaf(dy, dy, dz * dz));    // self first
+            // the best KNN_MAX are kept (static register indexing); the first k are written
+            if (d > bd[KNN_MAX - 1] || (d == bd[KNN_MAX - 1] && jj > bi[KNN_MAX - 1])) continue;
+            int ci = jj;
+#pragma unroll
+            for (int t = 0; t < KNN_MAX; t++) {                 // insertion, order (d, index)
+                if (d < bd[t] || (d == bd[t] && ci < bi[t])) {
+                    const float td = bd[t];
+                    const int ti = bi[t];
+                    bd[t] = d; bi[t] = ci;
+                    d = td; ci = ti;
+                }
+            }
+        }
+    }
+    if (q < n) {
+#pragma unroll
+        for (int t = 0; t < KNN_MAX; t++)
+            if (t < k) idx_out[q * k + t] = bi[t];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // A Phi for the BF16 inner operator of the mixed solve (A16 far field plus
 // its FP64 near blocks), stored FP32 at ldp: a CTA per (group of
 // APHI16_GROUP chunks, APHI16_ROWS rows) holds the group's columns and basis
@@ -978,6 +1027,15 @@ int mbem_dense_inverse(double* M, int64_t n, void* work, size_t work_bytes, void
     return MBEM_OK;
 }
 
+int mbem_knn(const float* points, int64_t n, int k, int64_t* idx, void* stream) {
+    MBEM_REQUIRE(n >= 0 && k >= 1 && k <= KNN_MAX && k <= n && (n == 0 || (points && idx)), MBEM_ERR_ARG,
+                 "knn needs 1 <= k <= min(%d, n)", KNN_MAX);
+    MBEM_REQUIRE(n < INT32_MAX, MBEM_ERR_SIZE, "too many nodes for knn");
+    if (n == 0) return MBEM_OK;
+    knn_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(points, n, k, idx);
+    return launch_status("knn_kernel");
+}
+
 size_t mbem_dense_inverse_f32_workspace_size(int64_t n) {
     return (size_t)GJB_BLOCK * n * sizeof(float) + (size_t)(n + 8) * sizeof(int) + 256;
 }
@@ -986,7 +1044,7 @@ int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t w
     MBEM_REQUIRE(n >= 0 && ld >= n && (n == 0 || M), MBEM_ERR_ARG, "bad matrix for the inverse");
     if (n == 0) return MBEM_OK;
     const size_t panel = (size_t)n * (GJB_BLOCK + 1) * sizeof(float);
-    constexpr size_t kSmem = 227 * 1024;
+    constexpr size_t kSmem = 227 * 1024 - 1024;      // the panel kernel's static arrays take the rest
     MBEM_REQUIRE(panel <= kSmem && ceil_div(n, GJB_TR) <= 65535, MBEM_ERR_UNSUPPORTED,
                  "the FP32 inverse holds its n x %d panel in shared memory: n <= %d", GJB_BLOCK,
                  (int)(kSmem / ((GJB_BLOCK + 1) * sizeof(float))));

@@ -110,6 +110,61 @@ def node_features(layout, chunks) -> np.ndarray:
     return f
 
 
+def device_nodes(asm):
+    """``layout_nodes`` from the assembly's device mesh arrays: (pos, nrm, h,
+    kind, slot) CUDA tensors, one row per node."""
+    pos, nrm, h, kind, slot = [], [], [], [], []
+    for si, s_ in enumerate(asm.layout.slots):
+        a = asm.device_patch_arrays(s_.patch)
+        m = s_.size // 3
+        K = m // s_.patch.mesh.n_triangles
+        tv = a["tv"].view(-1, 3, 3)
+        area = 0.5 * torch.linalg.cross(tv[:, 1] - tv[:, 0], tv[:, 2] - tv[:, 0]).norm(dim=1)
+        pos.append(a["coll"].view(-1, 3))
+        nrm.append(a["coll_n"].view(-1, 3))
+        h.append(torch.repeat_interleave(area.sqrt(), K))
+        kind.append(torch.full((m,), 1.0 if s_.kind == "b" else 0.0, dtype=torch.float64, device=tv.device))
+        slot.append(torch.full((m,), si, dtype=torch.int64, device=tv.device))
+    return torch.cat(pos), torch.cat(nrm), torch.cat(h), torch.cat(kind), torch.cat(slot)
+
+
+def node_features_device(asm, bj) -> torch.Tensor:
+    """``node_features`` on the device (the same sixteen features; the
+    neighbourhoods from ``mbem_knn``, ties to the lower index)."""
+    pos, nrm, h, kind, slot = device_nodes(asm)
+    dev = pos.device
+    n = pos.shape[0]
+    cof = bj.chunk_of_node()
+    C = bj.n_chunks
+    cnt = torch.zeros(C, dtype=torch.float64, device=dev).index_add_(0, cof, torch.ones(n, dtype=torch.float64,
+                                                                                        device=dev))
+    cen = torch.zeros((C, 3), dtype=torch.float64, device=dev).index_add_(0, cof, pos) / cnt[:, None]
+    dist = (pos - cen[cof]).norm(dim=1)
+    rad = torch.zeros(C, dtype=torch.float64, device=dev).scatter_reduce_(0, cof, dist, "amax")
+    hmax = torch.zeros(C, dtype=torch.float64, device=dev).scatter_reduce_(0, cof, h, "amax")
+    rad = rad + 1e-12 * torch.clamp(hmax, min=1.0)
+    k = min(NEIGHBOURS, n)
+    centred = (pos - pos.mean(dim=0)).float().contiguous()
+    nb = torch.empty((n, k), dtype=torch.int64, device=dev)
+    nat.call("mbem_knn", ptr(centred), n, k, ptr(nb), stream_handle())
+    same = slot[nb] == slot[:, None]
+    cnt_same = same.sum(dim=1).clamp(min=1).to(torch.float64)
+    off = ((pos[nb] - pos[:, None, :]) * same[..., None]).sum(dim=1) / cnt_same[:, None] / h[:, None]
+    rel = (pos - cen[cof]) / rad[cof][:, None]
+    f = torch.zeros((n, nat.NN_FEAT), dtype=torch.float64, device=dev)
+    f[:, 0:3] = rel
+    f[:, 3] = rel.norm(dim=1)
+    f[:, 4:7] = nrm
+    f[:, 7] = kind
+    f[:, 8:11] = off
+    f[:, 11] = off.norm(dim=1)
+    f[:, 12] = (nrm * rel).sum(dim=1)
+    f[:, 13] = torch.log(h / rad[cof])
+    f[:, 14] = 1.0
+    f[:, 15] = same.to(torch.float64).mean(dim=1)
+    return f.float().contiguous()
+
+
 # ---------------------------------------------------------------------------
 # the network
 # ---------------------------------------------------------------------------
@@ -159,7 +214,10 @@ class LearnedPreconditioner:
         import time
         t0 = time.perf_counter()
         self.params = torch.as_tensor(np.asarray(params, np.float32)).to(dev)
-        self.feat = torch.from_numpy(node_features(asm.layout, self.bj.chunk_nodes())).to(dev)
+        if mixed:
+            self.feat = node_features_device(asm, self.bj)
+        else:
+            self.feat = torch.from_numpy(node_features(asm.layout, self.bj.chunk_nodes())).to(dev)
         t1 = time.perf_counter()
         self.phi = mlp_forward(self.feat, self.params)
         self.basis = torch.empty((n, 6), dtype=torch.float32, device=dev)
@@ -199,6 +257,8 @@ class LearnedPreconditioner:
         operator, A_c and its FP32 inverse (mbem_nn_setup_mixed)."""
         import time
         inner = asm.bf16_inner()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
         ld32 = (nc + 3) // 4 * 4
         self.APhi = self.Ac_inv = None
         self.APhi32 = torch.empty((n, ld32), dtype=torch.float32, device=dev)
@@ -219,7 +279,7 @@ class LearnedPreconditioner:
                  need, st)
         self.built = True
         t3 = time.perf_counter()
-        self.setup_s = {"features_host": t1 - t0, "basis_device": t2 - t1, "coarse_operator_and_inverse": t3 - t2}
+        self.setup_s = {"features_device": t1 - t0, "basis_device": t2 - t1, "coarse_operator_and_inverse": t3 - t2}
 
     def struct(self):
         return self._struct

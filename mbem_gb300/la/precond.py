@@ -52,6 +52,65 @@ def cluster_leaves(points: np.ndarray, max_nodes: int) -> list:
     return leaves
 
 
+def cluster_order_device(points: torch.Tensor, max_nodes: int):
+    """The bisection tree of ``cluster_leaves`` built level by level on the
+    device: returns (order (m,) int64 CUDA, leaf sizes (L,) host int64), the
+    leaves as consecutive runs of ``order`` in the tree order of
+    ``cluster_leaves``. Each split is the one ``cluster_leaves`` makes
+    (median of the projection on the leading principal axis, ``proj <
+    median`` to the left, halves by rank when the projections coincide);
+    the 3 x 3 eigenproblems of a level are solved together on the host. Where
+    the two leading principal axes are degenerate the axis, and so the split,
+    may differ from the host's."""
+    dev = points.device
+    m = int(points.shape[0])
+    order = torch.arange(m, dtype=torch.int64, device=dev)
+    sizes = np.array([m], np.int64)
+    while m and sizes.max() > max_nodes:
+        S = sizes.size
+        seg = torch.repeat_interleave(torch.arange(S, device=dev), torch.from_numpy(sizes).to(dev))
+        P = points[order]
+        cnt = torch.from_numpy(sizes).to(dev, torch.float64)
+        mean = torch.zeros((S, 3), dtype=torch.float64, device=dev).index_add_(0, seg, P) / cnt[:, None]
+        X = P - mean[seg]
+        cov = torch.zeros((S, 3, 3), dtype=torch.float64, device=dev).index_add_(0, seg, X[:, :, None] * X[:, None, :])
+        big = sizes > max_nodes
+        axis = np.zeros((S, 3))
+        if big.any():
+            _, vecs = np.linalg.eigh(cov[torch.from_numpy(big).to(dev)].cpu().numpy())
+            axis[big] = vecs[:, :, -1]
+        proj = (X * torch.from_numpy(axis).to(dev)[seg]).sum(dim=1)
+        # projections sorted within each segment (stable: ties keep the current order)
+        by_proj = torch.argsort(proj, stable=True)
+        srt = by_proj[torch.argsort(seg[by_proj], stable=True)]
+        sproj = proj[srt]
+        start = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+        lo = torch.from_numpy(start + (sizes - 1) // 2).to(dev)
+        hi = torch.from_numpy(start + sizes // 2).to(dev)
+        median = 0.5 * (sproj[lo] + sproj[hi])
+        bigd = torch.from_numpy(big).to(dev)
+        left = (proj < median[seg]) & bigd[seg]
+        n_left = torch.zeros(S, dtype=torch.int64, device=dev).index_add_(0, seg, left.long())
+        nl = n_left.cpu().numpy()
+        flat = big & ((nl == 0) | (nl == sizes))
+        if flat.any():
+            # coincident projections: the lower half by rank goes left
+            rank = torch.empty(m, dtype=torch.int64, device=dev)
+            rank[srt] = torch.arange(m, device=dev) - torch.from_numpy(start).to(dev)[seg[srt]]
+            halves = rank < torch.from_numpy(sizes // 2).to(dev)[seg]
+            fl = torch.from_numpy(flat).to(dev)[seg]
+            left = torch.where(fl, halves, left)
+            nl = np.where(flat, sizes // 2, nl)
+        # stable partition: each segment's left part, then its right part
+        key = 2 * seg + (~left).long() * bigd[seg].long()
+        order = order[torch.argsort(key, stable=True)]
+        new = []
+        for sz, b, l in zip(sizes, big, nl):
+            new.extend([l, sz - l] if b else [sz])
+        sizes = np.array(new, np.int64)
+    return order, sizes
+
+
 class BlockJacobi:
     """M^-1 = blockdiag(A[c, c]^-1) over spatial chunks c of every slot.
 
@@ -96,6 +155,54 @@ class BlockJacobi:
         self.built = False
 
     @classmethod
+    def from_device_points(cls, n: int, groups, max_nodes: int = MAX_NODES):
+        """As the constructor, with the slots' node points as CUDA tensors and
+        the chunks made by ``cluster_order_device`` (no host pass over the
+        nodes)."""
+        if not 1 <= max_nodes <= MAX_NODES:
+            raise ValueError(f"max_nodes must be in [1, {MAX_NODES}]")
+        self = cls.__new__(cls)
+        dev = groups[0][1].device
+        dof_parts, sizes_all = [], []
+        for off, pts in groups:
+            order, sizes = cluster_order_device(pts.to(torch.float64), max_nodes)
+            # each leaf's nodes ascending, as the host constructor sorts them
+            leaf = torch.repeat_interleave(torch.arange(sizes.size, device=dev), torch.from_numpy(sizes).to(dev))
+            order = order[torch.argsort(leaf * (pts.shape[0] + 1) + order)]
+            dof_parts.append((off + 3 * order[:, None] + torch.arange(3, device=dev)).reshape(-1))
+            sizes_all.append(3 * sizes)
+        dofs = torch.cat(dof_parts) if dof_parts else torch.zeros(0, dtype=torch.int64, device=dev)
+        sizes = np.concatenate(sizes_all) if sizes_all else np.zeros(0, np.int64)
+        if dofs.numel() != n or int(sizes.sum()) != n:
+            raise ValueError("the slots' nodes do not partition the unknowns")
+        ptr_h = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        chunk = torch.repeat_interleave(torch.arange(sizes.size, device=dev, dtype=torch.int32),
+                                        torch.from_numpy(sizes).to(dev))
+        start = torch.from_numpy(ptr_h[:-1]).to(dev)
+        local = torch.empty(n, dtype=torch.int32, device=dev)
+        chunk_of = torch.empty(n, dtype=torch.int32, device=dev)
+        pos = torch.arange(n, device=dev)
+        local[dofs] = (pos - start[chunk.long()]).to(torch.int32)
+        chunk_of[dofs] = chunk
+        self.n = int(n)
+        self.n_chunks = int(sizes.size)
+        self.m_max = int(sizes.max()) if sizes.size else 1
+        self.chunk_sizes = sizes
+        self._chunks = None
+        self.device = dev
+        self._ptr = torch.from_numpy(ptr_h).to(dev)
+        self._dofs = dofs.contiguous()
+        self._local = local
+        self._chunk_of = chunk_of
+        nbytes = nat.lib().mbem_bj_inverse_bytes(self.n_chunks, self.m_max)
+        self.inv = torch.zeros(nbytes // 4, dtype=torch.float32, device=dev)
+        self._struct = nat.BlockJacobi(n=self.n, n_chunks=self.n_chunks, m_max=self.m_max,
+                                       chunk_ptr=ptr(self._ptr), dofs=ptr(self._dofs), local=ptr(self._local),
+                                       chunk_of=ptr(self._chunk_of), inv=ptr(self.inv))
+        self.built = False
+        return self
+
+    @classmethod
     def for_layout(cls, layout, max_nodes: int = MAX_NODES, device="cuda"):
         """Chunks over every slot of an ``UnknownLayout``, nodes at the
         slot patch's collocation points."""
@@ -107,7 +214,15 @@ class BlockJacobi:
 
     def chunk_nodes(self) -> list:
         """Node indices (unknowns 3i..3i+2) of every chunk, in chunk order."""
+        if self._chunks is None:
+            d = self._dofs.cpu().numpy()
+            p = self._ptr.cpu().numpy()
+            self._chunks = [d[p[c]:p[c + 1]] for c in range(self.n_chunks)]
         return [d[::3] // 3 for d in self._chunks]
+
+    def chunk_of_node(self) -> torch.Tensor:
+        """(n / 3,) int64 CUDA: the chunk of every node."""
+        return self._chunk_of[0::3].long()
 
     def build_dense(self, A: torch.Tensor):
         if A.dtype != torch.float64 or A.stride(1) != 1 or A.shape[0] != self.n:

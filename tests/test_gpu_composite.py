@@ -120,3 +120,26 @@ def test_composite_solve_matches_plain_mixed_solve(cube12):
     assert float((x1 - x0).norm() / x0.norm()) < 1e-7
     print(f"cube 12 inner steps: plain {steps0}, learned two-level {steps1} ({applies1} inner solves)")
     assert steps1 < steps0
+
+
+def test_device_features_equal_host_features(gpu):
+    """``node_features_device`` (mbem_knn neighbourhoods) equals the host
+    ``node_features`` on a cube whose vertices are jittered (no distance ties
+    among the neighbours), with the device-made chunks of the mixed operator."""
+    from mbem_gb300 import mesh as M
+    from mbem_gb300.backends.dense import DenseBackend
+    from mbem_gb300.la.learned import node_features, node_features_device
+    from mbem_gb300.model import BCType, Patch, Region, RegionModel, generate_system
+    cube = M.cube(8)
+    jitter = np.random.default_rng(8).normal(scale=0.01, size=cube.vertices.shape)
+    cube.vertices = cube.vertices + jitter
+    fault = M.centre_fault(4)
+    model = RegionModel([Region("body", M.ElasticMaterial(1.0, 1.0), [Patch("cube", cube, BCType.FREE_TRACTION)],
+                                np.zeros(3), faults=[Patch("fault", fault, BCType.FAULT,
+                                                           value=np.array([1.0, 0.0, 0.0]))])])
+    asm = DenseBackend(jump="calibrated", deflate=True, precision="mixed",
+                       precond="bf16_inner").assemble(generate_system(model), 0.25)
+    bj = asm.block_jacobi()
+    dev = node_features_device(asm, bj).cpu().numpy()
+    host = node_features(asm.layout, bj.chunk_nodes())
+    assert np.abs(dev - host).max() < 1e-5 * max(1.0, np.abs(host).max())
