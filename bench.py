@@ -913,6 +913,7 @@ def extra_workloads(args, peaks):
                      ("p1_variant_cube24", p1_variant_workload),
                      ("dense_lu_cube35", dense_lu_workload),
                      ("fault_traction_cube32_learned", fault_traction_workload),
+                     ("fault_traction_cube32_dip60_learned", lambda: fault_traction_workload(dip=60.0)),
                      ("p2_readout_1m", p2_readout_workload)):
         try:
             out[name] = fn()

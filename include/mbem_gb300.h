@@ -462,7 +462,7 @@ typedef struct {
 
 /* M (n x n, row-major FP32 at ld >= n, device) = M^-1 in place: Gauss-Jordan with
  * partial pivoting, 16 pivot columns a step (a one-CTA panel, then one
- * rank-16 update of the other columns); n <= 3403 (the panel lives in shared
+ * rank-16 update of the other columns); n <= 3214 (the panel lives in shared
  * memory). MBEM_ERR_NUMERIC when a column has no usable pivot. Synchronises
  * `stream`. No counterpart in the reference (it solves its small systems with
  * LAPACK on the host). */
@@ -480,6 +480,11 @@ int mbem_nn_setup_mixed(const mbem_inner_bf16* inner, const mbem_nn_precond* nn,
  * neighbourhoods of the learned preconditioner's features. No counterpart in
  * the reference. */
 int mbem_knn(const float* points, int64_t n, int k, int64_t* idx, void* stream);
+/* The same FP32 setup for a dense FP64 operator A (n x n at ld): A Phi with
+ * FP32 products, A_c, A_c^-1 (FP32). Replaces mbem_nn_setup_dense's FP64
+ * setup where a faster, preconditioner-accurate one serves. */
+int mbem_nn_setup_dense32(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift, int n_shift,
+                          void* work, size_t work_bytes, void* stream);
 size_t mbem_dense_inverse_f32_workspace_size(int64_t n);
 int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t work_bytes, void* stream);
 /* out (n_items, 9) = MLP(feat (n_items, MBEM_NN_FEAT)); act (n_items, 2H)

@@ -203,6 +203,7 @@ _SIGNATURES = {
     "mbem_lu_workspace_size": (c_size_t, [_I, c_int]),
     "mbem_lu_factor_f32": (c_int, [_P, _I, _I, _P, _P, c_size_t, _P, _P]),
     "mbem_lu_solve_f32": (c_int, [_P, _I, _I, _P, _P, _P, _P, _P]),
+    "mbem_nn_setup_dense32": (c_int, [_P, _I, _P, _P, c_int, _P, c_size_t, _P]),
     "mbem_nn_setup_mixed": (c_int, [_P, _P, _P, c_int, _P, c_size_t, _P]),
     "mbem_knn": (c_int, [_P, _I, c_int, _P, _P]),
     "mbem_dense_inverse_f32_workspace_size": (c_size_t, [_I]),

@@ -454,20 +454,15 @@ class AssembledDense:
         return [(s.offset, s.size) for s in self.layout.slots if s.kind == "u"]
 
     def block_jacobi(self, max_nodes: int | None = None):
-        """The cluster block-Jacobi preconditioner of this system (built once).
-        On the mixed operator the chunks are made on the device from the
-        device mesh arrays (``BlockJacobi.from_device_points``)."""
+        """The cluster block-Jacobi preconditioner of this system (built once);
+        the chunks are made on the device from the device mesh arrays
+        (``BlockJacobi.from_device_points``)."""
         from ..la.precond import MAX_NODES, BlockJacobi
         if self._bj is None or (max_nodes is not None and max_nodes != self._bj_nodes):
             self._bj_nodes = MAX_NODES if max_nodes is None else max_nodes
-            if self.op is not None:
-                groups = [(s.offset, self.device_patch_arrays(s.patch)["coll"].view(-1, 3))
-                          for s in self.layout.slots]
-                bj = BlockJacobi.from_device_points(self.layout.n_unknowns, groups, self._bj_nodes)
-                self._bj = bj.build_mixed(self.op)
-            else:
-                bj = BlockJacobi.for_layout(self.layout, self._bj_nodes)
-                self._bj = bj.build_dense(self.A)
+            groups = [(s.offset, self.device_patch_arrays(s.patch)["coll"].view(-1, 3)) for s in self.layout.slots]
+            bj = BlockJacobi.from_device_points(self.layout.n_unknowns, groups, self._bj_nodes)
+            self._bj = bj.build_mixed(self.op) if self.op is not None else bj.build_dense(self.A)
         return self._bj
 
     def device_patch_arrays(self, patch) -> dict:

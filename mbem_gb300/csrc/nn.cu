@@ -460,12 +460,21 @@ __global__ void gj_swap_columns_kernel(double* __restrict__ M, int64_t m, const 
 // its k best in registers (squared FP32 distances of coordinates centred on
 // the mesh's mean; ties to the lower index). The node itself comes first.
 // ---------------------------------------------------------------------------
-constexpr int KNN_MAX = 16, KNN_TILE = 1024;
+constexpr int KNN_MAX = 16, KNN_TILE = 1024, KNN_PARTS = 8, KNN_QPB = 32;   // queries a CTA of 256
 
+__device__ __forceinline__ bool knn_before(float d, int i, float e, int j) { return d < e || (d == e && i < j); }
+
+// KNN_PARTS threads per query node, each scanning the points j = part mod
+// KNN_PARTS of every shared-memory tile and keeping its best KNN_MAX in
+// registers (order: squared FP32 distance, then index; the node itself first);
+// the parts' lists are then merged in shared memory.
 __global__ void __launch_bounds__(256)
 knn_kernel(const float* __restrict__ p, int64_t n, int k, int64_t* __restrict__ idx_out) {
     __shared__ float tile[KNN_TILE * 3];
-    const int64_t q = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    __shared__ float md[KNN_QPB][KNN_PARTS * KNN_MAX];
+    __shared__ int mi[KNN_QPB][KNN_PARTS * KNN_MAX];
+    const int ql = threadIdx.x / KNN_PARTS, part = threadIdx.x % KNN_PARTS;
+    const int64_t q = (int64_t)blockIdx.x * KNN_QPB + ql;
     float qx = 0.f, qy = 0.f, qz = 0.f;
     if (q < n) { qx = p[3 * q]; qy = p[3 * q + 1]; qz = p[3 * q + 2]; }
     float bd[KNN_MAX];
@@ -478,16 +487,15 @@ knn_kernel(const float* __restrict__ p, int64_t n, int k, int64_t* __restrict__ 
         for (int t = threadIdx.x; t < 3 * m; t += 256) tile[t] = p[3 * j0 + t];
         __syncthreads();
         if (q >= n) continue;
-        for (int j = 0; j < m; j++) {
+        for (int j = part; j < m; j += KNN_PARTS) {
             const float dx = tile[3 * j] - qx, dy = tile[3 * j + 1] - qy, dz = tile[3 * j + 2] - qz;
             const int jj = (int)(j0 + j);
             float d = (jj == q) ? -1.0f : fmaf(dx, dx, fmaf(dy, dy, dz * dz));    // self first
-            // the best KNN_MAX are kept (static register indexing); the first k are written
-            if (d > bd[KNN_MAX - 1] || (d == bd[KNN_MAX - 1] && jj > bi[KNN_MAX - 1])) continue;
+            if (!knn_before(d, jj, bd[KNN_MAX - 1], bi[KNN_MAX - 1])) continue;
             int ci = jj;
 #pragma unroll
-            for (int t = 0; t < KNN_MAX; t++) {                 // insertion, order (d, index)
-                if (d < bd[t] || (d == bd[t] && ci < bi[t])) {
+            for (int t = 0; t < KNN_MAX; t++) {                 // insertion
+                if (knn_before(d, ci, bd[t], bi[t])) {
                     const float td = bd[t];
                     const int ti = bi[t];
                     bd[t] = d; bi[t] = ci;
@@ -496,11 +504,31 @@ knn_kernel(const float* __restrict__ p, int64_t n, int k, int64_t* __restrict__ 
             }
         }
     }
-    if (q < n) {
 #pragma unroll
-        for (int t = 0; t < KNN_MAX; t++)
-            if (t < k) idx_out[q * k + t] = bi[t];
+    for (int t = 0; t < KNN_MAX; t++) {
+        md[ql][part * KNN_MAX + t] = bd[t];
+        mi[ql][part * KNN_MAX + t] = bi[t];
     }
+    __syncthreads();
+    if (part != 0 || q >= n) return;
+    // merge: the other parts' lists into this thread's (already sorted) list
+    for (int e = KNN_MAX; e < KNN_PARTS * KNN_MAX; e++) {
+        float d = md[ql][e];
+        int ci = mi[ql][e];
+        if (!knn_before(d, ci, bd[KNN_MAX - 1], bi[KNN_MAX - 1])) continue;
+#pragma unroll
+        for (int t = 0; t < KNN_MAX; t++) {
+            if (knn_before(d, ci, bd[t], bi[t])) {
+                const float td = bd[t];
+                const int ti = bi[t];
+                bd[t] = d; bi[t] = ci;
+                d = td; ci = ti;
+            }
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < KNN_MAX; t++)
+        if (t < k) idx_out[q * k + t] = bi[t];
 }
 
 // ---------------------------------------------------------------------------
@@ -514,46 +542,73 @@ knn_kernel(const float* __restrict__ p, int64_t n, int k, int64_t* __restrict__ 
 // ---------------------------------------------------------------------------
 constexpr int APHI16_GROUP = 8, APHI16_ROWS = 128;
 
+__device__ __forceinline__ float aphi_load(const uint16_t* row, int c) {
+    return __uint_as_float((uint32_t)row[c] << 16);
+}
+__device__ __forceinline__ float aphi_load(const double* row, int c) { return (float)row[c]; }
+
+// T = uint16_t: the BF16 inner operator's far field; T = double: a dense FP64
+// operator (FP32 products: the coarse operator is a preconditioner's)
+template <typename T>
 __global__ void __launch_bounds__(256)
-nn_aphi_bf16_kernel(const uint16_t* __restrict__ A16, int64_t ld16, int64_t n, const int64_t* __restrict__ chunk_ptr,
-                    const int64_t* __restrict__ dofs, int64_t n_chunks, const float* __restrict__ basis,
-                    float* __restrict__ APhi, int64_t ldp) {
+nn_aphi_gather_kernel(const T* __restrict__ A16, int64_t ld16, int64_t n, const int64_t* __restrict__ chunk_ptr,
+                      const int64_t* __restrict__ dofs, int64_t n_chunks, const float* __restrict__ basis,
+                      float* __restrict__ APhi, int64_t ldp) {
     extern __shared__ float gsm[];
+    constexpr int RW = 4;                                       // rows a warp, their loads in flight together
     const int64_t cb = (int64_t)blockIdx.x * APHI16_GROUP;
     const int64_t ce = lmin(n_chunks, cb + APHI16_GROUP);
     const int64_t d0 = chunk_ptr[cb];
     const int m = (int)(chunk_ptr[ce] - d0);
     float* bs = gsm;                                            // [m][NCV]
     int* col = reinterpret_cast<int*>(gsm + (size_t)m * NCV);   // [m]
+    __shared__ int cptr[APHI16_GROUP + 1];
     for (int t = threadIdx.x; t < m; t += 256) {
         const int64_t d = dofs[d0 + t];
         col[t] = (int)d;
 #pragma unroll
         for (int k = 0; k < NCV; k++) bs[t * NCV + k] = basis[d * NCV + k];
     }
+    if (threadIdx.x <= ce - cb) cptr[threadIdx.x] = (int)(chunk_ptr[cb + threadIdx.x] - d0);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t r1 = lmin(n, ((int64_t)blockIdx.y + 1) * APHI16_ROWS);
-    for (int64_t r = (int64_t)blockIdx.y * APHI16_ROWS + warp; r < r1; r += 8) {
-        const uint16_t* Ar = A16 + r * ld16;
+    const int64_t rb = (int64_t)blockIdx.y * APHI16_ROWS;
+    const int64_t r1 = lmin(n, rb + APHI16_ROWS);
+    for (int64_t r0 = rb + (int64_t)warp * RW; r0 < r1; r0 += 8 * RW) {
+        const T* Ar[RW];
+#pragma unroll
+        for (int q = 0; q < RW; q++) Ar[q] = A16 + lmin(r0 + q, n - 1) * ld16;
         for (int64_t c = cb; c < ce; c++) {
-            const int lo = (int)(chunk_ptr[c] - d0), hi = (int)(chunk_ptr[c + 1] - d0);
-            float acc[NCV] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            const int lo = cptr[c - cb], hi = cptr[c - cb + 1];
+            float acc[RW][NCV];
+#pragma unroll
+            for (int q = 0; q < RW; q++)
+#pragma unroll
+                for (int k = 0; k < NCV; k++) acc[q][k] = 0.f;
             for (int t = lo + lane; t < hi; t += 32) {
-                const float v = __uint_as_float((uint32_t)Ar[col[t]] << 16);
+                const int cc = col[t];
+                float v[RW];
 #pragma unroll
-                for (int k = 0; k < NCV; k++) acc[k] = fmaf(v, bs[t * NCV + k], acc[k]);
+                for (int q = 0; q < RW; q++) v[q] = aphi_load(Ar[q], cc);
+#pragma unroll
+                for (int k = 0; k < NCV; k++) {
+                    const float b = bs[t * NCV + k];
+#pragma unroll
+                    for (int q = 0; q < RW; q++) acc[q][k] = fmaf(v[q], b, acc[q][k]);
+                }
             }
 #pragma unroll
-            for (int k = 0; k < NCV; k++)
+            for (int q = 0; q < RW; q++)
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
-            if (lane < NCV) {
-                float v = acc[0];
+                for (int k = 0; k < NCV; k++)
 #pragma unroll
-                for (int k = 1; k < NCV; k++) v = lane == k ? acc[k] : v;
-                APhi[r * ldp + NCV * c + lane] = v;
-            }
+                    for (int o = 16; o > 0; o >>= 1) acc[q][k] += __shfl_xor_sync(0xffffffffu, acc[q][k], o);
+            // lane q * NCV + k writes row r0 + q, coarse column NCV c + k
+#pragma unroll
+            for (int q = 0; q < RW; q++)
+#pragma unroll
+                for (int k = 0; k < NCV; k++)
+                    if (lane == q * NCV + k && r0 + q < r1) APhi[(r0 + q) * ldp + NCV * c + k] = acc[q][k];
         }
     }
 }
@@ -593,14 +648,14 @@ nn_coarse_matrix_f32_kernel(const float* __restrict__ APhi, int64_t ldp, int64_t
     if (q >= n_coarse) return;
     const int64_t c0 = chunk_ptr[c];
     const int m = (int)(chunk_ptr[c + 1] - c0);
-    double s[NCV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    float s[NCV] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int t = 0; t < m; t++) {
         const int64_t d = dofs[c0 + t];
-        const double v = APhi[d * ldp + q];
+        const float v = APhi[d * ldp + q];
 #pragma unroll
-        for (int k = 0; k < NCV; k++) s[k] += (double)basis[d * NCV + k] * v;
+        for (int k = 0; k < NCV; k++) s[k] = fmaf(basis[d * NCV + k], v, s[k]);
     }
-    for (int k = 0; k < NCV; k++) Ac[(NCV * c + k) * ldc + q] = (float)s[k];
+    for (int k = 0; k < NCV; k++) Ac[(NCV * c + k) * ldc + q] = s[k];
 }
 
 // Ac[p, q] += sum_j U[p, j] U[q, j] (FP32 coarse matrix at ldc)
@@ -623,118 +678,230 @@ __global__ void nn_sub_kernel(const double* __restrict__ a, const double* __rest
 
 // ---------------------------------------------------------------------------
 // Blocked Gauss-Jordan inverse in FP32 (the coarse matrix of the mixed-operator
-// preconditioner). Pivot columns are taken GJB_BLOCK at a time:
-//  - the panel kernel (one CTA, the panel's n x b values in shared memory)
-//    runs the b pivot steps with partial pivoting over the rows not yet used
-//    as pivots; the panel then holds, in GJ form, [B^-1 ; -A_RB B^-1] for
-//    the pivot rows B and the other rows R;
-//  - the swap kernel applies the b row interchanges to every other column
-//    and copies the pivot rows X_B aside;
+// preconditioner), with partial pivoting but no row interchanges: column k
+// takes as its pivot the unused row pi(k) of largest magnitude, and the
+// in-place result R holds the inverse with its rows and columns renamed,
+// A^-1[k, pi(j)] = R[pi(k), j] (gj_unpermute_kernel writes it out).
+// Pivot columns go GJB_BLOCK at a time:
+//  - the panel kernel (one CTA; the panel's n x b values in shared memory,
+//    each thread owning fixed rows, so a pivot step needs two barriers: one
+//    after the candidates, one after the pivot row is read) runs the b pivot
+//    steps; the panel then holds, in GJ form, [B^-1 ; -A_RB B^-1] on the
+//    pivot rows B and the others R;
+//  - the gather kernel copies the pivot rows X_B of every other column;
 //  - the update kernel: X_B <- B^-1 X_B, X_R <- X_R + (-A_RB B^-1) X_B, i.e.
 //    every row gets P[i, :] X_B (pivot rows replaced, others added to).
-// The column interchanges are undone at the end (gj_swap_columns_f32_kernel).
 // A column with no usable pivot (all zero or NaN) sets *bad.
 // ---------------------------------------------------------------------------
 constexpr int GJB_BLOCK = 16;
+constexpr int GJB_LDS = GJB_BLOCK + 1;       // odd row stride: a warp's row accesses fall in distinct banks
 constexpr int GJB_PANEL_THREADS = 1024;
 
 __global__ void __launch_bounds__(GJB_PANEL_THREADS)
 gjb_panel_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b, int* __restrict__ piv,
-                 int* __restrict__ bad) {
-    extern __shared__ float P[];                  // [n][GJB_BLOCK], then the column's factors f[n]
-    float* fcol = P + n * GJB_BLOCK;
+                 int* __restrict__ used, int* __restrict__ bad) {
+    extern __shared__ float P[];                  // [n][GJB_LDS], then the used flags (n ints)
+    int* us = reinterpret_cast<int*>(P + n * GJB_LDS);
     __shared__ float rv[GJB_PANEL_THREADS / 32];
     __shared__ int ri[GJB_PANEL_THREADS / 32];
-    __shared__ int s_p;
+    __shared__ int rf[GJB_PANEL_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     for (int64_t e = tid; e < n * GJB_BLOCK; e += GJB_PANEL_THREADS) {
         const int64_t i = e / GJB_BLOCK;
         const int c = (int)(e % GJB_BLOCK);
-        P[e] = c < b ? M[i * ld + k0 + c] : 0.0f;
+        P[i * GJB_LDS + c] = c < b ? M[i * ld + k0 + c] : 0.0f;
     }
+    for (int64_t i = tid; i < n; i += GJB_PANEL_THREADS) us[i] = used[i];
     __syncthreads();
     for (int t = 0; t < b; t++) {
         const int64_t k = k0 + t;
+        // candidates: the largest |P[i][t]| over this thread's unused rows
+        // (lowest row on ties; NaN never wins), and the lowest unused row
         float bv = -1.0f;
-        int bi = -1;
-        for (int64_t i = k + tid; i < n; i += GJB_PANEL_THREADS) {
-            const float v = fabsf(P[i * GJB_BLOCK + t]);
-            if (v > bv) { bv = v; bi = (int)i; }           // NaN never wins
+        int bi = -1, fi = 0x7fffffff;
+        for (int64_t i = tid; i < n; i += GJB_PANEL_THREADS) {
+            if (us[i]) continue;
+            if (fi == 0x7fffffff) fi = (int)i;
+            const float v = fabsf(P[i * GJB_LDS + t]);
+            if (v > bv) { bv = v; bi = (int)i; }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
             const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            const int of = __shfl_xor_sync(0xffffffffu, fi, o);
             if (ov > bv || (ov == bv && oi >= 0 && (bi < 0 || oi < bi))) { bv = ov; bi = oi; }
+            fi = min(fi, of);
         }
-        if (lane == 0) { rv[wid] = bv; ri[wid] = bi; }
+        if (lane == 0) { rv[wid] = bv; ri[wid] = bi; rf[wid] = fi; }
         __syncthreads();
-        if (tid == 0) {
-            float v = rv[0];
-            int i0 = ri[0];
-            for (int w = 1; w < GJB_PANEL_THREADS / 32; w++)
-                if (rv[w] > v || (rv[w] == v && ri[w] >= 0 && (i0 < 0 || ri[w] < i0))) { v = rv[w]; i0 = ri[w]; }
-            if (i0 < 0 || !(v > 0.0f)) {
-                atomicExch(bad, 1);
-                i0 = (int)k;
-            }
-            s_p = i0;
-            piv[k] = i0;
+        // every warp reduces the warps' candidates: every thread knows the pivot
+        bv = rv[lane];
+        bi = ri[lane];
+        fi = rf[lane];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            const int of = __shfl_xor_sync(0xffffffffu, fi, o);
+            if (ov > bv || (ov == bv && oi >= 0 && (bi < 0 || oi < bi))) { bv = ov; bi = oi; }
+            fi = min(fi, of);
         }
-        __syncthreads();
-        const int64_t p = s_p;
-        if (p != k && tid < GJB_BLOCK) {
-            const float a = P[k * GJB_BLOCK + tid];
-            P[k * GJB_BLOCK + tid] = P[p * GJB_BLOCK + tid];
-            P[p * GJB_BLOCK + tid] = a;
+        int64_t p = bi;
+        if (bi < 0 || !(bv > 0.0f)) {               // no usable pivot: the column is singular
+            if (tid == 0) atomicExch(bad, 1);
+            p = fi < (int)n ? fi : k;
         }
-        __syncthreads();
-        const float pv = P[k * GJB_BLOCK + t];
+        float prow[GJB_BLOCK];
+#pragma unroll
+        for (int c = 0; c < GJB_BLOCK; c++) prow[c] = P[p * GJB_LDS + c];
+        const float pv = prow[t];
         const float inv = pv != 0.0f ? 1.0f / pv : 0.0f;
-        __syncthreads();
-        if (tid < GJB_BLOCK) P[k * GJB_BLOCK + tid] = (tid == t) ? inv : P[k * GJB_BLOCK + tid] * inv;
-        // every row's factor read before any row is changed
-        for (int64_t i = tid; i < n; i += GJB_PANEL_THREADS) fcol[i] = P[i * GJB_BLOCK + t];
-        __syncthreads();
-        for (int64_t e = tid; e < n * GJB_BLOCK; e += GJB_PANEL_THREADS) {
-            const int64_t i = e / GJB_BLOCK;
-            const int c = (int)(e % GJB_BLOCK);
-            if (i == k) continue;
-            const float f = fcol[i];
-            P[e] = (c == t) ? -f * inv : fmaf(-f, P[k * GJB_BLOCK + c], P[e]);
+        if (tid == 0) piv[k] = (int)p;
+        __syncthreads();                             // row p read by all before it changes
+        for (int64_t i = tid; i < n; i += GJB_PANEL_THREADS) {
+            float* row = P + i * GJB_LDS;
+            if (i == p) {
+#pragma unroll
+                for (int c = 0; c < GJB_BLOCK; c++) row[c] = (c == t) ? inv : prow[c] * inv;
+                us[i] = (int)(k + 1);
+            } else {
+                const float g = -row[t] * inv;
+#pragma unroll
+                for (int c = 0; c < GJB_BLOCK; c++) row[c] = (c == t) ? g : fmaf(g, prow[c], row[c]);
+            }
         }
-        __syncthreads();
     }
+    __syncthreads();
     for (int64_t e = tid; e < n * GJB_BLOCK; e += GJB_PANEL_THREADS) {
         const int64_t i = e / GJB_BLOCK;
         const int c = (int)(e % GJB_BLOCK);
-        if (c < b) M[i * ld + k0 + c] = P[e];
+        if (c < b) M[i * ld + k0 + c] = P[i * GJB_LDS + c];
+    }
+    for (int64_t i = tid; i < n; i += GJB_PANEL_THREADS) used[i] = us[i];
+}
+
+// The same panel with each thread's rows in registers (n <= GJR_THREADS x
+// GJR_RPT): a pivot step shares only the candidates and the pivot row
+// through shared memory. The step loop is unrolled so every register index
+// is static.
+constexpr int GJR_THREADS = 512, GJR_RPT = 6, GJR_W = 8;
+
+template <int W>
+__global__ void __launch_bounds__(GJR_THREADS, 1)
+gjb_panel_reg_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b, int* __restrict__ piv,
+                     int* __restrict__ used, int* __restrict__ bad) {
+    __shared__ float rv[GJR_THREADS / 32];
+    __shared__ int ri[GJR_THREADS / 32];
+    __shared__ int rf[GJR_THREADS / 32];
+    __shared__ float prow_s[W];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    float R[GJR_RPT][W];
+    int us[GJR_RPT];
+#pragma unroll
+    for (int r = 0; r < GJR_RPT; r++) {
+        const int64_t i = tid + (int64_t)r * GJR_THREADS;
+        us[r] = i < n ? used[i] : 1;
+#pragma unroll
+        for (int c = 0; c < W; c++) R[r][c] = (i < n && c < b) ? M[i * ld + k0 + c] : 0.0f;
+    }
+#pragma unroll
+    for (int t = 0; t < W; t++) {
+        if (t >= b) break;
+        const int64_t k = k0 + t;
+        float bv = -1.0f;
+        int bi = -1, fi = 0x7fffffff;
+#pragma unroll
+        for (int r = 0; r < GJR_RPT; r++) {
+            if (us[r]) continue;
+            const int i = tid + r * GJR_THREADS;
+            fi = min(fi, i);
+            const float v = fabsf(R[r][t]);
+            if (v > bv || (v == bv && bi >= 0 && i < bi)) { bv = v; bi = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            const int of = __shfl_xor_sync(0xffffffffu, fi, o);
+            if (ov > bv || (ov == bv && oi >= 0 && (bi < 0 || oi < bi))) { bv = ov; bi = oi; }
+            fi = min(fi, of);
+        }
+        if (lane == 0) { rv[wid] = bv; ri[wid] = bi; rf[wid] = fi; }
+        __syncthreads();
+        bv = lane < GJR_THREADS / 32 ? rv[lane] : -1.0f;
+        bi = lane < GJR_THREADS / 32 ? ri[lane] : -1;
+        fi = lane < GJR_THREADS / 32 ? rf[lane] : 0x7fffffff;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            const int of = __shfl_xor_sync(0xffffffffu, fi, o);
+            if (ov > bv || (ov == bv && oi >= 0 && (bi < 0 || oi < bi))) { bv = ov; bi = oi; }
+            fi = min(fi, of);
+        }
+        int p = bi;
+        if (bi < 0 || !(bv > 0.0f)) {               // no usable pivot: the column is singular
+            if (tid == 0) atomicExch(bad, 1);
+            p = fi < (int)n ? fi : (int)k;
+        }
+        // the pivot row's owner publishes it
+        if (p % GJR_THREADS == tid) {
+            const int slot = p / GJR_THREADS;
+#pragma unroll
+            for (int r = 0; r < GJR_RPT; r++)
+                if (r == slot)
+#pragma unroll
+                    for (int c = 0; c < W; c++) prow_s[c] = R[r][c];
+        }
+        if (tid == 0) piv[k] = p;
+        __syncthreads();
+        // the pivot row is read from shared memory (broadcast) where it is used
+        const float pv = prow_s[t];
+        const float inv = pv != 0.0f ? 1.0f / pv : 0.0f;
+#pragma unroll
+        for (int r = 0; r < GJR_RPT; r++) {
+            const int i = tid + r * GJR_THREADS;
+            if (i == p) {
+#pragma unroll
+                for (int c = 0; c < W; c++) R[r][c] = (c == t) ? inv : prow_s[c] * inv;
+                us[r] = (int)(k + 1);
+            } else {
+                const float g = -R[r][t] * inv;
+#pragma unroll
+                for (int c = 0; c < W; c++) R[r][c] = (c == t) ? g : fmaf(g, prow_s[c], R[r][c]);
+            }
+        }
+        __syncthreads();                             // prow_s and the candidates are reused next step
+    }
+#pragma unroll
+    for (int r = 0; r < GJR_RPT; r++) {
+        const int64_t i = tid + (int64_t)r * GJR_THREADS;
+        if (i >= n) continue;
+#pragma unroll
+        for (int c = 0; c < W; c++)
+            if (c < b) M[i * ld + k0 + c] = R[r][c];
+        used[i] = us[r];
     }
 }
 
-// the panel's row interchanges on every other column, then X_B (b x n) aside
-__global__ void gjb_swap_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b,
-                                const int* __restrict__ piv, float* __restrict__ XB) {
+// X_B: the block's pivot rows on every other column
+__global__ void gjb_gather_kernel(const float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b,
+                                  const int* __restrict__ piv, float* __restrict__ XB) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n || (j >= k0 && j < k0 + b)) return;
-    for (int t = 0; t < b; t++) {
-        const int64_t p = piv[k0 + t];
-        if (p != k0 + t && p > k0 + t && p < n) {
-            const float a = M[(k0 + t) * ld + j];
-            M[(k0 + t) * ld + j] = M[p * ld + j];
-            M[p * ld + j] = a;
-        }
-    }
-    for (int t = 0; t < b; t++) XB[(int64_t)t * n + j] = M[(k0 + t) * ld + j];
+    for (int t = 0; t < b; t++) XB[(int64_t)t * n + j] = M[(int64_t)piv[k0 + t] * ld + j];
 }
 
-// M[i, j] = (i pivot row ? 0 : M[i, j]) + sum_t P[i, t] XB[t, j] for every
-// column j outside the panel; a CTA per 32 rows x 128 columns
+// M[i, j] = (i pivot row of the block ? 0 : M[i, j]) + sum_t P[i, t] XB[t, j]
+// for every column j outside the panel; a CTA per 32 rows x 128 columns
 constexpr int GJB_TR = 32, GJB_TC = 128;
 __global__ void __launch_bounds__(256)
-gjb_update_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b, const float* __restrict__ XB) {
+gjb_update_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b, const float* __restrict__ XB,
+                  const int* __restrict__ used) {
     __shared__ float Ps[GJB_TR][GJB_BLOCK];
     __shared__ float Xs[GJB_BLOCK][GJB_TC];
+    __shared__ int pivrow[GJB_TR];
     const int64_t i0 = (int64_t)blockIdx.y * GJB_TR, j0 = (int64_t)blockIdx.x * GJB_TC;
     for (int e = threadIdx.x; e < GJB_TR * GJB_BLOCK; e += 256) {
         const int r = e / GJB_BLOCK, t = e % GJB_BLOCK;
@@ -744,6 +911,11 @@ gjb_update_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int 
         const int t = e / GJB_TC, c = e % GJB_TC;
         Xs[t][c] = (t < b && j0 + c < n) ? XB[(int64_t)t * n + j0 + c] : 0.0f;
     }
+    if (threadIdx.x < GJB_TR) {
+        const int64_t i = i0 + threadIdx.x;
+        const int u = i < n ? used[i] - 1 : -1;
+        pivrow[threadIdx.x] = (u >= k0 && u < k0 + b) ? 1 : 0;
+    }
     __syncthreads();
     const int c = threadIdx.x % GJB_TC;
     const int64_t j = j0 + c;
@@ -751,24 +923,20 @@ gjb_update_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int 
     for (int r = threadIdx.x / GJB_TC; r < GJB_TR; r += 256 / GJB_TC) {
         const int64_t i = i0 + r;
         if (i >= n) break;
-        float acc = (i >= k0 && i < k0 + b) ? 0.0f : M[i * ld + j];
+        float acc = pivrow[r] ? 0.0f : M[i * ld + j];
 #pragma unroll
         for (int t = 0; t < GJB_BLOCK; t++) acc = fmaf(Ps[r][t], Xs[t][c], acc);
         M[i * ld + j] = acc;
     }
 }
 
-__global__ void gj_swap_columns_f32_kernel(float* __restrict__ M, int64_t m, int64_t ld, const int* __restrict__ piv) {
-    const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
-    if (i >= m) return;
-    for (int64_t k = m - 1; k >= 0; k--) {
-        const int64_t p = piv[k];
-        if (p != k && p >= 0 && p < m) {
-            const float t = M[i * ld + k];
-            M[i * ld + k] = M[i * ld + p];
-            M[i * ld + p] = t;
-        }
-    }
+// A^-1[k, pi(j)] = R[pi(k), j], from a copy R of the in-place result
+__global__ void gj_unpermute_kernel(const float* __restrict__ R, float* __restrict__ M, int64_t n, int64_t ld,
+                                    const int* __restrict__ piv) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * n) return;
+    const int64_t k = e / n, j = e % n;
+    M[k * ld + piv[j]] = R[(int64_t)piv[k] * n + j];
 }
 
 // ---------------------------------------------------------------------------
@@ -1032,41 +1200,53 @@ int mbem_knn(const float* points, int64_t n, int k, int64_t* idx, void* stream) 
                  "knn needs 1 <= k <= min(%d, n)", KNN_MAX);
     MBEM_REQUIRE(n < INT32_MAX, MBEM_ERR_SIZE, "too many nodes for knn");
     if (n == 0) return MBEM_OK;
-    knn_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(points, n, k, idx);
+    knn_kernel<<<(unsigned)ceil_div(n, KNN_QPB), 256, 0, (cudaStream_t)stream>>>(points, n, k, idx);
     return launch_status("knn_kernel");
 }
 
 size_t mbem_dense_inverse_f32_workspace_size(int64_t n) {
-    return (size_t)GJB_BLOCK * n * sizeof(float) + (size_t)(n + 8) * sizeof(int) + 256;
+    return (size_t)GJB_BLOCK * n * sizeof(float) + (size_t)n * n * sizeof(float) + (size_t)(2 * n + 8) * sizeof(int) +
+           4 * 256;
 }
 
 int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t work_bytes, void* stream) {
     MBEM_REQUIRE(n >= 0 && ld >= n && (n == 0 || M), MBEM_ERR_ARG, "bad matrix for the inverse");
     if (n == 0) return MBEM_OK;
-    const size_t panel = (size_t)n * (GJB_BLOCK + 1) * sizeof(float);
+    const size_t panel = (size_t)n * (GJB_LDS + 1) * sizeof(float);
     constexpr size_t kSmem = 227 * 1024 - 1024;      // the panel kernel's static arrays take the rest
     MBEM_REQUIRE(panel <= kSmem && ceil_div(n, GJB_TR) <= 65535, MBEM_ERR_UNSUPPORTED,
                  "the FP32 inverse holds its n x %d panel in shared memory: n <= %d", GJB_BLOCK,
-                 (int)(kSmem / ((GJB_BLOCK + 1) * sizeof(float))));
+                 (int)(kSmem / ((GJB_LDS + 1) * sizeof(float))));
     MBEM_REQUIRE(work && work_bytes >= mbem_dense_inverse_f32_workspace_size(n), MBEM_ERR_SIZE,
                  "inverse workspace too small");
     cudaStream_t st = (cudaStream_t)stream;
-    float* XB = static_cast<float*>(work);
-    int* piv = reinterpret_cast<int*>(XB + (size_t)GJB_BLOCK * n);
-    int* bad = piv + n;
+    char* w = static_cast<char*>(work);
+    auto take = [&](size_t bytes) { char* p = w; w += (bytes + 255) & ~(size_t)255; return p; };
+    float* XB = reinterpret_cast<float*>(take((size_t)GJB_BLOCK * n * sizeof(float)));
+    float* R = reinterpret_cast<float*>(take((size_t)n * n * sizeof(float)));
+    int* piv = reinterpret_cast<int*>(take((size_t)n * sizeof(int)));
+    int* used = reinterpret_cast<int*>(take((size_t)n * sizeof(int)));
+    int* bad = reinterpret_cast<int*>(take(sizeof(int)));
+    cudaMemsetAsync(used, 0, n * sizeof(int), st);
     cudaMemsetAsync(bad, 0, sizeof(int), st);
     cudaError_t ce = cudaFuncSetAttribute(gjb_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
     if (ce != cudaSuccess) return set_error(MBEM_ERR_CUDA, "inverse smem attribute: %s", cudaGetErrorString(ce));
     const dim3 ug((unsigned)ceil_div(n, GJB_TC), (unsigned)ceil_div(n, GJB_TR));
     int launches = 0;
-    for (int64_t k0 = 0; k0 < n; k0 += GJB_BLOCK) {
-        const int b = (int)lmin(GJB_BLOCK, n - k0);
-        gjb_panel_kernel<<<1, GJB_PANEL_THREADS, panel, st>>>(M, n, ld, k0, b, piv, bad);
-        gjb_swap_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(M, n, ld, k0, b, piv, XB);
-        gjb_update_kernel<<<ug, 256, 0, st>>>(M, n, ld, k0, b, XB);
+    const bool reg = n <= (int64_t)GJR_THREADS * GJR_RPT;       // the register panel, GJR_W columns a step
+    const int width = reg ? GJR_W : GJB_BLOCK;
+    for (int64_t k0 = 0; k0 < n; k0 += width) {
+        const int b = (int)lmin(width, n - k0);
+        if (reg)
+            gjb_panel_reg_kernel<GJR_W><<<1, GJR_THREADS, 0, st>>>(M, n, ld, k0, b, piv, used, bad);
+        else
+            gjb_panel_kernel<<<1, GJB_PANEL_THREADS, panel, st>>>(M, n, ld, k0, b, piv, used, bad);
+        gjb_gather_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(M, n, ld, k0, b, piv, XB);
+        gjb_update_kernel<<<ug, 256, 0, st>>>(M, n, ld, k0, b, XB, used);
         launches += 3;
     }
-    gj_swap_columns_f32_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(M, n, ld, piv);
+    cudaMemcpy2DAsync(R, n * sizeof(float), M, ld * sizeof(float), n * sizeof(float), n, cudaMemcpyDeviceToDevice, st);
+    gj_unpermute_kernel<<<(unsigned)ceil_div(n * n, 256), 256, 0, st>>>(R, M, n, ld, piv);
     count_launches(launches + 1);
     int e = launch_status("gauss_jordan_f32");
     if (e) return e;
@@ -1118,31 +1298,37 @@ size_t mbem_nn_apply_workspace_size(int64_t n, int64_t n_coarse) {
     return (size_t)(n + 2 * n_coarse) * sizeof(double) + 2 * (size_t)((lmax(n, n_coarse) + 15) / 16 * 16) * 4 + 64;
 }
 
-int mbem_nn_setup_mixed(const mbem_inner_bf16* inner, const mbem_nn_precond* nn, const double* shift, int n_shift,
-                        void* work, size_t work_bytes, void* stream) {
+}  // extern "C"
+
+namespace mbem {
+
+// A Phi (FP32) by the gather kernel from A (BF16 or FP64 rows at ld), the
+// near blocks added, then A_c (+ U U^T) and its FP32 inverse
+template <typename T>
+static int nn_setup32(const T* A, int64_t ld, int n_near, const mbem_near_blocks* near, const mbem_nn_precond* nn,
+                      const double* shift, int n_shift, void* work, size_t work_bytes, cudaStream_t st) {
     int e = nn_check(nn);
     if (e) return e;
-    MBEM_REQUIRE(inner && inner->A16 && inner->n == nn->n && inner->ld16 >= inner->n, MBEM_ERR_ARG,
-                 "bad BF16 inner operator");
-    MBEM_REQUIRE(nn->APhi32 && nn->Ac_inv32, MBEM_ERR_ARG, "the mixed setup writes FP32 APhi32 and Ac_inv32");
+    MBEM_REQUIRE(A && ld >= nn->n, MBEM_ERR_ARG, "bad operator for the coarse setup");
+    MBEM_REQUIRE(nn->APhi32 && nn->Ac_inv32, MBEM_ERR_ARG, "the FP32 setup writes APhi32 and Ac_inv32");
     MBEM_REQUIRE(n_shift >= 0 && (n_shift == 0 || shift != nullptr), MBEM_ERR_ARG, "bad coarse shift");
     const int64_t n = nn->n, nc = nn->n_coarse, ldp = nn->ld32;
     if (n == 0) return MBEM_OK;
     const mbem_block_jacobi* bj = nn->bj;
-    cudaStream_t st = (cudaStream_t)stream;
     const int64_t groups = ceil_div(bj->n_chunks, APHI16_GROUP);
     MBEM_REQUIRE(groups <= 65535 * 32 && ceil_div(n, APHI16_ROWS) <= 65535 && nc <= 65535, MBEM_ERR_UNSUPPORTED,
                  "learned preconditioner sizes beyond one launch");
     const size_t smem = (size_t)APHI16_GROUP * MBEM_BJ_MAX_DOF * (NCV * sizeof(float) + sizeof(int));
-    cudaError_t ce = cudaFuncSetAttribute(nn_aphi_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t ce = cudaFuncSetAttribute(nn_aphi_gather_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem);
     if (ce != cudaSuccess) return set_error(MBEM_ERR_CUDA, "APhi smem attribute: %s", cudaGetErrorString(ce));
     float* APhi = const_cast<float*>(nn->APhi32);
     float* Ac = const_cast<float*>(nn->Ac_inv32);
-    nn_aphi_bf16_kernel<<<dim3((unsigned)groups, (unsigned)ceil_div(n, APHI16_ROWS)), 256, smem, st>>>(
-        inner->A16, inner->ld16, n, bj->chunk_ptr, bj->dofs, bj->n_chunks, nn->basis, APhi, ldp);
-    if ((e = launch_status("nn_aphi_bf16_kernel"))) return e;
-    for (int q = 0; q < inner->n_near; q++) {
-        const mbem_near_blocks& nb = inner->near[q];
+    nn_aphi_gather_kernel<T><<<dim3((unsigned)groups, (unsigned)ceil_div(n, APHI16_ROWS)), 256, smem, st>>>(
+        A, ld, n, bj->chunk_ptr, bj->dofs, bj->n_chunks, nn->basis, APhi, ldp);
+    if ((e = launch_status("nn_aphi_gather_kernel"))) return e;
+    for (int q = 0; q < n_near; q++) {
+        const mbem_near_blocks& nb = near[q];
         if (nb.n_field == 0) continue;
         nn_aphi_near_kernel<<<(unsigned)ceil_div(nb.n_field * 32, 256), 256, 0, st>>>(nb, bj->chunk_of, nn->basis,
                                                                                     APhi, ldp);
@@ -1156,7 +1342,25 @@ int mbem_nn_setup_mixed(const mbem_inner_bf16* inner, const mbem_nn_precond* nn,
                                                                                                 n_shift);
         if ((e = launch_status("nn_coarse_shift_f32_kernel"))) return e;
     }
-    return mbem_dense_inverse_f32(Ac, nc, ldp, work, work_bytes, stream);
+    return mbem_dense_inverse_f32(Ac, nc, ldp, work, work_bytes, st);
+}
+
+}  // namespace mbem
+
+extern "C" {
+
+int mbem_nn_setup_mixed(const mbem_inner_bf16* inner, const mbem_nn_precond* nn, const double* shift, int n_shift,
+                        void* work, size_t work_bytes, void* stream) {
+    MBEM_REQUIRE(inner && inner->A16 && nn && inner->n == nn->n && inner->ld16 >= inner->n, MBEM_ERR_ARG,
+                 "bad BF16 inner operator");
+    return nn_setup32(inner->A16, inner->ld16, inner->n_near, inner->near, nn, shift, n_shift, work, work_bytes,
+                      (cudaStream_t)stream);
+}
+
+int mbem_nn_setup_dense32(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift, int n_shift,
+                          void* work, size_t work_bytes, void* stream) {
+    return nn_setup32(A, ld, 0, (const mbem_near_blocks*)nullptr, nn, shift, n_shift, work, work_bytes,
+                      (cudaStream_t)stream);
 }
 
 int mbem_nn_apply(const mbem_nn_precond* nn, const double* r, double* z, void* stream) {

@@ -203,8 +203,15 @@ class LearnedPreconditioner:
 
     PRECOND_KIND = 2
 
-    def __init__(self, asm, params, bj=None):
+    def __init__(self, asm, params, bj=None, setup: str = "fp32"):
+        """``setup``: "fp32" (the default: device node features, A Phi with
+        FP32 products, FP32 coarse inverse) or "fp64" (host features, FP64 A
+        Phi and Gauss-Jordan; a dense FP64 system only)."""
+        if setup not in ("fp32", "fp64"):
+            raise ValueError(f"setup must be 'fp32' or 'fp64' (got {setup!r})")
         mixed = asm.A is None
+        if mixed and setup == "fp64":
+            raise ValueError("the mixed operator's setup is FP32")
         if mixed and getattr(asm, "op", None) is None:
             raise NotImplementedError("the learned preconditioner needs a dense FP64 system or a mixed operator")
         self.bj = bj if bj is not None else asm.block_jacobi()
@@ -214,7 +221,7 @@ class LearnedPreconditioner:
         import time
         t0 = time.perf_counter()
         self.params = torch.as_tensor(np.asarray(params, np.float32)).to(dev)
-        if mixed:
+        if setup == "fp32":
             self.feat = node_features_device(asm, self.bj)
         else:
             self.feat = torch.from_numpy(node_features(asm.layout, self.bj.chunk_nodes())).to(dev)
@@ -230,8 +237,8 @@ class LearnedPreconditioner:
                                 device=dev)
         self._bj_struct = self.bj.struct()
         st = stream_handle()
-        if mixed:
-            self._setup_mixed(asm, n, nc, shift, dev, st, t0, t1)
+        if setup == "fp32":
+            self._setup32(asm, n, nc, shift, dev, st, t0)
             return
         self.APhi = torch.empty((n, nc), dtype=torch.float64, device=dev)
         self.Ac_inv = torch.empty((nc, nc), dtype=torch.float64, device=dev)
@@ -252,11 +259,12 @@ class LearnedPreconditioner:
         self.setup_s = {"features_host": t1 - t0, "basis_device": t2 - t1, "coarse_operator_device": t3 - t2,
                         "coarse_inverse_device": t4 - t3}
 
-    def _setup_mixed(self, asm, n, nc, shift, dev, st, t0, t1):
-        """The mixed operator's setup: A Phi (FP32) from its BF16 inner
-        operator, A_c and its FP32 inverse (mbem_nn_setup_mixed)."""
+    def _setup32(self, asm, n, nc, shift, dev, st, t0):
+        """The FP32 setup: A Phi from the mixed operator's BF16 inner operator
+        (mbem_nn_setup_mixed) or from the dense FP64 matrix
+        (mbem_nn_setup_dense32), A_c and its FP32 inverse."""
         import time
-        inner = asm.bf16_inner()
+        inner = asm.bf16_inner() if asm.A is None else None
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         ld32 = (nc + 3) // 4 * 4
@@ -268,15 +276,20 @@ class LearnedPreconditioner:
                                      Ac_inv32=ptr(self.Ac_inv32), ld32=ld32)
         need = int(nat.lib().mbem_dense_inverse_f32_workspace_size(nc))
         inv_work = torch.empty(need, dtype=torch.uint8, device=dev)
-        saved = inner.precond
-        inner.precond = None
-        ist = inner.struct()
-        inner.precond = saved
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        nat.call("mbem_nn_setup_mixed", ctypes.byref(ist), ctypes.byref(self._struct),
-                 ptr(shift) if shift is not None else None, 0 if shift is None else shift.shape[1], ptr(inv_work),
-                 need, st)
+        sh = (ptr(shift) if shift is not None else None, 0 if shift is None else shift.shape[1])
+        if inner is not None:
+            saved = inner.precond
+            inner.precond = None
+            ist = inner.struct()
+            inner.precond = saved
+            nat.call("mbem_nn_setup_mixed", ctypes.byref(ist), ctypes.byref(self._struct), *sh, ptr(inv_work), need,
+                     st)
+        else:
+            A = asm.A
+            nat.call("mbem_nn_setup_dense32", ptr(A), A.stride(0), ctypes.byref(self._struct), *sh, ptr(inv_work),
+                     need, st)
         self.built = True
         t3 = time.perf_counter()
         self.setup_s = {"features_device": t1 - t0, "basis_device": t2 - t1, "coarse_operator_and_inverse": t3 - t2}

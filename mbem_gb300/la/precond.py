@@ -52,63 +52,77 @@ def cluster_leaves(points: np.ndarray, max_nodes: int) -> list:
     return leaves
 
 
+def _segment_sums(v: torch.Tensor, ends: torch.Tensor) -> torch.Tensor:
+    """Sums of v (m, ...) over consecutive segments ending (exclusive) at ``ends``."""
+    c = torch.cumsum(v, dim=0)
+    c = torch.cat([torch.zeros_like(c[:1]), c])
+    starts = torch.cat([torch.zeros_like(ends[:1]), ends[:-1]])
+    return c[ends] - c[starts]
+
+
 def cluster_order_device(points: torch.Tensor, max_nodes: int):
     """The bisection tree of ``cluster_leaves`` built level by level on the
     device: returns (order (m,) int64 CUDA, leaf sizes (L,) host int64), the
     leaves as consecutive runs of ``order`` in the tree order of
     ``cluster_leaves``. Each split is the one ``cluster_leaves`` makes
     (median of the projection on the leading principal axis, ``proj <
-    median`` to the left, halves by rank when the projections coincide);
-    the 3 x 3 eigenproblems of a level are solved together on the host. Where
-    the two leading principal axes are degenerate the axis, and so the split,
-    may differ from the host's."""
+    median`` to the left, halves by rank when the projections coincide).
+    A level costs one small copy each way: the segments' sizes and 3 x 3
+    covariances to the host, whose eigenproblems are solved together there,
+    and their principal axes back. Where the two leading principal axes are
+    degenerate the axis, and so the split, may differ from the host's."""
     dev = points.device
     m = int(points.shape[0])
     order = torch.arange(m, dtype=torch.int64, device=dev)
-    sizes = np.array([m], np.int64)
-    while m and sizes.max() > max_nodes:
-        S = sizes.size
-        seg = torch.repeat_interleave(torch.arange(S, device=dev), torch.from_numpy(sizes).to(dev))
+    sizes = torch.tensor([m], dtype=torch.int64, device=dev)
+    pos = torch.arange(m, device=dev)
+    while m:
+        S = int(sizes.numel())
+        ends = torch.cumsum(sizes, 0)
+        starts = ends - sizes
+        is_start = torch.zeros(m + 1, dtype=torch.int64, device=dev)
+        is_start[starts] = 1
+        seg = torch.cumsum(is_start[:m], 0) - 1
         P = points[order]
-        cnt = torch.from_numpy(sizes).to(dev, torch.float64)
-        mean = torch.zeros((S, 3), dtype=torch.float64, device=dev).index_add_(0, seg, P) / cnt[:, None]
+        cnt = sizes.to(torch.float64)
+        mean = _segment_sums(P, ends) / cnt[:, None]
         X = P - mean[seg]
-        cov = torch.zeros((S, 3, 3), dtype=torch.float64, device=dev).index_add_(0, seg, X[:, :, None] * X[:, None, :])
-        big = sizes > max_nodes
+        cov = _segment_sums((X[:, :, None] * X[:, None, :]).reshape(m, 9), ends)
+        host = torch.cat([cnt[:, None], cov], dim=1).cpu().numpy()
+        sz_h = host[:, 0].astype(np.int64)
+        big = sz_h > max_nodes
+        if not big.any():
+            break
         axis = np.zeros((S, 3))
-        if big.any():
-            _, vecs = np.linalg.eigh(cov[torch.from_numpy(big).to(dev)].cpu().numpy())
-            axis[big] = vecs[:, :, -1]
+        _, vecs = np.linalg.eigh(host[big, 1:].reshape(-1, 3, 3))
+        axis[big] = vecs[:, :, -1]
         proj = (X * torch.from_numpy(axis).to(dev)[seg]).sum(dim=1)
         # projections sorted within each segment (stable: ties keep the current order)
         by_proj = torch.argsort(proj, stable=True)
         srt = by_proj[torch.argsort(seg[by_proj], stable=True)]
         sproj = proj[srt]
-        start = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
-        lo = torch.from_numpy(start + (sizes - 1) // 2).to(dev)
-        hi = torch.from_numpy(start + sizes // 2).to(dev)
-        median = 0.5 * (sproj[lo] + sproj[hi])
+        median = 0.5 * (sproj[starts + (sizes - 1) // 2] + sproj[starts + sizes // 2])
         bigd = torch.from_numpy(big).to(dev)
         left = (proj < median[seg]) & bigd[seg]
-        n_left = torch.zeros(S, dtype=torch.int64, device=dev).index_add_(0, seg, left.long())
-        nl = n_left.cpu().numpy()
-        flat = big & ((nl == 0) | (nl == sizes))
-        if flat.any():
-            # coincident projections: the lower half by rank goes left
-            rank = torch.empty(m, dtype=torch.int64, device=dev)
-            rank[srt] = torch.arange(m, device=dev) - torch.from_numpy(start).to(dev)[seg[srt]]
-            halves = rank < torch.from_numpy(sizes // 2).to(dev)[seg]
-            fl = torch.from_numpy(flat).to(dev)[seg]
-            left = torch.where(fl, halves, left)
-            nl = np.where(flat, sizes // 2, nl)
+        nl = _segment_sums(left.long(), ends)
+        flat = bigd & ((nl == 0) | (nl == sizes))
+        # coincident projections: the lower half by rank goes left
+        rank = torch.empty(m, dtype=torch.int64, device=dev)
+        rank[srt] = pos - starts[seg[srt]]
+        left = torch.where(flat[seg], rank < (sizes // 2)[seg], left)
+        nl = torch.where(flat, sizes // 2, nl)
         # stable partition: each segment's left part, then its right part
         key = 2 * seg + (~left).long() * bigd[seg].long()
         order = order[torch.argsort(key, stable=True)]
-        new = []
-        for sz, b, l in zip(sizes, big, nl):
-            new.extend([l, sz - l] if b else [sz])
-        sizes = np.array(new, np.int64)
-    return order, sizes
+        # the new segment list: a big segment becomes (left, right)
+        n_new = 1 + bigd.long()
+        new_start = torch.cumsum(n_new, 0) - n_new
+        new_sizes = torch.empty(int(S + big.sum()), dtype=torch.int64, device=dev)
+        new_sizes[new_start] = torch.where(bigd, nl, sizes)
+        bi = new_start[bigd] + 1
+        new_sizes[bi] = (sizes - nl)[bigd]
+        sizes = new_sizes
+    return order, sizes.cpu().numpy()
 
 
 class BlockJacobi:

@@ -33,7 +33,7 @@ def _inverse(M, ld=None):
     return buf[:, :n]
 
 
-@pytest.mark.parametrize("n, ld", [(1, 1), (5, 8), (16, 16), (17, 20), (100, 100), (1000, 1004), (3072, 3072)])
+@pytest.mark.parametrize("n, ld", [(1, 1), (5, 8), (16, 16), (17, 20), (100, 100), (1000, 1004), (3072, 3072), (3200, 3204)])
 def test_dense_inverse_f32(gpu, n, ld):
     g = torch.Generator(device="cpu").manual_seed(n)
     A = (torch.randn(n, n, generator=g, dtype=torch.float64) + 2.0 * np.sqrt(n) * torch.eye(n, dtype=torch.float64))
