@@ -781,110 +781,6 @@ gjb_panel_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b
     for (int64_t i = tid; i < n; i += GJB_PANEL_THREADS) used[i] = us[i];
 }
 
-// The same panel with each thread's rows in registers (n <= GJR_THREADS x
-// GJR_RPT): a pivot step shares only the candidates and the pivot row
-// through shared memory. The step loop is unrolled so every register index
-// is static.
-constexpr int GJR_THREADS = 512, GJR_RPT = 6, GJR_W = 8;
-
-template <int W>
-__global__ void __launch_bounds__(GJR_THREADS, 1)
-gjb_panel_reg_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b, int* __restrict__ piv,
-                     int* __restrict__ used, int* __restrict__ bad) {
-    __shared__ float rv[GJR_THREADS / 32];
-    __shared__ int ri[GJR_THREADS / 32];
-    __shared__ int rf[GJR_THREADS / 32];
-    __shared__ float prow_s[W];
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    float R[GJR_RPT][W];
-    int us[GJR_RPT];
-#pragma unroll
-    for (int r = 0; r < GJR_RPT; r++) {
-        const int64_t i = tid + (int64_t)r * GJR_THREADS;
-        us[r] = i < n ? used[i] : 1;
-#pragma unroll
-        for (int c = 0; c < W; c++) R[r][c] = (i < n && c < b) ? M[i * ld + k0 + c] : 0.0f;
-    }
-#pragma unroll
-    for (int t = 0; t < W; t++) {
-        if (t >= b) break;
-        const int64_t k = k0 + t;
-        float bv = -1.0f;
-        int bi = -1, fi = 0x7fffffff;
-#pragma unroll
-        for (int r = 0; r < GJR_RPT; r++) {
-            if (us[r]) continue;
-            const int i = tid + r * GJR_THREADS;
-            fi = min(fi, i);
-            const float v = fabsf(R[r][t]);
-            if (v > bv || (v == bv && bi >= 0 && i < bi)) { bv = v; bi = i; }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            const int of = __shfl_xor_sync(0xffffffffu, fi, o);
-            if (ov > bv || (ov == bv && oi >= 0 && (bi < 0 || oi < bi))) { bv = ov; bi = oi; }
-            fi = min(fi, of);
-        }
-        if (lane == 0) { rv[wid] = bv; ri[wid] = bi; rf[wid] = fi; }
-        __syncthreads();
-        bv = lane < GJR_THREADS / 32 ? rv[lane] : -1.0f;
-        bi = lane < GJR_THREADS / 32 ? ri[lane] : -1;
-        fi = lane < GJR_THREADS / 32 ? rf[lane] : 0x7fffffff;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            const int of = __shfl_xor_sync(0xffffffffu, fi, o);
-            if (ov > bv || (ov == bv && oi >= 0 && (bi < 0 || oi < bi))) { bv = ov; bi = oi; }
-            fi = min(fi, of);
-        }
-        int p = bi;
-        if (bi < 0 || !(bv > 0.0f)) {               // no usable pivot: the column is singular
-            if (tid == 0) atomicExch(bad, 1);
-            p = fi < (int)n ? fi : (int)k;
-        }
-        // the pivot row's owner publishes it
-        if (p % GJR_THREADS == tid) {
-            const int slot = p / GJR_THREADS;
-#pragma unroll
-            for (int r = 0; r < GJR_RPT; r++)
-                if (r == slot)
-#pragma unroll
-                    for (int c = 0; c < W; c++) prow_s[c] = R[r][c];
-        }
-        if (tid == 0) piv[k] = p;
-        __syncthreads();
-        // the pivot row is read from shared memory (broadcast) where it is used
-        const float pv = prow_s[t];
-        const float inv = pv != 0.0f ? 1.0f / pv : 0.0f;
-#pragma unroll
-        for (int r = 0; r < GJR_RPT; r++) {
-            const int i = tid + r * GJR_THREADS;
-            if (i == p) {
-#pragma unroll
-                for (int c = 0; c < W; c++) R[r][c] = (c == t) ? inv : prow_s[c] * inv;
-                us[r] = (int)(k + 1);
-            } else {
-                const float g = -R[r][t] * inv;
-#pragma unroll
-                for (int c = 0; c < W; c++) R[r][c] = (c == t) ? g : fmaf(g, prow_s[c], R[r][c]);
-            }
-        }
-        __syncthreads();                             // prow_s and the candidates are reused next step
-    }
-#pragma unroll
-    for (int r = 0; r < GJR_RPT; r++) {
-        const int64_t i = tid + (int64_t)r * GJR_THREADS;
-        if (i >= n) continue;
-#pragma unroll
-        for (int c = 0; c < W; c++)
-            if (c < b) M[i * ld + k0 + c] = R[r][c];
-        used[i] = us[r];
-    }
-}
-
 // X_B: the block's pivot rows on every other column
 __global__ void gjb_gather_kernel(const float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b,
                                   const int* __restrict__ piv, float* __restrict__ XB) {
@@ -1233,14 +1129,9 @@ int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t w
     if (ce != cudaSuccess) return set_error(MBEM_ERR_CUDA, "inverse smem attribute: %s", cudaGetErrorString(ce));
     const dim3 ug((unsigned)ceil_div(n, GJB_TC), (unsigned)ceil_div(n, GJB_TR));
     int launches = 0;
-    const bool reg = n <= (int64_t)GJR_THREADS * GJR_RPT;       // the register panel, GJR_W columns a step
-    const int width = reg ? GJR_W : GJB_BLOCK;
-    for (int64_t k0 = 0; k0 < n; k0 += width) {
-        const int b = (int)lmin(width, n - k0);
-        if (reg)
-            gjb_panel_reg_kernel<GJR_W><<<1, GJR_THREADS, 0, st>>>(M, n, ld, k0, b, piv, used, bad);
-        else
-            gjb_panel_kernel<<<1, GJB_PANEL_THREADS, panel, st>>>(M, n, ld, k0, b, piv, used, bad);
+    for (int64_t k0 = 0; k0 < n; k0 += GJB_BLOCK) {
+        const int b = (int)lmin(GJB_BLOCK, n - k0);
+        gjb_panel_kernel<<<1, GJB_PANEL_THREADS, panel, st>>>(M, n, ld, k0, b, piv, used, bad);
         gjb_gather_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(M, n, ld, k0, b, piv, XB);
         gjb_update_kernel<<<ug, 256, 0, st>>>(M, n, ld, k0, b, XB, used);
         launches += 3;

@@ -53,11 +53,15 @@ def cluster_leaves(points: np.ndarray, max_nodes: int) -> list:
 
 
 def _segment_sums(v: torch.Tensor, ends: torch.Tensor) -> torch.Tensor:
-    """Sums of v (m, ...) over consecutive segments ending (exclusive) at ``ends``."""
-    c = torch.cumsum(v, dim=0)
-    c = torch.cat([torch.zeros_like(c[:1]), c])
+    """Sums of v (m,) or (m, q) over consecutive segments ending (exclusive)
+    at ``ends``: prefix sums along the contiguous dimension of v^T (a scan
+    down the rows of a tall, narrow matrix is slow on the device)."""
+    t = v.reshape(v.shape[0], -1).T.contiguous()
+    c = torch.cumsum(t, dim=1)
+    c = torch.cat([torch.zeros_like(c[:, :1]), c], dim=1)
     starts = torch.cat([torch.zeros_like(ends[:1]), ends[:-1]])
-    return c[ends] - c[starts]
+    out = (c[:, ends] - c[:, starts]).T
+    return out.reshape((ends.shape[0],) + tuple(v.shape[1:]))
 
 
 def cluster_order_device(points: torch.Tensor, max_nodes: int):
