@@ -1,0 +1,221 @@
+// The far-field quadrature of the P0 pair kernels in FP32, shared by the mixed
+// operator (mixed.cu) and the compressed pair operator (aca.cu): collapsed
+// Gauss-Legendre rules on the source triangle, per-source constants, the
+// near / far decision and the T (double layer) and U (single layer) blocks.
+#pragma once
+#include <math.h>
+
+#include "common.cuh"
+#include "dfloat.cuh"
+
+namespace mbem {
+
+// ---------------------------------------------------------------------------
+// quadrature rules: collapsed Gauss-Legendre n x n on (0,0),(1,0),(0,1)
+// ---------------------------------------------------------------------------
+constexpr int QR_MIN = 3, QR_MAX = 8;      // P0 uses n = 3..6; nodal densities up to 8
+constexpr int QR_POINTS = 9 + 16 + 25 + 36 + 49 + 64;
+
+struct QuadRules {
+    float a[QR_POINTS];    // xi1 - 1/3
+    float b[QR_POINTS];    // xi2 - 1/3
+    float w[QR_POINTS];    // weights, sum 1/2 per rule
+    int off[QR_MAX + 1];
+};
+
+// Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on P_n.
+static void gauss_legendre(int n, double* x, double* w) {
+    for (int i = 0; i < n; i++) {
+        double z = cos(MBEM_PI * (i + 0.75) / (n + 0.5));
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; k++) {
+                double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            double dp = n * (z * p1 - p0) / (z * z - 1.0);
+            double dz = p1 / dp;
+            z -= dz;
+            if (fabs(dz) < 1e-16) break;
+        }
+        double p0 = 1.0, p1 = z;
+        for (int k = 2; k <= n; k++) {
+            double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+            p0 = p1;
+            p1 = p2;
+        }
+        double dp = n * (z * p1 - p0) / (z * z - 1.0);
+        x[i] = z;
+        w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+static QuadRules make_rules() {
+    QuadRules r;
+    int k = 0;
+    for (int n = 0; n <= QR_MAX; n++) r.off[n] = 0;
+    for (int n = QR_MIN; n <= QR_MAX; n++) {
+        r.off[n] = k;
+        double g[QR_MAX], gw[QR_MAX];
+        gauss_legendre(n, g, gw);
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                const double gi = 0.5 * (g[i] + 1.0), gj = 0.5 * (g[j] + 1.0);
+                const double wi = 0.5 * gw[i], wj = 0.5 * gw[j];
+                const double x1 = gi, x2 = gj * (1.0 - gi);
+                r.a[k] = (float)(x1 - 1.0 / 3.0);
+                r.b[k] = (float)(x2 - 1.0 / 3.0);
+                r.w[k] = (float)(wi * wj * (1.0 - gi));
+                k++;
+            }
+    }
+    return r;
+}
+
+static const QuadRules& rules() {
+    static const QuadRules r = make_rules();
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// double-float helpers
+// ---------------------------------------------------------------------------
+// (a_hi + a_lo) - (b_hi + b_lo) rounded to FP32 with the hi difference exact
+// (Knuth's TwoSum; the _rn intrinsics keep the compiler from contracting or
+// reassociating the error-free steps)
+__device__ __forceinline__ float df_diff(F2 a, F2 b) {
+    const float s = __fsub_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(-b.hi, bb));
+    return __fadd_rn(s, __fadd_rn(err, __fsub_rn(a.lo, b.lo)));
+}
+
+// ---------------------------------------------------------------------------
+// per-source far-field constants
+// ---------------------------------------------------------------------------
+struct SrcFar {
+    F2 c[3];            // centroid
+    float e1[3], e2[3]; // edges from vertex 0
+    float n[3];         // normal as passed (T kernel)
+    float area2, eps2;
+    float L2;           // longest edge squared
+    float rnear2;       // near radius squared
+    bool ok;
+};
+
+__device__ __forceinline__ void far_setup(const double* __restrict__ tv, const double* __restrict__ nrm,
+                                          double eps, double near_factor, SrcFar& s) {
+    const double e1x = tv[3] - tv[0], e1y = tv[4] - tv[1], e1z = tv[5] - tv[2];
+    const double e2x = tv[6] - tv[0], e2y = tv[7] - tv[1], e2z = tv[8] - tv[2];
+    const double e3x = tv[6] - tv[3], e3y = tv[7] - tv[4], e3z = tv[8] - tv[5];
+    const double cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
+    const double a2 = sqrt(cx * cx + cy * cy + cz * cz);
+    s.ok = a2 >= 1e-30;
+    const double l1 = sqrt(e1x * e1x + e1y * e1y + e1z * e1z);
+    const double l2 = sqrt(e2x * e2x + e2y * e2y + e2z * e2z);
+    const double l3 = sqrt(e3x * e3x + e3y * e3y + e3z * e3z);
+    const double Lm = fmax(fmax(l1, l2), l3);
+    const double h = (l1 + l2 + l3) / 3.0;    // mean edge length
+    const double rn = near_factor * fmax(eps, h);
+    for (int k = 0; k < 3; k++) s.c[k] = split_d((tv[k] + tv[3 + k] + tv[6 + k]) / 3.0);
+    s.e1[0] = (float)e1x; s.e1[1] = (float)e1y; s.e1[2] = (float)e1z;
+    s.e2[0] = (float)e2x; s.e2[1] = (float)e2y; s.e2[2] = (float)e2z;
+    if (nrm) {
+        s.n[0] = (float)nrm[0]; s.n[1] = (float)nrm[1]; s.n[2] = (float)nrm[2];
+    } else {
+        s.n[0] = s.n[1] = s.n[2] = 0.0f;
+    }
+    s.area2 = (float)a2;
+    s.eps2 = (float)(eps * eps);
+    s.L2 = (float)(Lm * Lm);
+    const double r2 = fmax(rn * rn, 2.25 * Lm * Lm);
+    s.rnear2 = (float)r2;
+}
+
+// The one near/far decision, shared by every kernel that needs it.
+__device__ __forceinline__ bool is_near(const F2 x[3], const SrcFar& s, float d[3], float& D2) {
+    d[0] = df_diff(x[0], s.c[0]);
+    d[1] = df_diff(x[1], s.c[1]);
+    d[2] = df_diff(x[2], s.c[2]);
+    D2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    return D2 < s.rnear2;
+}
+
+__device__ __forceinline__ int far_rule(float D2, float L2) {
+    // n by D / L_max (measured against the FP64 closed form: <= ~1.5e-7)
+    if (D2 >= 50.0f * L2) return 3;        // D/L >= 7.07
+    if (D2 >= 8.0f * L2) return 4;         // D/L >= 2.83
+    if (D2 >= 3.125f * L2) return 5;       // D/L >= 1.77
+    return 6;
+}
+
+// Far T block (FP32): out_ij = n_j alpha_i + n_i beta_j + d_ij gamma - 6 c5 W_ij
+// from the quadrature sums V3 = int d/R^3, V5 = int d/R^5,
+// t = int d |d|^2/R^5, W = int d d (d.n)/R^5 (d = x - y).
+template <bool TKERNEL>
+__device__ __forceinline__ void far_block(const QuadRules& Q, const SrcFar& s, const float dc[3], float D2,
+                                          const float c[6], float out[3][3]) {
+    const int nq = far_rule(D2, s.L2);
+    const int q0 = Q.off[nq], q1 = q0 + nq * nq;
+    float V3[3] = {0, 0, 0}, V5[3] = {0, 0, 0}, t[3] = {0, 0, 0};
+    float W00 = 0, W01 = 0, W02 = 0, W11 = 0, W12 = 0, W22 = 0;
+    float I1 = 0, I3 = 0;   // U kernel: int 1/R, int 1/R^3
+    for (int q = q0; q < q1; q++) {
+        const float a = Q.a[q], b = Q.b[q];
+        const float dx = dc[0] - (a * s.e1[0] + b * s.e2[0]);
+        const float dy = dc[1] - (a * s.e1[1] + b * s.e2[1]);
+        const float dz = dc[2] - (a * s.e1[2] + b * s.e2[2]);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float iR = rsqrtf(r2 + s.eps2);
+        const float w = Q.w[q];
+        const float iR2 = iR * iR;
+        const float w3 = w * iR2 * iR;
+        if (TKERNEL) {
+            const float w5 = w3 * iR2;
+            V3[0] += w3 * dx; V3[1] += w3 * dy; V3[2] += w3 * dz;
+            V5[0] += w5 * dx; V5[1] += w5 * dy; V5[2] += w5 * dz;
+            const float wt = w5 * r2;
+            t[0] += wt * dx; t[1] += wt * dy; t[2] += wt * dz;
+            const float wn = w5 * (dx * s.n[0] + dy * s.n[1] + dz * s.n[2]);
+            const float ux = wn * dx, uy = wn * dy, uz = wn * dz;
+            W00 += ux * dx; W01 += ux * dy; W02 += ux * dz;
+            W11 += uy * dy; W12 += uy * dz; W22 += uz * dz;
+        } else {
+            I1 += w * iR;
+            I3 += w3;
+            const float ux = w3 * dx, uy = w3 * dy, uz = w3 * dz;   // T2[3] = int d d / R^3
+            W00 += ux * dx; W01 += ux * dy; W02 += ux * dz;
+            W11 += uy * dy; W12 += uy * dz; W22 += uz * dz;
+        }
+    }
+    const float A = s.area2;
+    const float W[3][3] = {{W00, W01, W02}, {W01, W11, W12}, {W02, W12, W22}};
+    if (TKERNEL) {
+        const float* n = s.n;
+        const float nV3 = n[0] * V3[0] + n[1] * V3[1] + n[2] * V3[2];
+        const float nV5 = n[0] * V5[0] + n[1] * V5[1] + n[2] * V5[2];
+        const float ca = c[0] + 4.0f * c[1] + 2.0f * c[4];
+        const float cb = c[3] + c[4];
+        const float ce3 = c[2] * s.eps2, ce6 = c[5] * s.eps2;
+        const float gam = cb * nV3 + ce6 * nV5;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float al = ca * V3[i] - 3.0f * c[1] * t[i] + ce3 * V5[i];
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const float be = cb * V3[j] + ce6 * V5[j];
+                out[i][j] = A * (n[j] * al + n[i] * be - 6.0f * c[4] * W[i][j] + (i == j ? gam : 0.0f));
+            }
+        }
+    } else {
+        const float dg = c[0] * I1 + c[1] * s.eps2 * I3;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) out[i][j] = A * (c[2] * W[i][j] + (i == j ? dg : 0.0f));
+    }
+}
+
+
+}  // namespace mbem

@@ -322,6 +322,40 @@ def make_condense_small(path):
     np.savez_compressed(path, **out)
 
 
+def make_compressed_small(path):
+    """The reference's compressed pair operator (``la/hop.py``
+    ``PairCompressed``, T kernel, default tolerance and partition rules) on
+    the 12x12-per-face cube with eps = h/2: its partition (admissible and
+    dense blocks as element index lists), its statistics, and its material
+    view applied to a seeded random vector for mu = lam = 1."""
+    from mbem.la.hop import PairCompressed
+    import mbem.kernels.basis as kb
+
+    _, cube, _ = reference_cube_model(12, 8, 1.0, 1.0)
+    eps = (4.0 / 12) / 2.0
+    t0 = time.time()
+    pc = PairCompressed(cube, cube, "H", np.full(cube.n_triangles, eps), n_workers=1)
+    c = kb.t_coeffs(1.0, 1.0)
+    x = np.random.default_rng(12).normal(size=3 * cube.n_triangles)
+    y = pc.matvec(c, x)
+    part = pc._part
+
+    def flat(blocks):
+        rows = np.concatenate([r for r, _ in blocks]) if blocks else np.zeros(0, np.int64)
+        cols = np.concatenate([c_ for _, c_ in blocks]) if blocks else np.zeros(0, np.int64)
+        rp = np.concatenate([[0], np.cumsum([len(r) for r, _ in blocks])])
+        cp = np.concatenate([[0], np.cumsum([len(c_) for _, c_ in blocks])])
+        return rows, cols, rp, cp
+    ar, ac, arp, acp = flat(part.admissible)
+    dr, dc, drp, dcp = flat(part.dense)
+    print(f"compressed_small: {time.time() - t0:.1f} s; {pc.summary()}", flush=True)
+    np.savez_compressed(path, cube_vertices=cube.vertices, cube_triangles=cube.triangles, eps=eps, coeffs=c, x=x,
+                        y=y, adm_rows=ar, adm_cols=ac, adm_rptr=arp, adm_cptr=acp, dense_rows=dr, dense_cols=dc,
+                        dense_rptr=drp, dense_cptr=dcp, n_lowrank=pc.n_lowrank, n_dense=pc.n_dense,
+                        n_capped=pc.n_capped, n_retry=pc.n_retry, n_fallback=pc.n_fallback,
+                        max_verified_err=pc.max_verified_err, tol=pc.tol)
+
+
 def make_volume_small(path):
     """The volume sampler on the small cube + fault system (3 x 3 per face,
     fault 2 x 2, eps = h/2): a padded grid with points outside the body, its
@@ -421,6 +455,7 @@ def make_volume_regions(path):
 CASES = {"p0_pairs": make_p0_pairs, "cube_small": make_cube_small,
          "c1_rows": make_c1_rows, "nodal_pairs": make_nodal_pairs,
          "traction_small": make_traction_small, "condense_small": make_condense_small,
+         "compressed_small": make_compressed_small,
          "volume_small": make_volume_small,
          "volume_regions": make_volume_regions}
 
