@@ -908,6 +908,103 @@ def volume_workload(n_face=24, n_fault=16, n_grid=62, pad_cells=2, n_cpu=1024, c
     return out
 
 
+def compressed_workload(peaks, n_face=128, reps=20, cpu=True):
+    """The compressed pair operator (la/hop.py PairCompressed) on the cube's
+    self pair, T kernel, mu = lam = 1, eps = h/2: 128 x 128 per face is
+    196,608 elements, 589,824 unknowns, whose dense FP64 matrix (2.8 TB) is
+    ten times this GPU's HBM and whose mixed operator (FP32 far field + BF16
+    copy, 2.1 TB) would not fit either. Times the partition (host), the
+    material view's build (cross approximation of every admissible block,
+    dense blocks), and the product: device time with CUDA events over
+    back-to-back products (the working set, ~50 GB, is far above L2), and
+    end to end from a pinned host vector to a host result. The CPU baseline
+    is the C port of the reference's flat product (oracle/p0_oracle.c
+    oracle_flat_matvec, OpenMP on every host core) on the same factors."""
+    import torch
+    from mbem_gb300 import mesh
+    from mbem_gb300.kernels import basis as kb
+    from mbem_gb300.la.compressed import PairCompressed
+    cube = mesh.cube(n_face)
+    n = cube.n_triangles
+    eps = (4.0 / n_face) / 2
+    c = kb.t_coeffs(1.0, 1.0)
+    t0 = time.perf_counter()
+    pc = PairCompressed(cube, cube, "H", eps)
+    t_part = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    view = pc._view(c)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    st = pc.view_stats(c)
+    x = torch.randn(3 * n, dtype=torch.float64, device="cuda")
+    y = torch.empty(3 * n, dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        pc.apply_device(view, x, y)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        pc.apply_device(view, x, y)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    # end to end: pinned host x in, host y out, every product
+    xh = torch.randn(3 * n, dtype=torch.float64).pin_memory()
+    yh = torch.empty(3 * n, dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        x.copy_(xh, non_blocking=True)
+        pc.apply_device(view, x, y)
+        yh.copy_(y, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) / reps * 1e3
+    factor_bytes = st["lowrank_bytes"] + st["dense_bytes"]
+    vec_bytes = 8 * 3 * n * 2 + 4 * 3 * n * 2
+    achieved = (factor_bytes + vec_bytes) / (ms / 1e3) / 1e9
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    ranks = st["ranks"]
+    out = {"config": {"workload": f"cube{n_face} self pair, T kernel", "elements": n, "unknowns": 3 * n,
+                      "dense_fp64_bytes": 8 * (3 * n) ** 2, "tol": pc.tol,
+                      "l2": f"working set {factor_bytes / 1e9:.1f} GB, far above L2"},
+           "partition_s": t_part, "view_build_s": t_build, "view_build_breakdown_s": st["build_s"],
+           "n_admissible": pc.n_lowrank, "n_dense": pc.n_dense, "n_capped": st["n_capped"],
+           "n_retry": st["n_retry"], "n_fallback": st["n_fallback"], "max_verified_err": st["max_verified_err"],
+           "rank_columns": {"mean": float(ranks.mean()) if ranks.size else 0.0,
+                            "median": float(np.median(ranks)) if ranks.size else 0.0,
+                            "max": int(ranks.max()) if ranks.size else 0},
+           "lowrank_bytes": st["lowrank_bytes"], "dense_bytes": st["dense_bytes"], "held_bytes": pc.nbytes(),
+           "matvec_ms": ms, "gpu_launches_per_matvec": 3,
+           "e2e": {"value": e2e_ms, "unit": "ms per product", "h2d_bytes_per_step": 8 * 3 * n,
+                   "d2h_bytes_per_step": 8 * 3 * n},
+           "roofline": {"kernel": "compressed matvec (cm_gather + cm_project + cm_strip)", "bound": "hbm",
+                        "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                        "bytes_per_launch": factor_bytes + vec_bytes, "launch_ms": ms,
+                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks.get("hbm_gbs")
+                        else "fallback 6.8 TB/s (of fallback)"}}
+    if cpu:
+        from oracle import oracle as orc
+        threads = orc.set_threads(os.cpu_count() or 1)
+        host = pc.view_host(c)
+        xv = x.cpu().numpy()
+        y_gpu = pc.matvec(c, xv)
+        orc.flat_matvec(host, xv)
+        t0 = time.perf_counter()
+        n_cpu = 3
+        for _ in range(n_cpu):
+            y_cpu = orc.flat_matvec(host, xv)
+        cpu_ms = (time.perf_counter() - t0) / n_cpu * 1e3
+        out["cpu_baseline"] = {"value": cpu_ms, "unit": "ms per product", "cores": threads, "kind": "port",
+                               "sample": f"{n_cpu} complete products of the same factors (C port of "
+                                         f"flatview.py _flat_matvec, FP32 storage, FP64 sums); host "
+                                         f"{os.uname().machine}",
+                               "max_rel_diff_vs_gpu": float(np.linalg.norm(y_cpu - y_gpu) / np.linalg.norm(y_cpu))}
+        del host
+    del view, pc
+    torch.cuda.empty_cache()
+    return out
+
+
 def extra_workloads(args, peaks):
     out = {}
     for name, fn in (("volume_cube24_grid66", lambda: volume_workload(cpu=not args.skip_cpu)),
@@ -917,7 +1014,10 @@ def extra_workloads(args, peaks):
                      ("dense_lu_cube35", dense_lu_workload),
                      ("fault_traction_cube32_learned", fault_traction_workload),
                      ("fault_traction_cube32_dip60_learned", lambda: fault_traction_workload(dip=60.0)),
-                     ("p2_readout_1m", p2_readout_workload)):
+                     ("p2_readout_1m", p2_readout_workload),
+                     ("compressed_cube128_self_H", lambda: compressed_workload(peaks, cpu=not args.skip_cpu))):
+        if args.extra and name not in args.extra.split(","):
+            continue
         try:
             out[name] = fn()
         except Exception as err:     # one workload failing must not hide the headline
@@ -1133,6 +1233,7 @@ def main():
     ap.add_argument("--skip-variant", action="store_true", help="skip timing the other mixed preconditioner")
     ap.add_argument("--skip-extra", action="store_true",
                     help="skip the many-right-hand-side and FAULT_TRACTION workloads")
+    ap.add_argument("--extra", default="", help="comma-separated names of the extra workloads to run (default: all)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

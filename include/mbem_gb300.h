@@ -716,6 +716,122 @@ int mbem_solid_angle_sum(const float* records, const double* tri_verts, int64_t 
 int mbem_mesh_distance(const float* records, const double* tri_verts, int64_t n_tri, const double* points,
                        int64_t n_pts, double max_edge, double* dist, int64_t* idx, void* stream);
 
+/* ---- compressed pair operator: one (field mesh, source mesh, kernel) pair
+ * with P0 sources, its admissible blocks in low-rank form and the rest
+ * dense (src/mbem/la/hop.py:137 PairCompressed, :489 matvec; la/aca.py
+ * compress_block / aca_single; la/flatview.py FlatView). Elements are
+ * numbered in the cluster-tree order, so that every block is a pair of
+ * contiguous element ranges; the caller keeps the permutation. Factors and
+ * dense blocks are stored in FP32 (the reference's storage type at a block
+ * tolerance >= 1e-5, flatview.py:127-136). ------------------------------ */
+typedef struct {
+    int kernel;                /* 0 T ("H", 6 coefficients), 1 U ("G", 3) */
+    const double* x_field;     /* (n_field, 3) collocation points, tree order, device */
+    int64_t n_field;
+    const double* tri_verts;   /* (n_src, 9) source corners, tree order, device */
+    const double* normals;     /* (n_src, 3) source normals (T kernel), device */
+    const double* eps;         /* (n_src) mollifier radii, device */
+    int64_t n_src;
+    double coeffs[6];          /* basis.py t_coeffs / u_coeffs of the material */
+    double near_factor;        /* pairs within near_factor * max(eps, mean edge) or 1.5 longest edges
+                                  of the source centroid take the FP64 closed form, the rest the FP32
+                                  far quadrature (the mixed operator's split) */
+    void* prep;                /* device, mbem_pair_prep_bytes; filled by mbem_pair_prepare */
+} mbem_pair_geometry;
+size_t mbem_pair_prep_bytes(int64_t n_field, int64_t n_src);
+int mbem_pair_prepare(const mbem_pair_geometry* g, void* stream);
+
+/* Cross approximation of a batch of admissible blocks (aca.py:334-419
+ * aca_single, :579-658 compress_block): one CTA per block, 3 x 3 element
+ * pivots, stopped when the residual on 10 x 10 sampled element pairs falls
+ * below tol / 2 of the sample's norm; certified on 3 random element rows and
+ * 3 random element columns evaluated exactly; a certificate above 3 tol
+ * reruns the block at tol / 10 and a second failure, or the rank cap,
+ * leaves the block to be applied exactly. Factors are written transposed:
+ * U^T (3 max_pivots[i] rows of pad4(3 nr[i]) floats) at U + u_off[i] and
+ * V^T likewise at V + v_off[i] (offsets multiples of 4 floats). */
+#define MBEM_ACA_LOWRANK 0
+#define MBEM_ACA_CAPPED 1       /* the rank cap was reached: apply exactly */
+#define MBEM_ACA_FAILED 2       /* the retry failed its certificate too: apply exactly */
+#define MBEM_ACA_RETRIED 4      /* flag: the first certificate failed */
+typedef struct {
+    int64_t n_blocks;
+    const int32_t* r0;          /* device (n_blocks): first field element of each block */
+    const int32_t* nr;          /*   field elements */
+    const int32_t* c0;          /*   first source element */
+    const int32_t* nc;          /*   source elements */
+    const int32_t* max_pivots;  /*   rank cap in element pivots (aca.py:618-620) */
+    const int64_t* u_off;       /*   float offsets of each block's factors */
+    const int64_t* v_off;
+    float* U;
+    float* V;
+    int32_t* rank;              /* out: factor columns, 3 x pivots (0 unless low rank) */
+    int32_t* status;            /* out: MBEM_ACA_* */
+    float* err;                 /* out: certified relative Frobenius error of the factors kept */
+    double tol;                 /* block tolerance (BLOCK_COMPRESSION_TOL) */
+    uint64_t seed;              /* sample and certificate lines of block i come from (seed, first_index + i) */
+    int64_t first_index;
+    int max_nr, max_nc, max_pivots_all;  /* maxima over the batch (shared-memory size) */
+} mbem_aca_batch;
+int mbem_aca_compress(const mbem_pair_geometry* g, const mbem_aca_batch* b, void* stream);
+/* Copies the first rank[i] rows of each block's U^T and V^T from the batch
+ * scratch to their final offsets. */
+int mbem_aca_compact(int64_t n_blocks, const int32_t* nr, const int32_t* nc, const int32_t* rank,
+                     const int64_t* u_src, const int64_t* v_src, const float* U_src, const float* V_src,
+                     const int64_t* u_dst, const int64_t* v_dst, float* U_dst, float* V_dst, void* stream);
+/* Dense blocks (flatview.py:41-118 dense_leaves): block i as a (3 nr, pad4(3 nc))
+ * row-major FP32 matrix at D + d_off[i]; col_ptr (n_blocks + 1) is the prefix
+ * sum of nc (one thread per block column). */
+int mbem_pair_dense_blocks(const mbem_pair_geometry* g, int64_t n_blocks, const int32_t* r0, const int32_t* nr,
+                           const int32_t* c0, const int32_t* nc, const int64_t* d_off, const int64_t* col_ptr,
+                           float* D, void* stream);
+
+/* The flat operator of one material (FlatView): low-rank blocks, dense
+ * blocks, and the field rows cut into strips (the finest ranges every block's
+ * rows are a union of); strip s owns rows [strip_r0, strip_r0 + strip_nr)
+ * (elements) and applies the blocks strip_items[strip_ptr[s] ..
+ * strip_ptr[s+1]) in that order (id < n_lr: low rank; else n_lr + dense id),
+ * so every output row has one writer and a fixed summation order. */
+typedef struct {
+    int64_t n_field, n_src;       /* elements */
+    const int64_t* field_order;   /* device: tree position -> field element */
+    const int64_t* src_order;     /* device: tree position -> source element */
+    int64_t n_lr;
+    const int32_t* lr_r0;
+    const int32_t* lr_nr;
+    const int32_t* lr_c0;
+    const int32_t* lr_nc;
+    const int32_t* lr_rank;       /* factor columns */
+    const int64_t* lr_u;          /* float offsets of U^T / V^T (rank rows of pad4(3 n) floats) */
+    const int64_t* lr_v;
+    const int64_t* lr_w;          /* offsets into the rank-sized projections (sum of ranks) */
+    const float* U;
+    const float* V;
+    int64_t n_w;
+    int64_t n_dense;
+    const int32_t* d_r0;
+    const int32_t* d_nr;
+    const int32_t* d_c0;
+    const int32_t* d_nc;
+    const int64_t* d_off;
+    const float* D;
+    int64_t n_strips;
+    const int32_t* strip_r0;
+    const int32_t* strip_nr;
+    const int64_t* strip_ptr;
+    const int32_t* strip_items;
+    int max_strip;                /* largest strip_nr */
+    int max_lr_nc;                /* largest lr_nc */
+} mbem_compressed_view;
+size_t mbem_compressed_matvec_workspace_size(const mbem_compressed_view* v);
+/* y (3 n_field, original element order) = A x (3 n_src); FP32 factors and
+ * blocks, FP32 products summed per block, FP64 across blocks. */
+int mbem_compressed_matvec(const mbem_compressed_view* v, const double* x, double* y, void* work,
+                           size_t work_bytes, void* stream);
+/* The operator as a dense FP64 (3 n_field, 3 n_src) matrix at ld (original
+ * order), for checks at small sizes (FlatView.to_dense). */
+int mbem_compressed_to_dense(const mbem_compressed_view* v, double* out, int64_t ld, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

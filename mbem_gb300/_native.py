@@ -94,6 +94,33 @@ class MmReport(Structure):
                 ("cycles", c_int)]
 
 
+class PairGeometry(Structure):
+    _fields_ = [("kernel", c_int), ("x_field", c_void_p), ("n_field", c_int64), ("tri_verts", c_void_p),
+                ("normals", c_void_p), ("eps", c_void_p), ("n_src", c_int64), ("coeffs", c_double * 6),
+                ("near_factor", c_double), ("prep", c_void_p)]
+
+
+class AcaBatch(Structure):
+    _fields_ = [("n_blocks", c_int64), ("r0", c_void_p), ("nr", c_void_p), ("c0", c_void_p), ("nc", c_void_p),
+                ("max_pivots", c_void_p), ("u_off", c_void_p), ("v_off", c_void_p), ("U", c_void_p),
+                ("V", c_void_p), ("rank", c_void_p), ("status", c_void_p), ("err", c_void_p), ("tol", c_double),
+                ("seed", ctypes.c_uint64), ("first_index", c_int64), ("max_nr", c_int), ("max_nc", c_int),
+                ("max_pivots_all", c_int)]
+
+
+class CompressedView(Structure):
+    _fields_ = [("n_field", c_int64), ("n_src", c_int64), ("field_order", c_void_p), ("src_order", c_void_p),
+                ("n_lr", c_int64), ("lr_r0", c_void_p), ("lr_nr", c_void_p), ("lr_c0", c_void_p),
+                ("lr_nc", c_void_p), ("lr_rank", c_void_p), ("lr_u", c_void_p), ("lr_v", c_void_p),
+                ("lr_w", c_void_p), ("U", c_void_p), ("V", c_void_p), ("n_w", c_int64), ("n_dense", c_int64),
+                ("d_r0", c_void_p), ("d_nr", c_void_p), ("d_c0", c_void_p), ("d_nc", c_void_p),
+                ("d_off", c_void_p), ("D", c_void_p), ("n_strips", c_int64), ("strip_r0", c_void_p),
+                ("strip_nr", c_void_p), ("strip_ptr", c_void_p), ("strip_items", c_void_p), ("max_strip", c_int),
+                ("max_lr_nc", c_int)]
+
+
+ACA_LOWRANK, ACA_CAPPED, ACA_FAILED, ACA_RETRIED = 0, 1, 2, 4
+
 MM_SEGMENT = 512
 MM_MAX_RESTART = 64
 
@@ -224,6 +251,14 @@ _SIGNATURES = {
     "mbem_mm_solve": (c_int, [_P, _P, _P, c_double, c_int, c_int, POINTER(MmReport), _P]),
     "mbem_mm_check": (c_int, [_P]),
     "mbem_mm_solve_mixed": (c_int, [_P, _P, _P, c_double, c_double, c_int, c_int, c_int, POINTER(MmReport), _P]),
+    "mbem_pair_prep_bytes": (c_size_t, [_I, _I]),
+    "mbem_pair_prepare": (c_int, [POINTER(PairGeometry), _P]),
+    "mbem_aca_compress": (c_int, [POINTER(PairGeometry), POINTER(AcaBatch), _P]),
+    "mbem_aca_compact": (c_int, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "mbem_pair_dense_blocks": (c_int, [POINTER(PairGeometry), _I, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "mbem_compressed_matvec_workspace_size": (c_size_t, [POINTER(CompressedView)]),
+    "mbem_compressed_matvec": (c_int, [POINTER(CompressedView), _P, _P, _P, c_size_t, _P]),
+    "mbem_compressed_to_dense": (c_int, [POINTER(CompressedView), _P, _I, _P]),
 }
 
 _lib = None

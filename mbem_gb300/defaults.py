@@ -57,3 +57,18 @@ MIXED_BLOCK = 64                      # BF16 scale block (rows x columns)
 MIXED_NEAR_RADIUS_FACTOR = 3.0        # near field: centroid distance < 3 max(eps, h)
 MIXED_INNER_ITERATIONS = 40           # at most this many BF16 inner GMRES steps per outer step
 MIXED_INNER_RTOL = 1e-5               # ... or until the inner residual estimate is this small
+
+# ---- compressed pair operator (defaults.py:128-320 of the reference) ----
+BLOCK_COMPRESSION_TOL = 1e-4           # relative Frobenius tolerance of an admissible block
+CLUSTER_MIN_LEAF = 96                  # cluster-tree leaves hold at most this many elements
+ADMISSIBILITY_ETA = 2.0                # admissible: min(diam_f, diam_s) < eta * dist(box_f, box_s)
+ACA_MIN_BLOCK = 64                     # admissible blocks with a side below this are dense
+MAX_ADMISSIBLE_BLOCK = 1024            # admissible blocks have at most this many elements a side
+ACA_MAX_RANK_FRACTION = 1.0 / 3.0      # rank cap in element pivots, of the shorter side
+ACA_CERTIFY_LINES = 3                  # exact element rows and columns of the certificate
+ACA_CERTIFY_FACTOR = 3.0               # certificate limit, times the tolerance
+ACA_RETRY_TOL_FACTOR = 10.0            # a failed certificate reruns the block at tol / this
+ACA_SEED = 12345                       # seed of the sample and certificate lines
+COMPRESSED_NEAR_RADIUS_FACTOR = MIXED_NEAR_RADIUS_FACTOR   # FP64 closed form inside this radius
+COMPRESSED_SCRATCH_BYTES = 4 << 30     # cross-approximation scratch per batch of blocks
+COMPRESSED_VIEW_CACHE = 4              # material views kept per pair operator

@@ -16,6 +16,7 @@
  */
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #ifdef _OPENMP
@@ -735,4 +736,78 @@ void oracle_dgemv(const double *A, int64_t n_rows, int64_t n_cols, const double 
         for (int64_t c = 0; c < n_cols; c++) acc += a[c] * x[c];
         y[r] = acc;
     }
+}
+
+/* ====================================================================== */
+/* Flat compressed product (flatview.py FlatView.matvec, _flat_matvec)     */
+/* ====================================================================== */
+/* y = A x for the flat layout of one material view: low-rank block i with
+ * U^T (rank rows of pad4(3 nr) floats) at U + lr_u[i] and V^T likewise at
+ * V + lr_v[i]; dense block d row-major (3 nr, pad4(3 nc)) at D + d_off[d];
+ * element ranges in the tree order (field_order / src_order map positions to
+ * elements). Phase 1 forms w_i = V_i^T x per block; phase 2 owns rows: strip
+ * s adds the blocks strip_items[strip_ptr[s] .. strip_ptr[s+1]) in order.
+ * FP32 storage, FP64 arithmetic (as the reference). */
+static inline int64_t pad4_64(int64_t n) { return (n + 3) / 4 * 4; }
+
+void oracle_flat_matvec(int64_t n_field, int64_t n_src, const int64_t *field_order,
+                        const int64_t *src_order, int64_t n_lr, const int32_t *lr_r0,
+                        const int32_t *lr_nr, const int32_t *lr_c0, const int32_t *lr_nc,
+                        const int32_t *lr_rank, const int64_t *lr_u, const int64_t *lr_v,
+                        const int64_t *lr_w, const float *U, const float *V, int64_t n_w,
+                        const int32_t *d_r0, const int32_t *d_nc, const int32_t *d_c0,
+                        const int64_t *d_off, const float *D, int64_t n_strips,
+                        const int32_t *strip_r0, const int32_t *strip_nr, const int64_t *strip_ptr,
+                        const int32_t *strip_items, const double *x, double *y) {
+    double *xs = (double *)malloc(sizeof(double) * (size_t)(3 * n_src + 1));
+    double *w = (double *)malloc(sizeof(double) * (size_t)(n_w + 1));
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < n_src; p++)
+        for (int a = 0; a < 3; a++) xs[3 * p + a] = x[3 * src_order[p] + a];
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n_lr; i++) {
+        const int64_t nc3 = 3 * (int64_t)lr_nc[i], ldv = pad4_64(nc3);
+        const double *xc = xs + 3 * (int64_t)lr_c0[i];
+        for (int k = 0; k < lr_rank[i]; k++) {
+            const float *row = V + lr_v[i] + k * ldv;
+            double acc = 0.0;
+            for (int64_t c = 0; c < nc3; c++) acc += (double)row[c] * xc[c];
+            w[lr_w[i] + k] = acc;
+        }
+    }
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t s = 0; s < n_strips; s++) {
+        const int64_t R = 3 * (int64_t)strip_nr[s], sr0 = strip_r0[s];
+        double acc[3 * 1024];
+        double *a = R <= 3 * 1024 ? acc : (double *)malloc(sizeof(double) * (size_t)R);
+        for (int64_t r = 0; r < R; r++) a[r] = 0.0;
+        for (int64_t q = strip_ptr[s]; q < strip_ptr[s + 1]; q++) {
+            const int64_t id = strip_items[q];
+            if (id < n_lr) {
+                const int64_t ldu = pad4_64(3 * (int64_t)lr_nr[id]);
+                const float *Ub = U + lr_u[id] + 3 * (sr0 - lr_r0[id]);
+                const double *wi = w + lr_w[id];
+                for (int k = 0; k < lr_rank[id]; k++) {
+                    const float *u = Ub + k * ldu;
+                    for (int64_t r = 0; r < R; r++) a[r] += (double)u[r] * wi[k];
+                }
+            } else {
+                const int64_t d = id - n_lr;
+                const int64_t nc3 = 3 * (int64_t)d_nc[d], ld = pad4_64(nc3);
+                const float *Db = D + d_off[d] + 3 * (sr0 - d_r0[d]) * ld;
+                const double *xc = xs + 3 * (int64_t)d_c0[d];
+                for (int64_t r = 0; r < R; r++) {
+                    const float *row = Db + r * ld;
+                    double t = 0.0;
+                    for (int64_t c = 0; c < nc3; c++) t += (double)row[c] * xc[c];
+                    a[r] += t;
+                }
+            }
+        }
+        for (int64_t r = 0; r < R; r++) y[3 * field_order[sr0 + r / 3] + r % 3] = a[r];
+        if (a != acc) free(a);
+    }
+    (void)n_field;
+    free(xs);
+    free(w);
 }

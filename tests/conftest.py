@@ -90,3 +90,14 @@ def rel_err(a, b) -> float:
 @pytest.fixture(scope="session")
 def condense_small():
     return load_golden("condense_small")
+
+
+@pytest.fixture(scope="session")
+def compressed_small():
+    return load_golden("compressed_small")
+
+
+def golden_blocks(g: dict, key: str) -> list:
+    """A block list stored flat (rows, cols and their offsets) as (rows, cols) pairs."""
+    rows, cols, rp, cp = (g[f"{key}_{s}"] for s in ("rows", "cols", "rptr", "cptr"))
+    return [(rows[rp[i]:rp[i + 1]], cols[cp[i]:cp[i + 1]]) for i in range(rp.size - 1)]

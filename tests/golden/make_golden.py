@@ -324,21 +324,16 @@ def make_condense_small(path):
 
 def make_compressed_small(path):
     """The reference's compressed pair operator (``la/hop.py``
-    ``PairCompressed``, T kernel, default tolerance and partition rules) on
-    the 12x12-per-face cube with eps = h/2: its partition (admissible and
+    ``PairCompressed``, default tolerance and partition rules) for the pair
+    (field: the 12x12-per-face cube's centroids, source: the 16x16 centre
+    fault, eps = h_fault / 2), both kernels: its partition (admissible and
     dense blocks as element index lists), its statistics, and its material
-    view applied to a seeded random vector for mu = lam = 1."""
+    view (mu = lam = 1) applied to a seeded random vector. Also the
+    partition alone (no kernel work) of the 24x24-per-face cube's self pair,
+    whose tree has admissible blocks at several levels."""
+    from mbem.la.cluster import build_cluster_tree, build_partition
     from mbem.la.hop import PairCompressed
     import mbem.kernels.basis as kb
-
-    _, cube, _ = reference_cube_model(12, 8, 1.0, 1.0)
-    eps = (4.0 / 12) / 2.0
-    t0 = time.time()
-    pc = PairCompressed(cube, cube, "H", np.full(cube.n_triangles, eps), n_workers=1)
-    c = kb.t_coeffs(1.0, 1.0)
-    x = np.random.default_rng(12).normal(size=3 * cube.n_triangles)
-    y = pc.matvec(c, x)
-    part = pc._part
 
     def flat(blocks):
         rows = np.concatenate([r for r, _ in blocks]) if blocks else np.zeros(0, np.int64)
@@ -346,14 +341,42 @@ def make_compressed_small(path):
         rp = np.concatenate([[0], np.cumsum([len(r) for r, _ in blocks])])
         cp = np.concatenate([[0], np.cumsum([len(c_) for _, c_ in blocks])])
         return rows, cols, rp, cp
-    ar, ac, arp, acp = flat(part.admissible)
-    dr, dc, drp, dcp = flat(part.dense)
-    print(f"compressed_small: {time.time() - t0:.1f} s; {pc.summary()}", flush=True)
-    np.savez_compressed(path, cube_vertices=cube.vertices, cube_triangles=cube.triangles, eps=eps, coeffs=c, x=x,
-                        y=y, adm_rows=ar, adm_cols=ac, adm_rptr=arp, adm_cptr=acp, dense_rows=dr, dense_cols=dc,
-                        dense_rptr=drp, dense_cptr=dcp, n_lowrank=pc.n_lowrank, n_dense=pc.n_dense,
-                        n_capped=pc.n_capped, n_retry=pc.n_retry, n_fallback=pc.n_fallback,
-                        max_verified_err=pc.max_verified_err, tol=pc.tol)
+
+    out = {}
+    _, cube24, _ = reference_cube_model(24, 8, 1.0, 1.0)
+    tree = build_cluster_tree(kb.MeshArrays().field_points(cube24))
+    part = build_partition(tree, tree)
+    for key, blocks in (("self24_adm", part.admissible), ("self24_dense", part.dense)):
+        r, c_, rp, cp = flat(blocks)
+        out.update({f"{key}_rows": r, f"{key}_cols": c_, f"{key}_rptr": rp, f"{key}_cptr": cp})
+    out["self24_vertices"] = cube24.vertices
+    out["self24_triangles"] = cube24.triangles
+    print(f"compressed_small: cube-24 self partition {len(part.admissible)} admissible, "
+          f"{len(part.dense)} dense", flush=True)
+
+    _, cube, fault = reference_cube_model(12, 16, 1.0, 1.0)
+    eps = (1.0 / 16) / 2.0
+    x = np.random.default_rng(12).normal(size=3 * fault.n_triangles)
+    out.update(cube_vertices=cube.vertices, cube_triangles=cube.triangles, fault_vertices=fault.vertices,
+               fault_triangles=fault.triangles, eps=eps, x=x)
+    for kernel, coeffs in (("H", kb.t_coeffs(1.0, 1.0)), ("G", kb.u_coeffs(1.0, 1.0))):
+        t0 = time.time()
+        pc = PairCompressed(cube, fault, kernel, np.full(fault.n_triangles, eps), n_workers=1)
+        y = pc.matvec(coeffs, x)
+        p = pc._part
+        ar, ac, arp, acp = flat(p.admissible)
+        dr, dc, drp, dcp = flat(p.dense)
+        print(f"compressed_small {kernel}: {time.time() - t0:.1f} s; {pc.summary()}", flush=True)
+        view = pc._view(coeffs)
+        out.update({f"{kernel}_coeffs": coeffs, f"{kernel}_y": y, f"{kernel}_adm_rows": ar,
+                    f"{kernel}_adm_cols": ac, f"{kernel}_adm_rptr": arp, f"{kernel}_adm_cptr": acp,
+                    f"{kernel}_dense_rows": dr, f"{kernel}_dense_cols": dc, f"{kernel}_dense_rptr": drp,
+                    f"{kernel}_dense_cptr": dcp, f"{kernel}_n_lowrank": pc.n_lowrank,
+                    f"{kernel}_n_dense": pc.n_dense, f"{kernel}_n_capped": pc.n_capped,
+                    f"{kernel}_n_retry": pc.n_retry, f"{kernel}_n_fallback": pc.n_fallback,
+                    f"{kernel}_max_verified_err": pc.max_verified_err, f"{kernel}_tol": pc.tol,
+                    f"{kernel}_ranks": np.asarray(view.ranks), f"{kernel}_nbytes": view.nbytes()})
+    np.savez_compressed(path, **out)
 
 
 def make_volume_small(path):
