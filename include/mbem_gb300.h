@@ -744,7 +744,8 @@ int mbem_pair_prepare(const mbem_pair_geometry* g, void* stream);
 /* Cross approximation of a batch of admissible blocks (aca.py:334-419
  * aca_single, :579-658 compress_block): one CTA per block, 3 x 3 element
  * pivots, stopped when the residual on 10 x 10 sampled element pairs falls
- * below tol / 2 of the sample's norm; certified on 3 random element rows and
+ * below tol / 2 of the sample's norm; recompressed (see recompress_max);
+ * certified on 3 random element rows and
  * 3 random element columns evaluated exactly; a certificate above 3 tol
  * reruns the block at tol / 10 and a second failure, or the rank cap,
  * leaves the block to be applied exactly. Factors are written transposed:
@@ -766,12 +767,16 @@ typedef struct {
     float* U;
     float* V;
     int32_t* rank;              /* out: factor columns, 3 x pivots (0 unless low rank) */
-    int32_t* status;            /* out: MBEM_ACA_* */
+    int32_t* status;            /* out: MBEM_ACA_* in bits 0-2; bits 8-15 and 16-23: the sweeps of the
+                                   last recompression's two Jacobi passes (0: not recompressed) */
     float* err;                 /* out: certified relative Frobenius error of the factors kept */
     double tol;                 /* block tolerance (BLOCK_COMPRESSION_TOL) */
     uint64_t seed;              /* sample and certificate lines of block i come from (seed, first_index + i) */
     int64_t first_index;
     int max_nr, max_nc, max_pivots_all;  /* maxima over the batch (shared-memory size) */
+    int recompress_max;         /* converged factors of 2 .. recompress_max columns are recompressed (the
+                                   SVD of U V^T truncated at tol / 2, aca.py:422-438) before the
+                                   certificate; 0 keeps the cross approximation's own factors */
 } mbem_aca_batch;
 int mbem_aca_compress(const mbem_pair_geometry* g, const mbem_aca_batch* b, void* stream);
 /* Copies the first rank[i] rows of each block's U^T and V^T from the batch
@@ -779,9 +784,9 @@ int mbem_aca_compress(const mbem_pair_geometry* g, const mbem_aca_batch* b, void
 int mbem_aca_compact(int64_t n_blocks, const int32_t* nr, const int32_t* nc, const int32_t* rank,
                      const int64_t* u_src, const int64_t* v_src, const float* U_src, const float* V_src,
                      const int64_t* u_dst, const int64_t* v_dst, float* U_dst, float* V_dst, void* stream);
-/* Dense blocks (flatview.py:41-118 dense_leaves): block i as a (3 nr, pad4(3 nc))
- * row-major FP32 matrix at D + d_off[i]; col_ptr (n_blocks + 1) is the prefix
- * sum of nc (one thread per block column). */
+/* Dense blocks (flatview.py:41-118 dense_leaves): block i transposed, D^T as
+ * 3 nc rows of pad4(3 nr) FP32 (padding zero), at D + d_off[i]; col_ptr
+ * (n_blocks + 1) is the prefix sum of nc (one thread per block column). */
 int mbem_pair_dense_blocks(const mbem_pair_geometry* g, int64_t n_blocks, const int32_t* r0, const int32_t* nr,
                            const int32_t* c0, const int32_t* nc, const int64_t* d_off, const int64_t* col_ptr,
                            float* D, void* stream);
@@ -791,7 +796,12 @@ int mbem_pair_dense_blocks(const mbem_pair_geometry* g, int64_t n_blocks, const 
  * rows are a union of); strip s owns rows [strip_r0, strip_r0 + strip_nr)
  * (elements) and applies the blocks strip_items[strip_ptr[s] ..
  * strip_ptr[s+1]) in that order (id < n_lr: low rank; else n_lr + dense id),
- * so every output row has one writer and a fixed summation order. */
+ * so every output row has one writer and a fixed summation order. The
+ * product streams each strip's blocks as units of MBEM_COMPRESSED_UNIT
+ * factor rows: unit u = rows [unit_k0[u], unit_k0[u] + 32) of block
+ * unit_item[u] (the transposed factor U^T, or D^T of a dense block), listed
+ * per strip in item order at unit_ptr[s] .. unit_ptr[s+1]. */
+#define MBEM_COMPRESSED_UNIT 32
 typedef struct {
     int64_t n_field, n_src;       /* elements */
     const int64_t* field_order;   /* device: tree position -> field element */
@@ -822,6 +832,9 @@ typedef struct {
     const int32_t* strip_items;
     int max_strip;                /* largest strip_nr */
     int max_lr_nc;                /* largest lr_nc */
+    const int64_t* unit_ptr;      /* (n_strips + 1) */
+    const int32_t* unit_item;
+    const int32_t* unit_k0;
 } mbem_compressed_view;
 size_t mbem_compressed_matvec_workspace_size(const mbem_compressed_view* v);
 /* y (3 n_field, original element order) = A x (3 n_src); FP32 factors and

@@ -105,7 +105,7 @@ class AcaBatch(Structure):
                 ("max_pivots", c_void_p), ("u_off", c_void_p), ("v_off", c_void_p), ("U", c_void_p),
                 ("V", c_void_p), ("rank", c_void_p), ("status", c_void_p), ("err", c_void_p), ("tol", c_double),
                 ("seed", ctypes.c_uint64), ("first_index", c_int64), ("max_nr", c_int), ("max_nc", c_int),
-                ("max_pivots_all", c_int)]
+                ("max_pivots_all", c_int), ("recompress_max", c_int)]
 
 
 class CompressedView(Structure):
@@ -116,7 +116,10 @@ class CompressedView(Structure):
                 ("d_r0", c_void_p), ("d_nr", c_void_p), ("d_c0", c_void_p), ("d_nc", c_void_p),
                 ("d_off", c_void_p), ("D", c_void_p), ("n_strips", c_int64), ("strip_r0", c_void_p),
                 ("strip_nr", c_void_p), ("strip_ptr", c_void_p), ("strip_items", c_void_p), ("max_strip", c_int),
-                ("max_lr_nc", c_int)]
+                ("max_lr_nc", c_int), ("unit_ptr", c_void_p), ("unit_item", c_void_p), ("unit_k0", c_void_p)]
+
+
+COMPRESSED_UNIT = 32
 
 
 ACA_LOWRANK, ACA_CAPPED, ACA_FAILED, ACA_RETRIED = 0, 1, 2, 4

@@ -54,6 +54,7 @@ constexpr double ACA_RETRY_FACTOR = 10.0; // ACA_RETRY_TOL_FACTOR
 constexpr double ACA_PINV_RCOND = 1e-6;   // FP32 entries (see the header comment)
 constexpr int CM_THREADS = 256;
 constexpr int CM_WARPS = CM_THREADS / 32;
+constexpr int CM_UNIT = 32;               // factor rows a work unit of the strip product (MBEM_COMPRESSED_UNIT)
 
 __host__ __device__ __forceinline__ int pad4(int n) { return (n + 3) & ~3; }
 inline size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -307,6 +308,172 @@ __device__ __forceinline__ void block_argmax(float& v, int& i, float* rv, int* r
     for (int k = 1; k < ACA_WARPS; k++) am_merge(v, i, rv[k], ri[k]);
 }
 
+// ---------------------------------------------------------------------------
+// recompression of the cross approximation (aca.py:422-428 recompress):
+// the SVD of U V^T truncated at the tail rule of aca.py:431-438 _svd_keep,
+// by one-sided Jacobi on the factor rows in place (each factor is stored
+// transposed, so a column of U or V is a contiguous row here)
+// ---------------------------------------------------------------------------
+// Pairs this close to orthogonal are left alone (1e-3 was measured to keep
+// more blocks exact: the truncation then misjudges the tail); the certificate
+// checks the truncated factors either way.
+constexpr float OSJ_ORTH = 1e-5f;
+constexpr int OSJ_SWEEPS = 24;
+
+// Rows p and q of round `step` of the circle-method tournament on n (even)
+// players: every pair meets once in n - 1 rounds, pairs of a round are disjoint.
+__device__ __forceinline__ void osj_pair(int i, int step, int n, int& p, int& q) {
+    const int m = n - 1;
+    if (i == 0) {
+        p = step % m;
+        q = m;
+    } else {
+        p = (step + i) % m;
+        q = (step - i + m) % m;
+    }
+}
+
+// Sweeps of one-sided Jacobi on the K rows of A (length la, stride lda) until
+// every pair is orthogonal to OSJ_ORTH; each rotation is applied to the rows
+// of B too (length lb, stride ldb), so the product A^T B is unchanged. One
+// warp a pair; dot products and rotations in FP32 (the FP64 pipe of this
+// part is 1/64 of the FP32 one, and FP32 resolves the orthogonality test).
+__device__ int osj_sweeps(float* A, int lda, int la, float* B, int ldb, int lb, int K, int* flag) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = K + (K & 1);
+    int sweep = 0;
+    for (; sweep < OSJ_SWEEPS; sweep++) {
+        if (threadIdx.x == 0) *flag = 0;
+        __syncthreads();
+        for (int step = 0; step < n - 1; step++) {
+            for (int i = warp; i < n / 2; i += ACA_WARPS) {
+                int p, q;
+                osj_pair(i, step, n, p, q);
+                if (p >= K || q >= K) continue;
+                float* ap = A + (int64_t)p * lda;
+                float* aq = A + (int64_t)q * lda;
+                float spp = 0.0f, sqq = 0.0f, spq = 0.0f;
+#pragma unroll 4
+                for (int c = lane; c < la; c += 32) {
+                    const float x = ap[c], y = aq[c];
+                    spp += x * x;
+                    sqq += y * y;
+                    spq += x * y;
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    spp += __shfl_xor_sync(0xffffffffu, spp, o);
+                    sqq += __shfl_xor_sync(0xffffffffu, sqq, o);
+                    spq += __shfl_xor_sync(0xffffffffu, spq, o);
+                }
+                if (!(fabsf(spq) > OSJ_ORTH * (sqrtf(spp) * sqrtf(sqq)))) continue;
+                const float ze = (sqq - spp) / (2.0f * spq);
+                const float t = copysignf(1.0f, ze) / (fabsf(ze) + sqrtf(1.0f + ze * ze));
+                const float cd = rsqrtf(1.0f + t * t);
+                const float c = cd, sn = cd * t;
+#pragma unroll 4
+                for (int e = lane; e < la; e += 32) {
+                    const float x = ap[e], y = aq[e];
+                    ap[e] = c * x - sn * y;
+                    aq[e] = sn * x + c * y;
+                }
+                float* bp = B + (int64_t)p * ldb;
+                float* bq = B + (int64_t)q * ldb;
+#pragma unroll 4
+                for (int e = lane; e < lb; e += 32) {
+                    const float x = bp[e], y = bq[e];
+                    bp[e] = c * x - sn * y;
+                    bq[e] = sn * x + c * y;
+                }
+                if (lane == 0) *flag = 1;
+            }
+            __syncthreads();
+        }
+        if (*flag == 0) break;
+        __syncthreads();
+    }
+    __syncthreads();
+    return sweep + 1;
+}
+
+// squared norm of row k of A over la entries (one warp), in FP64
+__device__ __forceinline__ double row_norm2(const float* A, int lda, int la, int k) {
+    const int lane = threadIdx.x & 31;
+    float s = 0.0f;
+    for (int c = lane; c < la; c += 32) {
+        const float x = A[(int64_t)k * lda + c];
+        s += x * x;
+    }
+    double d = s;
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    return d;
+}
+
+// U V^T (U^T: K rows of la at ldu; V^T: K rows of lb at ldv) replaced by its
+// SVD truncated to the smallest k with ||s[k:]|| <= tol s[0] (at least 1):
+// one-sided Jacobi on V's columns (rotations carried to U), V's columns
+// normalised with their norms moved to U, one-sided Jacobi on U's columns
+// (carried to V); then U's column norms are the singular values, and the kept
+// rows are compacted in place. sig: 3K words of shared memory (values,
+// ranks, sorted values).
+// Returns k.
+__device__ int recompress(float* U, int ldu, int la, float* V, int ldv, int lb, int K, double tol, float* sig,
+                          int* rk, int* flag, int* sweeps) {
+    const int warp = threadIdx.x >> 5;
+    const int s1 = osj_sweeps(V, ldv, lb, U, ldu, la, K, flag);
+    for (int k = warp; k < K; k += ACA_WARPS) {
+        const double nv = sqrt(row_norm2(V, ldv, lb, k));
+        const float su = (float)nv, sv = nv > 0.0 ? (float)(1.0 / nv) : 0.0f;
+        const int lane = threadIdx.x & 31;
+        for (int e = lane; e < la; e += 32) U[(int64_t)k * ldu + e] *= su;
+        for (int e = lane; e < lb; e += 32) V[(int64_t)k * ldv + e] *= sv;
+    }
+    __syncthreads();
+    const int s2 = osj_sweeps(U, ldu, la, V, ldv, lb, K, flag);
+    *sweeps = min(s1, 255) | (min(s2, 255) << 8);
+    for (int k = warp; k < K; k += ACA_WARPS) {
+        const double d = sqrt(row_norm2(U, ldu, la, k));
+        if ((threadIdx.x & 31) == 0) sig[k] = (float)d;
+    }
+    __syncthreads();
+    // rank of each singular value (descending, ties by index)
+    for (int j = threadIdx.x; j < K; j += blockDim.x) {
+        int r = 0;
+        const float sj = sig[j];
+        for (int i = 0; i < K; i++) r += (sig[i] > sj || (sig[i] == sj && i < j)) ? 1 : 0;
+        rk[j] = r;
+    }
+    __syncthreads();
+    float* srt = sig + 2 * K;     // the values in descending order
+    for (int j = threadIdx.x; j < K; j += blockDim.x) srt[rk[j]] = sig[j];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double s0 = srt[0];
+        double dropped = 0.0;
+        int keep = K;
+        for (int r = K - 1; r >= 1; r--) {
+            const double sr = srt[r];
+            if (dropped + sr * sr > tol * tol * s0 * s0) break;
+            dropped += sr * sr;
+            keep = r;
+        }
+        *flag = keep;
+    }
+    __syncthreads();
+    const int keep = *flag;
+    // stable in-place compaction of the kept rows (a row only moves down)
+    int dst = 0;
+    for (int j = 0; j < K; j++) {
+        if (rk[j] >= keep) continue;
+        if (dst != j) {
+            for (int e = threadIdx.x; e < ldu; e += blockDim.x) U[(int64_t)dst * ldu + e] = U[(int64_t)j * ldu + e];
+            for (int e = threadIdx.x; e < ldv; e += blockDim.x) V[(int64_t)dst * ldv + e] = V[(int64_t)j * ldv + e];
+        }
+        dst++;
+        __syncthreads();
+    }
+    return keep;
+}
+
 struct AcaArgs {
     const int32_t* r0;
     const int32_t* nr;
@@ -326,6 +493,7 @@ struct AcaArgs {
     int ldr;    // shared row-buffer stride, pad4(3 max_nc)
     int kcap;   // 3 x the largest rank cap
     int max_nr;
+    int recompress_max;   // recompress factors of at most this many columns (0: never)
 };
 
 inline size_t aca_smem_bytes(int max_nr, int max_nc, int max_pivots) {
@@ -334,7 +502,7 @@ inline size_t aca_smem_bytes(int max_nr, int max_nc, int max_pivots) {
 }
 
 template <bool TK>
-__global__ void __launch_bounds__(ACA_THREADS) aca_kernel(AcaArgs a, Geo g, QuadRules Q) {
+__global__ void __launch_bounds__(ACA_THREADS, 2) aca_kernel(AcaArgs a, Geo g, QuadRules Q) {
     extern __shared__ __align__(16) float sm[];
     __shared__ double red_d[ACA_WARPS];
     __shared__ float red_f[ACA_WARPS];
@@ -385,7 +553,7 @@ __global__ void __launch_bounds__(ACA_THREADS) aca_kernel(AcaArgs a, Geo g, Quad
     }
     const double snorm2 = block_sum(part, red_d);
 
-    int status = MBEM_ACA_FAILED, rank_out = 0;
+    int status = MBEM_ACA_FAILED, rank_out = 0, sweeps = 0;
     float err_out = 0.0f;
     bool retried = false;
     double tol = a.tol;
@@ -515,8 +683,12 @@ __global__ void __launch_bounds__(ACA_THREADS) aca_kernel(AcaArgs a, Geo g, Quad
             status = MBEM_ACA_CAPPED;
             break;
         }
+        if (K >= 2 && K <= a.recompress_max) {
+            __syncthreads();
+            K = recompress(U, ldu, 3 * nr, V, ldv, 3 * nc, K, 0.5 * tol, R, (int*)(R + K), &rp, &sweeps);
+        }
         // certificate: 3 exact element rows and 3 exact element columns
-        double dr = 0.0, er = 0.0, dc = 0.0, ec = 0.0;
+        float dr = 0.0f, er = 0.0f, dc = 0.0f, ec = 0.0f;   // per thread (FP32); summed in FP64 below
         for (int q = 0; q < nc_r; q++) {
             const int i = lines[2 * ACA_SAMPLE + q];
             __syncthreads();
@@ -543,9 +715,9 @@ __global__ void __launch_bounds__(ACA_THREADS) aca_kernel(AcaArgs a, Geo g, Quad
                 for (int aa = 0; aa < 3; aa++)
 #pragma unroll
                     for (int bb = 0; bb < 3; bb++) {
-                        const double df = (double)ap[aa][bb] - (double)e[aa][bb];
+                        const float df = ap[aa][bb] - e[aa][bb];
                         dr += df * df;
-                        er += (double)e[aa][bb] * e[aa][bb];
+                        er += e[aa][bb] * e[aa][bb];
                     }
             }
         }
@@ -575,17 +747,15 @@ __global__ void __launch_bounds__(ACA_THREADS) aca_kernel(AcaArgs a, Geo g, Quad
                 for (int aa = 0; aa < 3; aa++)
 #pragma unroll
                     for (int bb = 0; bb < 3; bb++) {
-                        const double df = (double)ap[aa][bb] - (double)e[aa][bb];
+                        const float df = ap[aa][bb] - e[aa][bb];
                         dc += df * df;
-                        ec += (double)e[aa][bb] * e[aa][bb];
+                        ec += e[aa][bb] * e[aa][bb];
                     }
             }
         }
-        dr = block_sum(dr, red_d);
-        er = block_sum(er, red_d);
-        dc = block_sum(dc, red_d);
-        ec = block_sum(ec, red_d);
-        const double err = fmax(er > 0.0 ? sqrt(dr / er) : 0.0, ec > 0.0 ? sqrt(dc / ec) : 0.0);
+        const double sdr = block_sum(dr, red_d), ser = block_sum(er, red_d);
+        const double sdc = block_sum(dc, red_d), sec = block_sum(ec, red_d);
+        const double err = fmax(ser > 0.0 ? sqrt(sdr / ser) : 0.0, sec > 0.0 ? sqrt(sdc / sec) : 0.0);
         if (err <= ACA_CERT_FACTOR * a.tol) {
             status = MBEM_ACA_LOWRANK;
             rank_out = K;
@@ -602,7 +772,7 @@ __global__ void __launch_bounds__(ACA_THREADS) aca_kernel(AcaArgs a, Geo g, Quad
     }
     if (t == 0) {
         a.rank[blk] = status == MBEM_ACA_LOWRANK ? rank_out : 0;
-        a.status[blk] = status | (retried ? MBEM_ACA_RETRIED : 0);
+        a.status[blk] = status | (retried ? MBEM_ACA_RETRIED : 0) | (sweeps << 8);
         a.err[blk] = err_out;
     }
 }
@@ -635,7 +805,9 @@ struct DenseArgs {
     float* D;
 };
 
-// one thread per (block, source column): the source's constants once, every row of the block
+// one thread per (block, source column): the source's constants once, every
+// row of the block. Blocks are stored transposed: D^T (3 nc rows of
+// pad4(3 nr) floats), so that the product streams them like the U^T factors.
 template <bool TK>
 __global__ void __launch_bounds__(128) pair_dense_kernel(DenseArgs a, Geo g, QuadRules Q) {
     const int64_t it = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -649,9 +821,9 @@ __global__ void __launch_bounds__(128) pair_dense_kernel(DenseArgs a, Geo g, Qua
     const int64_t j = it - a.col_ptr[lo];
     const int64_t s = a.c0[lo] + j;
     const int nr = a.nr[lo];
-    const int64_t ld = pad4(3 * a.nc[lo]);
+    const int64_t ld = pad4(3 * nr);
     const int64_t f0 = a.r0[lo];
-    float* out = a.D + a.d_off[lo] + 3 * j;
+    float* out = a.D + a.d_off[lo] + 3 * j * ld;    // rows 3j .. 3j+2 of D^T
     const SrcFar sr = g.src[s];
     for (int i = 0; i < nr; i++) {
         float e[3][3];
@@ -659,15 +831,11 @@ __global__ void __launch_bounds__(128) pair_dense_kernel(DenseArgs a, Geo g, Qua
 #pragma unroll
         for (int aa = 0; aa < 3; aa++)
 #pragma unroll
-            for (int bb = 0; bb < 3; bb++) out[(3 * i + aa) * ld + bb] = e[aa][bb];
+            for (int bb = 0; bb < 3; bb++) out[bb * ld + 3 * i + aa] = e[aa][bb];
     }
-    if (j == 0) {
-        // the padding columns of every row stay finite
-        const int pad = (int)ld - 3 * a.nc[lo];
-        float* base = a.D + a.d_off[lo];
-        for (int r = 0; r < 3 * nr; r++)
-            for (int c = 0; c < pad; c++) base[(int64_t)r * ld + 3 * a.nc[lo] + c] = 0.0f;
-    }
+    // the padding of this column's three rows stays finite (the product reads it)
+    for (int bb = 0; bb < 3; bb++)
+        for (int c = 3 * nr; c < ld; c++) out[bb * ld + c] = 0.0f;
 }
 
 // ---------------------------------------------------------------------------
@@ -676,13 +844,15 @@ __global__ void __launch_bounds__(128) pair_dense_kernel(DenseArgs a, Geo g, Qua
 __global__ void cm_gather_kernel(const double* __restrict__ x, const int64_t* __restrict__ order, int64_t n,
                                  float* __restrict__ xs) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    if (blockIdx.x == 0 && threadIdx.x < 4) xs[3 * n + threadIdx.x] = 0.0f;   // read by the last padded block
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * n; q += stride) {
         const int64_t p = q / 3;
         xs[q] = (float)x[3 * order[p] + (q - 3 * p)];
     }
 }
 
-// w_i = V_i^T x[cols_i] for every low-rank block: one CTA a block, one warp a factor row
+// w_i = V_i^T x[cols_i] for every low-rank block: one CTA a block, each warp
+// four factor rows at a time (four 16-byte loads in flight a lane)
 __global__ void __launch_bounds__(CM_THREADS) cm_project_kernel(mbem_compressed_view v, const float* __restrict__ xs,
                                                                 float* __restrict__ w) {
     extern __shared__ __align__(16) float xseg[];
@@ -693,75 +863,111 @@ __global__ void __launch_bounds__(CM_THREADS) cm_project_kernel(mbem_compressed_
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float4* x4 = (const float4*)xseg;
-    for (int k = warp; k < K; k += CM_WARPS) {
-        const float4* row = (const float4*)(v.V + v.lr_v[i] + (int64_t)k * ldv);
-        float acc = 0.0f;
-        for (int q = lane; q < ldv / 4; q += 32) {
-            const float4 a = __ldg(row + q), b = x4[q];
-            acc += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+    const float* V = v.V + v.lr_v[i];
+    const int n4 = ldv / 4;
+    for (int k0 = 4 * warp; k0 < K; k0 += 4 * CM_WARPS) {
+        const int nk = min(4, K - k0);
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int q = lane; q < n4; q += 32) {
+            const float4 b = x4[q];
+#pragma unroll
+            for (int m = 0; m < 4; m++) {
+                if (m < nk) {
+                    const float4 a = __ldg((const float4*)(V + (int64_t)(k0 + m) * ldv) + q);
+                    acc[m] += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+                }
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) w[v.lr_w[i] + k] = acc;
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            float t = acc[m];
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0 && m < nk) w[v.lr_w[i] + k0 + m] = t;
+        }
     }
 }
 
-// y rows of one strip: its low-rank blocks (one thread a row), then its dense
-// blocks (one warp a row), each block summed in FP32 and added in FP64. The
-// block has at least one thread per strip row (blockDim = 3 max_strip rounded
-// up to a warp, at most 1024).
-__global__ void __launch_bounds__(1024) cm_strip_kernel(mbem_compressed_view v, const float* __restrict__ xs,
-                                                        const float* __restrict__ w, double* __restrict__ y) {
-    extern __shared__ double acc[];
+// y rows of one strip. Every block of the strip is the same kind of item: K
+// rows of a transposed factor (U^T of a low-rank block with its projection w,
+// or D^T of a dense block with the gathered x) times K coefficients. Items are
+// cut into units of at most CM_UNIT rows (the strip's unit list, in item
+// order), and warps take the units round robin, so that the warps of a strip
+// finish together. A lane owns rows lane + 32 m (m < CM_RPL) of the strip,
+// sums a unit in FP32 (four factor rows of loads in flight) and adds it to FP64
+// accumulators; the warps' sums are added in warp order, so every row has one
+// writer and a fixed summation order. Strips of more than 32 CM_RPL rows are
+// done in chunks of that many rows.
+constexpr int CM_RPL = 9;                // rows a lane: 288 rows = a strip of 96 elements
+constexpr int CM_STRIP_WARPS = 8;
+__global__ void __launch_bounds__(CM_STRIP_WARPS * 32) cm_strip_kernel(mbem_compressed_view v,
+                                                                       const float* __restrict__ xs,
+                                                                       const float* __restrict__ w,
+                                                                       double* __restrict__ y) {
+    __shared__ double part[CM_STRIP_WARPS][32 * CM_RPL];
     const int64_t s = blockIdx.x;
     const int sr0 = v.strip_r0[s], R = 3 * v.strip_nr[s];
-    const int nt = blockDim.x, nw = nt >> 5;
-    double* acc_lr = acc;
-    double* acc_d = acc + 3 * v.max_strip;
-    for (int r = threadIdx.x; r < R; r += nt) {
-        acc_lr[r] = 0.0;
-        acc_d[r] = 0.0;
-    }
-    __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int64_t q = v.strip_ptr[s]; q < v.strip_ptr[s + 1]; q++) {
-        const int id = v.strip_items[q];
-        if (id < v.n_lr) {
-            const int K = v.lr_rank[id];
-            const int64_t ldu = pad4(3 * v.lr_nr[id]);
-            const float* U = v.U + v.lr_u[id] + 3 * (int64_t)(sr0 - v.lr_r0[id]);
-            const float* wi = w + v.lr_w[id];
-            for (int r = threadIdx.x; r < R; r += nt) {
-                float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
-                const float* u = U + r;
-                int k = 0;
-                for (; k + 4 <= K; k += 4) {
-                    a0 += __ldg(u + k * ldu) * wi[k];
-                    a1 += __ldg(u + (k + 1) * ldu) * wi[k + 1];
-                    a2 += __ldg(u + (k + 2) * ldu) * wi[k + 2];
-                    a3 += __ldg(u + (k + 3) * ldu) * wi[k + 3];
-                }
-                for (; k < K; k++) a0 += __ldg(u + k * ldu) * wi[k];
-                acc_lr[r] += (double)((a0 + a1) + (a2 + a3));
+    const int64_t u0 = v.unit_ptr[s], u1 = v.unit_ptr[s + 1];
+    for (int rc = 0; rc < R; rc += 32 * CM_RPL) {
+        const int Rc = min(32 * CM_RPL, R - rc);
+        double acc[CM_RPL];
+#pragma unroll
+        for (int m = 0; m < CM_RPL; m++) acc[m] = 0.0;
+        for (int64_t u = u0 + warp; u < u1; u += CM_STRIP_WARPS) {
+            const int id = v.unit_item[u];
+            const int k0 = v.unit_k0[u];
+            const float* base;
+            const float* cf;
+            int K;
+            int64_t ld;
+            if (id < v.n_lr) {
+                K = v.lr_rank[id];
+                ld = pad4(3 * v.lr_nr[id]);
+                base = v.U + v.lr_u[id] + 3 * (int64_t)(sr0 - v.lr_r0[id]) + rc;
+                cf = w + v.lr_w[id];
+            } else {
+                const int d = id - (int)v.n_lr;
+                K = 3 * v.d_nc[d];
+                ld = pad4(3 * v.d_nr[d]);
+                base = v.D + v.d_off[d] + 3 * (int64_t)(sr0 - v.d_r0[d]) + rc;
+                cf = xs + 3 * (int64_t)v.d_c0[d];
             }
-        } else {
-            const int d = id - (int)v.n_lr;
-            const int nc3 = 3 * v.d_nc[d];
-            const int64_t ld = pad4(nc3);
-            const float* D = v.D + v.d_off[d] + 3 * (int64_t)(sr0 - v.d_r0[d]) * ld;
-            const float* xd = xs + 3 * (int64_t)v.d_c0[d];
-            for (int r = warp; r < R; r += nw) {
-                const float* row = D + r * ld;
-                float a = 0.0f;
-                for (int c = lane; c < nc3; c += 32) a += __ldg(row + c) * xd[c];
-                for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-                if (lane == 0) acc_d[r] += (double)a;
+            const int k1 = min(K, k0 + CM_UNIT);
+            float p[CM_RPL];
+#pragma unroll
+            for (int m = 0; m < CM_RPL; m++) p[m] = 0.0f;
+            const float* row = base + lane;
+            int k = k0;
+            for (; k + 4 <= k1; k += 4) {
+                float vv[4][CM_RPL];
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+#pragma unroll
+                    for (int m = 0; m < CM_RPL; m++)
+                        vv[j][m] = (lane + 32 * m < Rc) ? __ldg(row + (int64_t)(k + j) * ld + 32 * m) : 0.0f;
+                const float c0 = cf[k], c1 = cf[k + 1], c2 = cf[k + 2], c3 = cf[k + 3];
+#pragma unroll
+                for (int m = 0; m < CM_RPL; m++) p[m] += ((vv[0][m] * c0 + vv[1][m] * c1) + (vv[2][m] * c2 + vv[3][m] * c3));
             }
+            for (; k < k1; k++) {
+                const float c = cf[k];
+#pragma unroll
+                for (int m = 0; m < CM_RPL; m++)
+                    if (lane + 32 * m < Rc) p[m] += __ldg(row + (int64_t)k * ld + 32 * m) * c;
+            }
+#pragma unroll
+            for (int m = 0; m < CM_RPL; m++) acc[m] += (double)p[m];
         }
-    }
-    __syncthreads();
-    for (int r = threadIdx.x; r < R; r += nt) {
-        const int64_t p = sr0 + r / 3;
-        y[3 * v.field_order[p] + r % 3] = acc_lr[r] + acc_d[r];
+#pragma unroll
+        for (int m = 0; m < CM_RPL; m++) part[warp][lane + 32 * m] = acc[m];
+        __syncthreads();
+        for (int r = threadIdx.x; r < Rc; r += blockDim.x) {
+            double t = 0.0;
+            for (int ww = 0; ww < CM_STRIP_WARPS; ww++) t += part[ww][r];
+            const int64_t p = sr0 + (rc + r) / 3;
+            y[3 * v.field_order[p] + (rc + r) % 3] = t;
+        }
+        __syncthreads();
     }
 }
 
@@ -781,7 +987,7 @@ __global__ void cm_dense_kernel(mbem_compressed_view v, double* __restrict__ out
             const float* V = v.V + v.lr_v[b];
             for (int k = 0; k < v.lr_rank[b]; k++) val += (double)U[(int64_t)k * ldu + r] * (double)V[(int64_t)k * ldc + c];
         } else {
-            val = v.D[v.d_off[d] + (int64_t)r * ldc + c];
+            val = v.D[v.d_off[d] + (int64_t)c * ldu + r];     // D^T
         }
         const int64_t row = 3 * v.field_order[r0 + r / 3] + r % 3;
         const int64_t col = 3 * v.src_order[c0 + c / 3] + c % 3;
@@ -869,6 +1075,7 @@ int mbem_aca_compress(const mbem_pair_geometry* g, const mbem_aca_batch* b, void
     a.ldr = pad4(3 * b->max_nc);
     a.kcap = 3 * b->max_pivots_all;
     a.max_nr = b->max_nr;
+    a.recompress_max = b->recompress_max;
     const Geo G = make_geo(g);
     cudaStream_t st = (cudaStream_t)stream;
     if (g->kernel == 0) {
@@ -930,7 +1137,7 @@ int mbem_pair_dense_blocks(const mbem_pair_geometry* g, int64_t n_blocks, const 
 
 size_t mbem_compressed_matvec_workspace_size(const mbem_compressed_view* v) {
     if (!v) return 0;
-    return round256((size_t)3 * v->n_src * sizeof(float)) + round256((size_t)v->n_w * sizeof(float));
+    return round256((size_t)(3 * v->n_src + 4) * sizeof(float)) + round256((size_t)v->n_w * sizeof(float));
 }
 
 int mbem_compressed_matvec(const mbem_compressed_view* v, const double* x, double* y, void* work,
@@ -938,15 +1145,13 @@ int mbem_compressed_matvec(const mbem_compressed_view* v, const double* x, doubl
     MBEM_REQUIRE(v && x && y && work, MBEM_ERR_ARG, "compressed matvec: null pointer");
     MBEM_REQUIRE(work_bytes >= mbem_compressed_matvec_workspace_size(v), MBEM_ERR_SIZE,
                  "compressed matvec: workspace too small");
-    MBEM_REQUIRE(v->max_strip >= 0 && (size_t)v->max_strip * 6 * sizeof(double) <= 200 * 1024, MBEM_ERR_SIZE,
-                 "compressed matvec: strip of %d elements too large", v->max_strip);
     MBEM_REQUIRE((size_t)pad4(3 * v->max_lr_nc) * sizeof(float) <= 200 * 1024, MBEM_ERR_SIZE,
                  "compressed matvec: block of %d source elements too large", v->max_lr_nc);
     MBEM_REQUIRE(((uintptr_t)v->V % 16) == 0 || v->n_lr == 0, MBEM_ERR_ARG,
                  "compressed matvec: V must be 16-byte aligned");
     cudaStream_t st = (cudaStream_t)stream;
     float* xs = (float*)work;
-    float* w = (float*)((char*)work + round256((size_t)3 * v->n_src * sizeof(float)));
+    float* w = (float*)((char*)work + round256((size_t)(3 * v->n_src + 4) * sizeof(float)));
     int n = 0;
     if (v->n_src > 0) {
         cm_gather_kernel<<<(unsigned)lmin(ceil_div(3 * v->n_src, 256), 8192), 256, 0, st>>>(x, v->src_order,
@@ -961,11 +1166,7 @@ int mbem_compressed_matvec(const mbem_compressed_view* v, const double* x, doubl
         n++;
     }
     if (v->n_strips > 0) {
-        const size_t sm = (size_t)v->max_strip * 6 * sizeof(double);
-        int rc = set_smem((const void*)cm_strip_kernel, sm);
-        if (rc) return rc;
-        const int nt = (int)lmin(1024, lmax(128, ceil_div(3 * (int64_t)v->max_strip, 32) * 32));
-        cm_strip_kernel<<<(unsigned)v->n_strips, nt, sm, st>>>(*v, xs, w, y);
+        cm_strip_kernel<<<(unsigned)v->n_strips, CM_STRIP_WARPS * 32, 0, st>>>(*v, xs, w, y);
         n++;
     }
     return n ? launch_status("compressed_matvec", n) : MBEM_OK;

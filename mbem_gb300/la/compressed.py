@@ -20,12 +20,13 @@ approximation with 3 x 3 element pivots (``mbem_aca_compress``: one CTA a
 block; stopped on the true residual of a 10 x 10 element sample; certified on
 3 exact element rows and 3 exact element columns; a failed certificate reruns
 the block at tol / 10; a second failure, or the rank cap, leaves the block
-exact). Dense blocks are evaluated into one flat FP32 buffer
+exact). Dense blocks are evaluated into one flat FP32 buffer, each transposed
 (``mbem_pair_dense_blocks``). The product (``mbem_compressed_matvec``) runs
 three kernels: the gather of x into tree order, the projections
 ``w_i = V_i^T x`` of every low-rank block, and one CTA per field-row strip
-that adds its low-rank and dense blocks in a fixed order and writes its rows
-of y, so no row has two writers.
+whose warps stream the strip's blocks (rows of U^T times w, rows of D^T
+times x) and add their sums in warp order, so no row has two writers and the
+result is bitwise repeatable.
 
 What differs from the reference. A view is compressed per material directly
 (the material's coefficients enter the pair kernel), where the reference
@@ -265,6 +266,21 @@ def row_strips(n_rows: int, r0: np.ndarray, nr: np.ndarray):
             item[o].astype(np.int32))
 
 
+def strip_units(sptr: np.ndarray, items: np.ndarray, rows_of_item: np.ndarray, unit: int = nat.COMPRESSED_UNIT):
+    """Each strip's blocks cut into work units of at most ``unit`` factor
+    rows, in item order: (unit_ptr, unit_item, unit_k0). ``rows_of_item``:
+    the factor rows of every block id (rank, or 3 nc for a dense block)."""
+    k = np.asarray(rows_of_item, np.int64)[items]
+    nu = np.maximum(1, (k + unit - 1) // unit)
+    tot = int(nu.sum())
+    item = np.repeat(items, nu).astype(np.int32)
+    first = np.repeat(np.cumsum(nu) - nu, nu)
+    k0 = ((np.arange(tot) - first) * unit).astype(np.int32)
+    cs = np.concatenate([[0], np.cumsum(nu)])
+    uptr = cs[np.asarray(sptr, np.int64)].astype(np.int64)
+    return uptr, item, k0
+
+
 def _pad4(n):
     return (np.asarray(n, np.int64) + 3) // 4 * 4
 
@@ -343,7 +359,8 @@ class PairCompressed:
                  partition=None,
                  seed: int = defaults.ACA_SEED,
                  near_factor: float = defaults.COMPRESSED_NEAR_RADIUS_FACTOR,
-                 scratch_bytes: int = defaults.COMPRESSED_SCRATCH_BYTES):
+                 scratch_bytes: int = defaults.COMPRESSED_SCRATCH_BYTES,
+                 recompress_max: int = defaults.ACA_RECOMPRESS_MAX):
         self.n_basis = kernel_n_basis(kernel)          # raises on a traction kernel
         if kernel not in (KERNEL_T, KERNEL_U):
             raise ValueError(f"unknown kernel {kernel!r}")
@@ -354,6 +371,7 @@ class PairCompressed:
         self.seed = int(seed)
         self.near_factor = float(near_factor)
         self.scratch_bytes = int(scratch_bytes)
+        self.recompress_max = int(recompress_max)
         arrays = arrays if arrays is not None else kb.MeshArrays()
         x_field = arrays.field_points(field_mesh)
         tri_verts, normals = arrays.source_arrays(source_mesh)
@@ -488,6 +506,7 @@ class PairCompressed:
             b.first_index = lo
             b.max_nr, b.max_nc = int(nr[sl].max()), int(nc[sl].max())
             b.max_pivots_all = int(cap[sl].max())
+            b.recompress_max = self.recompress_max
             nat.call("mbem_aca_compress", ctypes.byref(g), ctypes.byref(b), st)
             rank[sl], status[sl], err[sl] = rk.cpu().numpy(), stt.cpu().numpy(), er.cpu().numpy()
             usz = rank[sl].astype(np.int64) * ldu[sl]
@@ -528,7 +547,7 @@ class PairCompressed:
         d_nr = np.concatenate([nr[ex], dnr]).astype(np.int32)
         d_c0 = np.concatenate([c0[ex], dc0]).astype(np.int32)
         d_nc = np.concatenate([nc[ex], dnc]).astype(np.int32)
-        dsz = 3 * d_nr.astype(np.int64) * _pad4(3 * d_nc)
+        dsz = 3 * d_nc.astype(np.int64) * _pad4(3 * d_nr)      # D^T: 3 nc rows of pad4(3 nr)
         d_off = _exclusive(dsz)
         total = int(dsz.sum())
         free, _ = torch.cuda.mem_get_info()
@@ -569,6 +588,10 @@ class PairCompressed:
         s.strip_r0, s.strip_nr = _i32(v, sr0, "strip_r0"), _i32(v, snr, "strip_nr")
         s.strip_ptr, s.strip_items = _i64(v, sptr, "strip_ptr"), _i32(v, sitems, "strip_items")
         s.max_strip = int(snr.max()) if snr.size else 0
+        item_rows = np.concatenate([lr_rank.astype(np.int64), 3 * d_nc.astype(np.int64)])
+        uptr, uitem, uk0 = strip_units(sptr, sitems, item_rows)
+        s.unit_ptr, s.unit_item, s.unit_k0 = _i64(v, uptr, "unit_ptr"), _i32(v, uitem, "unit_item"), \
+            _i32(v, uk0, "unit_k0")
         s.max_lr_nc = int(nc[low].max()) if s.n_lr else 0
         v.work_bytes = int(nat.lib().mbem_compressed_matvec_workspace_size(ctypes.byref(s)))
         v.work = torch.empty(max(16, v.work_bytes), dtype=torch.uint8, device=self._x.device)
@@ -582,7 +605,8 @@ class PairCompressed:
             "n_fallback": int(((status & 3) == nat.ACA_FAILED).sum()),
             "max_verified_err": float(err[low].max()) if low.any() else 0.0,
             "ranks": lr_rank.copy(),
-            "status": status.copy(),
+            "status": status & 7,
+            "jacobi_sweeps": np.stack([(status >> 8) & 255, (status >> 16) & 255], axis=1),
             "err": err.copy(),
             "lowrank_bytes": lr_bytes,
             "dense_bytes": 4 * total,

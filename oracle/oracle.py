@@ -42,8 +42,8 @@ def lib():
         h.oracle_matrix.argtypes = [ctypes.c_int, P, I, P, P, P, I, P, I, I, P]
         h.oracle_contract.argtypes = [ctypes.c_int, P, I, P, P, P, I, P, P, I, I, P]
         h.oracle_dgemv.argtypes = [P, I, I, P, I, I, P]
-        h.oracle_flat_matvec.argtypes = [I, I, P, P, I, P, P, P, P, P, P, P, P, P, P, I, P, P, P, P, P, I, P, P,
-                                         P, P, P, P]
+        h.oracle_flat_matvec.argtypes = [I, I, P, P, I, P, P, P, P, P, P, P, P, P, P, I, P, P, P, P, P, P, I, P,
+                                         P, P, P, P, P]
         h.oracle_flat_matvec.restype = None
         h.oracle_set_threads.argtypes = [ctypes.c_int]
         h.oracle_set_threads.restype = ctypes.c_int
@@ -122,7 +122,8 @@ def flat_matvec(view: dict, x) -> np.ndarray:
     lib().oracle_flat_matvec(
         int(v["n_field"]), int(v["n_src"]), _p(v["field_order"]), _p(v["src_order"]), int(v["n_lr"]),
         _p(v["lr_r0"]), _p(v["lr_nr"]), _p(v["lr_c0"]), _p(v["lr_nc"]), _p(v["lr_rank"]), _p(v["lr_u"]),
-        _p(v["lr_v"]), _p(v["lr_w"]), _p(v["U"]), _p(v["V"]), int(v["n_w"]), _p(v["d_r0"]), _p(v["d_nc"]),
+        _p(v["lr_v"]), _p(v["lr_w"]), _p(v["U"]), _p(v["V"]), int(v["n_w"]), _p(v["d_r0"]), _p(v["d_nr"]),
+        _p(v["d_nc"]),
         _p(v["d_c0"]), _p(v["d_off"]), _p(v["D"]), int(v["n_strips"]), _p(v["strip_r0"]), _p(v["strip_nr"]),
         _p(v["strip_ptr"]), _p(v["strip_items"]), _p(x), _p(y))
     return y

@@ -743,7 +743,8 @@ void oracle_dgemv(const double *A, int64_t n_rows, int64_t n_cols, const double 
 /* ====================================================================== */
 /* y = A x for the flat layout of one material view: low-rank block i with
  * U^T (rank rows of pad4(3 nr) floats) at U + lr_u[i] and V^T likewise at
- * V + lr_v[i]; dense block d row-major (3 nr, pad4(3 nc)) at D + d_off[d];
+ * V + lr_v[i]; dense block d transposed, D^T (3 nc rows of pad4(3 nr)), at
+ * D + d_off[d];
  * element ranges in the tree order (field_order / src_order map positions to
  * elements). Phase 1 forms w_i = V_i^T x per block; phase 2 owns rows: strip
  * s adds the blocks strip_items[strip_ptr[s] .. strip_ptr[s+1]) in order.
@@ -755,7 +756,7 @@ void oracle_flat_matvec(int64_t n_field, int64_t n_src, const int64_t *field_ord
                         const int32_t *lr_nr, const int32_t *lr_c0, const int32_t *lr_nc,
                         const int32_t *lr_rank, const int64_t *lr_u, const int64_t *lr_v,
                         const int64_t *lr_w, const float *U, const float *V, int64_t n_w,
-                        const int32_t *d_r0, const int32_t *d_nc, const int32_t *d_c0,
+                        const int32_t *d_r0, const int32_t *d_nr, const int32_t *d_nc, const int32_t *d_c0,
                         const int64_t *d_off, const float *D, int64_t n_strips,
                         const int32_t *strip_r0, const int32_t *strip_nr, const int64_t *strip_ptr,
                         const int32_t *strip_items, const double *x, double *y) {
@@ -793,14 +794,12 @@ void oracle_flat_matvec(int64_t n_field, int64_t n_src, const int64_t *field_ord
                 }
             } else {
                 const int64_t d = id - n_lr;
-                const int64_t nc3 = 3 * (int64_t)d_nc[d], ld = pad4_64(nc3);
-                const float *Db = D + d_off[d] + 3 * (sr0 - d_r0[d]) * ld;
+                const int64_t nc3 = 3 * (int64_t)d_nc[d], ld = pad4_64(3 * (int64_t)d_nr[d]);
+                const float *Db = D + d_off[d] + 3 * (sr0 - d_r0[d]);
                 const double *xc = xs + 3 * (int64_t)d_c0[d];
-                for (int64_t r = 0; r < R; r++) {
-                    const float *row = Db + r * ld;
-                    double t = 0.0;
-                    for (int64_t c = 0; c < nc3; c++) t += (double)row[c] * xc[c];
-                    a[r] += t;
+                for (int64_t c = 0; c < nc3; c++) {
+                    const float *col = Db + c * ld;
+                    for (int64_t r = 0; r < R; r++) a[r] += (double)col[r] * xc[c];
                 }
             }
         }

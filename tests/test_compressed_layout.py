@@ -113,6 +113,20 @@ def test_row_strips_cover_each_block_row_once():
         assert np.array_equal(cover[b], want)
 
 
+def test_strip_units_cover_every_factor_row_once():
+    from mbem_gb300.la import compressed as cm
+    rng = np.random.default_rng(8)
+    sptr = np.array([0, 3, 3, 7, 8])                  # an empty strip in the middle
+    items = rng.integers(0, 6, 8).astype(np.int32)
+    rows = np.array([5, 32, 33, 64, 0, 100])          # factor rows of each block id
+    uptr, uitem, uk0 = cm.strip_units(sptr, items, rows, unit=32)
+    assert uptr[0] == 0 and uptr[-1] == uitem.size
+    for s in range(sptr.size - 1):
+        got = list(zip(uitem[uptr[s]:uptr[s + 1]], uk0[uptr[s]:uptr[s + 1]]))
+        want = [(b, k) for b in items[sptr[s]:sptr[s + 1]] for k in range(0, max(rows[b], 1), 32)]
+        assert got == want
+
+
 def test_rank_caps_follow_the_reference_rule():
     from mbem_gb300.la import compressed as cm
     nr = np.array([64, 100, 1024, 20, 5, 300])
@@ -148,13 +162,14 @@ def test_flat_product_port_on_a_handmade_view(oracle):
         A[np.ix_(rows, cols)] += blk
     D, d_off = [], []
     for r0, nr, c0, nc in dn:
-        ld = int(cm._pad4(3 * nc))
-        d = rng.normal(size=(3 * nr, ld)).astype(np.float32)
+        ld = int(cm._pad4(3 * nr))
+        d = rng.normal(size=(3 * nc, ld)).astype(np.float32)      # stored transposed
+        d[:, 3 * nr:] = 0
         d_off.append(sum(x.size for x in D))
         D.append(d.ravel())
         rows = (3 * fo[r0:r0 + nr, None] + np.arange(3)).ravel()
         cols = (3 * so[c0:c0 + nc, None] + np.arange(3)).ravel()
-        A[np.ix_(rows, cols)] += d[:, :3 * nc].astype(float)
+        A[np.ix_(rows, cols)] += d[:, :3 * nr].astype(float).T
     all_r0 = np.array([b[0] for b in lr] + [b[0] for b in dn])
     all_nr = np.array([b[1] for b in lr] + [b[1] for b in dn])
     sr0, snr, sptr, sit = cm.row_strips(nf, all_r0, all_nr)
@@ -164,7 +179,8 @@ def test_flat_product_port_on_a_handmade_view(oracle):
                 lr_c0=np.array([b[2] for b in lr], np.int32), lr_nc=np.array([b[3] for b in lr], np.int32),
                 lr_rank=ranks, lr_u=np.array(lr_u, np.int64), lr_v=np.array(lr_v, np.int64),
                 lr_w=cm._exclusive(ranks), U=np.concatenate(U), V=np.concatenate(V), n_w=int(ranks.sum()),
-                d_r0=np.array([b[0] for b in dn], np.int32), d_nc=np.array([b[3] for b in dn], np.int32),
+                d_r0=np.array([b[0] for b in dn], np.int32), d_nr=np.array([b[1] for b in dn], np.int32),
+                d_nc=np.array([b[3] for b in dn], np.int32),
                 d_c0=np.array([b[2] for b in dn], np.int32), d_off=np.array(d_off, np.int64), D=np.concatenate(D),
                 n_strips=sr0.size, strip_r0=sr0, strip_nr=snr, strip_ptr=sptr, strip_items=sit)
     x = rng.normal(size=3 * ns)
