@@ -24,6 +24,9 @@ volume    the volume sampler's geometry on cube 24 (6,912 triangles): region
 vsample   the mixed readout of the same 40^3 grid after a mixed solve of cube 24
           + fault 16: readout_far_kernel<EIG> (stress and eigenstress) and
           disp_readout_kernel, each over the cube and the fault
+compressed  the compressed pair operator of the cube 64 self pair, T kernel
+          (49,152 elements): its build (aca_kernel, pair_dense_kernel) and eight
+          products (cm_gather_kernel, cm_project_kernel, cm_strip_kernel)
 """
 
 from __future__ import annotations
@@ -143,6 +146,17 @@ def run(which: str) -> None:
                            precond="bf16_inner").assemble(generate_system(model), eps).solve()
         grid = V.make_grid(model, 4.0 / 40)
         V.sample(model, sol, eps, grid, V.classify(model, grid), precision="mixed")
+    elif which == "compressed":
+        from mbem_gb300 import mesh
+        from mbem_gb300.kernels import basis as kb
+        from mbem_gb300.la.compressed import PairCompressed
+        c = mesh.cube(64)
+        pc = PairCompressed(c, c, "H", (4.0 / 64) / 2)
+        view = pc._view(kb.t_coeffs(1.0, 1.0))
+        x = torch.randn(3 * c.n_triangles, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        for _ in range(8):
+            pc.apply_device(view, x, y)
     else:
         raise SystemExit(f"unknown case {which!r}")
     torch.cuda.synchronize()
