@@ -580,8 +580,13 @@ def fault_traction_workload(n_face=32, n_fault=24, dip=90.0):
     """The FAULT_TRACTION cube (32 x 32 per face, fault 24 x 24, uniform
     shear drop 1e-3 mu): FGMRES with block-Jacobi, with the learned coarse
     space (shipped parameters, trained on 12- and 16-per-face meshes), and
-    without a preconditioner."""
+    without a preconditioner, on the FP64 operator; then on the mixed
+    operator, the BF16 inner solve with the learned preconditioner or
+    block-Jacobi inside it."""
+    import ctypes
+
     import torch
+    from mbem_gb300 import _native as nat
     from mbem_gb300.backends.dense import DenseBackend
     from mbem_gb300.cases import fault_traction_model
     from mbem_gb300.la.learned import LearnedPreconditioner
@@ -615,8 +620,49 @@ def fault_traction_workload(n_face=32, n_fault=24, dip=90.0):
     out["none"] = {"solve_s": t_plain, "iterations": asm.report.iterations, "true_relres": asm.report.true_relres,
                    "converged": asm.report.converged}
     out["learned_vs_block_jacobi_time"] = out["block_jacobi"]["time_to_solve_s"] / out["learned"]["time_to_solve_s"]
+    x64 = asm.solve_device(precond=LearnedPreconditioner(asm, params))
     del asm
     torch.cuda.empty_cache()
+    # the same system on the mixed operator (FP32 far field + BF16 copy, FP64
+    # near blocks; the fault's traction rows assembled in FP64 and split):
+    # the BF16 inner solve with the learned two-level preconditioner or with
+    # block-Jacobi inside it, and block-Jacobi on the outer solve
+    mixed = DenseBackend(jump="calibrated", deflate=True, rtol=RTOL, restart=RESTART, maxiter=1000,
+                         precision="mixed", precond="bf16_inner")
+    for timed in (False, True):
+        amx, t_asm = _sync_time(lambda: mixed.assemble(system, eps))
+        res = {}
+        for name in ("bf16_learned", "bf16_block_jacobi", "block_jacobi"):
+            amx._bj = None
+            amx._learned = None
+
+            def setup():
+                if name == "bf16_learned":
+                    return amx.bf16_learned(params)
+                if name == "bf16_block_jacobi":
+                    inner = amx.bf16_inner()
+                    inner.set_preconditioner(amx.block_jacobi())
+                    return inner
+                return amx.block_jacobi()
+            pc, t_setup = _sync_time(setup)
+            steps, applies = ctypes.c_int64(0), ctypes.c_int64(0)
+            nat.lib().mbem_inner_bf16_stats(0, ctypes.byref(steps), ctypes.byref(applies), None)
+            x, t_solve = _sync_time(lambda: amx.solve_device(precond=pc))
+            nat.lib().mbem_inner_bf16_stats(0, ctypes.byref(steps), ctypes.byref(applies), None)
+            rep = amx.report
+            res[name] = {"setup_s": t_setup, "solve_s": t_solve, "outer_iterations": rep.iterations,
+                         "inner_steps": int(steps.value),
+                         "true_relres": rep.true_relres, "converged": rep.converged,
+                         "time_to_solve_s": t_asm + t_setup + t_solve,
+                         "max_rel_diff_vs_fp64_solution": float((x - x64).norm() / x64.norm())}
+        if timed:
+            out["mixed"] = {"assembly_s": t_asm, **res,
+                            "learned_vs_block_jacobi_time": res["bf16_block_jacobi"]["time_to_solve_s"]
+                            / res["bf16_learned"]["time_to_solve_s"],
+                            "speedup_vs_fp64_learned": out["learned"]["time_to_solve_s"]
+                            / res["bf16_learned"]["time_to_solve_s"]}
+        del amx
+        torch.cuda.empty_cache()
     return out
 
 

@@ -112,6 +112,16 @@ int mbem_traction_matrix(const double* x_field, const double* n_field, int64_t n
                          int order, int which, double alpha, double* out, int64_t ld_out,
                          void* stream);
 
+/* The same traction rows (which = "slip", an order-0 source patch) for the
+ * mixed operator: far pairs by FP32 quadrature of the point integrand (DD
+ * stress minus eigenstress), near pairs (the near list near_rowptr/near_cols
+ * of mbem_near_count/mbem_near_fill at near_factor) by the FP64 closed form;
+ * out (3 n_pts, 3 n_src) at ld_out, accumulated (out += alpha * rows). */
+int mbem_traction_matrix_mixed(const double* x_field, const double* n_field, int64_t n_pts,
+                               const double* tri_verts, const double* normals, const double* eps, int64_t n_src,
+                               double mu, double lam, double near_factor, double alpha, const int64_t* near_rowptr,
+                               const int64_t* near_cols, int64_t nnz, double* out, int64_t ld_out, void* stream);
+
 /* ---- dense-system helpers of the calibrated dense backend
  * (src/mbem/backends/dense.py:480-528). ------------------------------- */
 

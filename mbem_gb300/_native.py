@@ -254,6 +254,7 @@ _SIGNATURES = {
     "mbem_mm_solve": (c_int, [_P, _P, _P, c_double, c_int, c_int, POINTER(MmReport), _P]),
     "mbem_mm_check": (c_int, [_P]),
     "mbem_mm_solve_mixed": (c_int, [_P, _P, _P, c_double, c_double, c_int, c_int, c_int, POINTER(MmReport), _P]),
+    "mbem_traction_matrix_mixed": (c_int, [_P, _P, _I, _P, _P, _P, _I, _D, _D, _D, _D, _P, _P, _I, _P, _I, _P]),
     "mbem_pair_prep_bytes": (c_size_t, [_I, _I]),
     "mbem_pair_prepare": (c_int, [POINTER(PairGeometry), _P]),
     "mbem_aca_compress": (c_int, [POINTER(PairGeometry), POINTER(AcaBatch), _P]),

@@ -278,7 +278,16 @@ class AssembledDense:
                if self.precond in ("bf16_inner", "bf16_learned") else None)
         op = MixedOperator(A32, [], A16)
         placed = {}
-        for t in self.system.terms:
+        # FAULT_TRACTION rows are assembled in FP64 (their kernels have no FP32
+        # quadrature here), transformed like the FP64 system's, then split
+        # into FP32 / BF16 far entries and FP64 near blocks (_traction_rows)
+        trac = {self.layout.slot(f, "b").offset: (region, f) for region, f in self.system.traction_faults()}
+        for r0, (_, f) in trac.items():
+            if f.order:
+                raise NotImplementedError("mixed precision: FAULT_TRACTION rows of an order > 0 fault")
+        terms = [t for t in self.system.terms if t.row.offset not in trac]
+        trac_terms = [t for t in self.system.terms if t.row.offset in trac]
+        for t in terms:
             mat = self.materials[t.region.name]
             view = A32[t.row.offset:t.row.stop, t.col.offset:t.col.stop]
             view16 = None if A16 is None else A16[t.row.offset:t.row.stop, t.col.offset:t.col.stop]
@@ -310,7 +319,7 @@ class AssembledDense:
                 return rs if scale == 1.0 else rs * (1.0 / scale)
             self.calib = calibrated_diagonal(self.system, rowsum)
         missing = torch.zeros(1, dtype=torch.int32, device=dev)
-        for t, nl in zip(self.system.terms, op.near):
+        for t, nl in zip(terms, op.near):
             D = term_diagonal(t, self.calib)
             if D is None:
                 continue
@@ -327,8 +336,18 @@ class AssembledDense:
             raise RuntimeError("mixed precision: a collocation row has no self block in its near list")
         b = torch.zeros(n, dtype=torch.float64, device=dev)
         for rt in self.system.rhs_terms:
-            bop, _ = block(rt.field_patch, rt.source_patch, rt.kernel, rt.region)
+            if rt.kernel in (KERNEL_HT, KERNEL_GT) and not np.any(np.asarray(rt.vector, float)):
+                continue                        # a zero density adds nothing (e.g. a traction-free patch)
             dens = as_cuda(np.asarray(rt.vector, float))
+            if rt.kernel in (KERNEL_HT, KERNEL_GT):
+                tmp = torch.zeros((3 * rt.field_patch.n_dofs, 3 * rt.source_patch.n_nodes), dtype=torch.float64,
+                                  device=dev)
+                self._block_into(tmp, rt.field_patch, rt.source_patch, rt.kernel, self.materials[rt.region.name],
+                                 1.0, True)
+                b[rt.row.offset:rt.row.stop] += rt.scale * (tmp @ dens)
+                del tmp
+                continue
+            bop, _ = block(rt.field_patch, rt.source_patch, rt.kernel, rt.region)
             y = bop.matvec(dens)
             b[rt.row.offset:rt.row.stop] += rt.scale * y
         for rv in self.system.rhs_values:
@@ -342,12 +361,79 @@ class AssembledDense:
                 bview += rt.scale_half * u_c
             else:
                 bview -= torch.einsum("nij,nj->ni", self.calib[(id(rt.region), id(rt.field_patch))], u_c)
-        if self.system.traction_faults():
-            raise NotImplementedError("mixed precision: FAULT_TRACTION rows are not in the mixed operator")
+        for r0, (region, f) in trac.items():
+            self._traction_rows(op, r0, region, f, [t for t in trac_terms if t.row.offset == r0], b)
         self._arrays = None
         self.op = op
         self.A = None
         self.b = b
+
+    def _traction_rows(self, op, r0, region, f, trac_terms, b):
+        """One FAULT_TRACTION fault's rows of the mixed operator: assembled in
+        FP64 over every column, their free terms added, the fault-row
+        transformation applied (``fault_rows_one``: frame, drag, constraint
+        and locked rows, as the FP64 system gets them), then split by the
+        mixed operator's near rule per source slot: near pairs as FP64 blocks
+        in the near lists, the rest into the FP32 far field and its BF16 copy."""
+        from ..la.mixed import NearList, near_list
+        from .fault_rows import fault_rows_one
+        n = self.layout.n_unknowns
+        m = 3 * f.n_dofs
+        dev = op.A32.device
+        R = torch.zeros((m, n), dtype=torch.float64, device=dev)
+        fa = self._patch_arrays(f)
+        xf = fa["coll"]
+        near = {}       # column slot offset -> its near list (rowptr, cols)
+        for slot in self.layout.slots:
+            if slot.size == 0:
+                continue
+            if slot.patch.order:
+                raise NotImplementedError("mixed precision: FAULT_TRACTION rows over an order > 0 patch")
+            sp = self._patch_arrays(slot.patch)
+            near[slot.offset] = near_list(xf, sp["tv"], sp["eps"], self.near_factor)
+        for t in trac_terms:
+            mat = self.materials[t.region.name]
+            if t.kernel == KERNEL_HT and t.source_patch.order == 0 and t.col.offset in near:
+                # FP32 far quadrature + FP64 near pairs, straight into the FP64 rows
+                sp = self._patch_arrays(t.source_patch)
+                rowptr, cols = near[t.col.offset]
+                blk = R[:, t.col.offset:t.col.stop]
+                nat.call("mbem_traction_matrix_mixed", ptr(xf), ptr(fa["coll_n"]), xf.shape[0], ptr(sp["tv"]),
+                         ptr(sp["normals"]), ptr(sp["eps"]), t.source_patch.n_triangles, float(mat.mu),
+                         float(mat.lam), float(self.near_factor), float(t.scale), ptr(rowptr), ptr(cols),
+                         int(cols.numel()), ptr(blk), R.stride(0), stream_handle())
+            else:
+                self._block_into(R[:, t.col.offset:t.col.stop], t.field_patch, t.source_patch, t.kernel, mat,
+                                 t.scale, True)
+            D = term_diagonal(t, self.calib)
+            if D is not None:
+                Dd = as_cuda(np.ascontiguousarray(D)) if not isinstance(D, torch.Tensor) else D.contiguous()
+                shape = np.ascontiguousarray(t.field_patch.collocation_shape(), dtype=float)
+                nat.call("mbem_add_block_diagonal", ptr(R[:, t.col.offset:]), R.stride(0), ptr(Dd),
+                         t.field_patch.n_nodes, shape.shape[0], nat.dbl_array(shape.ravel()), stream_handle())
+        fault_rows_one(R, b[r0:r0 + m], region, f, r0, self.fault_drag)
+        A32 = op.A32[r0:r0 + m, :n]
+        A32.copy_(R)
+        A16 = None if op.A16 is None else op.A16[r0:r0 + m, :n]
+        if A16 is not None:
+            A16.copy_(R)
+        three = torch.arange(3, device=dev)
+        for slot in self.layout.slots:
+            if slot.offset not in near:
+                continue
+            rowptr, cols = near[slot.offset]
+            nnz = int(cols.numel())
+            if nnz == 0:
+                continue
+            fidx = torch.repeat_interleave(torch.arange(xf.shape[0], device=dev), rowptr[1:] - rowptr[:-1])
+            rr = (3 * fidx[:, None] + three)[:, :, None].expand(nnz, 3, 3)
+            cc = (slot.offset + 3 * cols[:, None] + three)[:, None, :].expand(nnz, 3, 3)
+            vals = R[rr, cc].reshape(nnz, 9).contiguous()
+            A32[rr, cc] = 0.0
+            if A16 is not None:
+                A16[rr, cc] = 0.0
+            op.near.append(NearList(r0, slot.offset, xf.shape[0], rowptr, cols, vals))
+        del R
 
     def _build(self):
         if self.precision == "mixed":
@@ -408,6 +494,8 @@ class AssembledDense:
                      ptr(Dd), t.field_patch.n_nodes, K, nat.dbl_array(shape.ravel()), stream_handle())
 
         for rt in self.system.rhs_terms:
+            if rt.kernel in (KERNEL_HT, KERNEL_GT) and not np.any(np.asarray(rt.vector, float)):
+                continue                        # a zero density adds nothing (e.g. a traction-free patch)
             mat = self.materials[rt.region.name]
             bview = b[rt.row.offset:rt.row.stop].view(-1, 3)
             f = self._patch_arrays(rt.field_patch)

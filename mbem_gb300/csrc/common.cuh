@@ -42,6 +42,12 @@ int nodal_pairs_stress(const double* x, const double* tv, const double* normals,
                        const double* density, double mu, double lam, int order, const int64_t* pair_obs,
                        const int32_t* pair_src, int64_t n_pairs, double* out, cudaStream_t st,
                        double* out_eig = nullptr);
+// FP64 traction blocks of listed (field point, source) pairs of an order-0
+// source patch, added into out (ld) at columns 3 s .. 3 s + 2 (nodal.cu).
+int traction_pairs(const double* x_field, const double* n_field, int64_t n_pts, const double* tri_verts,
+                   const double* normals, const double* eps, int64_t n_src, double mu, double lam, int which,
+                   double alpha, const int64_t* rowptr, const int64_t* cols, int64_t nnz, double* out, int64_t ld,
+                   cudaStream_t st);
 int nodal_contract(int kind, const double* x, int64_t nf, const double* tv, const double* normals,
                    const double* eps, int64_t ns, const double* density, const double* coeffs,
                    double mu, double lam, int order, double alpha, int accumulate, double* out,

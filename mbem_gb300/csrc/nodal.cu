@@ -816,6 +816,9 @@ struct NodalArgs {
     double* out;
     int64_t ld;
     int64_t plane;
+    const int64_t* pair_rowptr;   // listed pairs (traction rows of the mixed operator): field point f's
+    const int64_t* pair_cols;     // sources at pair_cols[pair_rowptr[f] .. pair_rowptr[f+1]); NULL: all pairs
+    int64_t n_pairs;
 };
 
 constexpr int ND_THREADS = 64;
@@ -955,8 +958,22 @@ nodal_contract_kernel(NodalArgs a, NodalSpec sp, int kind, int split) {
 __global__ void __launch_bounds__(ND_THREADS)
 nodal_traction_kernel(NodalArgs a, NodalSpec sp) {
     const int64_t idx = (int64_t)blockIdx.x * ND_THREADS + threadIdx.x;
-    if (idx >= a.n_field_pts * a.n_src) return;
-    const int64_t f = idx / a.n_src, s = idx % a.n_src;
+    int64_t f, s;
+    if (a.pair_cols) {
+        if (idx >= a.n_pairs) return;
+        int64_t lo = 0, hi = a.n_field_pts;
+        while (hi - lo > 1) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (a.pair_rowptr[mid] <= idx) lo = mid;
+            else hi = mid;
+        }
+        f = lo;
+        s = a.pair_cols[idx];
+    } else {
+        if (idx >= a.n_field_pts * a.n_src) return;
+        f = idx / a.n_src;
+        s = idx % a.n_src;
+    }
     const int K = sp.K;
     const double* nf = a.n_field + 3 * f;
     double W[4][ND_MAXK][5][5];
@@ -984,7 +1001,7 @@ nodal_traction_kernel(NodalArgs a, NodalSpec sp) {
             M.z = z;
             if (sw == 1) far_moments_p0<true>(g, X1, X2, h2, q0, q1, M);
             else far_moments_p0<false>(g, X1, X2, h2, q0, q1, M);
-            const int64_t id = a.ids[s];
+            const int64_t id = a.ids ? a.ids[s] : s;
             if (id < 0 || id >= a.n_cols) return;
             for (int j = 0; j < 3; j++) {
                 const double d[3] = {j == 0 ? 1.0 : 0.0, j == 1 ? 1.0 : 0.0, j == 2 ? 1.0 : 0.0};
@@ -1000,7 +1017,7 @@ nodal_traction_kernel(NodalArgs a, NodalSpec sp) {
     }
     const double z = nodal_pair_tables(sp, g, a.x_field + 3 * f, eps, W, S);
     for (int k = 0; k < K; k++) {
-        const int64_t id = a.ids[s * K + k];
+        const int64_t id = a.ids ? a.ids[s * K + k] : s * K + k;
         if (id < 0 || id >= a.n_cols) continue;        // outside the block: never written
         const int64_t col = 3 * id;
         for (int j = 0; j < 3; j++) {
@@ -1205,6 +1222,32 @@ extern "C" int mbem_near_eval_nodal(int kernel, int order, const double* x_field
         a, sp, kernel, rowptr, cols, nnz, vals);
     return launch_status("nodal_near_eval_kernel");
 }
+
+namespace mbem {
+// FP64 traction blocks of listed (field point, source) pairs of an order-0
+// source patch (the near pairs of the mixed operator's traction rows), added
+// into out at column 3 s + j: the per-pair code of mbem_traction_matrix.
+int traction_pairs(const double* x_field, const double* n_field, int64_t n_pts, const double* tri_verts,
+                   const double* normals, const double* eps, int64_t n_src, double mu, double lam, int which,
+                   double alpha, const int64_t* rowptr, const int64_t* cols, int64_t nnz, double* out, int64_t ld,
+                   cudaStream_t st) {
+    int e = ensure_rules();
+    if (e) return e;
+    const int flags = (which == 1) ? KF_S : (which == 2 ? KF_E : KF_H);
+    const NodalSpec sp = make_spec(0, flags);
+    MBEM_REQUIRE(sp.valid, MBEM_ERR_UNSUPPORTED, "nodal degrees beyond the P2 tables");
+    NodalArgs a;
+    memset(&a, 0, sizeof(a));
+    a.x_field = x_field; a.n_field = n_field; a.n_field_pts = n_pts; a.tri_verts = tri_verts;
+    a.normals = normals; a.eps = eps; a.n_src = n_src; a.n_cols = n_src;
+    a.mu = mu; a.lam = lam; a.alpha = alpha; a.which = which; a.out = out; a.ld = ld;
+    a.pair_rowptr = rowptr; a.pair_cols = cols; a.n_pairs = nnz;
+    a.ids = nullptr;
+    if (nnz == 0) return MBEM_OK;
+    nodal_traction_kernel<<<(unsigned)ceil_div(nnz, ND_THREADS), ND_THREADS, 0, st>>>(a, sp);
+    return launch_status("nodal_traction_kernel");
+}
+}  // namespace mbem
 
 extern "C" int mbem_traction_matrix(const double* x_field, const double* n_field, int64_t n_pts,
                                     const double* tri_verts, const double* normals, const double* eps,
