@@ -153,14 +153,49 @@ __device__ __forceinline__ int far_rule(float D2, float L2) {
 // Far T block (FP32): out_ij = n_j alpha_i + n_i beta_j + d_ij gamma - 6 c5 W_ij
 // from the quadrature sums V3 = int d/R^3, V5 = int d/R^5,
 // t = int d |d|^2/R^5, W = int d d (d.n)/R^5 (d = x - y).
+// U block: out_ij = c2 W_ij + d_ij (c0 I1 + c1 eps^2 I3), W = int d d / R^3.
+struct FarSums {
+    float V3[3], V5[3], t[3];
+    float W00, W01, W02, W11, W12, W22;
+    float I1, I3;
+};
+
+template <bool TKERNEL>
+__device__ __forceinline__ void far_epilogue(const SrcFar& s, const FarSums& m, const float c[6], float out[3][3]) {
+    const float A = s.area2;
+    const float W[3][3] = {{m.W00, m.W01, m.W02}, {m.W01, m.W11, m.W12}, {m.W02, m.W12, m.W22}};
+    if (TKERNEL) {
+        const float* n = s.n;
+        const float nV3 = n[0] * m.V3[0] + n[1] * m.V3[1] + n[2] * m.V3[2];
+        const float nV5 = n[0] * m.V5[0] + n[1] * m.V5[1] + n[2] * m.V5[2];
+        const float ca = c[0] + 4.0f * c[1] + 2.0f * c[4];
+        const float cb = c[3] + c[4];
+        const float ce3 = c[2] * s.eps2, ce6 = c[5] * s.eps2;
+        const float gam = cb * nV3 + ce6 * nV5;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float al = ca * m.V3[i] - 3.0f * c[1] * m.t[i] + ce3 * m.V5[i];
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const float be = cb * m.V3[j] + ce6 * m.V5[j];
+                out[i][j] = A * (n[j] * al + n[i] * be - 6.0f * c[4] * W[i][j] + (i == j ? gam : 0.0f));
+            }
+        }
+    } else {
+        const float dg = c[0] * m.I1 + c[1] * s.eps2 * m.I3;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) out[i][j] = A * (c[2] * W[i][j] + (i == j ? dg : 0.0f));
+    }
+}
+
 template <bool TKERNEL>
 __device__ __forceinline__ void far_block(const QuadRules& Q, const SrcFar& s, const float dc[3], float D2,
                                           const float c[6], float out[3][3]) {
     const int nq = far_rule(D2, s.L2);
     const int q0 = Q.off[nq], q1 = q0 + nq * nq;
-    float V3[3] = {0, 0, 0}, V5[3] = {0, 0, 0}, t[3] = {0, 0, 0};
-    float W00 = 0, W01 = 0, W02 = 0, W11 = 0, W12 = 0, W22 = 0;
-    float I1 = 0, I3 = 0;   // U kernel: int 1/R, int 1/R^3
+    FarSums m = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int q = q0; q < q1; q++) {
         const float a = Q.a[q], b = Q.b[q];
         const float dx = dc[0] - (a * s.e1[0] + b * s.e2[0]);
@@ -173,48 +208,82 @@ __device__ __forceinline__ void far_block(const QuadRules& Q, const SrcFar& s, c
         const float w3 = w * iR2 * iR;
         if (TKERNEL) {
             const float w5 = w3 * iR2;
-            V3[0] += w3 * dx; V3[1] += w3 * dy; V3[2] += w3 * dz;
-            V5[0] += w5 * dx; V5[1] += w5 * dy; V5[2] += w5 * dz;
+            m.V3[0] += w3 * dx; m.V3[1] += w3 * dy; m.V3[2] += w3 * dz;
+            m.V5[0] += w5 * dx; m.V5[1] += w5 * dy; m.V5[2] += w5 * dz;
             const float wt = w5 * r2;
-            t[0] += wt * dx; t[1] += wt * dy; t[2] += wt * dz;
+            m.t[0] += wt * dx; m.t[1] += wt * dy; m.t[2] += wt * dz;
             const float wn = w5 * (dx * s.n[0] + dy * s.n[1] + dz * s.n[2]);
             const float ux = wn * dx, uy = wn * dy, uz = wn * dz;
-            W00 += ux * dx; W01 += ux * dy; W02 += ux * dz;
-            W11 += uy * dy; W12 += uy * dz; W22 += uz * dz;
+            m.W00 += ux * dx; m.W01 += ux * dy; m.W02 += ux * dz;
+            m.W11 += uy * dy; m.W12 += uy * dz; m.W22 += uz * dz;
         } else {
-            I1 += w * iR;
-            I3 += w3;
+            m.I1 += w * iR;
+            m.I3 += w3;
             const float ux = w3 * dx, uy = w3 * dy, uz = w3 * dz;   // T2[3] = int d d / R^3
-            W00 += ux * dx; W01 += ux * dy; W02 += ux * dz;
-            W11 += uy * dy; W12 += uy * dz; W22 += uz * dz;
+            m.W00 += ux * dx; m.W01 += ux * dy; m.W02 += ux * dz;
+            m.W11 += uy * dy; m.W12 += uy * dz; m.W22 += uz * dz;
         }
     }
-    const float A = s.area2;
-    const float W[3][3] = {{W00, W01, W02}, {W01, W11, W12}, {W02, W12, W22}};
-    if (TKERNEL) {
-        const float* n = s.n;
-        const float nV3 = n[0] * V3[0] + n[1] * V3[1] + n[2] * V3[2];
-        const float nV5 = n[0] * V5[0] + n[1] * V5[1] + n[2] * V5[2];
-        const float ca = c[0] + 4.0f * c[1] + 2.0f * c[4];
-        const float cb = c[3] + c[4];
-        const float ce3 = c[2] * s.eps2, ce6 = c[5] * s.eps2;
-        const float gam = cb * nV3 + ce6 * nV5;
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            const float al = ca * V3[i] - 3.0f * c[1] * t[i] + ce3 * V5[i];
-#pragma unroll
-            for (int j = 0; j < 3; j++) {
-                const float be = cb * V3[j] + ce6 * V5[j];
-                out[i][j] = A * (n[j] * al + n[i] * be - 6.0f * c[4] * W[i][j] + (i == j ? gam : 0.0f));
-            }
+    far_epilogue<TKERNEL>(s, m, c, out);
+}
+
+// Two field points of one source at once (both far), in packed FP32
+// (FFMA2 / FMUL2 / FADD2 on float2 lanes): the quadrature point offsets are
+// shared, every per-point quantity is a pair. Both points take the rule of
+// the nearer one (a rule at least as accurate as its own for the farther).
+__device__ __forceinline__ float2 f2s(float v) { return make_float2(v, v); }
+
+template <bool TKERNEL>
+__device__ __forceinline__ void far_block2(const QuadRules& Q, const SrcFar& s, const float da[3], const float db[3],
+                                           float D2a, float D2b, const float c[6], float outa[3][3],
+                                           float outb[3][3]) {
+    const int nq = far_rule(fminf(D2a, D2b), s.L2);
+    const int q0 = Q.off[nq], q1 = q0 + nq * nq;
+    const float2 dc0 = make_float2(da[0], db[0]), dc1 = make_float2(da[1], db[1]), dc2 = make_float2(da[2], db[2]);
+    const float2 e2 = f2s(s.eps2);
+    const float2 n0 = f2s(s.n[0]), n1 = f2s(s.n[1]), n2 = f2s(s.n[2]);
+    const float2 z = f2s(0.0f);
+    float2 V30 = z, V31 = z, V32 = z, V50 = z, V51 = z, V52 = z, t0 = z, t1 = z, t2 = z;
+    float2 W00 = z, W01 = z, W02 = z, W11 = z, W12 = z, W22 = z, I1 = z, I3 = z;
+    for (int q = q0; q < q1; q++) {
+        const float a = Q.a[q], b = Q.b[q];
+        const float ox = a * s.e1[0] + b * s.e2[0];
+        const float oy = a * s.e1[1] + b * s.e2[1];
+        const float oz = a * s.e1[2] + b * s.e2[2];
+        const float2 dx = __fadd2_rn(dc0, f2s(-ox));
+        const float2 dy = __fadd2_rn(dc1, f2s(-oy));
+        const float2 dz = __fadd2_rn(dc2, f2s(-oz));
+        const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+        const float2 re = __fadd2_rn(r2, e2);
+        const float2 iR = make_float2(rsqrtf(re.x), rsqrtf(re.y));
+        const float2 w = f2s(Q.w[q]);
+        const float2 iR2 = __fmul2_rn(iR, iR);
+        const float2 w3 = __fmul2_rn(__fmul2_rn(w, iR2), iR);
+        if (TKERNEL) {
+            const float2 w5 = __fmul2_rn(w3, iR2);
+            V30 = __ffma2_rn(w3, dx, V30); V31 = __ffma2_rn(w3, dy, V31); V32 = __ffma2_rn(w3, dz, V32);
+            V50 = __ffma2_rn(w5, dx, V50); V51 = __ffma2_rn(w5, dy, V51); V52 = __ffma2_rn(w5, dz, V52);
+            const float2 wt = __fmul2_rn(w5, r2);
+            t0 = __ffma2_rn(wt, dx, t0); t1 = __ffma2_rn(wt, dy, t1); t2 = __ffma2_rn(wt, dz, t2);
+            const float2 dn = __ffma2_rn(dx, n0, __ffma2_rn(dy, n1, __fmul2_rn(dz, n2)));
+            const float2 wn = __fmul2_rn(w5, dn);
+            const float2 ux = __fmul2_rn(wn, dx), uy = __fmul2_rn(wn, dy), uz = __fmul2_rn(wn, dz);
+            W00 = __ffma2_rn(ux, dx, W00); W01 = __ffma2_rn(ux, dy, W01); W02 = __ffma2_rn(ux, dz, W02);
+            W11 = __ffma2_rn(uy, dy, W11); W12 = __ffma2_rn(uy, dz, W12); W22 = __ffma2_rn(uz, dz, W22);
+        } else {
+            I1 = __ffma2_rn(w, iR, I1);
+            I3 = __fadd2_rn(I3, w3);
+            const float2 ux = __fmul2_rn(w3, dx), uy = __fmul2_rn(w3, dy), uz = __fmul2_rn(w3, dz);
+            W00 = __ffma2_rn(ux, dx, W00); W01 = __ffma2_rn(ux, dy, W01); W02 = __ffma2_rn(ux, dz, W02);
+            W11 = __ffma2_rn(uy, dy, W11); W12 = __ffma2_rn(uy, dz, W12); W22 = __ffma2_rn(uz, dz, W22);
         }
-    } else {
-        const float dg = c[0] * I1 + c[1] * s.eps2 * I3;
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int j = 0; j < 3; j++) out[i][j] = A * (c[2] * W[i][j] + (i == j ? dg : 0.0f));
     }
+    const FarSums ma = {{V30.x, V31.x, V32.x}, {V50.x, V51.x, V52.x}, {t0.x, t1.x, t2.x}, W00.x, W01.x, W02.x,
+                        W11.x, W12.x, W22.x, I1.x, I3.x};
+    const FarSums mb = {{V30.y, V31.y, V32.y}, {V50.y, V51.y, V52.y}, {t0.y, t1.y, t2.y}, W00.y, W01.y, W02.y,
+                        W11.y, W12.y, W22.y, I1.y, I3.y};
+    far_epilogue<TKERNEL>(s, ma, c, outa);
+    far_epilogue<TKERNEL>(s, mb, c, outb);
 }
 
 

@@ -234,29 +234,8 @@ far_assemble_kernel(FarArgs a, QuadRules Q) {
         }
         __syncthreads();
         const int nf = (int)lmin(FAR_FIELD_TILE, a.n_field - f0);
-        for (int ff = 0; ff < nf; ff++) {
-            const int64_t f = f0 + ff;
-            float d[3], D2;
-            float blk[K][3][3];
-            const bool near = is_near(xs[ff], src, d, D2) && active;
-            if (a.near_mask) {
-                const unsigned m = __ballot_sync(0xffffffffu, near);
-                // lane 0 of a warp with at least one source writes its word
-                if ((threadIdx.x & 31) == 0 && (s >> 5) < n_words) a.near_mask[f * n_words + (s >> 5)] = m;
-            }
-            if (!active) continue;
-            if (near || !src.ok) {
-#pragma unroll
-                for (int k = 0; k < K; k++)
-#pragma unroll
-                    for (int i = 0; i < 3; i++)
-#pragma unroll
-                        for (int j = 0; j < 3; j++) blk[k][i][j] = 0.0f;
-            } else if (ORDER == 0) {
-                far_block<TKERNEL>(Q, src, d, D2, a.c, blk[0]);
-            } else {
-                far_block_nodal<TKERNEL, ORDER>(Q, src, d, D2, a.c, blk);
-            }
+        // blocks of field point f into the FP32 matrix (and its BF16 copy)
+        auto store = [&](int64_t f, const float (*blk)[3][3]) {
             // columns 3 (K s + k) + j
 #pragma unroll
             for (int i = 0; i < 3; i++) {
@@ -276,6 +255,56 @@ far_assemble_kernel(FarArgs a, QuadRules Q) {
                         for (int j = 0; j < 3; j++)
                             row[3 * k + j] = __bfloat16_as_ushort(__float2bfloat16_rn(a.alpha * blk[k][i][j]));
                 }
+            }
+        };
+        auto mask = [&](int64_t f, bool near) {
+            if (a.near_mask) {
+                const unsigned m = __ballot_sync(0xffffffffu, near);
+                // lane 0 of a warp with at least one source writes its word
+                if ((threadIdx.x & 31) == 0 && (s >> 5) < n_words) a.near_mask[f * n_words + (s >> 5)] = m;
+            }
+        };
+        // P0: field points two at a time in packed FP32 when both are far
+        for (int ff = 0; ff < nf; ff += (ORDER == 0 ? 2 : 1)) {
+            const int64_t f = f0 + ff;
+            const bool two = ORDER == 0 && ff + 1 < nf;
+            float d[3], D2, d2[3], D2b = 0.0f;
+            float blk[K][3][3], blk2[K][3][3];
+            const bool near = is_near(xs[ff], src, d, D2) && active;
+            const bool near2 = two && is_near(xs[ff + 1], src, d2, D2b) && active;
+            mask(f, near);
+            if (two) mask(f + 1, near2);
+            if (!active) continue;
+            const bool pair = two && src.ok && !near && !near2;
+            if (pair) {
+                far_block2<TKERNEL>(Q, src, d, d2, D2, D2b, a.c, blk[0], blk2[0]);
+            } else if (near || !src.ok) {
+#pragma unroll
+                for (int k = 0; k < K; k++)
+#pragma unroll
+                    for (int i = 0; i < 3; i++)
+#pragma unroll
+                        for (int j = 0; j < 3; j++) blk[k][i][j] = 0.0f;
+            } else if (ORDER == 0) {
+                far_block<TKERNEL>(Q, src, d, D2, a.c, blk[0]);
+            } else {
+                far_block_nodal<TKERNEL, ORDER>(Q, src, d, D2, a.c, blk);
+            }
+            store(f, blk);
+            if (two) {
+                if (!pair) {
+                    if (near2 || !src.ok) {
+#pragma unroll
+                        for (int k = 0; k < K; k++)
+#pragma unroll
+                            for (int i = 0; i < 3; i++)
+#pragma unroll
+                                for (int j = 0; j < 3; j++) blk2[k][i][j] = 0.0f;
+                    } else {
+                        far_block<TKERNEL>(Q, src, d2, D2b, a.c, blk2[0]);
+                    }
+                }
+                store(f + 1, blk2);
             }
         }
     }
