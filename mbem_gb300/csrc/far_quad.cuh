@@ -104,33 +104,35 @@ struct SrcFar {
     bool ok;
 };
 
+// Edges as exact FP64 differences rounded to FP32, the centroid in
+// double-float; everything else in FP32 (the FP64 pipe runs 1/64 of FP32 here,
+// and every CTA of the far-field kernels sets up its sources).
 __device__ __forceinline__ void far_setup(const double* __restrict__ tv, const double* __restrict__ nrm,
                                           double eps, double near_factor, SrcFar& s) {
-    const double e1x = tv[3] - tv[0], e1y = tv[4] - tv[1], e1z = tv[5] - tv[2];
-    const double e2x = tv[6] - tv[0], e2y = tv[7] - tv[1], e2z = tv[8] - tv[2];
-    const double e3x = tv[6] - tv[3], e3y = tv[7] - tv[4], e3z = tv[8] - tv[5];
-    const double cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
-    const double a2 = sqrt(cx * cx + cy * cy + cz * cz);
-    s.ok = a2 >= 1e-30;
-    const double l1 = sqrt(e1x * e1x + e1y * e1y + e1z * e1z);
-    const double l2 = sqrt(e2x * e2x + e2y * e2y + e2z * e2z);
-    const double l3 = sqrt(e3x * e3x + e3y * e3y + e3z * e3z);
-    const double Lm = fmax(fmax(l1, l2), l3);
-    const double h = (l1 + l2 + l3) / 3.0;    // mean edge length
-    const double rn = near_factor * fmax(eps, h);
-    for (int k = 0; k < 3; k++) s.c[k] = split_d((tv[k] + tv[3 + k] + tv[6 + k]) / 3.0);
-    s.e1[0] = (float)e1x; s.e1[1] = (float)e1y; s.e1[2] = (float)e1z;
-    s.e2[0] = (float)e2x; s.e2[1] = (float)e2y; s.e2[2] = (float)e2z;
+    const float e1x = (float)(tv[3] - tv[0]), e1y = (float)(tv[4] - tv[1]), e1z = (float)(tv[5] - tv[2]);
+    const float e2x = (float)(tv[6] - tv[0]), e2y = (float)(tv[7] - tv[1]), e2z = (float)(tv[8] - tv[2]);
+    const float e3x = (float)(tv[6] - tv[3]), e3y = (float)(tv[7] - tv[4]), e3z = (float)(tv[8] - tv[5]);
+    const float cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
+    const float a2 = sqrtf(cx * cx + cy * cy + cz * cz);
+    s.ok = a2 >= 1e-30f;
+    const float l1 = sqrtf(e1x * e1x + e1y * e1y + e1z * e1z);
+    const float l2 = sqrtf(e2x * e2x + e2y * e2y + e2z * e2z);
+    const float l3 = sqrtf(e3x * e3x + e3y * e3y + e3z * e3z);
+    const float Lm = fmaxf(fmaxf(l1, l2), l3);
+    const float h = (l1 + l2 + l3) * (1.0f / 3.0f);    // mean edge length
+    const float rn = (float)near_factor * fmaxf((float)eps, h);
+    for (int k = 0; k < 3; k++) s.c[k] = split_d((tv[k] + tv[3 + k] + tv[6 + k]) * (1.0 / 3.0));
+    s.e1[0] = e1x; s.e1[1] = e1y; s.e1[2] = e1z;
+    s.e2[0] = e2x; s.e2[1] = e2y; s.e2[2] = e2z;
     if (nrm) {
         s.n[0] = (float)nrm[0]; s.n[1] = (float)nrm[1]; s.n[2] = (float)nrm[2];
     } else {
         s.n[0] = s.n[1] = s.n[2] = 0.0f;
     }
-    s.area2 = (float)a2;
+    s.area2 = a2;
     s.eps2 = (float)(eps * eps);
-    s.L2 = (float)(Lm * Lm);
-    const double r2 = fmax(rn * rn, 2.25 * Lm * Lm);
-    s.rnear2 = (float)r2;
+    s.L2 = Lm * Lm;
+    s.rnear2 = fmaxf(rn * rn, 2.25f * Lm * Lm);
 }
 
 // The one near/far decision, shared by every kernel that needs it.
