@@ -754,8 +754,7 @@ int mbem_pair_prepare(const mbem_pair_geometry* g, void* stream);
 /* Cross approximation of a batch of admissible blocks (aca.py:334-419
  * aca_single, :579-658 compress_block): one CTA per block, 3 x 3 element
  * pivots, stopped when the residual on 10 x 10 sampled element pairs falls
- * below tol / 2 of the sample's norm; recompressed (see recompress_max);
- * certified on 3 random element rows and
+ * below tol / 2 of the sample's norm; certified on 3 random element rows and
  * 3 random element columns evaluated exactly; a certificate above 3 tol
  * reruns the block at tol / 10 and a second failure, or the rank cap,
  * leaves the block to be applied exactly. Factors are written transposed:
@@ -777,18 +776,45 @@ typedef struct {
     float* U;
     float* V;
     int32_t* rank;              /* out: factor columns, 3 x pivots (0 unless low rank) */
-    int32_t* status;            /* out: MBEM_ACA_* in bits 0-2; bits 8-15 and 16-23: the sweeps of the
-                                   last recompression's two Jacobi passes (0: not recompressed) */
+    int32_t* status;            /* out: MBEM_ACA_* */
     float* err;                 /* out: certified relative Frobenius error of the factors kept */
     double tol;                 /* block tolerance (BLOCK_COMPRESSION_TOL) */
     uint64_t seed;              /* sample and certificate lines of block i come from (seed, first_index + i) */
     int64_t first_index;
     int max_nr, max_nc, max_pivots_all;  /* maxima over the batch (shared-memory size) */
-    int recompress_max;         /* converged factors of 2 .. recompress_max columns are recompressed (the
-                                   SVD of U V^T truncated at tol / 2, aca.py:422-438) before the
-                                   certificate; 0 keeps the cross approximation's own factors */
 } mbem_aca_batch;
 int mbem_aca_compress(const mbem_pair_geometry* g, const mbem_aca_batch* b, void* stream);
+/* Recompression of cross-approximation factors (aca.py:422-438 recompress):
+ * the SVD of U V^T truncated at tol / 2, through its K x K core (double-float
+ * Grams, FP64 Cholesky factors Ru, Rv, one-sided Jacobi on C = Ru Rv^T in
+ * FP32; U' = U Rv^T Y_k, V' = V Ru^T (C Y)_k S_k^-2), written transposed to
+ * Ur / Vr (capacity rank[i] rows each) and certified on the block's
+ * certificate lines (those of mbem_aca_compress for the same seed and block
+ * index); rank_out[i] = the columns kept, or 0 when the block is not
+ * recompressed (rank outside [2, max_rank]) or its certificate exceeds 3 tol. */
+typedef struct {
+    int64_t n_blocks;
+    const int32_t* r0;
+    const int32_t* nr;
+    const int32_t* c0;
+    const int32_t* nc;
+    const int32_t* rank;        /* factor columns of the cross approximation */
+    const int64_t* u_off;       /* its factors, as mbem_aca_compress wrote them */
+    const int64_t* v_off;
+    const float* U;
+    const float* V;
+    const int64_t* ur_off;      /* out: float offsets of the recompressed factors */
+    const int64_t* vr_off;
+    float* Ur;
+    float* Vr;
+    int32_t* rank_out;
+    float* err_out;
+    const int64_t* index;       /* the block's index for its certificate lines */
+    double tol;
+    uint64_t seed;
+    int max_rank;               /* at most 64 (shared-memory size) */
+} mbem_aca_recompression;
+int mbem_aca_recompress(const mbem_pair_geometry* g, const mbem_aca_recompression* r, void* stream);
 /* Copies the first rank[i] rows of each block's U^T and V^T from the batch
  * scratch to their final offsets. */
 int mbem_aca_compact(int64_t n_blocks, const int32_t* nr, const int32_t* nc, const int32_t* rank,

@@ -105,7 +105,18 @@ class AcaBatch(Structure):
                 ("max_pivots", c_void_p), ("u_off", c_void_p), ("v_off", c_void_p), ("U", c_void_p),
                 ("V", c_void_p), ("rank", c_void_p), ("status", c_void_p), ("err", c_void_p), ("tol", c_double),
                 ("seed", ctypes.c_uint64), ("first_index", c_int64), ("max_nr", c_int), ("max_nc", c_int),
-                ("max_pivots_all", c_int), ("recompress_max", c_int)]
+                ("max_pivots_all", c_int)]
+
+
+class AcaRecompression(Structure):
+    _fields_ = [("n_blocks", c_int64), ("r0", c_void_p), ("nr", c_void_p), ("c0", c_void_p), ("nc", c_void_p),
+                ("rank", c_void_p), ("u_off", c_void_p), ("v_off", c_void_p), ("U", c_void_p), ("V", c_void_p),
+                ("ur_off", c_void_p), ("vr_off", c_void_p), ("Ur", c_void_p), ("Vr", c_void_p),
+                ("rank_out", c_void_p), ("err_out", c_void_p), ("index", c_void_p), ("tol", c_double),
+                ("seed", ctypes.c_uint64), ("max_rank", c_int)]
+
+
+RC_KMAX = 64
 
 
 class CompressedView(Structure):
@@ -259,6 +270,7 @@ _SIGNATURES = {
     "mbem_pair_prepare": (c_int, [POINTER(PairGeometry), _P]),
     "mbem_aca_compress": (c_int, [POINTER(PairGeometry), POINTER(AcaBatch), _P]),
     "mbem_aca_compact": (c_int, [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "mbem_aca_recompress": (c_int, [POINTER(PairGeometry), POINTER(AcaRecompression), _P]),
     "mbem_pair_dense_blocks": (c_int, [POINTER(PairGeometry), _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "mbem_compressed_matvec_workspace_size": (c_size_t, [POINTER(CompressedView)]),
     "mbem_compressed_matvec": (c_int, [POINTER(CompressedView), _P, _P, _P, c_size_t, _P]),

@@ -30,8 +30,9 @@
 // rank-deficient pivot adds only its rank in columns (the reference adds three
 // and drops the empty one when it recompresses); the
 // sample and certificate lines come from a counter-based generator seeded
-// per block instead of numpy's; the factors are not recompressed by a
-// QR + SVD (they are certified as stored).
+// per block instead of numpy's; the optional recompression (rc_kernel) works
+// on the K x K core of the factors instead of a QR of each factor, and is
+// certified again (the reference certifies the recompressed factors once).
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
@@ -309,10 +310,7 @@ __device__ __forceinline__ void block_argmax(float& v, int& i, float* rv, int* r
 }
 
 // ---------------------------------------------------------------------------
-// recompression of the cross approximation (aca.py:422-428 recompress):
-// the SVD of U V^T truncated at the tail rule of aca.py:431-438 _svd_keep,
-// by one-sided Jacobi on the factor rows in place (each factor is stored
-// transposed, so a column of U or V is a contiguous row here)
+// one-sided Jacobi (the recompression's SVD of its K x K core, rc_kernel)
 // ---------------------------------------------------------------------------
 // Pairs this close to orthogonal are left alone (1e-3 was measured to keep
 // more blocks exact: the truncation then misjudges the tail); the certificate
@@ -408,70 +406,17 @@ __device__ __forceinline__ double row_norm2(const float* A, int lda, int la, int
     return d;
 }
 
-// U V^T (U^T: K rows of la at ldu; V^T: K rows of lb at ldv) replaced by its
-// SVD truncated to the smallest k with ||s[k:]|| <= tol s[0] (at least 1):
-// one-sided Jacobi on V's columns (rotations carried to U), V's columns
-// normalised with their norms moved to U, one-sided Jacobi on U's columns
-// (carried to V); then U's column norms are the singular values, and the kept
-// rows are compacted in place. sig: 3K words of shared memory (values,
-// ranks, sorted values).
-// Returns k.
-__device__ int recompress(float* U, int ldu, int la, float* V, int ldv, int lb, int K, double tol, float* sig,
-                          int* rk, int* flag, int* sweeps) {
-    const int warp = threadIdx.x >> 5;
-    const int s1 = osj_sweeps(V, ldv, lb, U, ldu, la, K, flag);
-    for (int k = warp; k < K; k += ACA_WARPS) {
-        const double nv = sqrt(row_norm2(V, ldv, lb, k));
-        const float su = (float)nv, sv = nv > 0.0 ? (float)(1.0 / nv) : 0.0f;
-        const int lane = threadIdx.x & 31;
-        for (int e = lane; e < la; e += 32) U[(int64_t)k * ldu + e] *= su;
-        for (int e = lane; e < lb; e += 32) V[(int64_t)k * ldv + e] *= sv;
-    }
-    __syncthreads();
-    const int s2 = osj_sweeps(U, ldu, la, V, ldv, lb, K, flag);
-    *sweeps = min(s1, 255) | (min(s2, 255) << 8);
-    for (int k = warp; k < K; k += ACA_WARPS) {
-        const double d = sqrt(row_norm2(U, ldu, la, k));
-        if ((threadIdx.x & 31) == 0) sig[k] = (float)d;
-    }
-    __syncthreads();
-    // rank of each singular value (descending, ties by index)
-    for (int j = threadIdx.x; j < K; j += blockDim.x) {
-        int r = 0;
-        const float sj = sig[j];
-        for (int i = 0; i < K; i++) r += (sig[i] > sj || (sig[i] == sj && i < j)) ? 1 : 0;
-        rk[j] = r;
-    }
-    __syncthreads();
-    float* srt = sig + 2 * K;     // the values in descending order
-    for (int j = threadIdx.x; j < K; j += blockDim.x) srt[rk[j]] = sig[j];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const double s0 = srt[0];
-        double dropped = 0.0;
-        int keep = K;
-        for (int r = K - 1; r >= 1; r--) {
-            const double sr = srt[r];
-            if (dropped + sr * sr > tol * tol * s0 * s0) break;
-            dropped += sr * sr;
-            keep = r;
-        }
-        *flag = keep;
-    }
-    __syncthreads();
-    const int keep = *flag;
-    // stable in-place compaction of the kept rows (a row only moves down)
-    int dst = 0;
-    for (int j = 0; j < K; j++) {
-        if (rk[j] >= keep) continue;
-        if (dst != j) {
-            for (int e = threadIdx.x; e < ldu; e += blockDim.x) U[(int64_t)dst * ldu + e] = U[(int64_t)j * ldu + e];
-            for (int e = threadIdx.x; e < ldv; e += blockDim.x) V[(int64_t)dst * ldv + e] = V[(int64_t)j * ldv + e];
-        }
-        dst++;
-        __syncthreads();
-    }
-    return keep;
+// The sample rows and columns (ACA_SAMPLE each) and the certificate rows and
+// columns (ACA_CERT each) of block `index`, from a counter-based stream seeded
+// by (seed, index): lines[0..9] rows, [10..19] columns, [20..22] certificate
+// rows, [23..25] certificate columns.
+__device__ void draw_lines(uint64_t seed, int64_t index, int nr, int nc, int* lines) {
+    uint64_t st = seed ^ (0xD1B54A32D192ED03ull * (uint64_t)(index + 1));
+    splitmix(st);
+    draw_distinct(st, nr, min(ACA_SAMPLE, nr), lines);
+    draw_distinct(st, nc, min(ACA_SAMPLE, nc), lines + ACA_SAMPLE);
+    draw_distinct(st, nr, min(ACA_CERT, nr), lines + 2 * ACA_SAMPLE);
+    draw_distinct(st, nc, min(ACA_CERT, nc), lines + 2 * ACA_SAMPLE + ACA_CERT);
 }
 
 struct AcaArgs {
@@ -493,7 +438,6 @@ struct AcaArgs {
     int ldr;    // shared row-buffer stride, pad4(3 max_nc)
     int kcap;   // 3 x the largest rank cap
     int max_nr;
-    int recompress_max;   // recompress factors of at most this many columns (0: never)
 };
 
 inline size_t aca_smem_bytes(int max_nr, int max_nc, int max_pivots) {
@@ -529,14 +473,7 @@ __global__ void __launch_bounds__(ACA_THREADS, 2) aca_kernel(AcaArgs a, Geo g, Q
 
     const int ns_r = min(ACA_SAMPLE, nr), ns_c = min(ACA_SAMPLE, nc);
     const int nc_r = min(ACA_CERT, nr), nc_c = min(ACA_CERT, nc);
-    if (t == 0) {
-        uint64_t st = a.seed ^ (0xD1B54A32D192ED03ull * (uint64_t)(a.first_index + blk + 1));
-        splitmix(st);
-        draw_distinct(st, nr, ns_r, lines);
-        draw_distinct(st, nc, ns_c, lines + ACA_SAMPLE);
-        draw_distinct(st, nr, nc_r, lines + 2 * ACA_SAMPLE);
-        draw_distinct(st, nc, nc_c, lines + 2 * ACA_SAMPLE + ACA_CERT);
-    }
+    if (t == 0) draw_lines(a.seed, a.first_index + blk, nr, nc, lines);
     __syncthreads();
 
     // exact sample
@@ -553,7 +490,7 @@ __global__ void __launch_bounds__(ACA_THREADS, 2) aca_kernel(AcaArgs a, Geo g, Q
     }
     const double snorm2 = block_sum(part, red_d);
 
-    int status = MBEM_ACA_FAILED, rank_out = 0, sweeps = 0;
+    int status = MBEM_ACA_FAILED, rank_out = 0;
     float err_out = 0.0f;
     bool retried = false;
     double tol = a.tol;
@@ -683,10 +620,6 @@ __global__ void __launch_bounds__(ACA_THREADS, 2) aca_kernel(AcaArgs a, Geo g, Q
             status = MBEM_ACA_CAPPED;
             break;
         }
-        if (K >= 2 && K <= a.recompress_max) {
-            __syncthreads();
-            K = recompress(U, ldu, 3 * nr, V, ldv, 3 * nc, K, 0.5 * tol, R, (int*)(R + K), &rp, &sweeps);
-        }
         // certificate: 3 exact element rows and 3 exact element columns
         float dr = 0.0f, er = 0.0f, dc = 0.0f, ec = 0.0f;   // per thread (FP32); summed in FP64 below
         for (int q = 0; q < nc_r; q++) {
@@ -772,8 +705,271 @@ __global__ void __launch_bounds__(ACA_THREADS, 2) aca_kernel(AcaArgs a, Geo g, Q
     }
     if (t == 0) {
         a.rank[blk] = status == MBEM_ACA_LOWRANK ? rank_out : 0;
-        a.status[blk] = status | (retried ? MBEM_ACA_RETRIED : 0) | (sweeps << 8);
+        a.status[blk] = status | (retried ? MBEM_ACA_RETRIED : 0);
         a.err[blk] = err_out;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// recompression (aca.py:422-438): the SVD of U V^T truncated at tol by its
+// K x K core. Grams Gu = U^T U, Gv = V^T V in double-float (exact FP32
+// products, compensated sums), Cholesky Gu + d = Ru^T Ru, Gv + d = Rv^T Rv in
+// FP64 (d = 1e-12 of the largest diagonal entry), C = Ru Rv^T, one-sided
+// Jacobi on C's columns in FP32: C Y = X S. Keeping k singular values,
+// U' = U (Rv^T Y_k) and V' = V (Ru^T (C Y)_k S_k^-2), which equal
+// Qu X_k S_k and Qv Y_k with no triangular solve. The kept factors are then
+// certified on the block's own certificate lines; a block whose certificate
+// exceeds 3 tol keeps its cross-approximation factors.
+// ---------------------------------------------------------------------------
+constexpr int RC_KMAX = 64;
+
+struct RcArgs {
+    const int32_t* r0;
+    const int32_t* nr;
+    const int32_t* c0;
+    const int32_t* nc;
+    const int32_t* rank;
+    const int64_t* u_off;
+    const int64_t* v_off;
+    const float* U;
+    const float* V;
+    const int64_t* ur_off;
+    const int64_t* vr_off;
+    float* Ur;
+    float* Vr;
+    int32_t* rank_out;
+    float* err_out;
+    const int64_t* index;
+    double tol;
+    uint64_t seed;
+    int kmax;
+};
+
+inline size_t rc_smem_bytes(int kmax) {
+    const size_t k2 = (size_t)kmax * kmax;
+    return 2 * k2 * sizeof(double) + 4 * k2 * sizeof(float) + 3 * (size_t)kmax * sizeof(float) + 64;
+}
+
+// G[i][j] = sum_r A[i][r] A[j][r] (K rows of length len at stride ld), one warp
+// a pair, exact products summed in double-float per lane, then in FP64
+__device__ void rc_gram(const float* __restrict__ A, int64_t ld, int len, int K, double* G) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int np = K * (K + 1) / 2;
+    for (int p = warp; p < np; p += nw) {
+        int i = 0, rem = p;
+        while (rem >= K - i) {
+            rem -= K - i;
+            i++;
+        }
+        const int j = i + rem;
+        const float* ai = A + (int64_t)i * ld;
+        const float* aj = A + (int64_t)j * ld;
+        float sh = 0.0f, sl = 0.0f;
+        for (int r = lane; r < len; r += 32) {
+            const float x = ai[r], y = aj[r];
+            const float pr = __fmul_rn(x, y);
+            const float pe = __fmaf_rn(x, y, -pr);
+            const float sn = __fadd_rn(sh, pr);
+            const float bb = __fsub_rn(sn, sh);
+            sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(__fsub_rn(sh, __fsub_rn(sn, bb)), __fsub_rn(pr, bb)), pe));
+            sh = sn;
+        }
+        double v = (double)sh + (double)sl;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) {
+            G[i * K + j] = v;
+            G[j * K + i] = v;
+        }
+    }
+}
+
+// In place, the upper Cholesky factor R (R^T R = G + d I) of a K x K FP64 matrix
+// (row-major; the strict lower part is left undefined)
+__device__ void rc_cholesky(double* G, int K) {
+    __shared__ double piv;
+    double dmax = 0.0;
+    for (int i = 0; i < K; i++) dmax = fmax(dmax, G[i * K + i]);
+    const double d = 1e-12 * dmax + 1e-300;
+    for (int k = 0; k < K; k++) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const double g = G[k * K + k] + d;
+            piv = g > 0.0 ? sqrt(g) : sqrt(d);
+            G[k * K + k] = piv;
+        }
+        __syncthreads();
+        const double ip = 1.0 / piv;
+        for (int j = k + 1 + threadIdx.x; j < K; j += blockDim.x) G[k * K + j] *= ip;
+        __syncthreads();
+        // trailing update of the upper part: G[i][j] -= R[k][i] R[k][j], k < i <= j
+        const int m = K - k - 1;
+        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+            const int i = k + 1 + e / m, j = k + 1 + e % m;
+            if (j >= i) G[i * K + j] -= G[k * K + i] * G[k * K + j];
+        }
+    }
+    __syncthreads();
+}
+
+template <bool TK>
+__global__ void __launch_bounds__(ACA_THREADS) rc_kernel(RcArgs a, Geo g, QuadRules Q) {
+    extern __shared__ __align__(16) float rsmf[];
+    double* rsm = reinterpret_cast<double*>(rsmf);
+    __shared__ int lines[2 * ACA_SAMPLE + 2 * ACA_CERT];
+    __shared__ int flag;
+    __shared__ double red_d[ACA_WARPS];
+    const int64_t blk = blockIdx.x;
+    const int t = threadIdx.x;
+    const int K = a.rank[blk];
+    if (K < 2 || K > a.kmax) {
+        if (t == 0) {
+            a.rank_out[blk] = 0;
+            a.err_out[blk] = 0.0f;
+        }
+        return;
+    }
+    const int r0 = a.r0[blk], nr = a.nr[blk], c0 = a.c0[blk], nc = a.nc[blk];
+    const int la = 3 * nr, lb = 3 * nc, ldu = pad4(la), ldv = pad4(lb);
+    const int KX = a.kmax;
+    double* Gu = rsm;
+    double* Gv = Gu + KX * KX;
+    float* Ct = (float*)(Gv + KX * KX);     // row i: column i of C (then of C Y)
+    float* Yt = Ct + KX * KX;               // row i: column i of Y
+    float* Cu = Yt + KX * KX;               // K x k, row-major at stride K
+    float* Cv = Cu + KX * KX;
+    float* sig = Cv + KX * KX;              // 3 K words
+    int* rk = (int*)(sig + K);
+    const float* U = a.U + a.u_off[blk];
+    const float* V = a.V + a.v_off[blk];
+    rc_gram(U, ldu, la, K, Gu);
+    rc_gram(V, ldv, lb, K, Gv);
+    __syncthreads();
+    rc_cholesky(Gu, K);
+    rc_cholesky(Gv, K);
+    // C = Ru Rv^T: C[i][j] = sum_{l >= max(i, j)} Ru[i][l] Rv[j][l]; stored as Ct[j][i]
+    for (int e = t; e < K * K; e += blockDim.x) {
+        const int i = e / K, j = e % K;
+        double v = 0.0;
+        for (int l = max(i, j); l < K; l++) v += Gu[i * K + l] * Gv[j * K + l];
+        Ct[j * K + i] = (float)v;
+        Yt[j * K + i] = i == j ? 1.0f : 0.0f;
+    }
+    __syncthreads();
+    osj_sweeps(Ct, K, K, Yt, K, K, K, &flag);
+    for (int k = t >> 5; k < K; k += ACA_WARPS) {
+        const double d = sqrt(row_norm2(Ct, K, K, k));
+        if ((t & 31) == 0) sig[k] = (float)d;
+    }
+    __syncthreads();
+    for (int j = t; j < K; j += blockDim.x) {
+        int r = 0;
+        const float sj = sig[j];
+        for (int i = 0; i < K; i++) r += (sig[i] > sj || (sig[i] == sj && i < j)) ? 1 : 0;
+        rk[j] = r;
+    }
+    __syncthreads();
+    float* srt = sig + 2 * K;
+    for (int j = t; j < K; j += blockDim.x) srt[rk[j]] = sig[j];
+    __syncthreads();
+    if (t == 0) {
+        const double s0 = srt[0], tl = 0.5 * a.tol;
+        double dropped = 0.0;
+        int keep = K;
+        for (int r = K - 1; r >= 1; r--) {
+            const double sr = srt[r];
+            if (dropped + sr * sr > tl * tl * s0 * s0) break;
+            dropped += sr * sr;
+            keep = r;
+        }
+        flag = keep;
+    }
+    __syncthreads();
+    const int kk = flag;
+    // Cu[:, q] = Rv^T y_j and Cv[:, q] = Ru^T (C y)_j / s_j^2 for the kept j (q its rank)
+    for (int e = t; e < K * K; e += blockDim.x) {
+        const int i = e / K, j = e % K;
+        const int q = rk[j];
+        if (q >= kk) continue;
+        double cu = 0.0, cv = 0.0;
+        for (int l = 0; l <= i; l++) {
+            cu += Gv[l * K + i] * (double)Yt[j * K + l];
+            cv += Gu[l * K + i] * (double)Ct[j * K + l];
+        }
+        const double sj = sig[j];
+        Cu[i * K + q] = (float)cu;
+        Cv[i * K + q] = sj > 0.0 ? (float)(cv / (sj * sj)) : 0.0f;
+    }
+    __syncthreads();
+    // U'^T[q][r] = sum_i U^T[i][r] Cu[i][q]; likewise V'
+    float* Ur = a.Ur + a.ur_off[blk];
+    float* Vr = a.Vr + a.vr_off[blk];
+    for (int r = t; r < ldu; r += blockDim.x) {
+        for (int q = 0; q < kk; q++) {
+            float acc = 0.0f;
+            if (r < la)
+                for (int i = 0; i < K; i++) acc += U[(int64_t)i * ldu + r] * Cu[i * K + q];
+            Ur[(int64_t)q * ldu + r] = acc;
+        }
+    }
+    for (int r = t; r < ldv; r += blockDim.x) {
+        for (int q = 0; q < kk; q++) {
+            float acc = 0.0f;
+            if (r < lb)
+                for (int i = 0; i < K; i++) acc += V[(int64_t)i * ldv + r] * Cv[i * K + q];
+            Vr[(int64_t)q * ldv + r] = acc;
+        }
+    }
+    // certificate of the new factors on the block's certificate lines
+    if (t == 0) draw_lines(a.seed, a.index[blk], nr, nc, lines);
+    __syncthreads();
+    float dr = 0.0f, er = 0.0f;
+    const int nc_r = min(ACA_CERT, nr), nc_c = min(ACA_CERT, nc);
+    for (int q = 0; q < nc_r; q++) {
+        const int i = lines[2 * ACA_SAMPLE + q];
+        for (int j = t; j < nc; j += blockDim.x) {
+            float e[3][3], ap[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            pair_eval<TK>(g, Q, r0 + i, c0 + j, e);
+            for (int k = 0; k < kk; k++) {
+                const float* vk = Vr + (int64_t)k * ldv + 3 * j;
+                const float* uk = Ur + (int64_t)k * ldu + 3 * i;
+                for (int aa = 0; aa < 3; aa++)
+                    for (int bb = 0; bb < 3; bb++) ap[aa][bb] += uk[aa] * vk[bb];
+            }
+            for (int aa = 0; aa < 3; aa++)
+                for (int bb = 0; bb < 3; bb++) {
+                    const float df = ap[aa][bb] - e[aa][bb];
+                    dr += df * df;
+                    er += e[aa][bb] * e[aa][bb];
+                }
+        }
+    }
+    float dc = 0.0f, ec = 0.0f;
+    for (int q = 0; q < nc_c; q++) {
+        const int j = lines[2 * ACA_SAMPLE + ACA_CERT + q];
+        for (int i = t; i < nr; i += blockDim.x) {
+            float e[3][3], ap[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            pair_eval<TK>(g, Q, r0 + i, c0 + j, e);
+            for (int k = 0; k < kk; k++) {
+                const float* vk = Vr + (int64_t)k * ldv + 3 * j;
+                const float* uk = Ur + (int64_t)k * ldu + 3 * i;
+                for (int aa = 0; aa < 3; aa++)
+                    for (int bb = 0; bb < 3; bb++) ap[aa][bb] += uk[aa] * vk[bb];
+            }
+            for (int aa = 0; aa < 3; aa++)
+                for (int bb = 0; bb < 3; bb++) {
+                    const float df = ap[aa][bb] - e[aa][bb];
+                    dc += df * df;
+                    ec += e[aa][bb] * e[aa][bb];
+                }
+        }
+    }
+    const double sdr = block_sum(dr, red_d), ser = block_sum(er, red_d);
+    const double sdc = block_sum(dc, red_d), sec = block_sum(ec, red_d);
+    const double err = fmax(ser > 0.0 ? sqrt(sdr / ser) : 0.0, sec > 0.0 ? sqrt(sdc / sec) : 0.0);
+    if (t == 0) {
+        const bool ok = err <= ACA_CERT_FACTOR * a.tol;
+        a.rank_out[blk] = ok ? kk : 0;
+        a.err_out[blk] = (float)err;
     }
 }
 
@@ -1075,7 +1271,6 @@ int mbem_aca_compress(const mbem_pair_geometry* g, const mbem_aca_batch* b, void
     a.ldr = pad4(3 * b->max_nc);
     a.kcap = 3 * b->max_pivots_all;
     a.max_nr = b->max_nr;
-    a.recompress_max = b->recompress_max;
     const Geo G = make_geo(g);
     cudaStream_t st = (cudaStream_t)stream;
     if (g->kernel == 0) {
@@ -1088,6 +1283,52 @@ int mbem_aca_compress(const mbem_pair_geometry* g, const mbem_aca_batch* b, void
         aca_kernel<false><<<(unsigned)b->n_blocks, ACA_THREADS, smem, st>>>(a, G, rules());
     }
     return launch_status("aca_kernel");
+}
+
+int mbem_aca_recompress(const mbem_pair_geometry* g, const mbem_aca_recompression* r, void* stream) {
+    int rc = check_geometry(g);
+    if (rc) return rc;
+    MBEM_REQUIRE(r && r->n_blocks >= 0, MBEM_ERR_ARG, "recompress: bad arguments");
+    if (r->n_blocks == 0) return MBEM_OK;
+    MBEM_REQUIRE(r->r0 && r->nr && r->c0 && r->nc && r->rank && r->u_off && r->v_off && r->U && r->V && r->ur_off &&
+                     r->vr_off && r->Ur && r->Vr && r->rank_out && r->err_out && r->index,
+                 MBEM_ERR_ARG, "recompress: null pointer");
+    MBEM_REQUIRE(r->max_rank >= 2 && r->max_rank <= RC_KMAX, MBEM_ERR_SIZE, "recompress: max_rank must be in [2, %d]",
+                 RC_KMAX);
+    MBEM_REQUIRE(r->tol > 0.0, MBEM_ERR_ARG, "recompress: tolerance must be positive");
+    RcArgs a;
+    a.r0 = r->r0;
+    a.nr = r->nr;
+    a.c0 = r->c0;
+    a.nc = r->nc;
+    a.rank = r->rank;
+    a.u_off = r->u_off;
+    a.v_off = r->v_off;
+    a.U = r->U;
+    a.V = r->V;
+    a.ur_off = r->ur_off;
+    a.vr_off = r->vr_off;
+    a.Ur = r->Ur;
+    a.Vr = r->Vr;
+    a.rank_out = r->rank_out;
+    a.err_out = r->err_out;
+    a.index = r->index;
+    a.tol = r->tol;
+    a.seed = r->seed;
+    a.kmax = r->max_rank;
+    const size_t smem = rc_smem_bytes(r->max_rank);
+    const Geo G = make_geo(g);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (g->kernel == 0) {
+        rc = set_smem((const void*)rc_kernel<true>, smem);
+        if (rc) return rc;
+        rc_kernel<true><<<(unsigned)r->n_blocks, ACA_THREADS, smem, st>>>(a, G, rules());
+    } else {
+        rc = set_smem((const void*)rc_kernel<false>, smem);
+        if (rc) return rc;
+        rc_kernel<false><<<(unsigned)r->n_blocks, ACA_THREADS, smem, st>>>(a, G, rules());
+    }
+    return launch_status("rc_kernel");
 }
 
 int mbem_aca_compact(int64_t n_blocks, const int32_t* nr, const int32_t* nc, const int32_t* rank,

@@ -69,7 +69,7 @@ ACA_CERTIFY_LINES = 3                  # exact element rows and columns of the c
 ACA_CERTIFY_FACTOR = 3.0               # certificate limit, times the tolerance
 ACA_RETRY_TOL_FACTOR = 10.0            # a failed certificate reruns the block at tol / this
 ACA_SEED = 12345                       # seed of the sample and certificate lines
-ACA_RECOMPRESS_MAX = 0                 # recompress factors of at most this many columns (0: off; see PairCompressed)
+ACA_RECOMPRESS_MAX = 64                # recompress factors of at most this many columns (0: off)
 COMPRESSED_NEAR_RADIUS_FACTOR = MIXED_NEAR_RADIUS_FACTOR   # FP64 closed form inside this radius
 COMPRESSED_SCRATCH_BYTES = 4 << 30     # cross-approximation scratch per batch of blocks
 COMPRESSED_VIEW_CACHE = 4              # material views kept per pair operator

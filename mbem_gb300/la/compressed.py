@@ -361,6 +361,10 @@ class PairCompressed:
                  near_factor: float = defaults.COMPRESSED_NEAR_RADIUS_FACTOR,
                  scratch_bytes: int = defaults.COMPRESSED_SCRATCH_BYTES,
                  recompress_max: int = defaults.ACA_RECOMPRESS_MAX):
+        """``recompress_max``: factors of 2 .. recompress_max columns (at most
+        64) are recompressed (the SVD of U V^T truncated at tol / 2, as
+        aca.py:422-438 does) and kept when their certificate holds; 0 keeps
+        the cross approximation's own factors."""
         self.n_basis = kernel_n_basis(kernel)          # raises on a traction kernel
         if kernel not in (KERNEL_T, KERNEL_U):
             raise ValueError(f"unknown kernel {kernel!r}")
@@ -459,15 +463,16 @@ class PairCompressed:
 
     def _compress(self, g, v: _View):
         """Cross approximation of every admissible block, in batches whose
-        scratch fits ``scratch_bytes``; returns per block (status, rank, err)
-        and the compacted factors with their offsets."""
+        scratch fits ``scratch_bytes``, then the recompression of its factors;
+        returns per block (status, rank, err), the compacted factors with
+        their offsets, and the count of blocks recompressed."""
         r0, nr, c0, nc = self._adm_ranges
         n = r0.size
         status = np.zeros(n, np.int32)
         rank = np.zeros(n, np.int32)
         err = np.zeros(n, np.float32)
         if n == 0:
-            return status, rank, err, None, None, np.zeros(0, np.int64), np.zeros(0, np.int64)
+            return status, rank, err, None, None, np.zeros(0, np.int64), np.zeros(0, np.int64), 0
         cap = rank_caps(nr, nc)
         ldu, ldv = _pad4(3 * nr), _pad4(3 * nc)
         cap_floats = 3 * cap.astype(np.int64) * (ldu + ldv)
@@ -478,6 +483,7 @@ class PairCompressed:
         u_fin = np.zeros(n, np.int64)
         v_fin = np.zeros(n, np.int64)
         u_base = v_base = 0
+        n_rc = 0
         lo = 0
         while lo < n:
             hi = lo + 1
@@ -506,16 +512,58 @@ class PairCompressed:
             b.first_index = lo
             b.max_nr, b.max_nc = int(nr[sl].max()), int(nc[sl].max())
             b.max_pivots_all = int(cap[sl].max())
-            b.recompress_max = self.recompress_max
             nat.call("mbem_aca_compress", ctypes.byref(g), ctypes.byref(b), st)
             rank[sl], status[sl], err[sl] = rk.cpu().numpy(), stt.cpu().numpy(), er.cpu().numpy()
+            rb = rank[sl].astype(np.int64)
+            # recompression of the converged factors (their K x K core), kept when
+            # its certificate holds; the rest keep the cross approximation's
+            kmax = min(self.recompress_max, nat.RC_KMAX)
+            elig = np.flatnonzero(((status[sl] & 3) == nat.ACA_LOWRANK) & (rb >= 2) & (rb <= kmax)) \
+                if kmax >= 2 else np.zeros(0, np.int64)
+            rc_rank = np.zeros(hi - lo, np.int32)
+            Ur = Vr = None
+            if elig.size:
+                ucap_r = rb[elig] * ldu[sl][elig]
+                vcap_r = rb[elig] * ldv[sl][elig]
+                Ur = torch.empty(max(4, int(ucap_r.sum())), dtype=torch.float32, device=dev)
+                Vr = torch.empty(max(4, int(vcap_r.sum())), dtype=torch.float32, device=dev)
+                ro = torch.zeros(elig.size, dtype=torch.int32, device=dev)
+                re_ = torch.zeros(elig.size, dtype=torch.float32, device=dev)
+                r = nat.AcaRecompression()
+                r.n_blocks = int(elig.size)
+                r.r0, r.nr = _i32(tmp, r0[sl][elig]), _i32(tmp, nr[sl][elig])
+                r.c0, r.nc = _i32(tmp, c0[sl][elig]), _i32(tmp, nc[sl][elig])
+                r.rank = _i32(tmp, rb[elig])
+                r.u_off, r.v_off = _i64(tmp, _exclusive(ucap)[elig]), _i64(tmp, _exclusive(vcap)[elig])
+                r.U, r.V = ptr(U), ptr(V)
+                r.ur_off, r.vr_off = _i64(tmp, _exclusive(ucap_r)), _i64(tmp, _exclusive(vcap_r))
+                r.Ur, r.Vr = ptr(Ur), ptr(Vr)
+                r.rank_out, r.err_out = ptr(ro), ptr(re_)
+                r.index = _i64(tmp, lo + elig)
+                r.tol = self.tol
+                r.seed = self.seed
+                r.max_rank = int(rb[elig].max())
+                nat.call("mbem_aca_recompress", ctypes.byref(g), ctypes.byref(r), st)
+                ok = ro.cpu().numpy()
+                got = ok > 0
+                rc_rank[elig[got]] = ok[got]
+                err[lo + elig[got]] = re_.cpu().numpy()[got]
+                rank[lo + elig[got]] = ok[got]
+                rc_src_u, rc_src_v = np.zeros(hi - lo, np.int64), np.zeros(hi - lo, np.int64)
+                rc_src_u[elig], rc_src_v[elig] = _exclusive(ucap_r), _exclusive(vcap_r)
             usz = rank[sl].astype(np.int64) * ldu[sl]
             vsz = rank[sl].astype(np.int64) * ldv[sl]
             Uc = torch.empty(max(4, int(usz.sum())), dtype=torch.float32, device=dev)
             Vc = torch.empty(max(4, int(vsz.sum())), dtype=torch.float32, device=dev)
             ud, vd = _exclusive(usz), _exclusive(vsz)
-            nat.call("mbem_aca_compact", hi - lo, b.nr, b.nc, ptr(rk), b.u_off, b.v_off, ptr(U), ptr(V),
-                     _i64(tmp, ud), _i64(tmp, vd), ptr(Uc), ptr(Vc), st)
+            raw_rank = np.where(rc_rank > 0, 0, rank[sl]).astype(np.int32)
+            dst_u, dst_v = _i64(tmp, ud), _i64(tmp, vd)
+            nat.call("mbem_aca_compact", hi - lo, b.nr, b.nc, _i32(tmp, raw_rank), b.u_off, b.v_off, ptr(U), ptr(V),
+                     dst_u, dst_v, ptr(Uc), ptr(Vc), st)
+            if Ur is not None and (rc_rank > 0).any():
+                nat.call("mbem_aca_compact", hi - lo, b.nr, b.nc, _i32(tmp, rc_rank), _i64(tmp, rc_src_u),
+                         _i64(tmp, rc_src_v), ptr(Ur), ptr(Vr), dst_u, dst_v, ptr(Uc), ptr(Vc), st)
+            n_rc += int((rc_rank > 0).sum())
             torch.cuda.current_stream().synchronize()
             u_fin[sl] = u_base + ud
             v_fin[sl] = v_base + vd
@@ -523,11 +571,11 @@ class PairCompressed:
             v_base += Vc.numel()
             Us.append(Uc)
             Vs.append(Vc)
-            del U, V, tmp
+            del U, V, Ur, Vr, tmp
             lo = hi
         U = torch.cat(Us) if len(Us) > 1 else Us[0]
         V = torch.cat(Vs) if len(Vs) > 1 else Vs[0]
-        return status, rank, err, U, V, u_fin, v_fin
+        return status, rank, err, U, V, u_fin, v_fin, n_rc
 
     def _build_view(self, c: np.ndarray) -> _View:
         v = _View()
@@ -535,7 +583,7 @@ class PairCompressed:
         t0 = time.perf_counter()
         g = self._geometry(c, v.keep)
         t1 = time.perf_counter()
-        status, rank, err, U, V, u_off, v_off = self._compress(g, v)
+        status, rank, err, U, V, u_off, v_off, n_rc = self._compress(g, v)
         sync()
         t2 = time.perf_counter()
         low = (status & 3) == nat.ACA_LOWRANK
@@ -603,10 +651,10 @@ class PairCompressed:
             "n_capped": int(((status & 3) == nat.ACA_CAPPED).sum()),
             "n_retry": int(((status & nat.ACA_RETRIED) != 0).sum()),
             "n_fallback": int(((status & 3) == nat.ACA_FAILED).sum()),
+            "n_recompressed": n_rc,
             "max_verified_err": float(err[low].max()) if low.any() else 0.0,
             "ranks": lr_rank.copy(),
             "status": status & 7,
-            "jacobi_sweeps": np.stack([(status >> 8) & 255, (status >> 16) & 255], axis=1),
             "err": err.copy(),
             "lowrank_bytes": lr_bytes,
             "dense_bytes": 4 * total,

@@ -87,6 +87,10 @@ def test_matches_the_reference_operator(golden_pair, kernel):
           f"{err_ref_exact:.2e}; {pc.summary()}")
     assert err_ref < TOL and err_exact < TOL
     assert pc.max_verified_err <= 3 * TOL
+    # recompressed, the factors' ranks are the reference's to within a quarter
+    ranks = pc.view_stats(c)["ranks"]
+    print(f"{kernel}: mean rank {ranks.mean():.1f} against the reference's {g[f'{kernel}_ranks'].mean():.1f}")
+    assert ranks.mean() <= 1.25 * g[f"{kernel}_ranks"].mean()
     lr, ex, _ = _block_errors(pc, c, A)
     assert lr.size > 0 and lr.max() < 3 * 3 * TOL
     assert ex.max() < 1e-6
@@ -129,6 +133,27 @@ def test_product_matches_the_c_port_on_the_same_factors(oracle):
     y = pc.matvec(c, x)
     y_port = oracle.flat_matvec(pc.view_host(c), x)
     assert np.linalg.norm(y - y_port) / np.linalg.norm(y_port) < 1e-6
+
+
+def test_recompression_keeps_the_operator():
+    """With and without the recompression of the cross approximation's
+    factors: the same operator to the tolerance, fewer factor columns."""
+    from mbem_gb300 import mesh
+    from mbem_gb300.kernels import basis as kb
+    from mbem_gb300.la.compressed import PairCompressed
+    cube = mesh.cube(16)
+    c = kb.t_coeffs(1.0, 1.0)
+    raw = PairCompressed(cube, cube, "H", 0.125, recompress_max=0)
+    rec = PairCompressed(cube, cube, "H", 0.125)
+    x = np.random.default_rng(9).normal(size=3 * cube.n_triangles)
+    ye = _exact("H", cube, cube, 0.125, c) @ x
+    for pc in (raw, rec):
+        y = pc.matvec(c, x)
+        assert np.linalg.norm(y - ye) / np.linalg.norm(ye) < TOL
+    sr, sw = rec.view_stats(c), raw.view_stats(c)
+    assert sr["n_recompressed"] > 0 and sw["n_recompressed"] == 0
+    assert sr["ranks"].sum() < sw["ranks"].sum()
+    assert sr["max_verified_err"] <= 3 * TOL
 
 
 def test_tight_tolerance_leaves_blocks_exact():
