@@ -105,15 +105,20 @@ struct SrcFar {
 };
 
 // Edges as exact FP64 differences rounded to FP32, the centroid in
-// double-float; everything else in FP32 (the FP64 pipe runs 1/64 of FP32 here,
-// and every CTA of the far-field kernels sets up its sources).
+// double-float, twice the area in FP64 (it scales every entry of the source:
+// an FP32 cross product would bias each source's column by ~1e-7); the
+// lengths and radii, which only choose rules and near pairs, in FP32 (the FP64
+// pipe runs 1/64 of FP32 here, and every CTA of the far-field kernels sets up
+// its sources).
 __device__ __forceinline__ void far_setup(const double* __restrict__ tv, const double* __restrict__ nrm,
                                           double eps, double near_factor, SrcFar& s) {
-    const float e1x = (float)(tv[3] - tv[0]), e1y = (float)(tv[4] - tv[1]), e1z = (float)(tv[5] - tv[2]);
-    const float e2x = (float)(tv[6] - tv[0]), e2y = (float)(tv[7] - tv[1]), e2z = (float)(tv[8] - tv[2]);
+    const double d1x = tv[3] - tv[0], d1y = tv[4] - tv[1], d1z = tv[5] - tv[2];
+    const double d2x = tv[6] - tv[0], d2y = tv[7] - tv[1], d2z = tv[8] - tv[2];
+    const double cx = d1y * d2z - d1z * d2y, cy = d1z * d2x - d1x * d2z, cz = d1x * d2y - d1y * d2x;
+    const float a2 = (float)sqrt(cx * cx + cy * cy + cz * cz);
+    const float e1x = (float)d1x, e1y = (float)d1y, e1z = (float)d1z;
+    const float e2x = (float)d2x, e2y = (float)d2y, e2z = (float)d2z;
     const float e3x = (float)(tv[6] - tv[3]), e3y = (float)(tv[7] - tv[4]), e3z = (float)(tv[8] - tv[5]);
-    const float cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
-    const float a2 = sqrtf(cx * cx + cy * cy + cz * cz);
     s.ok = a2 >= 1e-30f;
     const float l1 = sqrtf(e1x * e1x + e1y * e1y + e1z * e1z);
     const float l2 = sqrtf(e2x * e2x + e2y * e2y + e2z * e2z);
