@@ -871,6 +871,9 @@ typedef struct {
     const int64_t* unit_ptr;      /* (n_strips + 1) */
     const int32_t* unit_item;
     const int32_t* unit_k0;
+    int64_t n_proj;               /* the projections w_i = V_i^T x in units of four factor rows: */
+    const int32_t* proj_block;    /*   unit u = rows proj_k0[u] .. +3 of low-rank block proj_block[u] */
+    const int32_t* proj_k0;
 } mbem_compressed_view;
 size_t mbem_compressed_matvec_workspace_size(const mbem_compressed_view* v);
 /* y (3 n_field, original element order) = A x (3 n_src); FP32 factors and

@@ -127,7 +127,8 @@ class CompressedView(Structure):
                 ("d_r0", c_void_p), ("d_nr", c_void_p), ("d_c0", c_void_p), ("d_nc", c_void_p),
                 ("d_off", c_void_p), ("D", c_void_p), ("n_strips", c_int64), ("strip_r0", c_void_p),
                 ("strip_nr", c_void_p), ("strip_ptr", c_void_p), ("strip_items", c_void_p), ("max_strip", c_int),
-                ("max_lr_nc", c_int), ("unit_ptr", c_void_p), ("unit_item", c_void_p), ("unit_k0", c_void_p)]
+                ("max_lr_nc", c_int), ("unit_ptr", c_void_p), ("unit_item", c_void_p), ("unit_k0", c_void_p),
+                ("n_proj", c_int64), ("proj_block", c_void_p), ("proj_k0", c_void_p)]
 
 
 COMPRESSED_UNIT = 32

@@ -1047,39 +1047,41 @@ __global__ void cm_gather_kernel(const double* __restrict__ x, const int64_t* __
     }
 }
 
-// w_i = V_i^T x[cols_i] for every low-rank block: one CTA a block, each warp
-// four factor rows at a time (four 16-byte loads in flight a lane)
+// w_i = V_i^T x[cols_i] for every low-rank block: one warp a unit of four
+// factor rows of one block (proj_block / proj_k0), so that a block of many
+// rows is shared among many warps and a small one takes one; 16-byte loads of
+// V, x from the gathered vector (L1/L2-resident), the padding columns of V
+// (zeros) against zeros
 __global__ void __launch_bounds__(CM_THREADS) cm_project_kernel(mbem_compressed_view v, const float* __restrict__ xs,
                                                                 float* __restrict__ w) {
-    extern __shared__ __align__(16) float xseg[];
-    const int64_t i = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t u = (int64_t)blockIdx.x * CM_WARPS + warp;
+    if (u >= v.n_proj) return;
+    const int64_t i = v.proj_block[u];
+    const int k0 = v.proj_k0[u];
     const int nc3 = 3 * v.lr_nc[i], ldv = pad4(nc3), K = v.lr_rank[i];
     const float* xsrc = xs + 3 * (int64_t)v.lr_c0[i];
-    for (int c = threadIdx.x; c < ldv; c += CM_THREADS) xseg[c] = c < nc3 ? xsrc[c] : 0.0f;
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const float4* x4 = (const float4*)xseg;
     const float* V = v.V + v.lr_v[i];
     const int n4 = ldv / 4;
-    for (int k0 = 4 * warp; k0 < K; k0 += 4 * CM_WARPS) {
-        const int nk = min(4, K - k0);
-        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        for (int q = lane; q < n4; q += 32) {
-            const float4 b = x4[q];
-#pragma unroll
-            for (int m = 0; m < 4; m++) {
-                if (m < nk) {
-                    const float4 a = __ldg((const float4*)(V + (int64_t)(k0 + m) * ldv) + q);
-                    acc[m] += a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
-                }
-            }
-        }
+    const int nk = min(4, K - k0);
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int q = lane; q < n4; q += 32) {
+        const int c = 4 * q;
+        const float b0 = xsrc[c], b1 = c + 1 < nc3 ? xsrc[c + 1] : 0.0f;
+        const float b2 = c + 2 < nc3 ? xsrc[c + 2] : 0.0f, b3 = c + 3 < nc3 ? xsrc[c + 3] : 0.0f;
 #pragma unroll
         for (int m = 0; m < 4; m++) {
-            float t = acc[m];
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-            if (lane == 0 && m < nk) w[v.lr_w[i] + k0 + m] = t;
+            if (m < nk) {
+                const float4 a = __ldg((const float4*)(V + (int64_t)(k0 + m) * ldv) + q);
+                acc[m] += a.x * b0 + a.y * b1 + a.z * b2 + a.w * b3;
+            }
         }
+    }
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        float t = acc[m];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0 && m < nk) w[v.lr_w[i] + k0 + m] = t;
     }
 }
 
@@ -1386,8 +1388,6 @@ int mbem_compressed_matvec(const mbem_compressed_view* v, const double* x, doubl
     MBEM_REQUIRE(v && x && y && work, MBEM_ERR_ARG, "compressed matvec: null pointer");
     MBEM_REQUIRE(work_bytes >= mbem_compressed_matvec_workspace_size(v), MBEM_ERR_SIZE,
                  "compressed matvec: workspace too small");
-    MBEM_REQUIRE((size_t)pad4(3 * v->max_lr_nc) * sizeof(float) <= 200 * 1024, MBEM_ERR_SIZE,
-                 "compressed matvec: block of %d source elements too large", v->max_lr_nc);
     MBEM_REQUIRE(((uintptr_t)v->V % 16) == 0 || v->n_lr == 0, MBEM_ERR_ARG,
                  "compressed matvec: V must be 16-byte aligned");
     cudaStream_t st = (cudaStream_t)stream;
@@ -1399,11 +1399,9 @@ int mbem_compressed_matvec(const mbem_compressed_view* v, const double* x, doubl
                                                                                           v->n_src, xs);
         n++;
     }
-    if (v->n_lr > 0) {
-        const size_t sm = (size_t)pad4(3 * v->max_lr_nc) * sizeof(float);
-        int rc = set_smem((const void*)cm_project_kernel, sm);
-        if (rc) return rc;
-        cm_project_kernel<<<(unsigned)v->n_lr, CM_THREADS, sm, st>>>(*v, xs, w);
+    if (v->n_proj > 0) {
+        MBEM_REQUIRE(v->proj_block && v->proj_k0, MBEM_ERR_ARG, "compressed matvec: no projection units");
+        cm_project_kernel<<<(unsigned)ceil_div(v->n_proj, CM_WARPS), CM_THREADS, 0, st>>>(*v, xs, w);
         n++;
     }
     if (v->n_strips > 0) {

@@ -640,6 +640,12 @@ class PairCompressed:
         uptr, uitem, uk0 = strip_units(sptr, sitems, item_rows)
         s.unit_ptr, s.unit_item, s.unit_k0 = _i64(v, uptr, "unit_ptr"), _i32(v, uitem, "unit_item"), \
             _i32(v, uk0, "unit_k0")
+        # projection units: four factor rows of one low-rank block each
+        npu = (lr_rank.astype(np.int64) + 3) // 4
+        s.n_proj = int(npu.sum())
+        pblk = np.repeat(np.arange(lr_rank.size), npu)
+        pk0 = (np.arange(s.n_proj) - np.repeat(np.cumsum(npu) - npu, npu)) * 4
+        s.proj_block, s.proj_k0 = _i32(v, pblk, "proj_block"), _i32(v, pk0, "proj_k0")
         s.max_lr_nc = int(nc[low].max()) if s.n_lr else 0
         v.work_bytes = int(nat.lib().mbem_compressed_matvec_workspace_size(ctypes.byref(s)))
         v.work = torch.empty(max(16, v.work_bytes), dtype=torch.uint8, device=self._x.device)
