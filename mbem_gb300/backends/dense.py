@@ -200,12 +200,10 @@ class AssembledDense:
         key = id(patch)
         v = self._arrays.get(key)
         if v is None:
-            tv = patch.tri_verts()
-            normals, _ = patch.mesh.normals_and_areas()
+            tv, normals, coll, coll_n = patch.geometry()
             eps_arr = kb.resolve_patch_eps(self.eps, patch)
             v = dict(tv=as_cuda(tv), normals=as_cuda(normals), eps=as_cuda(eps_arr),
-                     coll=as_cuda(patch.collocation_points()),
-                     coll_n=as_cuda(patch.collocation_normals()))
+                     coll=as_cuda(coll), coll_n=as_cuda(coll_n))
             self._arrays[key] = v
         return v
 

@@ -134,9 +134,14 @@ def as_eps_array(eps, n_source: int) -> np.ndarray:
 
 def element_sizes(mesh) -> np.ndarray:
     """(N_src,) size of each triangle: the mean of its three edge lengths."""
-    corners = np.take(np.asarray(mesh.vertices, float), np.asarray(mesh.triangles), axis=0)
-    edges = np.roll(corners, -1, axis=1) - corners
-    return np.sqrt((edges * edges).sum(axis=2)).mean(axis=1)
+    v = np.asarray(mesh.vertices, float)
+    t = np.asarray(mesh.triangles)
+    c0, c1, c2 = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
+
+    def length(e):
+        return np.sqrt(e[:, 0] * e[:, 0] + e[:, 1] * e[:, 1] + e[:, 2] * e[:, 2])
+
+    return (length(c1 - c0) + length(c2 - c1) + length(c0 - c2)) / 3.0
 
 
 def resolve_eps(eps, mesh) -> np.ndarray:

@@ -25,6 +25,7 @@ import numpy as np
 from .. import defaults
 from ..kernels.basis import lagrange_nodes, lagrange_shape
 from ..kernels.tri_nodal import n_nodes
+from ..mesh import centroids_of, normals_and_areas_of
 
 
 class BCType(enum.Enum):
@@ -87,10 +88,18 @@ class Patch:
         height over longest edge, 2 area / L_max^2, must exceed
         MIN_TRIANGLE_HEIGHT_OVER_L, or the kernels have no frame to integrate
         over and "auto" eps no size."""
-        corners = np.take(np.asarray(self.mesh.vertices, float), np.asarray(self.mesh.triangles), axis=0)
-        sides = np.roll(corners, -1, axis=1) - corners
-        longest2 = (sides * sides).sum(axis=2).max(axis=1)
-        twice_area = np.linalg.norm(np.cross(sides[:, 0], -sides[:, 2]), axis=1)
+        v = np.asarray(self.mesh.vertices, float)
+        t = np.asarray(self.mesh.triangles)
+        p0, p1, p2 = v[t[:, 0]], v[t[:, 1]], v[t[:, 2]]
+        e0, e1, e2 = p1 - p0, p2 - p1, p0 - p2
+        longest2 = np.maximum(np.maximum(np.einsum("ij,ij->i", e0, e0), np.einsum("ij,ij->i", e1, e1)),
+                              np.einsum("ij,ij->i", e2, e2))
+        # |e0 x (p2 - p0)| = twice the area
+        f = p2 - p0
+        cx = e0[:, 1] * f[:, 2] - e0[:, 2] * f[:, 1]
+        cy = e0[:, 2] * f[:, 0] - e0[:, 0] * f[:, 2]
+        cz = e0[:, 0] * f[:, 1] - e0[:, 1] * f[:, 0]
+        twice_area = np.sqrt(cx * cx + cy * cy + cz * cz)
         quality = twice_area / np.where(longest2 > 0.0, longest2, 1.0)
         limit = defaults.MIN_TRIANGLE_HEIGHT_OVER_L
         flat = np.flatnonzero(quality <= limit)
@@ -132,23 +141,32 @@ class Patch:
     def tri_verts(self) -> np.ndarray:
         return np.ascontiguousarray(np.asarray(self.mesh.vertices, float)[np.asarray(self.mesh.triangles)])
 
-    def _points(self, lam) -> np.ndarray:
-        return np.einsum("kv,svc->skc", lam, self.tri_verts()).reshape(-1, 3)
+    def _points(self, lam, tv=None) -> np.ndarray:
+        tv = self.tri_verts() if tv is None else tv
+        return np.einsum("kv,svc->skc", lam, tv).reshape(-1, 3)
 
-    def nodes(self) -> np.ndarray:
+    def nodes(self, tv=None) -> np.ndarray:
         if self.order == 0:
-            return np.asarray(self.mesh.centroids(), float)
-        return self._points(lagrange_nodes(self.order))
+            return centroids_of(self.tri_verts() if tv is None else tv)
+        return self._points(lagrange_nodes(self.order), tv)
 
-    def collocation_points(self) -> np.ndarray:
+    def collocation_points(self, tv=None) -> np.ndarray:
         t = defaults.COLLOCATION_SHRINK_BY_ORDER[self.order]
         if t == 0.0:
-            return self.nodes()
-        return self._points(lagrange_nodes(self.order, t))
+            return self.nodes(tv)
+        return self._points(lagrange_nodes(self.order, t), tv)
 
-    def collocation_normals(self) -> np.ndarray:
-        normals, _ = self.mesh.normals_and_areas()
+    def collocation_normals(self, normals=None) -> np.ndarray:
+        if normals is None:
+            normals, _ = self.mesh.normals_and_areas()
         return np.ascontiguousarray(np.repeat(np.asarray(normals, float), n_nodes(self.order), axis=0))
+
+    def geometry(self):
+        """(corners (n, 3, 3), unit normals (n, 3), collocation points,
+        collocation normals) from one gather of the corners."""
+        tv = self.tri_verts()
+        normals, _ = normals_and_areas_of(tv)
+        return tv, normals, self.collocation_points(tv), self.collocation_normals(normals)
 
     def collocation_shape(self) -> np.ndarray:
         t = defaults.COLLOCATION_SHRINK_BY_ORDER[self.order]
@@ -240,10 +258,16 @@ class Region:
 
 def solid_angle_sum(mesh, x) -> float:
     """Sum over the triangles of the van Oosterom signed solid angle seen from x."""
-    tv = np.asarray(mesh.vertices, float)[np.asarray(mesh.triangles)] - np.asarray(x, float)
-    r1, r2, r3 = tv[:, 0], tv[:, 1], tv[:, 2]
-    R1, R2, R3 = (np.linalg.norm(r, axis=1) for r in (r1, r2, r3))
-    numer = np.einsum("ij,ij->i", r1, np.cross(r2, r3))
+    rel = np.asarray(mesh.vertices, float) - np.asarray(x, float)
+    R = np.sqrt(np.einsum("ij,ij->i", rel, rel))
+    # the triple product per vertex-relative vector, by its cofactors
+    t = np.asarray(mesh.triangles)
+    a, b, c = t[:, 0], t[:, 1], t[:, 2]
+    r1, r2, r3 = rel[a], rel[b], rel[c]
+    R1, R2, R3 = R[a], R[b], R[c]
+    numer = (r1[:, 0] * (r2[:, 1] * r3[:, 2] - r2[:, 2] * r3[:, 1])
+             + r1[:, 1] * (r2[:, 2] * r3[:, 0] - r2[:, 0] * r3[:, 2])
+             + r1[:, 2] * (r2[:, 0] * r3[:, 1] - r2[:, 1] * r3[:, 0]))
     denom = (R1 * R2 * R3 + R3 * np.einsum("ij,ij->i", r1, r2) + R1 * np.einsum("ij,ij->i", r2, r3)
              + R2 * np.einsum("ij,ij->i", r1, r3))
     return float(np.sum(2.0 * np.arctan2(numer, denom)))
@@ -267,15 +291,17 @@ class RegionModel:
         self._sigma: dict = {}
         self.validate()
 
-    def _infer_sigma(self, region: Region, patch: Patch) -> int:
+    def _infer_sigma(self, region: Region, patch: Patch, seen: float | None = None) -> int:
         """The sign rule (core.py:713-729): +1 when the patch is seen from
         the region's probe point with a positive solid angle (outward
         normals), -1 when negative. A closed patch that does not enclose the
         probe bounds a cavity: its sign is the opposite of the solid angle it
-        subtends at its own vertex centroid. An override wins."""
+        subtends at its own vertex centroid. An override wins. ``seen`` is
+        the patch's solid angle at the probe point when already summed."""
         if patch.name in region.orientation_overrides:
             return int(region.orientation_overrides[patch.name])
-        seen = solid_angle_sum(patch.mesh, region.probe_point)
+        if seen is None:
+            seen = solid_angle_sum(patch.mesh, region.probe_point)
         if abs(seen) > _OPEN_FLOOR:
             return int(np.sign(seen))
         from_inside = solid_angle_sum(patch.mesh, np.asarray(patch.mesh.vertices, float).mean(axis=0))
@@ -318,8 +344,9 @@ class RegionModel:
                 continue
             closure = 0.0
             for p in r.patches:
-                self._sigma[(r.name, p.name)] = self._infer_sigma(r, p)
-                closure += self._sigma[(r.name, p.name)] * solid_angle_sum(p.mesh, r.probe_point)
+                seen = solid_angle_sum(p.mesh, r.probe_point)
+                self._sigma[(r.name, p.name)] = self._infer_sigma(r, p, seen)
+                closure += self._sigma[(r.name, p.name)] * seen
             if abs(closure / (4.0 * np.pi) - 1.0) > 1e-3:
                 raise ValueError(f"region '{r.name}' is not closed around its probe point: the signed solid "
                                  f"angles sum to {closure:.6f} sr, not 4 pi")
