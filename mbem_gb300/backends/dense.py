@@ -107,6 +107,10 @@ def _checked_drag(system: BlockSystem, drag) -> dict:
     return drag
 
 
+# one high-priority side stream per device for the assembly warnings
+_SIDE_STREAMS: dict = {}
+
+
 def _f32_matrix(rows: int, cols: int, dev, zero: bool = False) -> torch.Tensor:
     """An FP32 (rows, cols) matrix whose rows start on 16-byte boundaries
     (leading dimension rounded up to 4), as the streaming matvecs need."""
@@ -169,7 +173,10 @@ class AssembledDense:
         require_anchor_or_deflate(system, jump, deflate)
         require_cuda()
         from .diagnostics import warn_assembly
-        warn_assembly(system, eps, jump)
+        # the mixed assembly runs them once its far-field kernels are enqueued
+        self._warn_pending = precision == "mixed"
+        if not self._warn_pending:
+            warn_assembly(system, eps, jump)
         self.fault_drag = _checked_drag(system, fault_drag)
         self.lu = lu
         self._factor = None
@@ -245,21 +252,40 @@ class AssembledDense:
 
     # -- mixed precision: FP32 far field + FP64 near blocks -------------
     def _mixed_block(self, far_out, q, p, kernel, material, alpha, row0, col0, far16_out=None):
-        from ..la.mixed import far_near_block
+        from ..la.mixed import near_blocks
+        return near_blocks(self._mixed_launch(far_out, q, p, kernel, material, alpha, row0, col0, far16_out))
+
+    def _mixed_launch(self, far_out, q, p, kernel, material, alpha, row0, col0, far16_out=None):
+        """Enqueues one block's far-field kernel; ``near_blocks`` of the
+        result reads its near list."""
+        from ..la.mixed import far_launch
         if kernel not in (KERNEL_T, KERNEL_U):
             raise NotImplementedError("traction rows are not in the mixed-precision operator")
         f = self._patch_arrays(q)
         s = self._patch_arrays(p)
-        if kernel == KERNEL_T:
-            coeffs = kb.t_coeffs(material.mu, material.lam)
-            return far_near_block("T", f["coll"], s["tv"], s["normals"], s["eps"], coeffs, alpha, far_out,
-                                  row0, col0, self.near_factor, self._timer, far16_out, p.order)
-        coeffs = kb.u_coeffs(material.mu, material.lam)
-        return far_near_block("U", f["coll"], s["tv"], s["normals"], s["eps"], coeffs, alpha, far_out, row0,
-                              col0, self.near_factor, self._timer, far16_out, p.order)
+        name = "T" if kernel == KERNEL_T else "U"
+        coeffs = (kb.t_coeffs if kernel == KERNEL_T else kb.u_coeffs)(material.mu, material.lam)
+        return far_launch(name, f["coll"], s["tv"], s["normals"], s["eps"], coeffs, alpha, far_out, row0, col0,
+                          self.near_factor, self._timer, far16_out, p.order)
+
+    def _warn_on_side_stream(self):
+        """The assembly warnings (their distance kernels and reads) on a
+        high-priority side stream, so that they overlap the kernels already
+        enqueued on the current one."""
+        from .diagnostics import warn_assembly
+        if not self._warn_pending:
+            return
+        self._warn_pending = False
+        dev = torch.cuda.current_device()
+        side = _SIDE_STREAMS.get(dev)
+        if side is None:
+            side = _SIDE_STREAMS[dev] = torch.cuda.Stream(priority=-1)
+        with torch.cuda.stream(side):
+            warn_assembly(self.system, self.eps, self.jump)
+        side.synchronize()
 
     def _build_mixed(self):
-        from ..la.mixed import MixedOperator
+        from ..la.mixed import MixedOperator, near_blocks
         dev = require_cuda()
         n = self.layout.n_unknowns
         self._arrays = self._arrays_in if self._arrays_in is not None else {}
@@ -285,14 +311,21 @@ class AssembledDense:
                 raise NotImplementedError("mixed precision: FAULT_TRACTION rows of an order > 0 fault")
         terms = [t for t in self.system.terms if t.row.offset not in trac]
         trac_terms = [t for t in self.system.terms if t.row.offset in trac]
+        # every far-field kernel is enqueued first; the assembly warnings run
+        # on a side stream while they work, then the near lists are read
+        launched = []
         for t in terms:
             mat = self.materials[t.region.name]
             view = A32[t.row.offset:t.row.stop, t.col.offset:t.col.stop]
             view16 = None if A16 is None else A16[t.row.offset:t.row.stop, t.col.offset:t.col.stop]
-            nl = self._mixed_block(view, t.field_patch, t.source_patch, t.kernel, mat, t.scale, t.row.offset,
-                                   t.col.offset, view16)
+            launched.append(self._mixed_launch(view, t.field_patch, t.source_patch, t.kernel, mat, t.scale,
+                                               t.row.offset, t.col.offset, view16))
+        self._warn_on_side_stream()
+        for t, fl in zip(terms, launched):
+            nl = near_blocks(fl)
             op.near.append(nl)
-            placed[(id(t.field_patch), id(t.source_patch), t.kernel, id(mat))] = (t, nl)
+            placed[(id(t.field_patch), id(t.source_patch), t.kernel, id(self.materials[t.region.name]))] = (t, nl)
+        del launched
 
         temp = {}
 

@@ -58,9 +58,11 @@ int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, floa
                  cudaStream_t st);
 
 // y = A16 x + near blocks x (BF16 far field, FP32 sums; FP64 near blocks);
-// xf: n_cols floats of scratch (16-byte aligned).
+// xf: n_cols floats of scratch (16-byte aligned). stop: an optional device
+// flag; when set as the kernels start they return without work.
 int bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_cols, int n_near,
-                const mbem_near_blocks* near, const double* x, double* y, float* xf, cudaStream_t st);
+                const mbem_near_blocks* near, const double* x, double* y, float* xf, cudaStream_t st,
+                const int* stop = nullptr);
 // z = the BF16 inner GMRES solve of r (precond kind 3).
 int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t st);
 

@@ -202,44 +202,7 @@ __global__ void dgemm_multi_kernel(const double* __restrict__ A, int64_t ld, int
 // ---------------------------------------------------------------------------
 constexpr int KV_THREADS = 256;
 constexpr int KV_COLS = 2 * KV_THREADS;      // columns per block
-constexpr int KV_MAXV = 64;                  // vectors per multi-dot pass
-
-// partial[b * k + i] = sum over block b's columns of V[i, c] * w[c]
-__global__ void __launch_bounds__(KV_THREADS)
-multidot_partial_kernel(const double* __restrict__ V, int64_t ldv, int k, int64_t n,
-                        const double* __restrict__ w, double* __restrict__ partial) {
-    __shared__ double red[KV_THREADS / 32][KV_MAXV];
-    const int64_t c0 = (int64_t)blockIdx.x * KV_COLS + 2 * threadIdx.x;
-    double w0 = 0.0, w1 = 0.0;
-    if (c0 < n) w0 = w[c0];
-    if (c0 + 1 < n) w1 = w[c0 + 1];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int i = 0; i < k; i++) {
-        const double* v = V + (int64_t)i * ldv;
-        double p = 0.0;
-        if (c0 < n) p = v[c0] * w0;
-        if (c0 + 1 < n) p = fma(v[c0 + 1], w1, p);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-        if (lane == 0) red[wid][i] = p;
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < k; i += KV_THREADS) {
-        double s = 0.0;
-        for (int q = 0; q < KV_THREADS / 32; q++) s += red[q][i];
-        partial[(int64_t)blockIdx.x * k + i] = s;
-    }
-}
-
-// h[i] (+)= sum_b partial[b * k + i], in block order
-__global__ void multidot_final_kernel(const double* __restrict__ partial, int nblocks, int k, int accumulate,
-                                      double* __restrict__ h) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k) return;
-    double s = 0.0;
-    for (int b = 0; b < nblocks; b++) s += partial[(int64_t)b * k + i];
-    h[i] = accumulate ? h[i] + s : s;
-}
+constexpr int KV_MAXV = 64;                  // vectors per pass over shared memory
 
 // w[c] += sign * sum_i V[i, c] h[i]
 __global__ void multiaxpy_kernel(double* __restrict__ w, const double* __restrict__ V, int64_t ldv, int k,
@@ -254,9 +217,10 @@ __global__ void multiaxpy_kernel(double* __restrict__ w, const double* __restric
     w[c] = acc;
 }
 
-// v_out = v_in * (1 / sqrt(*nrm2)), nrm2 on the device
+// v_out = v_in * (1 / sqrt(*nrm2)), nrm2 on the device; a set *stop returns at once
 __global__ void scale_by_rnorm_kernel(const double* __restrict__ v_in, double* __restrict__ v_out, int64_t n,
-                                      const double* __restrict__ nrm2) {
+                                      const double* __restrict__ nrm2, const int* __restrict__ stop) {
+    if (stop && *stop) return;
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
     const double s = *nrm2;
@@ -280,7 +244,9 @@ constexpr int PROJ_THREADS = 256;
 constexpr int PROJ_BLOCKS = 128;     // partial sums: 3 * PROJ_BLOCKS doubles
 
 __global__ void __launch_bounds__(PROJ_THREADS)
-proj_partial_kernel(const double* __restrict__ vin, URanges ur, double* __restrict__ partial) {
+proj_partial_kernel(const double* __restrict__ vin, URanges ur, double* __restrict__ partial,
+                    const int* __restrict__ stop) {
+    if (stop && *stop) return;
     __shared__ double red[PROJ_THREADS / 32][3];
     double acc[3] = {0.0, 0.0, 0.0};
     const int64_t stride = (int64_t)gridDim.x * PROJ_THREADS;
@@ -304,10 +270,9 @@ proj_partial_kernel(const double* __restrict__ vin, URanges ur, double* __restri
     }
 }
 
-__global__ void __launch_bounds__(PROJ_THREADS)
-proj_apply_kernel(const double* __restrict__ vin, double* __restrict__ vout, int64_t n, URanges ur,
-                  const double* __restrict__ partial, int nparts) {
-    __shared__ double mean[3];
+// the three component means over the u-slots from the partial sums (threads
+// 0..2 form them in block order; every thread returns after the barrier)
+__device__ void proj_means(URanges ur, const double* __restrict__ partial, int nparts, double* mean) {
     if (threadIdx.x < 3) {
         double s = 0.0;
         for (int b = 0; b < nparts; b++) s += partial[3 * b + threadIdx.x];
@@ -317,24 +282,346 @@ proj_apply_kernel(const double* __restrict__ vin, double* __restrict__ vout, int
         mean[threadIdx.x] = (total > 0) ? s / (double)(total / 3) : 0.0;
     }
     __syncthreads();
+}
+
+__device__ __forceinline__ double proj_mean_at(URanges ur, const double* mean, int64_t c) {
+    double m = 0.0;
+    for (int q = 0; q < ur.n; q++)
+        if (c >= ur.off[q] && c < ur.off[q] + ur.len[q]) m = mean[(c - ur.off[q]) % 3];
+    return m;
+}
+
+__global__ void __launch_bounds__(PROJ_THREADS)
+proj_apply_kernel(const double* __restrict__ vin, double* __restrict__ vout, int64_t n, URanges ur,
+                  const double* __restrict__ partial, int nparts, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    __shared__ double mean[3];
+    proj_means(ur, partial, nparts, mean);
     for (int64_t c = (int64_t)blockIdx.x * PROJ_THREADS + threadIdx.x; c < n;
-         c += (int64_t)gridDim.x * PROJ_THREADS) {
-        double m = 0.0;
-        for (int q = 0; q < ur.n; q++)
-            if (c >= ur.off[q] && c < ur.off[q] + ur.len[q]) m = mean[(c - ur.off[q]) % 3];
-        vout[c] = vin[c] - m;
-    }
+         c += (int64_t)gridDim.x * PROJ_THREADS)
+        vout[c] = vin[c] - proj_mean_at(ur, mean, c);
 }
 
 // vout = P vin (vout may alias vin); partial holds 3 * PROJ_BLOCKS doubles
 static int project(const double* vin, double* vout, int64_t n, const URanges& ur, double* partial,
-                   cudaStream_t st) {
-    proj_partial_kernel<<<PROJ_BLOCKS, PROJ_THREADS, 0, st>>>(vin, ur, partial);
+                   cudaStream_t st, const int* stop = nullptr) {
+    proj_partial_kernel<<<PROJ_BLOCKS, PROJ_THREADS, 0, st>>>(vin, ur, partial, stop);
     const unsigned g = (unsigned)lmin(ceil_div(n, PROJ_THREADS), 4 * 152);
-    proj_apply_kernel<<<g, PROJ_THREADS, 0, st>>>(vin, vout, n, ur, partial, PROJ_BLOCKS);
+    proj_apply_kernel<<<g, PROJ_THREADS, 0, st>>>(vin, vout, n, ur, partial, PROJ_BLOCKS, stop);
     return launch_status("project", 2);
 }
 
+// ---------------------------------------------------------------------------
+// Device-side Arnoldi steps (la/solver.py:115-245, with classical
+// Gram-Schmidt applied twice). After its product a GMRES step is four
+// kernels: kv_dot (the projection's subtraction fused in, then the first
+// pass's dots), kv_axpy_dot (the first pass's subtraction, the second pass's
+// dots), kv_axpy_norm (the second subtraction, |w|^2 and the Givens rotation
+// of the new Hessenberg column) and the scaling of the next basis vector.
+// Each of the first three writes per-block partial sums; the last block to
+// arrive adds them in block order, so the result does not depend on the
+// order in which blocks finish. The rotations, the rotated right-hand side g
+// and the triangular factor R stay on the device, next to a control block
+// whose `stop` makes every later step kernel return at once: the host can
+// enqueue step j + 1 before it has read whether step j ended the basis.
+// ---------------------------------------------------------------------------
+struct KrylovCtl {
+    unsigned int arrive[4];   // block arrivals of the fused kernels, zero between launches
+    int stop;                 // the basis has ended: the step kernels return at once
+    int used;                 // columns in the least-squares problem
+    int breakdown;            // a zero pivot ended the basis
+    int steps;                // rotations formed
+    double beta;              // |r| at the cycle start
+    double beta2;             // beta^2
+    double res;               // |g[used]|: the residual estimate
+};
+
+struct KvGivens {
+    double* cs;
+    double* sn;
+    double* g;        // m + 1: the rotated beta e1
+    double* R;        // m x m, column j at R + m j
+    int m;
+    int outer;        // 1: FGMRES's sign convention, breakdown only (the host stops it)
+    double rtol;      // the inner solve stops once |g[j+1]| < rtol beta (0: never)
+};
+
+// every thread of the block calls this after its partial stores; true in the
+// block that arrives last, which may then read every block's partials
+__device__ __forceinline__ bool kv_last_block(unsigned int* arrive) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(arrive, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+__device__ __forceinline__ double kv_sum_blocks(const double* partial, int nb, int k, int i) {
+    double s = 0.0;
+    for (int b = 0; b < nb; b++) s += __ldcg(partial + (int64_t)b * k + i);
+    return s;
+}
+
+// partial[b k + i] = sum over block b's two columns per thread of V[i, c] w[c]
+__device__ void kv_block_dots(const double* __restrict__ V, int64_t ldv, int k, int64_t n, int64_t c0, double w0,
+                              double w1, double* __restrict__ partial) {
+    __shared__ double red[KV_THREADS / 32][KV_MAXV];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i0 = 0; i0 < k; i0 += KV_MAXV) {
+        const int kc = min(KV_MAXV, k - i0);
+        for (int i = 0; i < kc; i++) {
+            const double* v = V + (int64_t)(i0 + i) * ldv;
+            double p = 0.0;
+            if (c0 < n) p = v[c0] * w0;
+            if (c0 + 1 < n) p = fma(v[c0 + 1], w1, p);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+            if (lane == 0) red[wid][i] = p;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < kc; i += KV_THREADS) {
+            double s = 0.0;
+            for (int q = 0; q < KV_THREADS / 32; q++) s += red[q][i];
+            partial[(int64_t)blockIdx.x * k + i0 + i] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// (w0, w1) += sign * sum_i V[i, (c0, c0 + 1)] h[i], in i order
+__device__ void kv_block_axpy(const double* __restrict__ V, int64_t ldv, int k, int64_t n, int64_t c0,
+                              const double* __restrict__ h, double sign, double& w0, double& w1) {
+    __shared__ double hs[KV_MAXV];
+    for (int i0 = 0; i0 < k; i0 += KV_MAXV) {
+        const int kc = min(KV_MAXV, k - i0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < kc; i += KV_THREADS) hs[i] = sign * h[i0 + i];
+        __syncthreads();
+        for (int i = 0; i < kc; i++) {
+            const double* v = V + (int64_t)(i0 + i) * ldv;
+            if (c0 < n) w0 = fma(v[c0], hs[i], w0);
+            if (c0 + 1 < n) w1 = fma(v[c0 + 1], hs[i], w1);
+        }
+    }
+}
+
+// partial[b] = sum over block b of w^2
+__device__ void kv_block_sumsq(int64_t n, int64_t c0, double w0, double w1, double* __restrict__ partial) {
+    __shared__ double red[KV_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double p = 0.0;
+    if (c0 < n) p = w0 * w0;
+    if (c0 + 1 < n) p = fma(w1, w1, p);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+    if (lane == 0) red[wid] = p;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < KV_THREADS / 32; q++) s += red[q];
+        partial[blockIdx.x] = s;
+    }
+}
+
+// The rotation of Hessenberg column j (la/solver.py:188-210): h[0..j] are
+// its Gram-Schmidt coefficients, h[j + 1] = |w|^2. The earlier rotations are
+// applied, a new one zeroes the subdiagonal, g is rotated and the column
+// stored in R. A zero pivot ends the basis before column j; on the inner
+// solve an invariant Krylov space (|w| = 0) or a residual estimate below
+// rtol beta ends it after.
+__device__ void kv_givens(KrylovCtl* ctl, const double* h, int j, const KvGivens& G) {
+    double* Rj = G.R + (int64_t)G.m * j;
+    for (int i = 0; i <= j; i++) Rj[i] = h[i];
+    const double sub = sqrt(fmax(h[j + 1], 0.0));
+    for (int i = 0; i < j; i++) {
+        const double a = Rj[i], b = Rj[i + 1];
+        Rj[i] = G.cs[i] * a + G.sn[i] * b;
+        Rj[i + 1] = -G.sn[i] * a + G.cs[i] * b;
+    }
+    const double hjj = Rj[j];
+    const double den = sqrt(hjj * hjj + sub * sub);
+    if (den == 0.0) {
+        ctl->breakdown = 1;
+        ctl->stop = 1;
+        return;
+    }
+    double c, s;
+    if (G.outer) {
+        c = fabs(hjj) > 0 ? fabs(hjj) / den : 0.0;
+        s = fabs(hjj) > 0 ? (hjj / fabs(hjj)) * sub / den : 1.0;
+        Rj[j] = c * hjj + s * sub;
+    } else {
+        c = hjj / den;
+        s = sub / den;
+        Rj[j] = den;
+    }
+    G.cs[j] = c;
+    G.sn[j] = s;
+    G.g[j + 1] = -s * G.g[j];
+    G.g[j] = c * G.g[j];
+    ctl->used = j + 1;
+    ctl->steps = j + 1;
+    ctl->res = fabs(G.g[j + 1]);
+    if (!G.outer && (sub == 0.0 || (G.rtol > 0.0 && ctl->res < G.rtol * ctl->beta))) ctl->stop = 1;
+}
+
+// beta = |w| for a new cycle: g[0] = beta and the control block's state
+// reset (its arrival counters are zero already); a zero beta ends the basis
+__global__ void __launch_bounds__(KV_THREADS)
+kv_norm_init_kernel(const double* __restrict__ w, int64_t n, double* __restrict__ partial, double* __restrict__ g,
+                    KrylovCtl* __restrict__ ctl) {
+    const int64_t c0 = (int64_t)blockIdx.x * KV_COLS + 2 * threadIdx.x;
+    const double w0 = c0 < n ? w[c0] : 0.0, w1 = c0 + 1 < n ? w[c0 + 1] : 0.0;
+    kv_block_sumsq(n, c0, w0, w1, partial);
+    if (!kv_last_block(&ctl->arrive[3])) return;
+    if (threadIdx.x == 0) {
+        const double s = kv_sum_blocks(partial, gridDim.x, 1, 0);
+        const double beta = sqrt(s);
+        ctl->beta = beta;
+        ctl->beta2 = s;
+        ctl->res = beta;
+        ctl->used = ctl->steps = ctl->breakdown = 0;
+        ctl->stop = !(beta > 0.0);
+        g[0] = beta;
+        ctl->arrive[3] = 0;
+    }
+}
+
+// h[i] = V[i] . w, i < k; with proj_part, w is first replaced by P w (the
+// projection's subtraction; its partial sums from proj_partial_kernel)
+__global__ void __launch_bounds__(KV_THREADS)
+kv_dot_kernel(const double* __restrict__ V, int64_t ldv, int k, int64_t n, double* __restrict__ w, URanges ur,
+              const double* __restrict__ proj_part, double* __restrict__ partial, double* __restrict__ h,
+              KrylovCtl* __restrict__ ctl) {
+    if (ctl->stop) return;
+    const int64_t c0 = (int64_t)blockIdx.x * KV_COLS + 2 * threadIdx.x;
+    double w0 = c0 < n ? w[c0] : 0.0, w1 = c0 + 1 < n ? w[c0 + 1] : 0.0;
+    if (proj_part) {
+        __shared__ double mean[3];
+        proj_means(ur, proj_part, PROJ_BLOCKS, mean);
+        if (c0 < n) w[c0] = w0 = w0 - proj_mean_at(ur, mean, c0);
+        if (c0 + 1 < n) w[c0 + 1] = w1 = w1 - proj_mean_at(ur, mean, c0 + 1);
+    }
+    kv_block_dots(V, ldv, k, n, c0, w0, w1, partial);
+    if (!kv_last_block(&ctl->arrive[0])) return;
+    for (int i = threadIdx.x; i < k; i += KV_THREADS) h[i] = kv_sum_blocks(partial, gridDim.x, k, i);
+    if (threadIdx.x == 0) ctl->arrive[0] = 0;
+}
+
+// w -= V h (the first pass), then h2[i] = V[i] . w and h[i] += h2[i]
+__global__ void __launch_bounds__(KV_THREADS)
+kv_axpy_dot_kernel(const double* __restrict__ V, int64_t ldv, int k, int64_t n, double* __restrict__ w,
+                   double* __restrict__ h, double* __restrict__ partial, double* __restrict__ h2,
+                   KrylovCtl* __restrict__ ctl) {
+    if (ctl->stop) return;
+    const int64_t c0 = (int64_t)blockIdx.x * KV_COLS + 2 * threadIdx.x;
+    double w0 = c0 < n ? w[c0] : 0.0, w1 = c0 + 1 < n ? w[c0 + 1] : 0.0;
+    kv_block_axpy(V, ldv, k, n, c0, h, -1.0, w0, w1);
+    if (c0 < n) w[c0] = w0;
+    if (c0 + 1 < n) w[c0 + 1] = w1;
+    kv_block_dots(V, ldv, k, n, c0, w0, w1, partial);
+    if (!kv_last_block(&ctl->arrive[1])) return;
+    for (int i = threadIdx.x; i < k; i += KV_THREADS) {
+        const double s = kv_sum_blocks(partial, gridDim.x, k, i);
+        h2[i] = s;
+        h[i] += s;
+    }
+    if (threadIdx.x == 0) ctl->arrive[1] = 0;
+}
+
+// w -= V h2 (the second pass), h[k] = |w|^2 and the rotation of column k - 1
+__global__ void __launch_bounds__(KV_THREADS)
+kv_axpy_norm_kernel(const double* __restrict__ V, int64_t ldv, int k, int64_t n, double* __restrict__ w,
+                    const double* __restrict__ h2, double* __restrict__ partial, double* __restrict__ h,
+                    KvGivens G, KrylovCtl* __restrict__ ctl) {
+    if (ctl->stop) return;
+    const int64_t c0 = (int64_t)blockIdx.x * KV_COLS + 2 * threadIdx.x;
+    double w0 = c0 < n ? w[c0] : 0.0, w1 = c0 + 1 < n ? w[c0 + 1] : 0.0;
+    kv_block_axpy(V, ldv, k, n, c0, h2, -1.0, w0, w1);
+    if (c0 < n) w[c0] = w0;
+    if (c0 + 1 < n) w[c0 + 1] = w1;
+    kv_block_sumsq(n, c0, w0, w1, partial);
+    if (!kv_last_block(&ctl->arrive[2])) return;
+    if (threadIdx.x == 0) {
+        h[k] = kv_sum_blocks(partial, gridDim.x, 1, 0);
+        kv_givens(ctl, h, k - 1, G);
+        ctl->arrive[2] = 0;
+    }
+}
+
+// y = R^-1 g over the columns in use: one warp, rows from the bottom, each
+// row's sum by lanes then a fixed shuffle tree
+constexpr int KV_MAX_BACKSOLVE = 1024;
+
+__global__ void kv_backsolve_kernel(const KrylovCtl* __restrict__ ctl, const double* __restrict__ R, int m,
+                                    const double* __restrict__ g, double* __restrict__ y) {
+    __shared__ double ys[KV_MAX_BACKSOLVE];
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x >= 32) return;
+    const int used = min(ctl->used, KV_MAX_BACKSOLVE);
+    for (int i = used - 1; i >= 0; i--) {
+        double s = 0.0;
+        for (int q = i + 1 + lane; q < used; q += 32) s = fma(R[i + (int64_t)m * q], ys[q], s);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) ys[i] = (g[i] - s) / R[i + (int64_t)m * i];
+        __syncwarp();
+    }
+    for (int i = lane; i < used; i += 32) y[i] = ys[i];
+}
+
+// Pinned host copies of a control block, in two slots per loop, so that the
+// host reads step j - 1's while step j's copy is in flight. One small pinned
+// buffer per host thread, kept for the thread's life: the inner solve uses
+// slots 0-1, the FGMRES that calls it slots 2-3.
+static KrylovCtl* kv_pinned_slots() {
+    struct Holder {
+        KrylovCtl* p = nullptr;
+        ~Holder() {
+            if (p) cudaFreeHost(p);
+        }
+    };
+    thread_local Holder h;
+    if (!h.p && cudaHostAlloc(reinterpret_cast<void**>(&h.p), 4 * sizeof(KrylovCtl), cudaHostAllocDefault) !=
+                    cudaSuccess)
+        h.p = nullptr;
+    return h.p;
+}
+
+struct KvStatus {
+    KrylovCtl* slot = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaStream_t st = nullptr;
+
+    int init(cudaStream_t s, int first_slot) {
+        st = s;
+        KrylovCtl* base = kv_pinned_slots();
+        if (!base) return set_error(MBEM_ERR_CUDA, "pinned status buffer: %s", cudaGetErrorString(cudaGetLastError()));
+        slot = base + first_slot;
+        for (int i = 0; i < 2; i++)
+            if (cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess)
+                return launch_status("status event", 0);
+        return MBEM_OK;
+    }
+    // copy the control block after step j's kernels
+    int post(const KrylovCtl* dev, int j) {
+        cudaMemcpyAsync(&slot[j & 1], dev, sizeof(KrylovCtl), cudaMemcpyDeviceToHost, st);
+        cudaEventRecord(ev[j & 1], st);
+        return launch_status("status copy", 0);
+    }
+    // the control block as step j left it (waits for that step only)
+    int wait(int j, KrylovCtl* out) {
+        if (cudaEventSynchronize(ev[j & 1]) != cudaSuccess) return launch_status("status wait", 0);
+        *out = slot[j & 1];
+        return MBEM_OK;
+    }
+    ~KvStatus() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
 
 // ---------------------------------------------------------------------------
 // FGMRES (la/solver.py:115-245) with classical Gram-Schmidt applied twice
@@ -347,11 +634,15 @@ struct FgmresWork {
     double* w;        // n
     double* t;        // n
     double* r;        // n
-    double* partial;  // nblocks * (m+1)
-    double* h;        // m+2
+    double* partial;  // nblocks * (m+2)
+    double* h;        // m+2: the new column's coefficients, |w|^2 at j+1
     double* h2;       // m+2
-    double* y;        // m
-    double* scal;     // 8
+    double* y;        // m+1
+    double* cs;       // m
+    double* sn;       // m
+    double* g;        // m+1
+    double* R;        // m x m
+    KrylovCtl* ctl;
     float* xh;        // n (mixed operator: split of the matvec input)
     float* xl;        // n
     double* proj;     // 3 * PROJ_BLOCKS projection partial sums
@@ -377,7 +668,11 @@ static size_t fgmres_layout(int64_t n, int m, char* base, FgmresWork* w) {
     tmp.h = take(m + 2);
     tmp.h2 = take(m + 2);
     tmp.y = take(m + 1);
-    tmp.scal = take(8);
+    tmp.cs = take(m);
+    tmp.sn = take(m);
+    tmp.g = take(m + 1);
+    tmp.R = take((size_t)m * m);
+    tmp.ctl = reinterpret_cast<KrylovCtl*>(take((sizeof(KrylovCtl) + 7) / 8));
     tmp.xh = reinterpret_cast<float*>(take((n + 1) / 2));
     tmp.xl = reinterpret_cast<float*>(take((n + 1) / 2));
     tmp.proj = take(3 * PROJ_BLOCKS);
@@ -395,12 +690,12 @@ struct Fgmres {
     FgmresWork W;
     int64_t nb;
 
-    int proj(const double* in, double* out) {
+    int proj(const double* in, double* out, const int* stop = nullptr) {
         if (!deflate) {
             if (in != out) cudaMemcpyAsync(out, in, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
             return launch_status("copy", 0);
         }
-        return project(in, out, n, ur, W.proj, st);
+        return project(in, out, n, ur, W.proj, st, stop);
     }
     // out = P A P in (uses W.t)
     int op(const double* in, double* out) {
@@ -441,17 +736,6 @@ struct Fgmres {
     int matvecs = 0;
     double matvec_ms = 0.0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
-    // h[0..k) (+)= V[0..k) . w
-    int multidot(const double* V, int k, const double* w, double* h, int accumulate) {
-        for (int i0 = 0; i0 < k; i0 += KV_MAXV) {
-            const int kc = min(KV_MAXV, k - i0);
-            multidot_partial_kernel<<<(unsigned)nb, KV_THREADS, 0, st>>>(V + (int64_t)i0 * n, n, kc, n, w,
-                                                                        W.partial);
-            multidot_final_kernel<<<1, 64, 0, st>>>(W.partial, (int)nb, kc, accumulate, h + i0);
-            count_launches(2);
-        }
-        return launch_status("multidot", 0);
-    }
     int multiaxpy(double* w, const double* V, int k, const double* h, double sign) {
         for (int i0 = 0; i0 < k; i0 += KV_MAXV) {
             const int kc = min(KV_MAXV, k - i0);
@@ -461,37 +745,59 @@ struct Fgmres {
         }
         return launch_status("multiaxpy", 0);
     }
-    int norm2(const double* v, double* out_dev) { return multidot(v, 1, v, out_dev, 0); }
+    // beta = |v| into the control block, g[0] = beta (a new cycle)
+    int norm_init(const double* v, double* partial, double* g, KrylovCtl* ctl) {
+        kv_norm_init_kernel<<<(unsigned)nb, KV_THREADS, 0, st>>>(v, n, partial, g, ctl);
+        return launch_status("norm init", 1);
+    }
+    // one Arnoldi step after its product w: the CGS2 coefficients into h,
+    // |w|^2 into h[k], the rotation of column k - 1, and V[k] = w / |w|
+    int arnoldi(double* V, int k, double* w, double* partial, double* h, double* h2, const KvGivens& G,
+                KrylovCtl* ctl, bool project_w, bool scale_next) {
+        const int* stop = &ctl->stop;
+        if (project_w) {
+            proj_partial_kernel<<<PROJ_BLOCKS, PROJ_THREADS, 0, st>>>(w, ur, W.proj, stop);
+            count_launches(1);
+        }
+        kv_dot_kernel<<<(unsigned)nb, KV_THREADS, 0, st>>>(V, n, k, n, w, ur, project_w ? W.proj : nullptr,
+                                                           partial, h, ctl);
+        kv_axpy_dot_kernel<<<(unsigned)nb, KV_THREADS, 0, st>>>(V, n, k, n, w, h, partial, h2, ctl);
+        kv_axpy_norm_kernel<<<(unsigned)nb, KV_THREADS, 0, st>>>(V, n, k, n, w, h2, partial, h, G, ctl);
+        if (scale_next)
+            scale_by_rnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(w, V + (int64_t)k * n, n, h + k, stop);
+        return launch_status("arnoldi step", 3 + (scale_next ? 1 : 0));
+    }
 };
 
 // ---------------------------------------------------------------------------
 // The BF16 inner solve (precond kind 3): up to `k` GMRES steps from zero on
-// P (A16 + near) P. The Arnoldi steps (CGS2, as in FGMRES) write each
-// Hessenberg column straight into device memory. With rtol = 0 the k steps
-// run with no host synchronisation and the host reads the (k+1) x k matrix
-// once; with rtol > 0 it reads each new column, applies the Givens rotations
-// as it goes and stops once the residual estimate is below rtol |P r|. Then
-// z = V y from the small least-squares solution. A column whose new norm is
-// zero (an invariant Krylov space) ends the basis.
+// P (A16 + near) P, every step on the device (the Arnoldi kernels above).
+// The host enqueues step j + 1, then reads step j's control block from
+// pinned memory; once a step ended the basis (residual estimate below
+// rtol |P r|, an invariant Krylov space, or a zero pivot) it stops
+// enqueueing, and the one step already queued after it returns at once.
+// Then z = V y from the device back substitution. No stream-wide wait.
 // ---------------------------------------------------------------------------
-__global__ void add_vec_kernel(double* __restrict__ h, const double* __restrict__ d, int k) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < k) h[i] += d[i];
-}
-
 // inner steps and applications since the last mbem_inner_bf16_stats call,
-// and (when timing is on) the device time of their BF16 products
+// and (when timing is on) the device time of their BF16 products, read from
+// their events at that call
 static int64_t g_inner_steps = 0, g_inner_applies = 0;
 static int g_inner_timing = 0;
 static double g_inner_matvec_ms = 0.0;
+static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_inner_events;
 
 struct InnerWork {
     double* V;        // (k+1, n)
     double* w;        // n
-    double* partial;  // nblocks * (k+1)
-    double* H;        // k columns of (k+2): h[0..j], |w|^2 at j+1; then beta^2
+    double* partial;  // nblocks * (k+2)
+    double* h;        // k+2: the new column's coefficients, |w|^2 at j+1
     double* h2;       // k+1
     double* y;        // k
+    double* cs;       // k
+    double* sn;       // k
+    double* g;        // k+1
+    double* R;        // k x k
+    KrylovCtl* ctl;
     float* xf;        // n
     double* proj;     // 3 * PROJ_BLOCKS
     double* t;        // n: M v_j (right preconditioner), then V y
@@ -509,9 +815,14 @@ static size_t inner_layout(int64_t n, int k, char* base, InnerWork* w) {
     t.V = take((size_t)(k + 1) * n);
     t.w = take(n);
     t.partial = take((size_t)nb * (k + 2));
-    t.H = take((size_t)(k + 1) * (k + 2));
+    t.h = take(k + 2);
     t.h2 = take(k + 1);
     t.y = take(k);
+    t.cs = take(k);
+    t.sn = take(k);
+    t.g = take(k + 1);
+    t.R = take((size_t)k * k);
+    t.ctl = reinterpret_cast<KrylovCtl*>(take((sizeof(KrylovCtl) + 7) / 8));
     t.xf = reinterpret_cast<float*>(take((n + 1) / 2));
     t.proj = take(3 * PROJ_BLOCKS);
     t.t = take(n);
@@ -542,57 +853,28 @@ int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t
     F.deflate = p->n_u_ranges > 0;
     F.W.partial = I.partial;
     F.W.proj = I.proj;
-    const int ldh = k + 2;
-    double* beta2 = I.H + (size_t)k * ldh;
-    const unsigned gn = (unsigned)ceil_div(n, 256);
-    const bool adaptive = p->rtol > 0.0;
+    KvStatus S;
+    if ((e = S.init(st, 0))) return e;
+    const KvGivens G{I.cs, I.sn, I.g, I.R, k, 0, p->rtol};
+    const int* stop = &I.ctl->stop;
 
-    if ((e = F.proj(r, I.w))) return e;
-    if ((e = F.norm2(I.w, beta2))) return e;
-    scale_by_rnorm_kernel<<<gn, 256, 0, st>>>(I.w, I.V, n, beta2);
-    count_launches(1);
+    // beta = |P r|, V[0] = P r / beta
+    cudaMemsetAsync(I.ctl, 0, sizeof(KrylovCtl), st);
     cudaMemsetAsync(z, 0, n * sizeof(double), st);
-    double beta = -1.0;
-    if (adaptive) {
-        cudaMemcpyAsync(&beta, beta2, sizeof(double), cudaMemcpyDeviceToHost, st);
-        if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
-        beta = sqrt(beta);
-        if (!(beta > 0.0)) return launch_status("inner solve zero rhs", 0);
-    }
-    // Givens least squares min |beta e1 - Hbar y| (la/solver.py:188-210),
-    // one column at a time; returns true when the basis ends at column j
-    std::vector<double> R((size_t)k * k, 0.0), g(k + 1, 0.0), cs(k), sn(k), y(k, 0.0);
-    int used = 0;
-    auto absorb = [&](int j, const double* hc) -> bool {
-        std::vector<double> col(j + 2);
-        for (int i = 0; i <= j; i++) col[i] = hc[i];
-        col[j + 1] = sqrt(fmax(hc[j + 1], 0.0));
-        for (int i = 0; i < j; i++) {
-            const double a = col[i], b = col[i + 1];
-            col[i] = cs[i] * a + sn[i] * b;
-            col[i + 1] = -sn[i] * a + cs[i] * b;
-        }
-        const double den = sqrt(col[j] * col[j] + col[j + 1] * col[j + 1]);
-        if (den == 0.0) return true;
-        cs[j] = col[j] / den;
-        sn[j] = col[j + 1] / den;
-        col[j] = den;
-        g[j + 1] = -sn[j] * g[j];
-        g[j] = cs[j] * g[j];
-        for (int i = 0; i <= j; i++) R[(size_t)i * k + j] = col[i];
-        used = j + 1;
-        if (col[j + 1] == 0.0) return true;                         // invariant Krylov space: exact
-        return adaptive && fabs(g[j + 1]) < p->rtol * beta;
-    };
-    if (adaptive) g[0] = beta;
-    std::vector<double> hcol(k + 2);
+    if ((e = F.proj(r, I.w))) return e;
+    if ((e = F.norm_init(I.w, I.partial, I.g, I.ctl))) return e;
+    scale_by_rnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(I.w, I.V, n, &I.ctl->beta2, stop);
+    count_launches(1);
+    KrylovCtl seen;
+    memset(&seen, 0, sizeof(seen));
+    int posted = -1;
+    bool ended = false;
     for (int j = 0; j < k; j++) {
         const double* vj = I.V + (int64_t)j * n;
-        double* hc = I.H + (size_t)j * ldh;
         if (p->precond) {
             // right preconditioning: the step multiplies A16 by P M v_j
             if ((e = precond_apply(p->precond, p->precond_state, vj, I.t, st))) return e;
-            if ((e = F.proj(I.t, I.t))) return e;
+            if ((e = F.proj(I.t, I.t, stop))) return e;
             vj = I.t;
         }
         if (g_inner_timing) {
@@ -600,53 +882,31 @@ int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t
             cudaEventCreate(&ev[0]);
             cudaEventCreate(&ev[1]);
             cudaEventRecord(ev[0], st);
-            e = bf16_matvec(p->A16, p->ld16, n, n, p->n_near, p->near, vj, I.w, I.xf, st);
+            e = bf16_matvec(p->A16, p->ld16, n, n, p->n_near, p->near, vj, I.w, I.xf, st, stop);
             cudaEventRecord(ev[1], st);
-            F.pending.push_back({ev[0], ev[1]});
+            g_inner_events.push_back({ev[0], ev[1]});
             if (e) return e;
-        } else if ((e = bf16_matvec(p->A16, p->ld16, n, n, p->n_near, p->near, vj, I.w, I.xf, st))) {
+        } else if ((e = bf16_matvec(p->A16, p->ld16, n, n, p->n_near, p->near, vj, I.w, I.xf, st, stop))) {
             return e;
         }
-        if ((e = F.proj(I.w, I.w))) return e;
-        if ((e = F.multidot(I.V, j + 1, I.w, hc, 0))) return e;
-        if ((e = F.multiaxpy(I.w, I.V, j + 1, hc, -1.0))) return e;
-        if ((e = F.multidot(I.V, j + 1, I.w, I.h2, 0))) return e;
-        if ((e = F.multiaxpy(I.w, I.V, j + 1, I.h2, -1.0))) return e;
-        add_vec_kernel<<<1, 64, 0, st>>>(hc, I.h2, j + 1);
-        count_launches(1);
-        if ((e = F.norm2(I.w, hc + (j + 1)))) return e;
-        if (adaptive) {
-            cudaMemcpyAsync(hcol.data(), hc, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, st);
-            if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
-            if (absorb(j, hcol.data())) break;
-        }
-        if (j + 1 < k) {
-            scale_by_rnorm_kernel<<<gn, 256, 0, st>>>(I.w, I.V + (int64_t)(j + 1) * n, n, hc + (j + 1));
-            count_launches(1);
+        if ((e = F.arnoldi(I.V, j + 1, I.w, I.partial, I.h, I.h2, G, I.ctl, F.deflate, j + 1 < k))) return e;
+        if ((e = S.post(I.ctl, j))) return e;
+        posted = j;
+        if (j >= 1) {
+            if ((e = S.wait(j - 1, &seen))) return e;
+            if (seen.stop) {
+                ended = true;
+                break;
+            }
         }
     }
-    if (!adaptive) {
-        std::vector<double> H((size_t)(k + 1) * ldh);
-        cudaMemcpyAsync(H.data(), I.H, H.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
-        if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
-        beta = sqrt(H[(size_t)k * ldh]);
-        if (!(beta > 0.0)) return launch_status("inner solve zero rhs", 0);
-        g[0] = beta;
-        for (int j = 0; j < k; j++)
-            if (absorb(j, H.data() + (size_t)j * ldh)) break;
-    }
-    for (int i = used - 1; i >= 0; i--) {
-        double s2 = g[i];
-        for (int q = i + 1; q < used; q++) s2 -= R[(size_t)i * k + q] * y[q];
-        y[i] = s2 / R[(size_t)i * k + i];
-    }
+    if (!ended && (e = S.wait(posted, &seen))) return e;
+    const int used = seen.used;
     g_inner_steps += used;
     g_inner_applies += 1;
-    if (!adaptive && cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
-    F.collect_times();
-    g_inner_matvec_ms += F.matvec_ms;
-    if (used == 0) return launch_status("inner solve", 0);
-    cudaMemcpyAsync(I.y, y.data(), used * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (used == 0) return launch_status("inner solve", 0);       // a zero P r: z = 0
+    kv_backsolve_kernel<<<1, 32, 0, st>>>(I.ctl, I.R, k, I.g, I.y);
+    count_launches(1);
     if (p->precond) {
         // z = P M (V y)
         cudaMemsetAsync(I.w, 0, n * sizeof(double), st);
@@ -656,9 +916,20 @@ int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t
     } else if ((e = F.multiaxpy(z, I.V, used, I.y, 1.0))) {
         return e;
     }
-    // the host vector y must outlive the copy
-    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("inner solve sync", 0);
     return launch_status("inner solve", 0);
+}
+
+// the device time of the inner products recorded since the last call
+static void collect_inner_events() {
+    for (auto& pr : g_inner_events) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(pr.second) == cudaSuccess &&
+            cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess)
+            g_inner_matvec_ms += ms;
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    g_inner_events.clear();
 }
 
 }  // namespace mbem
@@ -738,6 +1009,7 @@ size_t mbem_inner_bf16_workspace_size(int64_t n, int iterations) {
 }
 
 void mbem_inner_bf16_stats(int timing, int64_t* steps, int64_t* applies, double* matvec_ms) {
+    collect_inner_events();
     if (steps) *steps = g_inner_steps;
     if (applies) *applies = g_inner_applies;
     if (matvec_ms) *matvec_ms = g_inner_matvec_ms;
@@ -799,21 +1071,21 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
     F.time_matvec = prm->time_matvec != 0;
     FgmresWork& W = F.W;
     cudaStream_t st = F.st;
+    KvStatus S;
+    if ((e = S.init(st, 2))) return e;
+    const KvGivens G{W.cs, W.sn, W.g, W.R, m, 1, 0.0};
 
     double* history = rep->history;
     memset(rep, 0, sizeof(*rep));
     rep->history = history;
-    std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m, 0.0), sn(m, 0.0), g(m + 1, 0.0), hcol(m + 2);
-    double bnorm2 = 0.0, tmp;
+    KrylovCtl seen;
 
-    // b' = P b (kept in W.r until the first residual overwrites it)
+    // |P b|
+    cudaMemsetAsync(W.ctl, 0, sizeof(KrylovCtl), st);
     if ((e = F.proj(b, W.r))) return e;
-    if ((e = F.norm2(W.r, W.scal))) return e;
-    cudaMemcpyAsync(&bnorm2, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
-    const double bnorm = sqrt(bnorm2);
-    double* bproj = W.w;   // hold P b in w across cycles would clash; recompute each cycle instead
-    (void)bproj;
+    if ((e = F.norm_init(W.r, W.partial, W.g, W.ctl))) return e;
+    if ((e = S.post(W.ctl, 0)) || (e = S.wait(0, &seen))) return e;
+    const double bnorm = seen.beta;
     if (bnorm == 0.0) {
         cudaMemsetAsync(x, 0, n * sizeof(double), st);
         rep->converged = 1;
@@ -843,25 +1115,22 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
             axpby_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.w, n, -1.0, 1.0);
             count_launches(1);
         }
-        if ((e = F.norm2(W.r, W.scal))) return e;
-        cudaMemcpyAsync(&tmp, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st);
-        if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
-        const double beta = sqrt(tmp);
+        // beta = |r| and g = beta e1 on the device; the host reads beta to
+        // decide whether the cycle runs
+        if ((e = F.norm_init(W.r, W.partial, W.g, W.ctl))) return e;
+        if ((e = S.post(W.ctl, 0)) || (e = S.wait(0, &seen))) return e;
+        const double beta = seen.beta;
         arnoldi = beta / bnorm;
         if (arnoldi < prm->rtol) {
-            rnorm2_final = tmp;
+            rnorm2_final = seen.beta2;
             break;
         }
         const int mm = min(m, maxiter - total);
-        std::fill(H.begin(), H.end(), 0.0);
-        std::fill(g.begin(), g.end(), 0.0);
-        g[0] = beta;
-        scale_by_rnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.V, n, W.scal);
+        scale_by_rnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.V, n, &W.ctl->beta2, nullptr);
         count_launches(1);
         int jdone = 0;
         for (int j = 0; j < mm; j++) {
             double* vj = W.V + (int64_t)j * n;
-            double* vn = W.V + (int64_t)(j + 1) * n;
             if (flexible) {
                 // z_j = M^-1 v_j, w = P A P z_j (right preconditioning, flexible: la/solver.py:160-170)
                 double* zj = W.Z + (int64_t)j * n;
@@ -873,28 +1142,12 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
             } else if ((e = F.op(vj, W.w))) {               // w = P A P v_j
                 return e;
             }
-            if ((e = F.multidot(W.V, j + 1, W.w, W.h, 0))) return e;
-            if ((e = F.multiaxpy(W.w, W.V, j + 1, W.h, -1.0))) return e;
-            if ((e = F.multidot(W.V, j + 1, W.w, W.h2, 0))) return e;
-            if ((e = F.multiaxpy(W.w, W.V, j + 1, W.h2, -1.0))) return e;
-            if ((e = F.norm2(W.w, W.h + (j + 1)))) return e;
-            scale_by_rnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.w, vn, n, W.h + (j + 1));
-            count_launches(1);
-            cudaMemcpyAsync(hcol.data(), W.h, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, st);
-            std::vector<double> h2col(j + 1);
-            cudaMemcpyAsync(h2col.data(), W.h2, (j + 1) * sizeof(double), cudaMemcpyDeviceToHost, st);
-            if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
-            for (int i = 0; i <= j; i++) H[(size_t)i * m + j] = hcol[i] + h2col[i];
-            H[(size_t)(j + 1) * m + j] = sqrt(hcol[j + 1]);
-            // apply accumulated Givens rotations, then form a new one (solver.py:188-205)
-            for (int i = 0; i < j; i++) {
-                const double hi = H[(size_t)i * m + j], hi1 = H[(size_t)(i + 1) * m + j];
-                H[(size_t)i * m + j] = cs[i] * hi + sn[i] * hi1;
-                H[(size_t)(i + 1) * m + j] = -sn[i] * hi + cs[i] * hi1;
-            }
-            const double hjj = H[(size_t)j * m + j], hj1 = H[(size_t)(j + 1) * m + j];
-            const double den = sqrt(hjj * hjj + hj1 * hj1);
-            if (den == 0.0) {
+            // CGS2, |w| and the rotation on the device; the host reads the
+            // residual estimate for its stopping and stagnation tests (the
+            // next step's preconditioner solve costs far more than this wait)
+            if ((e = F.arnoldi(W.V, j + 1, W.w, W.partial, W.h, W.h2, G, W.ctl, false, true))) return e;
+            if ((e = S.post(W.ctl, j)) || (e = S.wait(j, &seen))) return e;
+            if (seen.breakdown) {
                 // exact breakdown with a zero pivot: the Krylov space is
                 // invariant and this column adds nothing; finish with the
                 // iterate of the columns before it
@@ -902,15 +1155,9 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
                 breakdown = true;
                 break;
             }
-            cs[j] = fabs(hjj) > 0 ? fabs(hjj) / den : 0.0;
-            sn[j] = fabs(hjj) > 0 ? (hjj / fabs(hjj)) * hj1 / den : 1.0;
-            H[(size_t)j * m + j] = cs[j] * hjj + sn[j] * hj1;
-            H[(size_t)(j + 1) * m + j] = 0.0;
-            g[j + 1] = -sn[j] * g[j];
-            g[j] = cs[j] * g[j];
             total++;
             jdone = j + 1;
-            arnoldi = fabs(g[j + 1]) / bnorm;
+            arnoldi = seen.res / bnorm;
             if (rep->history && total <= maxiter) rep->history[total - 1] = arnoldi;
             if (arnoldi < best / prm->stagnation_factor) {
                 best = arnoldi;
@@ -922,15 +1169,9 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
             if (arnoldi < prm->rtol || total >= maxiter) break;
         }
         if (jdone > 0) {
-            // back substitution (solver.py:503-510), then x += V[:j]^T y
-            std::vector<double> y(jdone, 0.0);
-            for (int i = jdone - 1; i >= 0; i--) {
-                double s = g[i];
-                for (int q = i + 1; q < jdone; q++) s -= H[(size_t)i * m + q] * y[q];
-                y[i] = s / H[(size_t)i * m + i];
-            }
-            cudaMemcpyAsync(W.y, y.data(), jdone * sizeof(double), cudaMemcpyHostToDevice, st);
-            if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
+            // back substitution (solver.py:503-510) on the device, then x += V[:j]^T y
+            kv_backsolve_kernel<<<1, 32, 0, st>>>(W.ctl, W.R, m, W.g, W.y);
+            count_launches(1);
             if ((e = F.multiaxpy(x, flexible ? W.Z : W.V, jdone, W.y, 1.0))) return e;
             x_zero = false;
         }
@@ -939,23 +1180,22 @@ static int fgmres_run(const double* A, int64_t ld, const mbem_mixed_operator* mo
     }
     // true residual (solver.py:234) and the zero-mean representative P x
     // (P A P x = P A P (P x): projecting x leaves the residual unchanged)
-    if (rnorm2_final < 0.0) {
+    double rnorm2 = rnorm2_final;
+    if (rnorm2 < 0.0) {
         if ((e = F.proj(b, W.r))) return e;
         if (!x_zero) {
             if ((e = F.op(x, W.w))) return e;
             axpby_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(W.r, W.w, n, -1.0, 1.0);
             count_launches(1);
         }
-        if ((e = F.norm2(W.r, W.scal))) return e;
-        cudaMemcpyAsync(&tmp, W.scal, sizeof(double), cudaMemcpyDeviceToHost, st);
-        if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
-    } else {
-        tmp = rnorm2_final;
+        if ((e = F.norm_init(W.r, W.partial, W.g, W.ctl))) return e;
+        if ((e = S.post(W.ctl, 0)) || (e = S.wait(0, &seen))) return e;
+        rnorm2 = seen.beta2;
     }
     if ((e = F.proj(x, x))) return e;
     if (cudaStreamSynchronize(st) != cudaSuccess) return launch_status("fgmres sync", 0);
     if (mop && (e = mixed_wait_check(st))) return e;
-    rep->true_relres = sqrt(tmp) / bnorm;
+    rep->true_relres = sqrt(rnorm2) / bnorm;
     rep->arnoldi_relres = arnoldi;
     rep->iterations = total;
     F.collect_times();

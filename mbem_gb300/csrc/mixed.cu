@@ -693,10 +693,12 @@ sgemv_df_kernel(const float* __restrict__ A, int64_t ld, int64_t n_rows, int64_t
 }
 
 // y[3f + i] += sum_k vals[k, i, j] x[3 cols[k] + j]: one warp per row block,
-// lanes over its near blocks, fixed-order warp reduction
+// lanes over its near blocks, fixed-order warp reduction. A set *stop (a
+// Krylov step enqueued after its basis ended) makes it return at once.
 __global__ void near_matvec_kernel(const int64_t* __restrict__ rowptr, const int64_t* __restrict__ cols,
                                    const double* __restrict__ vals, int64_t n_field, const double* __restrict__ x,
-                                   double* __restrict__ y) {
+                                   double* __restrict__ y, const int* __restrict__ stop) {
+    if (stop && *stop) return;
     const int64_t f = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x & 31;
     if (f >= n_field) return;
@@ -926,7 +928,7 @@ int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, floa
     for (int q = 0; q < op->n_near; q++) {
         const mbem_near_blocks& nb = op->near[q];
         near_matvec_kernel<<<(unsigned)ceil_div(nb.n_field, 8), 256, 0, st>>>(
-            nb.rowptr, nb.cols, nb.vals, nb.n_field, x + nb.col0, y + nb.row0);
+            nb.rowptr, nb.cols, nb.vals, nb.n_field, x + nb.col0, y + nb.row0, nullptr);
         launches++;
     }
     return launch_status("mixed_matvec", launches);
@@ -948,7 +950,9 @@ int mixed_matvec(const mbem_mixed_operator* op, const double* x, double* y, floa
 template <int R, int CH, int S>
 constexpr size_t bp_smem() { return (size_t)S * (R * CH * 2 + CH * 4) + 2 * S * 8; }
 
-__global__ void d2f_kernel(const double* __restrict__ x, int64_t n, float* __restrict__ xf) {
+__global__ void d2f_kernel(const double* __restrict__ x, int64_t n, float* __restrict__ xf,
+                           const int* __restrict__ stop) {
+    if (stop && *stop) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) xf[i] = (float)x[i];
 }
@@ -959,8 +963,10 @@ __device__ __forceinline__ float bf16_hi(uint32_t u) { return __uint_as_float(u 
 template <int BP_ROWS, int BP_CH, int BP_STAGES>
 __global__ void __launch_bounds__(32 * (BP_ROWS / 2 + 1))
 sgemv_bf16_tma_kernel(const uint16_t* __restrict__ A, int64_t ld, int64_t n_rows, int64_t n_main, int64_t n_cols,
-                      const float* __restrict__ xf, double* __restrict__ y) {
+                      const float* __restrict__ xf, double* __restrict__ y, const int* __restrict__ stop) {
     constexpr int BP_WARPS = BP_ROWS / 2;
+    // the whole CTA leaves before any barrier exists
+    if (stop && *stop) return;
     extern __shared__ __align__(128) unsigned char smem[];
     uint16_t* sA = reinterpret_cast<uint16_t*>(smem);                                // [S][ROWS][CH]
     float* sX = reinterpret_cast<float*>(sA + (size_t)BP_STAGES * BP_ROWS * BP_CH);   // [S][CH]
@@ -1066,24 +1072,24 @@ sgemv_bf16_tma_kernel(const uint16_t* __restrict__ A, int64_t ld, int64_t n_rows
 
 template <int R, int CH, int S>
 static int bf16_tma_launch(const uint16_t* A, int64_t ld, int64_t nr, int64_t n_main, int64_t nc, const float* xf,
-                           double* y, cudaStream_t st) {
+                           double* y, const int* stop, cudaStream_t st) {
     constexpr size_t smem = bp_smem<R, CH, S>();
     static_assert(smem <= 232448, "ring exceeds 227 KB of shared memory");
     const cudaError_t e = cudaFuncSetAttribute(sgemv_bf16_tma_kernel<R, CH, S>,
                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return set_error(MBEM_ERR_CUDA, "bf16 gemv smem attribute: %s", cudaGetErrorString(e));
     sgemv_bf16_tma_kernel<R, CH, S><<<(unsigned)ceil_div(nr, R), 32 * (R / 2 + 1), smem, st>>>(A, ld, nr, n_main,
-                                                                                               nc, xf, y);
+                                                                                               nc, xf, y, stop);
     return MBEM_OK;
 }
 
 // the BF16 matvec with tile configuration `cfg` of kBf16Tiles
 static int launch_bf16_tma(int cfg, const uint16_t* A, int64_t ld, int64_t nr, int64_t n_main, int64_t nc,
-                           const float* xf, double* y, cudaStream_t st) {
+                           const float* xf, double* y, const int* stop, cudaStream_t st) {
 #define MBEM_BF_CASE(i)                                                                                        \
     case i:                                                                                                    \
         return bf16_tma_launch<kBf16Tiles[i].rows, kBf16Tiles[i].ch, kBf16Tiles[i].stages>(A, ld, nr, n_main, nc, \
-                                                                                           xf, y, st);
+                                                                                           xf, y, stop, st);
     static_assert(count_of(kBf16Tiles) == 6, "one case per configuration");
     switch (cfg) {
         MBEM_BF_CASE(0)
@@ -1099,21 +1105,22 @@ static int launch_bf16_tma(int cfg, const uint16_t* A, int64_t ld, int64_t nr, i
 }
 
 int bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_cols, int n_near,
-                const mbem_near_blocks* near, const double* x, double* y, float* xf, cudaStream_t st) {
+                const mbem_near_blocks* near, const double* x, double* y, float* xf, cudaStream_t st,
+                const int* stop) {
     MBEM_REQUIRE(A16 && x && y && xf && n_rows >= 0 && n_cols >= 0 && ld16 >= n_cols, MBEM_ERR_ARG,
                  "bad BF16 matvec args");
     MBEM_REQUIRE((uintptr_t)A16 % 16 == 0 && ld16 % 8 == 0 && (uintptr_t)xf % 16 == 0, MBEM_ERR_ARG,
                  "the BF16 matrix and the scratch must be 16-byte aligned with ld16 %% 8 == 0");
     MBEM_REQUIRE(n_near >= 0 && (n_near == 0 || near), MBEM_ERR_ARG, "bad near blocks");
     if (n_rows == 0) return MBEM_OK;
-    d2f_kernel<<<(unsigned)ceil_div(n_cols > 0 ? n_cols : 1, 256), 256, 0, st>>>(x, n_cols, xf);
+    d2f_kernel<<<(unsigned)ceil_div(n_cols > 0 ? n_cols : 1, 256), 256, 0, st>>>(x, n_cols, xf, stop);
     const int64_t n_main = n_cols & ~(int64_t)7;
-    int e = launch_bf16_tma(tune_get(MBEM_TUNE_BF16_MATVEC), A16, ld16, n_rows, n_main, n_cols, xf, y, st);
+    int e = launch_bf16_tma(tune_get(MBEM_TUNE_BF16_MATVEC), A16, ld16, n_rows, n_main, n_cols, xf, y, stop, st);
     if (e) return e;
     for (int q = 0; q < n_near; q++) {
         const mbem_near_blocks& nb = near[q];
         near_matvec_kernel<<<(unsigned)ceil_div(nb.n_field, 8), 256, 0, st>>>(
-            nb.rowptr, nb.cols, nb.vals, nb.n_field, x + nb.col0, y + nb.row0);
+            nb.rowptr, nb.cols, nb.vals, nb.n_field, x + nb.col0, y + nb.row0, stop);
     }
     return launch_status("bf16_matvec", 2 + n_near);
 }

@@ -62,6 +62,33 @@ def far_near_block(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha:
     order 1/2) in FP64, listed by field point over source nodes.
     ``far16_out``: an optional BF16 view of the same shape that receives the
     far part rounded to BF16 in the same pass."""
+    return near_blocks(far_launch(kernel, x_field, tri_verts, normals, eps, coeffs, alpha, far_out, row0, col0,
+                                  near_factor, timer, far16_out, order))
+
+
+@dataclass
+class FarLaunch:
+    """A far-field block whose kernel is enqueued and whose near list is not
+    read yet (``near_blocks`` reads it: the count is one wait on the stream)."""
+    kernel: int
+    order: int
+    x_field: torch.Tensor
+    tri_verts: torch.Tensor
+    normals: torch.Tensor
+    eps: torch.Tensor
+    coeffs: object
+    alpha: float
+    row0: int
+    col0: int
+    mask: torch.Tensor
+
+
+def far_launch(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha: float,
+               far_out: torch.Tensor, row0: int = 0, col0: int = 0,
+               near_factor: float = defaults.MIXED_NEAR_RADIUS_FACTOR, timer=None,
+               far16_out: torch.Tensor | None = None, order: int = 0) -> FarLaunch:
+    """The far half of ``far_near_block``: enqueues the far-field kernel
+    (which also votes the near pairs into a bit mask) and returns at once."""
     k = _KERNEL_ID[kernel]
     nf, ns = x_field.shape[0], tri_verts.shape[0]
     K = {0: 1, 1: 3, 2: 6}[int(order)]
@@ -87,6 +114,19 @@ def far_near_block(kernel: str, x_field, tri_verts, normals, eps, coeffs, alpha:
     if ev is not None:
         ev[1].record()
         timer.append(("far_" + kernel, nf, ns, ev[0], ev[1]))
+    return FarLaunch(k, int(order), x_field, tri_verts, normals, eps, c, float(alpha), row0, col0, mask)
+
+
+def near_blocks(fl: FarLaunch) -> NearList:
+    """The near half of ``far_near_block``: the near list read from the far
+    kernel's mask and the near blocks evaluated in FP64."""
+    k, c, x_field, tri_verts, normals, eps, alpha = (fl.kernel, fl.coeffs, fl.x_field, fl.tri_verts, fl.normals,
+                                                     fl.eps, fl.alpha)
+    mask, row0, col0 = fl.mask, fl.row0, fl.col0
+    nf, ns = x_field.shape[0], tri_verts.shape[0]
+    K = {0: 1, 1: 3, 2: 6}[fl.order]
+    order = fl.order
+    fl.mask = None
     rowptr = torch.empty(nf + 1, dtype=torch.int64, device=x_field.device)
     work = torch.empty(int(nat.lib().mbem_near_list_workspace_size(nf)), dtype=torch.uint8,
                        device=x_field.device)
