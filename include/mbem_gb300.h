@@ -470,12 +470,6 @@ typedef struct {
     int64_t ld32;                    /* their leading dimension: >= n_coarse, a multiple of 4 */
 } mbem_nn_precond;
 
-/* M (n x n, row-major FP32 at ld >= n, device) = M^-1 in place: Gauss-Jordan with
- * partial pivoting, 16 pivot columns a step (a one-CTA panel, then one
- * rank-16 update of the other columns); n <= 3214 (the panel lives in shared
- * memory). MBEM_ERR_NUMERIC when a column has no usable pivot. Synchronises
- * `stream`. No counterpart in the reference (it solves its small systems with
- * LAPACK on the host). */
 /* The learned preconditioner on the mixed operator: A Phi (FP32) from the
  * BF16 inner operator (its A16 far field and FP64 near blocks), A_c = Phi^T A
  * Phi (+ U U^T from `shift`, n_shift columns, for a calibrated system's
@@ -495,8 +489,39 @@ int mbem_knn(const float* points, int64_t n, int k, int64_t* idx, void* stream);
  * setup where a faster, preconditioner-accurate one serves. */
 int mbem_nn_setup_dense32(const double* A, int64_t ld, const mbem_nn_precond* nn, const double* shift, int n_shift,
                           void* work, size_t work_bytes, void* stream);
+/* M (n x n, row-major FP32 at ld >= n, device) = M^-1 in place. From n = 1024
+ * a blocked Gauss-Jordan without row interchanges is tried first (64-column
+ * blocks: the diagonal block inverted by one CTA, tiled FP32 updates of the
+ * rest); it stands when no pivot was zero or non-finite and |A X v - v| <=
+ * 1e-3 |v| for two fixed vectors v. Otherwise, and below n = 1024, Gauss-
+ * Jordan with partial pivoting, 16 pivot columns a step (a one-CTA panel,
+ * then one rank-16 update of the other columns); n <= 3214 (the panel lives
+ * in shared memory). MBEM_ERR_NUMERIC when a column has no usable pivot.
+ * Synchronises `stream`. No counterpart in the reference (it solves its small
+ * systems with LAPACK on the host). */
 size_t mbem_dense_inverse_f32_workspace_size(int64_t n);
 int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t work_bytes, void* stream);
+/* How many mbem_dense_inverse_f32 calls since the last call stood without
+ * row interchanges, and how many ran the pivoted inverse; resets both. */
+void mbem_dense_inverse_f32_stats(int64_t* no_interchange, int64_t* pivoted);
+/* One level of the principal-axis bisection of points (m x 3 FP64, device)
+ * that makes the block-Jacobi chunks (src/mbem/la/cluster.py:56-75, as
+ * build_cluster_tree splits; the reference runs it on the host with numpy).
+ * Segment s is order[seg_start[s] .. + seg_size[s]); a segment of at most
+ * max_nodes points is a leaf. mbem_cluster_stats writes mean (n_seg x 3) and
+ * stats (n_seg x 10: the count, then the 3 x 3 sums of (p - mean)(p -
+ * mean)^T) of every non-leaf segment; the caller finds each leading
+ * eigenvector (axis, n_seg x 3). mbem_cluster_split writes order_out: every
+ * non-leaf segment partitioned stably into its points with a projection on
+ * the axis below the median (the mean of the two middle order statistics)
+ * and the rest, nl[s] = the left count; a segment with an empty side is
+ * copied unchanged with nl[s] = -1, the projections (proj, m) left for the
+ * caller's rank rule; a leaf is copied with nl[s] = its size. */
+int mbem_cluster_stats(const double* pts, const int64_t* order, const int64_t* seg_start, const int64_t* seg_size,
+                       int64_t n_seg, int max_nodes, double* mean, double* stats, void* stream);
+int mbem_cluster_split(const double* pts, const int64_t* order, int64_t* order_out, const int64_t* seg_start,
+                       const int64_t* seg_size, int64_t n_seg, int max_nodes, const double* mean, const double* axis,
+                       double* proj, int64_t* nl, void* stream);
 /* out (n_items, 9) = MLP(feat (n_items, MBEM_NN_FEAT)); act (n_items, 2H)
  * keeps the hidden activations for training (NULL at inference). */
 int mbem_nn_forward(const float* feat, int64_t n_items, const float* params, float* act, float* out,

@@ -250,6 +250,9 @@ _SIGNATURES = {
     "mbem_knn": (c_int, [_P, _I, c_int, _P, _P]),
     "mbem_dense_inverse_f32_workspace_size": (c_size_t, [_I]),
     "mbem_dense_inverse_f32": (c_int, [_P, _I, _I, _P, c_size_t, _P]),
+    "mbem_dense_inverse_f32_stats": (None, [POINTER(c_int64), POINTER(c_int64)]),
+    "mbem_cluster_stats": (c_int, [_P, _P, _P, _P, _I, c_int, _P, _P, _P]),
+    "mbem_cluster_split": (c_int, [_P, _P, _P, _P, _P, _I, c_int, _P, _P, _P, _P, _P]),
     "mbem_lu_solve_t_f32": (c_int, [_P, _I, _I, _P, _P, _P, _P, _P]),
     "mbem_lu_stats": (None, [c_int, POINTER(c_double)]),
     "mbem_lu_solve_many_workspace_size": (c_size_t, [_I, _I]),

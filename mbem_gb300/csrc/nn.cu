@@ -836,6 +836,225 @@ __global__ void gj_unpermute_kernel(const float* __restrict__ R, float* __restri
 }
 
 // ---------------------------------------------------------------------------
+// Blocked Gauss-Jordan inverse without row interchanges: the first attempt of
+// the FP32 inverse at n >= GJNP_MIN_N. Block columns of GJNP_B; for block K
+// (its rows and columns K, the rest R), with D = M[K, K]:
+//   M[K, K] <- D^-1 (one CTA, D in shared memory),
+//   M[K, R] <- D^-1 M[K, R],
+//   M[R, R] <- M[R, R] - M[R, K] M[K, R]   (a tiled FP32 rank-GJNP_B update),
+//   M[R, K] <- -M[R, K] D^-1,
+// and after the last block M holds A^-1. Without a pivot search a block
+// column costs a few short kernels instead of a pass over every row for each
+// column, but its stability rests on the matrix (the coarse Galerkin matrix
+// of a second-kind operator has dominant diagonal blocks). So a zero or
+// non-finite pivot flags the attempt, the result must satisfy
+// |A X v - v| <= GJNP_CHECK |v| for two fixed vectors v, and otherwise the
+// pivoted inverse runs from the saved copy of A.
+// ---------------------------------------------------------------------------
+constexpr int GJNP_B = 64;
+constexpr int GJNP_MIN_N = 1024;
+constexpr double GJNP_CHECK = 1e-3;
+constexpr int GJNP_TILE = 128;             // update tile: 128 x 128 outputs, 256 threads of 8 x 8
+constexpr size_t GJNP_SMEM = 2 * (size_t)GJNP_B * GJNP_TILE * sizeof(float);
+
+// D^-1 in place in M[K, K] and into Dinv (b x b, row stride GJNP_B)
+__global__ void __launch_bounds__(256)
+gjnp_diag_kernel(float* __restrict__ M, int64_t ld, int64_t k0, int b, float* __restrict__ Dinv,
+                 int* __restrict__ bad) {
+    __shared__ float S[GJNP_B][GJNP_B + 1];
+    __shared__ float prow[GJNP_B], pcol[GJNP_B];
+    for (int e = threadIdx.x; e < GJNP_B * GJNP_B; e += 256) {
+        const int i = e / GJNP_B, c = e % GJNP_B;
+        S[i][c] = (i < b && c < b) ? M[(k0 + i) * ld + k0 + c] : 0.0f;
+    }
+    __syncthreads();
+    for (int t = 0; t < b; t++) {
+        if (threadIdx.x < b) {
+            prow[threadIdx.x] = S[t][threadIdx.x];
+            pcol[threadIdx.x] = S[threadIdx.x][t];
+        }
+        __syncthreads();
+        const float p = prow[t];
+        const bool ok = isfinite(p) && p != 0.0f;
+        if (!ok && threadIdx.x == 0) atomicExch(bad, 1);
+        const float inv = ok ? 1.0f / p : 1.0f;
+        for (int e = threadIdx.x; e < b * b; e += 256) {
+            const int i = e / b, c = e % b;
+            if (i == t) {
+                S[i][c] = (c == t) ? inv : prow[c] * inv;
+            } else {
+                const float g = pcol[i] * inv;
+                S[i][c] = (c == t) ? -g : fmaf(-g, prow[c], S[i][c]);
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < b * b; e += 256) {
+        const int i = e / b, c = e % b;
+        M[(k0 + i) * ld + k0 + c] = S[i][c];
+        Dinv[i * GJNP_B + c] = S[i][c];
+    }
+}
+
+// M[K, j] <- D^-1 M[K, j] for the columns j outside K; a CTA per 64 columns
+__global__ void __launch_bounds__(256)
+gjnp_row_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b, const float* __restrict__ Dinv) {
+    __shared__ float Ds[GJNP_B][GJNP_B + 1];
+    __shared__ float X[GJNP_B][GJNP_B + 1];
+    const int64_t j0 = (int64_t)blockIdx.x * GJNP_B;
+    for (int e = threadIdx.x; e < GJNP_B * GJNP_B; e += 256) {
+        const int r = e / GJNP_B, c = e % GJNP_B;
+        Ds[r][c] = (r < b && c < b) ? Dinv[r * GJNP_B + c] : 0.0f;
+        X[r][c] = (r < b && j0 + c < n) ? M[(k0 + r) * ld + j0 + c] : 0.0f;
+    }
+    __syncthreads();
+    const int c = threadIdx.x & (GJNP_B - 1);
+    const int64_t j = j0 + c;
+    if (j >= n || (j >= k0 && j < k0 + b)) return;
+    for (int r = threadIdx.x / GJNP_B; r < b; r += 256 / GJNP_B) {
+        float acc = 0.0f;
+        for (int t = 0; t < b; t++) acc = fmaf(Ds[r][t], X[t][c], acc);
+        M[(k0 + r) * ld + j] = acc;
+    }
+}
+
+// M[i, K] <- -M[i, K] D^-1 for the rows i outside K; a CTA per 64 rows
+__global__ void __launch_bounds__(256)
+gjnp_col_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b, const float* __restrict__ Dinv) {
+    __shared__ float Ds[GJNP_B][GJNP_B + 1];
+    __shared__ float Y[GJNP_B][GJNP_B + 1];
+    const int64_t i0 = (int64_t)blockIdx.x * GJNP_B;
+    for (int e = threadIdx.x; e < GJNP_B * GJNP_B; e += 256) {
+        const int r = e / GJNP_B, c = e % GJNP_B;
+        Ds[r][c] = (r < b && c < b) ? Dinv[r * GJNP_B + c] : 0.0f;
+        Y[r][c] = (c < b && i0 + r < n) ? M[(i0 + r) * ld + k0 + c] : 0.0f;
+    }
+    __syncthreads();
+    const int c = threadIdx.x & (GJNP_B - 1);
+    if (c >= b) return;
+    for (int r = threadIdx.x / GJNP_B; r < GJNP_B; r += 256 / GJNP_B) {
+        const int64_t i = i0 + r;
+        if (i >= n || (i >= k0 && i < k0 + b)) continue;
+        float acc = 0.0f;
+        for (int t = 0; t < b; t++) acc = fmaf(Y[r][t], Ds[t][c], acc);
+        M[i * ld + k0 + c] = -acc;
+    }
+}
+
+// M[i, j] -= sum_t M[i, k0 + t] M[k0 + t, j] for i, j outside K: a CTA per
+// 128 x 128 tile, the tile's column block and row block in shared memory,
+// each thread 8 x 8 outputs (rows ty*4 + {0..3}, 64 + ty*4 + {0..3}; columns
+// likewise by tx)
+__global__ void __launch_bounds__(256)
+gjnp_update_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b) {
+    extern __shared__ __align__(16) float gsm[];
+    float* As = gsm;                                   // [t][r]
+    float* Bs = gsm + GJNP_B * GJNP_TILE;              // [t][c]
+    const int64_t i0 = (int64_t)blockIdx.y * GJNP_TILE, j0 = (int64_t)blockIdx.x * GJNP_TILE;
+    for (int e = threadIdx.x; e < GJNP_B * GJNP_TILE; e += 256) {
+        const int t = e / GJNP_TILE, r = e % GJNP_TILE;
+        As[e] = (t < b && i0 + r < n) ? M[(i0 + r) * ld + k0 + t] : 0.0f;
+        Bs[e] = (t < b && j0 + r < n) ? M[(k0 + t) * ld + j0 + r] : 0.0f;
+    }
+    __syncthreads();
+    const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[i][j] = 0.0f;
+    for (int t = 0; t < b; t++) {
+        const float4 a0 = *reinterpret_cast<const float4*>(As + t * GJNP_TILE + ty * 4);
+        const float4 a1 = *reinterpret_cast<const float4*>(As + t * GJNP_TILE + 64 + ty * 4);
+        const float4 b0 = *reinterpret_cast<const float4*>(Bs + t * GJNP_TILE + tx * 4);
+        const float4 b1 = *reinterpret_cast<const float4*>(Bs + t * GJNP_TILE + 64 + tx * 4);
+        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int64_t row = i0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+        if (row >= n || (row >= k0 && row < k0 + b)) continue;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int64_t col = j0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+            if (col >= n || (col >= k0 && col < k0 + b)) continue;
+            M[row * ld + col] -= acc[i][j];
+        }
+    }
+}
+
+// the two fixed check vectors: v0 = 1, v1 alternates in sign by a hash of i
+__device__ __forceinline__ double gjnp_v(int64_t i, int q) {
+    if (q == 0) return 1.0;
+    uint32_t h = (uint32_t)i * 2654435761u;
+    h ^= h >> 15;
+    return (h & 1u) ? 1.0 : -1.0;
+}
+
+// y[:, q] = A x[:, q] (x = the check vectors when x is NULL): a warp per
+// row, FP64 sums in a fixed lane order
+__global__ void __launch_bounds__(256)
+gjnp_gemv2_kernel(const float* __restrict__ A, int64_t n, int64_t lda, const double* __restrict__ x,
+                  double* __restrict__ y) {
+    const int64_t row = (int64_t)blockIdx.x * 8 + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double s0 = 0.0, s1 = 0.0;
+    for (int64_t c = lane; c < n; c += 32) {
+        const double a = A[row * lda + c];
+        const double x0 = x ? x[2 * c] : gjnp_v(c, 0), x1 = x ? x[2 * c + 1] : gjnp_v(c, 1);
+        s0 = fma(a, x0, s0);
+        s1 = fma(a, x1, s1);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if (lane == 0) {
+        y[2 * row] = s0;
+        y[2 * row + 1] = s1;
+    }
+}
+
+// out[q] = |y[:, q] - v_q| / |v_q|, one CTA
+__global__ void __launch_bounds__(256)
+gjnp_check_kernel(const double* __restrict__ y, int64_t n, double* __restrict__ out) {
+    __shared__ double red[4][256 / 32];
+    double e0 = 0.0, e1 = 0.0, v0 = 0.0, v1 = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += 256) {
+        const double a = gjnp_v(i, 0), c = gjnp_v(i, 1);
+        const double d0 = y[2 * i] - a, d1 = y[2 * i + 1] - c;
+        e0 += d0 * d0;
+        e1 += d1 * d1;
+        v0 += a * a;
+        v1 += c * c;
+    }
+    double vals[4] = {e0, e1, v0, v1};
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) vals[q] += __shfl_xor_sync(0xffffffffu, vals[q], o);
+        if (lane == 0) red[q][wid] = vals[q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int q = 0; q < 4; q++)
+            for (int w = 0; w < 256 / 32; w++) s[q] += red[q][w];
+        // a non-finite result fails the check
+        out[0] = (s[0] >= 0.0) ? sqrt(s[0] / s[2]) : INFINITY;
+        out[1] = (s[1] >= 0.0) ? sqrt(s[1] / s[3]) : INFINITY;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // apply pieces
 // ---------------------------------------------------------------------------
 // q[6c + k] = sum_{d in c} basis[d][k] r[d]; a CTA per chunk
@@ -1100,6 +1319,70 @@ int mbem_knn(const float* points, int64_t n, int k, int64_t* idx, void* stream) 
     return launch_status("knn_kernel");
 }
 
+}  // extern "C"
+
+namespace mbem {
+
+// inverses that stood without row interchanges, and pivoted ones, since the
+// last mbem_dense_inverse_f32_stats call
+static int64_t g_inverse_counts[2] = {0, 0};
+
+// The blocked inverse without row interchanges: 1 when it passed its checks
+// (M holds A^-1), 0 when the pivoted inverse must run (M holds A again), or
+// minus an error code. R (n x n) keeps the copy of A; scratch holds D^-1,
+// the check's vectors and its result.
+static int gjnp_try(float* M, int64_t n, int64_t ld, float* R, char* scratch, size_t scratch_bytes, int* bad,
+                    cudaStream_t st) {
+    const size_t need = (size_t)GJNP_B * GJNP_B * sizeof(float) + 4 * (size_t)n * sizeof(double) + 64;
+    if (scratch_bytes < need) return 0;
+    float* Dinv = reinterpret_cast<float*>(scratch);
+    double* wv = reinterpret_cast<double*>(scratch + (size_t)GJNP_B * GJNP_B * sizeof(float));
+    double* yv = wv + 2 * n;
+    double* res = yv + 2 * n;
+    cudaError_t ce = cudaFuncSetAttribute(gjnp_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)GJNP_SMEM);
+    if (ce != cudaSuccess) return -set_error(MBEM_ERR_CUDA, "inverse update smem attribute: %s", cudaGetErrorString(ce));
+    cudaMemcpy2DAsync(R, n * sizeof(float), M, ld * sizeof(float), n * sizeof(float), n, cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(bad, 0, sizeof(int), st);
+    const unsigned g64 = (unsigned)ceil_div(n, GJNP_B);
+    const dim3 gt((unsigned)ceil_div(n, GJNP_TILE), (unsigned)ceil_div(n, GJNP_TILE));
+    int launches = 0;
+    for (int64_t k0 = 0; k0 < n; k0 += GJNP_B) {
+        const int b = (int)lmin(GJNP_B, n - k0);
+        gjnp_diag_kernel<<<1, 256, 0, st>>>(M, ld, k0, b, Dinv, bad);
+        gjnp_row_kernel<<<g64, 256, 0, st>>>(M, n, ld, k0, b, Dinv);
+        gjnp_update_kernel<<<gt, 256, GJNP_SMEM, st>>>(M, n, ld, k0, b);
+        gjnp_col_kernel<<<g64, 256, 0, st>>>(M, n, ld, k0, b, Dinv);
+        launches += 4;
+    }
+    // A (X v) against v for the two check vectors
+    gjnp_gemv2_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, st>>>(M, n, ld, nullptr, wv);
+    gjnp_gemv2_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, st>>>(R, n, n, wv, yv);
+    gjnp_check_kernel<<<1, 256, 0, st>>>(yv, n, res);
+    count_launches(launches + 3);
+    int e = launch_status("gauss_jordan_f32 (no interchanges)", 0);
+    if (e) return -e;
+    double hres[2] = {INFINITY, INFINITY};
+    int hbad = 1;
+    cudaMemcpyAsync(hres, res, sizeof(hres), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -launch_status("inverse sync", 0);
+    if (hbad == 0 && hres[0] <= GJNP_CHECK && hres[1] <= GJNP_CHECK) return 1;
+    // back to A for the pivoted inverse
+    cudaMemcpy2DAsync(M, ld * sizeof(float), R, n * sizeof(float), n * sizeof(float), n, cudaMemcpyDeviceToDevice, st);
+    return 0;
+}
+
+}  // namespace mbem
+
+extern "C" {
+
+void mbem_dense_inverse_f32_stats(int64_t* no_interchange, int64_t* pivoted) {
+    if (no_interchange) *no_interchange = g_inverse_counts[0];
+    if (pivoted) *pivoted = g_inverse_counts[1];
+    g_inverse_counts[0] = g_inverse_counts[1] = 0;
+}
+
 size_t mbem_dense_inverse_f32_workspace_size(int64_t n) {
     return (size_t)GJB_BLOCK * n * sizeof(float) + (size_t)n * n * sizeof(float) + (size_t)(2 * n + 8) * sizeof(int) +
            4 * 256;
@@ -1123,6 +1406,17 @@ int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t w
     int* piv = reinterpret_cast<int*>(take((size_t)n * sizeof(int)));
     int* used = reinterpret_cast<int*>(take((size_t)n * sizeof(int)));
     int* bad = reinterpret_cast<int*>(take(sizeof(int)));
+    if (n >= GJNP_MIN_N) {
+        // the inverse without row interchanges first (XB's room as its scratch)
+        const int got = gjnp_try(M, n, ld, R, reinterpret_cast<char*>(XB), (size_t)GJB_BLOCK * n * sizeof(float),
+                                 bad, st);
+        if (got < 0) return -got;
+        if (got == 1) {
+            g_inverse_counts[0]++;
+            return MBEM_OK;
+        }
+    }
+    g_inverse_counts[1]++;
     cudaMemsetAsync(used, 0, n * sizeof(int), st);
     cudaMemsetAsync(bad, 0, sizeof(int), st);
     cudaError_t ce = cudaFuncSetAttribute(gjb_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);

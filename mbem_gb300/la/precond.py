@@ -129,6 +129,67 @@ def cluster_order_device(points: torch.Tensor, max_nodes: int):
     return order, sizes.cpu().numpy()
 
 
+def cluster_order_cuda(points: torch.Tensor, max_nodes: int):
+    """``cluster_order_device``'s tree by the CUDA level kernels
+    (``mbem_cluster_stats`` / ``mbem_cluster_split``: a CTA a segment, the
+    median by an exact radix select, a stable partition): returns the same
+    (order (m,) int64 CUDA, leaf sizes (L,) host int64). A level costs one
+    small copy each way: the segments' sizes and covariances to the host,
+    whose 3 x 3 eigenproblems numpy solves together (so the axes are the
+    host rule's), and their axes back; a segment whose projections coincide
+    at the median is split by rank on the host (the rule's fallback)."""
+    if points.device.type != "cuda":
+        raise ValueError("cluster_order_cuda needs CUDA points")
+    dev = points.device
+    pts = points.to(torch.float64).contiguous()
+    m = int(pts.shape[0])
+    order = torch.arange(m, dtype=torch.int64, device=dev)
+    if m == 0:
+        return order, np.zeros(0, np.int64)
+    other = torch.empty_like(order)
+    proj = torch.empty(m, dtype=torch.float64, device=dev)
+    starts_h = np.zeros(1, np.int64)
+    sizes_h = np.array([m], np.int64)
+    st = stream_handle()
+    while True:
+        S = int(sizes_h.size)
+        starts = torch.from_numpy(starts_h).to(dev)
+        sizes = torch.from_numpy(sizes_h).to(dev)
+        mean = torch.empty((S, 3), dtype=torch.float64, device=dev)
+        stats = torch.empty((S, 10), dtype=torch.float64, device=dev)
+        nat.call("mbem_cluster_stats", ptr(pts), ptr(order), ptr(starts), ptr(sizes), S, int(max_nodes), ptr(mean),
+                 ptr(stats), st)
+        host = stats.cpu().numpy()
+        big = sizes_h > max_nodes
+        if not big.any():
+            break
+        axis = np.zeros((S, 3))
+        _, vecs = np.linalg.eigh(host[big, 1:].reshape(-1, 3, 3))
+        axis[big] = vecs[:, :, -1]
+        nl = torch.empty(S, dtype=torch.int64, device=dev)
+        nat.call("mbem_cluster_split", ptr(pts), ptr(order), ptr(other), ptr(starts), ptr(sizes), S, int(max_nodes),
+                 ptr(mean), ptr(torch.from_numpy(axis).to(dev)), ptr(proj), ptr(nl), st)
+        order, other = other, order
+        nl_h = nl.cpu().numpy()
+        for s_ in np.flatnonzero(nl_h < 0):
+            # coincident projections: the lower half by rank goes left
+            a, n_s = int(starts_h[s_]), int(sizes_h[s_])
+            cur = order[a:a + n_s].cpu().numpy()
+            rank_order = np.argsort(proj[a:a + n_s].cpu().numpy(), kind="stable")
+            left = np.zeros(n_s, bool)
+            left[rank_order[:n_s // 2]] = True
+            order[a:a + n_s] = torch.from_numpy(np.concatenate([cur[left], cur[~left]])).to(dev)
+            nl_h[s_] = n_s // 2
+        n_new = 1 + big.astype(np.int64)
+        new_sizes = np.empty(int(n_new.sum()), np.int64)
+        pos = np.cumsum(n_new) - n_new
+        new_sizes[pos] = np.where(big, nl_h, sizes_h)
+        new_sizes[pos[big] + 1] = (sizes_h - nl_h)[big]
+        sizes_h = new_sizes
+        starts_h = np.concatenate([[0], np.cumsum(sizes_h)[:-1]]).astype(np.int64)
+    return order, sizes_h
+
+
 class BlockJacobi:
     """M^-1 = blockdiag(A[c, c]^-1) over spatial chunks c of every slot.
 
@@ -175,7 +236,7 @@ class BlockJacobi:
     @classmethod
     def from_device_points(cls, n: int, groups, max_nodes: int = MAX_NODES):
         """As the constructor, with the slots' node points as CUDA tensors and
-        the chunks made by ``cluster_order_device`` (no host pass over the
+        the chunks made by ``cluster_order_cuda`` (no host pass over the
         nodes)."""
         if not 1 <= max_nodes <= MAX_NODES:
             raise ValueError(f"max_nodes must be in [1, {MAX_NODES}]")
@@ -183,7 +244,7 @@ class BlockJacobi:
         dev = groups[0][1].device
         dof_parts, sizes_all = [], []
         for off, pts in groups:
-            order, sizes = cluster_order_device(pts.to(torch.float64), max_nodes)
+            order, sizes = cluster_order_cuda(pts, max_nodes)
             # each leaf's nodes ascending, as the host constructor sorts them
             leaf = torch.repeat_interleave(torch.arange(sizes.size, device=dev), torch.from_numpy(sizes).to(dev))
             order = order[torch.argsort(leaf * (pts.shape[0] + 1) + order)]

@@ -1,7 +1,8 @@
 """The mixed solve with the learned two-level preconditioner inside its BF16
 inner solve (``precond="bf16_learned"``) and its pieces:
 
-- ``mbem_dense_inverse_f32`` (blocked Gauss-Jordan, partial pivoting):
+- ``mbem_dense_inverse_f32`` (blocked Gauss-Jordan, without row
+  interchanges where that passes its check, else with partial pivoting):
   M M^-1 = I to FP32 accuracy (5e-4 scaled by the condition), pivoting on a
   permutation, a leading dimension beyond n, a singular matrix refused;
 - ``mbem_nn_setup_mixed``: A Phi of the BF16 inner operator (A16 far field
@@ -42,6 +43,34 @@ def test_dense_inverse_f32(gpu, n, ld):
     err = float((A @ inv - torch.eye(n, dtype=torch.float64)).abs().max())
     cond = float(torch.linalg.cond(A))
     assert err < 5e-4 * max(1.0, cond / 10.0), (err, cond)
+
+
+def _inverse_counts():
+    import ctypes
+    from mbem_gb300 import _native as nat
+    a, b = ctypes.c_int64(0), ctypes.c_int64(0)
+    nat.lib().mbem_dense_inverse_f32_stats(ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
+
+
+@pytest.mark.parametrize("n, ld", [(1024, 1024), (1500, 1504), (3072, 3072)])
+def test_dense_inverse_f32_without_interchanges(gpu, n, ld):
+    """A matrix with dominant diagonal blocks (as the coarse Galerkin matrix
+    has) is inverted without row interchanges, to the same FP32 accuracy;
+    a row-permuted one fails that attempt's check and is inverted with
+    pivoting."""
+    g = torch.Generator(device="cpu").manual_seed(n + 7)
+    A = torch.randn(n, n, generator=g, dtype=torch.float64) / np.sqrt(n) + torch.eye(n, dtype=torch.float64)
+    _inverse_counts()
+    inv = _inverse(A.float().cuda(), ld).double().cpu()
+    assert _inverse_counts() == (1, 0)
+    err = float((A @ inv - torch.eye(n, dtype=torch.float64)).abs().max())
+    assert err < 5e-4 * max(1.0, float(torch.linalg.cond(A)) / 10.0), err
+    P = A[torch.randperm(n, generator=g)]
+    inv = _inverse(P.float().cuda(), ld).double().cpu()
+    assert _inverse_counts() == (0, 1)
+    err = float((P @ inv - torch.eye(n, dtype=torch.float64)).abs().max())
+    assert err < 5e-4 * max(1.0, float(torch.linalg.cond(P)) / 10.0), err
 
 
 def test_dense_inverse_f32_refuses_singular(gpu):
