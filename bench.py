@@ -471,7 +471,7 @@ def headline_accuracy(model, system, eps, x_mixed, arrays, n_readout=32):
                     "solved to the same tolerance (FP64 readout)"}
 
 
-def _precond_for(precision, choice="bf16_inner"):
+def _precond_for(precision, choice="bf16_learned"):
     """The headline solve's preconditioner: for the mixed operator the BF16
     inner solve, with (``bf16_learned``) or without (``bf16_inner``) the
     learned two-level preconditioner inside it; none for FP64 (the
@@ -1312,7 +1312,7 @@ def main():
     ap.add_argument("--skip-tune", action="store_true", help="keep the default tile shapes")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--precond", default="bf16_inner", choices=["bf16_learned", "bf16_inner"],
+    ap.add_argument("--precond", default="bf16_learned", choices=["bf16_learned", "bf16_inner"],
                     help="the mixed headline's preconditioner (the other is timed beside it)")
     ap.add_argument("--skip-variant", action="store_true", help="skip timing the other mixed preconditioner")
     ap.add_argument("--skip-extra", action="store_true",

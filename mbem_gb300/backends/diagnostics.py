@@ -52,13 +52,24 @@ def warn_half_jump_eps(system, eps, jump: str) -> None:
 
 
 def _clearance(points: np.ndarray, mesh, eps_of_element: np.ndarray):
-    """(number of points closer than the clearance limit, smallest d / eps)."""
+    """(number of points closer than the clearance limit, smallest d / eps;
+    inf when none is). A point farther from the mesh's bounding box than the
+    limit times the largest eps cannot count, so only the others go to the
+    exact distance."""
     from ..geometry import distance_to_mesh
     if points.shape[0] == 0 or mesh.n_triangles == 0:
         return 0, np.inf
-    d, idx = distance_to_mesh(points, mesh)
+    limit = defaults.COLLOCATION_FAULT_CLEARANCE_EPS
+    v = np.asarray(mesh.vertices, float)[np.unique(np.asarray(mesh.triangles))]
+    lo, hi = v.min(axis=0), v.max(axis=0)
+    gap = np.maximum(np.maximum(lo - points, points - hi), 0.0)
+    near = np.sqrt((gap * gap).sum(axis=1)) <= limit * float(np.max(eps_of_element))
+    if not near.any():
+        return 0, np.inf
+    d, idx = distance_to_mesh(points[near], mesh)
     ratio = np.asarray(d) / eps_of_element[np.asarray(idx)]
-    return int(np.count_nonzero(ratio < defaults.COLLOCATION_FAULT_CLEARANCE_EPS)), float(ratio.min())
+    count = int(np.count_nonzero(ratio < limit))
+    return count, (float(ratio.min()) if count else np.inf)
 
 
 def _report(found, what: str, where: str, tail: str) -> None:

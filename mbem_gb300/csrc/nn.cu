@@ -535,12 +535,15 @@ knn_kernel(const float* __restrict__ p, int64_t n, int k, int64_t* __restrict__ 
 // A Phi for the BF16 inner operator of the mixed solve (A16 far field plus
 // its FP64 near blocks), stored FP32 at ldp: a CTA per (group of
 // APHI16_GROUP chunks, APHI16_ROWS rows) holds the group's columns and basis
-// rows in shared memory and a warp per row gathers the row's entries on
-// those columns, chunk by chunk (each chunk's columns ascending, so a warp's
-// loads run along the mesh's element runs); every APhi entry has one writer.
-// The near blocks follow as FP32 atomic adds (nn_aphi_near_kernel).
+// rows in shared memory. A warp takes APHI16_RW rows at a time and two
+// chunks at once, sixteen lanes a chunk over its columns (each chunk's
+// columns ascending, so a lane group's loads run along the mesh's element
+// runs); the six basis columns go as three packed pairs (FFMA2), and each
+// chunk's 24 sums close with a four-level shuffle tree over its lanes (fixed
+// order). Every APhi entry has one writer. The near blocks follow as FP32
+// atomic adds (nn_aphi_near_kernel).
 // ---------------------------------------------------------------------------
-constexpr int APHI16_GROUP = 8, APHI16_ROWS = 128;
+constexpr int APHI16_GROUP = 8, APHI16_ROWS = 128, APHI16_RW = 4, APHI16_LG = 16;
 
 __device__ __forceinline__ float aphi_load(const uint16_t* row, int c) {
     return __uint_as_float((uint32_t)row[c] << 16);
@@ -554,61 +557,73 @@ __global__ void __launch_bounds__(256)
 nn_aphi_gather_kernel(const T* __restrict__ A16, int64_t ld16, int64_t n, const int64_t* __restrict__ chunk_ptr,
                       const int64_t* __restrict__ dofs, int64_t n_chunks, const float* __restrict__ basis,
                       float* __restrict__ APhi, int64_t ldp) {
-    extern __shared__ float gsm[];
-    constexpr int RW = 4;                                       // rows a warp, their loads in flight together
+    extern __shared__ __align__(16) float gsm[];
+    constexpr int RW = APHI16_RW, LG = APHI16_LG, NG = 32 / APHI16_LG;
     const int64_t cb = (int64_t)blockIdx.x * APHI16_GROUP;
     const int64_t ce = lmin(n_chunks, cb + APHI16_GROUP);
     const int64_t d0 = chunk_ptr[cb];
     const int m = (int)(chunk_ptr[ce] - d0);
-    float* bs = gsm;                                            // [m][NCV]
+    float2* bs = reinterpret_cast<float2*>(gsm);                // [m][3] pairs of basis columns
     int* col = reinterpret_cast<int*>(gsm + (size_t)m * NCV);   // [m]
     __shared__ int cptr[APHI16_GROUP + 1];
     for (int t = threadIdx.x; t < m; t += 256) {
         const int64_t d = dofs[d0 + t];
         col[t] = (int)d;
 #pragma unroll
-        for (int k = 0; k < NCV; k++) bs[t * NCV + k] = basis[d * NCV + k];
+        for (int p = 0; p < NCV / 2; p++) bs[t * 3 + p] = make_float2(basis[d * NCV + 2 * p], basis[d * NCV + 2 * p + 1]);
     }
     if (threadIdx.x <= ce - cb) cptr[threadIdx.x] = (int)(chunk_ptr[cb + threadIdx.x] - d0);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = lane / LG, gl = lane % LG;
     const int64_t rb = (int64_t)blockIdx.y * APHI16_ROWS;
     const int64_t r1 = lmin(n, rb + APHI16_ROWS);
     for (int64_t r0 = rb + (int64_t)warp * RW; r0 < r1; r0 += 8 * RW) {
         const T* Ar[RW];
 #pragma unroll
         for (int q = 0; q < RW; q++) Ar[q] = A16 + lmin(r0 + q, n - 1) * ld16;
-        for (int64_t c = cb; c < ce; c++) {
-            const int lo = cptr[c - cb], hi = cptr[c - cb + 1];
-            float acc[RW][NCV];
+        for (int64_t c0 = cb; c0 < ce; c0 += NG) {
+            const int64_t c = c0 + grp;
+            const bool cv = c < ce;
+            const int lo = cv ? cptr[c - cb] : 0, hi = cv ? cptr[c - cb + 1] : 0;
+            float2 acc[RW][NCV / 2];
 #pragma unroll
             for (int q = 0; q < RW; q++)
 #pragma unroll
-                for (int k = 0; k < NCV; k++) acc[q][k] = 0.f;
-            for (int t = lo + lane; t < hi; t += 32) {
+                for (int p = 0; p < NCV / 2; p++) acc[q][p] = make_float2(0.f, 0.f);
+            for (int t = lo + gl; t < hi; t += LG) {
                 const int cc = col[t];
                 float v[RW];
 #pragma unroll
                 for (int q = 0; q < RW; q++) v[q] = aphi_load(Ar[q], cc);
 #pragma unroll
-                for (int k = 0; k < NCV; k++) {
-                    const float b = bs[t * NCV + k];
+                for (int p = 0; p < NCV / 2; p++) {
+                    const float2 b = bs[t * 3 + p];
 #pragma unroll
-                    for (int q = 0; q < RW; q++) acc[q][k] = fmaf(v[q], b, acc[q][k]);
+                    for (int q = 0; q < RW; q++) acc[q][p] = __ffma2_rn(make_float2(v[q], v[q]), b, acc[q][p]);
                 }
             }
+            // the group's lanes: a fixed xor tree; every lane ends with the sums
 #pragma unroll
             for (int q = 0; q < RW; q++)
 #pragma unroll
-                for (int k = 0; k < NCV; k++)
+                for (int p = 0; p < NCV / 2; p++)
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) acc[q][k] += __shfl_xor_sync(0xffffffffu, acc[q][k], o);
-            // lane q * NCV + k writes row r0 + q, coarse column NCV c + k
+                    for (int o = LG / 2; o > 0; o >>= 1) {
+                        acc[q][p].x += __shfl_xor_sync(0xffffffffu, acc[q][p].x, o);
+                        acc[q][p].y += __shfl_xor_sync(0xffffffffu, acc[q][p].y, o);
+                    }
+            // output e = q * NCV + k (24 of them) is written by the group's lane e % LG
+            if (cv) {
 #pragma unroll
-            for (int q = 0; q < RW; q++)
+                for (int q = 0; q < RW; q++)
 #pragma unroll
-                for (int k = 0; k < NCV; k++)
-                    if (lane == q * NCV + k && r0 + q < r1) APhi[(r0 + q) * ldp + NCV * c + k] = acc[q][k];
+                    for (int k = 0; k < NCV; k++) {
+                        const int e = q * NCV + k;
+                        if (gl == e % LG && r0 + q < r1)
+                            APhi[(r0 + q) * ldp + NCV * c + k] = (k & 1) ? acc[q][k / 2].y : acc[q][k / 2].x;
+                    }
+            }
         }
     }
 }
@@ -857,42 +872,56 @@ constexpr double GJNP_CHECK = 1e-3;
 constexpr int GJNP_TILE = 128;             // update tile: 128 x 128 outputs, 256 threads of 8 x 8
 constexpr size_t GJNP_SMEM = 2 * (size_t)GJNP_B * GJNP_TILE * sizeof(float);
 
-// D^-1 in place in M[K, K] and into Dinv (b x b, row stride GJNP_B)
+// D^-1 in place in M[K, K] and into Dinv (b x b, row stride GJNP_B). Thread
+// (c, g) holds column c's rows 16 g .. 16 g + 15 in registers; a block of
+// b < GJNP_B rows is padded with the identity, whose pivot steps change
+// nothing. The row and the column of pivot t go through shared memory,
+// double-buffered, so a step has one barrier.
 __global__ void __launch_bounds__(256)
 gjnp_diag_kernel(float* __restrict__ M, int64_t ld, int64_t k0, int b, float* __restrict__ Dinv,
                  int* __restrict__ bad) {
-    __shared__ float S[GJNP_B][GJNP_B + 1];
-    __shared__ float prow[GJNP_B], pcol[GJNP_B];
-    for (int e = threadIdx.x; e < GJNP_B * GJNP_B; e += 256) {
-        const int i = e / GJNP_B, c = e % GJNP_B;
-        S[i][c] = (i < b && c < b) ? M[(k0 + i) * ld + k0 + c] : 0.0f;
+    __shared__ float prow[2][GJNP_B], pcol[2][GJNP_B];
+    const int c = threadIdx.x & (GJNP_B - 1), g = threadIdx.x / GJNP_B;
+    float v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        const int i = 16 * g + j;
+        v[j] = (i < b && c < b) ? M[(k0 + i) * ld + k0 + c] : (i == c ? 1.0f : 0.0f);
     }
-    __syncthreads();
-    for (int t = 0; t < b; t++) {
-        if (threadIdx.x < b) {
-            prow[threadIdx.x] = S[t][threadIdx.x];
-            pcol[threadIdx.x] = S[threadIdx.x][t];
+    int flag = 0;
+#pragma unroll
+    for (int t = 0; t < GJNP_B; t++) {
+        const int buf = t & 1;
+        if (g == t / 16) prow[buf][c] = v[t % 16];
+        if (c == t) {
+#pragma unroll
+            for (int j = 0; j < 16; j++) pcol[buf][16 * g + j] = v[j];
         }
         __syncthreads();
-        const float p = prow[t];
+        const float p = prow[buf][t];
         const bool ok = isfinite(p) && p != 0.0f;
-        if (!ok && threadIdx.x == 0) atomicExch(bad, 1);
+        flag |= !ok;
         const float inv = ok ? 1.0f / p : 1.0f;
-        for (int e = threadIdx.x; e < b * b; e += 256) {
-            const int i = e / b, c = e % b;
+        const float rc = prow[buf][c];
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            const int i = 16 * g + j;
             if (i == t) {
-                S[i][c] = (c == t) ? inv : prow[c] * inv;
+                v[j] = (c == t) ? inv : rc * inv;
             } else {
-                const float g = pcol[i] * inv;
-                S[i][c] = (c == t) ? -g : fmaf(-g, prow[c], S[i][c]);
+                const float gg = pcol[buf][i] * inv;
+                v[j] = (c == t) ? -gg : fmaf(-gg, rc, v[j]);
             }
         }
-        __syncthreads();
     }
-    for (int e = threadIdx.x; e < b * b; e += 256) {
-        const int i = e / b, c = e % b;
-        M[(k0 + i) * ld + k0 + c] = S[i][c];
-        Dinv[i * GJNP_B + c] = S[i][c];
+    if (flag && threadIdx.x == 0) atomicExch(bad, 1);
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        const int i = 16 * g + j;
+        if (i < b && c < b) {
+            M[(k0 + i) * ld + k0 + c] = v[j];
+            Dinv[i * GJNP_B + c] = v[j];
+        }
     }
 }
 
