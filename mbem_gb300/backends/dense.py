@@ -268,6 +268,14 @@ class AssembledDense:
         return far_launch(name, f["coll"], s["tv"], s["normals"], s["eps"], coeffs, alpha, far_out, row0, col0,
                           self.near_factor, self._timer, far16_out, p.order)
 
+    @staticmethod
+    def _side_stream():
+        dev = torch.cuda.current_device()
+        side = _SIDE_STREAMS.get(dev)
+        if side is None:
+            side = _SIDE_STREAMS[dev] = torch.cuda.Stream(priority=-1)
+        return side
+
     def _warn_on_side_stream(self):
         """The assembly warnings (their distance kernels and reads) on a
         high-priority side stream, so that they overlap the kernels already
@@ -276,13 +284,33 @@ class AssembledDense:
         if not self._warn_pending:
             return
         self._warn_pending = False
-        dev = torch.cuda.current_device()
-        side = _SIDE_STREAMS.get(dev)
-        if side is None:
-            side = _SIDE_STREAMS[dev] = torch.cuda.Stream(priority=-1)
+        side = self._side_stream()
         with torch.cuda.stream(side):
             warn_assembly(self.system, self.eps, self.jump)
         side.synchronize()
+
+    def _learned_geometry_on_side_stream(self, arrays_ready):
+        """The learned preconditioner's mesh-only setup (the block-Jacobi
+        chunks, the node features, the network's coarse vectors) on the side
+        stream, behind the device mesh arrays (``arrays_ready``) but beside
+        the far-field kernels; ``block_jacobi`` and ``bf16_learned`` make
+        the current stream wait for it."""
+        from ..la.learned import LearnedGeometry
+        from ..la.precond import MAX_NODES, BlockJacobi
+        from ..la.train_learned import load_default
+        main = torch.cuda.current_stream()
+        side = self._side_stream()
+        side.wait_event(arrays_ready)
+        with torch.cuda.stream(side):
+            groups = [(s_.offset, self._patch_arrays(s_.patch)["coll"].view(-1, 3)) for s_ in self.layout.slots]
+            bj = BlockJacobi.from_device_points(self.layout.n_unknowns, groups, MAX_NODES)
+            geo = LearnedGeometry(self, bj, load_default())
+            done = torch.cuda.Event()
+            done.record(side)
+        # made on the side stream, used and freed behind the current one
+        for t in (bj._ptr, bj._dofs, bj._local, bj._chunk_of, bj.inv, *geo.tensors()):
+            t.record_stream(main)
+        self._pending_geometry = (bj, geo, done)
 
     def _build_mixed(self):
         from ..la.mixed import MixedOperator, near_blocks
@@ -311,8 +339,13 @@ class AssembledDense:
                 raise NotImplementedError("mixed precision: FAULT_TRACTION rows of an order > 0 fault")
         terms = [t for t in self.system.terms if t.row.offset not in trac]
         trac_terms = [t for t in self.system.terms if t.row.offset in trac]
-        # every far-field kernel is enqueued first; the assembly warnings run
-        # on a side stream while they work, then the near lists are read
+        # every far-field kernel is enqueued first; the assembly warnings (and,
+        # for the learned preconditioner, its mesh-only setup) run on a side
+        # stream while they work, then the near lists are read
+        for s_ in self.layout.slots:
+            self._patch_arrays(s_.patch)
+        arrays_ready = torch.cuda.Event()
+        arrays_ready.record()
         launched = []
         for t in terms:
             mat = self.materials[t.region.name]
@@ -321,6 +354,9 @@ class AssembledDense:
             launched.append(self._mixed_launch(view, t.field_patch, t.source_patch, t.kernel, mat, t.scale,
                                                t.row.offset, t.col.offset, view16))
         self._warn_on_side_stream()
+        self._pending_geometry = None
+        if self.precond == "bf16_learned":
+            self._learned_geometry_on_side_stream(arrays_ready)
         for t, fl in zip(terms, launched):
             nl = near_blocks(fl)
             op.near.append(nl)
@@ -577,6 +613,12 @@ class AssembledDense:
         the chunks are made on the device from the device mesh arrays
         (``BlockJacobi.from_device_points``)."""
         from ..la.precond import MAX_NODES, BlockJacobi
+        pend = getattr(self, "_pending_geometry", None)
+        if self._bj is None and pend is not None and max_nodes in (None, MAX_NODES) and self.op is not None:
+            bj, _, done = pend
+            torch.cuda.current_stream().wait_event(done)
+            self._bj_nodes = MAX_NODES
+            self._bj = bj.build_mixed(self.op)
         if self._bj is None or (max_nodes is not None and max_nodes != self._bj_nodes):
             self._bj_nodes = MAX_NODES if max_nodes is None else max_nodes
             groups = [(s.offset, self.device_patch_arrays(s.patch)["coll"].view(-1, 3)) for s in self.layout.slots]
@@ -621,7 +663,13 @@ class AssembledDense:
         from ..la.train_learned import load_default
         inner = self.bf16_inner()
         if getattr(self, "_learned", None) is None or params is not None:
-            self._learned = LearnedPreconditioner(self, load_default() if params is None else params)
+            pend = getattr(self, "_pending_geometry", None)
+            if params is None and pend is not None:
+                bj = self.block_jacobi()
+                geo = pend[1] if bj is pend[0] else None
+                self._learned = LearnedPreconditioner(self, load_default(), bj=bj, geometry=geo)
+            else:
+                self._learned = LearnedPreconditioner(self, load_default() if params is None else params)
         inner.set_preconditioner(self._learned)
         return inner
 

@@ -197,16 +197,46 @@ def mlp_forward(feat: torch.Tensor, params: torch.Tensor, act: torch.Tensor | No
 # ---------------------------------------------------------------------------
 # the preconditioner (inference)
 # ---------------------------------------------------------------------------
+class LearnedGeometry:
+    """The mesh-only half of the learned preconditioner's setup, on the
+    stream current when it is made: the network's input features, its
+    coarse vectors phi, the chunk bases and, for a deflated system, the
+    translation shift. ``bj``: the block-Jacobi chunks (their inverses may
+    come later)."""
+
+    def __init__(self, asm, bj, params, setup: str = "fp32"):
+        dev = bj.device
+        n = bj.n
+        nc = 6 * bj.n_chunks
+        self.params = torch.as_tensor(np.asarray(params, np.float32)).to(dev)
+        if setup == "fp32":
+            self.feat = node_features_device(asm, bj)
+        else:
+            self.feat = torch.from_numpy(node_features(asm.layout, bj.chunk_nodes())).to(dev)
+        self.phi = mlp_forward(self.feat, self.params)
+        self.basis = torch.empty((n, 6), dtype=torch.float32, device=dev)
+        rng = np.ascontiguousarray(np.asarray(asm.u_ranges(), dtype=np.int64).reshape(-1))
+        self.shift = torch.zeros((nc, 3), dtype=torch.float64, device=dev) if rng.size else None
+        nat.call("mbem_nn_basis", ctypes.byref(bj.struct()), ptr(self.phi),
+                 rng.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) if rng.size else None, len(rng) // 2,
+                 ptr(self.basis), ptr(self.shift) if self.shift is not None else None, stream_handle())
+
+    def tensors(self) -> list:
+        return [t for t in (self.params, self.feat, self.phi, self.basis, self.shift) if t is not None]
+
+
 class LearnedPreconditioner:
     """Block-Jacobi with the learned coarse space for one assembled FP64
     system. ``params``: the trained network (FP32, MBEM_NN_PARAMS)."""
 
     PRECOND_KIND = 2
 
-    def __init__(self, asm, params, bj=None, setup: str = "fp32"):
+    def __init__(self, asm, params, bj=None, setup: str = "fp32", geometry: LearnedGeometry | None = None):
         """``setup``: "fp32" (the default: device node features, A Phi with
         FP32 products, FP32 coarse inverse) or "fp64" (host features, FP64 A
-        Phi and Gauss-Jordan; a dense FP64 system only)."""
+        Phi and Gauss-Jordan; a dense FP64 system only). ``geometry``: the
+        mesh-only half made beforehand (``LearnedGeometry`` of the same
+        chunks and parameters), else made here."""
         if setup not in ("fp32", "fp64"):
             raise ValueError(f"setup must be 'fp32' or 'fp64' (got {setup!r})")
         mixed = asm.A is None
@@ -220,19 +250,10 @@ class LearnedPreconditioner:
         nc = 6 * self.bj.n_chunks
         import time
         t0 = time.perf_counter()
-        self.params = torch.as_tensor(np.asarray(params, np.float32)).to(dev)
-        if setup == "fp32":
-            self.feat = node_features_device(asm, self.bj)
-        else:
-            self.feat = torch.from_numpy(node_features(asm.layout, self.bj.chunk_nodes())).to(dev)
+        geo = geometry if geometry is not None else LearnedGeometry(asm, self.bj, params, setup)
+        self.params, self.feat, self.phi, self.basis = geo.params, geo.feat, geo.phi, geo.basis
+        shift = geo.shift
         t1 = time.perf_counter()
-        self.phi = mlp_forward(self.feat, self.params)
-        self.basis = torch.empty((n, 6), dtype=torch.float32, device=dev)
-        rng = np.ascontiguousarray(np.asarray(asm.u_ranges(), dtype=np.int64).reshape(-1))
-        shift = torch.zeros((nc, 3), dtype=torch.float64, device=dev) if rng.size else None
-        nat.call("mbem_nn_basis", ctypes.byref(self.bj.struct()), ptr(self.phi),
-                 rng.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) if rng.size else None, len(rng) // 2,
-                 ptr(self.basis), ptr(shift) if shift is not None else None, stream_handle())
         self.work = torch.empty(nat.lib().mbem_nn_apply_workspace_size(n, nc) // 8 + 1, dtype=torch.float64,
                                 device=dev)
         self._bj_struct = self.bj.struct()
@@ -245,17 +266,16 @@ class LearnedPreconditioner:
         self._struct = nat.NnPrecond(n=n, n_coarse=nc, bj=ctypes.pointer(self._bj_struct), basis=ptr(self.basis),
                                      APhi=ptr(self.APhi), Ac_inv=ptr(self.Ac_inv), work=ptr(self.work))
         A = asm.A
-        torch.cuda.synchronize()
         t2 = time.perf_counter()
         nat.call("mbem_nn_coarse_operator_dense", ptr(A), A.stride(0), ctypes.byref(self._struct),
                  ptr(shift) if shift is not None else None, 0 if shift is None else shift.shape[1], st)
-        torch.cuda.synchronize()
         t3 = time.perf_counter()
         need = nat.lib().mbem_dense_inverse_workspace_size(nc)
         inv_work = torch.empty(need, dtype=torch.uint8, device=dev)
         nat.call("mbem_dense_inverse", ptr(self.Ac_inv), nc, ptr(inv_work), need, st)
         self.built = True
         t4 = time.perf_counter()
+        # host times (the kernels run behind them; the inverse synchronises)
         self.setup_s = {"features_host": t1 - t0, "basis_device": t2 - t1, "coarse_operator_device": t3 - t2,
                         "coarse_inverse_device": t4 - t3}
 
@@ -265,7 +285,6 @@ class LearnedPreconditioner:
         (mbem_nn_setup_dense32), A_c and its FP32 inverse."""
         import time
         inner = asm.bf16_inner() if asm.A is None else None
-        torch.cuda.synchronize()
         t1 = time.perf_counter()
         ld32 = (nc + 3) // 4 * 4
         self.APhi = self.Ac_inv = None
@@ -276,7 +295,6 @@ class LearnedPreconditioner:
                                      Ac_inv32=ptr(self.Ac_inv32), ld32=ld32)
         need = int(nat.lib().mbem_dense_inverse_f32_workspace_size(nc))
         inv_work = torch.empty(need, dtype=torch.uint8, device=dev)
-        torch.cuda.synchronize()
         t2 = time.perf_counter()
         sh = (ptr(shift) if shift is not None else None, 0 if shift is None else shift.shape[1])
         if inner is not None:
@@ -292,6 +310,7 @@ class LearnedPreconditioner:
                      need, st)
         self.built = True
         t3 = time.perf_counter()
+        # host times: the inverse synchronises, so the last holds the device work queued before it
         self.setup_s = {"features_device": t1 - t0, "basis_device": t2 - t1, "coarse_operator_and_inverse": t3 - t2}
 
     def struct(self):
