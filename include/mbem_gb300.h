@@ -491,8 +491,8 @@ int mbem_nn_setup_dense32(const double* A, int64_t ld, const mbem_nn_precond* nn
                           void* work, size_t work_bytes, void* stream);
 /* M (n x n, row-major FP32 at ld >= n, device) = M^-1 in place. From n = 1024
  * a blocked Gauss-Jordan without row interchanges is tried first (64-column
- * blocks: the diagonal block inverted by one CTA, tiled FP32 updates of the
- * rest); it stands when no pivot was zero or non-finite and |A X v - v| <=
+ * blocks: the diagonal block inverted by one CTA, the rest updated on the
+ * tensor cores with both factors in three BF16 pieces); it stands when no pivot was zero or non-finite and |A X v - v| <=
  * 1e-3 |v| for two fixed vectors v. Otherwise, and below n = 1024, Gauss-
  * Jordan with partial pivoting, 16 pivot columns a step (a one-CTA panel,
  * then one rank-16 update of the other columns); n <= 3214 (the panel lives

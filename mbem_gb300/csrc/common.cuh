@@ -66,6 +66,11 @@ int bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t n_col
 // z = the BF16 inner GMRES solve of r (precond kind 3).
 int inner_bf16_apply(const void* state, const double* r, double* z, cudaStream_t st);
 
+// The rank-b (b <= 64) update of a blocked Gauss-Jordan inverse of the FP32 n x n
+// M at ld: M[i, j] -= M[i, K] M[K, j] for i, j outside K = [k0, k0 + b), on the
+// tensor cores (six BF16 piece products); Ls, Us: n x 384 BF16 each (scratch).
+int gj_block_update_tc(float* M, int64_t n, int64_t ld, int64_t k0, int b, uint16_t* Ls, uint16_t* Us,
+                       cudaStream_t st);
 // C[M x N] -= A[M x K] B[N x K]^T on the tensor cores (BF16 operands, FP32 C).
 int gemm_bf16_sub(const void* A, int64_t lda, const void* Bt, int64_t ldb, int64_t M, int64_t N, int64_t K, float* C,
                   int64_t ldc, cudaStream_t st);

@@ -331,6 +331,23 @@ static int lu_block_update(float* A, int64_t lda, int64_t row0, int64_t col0, in
     return gemm_bf16_sub(Ls, 6 * W, Us, 6 * W, M, N, 6 * W, C, ldc, st);
 }
 
+// The rank-b update of a blocked Gauss-Jordan inverse (FP32 M, n x n at ld),
+// in place: M[i, j] -= M[i, K] M[K, j] for i, j outside K = [k0, k0 + b),
+// with M[:, K] the block column before its own update and M[K, :] the block
+// row after it. The six-piece tensor-core product of lu_block_update, with
+// the pieces of the rows K of the column block and of the columns K of the
+// row block set to zero, so that those rows and columns are left as they are.
+int gj_block_update_tc(float* M, int64_t n, int64_t ld, int64_t k0, int b, uint16_t* Ls, uint16_t* Us,
+                       cudaStream_t st) {
+    MBEM_REQUIRE(b >= 1 && b <= LU_NB && k0 >= 0 && k0 + b <= n, MBEM_ERR_ARG, "bad Gauss-Jordan block");
+    lu_split_rows_kernel<LU_NB><<<(unsigned)ceil_div(n * LU_NB, 256), 256, 0, st>>>(M, ld, 0, k0, b, n, Ls);
+    lu_split_cols_kernel<LU_NB><<<(unsigned)ceil_div(n, 32), 256, 0, st>>>(M, ld, k0, 0, b, n, Us);
+    cudaMemsetAsync(Ls + k0 * LU_K6, 0, (size_t)b * LU_K6 * sizeof(uint16_t), st);
+    cudaMemsetAsync(Us + k0 * LU_K6, 0, (size_t)b * LU_K6 * sizeof(uint16_t), st);
+    count_launches(2);
+    return gemm_bf16_sub(Ls, LU_K6, Us, LU_K6, n, n, LU_K6, M, ld, st);
+}
+
 // X[r0 .. r0 + nb) (ncols columns at ldx) = T^-1 X with T the nb x nb
 // diagonal block of LU at (r0, r0): its unit lower triangle (lower) or its
 // upper triangle; one thread a column

@@ -856,7 +856,9 @@ __global__ void gj_unpermute_kernel(const float* __restrict__ R, float* __restri
 // (its rows and columns K, the rest R), with D = M[K, K]:
 //   M[K, K] <- D^-1 (one CTA, D in shared memory),
 //   M[K, R] <- D^-1 M[K, R],
-//   M[R, R] <- M[R, R] - M[R, K] M[K, R]   (a tiled FP32 rank-GJNP_B update),
+//   M[R, R] <- M[R, R] - M[R, K] M[K, R]   (on the tensor cores: both blocks
+//                                           in three BF16 pieces, six piece
+//                                           products, FP32 accumulation),
 //   M[R, K] <- -M[R, K] D^-1,
 // and after the last block M holds A^-1. Without a pivot search a block
 // column costs a few short kernels instead of a pass over every row for each
@@ -869,8 +871,7 @@ __global__ void gj_unpermute_kernel(const float* __restrict__ R, float* __restri
 constexpr int GJNP_B = 64;
 constexpr int GJNP_MIN_N = 1024;
 constexpr double GJNP_CHECK = 1e-3;
-constexpr int GJNP_TILE = 128;             // update tile: 128 x 128 outputs, 256 threads of 8 x 8
-constexpr size_t GJNP_SMEM = 2 * (size_t)GJNP_B * GJNP_TILE * sizeof(float);
+constexpr int GJNP_K6 = 6 * GJNP_B;         // the update's K: six BF16 pieces of each block
 
 // D^-1 in place in M[K, K] and into Dinv (b x b, row stride GJNP_B). Thread
 // (c, g) holds column c's rows 16 g .. 16 g + 15 in registers; a block of
@@ -967,53 +968,6 @@ gjnp_col_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b,
         float acc = 0.0f;
         for (int t = 0; t < b; t++) acc = fmaf(Y[r][t], Ds[t][c], acc);
         M[i * ld + k0 + c] = -acc;
-    }
-}
-
-// M[i, j] -= sum_t M[i, k0 + t] M[k0 + t, j] for i, j outside K: a CTA per
-// 128 x 128 tile, the tile's column block and row block in shared memory,
-// each thread 8 x 8 outputs (rows ty*4 + {0..3}, 64 + ty*4 + {0..3}; columns
-// likewise by tx)
-__global__ void __launch_bounds__(256)
-gjnp_update_kernel(float* __restrict__ M, int64_t n, int64_t ld, int64_t k0, int b) {
-    extern __shared__ __align__(16) float gsm[];
-    float* As = gsm;                                   // [t][r]
-    float* Bs = gsm + GJNP_B * GJNP_TILE;              // [t][c]
-    const int64_t i0 = (int64_t)blockIdx.y * GJNP_TILE, j0 = (int64_t)blockIdx.x * GJNP_TILE;
-    for (int e = threadIdx.x; e < GJNP_B * GJNP_TILE; e += 256) {
-        const int t = e / GJNP_TILE, r = e % GJNP_TILE;
-        As[e] = (t < b && i0 + r < n) ? M[(i0 + r) * ld + k0 + t] : 0.0f;
-        Bs[e] = (t < b && j0 + r < n) ? M[(k0 + t) * ld + j0 + r] : 0.0f;
-    }
-    __syncthreads();
-    const int ty = threadIdx.x / 16, tx = threadIdx.x % 16;
-    float acc[8][8];
-#pragma unroll
-    for (int i = 0; i < 8; i++)
-#pragma unroll
-        for (int j = 0; j < 8; j++) acc[i][j] = 0.0f;
-    for (int t = 0; t < b; t++) {
-        const float4 a0 = *reinterpret_cast<const float4*>(As + t * GJNP_TILE + ty * 4);
-        const float4 a1 = *reinterpret_cast<const float4*>(As + t * GJNP_TILE + 64 + ty * 4);
-        const float4 b0 = *reinterpret_cast<const float4*>(Bs + t * GJNP_TILE + tx * 4);
-        const float4 b1 = *reinterpret_cast<const float4*>(Bs + t * GJNP_TILE + 64 + tx * 4);
-        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-        for (int i = 0; i < 8; i++)
-#pragma unroll
-            for (int j = 0; j < 8; j++) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
-    }
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const int64_t row = i0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
-        if (row >= n || (row >= k0 && row < k0 + b)) continue;
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const int64_t col = j0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
-            if (col >= n || (col >= k0 && col < k0 + b)) continue;
-            M[row * ld + col] -= acc[i][j];
-        }
     }
 }
 
@@ -1360,29 +1314,26 @@ static int64_t g_inverse_counts[2] = {0, 0};
 // (M holds A^-1), 0 when the pivoted inverse must run (M holds A again), or
 // minus an error code. R (n x n) keeps the copy of A; scratch holds D^-1,
 // the check's vectors and its result.
-static int gjnp_try(float* M, int64_t n, int64_t ld, float* R, char* scratch, size_t scratch_bytes, int* bad,
-                    cudaStream_t st) {
+static int gjnp_try(float* M, int64_t n, int64_t ld, float* R, char* scratch, size_t scratch_bytes, uint16_t* Ls,
+                    uint16_t* Us, int* bad, cudaStream_t st) {
     const size_t need = (size_t)GJNP_B * GJNP_B * sizeof(float) + 4 * (size_t)n * sizeof(double) + 64;
     if (scratch_bytes < need) return 0;
     float* Dinv = reinterpret_cast<float*>(scratch);
     double* wv = reinterpret_cast<double*>(scratch + (size_t)GJNP_B * GJNP_B * sizeof(float));
     double* yv = wv + 2 * n;
     double* res = yv + 2 * n;
-    cudaError_t ce = cudaFuncSetAttribute(gjnp_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)GJNP_SMEM);
-    if (ce != cudaSuccess) return -set_error(MBEM_ERR_CUDA, "inverse update smem attribute: %s", cudaGetErrorString(ce));
     cudaMemcpy2DAsync(R, n * sizeof(float), M, ld * sizeof(float), n * sizeof(float), n, cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(bad, 0, sizeof(int), st);
     const unsigned g64 = (unsigned)ceil_div(n, GJNP_B);
-    const dim3 gt((unsigned)ceil_div(n, GJNP_TILE), (unsigned)ceil_div(n, GJNP_TILE));
     int launches = 0;
     for (int64_t k0 = 0; k0 < n; k0 += GJNP_B) {
         const int b = (int)lmin(GJNP_B, n - k0);
         gjnp_diag_kernel<<<1, 256, 0, st>>>(M, ld, k0, b, Dinv, bad);
         gjnp_row_kernel<<<g64, 256, 0, st>>>(M, n, ld, k0, b, Dinv);
-        gjnp_update_kernel<<<gt, 256, GJNP_SMEM, st>>>(M, n, ld, k0, b);
+        const int e = gj_block_update_tc(M, n, ld, k0, b, Ls, Us, st);
+        if (e) return -e;
         gjnp_col_kernel<<<g64, 256, 0, st>>>(M, n, ld, k0, b, Dinv);
-        launches += 4;
+        launches += 3;
     }
     // A (X v) against v for the two check vectors
     gjnp_gemv2_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, st>>>(M, n, ld, nullptr, wv);
@@ -1413,8 +1364,9 @@ void mbem_dense_inverse_f32_stats(int64_t* no_interchange, int64_t* pivoted) {
 }
 
 size_t mbem_dense_inverse_f32_workspace_size(int64_t n) {
+    const size_t pieces = n >= GJNP_MIN_N ? 2 * (((size_t)n * GJNP_K6 * sizeof(uint16_t) + 255) & ~(size_t)255) : 0;
     return (size_t)GJB_BLOCK * n * sizeof(float) + (size_t)n * n * sizeof(float) + (size_t)(2 * n + 8) * sizeof(int) +
-           4 * 256;
+           4 * 256 + pieces;
 }
 
 int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t work_bytes, void* stream) {
@@ -1437,8 +1389,10 @@ int mbem_dense_inverse_f32(float* M, int64_t n, int64_t ld, void* work, size_t w
     int* bad = reinterpret_cast<int*>(take(sizeof(int)));
     if (n >= GJNP_MIN_N) {
         // the inverse without row interchanges first (XB's room as its scratch)
+        uint16_t* Ls = reinterpret_cast<uint16_t*>(take((size_t)n * GJNP_K6 * sizeof(uint16_t)));
+        uint16_t* Us = reinterpret_cast<uint16_t*>(take((size_t)n * GJNP_K6 * sizeof(uint16_t)));
         const int got = gjnp_try(M, n, ld, R, reinterpret_cast<char*>(XB), (size_t)GJB_BLOCK * n * sizeof(float),
-                                 bad, st);
+                                 Ls, Us, bad, st);
         if (got < 0) return -got;
         if (got == 1) {
             g_inverse_counts[0]++;
