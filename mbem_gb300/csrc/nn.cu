@@ -553,7 +553,7 @@ __device__ __forceinline__ float aphi_load(const double* row, int c) { return (f
 // T = uint16_t: the BF16 inner operator's far field; T = double: a dense FP64
 // operator (FP32 products: the coarse operator is a preconditioner's)
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 nn_aphi_gather_kernel(const T* __restrict__ A16, int64_t ld16, int64_t n, const int64_t* __restrict__ chunk_ptr,
                       const int64_t* __restrict__ dofs, int64_t n_chunks, const float* __restrict__ basis,
                       float* __restrict__ APhi, int64_t ldp) {
@@ -591,16 +591,31 @@ nn_aphi_gather_kernel(const T* __restrict__ A16, int64_t ld16, int64_t n, const 
             for (int q = 0; q < RW; q++)
 #pragma unroll
                 for (int p = 0; p < NCV / 2; p++) acc[q][p] = make_float2(0.f, 0.f);
-            for (int t = lo + gl; t < hi; t += LG) {
-                const int cc = col[t];
-                float v[RW];
+            // two columns a lane per pass: eight loads in flight before the products
+            for (int t = lo + gl; t < hi; t += 2 * LG) {
+                const int t2 = t + LG;
+                const bool two = t2 < hi;
+                const int cc = col[t], cc2 = col[two ? t2 : t];
+                float v[RW], v2[RW];
 #pragma unroll
-                for (int q = 0; q < RW; q++) v[q] = aphi_load(Ar[q], cc);
+                for (int q = 0; q < RW; q++) {
+                    v[q] = aphi_load(Ar[q], cc);
+                    v2[q] = aphi_load(Ar[q], cc2);
+                }
 #pragma unroll
                 for (int p = 0; p < NCV / 2; p++) {
                     const float2 b = bs[t * 3 + p];
 #pragma unroll
                     for (int q = 0; q < RW; q++) acc[q][p] = __ffma2_rn(make_float2(v[q], v[q]), b, acc[q][p]);
+                }
+                if (two) {
+#pragma unroll
+                    for (int p = 0; p < NCV / 2; p++) {
+                        const float2 b = bs[t2 * 3 + p];
+#pragma unroll
+                        for (int q = 0; q < RW; q++)
+                            acc[q][p] = __ffma2_rn(make_float2(v2[q], v2[q]), b, acc[q][p]);
+                    }
                 }
             }
             // the group's lanes: a fixed xor tree; every lane ends with the sums
