@@ -24,6 +24,11 @@ volume    the volume sampler's geometry on cube 24 (6,912 triangles): region
 vsample   the mixed readout of the same 40^3 grid after a mixed solve of cube 24
           + fault 16: readout_far_kernel<EIG> (stress and eigenstress) and
           disp_readout_kernel, each over the cube and the fault
+learned48 the learned two-level preconditioner's setup on the mixed operator of
+          cube 48 + fault 32 (the headline's), twice after one assembly: the
+          chunks, block-Jacobi inverses, features, A Phi gather and the coarse
+          inverse (cluster_*, bj_build_kernel, knn_kernel, nn_*, gjnp_*)
+learned24 the same on cube 24 + fault 16
 compressed  the compressed pair operator of the cube 64 self pair, T kernel
           (49,152 elements): its build (aca_kernel, pair_dense_kernel) and eight
           products (cm_gather_kernel, cm_project_kernel, cm_strip_kernel)
@@ -146,6 +151,18 @@ def run(which: str) -> None:
                            precond="bf16_inner").assemble(generate_system(model), eps).solve()
         grid = V.make_grid(model, 4.0 / 40)
         V.sample(model, sol, eps, grid, V.classify(model, grid), precision="mixed")
+    elif which in ("learned48", "learned24"):
+        from mbem_gb300.la.learned import LearnedPreconditioner
+        from mbem_gb300.la.precond import MAX_NODES, BlockJacobi
+        from mbem_gb300.la.train_learned import load_default
+        model, eps = cube_fault_model(48, 32) if which == "learned48" else cube_fault_model(24, 16)
+        asm = DenseBackend(jump="calibrated", deflate=True, rtol=1e-8, precision="mixed",
+                           precond="bf16_learned").assemble(generate_system(model), eps)
+        params = load_default()
+        for _ in range(2):
+            groups = [(s_.offset, asm.device_patch_arrays(s_.patch)["coll"].view(-1, 3)) for s_ in asm.layout.slots]
+            bj = BlockJacobi.from_device_points(asm.layout.n_unknowns, groups, MAX_NODES).build_mixed(asm.op)
+            LearnedPreconditioner(asm, params, bj=bj)
     elif which == "compressed":
         from mbem_gb300 import mesh
         from mbem_gb300.kernels import basis as kb
