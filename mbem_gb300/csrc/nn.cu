@@ -535,7 +535,7 @@ knn_kernel(const float* __restrict__ p, int64_t n, int k, int64_t* __restrict__ 
 // A Phi for the BF16 inner operator of the mixed solve (A16 far field plus
 // its FP64 near blocks), stored FP32 at ldp: a CTA per (group of
 // APHI16_GROUP chunks, APHI16_ROWS rows) holds the group's columns and basis
-// rows in shared memory. A warp takes APHI16_RW rows at a time and two
+// rows in shared memory. A warp takes APHI16_RW (eight) rows at a time and two
 // chunks at once, sixteen lanes a chunk over its columns (each chunk's
 // columns ascending, so a lane group's loads run along the mesh's element
 // runs); the six basis columns go as three packed pairs (FFMA2), and each
@@ -543,7 +543,7 @@ knn_kernel(const float* __restrict__ p, int64_t n, int k, int64_t* __restrict__ 
 // order). Every APhi entry has one writer. The near blocks follow as FP32
 // atomic adds (nn_aphi_near_kernel).
 // ---------------------------------------------------------------------------
-constexpr int APHI16_GROUP = 8, APHI16_ROWS = 128, APHI16_RW = 4, APHI16_LG = 16;
+constexpr int APHI16_GROUP = 8, APHI16_ROWS = 128, APHI16_RW = 8, APHI16_LG = 16;
 
 __device__ __forceinline__ float aphi_load(const uint16_t* row, int c) {
     return __uint_as_float((uint32_t)row[c] << 16);
@@ -553,7 +553,7 @@ __device__ __forceinline__ float aphi_load(const double* row, int c) { return (f
 // T = uint16_t: the BF16 inner operator's far field; T = double: a dense FP64
 // operator (FP32 products: the coarse operator is a preconditioner's)
 template <typename T>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, 2)
 nn_aphi_gather_kernel(const T* __restrict__ A16, int64_t ld16, int64_t n, const int64_t* __restrict__ chunk_ptr,
                       const int64_t* __restrict__ dofs, int64_t n_chunks, const float* __restrict__ basis,
                       float* __restrict__ APhi, int64_t ldp) {
