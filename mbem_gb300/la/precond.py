@@ -180,14 +180,22 @@ def cluster_order_cuda(points: torch.Tensor, max_nodes: int):
             left[rank_order[:n_s // 2]] = True
             order[a:a + n_s] = torch.from_numpy(np.concatenate([cur[left], cur[~left]])).to(dev)
             nl_h[s_] = n_s // 2
-        n_new = 1 + big.astype(np.int64)
-        new_sizes = np.empty(int(n_new.sum()), np.int64)
-        pos = np.cumsum(n_new) - n_new
-        new_sizes[pos] = np.where(big, nl_h, sizes_h)
-        new_sizes[pos[big] + 1] = (sizes_h - nl_h)[big]
-        sizes_h = new_sizes
-        starts_h = np.concatenate([[0], np.cumsum(sizes_h)[:-1]]).astype(np.int64)
+        starts_h, sizes_h = next_segments(sizes_h, nl_h, big)
     return order, sizes_h
+
+
+def next_segments(sizes: np.ndarray, nl: np.ndarray, big: np.ndarray):
+    """The segment list of the next tree level: a split segment (``big``)
+    becomes its left part of ``nl`` points and its right part, in place; a
+    leaf stays. Returns (starts, sizes), int64."""
+    sizes = np.asarray(sizes, np.int64)
+    n_new = 1 + np.asarray(big, bool).astype(np.int64)
+    new_sizes = np.empty(int(n_new.sum()), np.int64)
+    pos = np.cumsum(n_new) - n_new
+    new_sizes[pos] = np.where(big, nl, sizes)
+    new_sizes[pos[big] + 1] = (sizes - nl)[big]
+    starts = np.concatenate([[0], np.cumsum(new_sizes)[:-1]]).astype(np.int64)
+    return starts, new_sizes
 
 
 class BlockJacobi:

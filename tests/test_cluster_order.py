@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 import torch
 
-from mbem_gb300.la.precond import cluster_leaves, cluster_order_device
+from mbem_gb300.la.precond import cluster_leaves, cluster_order_device, next_segments
 
 
 @pytest.mark.parametrize("m, max_nodes, seed", [(1, 75, 0), (75, 75, 1), (76, 75, 2), (1000, 75, 3),
@@ -61,3 +61,15 @@ def test_cuda_levels_coincident_points_split_by_rank(gpu):
     ref = cluster_leaves(pts, 40)
     got = np.split(order.cpu().numpy(), np.cumsum(sizes)[:-1])
     assert [np.sort(a).tolist() for a in got] == [np.sort(b).tolist() for b in ref]
+
+
+def test_next_segments_splits_in_place():
+    """The level bookkeeping of the CUDA bisection: split segments become
+    (left, right) where they stood, leaves stay, starts follow the sizes."""
+    sizes = np.array([100, 40, 77, 3])
+    big = sizes > 50
+    nl = np.array([50, 40, 38, 3])
+    starts, new = next_segments(sizes, nl, big)
+    assert new.tolist() == [50, 50, 40, 38, 39, 3]
+    assert starts.tolist() == [0, 50, 100, 140, 178, 217]
+    assert new.sum() == sizes.sum()
