@@ -276,9 +276,13 @@ int mbem_bf16_matvec(const uint16_t* A16, int64_t ld16, int64_t n_rows, int64_t 
 /* z = the iterate after `iterations` steps of GMRES from zero on
  * P (A16 + near) P z = P r (P: the deflation of params->u_ranges), as a
  * flexible right preconditioner of FGMRES on the accurate operator: the inner
- * steps read 2 bytes per far entry, the outer ones 4. The Arnoldi steps run
- * on the device; the host reads the Hessenberg matrix once per application
- * (rtol = 0) or one column per step (rtol > 0, to stop early). */
+ * steps read 2 bytes per far entry, the outer ones 4. The Arnoldi steps, the
+ * Givens rotations and the back substitution run on the device; the host
+ * enqueues step j + 1 before it reads step j's small status block (pinned
+ * memory behind an event), and stops enqueueing once a step ended the basis
+ * (residual estimate below rtol |P r|, rtol > 0; an invariant Krylov space;
+ * a zero pivot): the one step already queued behind it returns at once on
+ * the device. It does not synchronise `stream`: z is ready in stream order. */
 #define MBEM_INNER_MAX_ITERS 64
 typedef struct {
     int64_t n;                      /* system size (square) */
@@ -287,8 +291,8 @@ typedef struct {
     int n_near;
     const mbem_near_blocks* near;   /* HOST array of n_near FP64 near-block lists */
     int iterations;                 /* at most this many steps, 1..MBEM_INNER_MAX_ITERS */
-    double rtol;                    /* > 0: stop once the inner residual estimate is below rtol |P r|
-                                       (one host read per step); 0: all steps, one read in total */
+    double rtol;                    /* > 0: stop once the inner residual estimate is below rtol |P r|;
+                                       0: all steps (an exact breakdown still ends the basis) */
     int n_u_ranges;                 /* deflation ranges, as in mbem_fgmres_params */
     const int64_t* u_ranges;
     void* work;                     /* mbem_inner_bf16_workspace_size(n, iterations) bytes */
@@ -707,8 +711,10 @@ int mbem_fgmres_mixed(const mbem_mixed_operator* op, const double* b, double* x,
 /* Solve A x = b (A FP64 (n,n) at leading dimension ld; b, x device (n,)).
  * x holds the initial guess on entry (zeros for none) and the solution on
  * exit (the zero-mean-translation representative P y when deflating).
- * Synchronises `stream` once per iteration (the Givens step runs on the
- * host on (restart+1) scalars). */
+ * The Gram-Schmidt passes, |w| and the Givens rotation of each step run on
+ * the device; the host waits for each step's small status block (an event,
+ * not a stream-wide wait) for its stopping and stagnation tests, and the
+ * call synchronises `stream` once at its end. */
 int mbem_fgmres_dense(const double* A, int64_t ld, int64_t n, const double* b, double* x,
                       const mbem_fgmres_params* params, void* work, size_t work_bytes,
                       mbem_fgmres_report* report, void* stream);
