@@ -11,10 +11,16 @@
 namespace mbem {
 
 // ---------------------------------------------------------------------------
-// quadrature rules: collapsed Gauss-Legendre n x n on (0,0),(1,0),(0,1)
+// quadrature rules on (0,0),(1,0),(0,1): collapsed Gauss-Legendre n x n
+// (code n, n^2 points, exact to total degree 2n - 2), and Radon's symmetric
+// 7-point rule (code QR_RADON, exact to degree 5: the centroid and two orbits
+// of three points, from Radon (1948) / Stroud's table T2:5-1)
 // ---------------------------------------------------------------------------
-constexpr int QR_MIN = 3, QR_MAX = 8;      // P0 uses n = 3..6; nodal densities up to 8
-constexpr int QR_POINTS = 9 + 16 + 25 + 36 + 49 + 64;
+constexpr int QR_MIN = 3, QR_MAX = 8;      // P0 uses n = 4..6; nodal densities up to 8
+constexpr int QR_RADON = 2;                // the code of the 7-point rule
+constexpr int QR_POINTS = 9 + 16 + 25 + 36 + 49 + 64 + 7;
+
+__host__ __device__ __forceinline__ int rule_points(int code) { return code == QR_RADON ? 7 : code * code; }
 
 struct QuadRules {
     float a[QR_POINTS];    // xi1 - 1/3
@@ -69,6 +75,25 @@ static QuadRules make_rules() {
                 r.w[k] = (float)(wi * wj * (1.0 - gi));
                 k++;
             }
+    }
+    // Radon: weights for the triangle of area 1/2
+    r.off[QR_RADON] = k;
+    const double s15 = sqrt(15.0);
+    const double orbit[2][3] = {{(6.0 - s15) / 21.0, (9.0 + 2.0 * s15) / 21.0, (155.0 - s15) / 2400.0},
+                                {(6.0 + s15) / 21.0, (9.0 - 2.0 * s15) / 21.0, (155.0 + s15) / 2400.0}};
+    r.a[k] = 0.0f;
+    r.b[k] = 0.0f;
+    r.w[k] = (float)(9.0 / 80.0);
+    k++;
+    for (int o = 0; o < 2; o++) {
+        const double p = orbit[o][0], q = orbit[o][1];
+        const double pts[3][2] = {{p, p}, {p, q}, {q, p}};
+        for (int t = 0; t < 3; t++) {
+            r.a[k] = (float)(pts[t][0] - 1.0 / 3.0);
+            r.b[k] = (float)(pts[t][1] - 1.0 / 3.0);
+            r.w[k] = (float)orbit[o][2];
+            k++;
+        }
     }
     return r;
 }
@@ -149,12 +174,21 @@ __device__ __forceinline__ bool is_near(const F2 x[3], const SrcFar& s, float d[
     return D2 < s.rnear2;
 }
 
-__device__ __forceinline__ int far_rule(float D2, float L2) {
-    // n by D / L_max (measured against the FP64 closed form: <= ~1.5e-7)
+// the collapsed rule n by D / L_max (measured against the FP64 closed form:
+// <= ~1.7e-7); the nodal far blocks add their order to it
+__device__ __forceinline__ int far_rule_collapsed(float D2, float L2) {
     if (D2 >= 50.0f * L2) return 3;        // D/L >= 7.07
     if (D2 >= 8.0f * L2) return 4;         // D/L >= 2.83
     if (D2 >= 3.125f * L2) return 5;       // D/L >= 1.77
     return 6;
+}
+
+// the P0 rule: Radon's 7 points from D/L >= 5 (<= 8.8e-8 of the closed form
+// there, 1.1e-8 at D/L = 7.07 where the collapsed 3 x 3 rule's 9 points give
+// 1.7e-7), else the collapsed rules
+__device__ __forceinline__ int far_rule(float D2, float L2) {
+    if (D2 >= 25.0f * L2) return QR_RADON;
+    return far_rule_collapsed(D2, L2);
 }
 
 // Far T block (FP32): out_ij = n_j alpha_i + n_i beta_j + d_ij gamma - 6 c5 W_ij
@@ -201,7 +235,7 @@ template <bool TKERNEL>
 __device__ __forceinline__ void far_block(const QuadRules& Q, const SrcFar& s, const float dc[3], float D2,
                                           const float c[6], float out[3][3]) {
     const int nq = far_rule(D2, s.L2);
-    const int q0 = Q.off[nq], q1 = q0 + nq * nq;
+    const int q0 = Q.off[nq], q1 = q0 + rule_points(nq);
     FarSums m = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int q = q0; q < q1; q++) {
         const float a = Q.a[q], b = Q.b[q];
@@ -245,7 +279,7 @@ __device__ __forceinline__ void far_block2(const QuadRules& Q, const SrcFar& s, 
                                            float D2a, float D2b, const float c[6], float outa[3][3],
                                            float outb[3][3]) {
     const int nq = far_rule(fminf(D2a, D2b), s.L2);
-    const int q0 = Q.off[nq], q1 = q0 + nq * nq;
+    const int q0 = Q.off[nq], q1 = q0 + rule_points(nq);
     const float2 dc0 = make_float2(da[0], db[0]), dc1 = make_float2(da[1], db[1]), dc2 = make_float2(da[2], db[2]);
     const float2 e2 = f2s(s.eps2);
     const float2 n0 = f2s(s.n[0]), n1 = f2s(s.n[1]), n2 = f2s(s.n[2]);

@@ -61,7 +61,7 @@ __device__ __forceinline__ void far_block_nodal(const QuadRules& Q, const SrcFar
     constexpr int K = ORDER == 1 ? 3 : 6;
     // the shape functions raise the integrand's degree: ORDER more points a
     // direction than the P0 rule at the same D / L
-    const int nq = min(far_rule(D2, s.L2) + ORDER, QR_MAX);
+    const int nq = min(far_rule_collapsed(D2, s.L2) + ORDER, QR_MAX);
     const int q0 = Q.off[nq], q1 = q0 + nq * nq;
     float V3[K][3], V5[K][3], t[K][3], W[K][6], I1[K], I3[K];
 #pragma unroll
